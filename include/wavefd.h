@@ -1,0 +1,142 @@
+/*
+ * wavefd.h - C ABI of the GB300 finite-difference acoustic wave path.
+ *
+ * Plain pointers and sizes only. Every array argument is a DEVICE pointer
+ * owned by the caller (PyTorch tensors on the Python side); the library
+ * allocates nothing: all scratch lives in a caller-provided workspace whose
+ * size wfd_workspace_bytes() reports. Calls are asynchronous on `stream`
+ * (a cudaStream_t passed as void*; NULL = legacy default stream), return 0 or a
+ * negative WFD_ERR_* status, never abort, and are reentrant per stream.
+ *
+ * Grid convention: fields are indexed (z, y, x), x fastest; 2D problems have
+ * ny == 1 and y == 0 in every position. The outer ring of R = order/2 cells is
+ * held fixed (homogeneous Dirichlet, as padded_step holds its ring of 1); the
+ * interior is updated by
+ *     u_{n+1} = g (2 u_n + (v dt)^2 L u_n + src_scale * w_n) - g^2 u_{n-1},
+ * L the order-`order` central Laplacian, g = sponge_z[z] sponge_y[y] sponge_x[x]
+ * (a NULL profile counts as 1). Sources and receivers must lie in the interior.
+ * Traces: traces[s][n][r] = u_{n+1}(rec[s][r]), n = 0 .. nt-1.
+ */
+#ifndef WAVEFD_H
+#define WAVEFD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WFD_OK 0
+#define WFD_ERR_INVALID (-1)   /* bad argument: shape, order, null pointer, alignment */
+#define WFD_ERR_WORKSPACE (-2) /* workspace too small or not 256-byte aligned */
+#define WFD_ERR_CUDA (-3)      /* a CUDA runtime / driver call failed */
+#define WFD_ERR_UNSTABLE (-4)  /* vmax * dt violates the CFL bound of the stencil */
+#define WFD_ERR_POSITION (-5)  /* a source or receiver outside the updated interior */
+#define WFD_ERR_TIMEOUT (-6)   /* a kernel gave up waiting for a TMA tile */
+#define WFD_ERR_STATE (-7)     /* wfd_backward without a preceding checkpointed forward */
+
+typedef struct wfd_problem {
+    int32_t ndim;          /* 2 or 3 */
+    int32_t order;         /* space order: 2, 4 or 8 */
+    int32_t nz, ny, nx;    /* cells per axis; ny = 1 when ndim == 2 */
+    int32_t nshot;         /* shots sharing this velocity model */
+    int32_t nt;            /* time steps */
+    int32_t nsrc, nrec;    /* sources / receivers per shot */
+    int32_t ckpt_every;    /* steps between checkpoints; 0 = ceil(sqrt(nt)) */
+    int32_t ckpt_bf16;     /* 1: checkpoint snapshots stored as BF16, 0: FP32 */
+    int32_t lap_bf16;      /* 1: per-segment L u store in BF16, 0: FP32 */
+    int32_t shots_per_cta; /* shots one CTA walks through per step; 0 = automatic */
+    float dt;              /* time step */
+    float dz, dy, dx;      /* grid spacing (dy ignored in 2D) */
+    float src_scale;       /* factor on every injected wavelet sample */
+    float vmax;            /* max velocity for the CFL check; <= 0 skips the check */
+} wfd_problem;
+
+/* Human-readable text of a status code. */
+const char* wfd_strerror(int status);
+
+/* Detail of the last failure on the calling thread ("" if none). */
+const char* wfd_last_error(void);
+
+/* ABI version: (major << 16) | minor. */
+int wfd_version(void);
+
+/* Workspace size for wfd_forward (with_gradient = 0) or for the
+ * forward + backward pair (with_gradient = 1). Host-only, no CUDA call. */
+int wfd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes);
+
+/*
+ * Forward modelling of p->nshot shots through one velocity model.
+ * Replaces the reference solver's forward call: cuwave `simulate` /
+ * `measure(sim, sources, indicator, sensors)` as driven by
+ * projects/18_fwi/plate.py:64 (full matrix capture) and
+ * projects/18_fwi/2D_scalar_wave_forward_B_hai.py:30.
+ *   vel      [nz][ny][nx] FP32 velocity
+ *   sponge_* [nz], [ny], [nx] FP32 damping profiles or NULL
+ *   wavelet  [nshot][nt][nsrc] FP32 source samples
+ *   src, rec [nshot][nsrc|nrec][3] int32 (z, y, x)
+ *   traces   [nshot][nt][nrec] FP32 output (may be NULL)
+ *   save_checkpoints: 1 keeps the state wfd_backward needs in the workspace
+ *   (which must then be sized with with_gradient = 1).
+ */
+int wfd_forward(const wfd_problem* p, const float* vel, const float* sponge_z,
+                const float* sponge_y, const float* sponge_x, const float* wavelet,
+                const int32_t* src, const int32_t* rec, float* traces, int save_checkpoints,
+                void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Adjoint of the forward above for a trace cotangent `dtraces`
+ * ([nshot][nt][nrec]): grad_vel [nz][ny][nx] = (dF/dvel)^T dtraces (summed over
+ * shots; 0 on the fixed ring) and, when grad_wavelet is not NULL,
+ * grad_wavelet [nshot][nt][nsrc] = (dF/dwavelet)^T dtraces. Uses the checkpoints
+ * of the preceding wfd_forward(save_checkpoints = 1) on the same workspace and
+ * inputs, recomputing the forward per segment; one backward per forward.
+ * Together with wfd_forward this is the reference solver's gradient,
+ * cuwave `misfit_gradient(sim, sources, gamma, sensors, observed)` as used by
+ * projects/18_fwi/2D_fwi.py:40, for a cotangent the caller chooses.
+ */
+int wfd_backward(const wfd_problem* p, const float* vel, const float* sponge_z,
+                 const float* sponge_y, const float* sponge_x, const float* wavelet,
+                 const int32_t* src, const int32_t* rec, const float* dtraces, float* grad_vel,
+                 float* grad_wavelet, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * L2 misfit J = 1/2 sum (d - observed)^2 (accumulated in FP64 into the device
+ * double *misfit) and its gradient, in one call: forward with checkpoints,
+ * residual, backward. Replaces cuwave `misfit_gradient` -> (cost, gradient),
+ * projects/18_fwi/2D_fwi.py:40, and `misfit`, as called by
+ * projects/9_structural_optimization/fwi_penalization.py:138-143.
+ * traces (optional) receives the modelled traces; grad_wavelet may be NULL.
+ */
+int wfd_misfit_gradient(const wfd_problem* p, const float* vel, const float* sponge_z,
+                        const float* sponge_y, const float* sponge_x, const float* wavelet,
+                        const int32_t* src, const int32_t* rec, const float* observed,
+                        float* traces, float* grad_vel, float* grad_wavelet, double* misfit,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* Synchronises `stream`, returns the first device-side error recorded in the
+ * workspace since the last call (WFD_ERR_TIMEOUT, WFD_ERR_POSITION) or 0, and
+ * clears it. */
+int wfd_status(void* workspace, void* stream);
+
+/* FP64 sum of squares of n FP32 values, added into the device double *out
+ * (gradient norms). */
+int wfd_sum_sq(const float* x, int64_t n, double* out, void* stream);
+
+/*
+ * One order-2, constant-speed, Dirichlet step with the reference kernel's
+ * exact signature and semantics: padded_step, projects/18_simple_wave_fd/
+ * step2D_wave.cu:59-65, launched as in 2D_wave_cuda_padding.py:66-76.
+ * u0, u1, u2 are [N][M_padded] FP32; rows 1..N-2 and columns 1..M-2 of u2
+ * receive -u0 + 2 u1 + dt^2 c^2 (Lap_x/dx^2 + Lap_y/dy^2) (i along N uses dx,
+ * j along M uses dy); u2 may alias u0. M_padded must be a multiple of 4 and
+ * the pointers 16-byte aligned (the reference pads rows to 32).
+ */
+int wfd_step2d_order2(const float* u0, const float* u1, float* u2, float wavespeed, float dt,
+                      float dx, float dy, int N, int M, int M_padded, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WAVEFD_H */

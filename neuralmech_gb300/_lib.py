@@ -1,0 +1,98 @@
+"""ctypes binding of libwavefd.so (include/wavefd.h).
+
+The library is the product path: there is no CPU or PyTorch fallback. If the
+shared object is missing it is built with nvcc when available; if that is not
+possible, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libwavefd.so")
+
+WFD_OK = 0
+WFD_ERR_INVALID = -1
+WFD_ERR_WORKSPACE = -2
+WFD_ERR_CUDA = -3
+WFD_ERR_UNSTABLE = -4
+WFD_ERR_POSITION = -5
+WFD_ERR_TIMEOUT = -6
+WFD_ERR_STATE = -7
+
+# Every symbol include/wavefd.h declares.
+EXPORTS = (
+    "wfd_strerror", "wfd_last_error", "wfd_version", "wfd_workspace_bytes", "wfd_forward",
+    "wfd_backward", "wfd_misfit_gradient", "wfd_status", "wfd_sum_sq", "wfd_step2d_order2",
+)
+
+
+class Problem(ctypes.Structure):
+    """Mirror of ``wfd_problem`` (include/wavefd.h)."""
+    _fields_ = [
+        ("ndim", ctypes.c_int32), ("order", ctypes.c_int32),
+        ("nz", ctypes.c_int32), ("ny", ctypes.c_int32), ("nx", ctypes.c_int32),
+        ("nshot", ctypes.c_int32), ("nt", ctypes.c_int32),
+        ("nsrc", ctypes.c_int32), ("nrec", ctypes.c_int32),
+        ("ckpt_every", ctypes.c_int32), ("ckpt_bf16", ctypes.c_int32),
+        ("lap_bf16", ctypes.c_int32), ("shots_per_cta", ctypes.c_int32),
+        ("dt", ctypes.c_float), ("dz", ctypes.c_float), ("dy", ctypes.c_float),
+        ("dx", ctypes.c_float), ("src_scale", ctypes.c_float), ("vmax", ctypes.c_float),
+    ]
+
+
+class WaveFDError(RuntimeError):
+    """A libwavefd call returned a negative status."""
+
+    def __init__(self, status: int, where: str, detail: str):
+        super().__init__(f"{where}: {detail} (status {status})")
+        self.status = status
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libwavefd.so (building it in-tree first if it is missing)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH) and build_if_missing:
+            from .build import build
+            build()
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with "
+                              "`python -m neuralmech_gb300.build` (needs nvcc)")
+        lib = ctypes.CDLL(LIB_PATH)
+        P = ctypes.POINTER(Problem)
+        vp, f, i32, d = ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p
+        sz = ctypes.c_size_t
+        lib.wfd_strerror.argtypes = [ctypes.c_int]
+        lib.wfd_strerror.restype = ctypes.c_char_p
+        lib.wfd_last_error.argtypes = []
+        lib.wfd_last_error.restype = ctypes.c_char_p
+        lib.wfd_version.argtypes = []
+        lib.wfd_workspace_bytes.argtypes = [P, ctypes.c_int, ctypes.POINTER(sz)]
+        lib.wfd_forward.argtypes = [P, f, f, f, f, f, i32, i32, f, ctypes.c_int, vp, sz, vp]
+        lib.wfd_backward.argtypes = [P, f, f, f, f, f, i32, i32, f, f, f, vp, sz, vp]
+        lib.wfd_misfit_gradient.argtypes = [P, f, f, f, f, f, i32, i32, f, f, f, f, d, vp, sz, vp]
+        lib.wfd_status.argtypes = [vp, vp]
+        lib.wfd_sum_sq.argtypes = [f, ctypes.c_int64, d, vp]
+        lib.wfd_step2d_order2.argtypes = [f, f, f, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                          ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
+        for name in EXPORTS:
+            if name not in ("wfd_strerror", "wfd_last_error"):
+                getattr(lib, name).restype = ctypes.c_int
+        _lib = lib
+        return lib
+
+
+def check(status: int, where: str) -> None:
+    if status != WFD_OK:
+        lib = load()
+        detail = lib.wfd_last_error().decode() or lib.wfd_strerror(status).decode()
+        raise WaveFDError(status, where, detail)

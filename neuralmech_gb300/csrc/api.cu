@@ -1,0 +1,623 @@
+// C-ABI layer of the wave path (include/wavefd.h): argument checks, workspace
+// layout, TMA descriptors, and the time loops of the forward, the
+// checkpointed adjoint and the misfit gradient. Host code only; all device
+// work is in stencil2d.cu / stencil3d.cu / aux.cu.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/wavefd.h"
+#include "internal.h"
+
+using namespace wfd;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+int fail(int status, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+#define WFD_CUDA(call)                                                                      \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail(WFD_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));     \
+    } while (0)
+
+// ------------------------------------------------------------------ TMA maps
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                 const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                 const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder() {
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    return fn;
+}
+
+// Tiled map over a field buffer [nshot][nz][ny][ld] with extent nx in x
+// (reads past nx, or past any edge, fill zeros).
+int make_field_map(CUtensorMap* map, const void* base, bool bf16, int ndim, int nz, int ny,
+                   int nx, int ld, int nshot, const cuuint32_t* box) {
+    EncodeTiled enc = encoder();
+    if (!enc) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+    const cuuint64_t es = bf16 ? 2 : 4;
+    cuuint64_t dims[4], strides[3];
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    int rank;
+    if (ndim == 2) {
+        rank = 3;
+        dims[0] = nx; dims[1] = nz; dims[2] = nshot;
+        strides[0] = ld * es;
+        strides[1] = (cuuint64_t)nz * ld * es;
+    } else {
+        rank = 4;
+        dims[0] = nx; dims[1] = ny; dims[2] = nz; dims[3] = nshot;
+        strides[0] = ld * es;
+        strides[1] = (cuuint64_t)ny * ld * es;
+        strides[2] = (cuuint64_t)nz * ny * ld * es;
+    }
+    CUresult r = enc(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                     rank, const_cast<void*>(base), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return WFD_OK;
+}
+
+// ------------------------------------------------------------------ geometry
+struct Geom {
+    int ndim, R, nz, ny, nx, ld;
+    long long plane, cells;  // z stride; cells per shot (padded)
+    int tile_z, tile_y, tile_x, tiles_z, tiles_y, tiles_x, ntiles;
+    int spc;                 // shots per CTA
+    int K, nseg, k0_last;    // checkpoint interval, segments, first step of the last segment
+    float c0, cz[4], cy[4], cx[4];
+};
+
+int cdiv(long long a, long long b) { return int((a + b - 1) / b); }
+
+void fd_weights(int order, double* a) {
+    const int R = order / 2;
+    auto fact = [](int n) { double f = 1; for (int i = 2; i <= n; ++i) f *= i; return f; };
+    double s = 0;
+    for (int k = 1; k <= R; ++k) {
+        a[k] = 2.0 * ((k % 2) ? 1.0 : -1.0) * fact(R) * fact(R) /
+               (double(k) * k * fact(R - k) * fact(R + k));
+        s += a[k];
+    }
+    a[0] = -2.0 * s;
+}
+
+int check_problem(const wfd_problem* p) {
+    if (!p) return fail(WFD_ERR_INVALID, "problem is NULL");
+    if (p->ndim != 2 && p->ndim != 3) return fail(WFD_ERR_INVALID, "ndim must be 2 or 3");
+    if (p->order != 2 && p->order != 4 && p->order != 8)
+        return fail(WFD_ERR_INVALID, "order must be 2, 4 or 8");
+    const int R = p->order / 2;
+    if (p->ndim == 2 && p->ny != 1) return fail(WFD_ERR_INVALID, "2D problems need ny == 1");
+    if (p->ndim == 3 && !step3d_available())
+        return fail(WFD_ERR_INVALID, "3D kernel not built into this library");
+    if (p->nz < 2 * R + 1 || p->nx < 2 * R + 1 || (p->ndim == 3 && p->ny < 2 * R + 1))
+        return fail(WFD_ERR_INVALID, "grid too small for order %d", p->order);
+    if (p->nx > (1 << 24) || p->nz > (1 << 24) || p->ny > (1 << 24))
+        return fail(WFD_ERR_INVALID, "grid axis too large");
+    if ((long long)p->nz * p->ny * (long long)(p->nx + 8) >= (1ll << 31))
+        return fail(WFD_ERR_INVALID, "more than 2^31 cells per shot");
+    if (p->nshot < 1 || p->nt < 1 || p->nsrc < 0 || p->nrec < 0)
+        return fail(WFD_ERR_INVALID, "nshot, nt must be >= 1 and nsrc, nrec >= 0");
+    if (p->nshot > 65535 * 64) return fail(WFD_ERR_INVALID, "too many shots");
+    if (!(p->dt > 0) || !(p->dx > 0) || !(p->dz > 0) || (p->ndim == 3 && !(p->dy > 0)))
+        return fail(WFD_ERR_INVALID, "dt and spacings must be positive");
+    if (p->ckpt_every < 0 || p->shots_per_cta < 0)
+        return fail(WFD_ERR_INVALID, "ckpt_every and shots_per_cta must be >= 0");
+    if (p->vmax > 0) {
+        double a[5];
+        fd_weights(p->order, a);
+        double S = std::fabs(a[0]);
+        for (int k = 1; k <= R; ++k) S += 2 * std::fabs(a[k]);
+        double inv2 = 1.0 / (p->dz * (double)p->dz) + 1.0 / (p->dx * (double)p->dx);
+        if (p->ndim == 3) inv2 += 1.0 / (p->dy * (double)p->dy);
+        const double lhs = p->vmax * (double)p->dt * std::sqrt(inv2 * S);
+        if (lhs > 2.0)
+            return fail(WFD_ERR_UNSTABLE, "vmax*dt = %g exceeds the CFL bound %g of order %d",
+                        p->vmax * (double)p->dt, 2.0 / std::sqrt(inv2 * S), p->order);
+    }
+    return WFD_OK;
+}
+
+Geom make_geom(const wfd_problem* p) {
+    Geom g{};
+    g.ndim = p->ndim;
+    g.R = p->order / 2;
+    g.nz = p->nz;
+    g.ny = p->ndim == 3 ? p->ny : 1;
+    g.nx = p->nx;
+    g.ld = (p->nx + 7) / 8 * 8;
+    g.plane = (long long)g.ny * g.ld;
+    g.cells = (long long)g.nz * g.plane;
+    if (g.ndim == 2) {
+        g.tile_z = T2_TZ; g.tile_y = 1; g.tile_x = T2_TX;
+    } else {
+        g.tile_z = T3_ZCHUNK; g.tile_y = T3_TY; g.tile_x = T3_TX;
+    }
+    g.tiles_z = cdiv(g.nz, g.tile_z);
+    g.tiles_y = cdiv(g.ny, g.tile_y);
+    g.tiles_x = cdiv(g.nx, g.tile_x);
+    g.ntiles = g.tiles_z * g.tiles_y * g.tiles_x;
+    if (p->shots_per_cta > 0) {
+        g.spc = std::min(p->shots_per_cta, p->nshot);
+    } else {
+        // enough CTAs for ~6 waves of 2 resident CTAs on 152 SMs, otherwise
+        // as many shots per CTA as possible (m and the gradient amortise over them)
+        const long long target = 152LL * 2 * 6;
+        long long spc = (long long)g.ntiles * p->nshot / target;
+        int s = 1;
+        while (2LL * s <= spc && 2 * s <= p->nshot) s *= 2;
+        g.spc = s;
+    }
+    while ((p->nshot + g.spc - 1) / g.spc > 65535) g.spc *= 2;
+    g.K = p->ckpt_every > 0 ? std::min(p->ckpt_every, p->nt)
+                            : std::max(1, (int)std::ceil(std::sqrt((double)p->nt)));
+    g.nseg = cdiv(p->nt, g.K);
+    g.k0_last = (g.nseg - 1) * g.K;
+    double a[5] = {0, 0, 0, 0, 0};
+    fd_weights(p->order, a);
+    const double sz = (double)p->dx * p->dx / ((double)p->dz * p->dz);
+    const double sy = g.ndim == 3 ? (double)p->dx * p->dx / ((double)p->dy * p->dy) : 0.0;
+    g.c0 = float(a[0] * (1.0 + sz + sy));
+    for (int k = 1; k <= 4; ++k) {
+        g.cz[k - 1] = k <= g.R ? float(a[k] * sz) : 0.f;
+        g.cy[k - 1] = k <= g.R ? float(a[k] * sy) : 0.f;
+        g.cx[k - 1] = k <= g.R ? float(a[k]) : 0.f;
+    }
+    return g;
+}
+
+// ------------------------------------------------------------------ workspace
+struct Layout {
+    size_t err, m, P0, P1, counts, src_off, src_ent, rec_off, rec_ent;
+    size_t Q0, Q1, G, ckpt, lap, res, total;
+    size_t field_bytes, ckpt_field_bytes, lap_field_bytes;
+};
+
+size_t up256(size_t v) { return (v + 255) / 256 * 256; }
+
+Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
+    Layout L{};
+    size_t o = 0;
+    auto take = [&](size_t bytes) { size_t at = o; o = up256(o + bytes); return at; };
+    const size_t keys = (size_t)p->nshot * g.ntiles;
+    L.field_bytes = (size_t)p->nshot * g.cells * 4;
+    L.err = take(256);
+    L.m = take((size_t)g.cells * 4);
+    L.P0 = take(L.field_bytes);
+    L.P1 = take(L.field_bytes);
+    L.counts = take(keys * 4);
+    L.src_off = take((keys + 1) * 4);
+    L.src_ent = take((size_t)p->nshot * p->nsrc * 8 + 8);
+    L.rec_off = take((keys + 1) * 4);
+    L.rec_ent = take((size_t)p->nshot * p->nrec * 8 + 8);
+    if (grad) {
+        L.ckpt_field_bytes = (size_t)p->nshot * g.cells * (p->ckpt_bf16 ? 2 : 4);
+        L.lap_field_bytes = (size_t)p->nshot * g.cells * (p->lap_bf16 ? 2 : 4);
+        L.Q0 = take(L.field_bytes);
+        L.Q1 = take(L.field_bytes);
+        L.G = take((size_t)g.cells * 4);
+        L.ckpt = take((size_t)g.nseg * 2 * L.ckpt_field_bytes);
+        L.lap = take((size_t)g.K * L.lap_field_bytes);
+        L.res = take((size_t)p->nshot * p->nt * p->nrec * 4 + 4);
+    }
+    L.total = o;
+    return L;
+}
+
+struct Work {
+    unsigned* err;
+    float *m, *P[2], *Q[2], *G, *res;
+    int* counts;
+    PointLists src, rec;
+    unsigned char *ckpt, *lap;
+};
+
+Work carve(void* ws, const Layout& L, bool grad) {
+    unsigned char* b = static_cast<unsigned char*>(ws);
+    Work w{};
+    w.err = reinterpret_cast<unsigned*>(b + L.err);
+    w.m = reinterpret_cast<float*>(b + L.m);
+    w.P[0] = reinterpret_cast<float*>(b + L.P0);
+    w.P[1] = reinterpret_cast<float*>(b + L.P1);
+    w.counts = reinterpret_cast<int*>(b + L.counts);
+    w.src.off = reinterpret_cast<int*>(b + L.src_off);
+    w.src.ent = reinterpret_cast<int2*>(b + L.src_ent);
+    w.rec.off = reinterpret_cast<int*>(b + L.rec_off);
+    w.rec.ent = reinterpret_cast<int2*>(b + L.rec_ent);
+    if (grad) {
+        w.Q[0] = reinterpret_cast<float*>(b + L.Q0);
+        w.Q[1] = reinterpret_cast<float*>(b + L.Q1);
+        w.G = reinterpret_cast<float*>(b + L.G);
+        w.ckpt = b + L.ckpt;
+        w.lap = b + L.lap;
+        w.res = reinterpret_cast<float*>(b + L.res);
+    }
+    return w;
+}
+
+int check_workspace(void* ws, size_t bytes, size_t need) {
+    if (!ws) return fail(WFD_ERR_WORKSPACE, "workspace is NULL");
+    if (reinterpret_cast<uintptr_t>(ws) % 256)
+        return fail(WFD_ERR_WORKSPACE, "workspace must be 256-byte aligned");
+    if (bytes < need)
+        return fail(WFD_ERR_WORKSPACE, "workspace of %zu bytes, %zu needed", bytes, need);
+    return WFD_OK;
+}
+
+bool aligned16(const void* p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; }
+
+// ------------------------------------------------------------------ stepping
+struct Stepper {
+    const wfd_problem* p;
+    Geom g;
+    cudaStream_t s;
+    unsigned* err;
+    const float* m;
+    const float *gz, *gy, *gx;
+
+    StepArgs base(float* u_new) const {
+        StepArgs a{};
+        a.u_new = u_new;
+        a.m = m;
+        a.m_const = 0.f;
+        a.gz = gz;
+        a.gy = gy;
+        a.gx = gx;
+        a.nz = g.nz; a.ny = g.ny; a.nx = g.nx; a.ld = g.ld;
+        a.plane = g.plane;
+        a.shot_stride = g.cells;
+        a.nshot = p->nshot;
+        a.shots_per_cta = g.spc;
+        a.tiles_x = g.tiles_x; a.tiles_y = g.tiles_y; a.tiles_z = g.tiles_z;
+        a.c0 = g.c0;
+        for (int k = 0; k < 4; ++k) { a.cz[k] = g.cz[k]; a.cy[k] = g.cy[k]; a.cx[k] = g.cx[k]; }
+        a.err = err;
+        return a;
+    }
+
+    int map_pair(const float* cur, const float* old, CUtensorMap* mc, CUtensorMap* mo) const {
+        int rc;
+        if (g.ndim == 2) {
+            const cuuint32_t bc[3] = {T2_W, cuuint32_t(T2_TZ + 2 * g.R), 1};
+            const cuuint32_t bo[3] = {T2_TX, T2_TZ, 1};
+            if ((rc = make_field_map(mc, cur, false, 2, g.nz, 1, g.nx, g.ld, p->nshot, bc))) return rc;
+            return make_field_map(mo, old, false, 2, g.nz, 1, g.nx, g.ld, p->nshot, bo);
+        }
+        const cuuint32_t bc[4] = {T3_W, cuuint32_t(T3_TY + 2 * g.R), 1, 1};
+        const cuuint32_t bo[4] = {T3_TX, T3_TY, 1, 1};
+        if ((rc = make_field_map(mc, cur, false, 3, g.nz, g.ny, g.nx, g.ld, p->nshot, bc))) return rc;
+        return make_field_map(mo, old, false, 3, g.nz, g.ny, g.nx, g.ld, p->nshot, bo);
+    }
+
+    int lap_map(const void* lap, bool bf16, CUtensorMap* ml) const {
+        if (g.ndim == 2) {
+            const cuuint32_t b[3] = {T2_TX, T2_TZ, 1};
+            return make_field_map(ml, lap, bf16, 2, g.nz, 1, g.nx, g.ld, p->nshot, b);
+        }
+        const cuuint32_t b[4] = {T3_TX, T3_TY, 1, 1};
+        return make_field_map(ml, lap, bf16, 3, g.nz, g.ny, g.nx, g.ld, p->nshot, b);
+    }
+
+    int launch(int mode, const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
+               const StepArgs& a) const {
+        cudaError_t e = g.ndim == 2 ? launch_step2d(g.R, mode, mc, mo, ml, a, s)
+                                    : launch_step3d(g.R, mode, mc, mo, ml, a, s);
+        if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "step launch failed: %s", cudaGetErrorString(e));
+        return WFD_OK;
+    }
+};
+
+int common_checks(const wfd_problem* p, const float* vel, const float* wavelet, const int32_t* src,
+                  const int32_t* rec) {
+    int rc = check_problem(p);
+    if (rc) return rc;
+    if (!vel) return fail(WFD_ERR_INVALID, "vel is NULL");
+    if (p->nsrc > 0 && (!wavelet || !src)) return fail(WFD_ERR_INVALID, "wavelet/src is NULL");
+    if (p->nrec > 0 && !rec) return fail(WFD_ERR_INVALID, "rec is NULL");
+    return WFD_OK;
+}
+
+int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
+          const int32_t* src, const int32_t* rec, cudaStream_t s) {
+    WFD_CUDA(launch_vel_to_m(vel, w.m, g.nz, g.ny, g.nx, g.ld, p->dt / p->dx, s));
+    WFD_CUDA(launch_build_lists(src, p->nshot, p->nsrc, g.nz, g.ny, g.nx, g.ld, g.R, g.tile_z,
+                                g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
+                                const_cast<int*>(w.src.off), const_cast<int2*>(w.src.ent), w.err, s));
+    WFD_CUDA(launch_build_lists(rec, p->nshot, p->nrec, g.nz, g.ny, g.nx, g.ld, g.R, g.tile_z,
+                                g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
+                                const_cast<int*>(w.rec.off), const_cast<int2*>(w.rec.ent), w.err, s));
+    return WFD_OK;
+}
+
+// Forward time loop. With save: checkpoints every K steps and the L u store of
+// the last segment (which the backward then does not recompute).
+int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
+                const Stepper& st, const float* wavelet, float* traces, bool save) {
+    cudaStream_t s = st.s;
+    WFD_CUDA(cudaMemsetAsync(w.P[0], 0, L.field_bytes, s));
+    WFD_CUDA(cudaMemsetAsync(w.P[1], 0, L.field_bytes, s));
+    CUtensorMap mc[2], mo[2], ml;
+    int rc;
+    for (int b = 0; b < 2; ++b)
+        if ((rc = st.map_pair(w.P[b], w.P[b], &mc[b], &mo[b]))) return rc;
+    const long long n_all = (long long)p->nshot * g.cells;
+    for (int n = 0; n < p->nt; ++n) {
+        const int bc = n & 1, bn = (n + 1) & 1;
+        if (save && n % g.K == 0) {
+            unsigned char* slot = w.ckpt + (size_t)(n / g.K) * 2 * L.ckpt_field_bytes;
+            WFD_CUDA(launch_pack(w.P[bn], slot, n_all, p->ckpt_bf16, s));
+            WFD_CUDA(launch_pack(w.P[bc], slot + L.ckpt_field_bytes, n_all, p->ckpt_bf16, s));
+        }
+        const bool lap = save && n >= g.k0_last;
+        StepArgs a = st.base(w.P[bn]);
+        a.inj = w.src;
+        a.inj_val = wavelet;
+        a.inj_np = p->nsrc; a.inj_nt = p->nt; a.inj_t = n;
+        a.inj_scale = p->src_scale;
+        if (p->nsrc == 0) a.inj.off = nullptr;
+        if (traces && n >= 1 && p->nrec > 0) {
+            a.smp = w.rec;
+            a.smp_out = traces;
+            a.smp_np = p->nrec; a.smp_nt = p->nt; a.smp_t = n - 1;
+            a.smp_scale = 1.f;
+        }
+        if (lap) {
+            a.lap = w.lap + (size_t)(n - g.k0_last) * L.lap_field_bytes;
+            a.lap_bf16 = p->lap_bf16;
+        }
+        if ((rc = st.launch(lap ? MODE_SAVE_LAP : MODE_PLAIN, mc[bc], mo[bn], mc[bc], a))) return rc;
+    }
+    if (traces && p->nrec > 0)
+        WFD_CUDA(launch_gather(w.P[p->nt & 1], g.cells, w.rec, g.ntiles, p->nshot, p->nrec, nullptr,
+                               1.f, 0, traces, p->nt, p->nt - 1, s));
+    return WFD_OK;
+}
+
+int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
+                 const Stepper& st, const float* wavelet, const float* dtraces, float* grad_vel,
+                 float* grad_wavelet, const float* vel) {
+    cudaStream_t s = st.s;
+    WFD_CUDA(cudaMemsetAsync(w.Q[0], 0, L.field_bytes, s));
+    WFD_CUDA(cudaMemsetAsync(w.Q[1], 0, L.field_bytes, s));
+    WFD_CUDA(cudaMemsetAsync(w.G, 0, (size_t)g.cells * 4, s));
+    int rc;
+    CUtensorMap pc[2], po[2], qc[2], qo[2];
+    for (int b = 0; b < 2; ++b) {
+        if ((rc = st.map_pair(w.P[b], w.P[b], &pc[b], &po[b]))) return rc;
+        if ((rc = st.map_pair(w.Q[b], w.Q[b], &qc[b], &qo[b]))) return rc;
+    }
+    std::vector<CUtensorMap> lm(g.K);
+    for (int k = 0; k < g.K; ++k)
+        if ((rc = st.lap_map(w.lap + (size_t)k * L.lap_field_bytes, p->lap_bf16, &lm[k]))) return rc;
+    const long long n_all = (long long)p->nshot * g.cells;
+
+    auto adjoint_step = [&](int k, bool with_grad, int slot) -> int {
+        const int bc = (k + 1) & 1, bn = k & 1;  // cur = q_{k+1}, new = q_k over q_{k+2}
+        StepArgs a = st.base(w.Q[bn]);
+        if (p->nrec > 0) {
+            a.inj = w.rec;
+            a.inj_val = dtraces;
+            a.inj_np = p->nrec; a.inj_nt = p->nt; a.inj_t = k - 1;
+            a.inj_scale = 1.f;
+            a.inj_times_m = 1;
+        }
+        if (grad_wavelet && k <= p->nt - 1 && p->nsrc > 0) {
+            a.smp = w.src;
+            a.smp_out = grad_wavelet;
+            a.smp_np = p->nsrc; a.smp_nt = p->nt; a.smp_t = k;
+            a.smp_scale = p->src_scale;
+            a.smp_div_m = 1;
+        }
+        int mode = MODE_PLAIN;
+        if (with_grad) {
+            mode = MODE_GRAD;
+            a.lap = w.lap + (size_t)slot * L.lap_field_bytes;
+            a.lap_bf16 = p->lap_bf16;
+            a.grad = w.G;
+        }
+        return st.launch(mode, qc[bc], qo[bn], with_grad ? lm[slot] : qc[bc], a);
+    };
+
+    if ((rc = adjoint_step(p->nt, false, 0))) return rc;
+    for (int j = g.nseg - 1; j >= 0; --j) {
+        const int k0 = j * g.K, k1 = std::min(p->nt, k0 + g.K);
+        if (j != g.nseg - 1) {
+            const unsigned char* slot = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
+            WFD_CUDA(launch_unpack(slot, w.P[(k0 + 1) & 1], n_all, p->ckpt_bf16, s));
+            WFD_CUDA(launch_unpack(slot + L.ckpt_field_bytes, w.P[k0 & 1], n_all, p->ckpt_bf16, s));
+            for (int k = k0; k < k1; ++k) {
+                const int bc = k & 1, bn = (k + 1) & 1;
+                StepArgs a = st.base(w.P[bn]);
+                if (p->nsrc > 0) {
+                    a.inj = w.src;
+                    a.inj_val = wavelet;
+                    a.inj_np = p->nsrc; a.inj_nt = p->nt; a.inj_t = k;
+                    a.inj_scale = p->src_scale;
+                }
+                a.lap = w.lap + (size_t)(k - k0) * L.lap_field_bytes;
+                a.lap_bf16 = p->lap_bf16;
+                if ((rc = st.launch(MODE_SAVE_LAP, pc[bc], po[bn], pc[bc], a))) return rc;
+            }
+        }
+        for (int k = k1 - 1; k >= std::max(k0, 1); --k)
+            if ((rc = adjoint_step(k, true, k - k0))) return rc;
+    }
+    if (grad_wavelet && p->nsrc > 0)  // q_1 at the sources -> d J / d w_0
+        WFD_CUDA(launch_gather(w.Q[1], g.cells, w.src, g.ntiles, p->nshot, p->nsrc, w.m,
+                               p->src_scale, 1, grad_wavelet, p->nt, 0, s));
+    WFD_CUDA(launch_grad_finalize(w.G, vel, grad_vel, g.nz, g.ny, g.nx, g.ld, g.R, s));
+    return WFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* wfd_strerror(int status) {
+    switch (status) {
+        case WFD_OK: return "ok";
+        case WFD_ERR_INVALID: return "invalid argument";
+        case WFD_ERR_WORKSPACE: return "workspace too small or misaligned";
+        case WFD_ERR_CUDA: return "CUDA call failed";
+        case WFD_ERR_UNSTABLE: return "time step violates the CFL bound";
+        case WFD_ERR_POSITION: return "source or receiver outside the updated interior";
+        case WFD_ERR_TIMEOUT: return "kernel timed out waiting for a TMA tile";
+        case WFD_ERR_STATE: return "backward without a checkpointed forward";
+        default: return "unknown status";
+    }
+}
+
+const char* wfd_last_error(void) { return g_last_error.c_str(); }
+
+int wfd_version(void) { return (1 << 16) | 0; }
+
+int wfd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes) {
+    int rc = check_problem(p);
+    if (rc) return rc;
+    if (!bytes) return fail(WFD_ERR_INVALID, "bytes is NULL");
+    const Geom g = make_geom(p);
+    *bytes = make_layout(p, g, with_gradient != 0).total;
+    return WFD_OK;
+}
+
+int wfd_forward(const wfd_problem* p, const float* vel, const float* sponge_z,
+                const float* sponge_y, const float* sponge_x, const float* wavelet,
+                const int32_t* src, const int32_t* rec, float* traces, int save_checkpoints,
+                void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = common_checks(p, vel, wavelet, src, rec);
+    if (rc) return rc;
+    const Geom g = make_geom(p);
+    const Layout L = make_layout(p, g, save_checkpoints != 0);
+    if ((rc = check_workspace(workspace, workspace_bytes, L.total))) return rc;
+    const Work w = carve(workspace, L, save_checkpoints != 0);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if ((rc = setup(p, g, w, vel, src, rec, s))) return rc;
+    Stepper st{p, g, s, w.err, w.m, sponge_z, p->ndim == 3 ? sponge_y : nullptr, sponge_x};
+    return run_forward(p, g, L, w, st, wavelet, traces, save_checkpoints != 0);
+}
+
+int wfd_backward(const wfd_problem* p, const float* vel, const float* sponge_z,
+                 const float* sponge_y, const float* sponge_x, const float* wavelet,
+                 const int32_t* src, const int32_t* rec, const float* dtraces, float* grad_vel,
+                 float* grad_wavelet, void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = common_checks(p, vel, wavelet, src, rec);
+    if (rc) return rc;
+    if (!grad_vel || (p->nrec > 0 && !dtraces))
+        return fail(WFD_ERR_INVALID, "grad_vel/dtraces is NULL");
+    const Geom g = make_geom(p);
+    const Layout L = make_layout(p, g, true);
+    if ((rc = check_workspace(workspace, workspace_bytes, L.total))) return rc;
+    const Work w = carve(workspace, L, true);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Stepper st{p, g, s, w.err, w.m, sponge_z, p->ndim == 3 ? sponge_y : nullptr, sponge_x};
+    return run_backward(p, g, L, w, st, wavelet, dtraces, grad_vel, grad_wavelet, vel);
+}
+
+int wfd_misfit_gradient(const wfd_problem* p, const float* vel, const float* sponge_z,
+                        const float* sponge_y, const float* sponge_x, const float* wavelet,
+                        const int32_t* src, const int32_t* rec, const float* observed,
+                        float* traces, float* grad_vel, float* grad_wavelet, double* misfit,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = common_checks(p, vel, wavelet, src, rec);
+    if (rc) return rc;
+    if (!grad_vel || !misfit || (p->nrec > 0 && !observed))
+        return fail(WFD_ERR_INVALID, "grad_vel/misfit/observed is NULL");
+    const Geom g = make_geom(p);
+    const Layout L = make_layout(p, g, true);
+    if ((rc = check_workspace(workspace, workspace_bytes, L.total))) return rc;
+    const Work w = carve(workspace, L, true);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if ((rc = setup(p, g, w, vel, src, rec, s))) return rc;
+    Stepper st{p, g, s, w.err, w.m, sponge_z, p->ndim == 3 ? sponge_y : nullptr, sponge_x};
+    float* d = traces ? traces : w.res;
+    if ((rc = run_forward(p, g, L, w, st, wavelet, d, true))) return rc;
+    const long long ntr = (long long)p->nshot * p->nt * p->nrec;
+    WFD_CUDA(cudaMemsetAsync(misfit, 0, sizeof(double), s));
+    if (ntr > 0) WFD_CUDA(launch_residual_misfit(d, observed, w.res, ntr, misfit, s));
+    return run_backward(p, g, L, w, st, wavelet, w.res, grad_vel, grad_wavelet, vel);
+}
+
+int wfd_status(void* workspace, void* stream) {
+    if (!workspace) return fail(WFD_ERR_WORKSPACE, "workspace is NULL");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned h = 0;
+    WFD_CUDA(cudaMemcpyAsync(&h, workspace, sizeof h, cudaMemcpyDeviceToHost, s));
+    WFD_CUDA(cudaStreamSynchronize(s));
+    WFD_CUDA(cudaMemsetAsync(workspace, 0, sizeof h, s));
+    if (h & DEV_ERR_TMA_TIMEOUT) return fail(WFD_ERR_TIMEOUT, "device: TMA wait timed out");
+    if (h & DEV_ERR_BAD_POSITION)
+        return fail(WFD_ERR_POSITION, "device: a source/receiver lies outside the interior");
+    return WFD_OK;
+}
+
+int wfd_sum_sq(const float* x, int64_t n, double* out, void* stream) {
+    if (!x || !out || n < 0) return fail(WFD_ERR_INVALID, "bad sum_sq arguments");
+    WFD_CUDA(launch_sum_sq(x, n, out, static_cast<cudaStream_t>(stream)));
+    return WFD_OK;
+}
+
+int wfd_step2d_order2(const float* u0, const float* u1, float* u2, float wavespeed, float dt,
+                      float dx, float dy, int N, int M, int M_padded, void* stream) {
+    if (!u0 || !u1 || !u2) return fail(WFD_ERR_INVALID, "NULL field");
+    if (N < 3 || M < 3 || M_padded < M || M_padded % 4)
+        return fail(WFD_ERR_INVALID, "need N, M >= 3 and M_padded >= M, M_padded %% 4 == 0");
+    if (!aligned16(u0) || !aligned16(u1) || !aligned16(u2))
+        return fail(WFD_ERR_INVALID, "fields must be 16-byte aligned");
+    if ((long long)N * M_padded >= (1ll << 31)) return fail(WFD_ERR_INVALID, "grid too large");
+    // rows i (N) are the kernel's z axis with spacing dx, columns j (M) its x
+    // axis with spacing dy; all of dt^2 c^2 / h^2 goes into the weights, m = 1.
+    const float cz = float((double)dt * dt * wavespeed * wavespeed / ((double)dx * dx));
+    const float cx = float((double)dt * dt * wavespeed * wavespeed / ((double)dy * dy));
+    StepArgs a{};
+    a.u_new = u2;
+    a.m = nullptr;
+    a.m_const = 1.f;
+    a.nz = N; a.ny = 1; a.nx = M; a.ld = M_padded;
+    a.plane = M_padded;
+    a.shot_stride = (long long)N * M_padded;
+    a.nshot = 1; a.shots_per_cta = 1;
+    a.tiles_x = cdiv(M, T2_TX); a.tiles_y = 1; a.tiles_z = cdiv(N, T2_TZ);
+    a.c0 = -2.f * (cz + cx);
+    a.cz[0] = cz;
+    a.cx[0] = cx;
+    a.err = nullptr;
+    CUtensorMap mc, mo;
+    const cuuint32_t bc[3] = {T2_W, T2_TZ + 2, 1};
+    const cuuint32_t bo[3] = {T2_TX, T2_TZ, 1};
+    int rc;
+    if ((rc = make_field_map(&mc, u1, false, 2, N, 1, M, M_padded, 1, bc))) return rc;
+    if ((rc = make_field_map(&mo, u0, false, 2, N, 1, M, M_padded, 1, bo))) return rc;
+    cudaError_t e = launch_step2d(1, MODE_PLAIN, mc, mo, mc, a, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "step launch failed: %s", cudaGetErrorString(e));
+    return WFD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,245 @@
+// Small helper kernels of the wave path: model conversion, per-tile point
+// lists, gathers, checkpoint packing, FP64 misfit / norm reductions.
+// All are launched once per call (or once per checkpoint), not per cell-step,
+// except the checkpoint pack which runs every ckpt_every steps.
+#include "common.cuh"
+#include "internal.h"
+
+namespace wfd {
+namespace {
+
+__global__ void vel_to_m_kernel(const float* __restrict__ vel, float* __restrict__ m, int nz,
+                                int ny, int nx, int ld, float scale) {
+    const long long n = (long long)nz * ny * ld;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = int(i % ld);
+        const long long zy = i / ld;
+        float v = 0.f;
+        if (x < nx) v = vel[zy * nx + x] * scale;
+        m[i] = v * v;
+    }
+}
+
+__device__ __forceinline__ bool decode(const int32_t* pos, int nz, int ny, int nx, int R, int& z,
+                                       int& y, int& x) {
+    z = pos[0];
+    y = pos[1];
+    x = pos[2];
+    const bool zok = z >= R && z < nz - R, xok = x >= R && x < nx - R;
+    const bool yok = ny == 1 ? y == 0 : (y >= R && y < ny - R);
+    return zok && yok && xok;
+}
+
+__global__ void count_kernel(const int32_t* __restrict__ pos, int nshot, int np, int nz, int ny,
+                             int nx, int R, int tz, int ty, int tx, int tiles_y, int tiles_x,
+                             int ntiles, int* counts, unsigned* err) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)nshot * np) return;
+    const int s = int(i / np);
+    int z, y, x;
+    if (!decode(pos + 3 * i, nz, ny, nx, R, z, y, x)) {
+        report(err, DEV_ERR_BAD_POSITION);
+        return;
+    }
+    const int t = ((z / tz) * tiles_y + (y / ty)) * tiles_x + (x / tx);
+    atomicAdd(&counts[(long long)s * ntiles + t], 1);
+}
+
+// Exclusive scan of counts into off[0..n] in one block; counts reset to 0 so
+// they serve as fill cursors.
+__global__ void scan_kernel(int* counts, int* off, int n) {
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int lo = min(n, t * per), hi = min(n, lo + per);
+    int sum = 0;
+    for (int i = lo; i < hi; ++i) sum += counts[i];
+    part[t] = sum;
+    __syncthreads();
+    for (int d = 1; d < (int)blockDim.x; d <<= 1) {
+        const int v = t >= d ? part[t - d] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = part[t] - sum;  // exclusive prefix of this thread's chunk
+    for (int i = lo; i < hi; ++i) {
+        off[i] = run;
+        run += counts[i];
+        counts[i] = 0;
+    }
+    if (t == blockDim.x - 1) off[n] = part[t];
+}
+
+__global__ void fill_kernel(const int32_t* __restrict__ pos, int nshot, int np, int nz, int ny,
+                            int nx, int ld, int R, int tz, int ty, int tx, int tiles_y,
+                            int tiles_x, int ntiles, int* cursor, const int* off, int2* ent) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)nshot * np) return;
+    const int s = int(i / np), p = int(i % np);
+    int z, y, x;
+    if (!decode(pos + 3 * i, nz, ny, nx, R, z, y, x)) return;
+    const long long key = (long long)s * ntiles + ((z / tz) * tiles_y + (y / ty)) * tiles_x + x / tx;
+    const int slot = off[key] + atomicAdd(&cursor[key], 1);
+    ent[slot] = make_int2(int(((long long)z * ny + y) * ld + x), p);
+}
+
+__global__ void gather_kernel(const float* __restrict__ u, long long shot_stride, const int* off,
+                              const int2* ent, int ntiles, int np, const float* m, float scale,
+                              int div_m, float* out, int out_nt, int out_t) {
+    const int s = blockIdx.y;
+    const int lo = off[(long long)s * ntiles], hi = off[(long long)(s + 1) * ntiles];
+    const int j = lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= hi) return;
+    const int2 en = ent[j];
+    float v = u[s * shot_stride + en.x] * scale;
+    if (div_m) v /= m[en.x];
+    out[((long long)s * out_nt + out_t) * np + en.y] = v;
+}
+
+__global__ void pack_kernel(const float4* __restrict__ src, void* dst, long long n4, int to_bf16) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float4 v = src[i];
+        if (to_bf16)
+            static_cast<uint2*>(dst)[i] = pack_bf16x4(v);
+        else
+            static_cast<float4*>(dst)[i] = v;
+    }
+}
+
+__global__ void unpack_kernel(const void* src, float4* __restrict__ dst, long long n4,
+                              int from_bf16) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
+         i += (long long)gridDim.x * blockDim.x) {
+        dst[i] = from_bf16 ? unpack_bf16x4(static_cast<const uint2*>(src)[i])
+                           : static_cast<const float4*>(src)[i];
+    }
+}
+
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double warp_sums[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) warp_sums[w] = v;
+    __syncthreads();
+    v = threadIdx.x < (blockDim.x >> 5) ? warp_sums[threadIdx.x] : 0.0;
+    if (w == 0)
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// res = d - obs (FP32); misfit += 1/2 sum res^2 accumulated in FP64.
+__global__ void residual_misfit_kernel(const float* __restrict__ d, const float* __restrict__ obs,
+                                       float* __restrict__ res, long long n, double* misfit) {
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float r = d[i] - obs[i];
+        res[i] = r;
+        acc += 0.5 * double(r) * double(r);
+    }
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) atomicAdd(misfit, acc);
+}
+
+__global__ void sum_sq_kernel(const float* __restrict__ x, long long n, double* out) {
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        acc += double(x[i]) * double(x[i]);
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) atomicAdd(out, acc);
+}
+
+// grad_vel = dJ/dv = (G / m) dm/dv = 2 G / v on the interior, 0 on the ring.
+__global__ void grad_finalize_kernel(const float* __restrict__ G, const float* __restrict__ vel,
+                                     float* __restrict__ gv, int nz, int ny, int nx, int ld,
+                                     int R) {
+    const long long n = (long long)nz * ny * nx;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = int(i % nx);
+        const long long zy = i / nx;
+        const int y = int(zy % ny), z = int(zy / ny);
+        const bool in = z >= R && z < nz - R && x >= R && x < nx - R &&
+                        (ny == 1 || (y >= R && y < ny - R));
+        gv[i] = in ? 2.f * G[zy * ld + x] / vel[i] : 0.f;
+    }
+}
+
+int grid_for(long long n, int block = 256) {
+    long long g = (n + block - 1) / block;
+    return int(g < 1 ? 1 : (g > 152 * 32 ? 152 * 32 : g));
+}
+
+}  // namespace
+
+cudaError_t launch_vel_to_m(const float* vel, float* m, int nz, int ny, int nx, int ld,
+                            float scale, cudaStream_t s) {
+    vel_to_m_kernel<<<grid_for((long long)nz * ny * ld), 256, 0, s>>>(vel, m, nz, ny, nx, ld, scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_lists(const int32_t* pos, int nshot, int np, int nz, int ny, int nx,
+                               int ld, int R, int tile_z, int tile_y, int tile_x, int tiles_z,
+                               int tiles_y, int tiles_x, int* counts, int* off, int2* ent,
+                               unsigned* err, cudaStream_t s) {
+    const int ntiles = tiles_z * tiles_y * tiles_x;
+    const long long nkeys = (long long)nshot * ntiles;
+    cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * nkeys, s);
+    if (e != cudaSuccess) return e;
+    const long long npts = (long long)nshot * np;
+    const int blocks = int((npts + 255) / 256);
+    if (npts > 0)
+        count_kernel<<<blocks, 256, 0, s>>>(pos, nshot, np, nz, ny, nx, R, tile_z, tile_y, tile_x,
+                                            tiles_y, tiles_x, ntiles, counts, err);
+    scan_kernel<<<1, 1024, 0, s>>>(counts, off, int(nkeys));
+    if (npts > 0)
+        fill_kernel<<<blocks, 256, 0, s>>>(pos, nshot, np, nz, ny, nx, ld, R, tile_z, tile_y,
+                                           tile_x, tiles_y, tiles_x, ntiles, counts, off, ent);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const float* u, long long shot_stride, PointLists lists, int ntiles,
+                          int nshot, int np, const float* m, float scale, int div_m, float* out,
+                          int out_nt, int out_t, cudaStream_t s) {
+    if (np == 0 || nshot == 0) return cudaSuccess;
+    const dim3 grid((np + 127) / 128, nshot);
+    gather_kernel<<<grid, 128, 0, s>>>(u, shot_stride, lists.off, lists.ent, ntiles, np, m, scale,
+                                       div_m, out, out_nt, out_t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack(const float* src, void* dst, long long n, int to_bf16, cudaStream_t s) {
+    pack_kernel<<<grid_for(n / 4), 256, 0, s>>>(reinterpret_cast<const float4*>(src), dst, n / 4,
+                                                to_bf16);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(const void* src, float* dst, long long n, int from_bf16, cudaStream_t s) {
+    unpack_kernel<<<grid_for(n / 4), 256, 0, s>>>(src, reinterpret_cast<float4*>(dst), n / 4,
+                                                  from_bf16);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_residual_misfit(const float* d, const float* obs, float* res, long long n,
+                                   double* misfit, cudaStream_t s) {
+    residual_misfit_kernel<<<grid_for(n), 256, 0, s>>>(d, obs, res, n, misfit);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sum_sq(const float* x, long long n, double* out, cudaStream_t s) {
+    sum_sq_kernel<<<grid_for(n), 256, 0, s>>>(x, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grad_finalize(const float* G, const float* vel, float* grad_vel, int nz,
+                                 int ny, int nx, int ld, int R, cudaStream_t s) {
+    grad_finalize_kernel<<<grid_for((long long)nz * ny * nx), 256, 0, s>>>(G, vel, grad_vel, nz,
+                                                                         ny, nx, ld, R);
+    return cudaGetLastError();
+}
+
+}  // namespace wfd

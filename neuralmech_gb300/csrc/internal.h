@@ -1,0 +1,118 @@
+// Internal interface between the C-ABI layer (api.cu) and the kernels.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace wfd {
+
+// Device error bits, OR-ed into the workspace's status word.
+enum : unsigned {
+    DEV_ERR_TMA_TIMEOUT = 1u << 0,   // an mbarrier wait for a TMA tile gave up
+    DEV_ERR_BAD_POSITION = 1u << 1,  // a source/receiver outside the updated interior
+};
+
+// ---------------------------------------------------------------- 2D tiles
+// One CTA = 256 threads = 8 warps. A lane owns 4 consecutive x cells (one
+// float4); a warp owns RB consecutive rows; the CTA tile is TX x TZ cells.
+// u_n is staged with a halo of R rows and XH = 4 columns (XH keeps every TMA
+// x coordinate 16-byte aligned for any R <= 4).
+constexpr int T2_THREADS = 256;
+constexpr int T2_TX = 128;
+constexpr int T2_XH = 4;
+constexpr int T2_W = T2_TX + 2 * T2_XH;  // staged row length (floats)
+constexpr int T2_RB = 4;
+constexpr int T2_TZ = 8 * T2_RB;         // 32 rows
+constexpr int T2_STAGES = 2;
+
+// What a step kernel does besides the stencil update.
+enum StepMode : int {
+    MODE_PLAIN = 0,     // update only
+    MODE_SAVE_LAP = 1,  // update + store L u_n (forward recompute)
+    MODE_GRAD = 2,      // update + accumulate q_{k+1} * L u_k into the gradient (adjoint)
+};
+
+// A set of points (sources or receivers) bucketed by the tile that owns them.
+// off[s * ntiles + t] .. off[s * ntiles + t + 1] index ent[], ent = {cell, p}
+// with cell the in-shot linear index (z * plane + y * ld + x) and p the point
+// number within the shot.
+struct PointLists {
+    const int* off = nullptr;
+    const int2* ent = nullptr;
+};
+
+struct StepArgs {
+    float* u_new;              // overwritten level, [nshot][cells] (aliases the u_{n-1} buffer)
+    const float* m;            // (v dt / dx)^2, [cells]; null -> m_const
+    float m_const;
+    const float* gz;           // sponge profiles (null = no sponge on that axis)
+    const float* gy;
+    const float* gx;
+    int nz, ny, nx, ld;        // ny = 1 in 2D
+    long long plane;           // ny * ld (3D) or ld (2D): z stride
+    long long shot_stride;     // cells per shot (nz * plane)
+    int nshot, shots_per_cta;
+    int tiles_x, tiles_y, tiles_z;
+    float c0;                  // centre weight (all axes)
+    float cz[4], cy[4], cx[4]; // axis weights for k = 1..R, already scaled by (dx/h)^2
+    // injection into u_new: u += g * scale * val (* m at the cell when inj_times_m)
+    PointLists inj;
+    const float* inj_val;      // [nshot][inj_nt][inj_np]
+    int inj_np, inj_nt, inj_t;
+    float inj_scale;
+    int inj_times_m;
+    // sampling of the staged level u_n: out[s][smp_t][p] = scale * u_n(cell) (/ m)
+    PointLists smp;
+    float* smp_out;            // [nshot][smp_nt][smp_np]
+    int smp_np, smp_nt, smp_t;
+    float smp_scale;
+    int smp_div_m;
+    // Laplacian store (MODE_SAVE_LAP writes, MODE_GRAD reads via TMA)
+    void* lap;                 // [nshot][cells] FP32 or BF16
+    int lap_bf16;
+    float* grad;               // [cells], MODE_GRAD accumulation target
+    unsigned* err;
+};
+
+// Launches one time step of the 2D kernel of half-width R (1, 2, 4) and mode.
+// map_cur: u_n (box T2_W x (T2_TZ + 2R) x 1); map_old: u_{n-1} (box T2_TX x T2_TZ x 1);
+// map_lap: Laplacian store (box T2_TX x T2_TZ x 1), used by MODE_GRAD only.
+cudaError_t launch_step2d(int R, int mode, const CUtensorMap& map_cur, const CUtensorMap& map_old,
+                          const CUtensorMap& map_lap, const StepArgs& a, cudaStream_t s);
+size_t step2d_smem_bytes(int R, int mode);
+
+// ---------------------------------------------------------------- 3D tiles
+// One CTA marches along z through a (TY x TX) column of the grid, 4 x cells
+// per thread, a register queue of 2R+1 planes per cell.
+constexpr int T3_TX = 64;
+constexpr int T3_TY = 16;
+constexpr int T3_XH = 4;
+constexpr int T3_W = T3_TX + 2 * T3_XH;
+constexpr int T3_THREADS = (T3_TX / 4) * T3_TY;  // 256
+constexpr int T3_ZCHUNK = 64;                    // planes per CTA (z blocking)
+constexpr int T3_STAGES = 4;
+
+cudaError_t launch_step3d(int R, int mode, const CUtensorMap& map_cur, const CUtensorMap& map_old,
+                          const CUtensorMap& map_lap, const StepArgs& a, cudaStream_t s);
+size_t step3d_smem_bytes(int R, int mode);
+bool step3d_available();
+
+// ---------------------------------------------------------------- helpers (aux.cu)
+cudaError_t launch_vel_to_m(const float* vel, float* m, int nz, int ny, int nx, int ld,
+                            float scale, cudaStream_t s);
+cudaError_t launch_build_lists(const int32_t* pos, int nshot, int np, int nz, int ny, int nx,
+                               int ld, int R, int tile_z, int tile_y, int tile_x, int tiles_z,
+                               int tiles_y, int tiles_x, int* counts, int* off, int2* ent,
+                               unsigned* err, cudaStream_t s);
+cudaError_t launch_gather(const float* u, long long shot_stride, PointLists lists, int ntiles,
+                          int nshot, int np, const float* m, float scale, int div_m,
+                          float* out, int out_nt, int out_t, cudaStream_t s);
+cudaError_t launch_pack(const float* src, void* dst, long long n, int to_bf16, cudaStream_t s);
+cudaError_t launch_unpack(const void* src, float* dst, long long n, int from_bf16, cudaStream_t s);
+cudaError_t launch_residual_misfit(const float* d, const float* obs, float* res, long long n,
+                                   double* misfit, cudaStream_t s);
+cudaError_t launch_grad_finalize(const float* G, const float* vel, float* grad_vel, int nz,
+                                 int ny, int nx, int ld, int R, cudaStream_t s);
+cudaError_t launch_sum_sq(const float* x, long long n, double* out, cudaStream_t s);
+
+}  // namespace wfd

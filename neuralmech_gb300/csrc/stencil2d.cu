@@ -1,0 +1,307 @@
+// 2D time-step kernel of the acoustic wave path (sm_103a).
+//
+// One launch advances every shot of a batch by one step:
+//   u_{n+1} = g (2 u_n + m L u_n) - g^2 u_{n-1}    on the interior,
+// with m = (v dt / dx)^2, L the order-2R central Laplacian (per-axis weights
+// pre-scaled by (dx/h)^2) and g = gz[z] gx[x] the sponge factor. It replaces
+// the reference's padded_step (projects/18_simple_wave_fd/step2D_wave.cu:59-81),
+// which is the R = 1, g = 1, constant-m case.
+//
+// Layout in HBM: each field is [shot][z][ld] FP32, ld a multiple of 8; the
+// model m is [z][ld], shared by all shots. u_{n+1} overwrites u_{n-1} in place.
+//
+// Per CTA (256 threads): a 128 x 32 tile of one shot at a time, over
+// `shots_per_cta` shots of the batch. For each shot a TMA bulk-tensor load
+// brings u_n with a halo of R rows and 4 columns and the u_{n-1} tile into
+// shared memory; two stages are in flight so the next shot's tiles load while
+// this one computes. m, the sponge factors and the gradient accumulator stay
+// in registers across the shots, so m is read once per tile per step and the
+// gradient written once per tile per step. Lane l owns x = x0 + 4l .. +3
+// (float4 loads/stores); warp w owns rows z0 + 4w .. +3, with the vertical
+// taps held in a register window.
+//
+// Fused per-step point work, bucketed by tile (PointLists):
+//   * sampling of the staged u_n at receivers (traces of the previous step),
+//   * injection into u_{n+1} (sources, or m-scaled residuals in the adjoint),
+//   * MODE_SAVE_LAP: L u_n stored (FP32 or BF16) for the adjoint's imaging term,
+//   * MODE_GRAD: q_{k+1} L u_k accumulated into the gradient.
+#include "common.cuh"
+#include "internal.h"
+
+namespace wfd {
+namespace {
+
+__host__ __device__ constexpr int align_up(int v, int a) { return (v + a - 1) / a * a; }
+
+template <int R, int MODE>
+struct Layout2D {
+    static constexpr int H = T2_TZ + 2 * R;
+    static constexpr int CUR = H * T2_W * 4;  // TMA box bytes of u_n
+    static constexpr int OLD = T2_TZ * T2_TX * 4;
+    static constexpr int LAP = MODE == MODE_GRAD ? T2_TZ * T2_TX * 4 : 0;
+    // every TMA destination starts on a 128-byte boundary
+    static constexpr int CUR_AL = align_up(CUR, 128);
+    static constexpr int OLD_AL = align_up(OLD, 128);
+    static constexpr int STAGE = align_up(CUR_AL + OLD_AL + LAP, 128);
+    static constexpr int BYTES = T2_STAGES * STAGE + 64 + 128;  // + barriers + alignment slack
+};
+
+__device__ __forceinline__ float comp(const float4& v, int e) {
+    return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+}
+
+template <int R, int MODE>
+__global__ void __launch_bounds__(T2_THREADS, 2)
+    step2d_kernel(const __grid_constant__ CUtensorMap map_cur,
+                  const __grid_constant__ CUtensorMap map_old,
+                  const __grid_constant__ CUtensorMap map_lap, const StepArgs a) {
+    using L = Layout2D<R, MODE>;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* base = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base + T2_STAGES * L::STAGE);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tile = blockIdx.x;
+    const int ntiles = a.tiles_x * a.tiles_z;
+    const int x0 = (tile % a.tiles_x) * T2_TX;
+    const int z0 = (tile / a.tiles_x) * T2_TZ;
+    const int s0 = blockIdx.y * a.shots_per_cta;
+    const int ns = min(a.nshot - s0, a.shots_per_cta);
+    if (ns <= 0) return;
+
+    const uint32_t lap_bytes =
+        MODE == MODE_GRAD ? uint32_t(T2_TZ * T2_TX * (a.lap_bf16 ? 2 : 4)) : 0u;
+    const uint32_t stage_tx = uint32_t(L::CUR + L::OLD) + lap_bytes;
+    auto cur_buf = [&](int b) { return reinterpret_cast<float*>(base + b * L::STAGE); };
+    auto old_buf = [&](int b) { return reinterpret_cast<float*>(base + b * L::STAGE + L::CUR_AL); };
+    auto lap_buf = [&](int b) { return base + b * L::STAGE + L::CUR_AL + L::OLD_AL; };
+
+    auto issue = [&](int i) {  // called by thread 0 only
+        const int b = i % T2_STAGES;
+        mbar_arrive_expect_tx(&bars[b], stage_tx);
+        tma_load_3d(cur_buf(b), &map_cur, x0 - T2_XH, z0 - R, s0 + i, &bars[b]);
+        tma_load_3d(old_buf(b), &map_old, x0, z0, s0 + i, &bars[b]);
+        if (MODE == MODE_GRAD) tma_load_3d(lap_buf(b), &map_lap, x0, z0, s0 + i, &bars[b]);
+    };
+
+    if (tid == 0) {
+        for (int b = 0; b < T2_STAGES; ++b) mbar_init(&bars[b], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int i = 0; i < min(ns, T2_STAGES); ++i) issue(i);
+
+    // ---- per-thread constants, reused for every shot of the CTA
+    const int x = x0 + 4 * lane;
+    const int zb = z0 + warp * T2_RB;
+    float4 mrow[T2_RB];
+    float gzr[T2_RB];
+    bool zin[T2_RB];
+#pragma unroll
+    for (int r = 0; r < T2_RB; ++r) {
+        const int z = zb + r;
+        if (a.m != nullptr && z < a.nz && x < a.ld)
+            mrow[r] = __ldg(reinterpret_cast<const float4*>(a.m + (long long)z * a.ld + x));
+        else
+            mrow[r] = make_float4(a.m_const, a.m_const, a.m_const, a.m_const);
+        gzr[r] = (a.gz != nullptr && z < a.nz) ? __ldg(a.gz + z) : 1.f;
+        zin[r] = z >= R && z < a.nz - R;
+    }
+    float gxe[4];
+    bool xin[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        gxe[e] = (a.gx != nullptr && x + e < a.nx) ? __ldg(a.gx + x + e) : 1.f;
+        xin[e] = x + e >= R && x + e < a.nx - R;
+    }
+    const bool all_x = xin[0] && xin[1] && xin[2] && xin[3];
+
+    float4 gacc[T2_RB];
+#pragma unroll
+    for (int r = 0; r < T2_RB; ++r) gacc[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+
+    for (int i = 0; i < ns; ++i) {
+        const int s = s0 + i, b = i % T2_STAGES;
+        if (!mbar_wait(&bars[b], (i / T2_STAGES) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
+        const float* cur = cur_buf(b);
+        const float* old = old_buf(b);
+        float* un = a.u_new + (long long)s * a.shot_stride;
+
+        float4 V[T2_RB + 2 * R];
+#pragma unroll
+        for (int j = 0; j < T2_RB + 2 * R; ++j)
+            V[j] = *reinterpret_cast<const float4*>(cur + (warp * T2_RB + j) * T2_W + T2_XH +
+                                                    4 * lane);
+#pragma unroll
+        for (int r = 0; r < T2_RB; ++r) {
+            const int z = zb + r;
+            const float* row = cur + (warp * T2_RB + r + R) * T2_W + 4 * lane;
+            const float4 lv = *reinterpret_cast<const float4*>(row);
+            const float4 cv = V[r + R];
+            const float4 rv = *reinterpret_cast<const float4*>(row + 2 * T2_XH);
+            const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y,
+                                 cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
+            const float4 ov =
+                *reinterpret_cast<const float4*>(old + (warp * T2_RB + r) * T2_TX + 4 * lane);
+            float lap[4], nv[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                float acc = a.c0 * w[4 + e];
+#pragma unroll
+                for (int k = 1; k <= R; ++k) {
+                    acc = fmaf(a.cx[k - 1], w[4 + e - k] + w[4 + e + k], acc);
+                    acc = fmaf(a.cz[k - 1], comp(V[r + R - k], e) + comp(V[r + R + k], e), acc);
+                }
+                lap[e] = acc;
+                const float g = gzr[r] * gxe[e];
+                const float c = w[4 + e];
+                nv[e] = g * fmaf(comp(mrow[r], e), acc, 2.f * c) - (g * g) * comp(ov, e);
+            }
+            const long long off = (long long)z * a.ld + x;
+            if (zin[r] && all_x) {
+                *reinterpret_cast<float4*>(un + off) = make_float4(nv[0], nv[1], nv[2], nv[3]);
+            } else if (zin[r]) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (xin[e]) un[off + e] = nv[e];
+            }
+            if (MODE == MODE_SAVE_LAP && zin[r]) {
+                const long long lo = (long long)s * a.shot_stride + off;
+                const float4 lp = make_float4(lap[0], lap[1], lap[2], lap[3]);
+                if (all_x) {
+                    if (a.lap_bf16)
+                        *reinterpret_cast<uint2*>(static_cast<__nv_bfloat16*>(a.lap) + lo) =
+                            pack_bf16x4(lp);
+                    else
+                        *reinterpret_cast<float4*>(static_cast<float*>(a.lap) + lo) = lp;
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        if (xin[e]) {
+                            if (a.lap_bf16)
+                                static_cast<__nv_bfloat16*>(a.lap)[lo + e] =
+                                    __float2bfloat16_rn(lap[e]);
+                            else
+                                static_cast<float*>(a.lap)[lo + e] = lap[e];
+                        }
+                }
+            }
+            if (MODE == MODE_GRAD && zin[r]) {
+                const unsigned char* lb = lap_buf(b);
+                const int li = (warp * T2_RB + r) * T2_TX + 4 * lane;
+                const float4 lu =
+                    a.lap_bf16 ? unpack_bf16x4(*reinterpret_cast<const uint2*>(
+                                     reinterpret_cast<const __nv_bfloat16*>(lb) + li))
+                               : *reinterpret_cast<const float4*>(
+                                     reinterpret_cast<const float*>(lb) + li);
+                gacc[r].x += xin[0] ? cv.x * lu.x : 0.f;
+                gacc[r].y += xin[1] ? cv.y * lu.y : 0.f;
+                gacc[r].z += xin[2] ? cv.z * lu.z : 0.f;
+                gacc[r].w += xin[3] ? cv.w * lu.w : 0.f;
+            }
+        }
+
+        // sampling of the staged level u_n (receivers of the previous step,
+        // or the adjoint field at the sources)
+        if (a.smp.off != nullptr) {
+            const int lo = a.smp.off[s * ntiles + tile], hi = a.smp.off[s * ntiles + tile + 1];
+            for (int j = lo + tid; j < hi; j += T2_THREADS) {
+                const int2 en = a.smp.ent[j];
+                const int z = en.x / a.ld, xx = en.x - z * a.ld;
+                float v = cur[(z - z0 + R) * T2_W + (xx - x0 + T2_XH)] * a.smp_scale;
+                if (a.smp_div_m) v /= (a.m != nullptr ? a.m[en.x] : a.m_const);
+                a.smp_out[((long long)s * a.smp_nt + a.smp_t) * a.smp_np + en.y] = v;
+            }
+        }
+        __syncthreads();  // stage b fully read; this shot's u_{n+1} stores done
+        if (tid == 0 && i + T2_STAGES < ns) {
+            fence_proxy_async_smem();
+            issue(i + T2_STAGES);
+        }
+        // injection into u_{n+1}, after every store of this shot
+        if (a.inj.off != nullptr) {
+            const int lo = a.inj.off[s * ntiles + tile], hi = a.inj.off[s * ntiles + tile + 1];
+            for (int j = lo + tid; j < hi; j += T2_THREADS) {
+                const int2 en = a.inj.ent[j];
+                const int z = en.x / a.ld, xx = en.x - z * a.ld;
+                float v = a.inj_val[((long long)s * a.inj_nt + a.inj_t) * a.inj_np + en.y] *
+                          a.inj_scale;
+                if (a.inj_times_m) v *= (a.m != nullptr ? a.m[en.x] : a.m_const);
+                const float g = (a.gz ? a.gz[z] : 1.f) * (a.gx ? a.gx[xx] : 1.f);
+                atomicAdd(un + en.x, g * v);
+            }
+        }
+    }
+
+    if (MODE == MODE_GRAD) {
+#pragma unroll
+        for (int r = 0; r < T2_RB; ++r) {
+            if (!zin[r]) continue;
+            float* gp = a.grad + (long long)(zb + r) * a.ld + x;
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (xin[e]) atomicAdd(gp + e, comp(gacc[r], e));
+        }
+    }
+}
+
+template <int R, int MODE>
+cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
+                        const StepArgs& a, cudaStream_t s) {
+    using L = Layout2D<R, MODE>;
+    static int configured_device = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (configured_device != dev) {
+        cudaError_t e = cudaFuncSetAttribute(step2d_kernel<R, MODE>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
+        if (e != cudaSuccess) return e;
+        configured_device = dev;
+    }
+    const dim3 grid(a.tiles_x * a.tiles_z, (a.nshot + a.shots_per_cta - 1) / a.shots_per_cta);
+    step2d_kernel<R, MODE><<<grid, T2_THREADS, L::BYTES, s>>>(mc, mo, ml, a);
+    return cudaGetLastError();
+}
+
+template <int R>
+cudaError_t dispatch_mode(int mode, const CUtensorMap& mc, const CUtensorMap& mo,
+                          const CUtensorMap& ml, const StepArgs& a, cudaStream_t s) {
+    switch (mode) {
+        case MODE_PLAIN: return launch_impl<R, MODE_PLAIN>(mc, mo, ml, a, s);
+        case MODE_SAVE_LAP: return launch_impl<R, MODE_SAVE_LAP>(mc, mo, ml, a, s);
+        case MODE_GRAD: return launch_impl<R, MODE_GRAD>(mc, mo, ml, a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_step2d(int R, int mode, const CUtensorMap& mc, const CUtensorMap& mo,
+                          const CUtensorMap& ml, const StepArgs& a, cudaStream_t s) {
+    switch (R) {
+        case 1: return dispatch_mode<1>(mode, mc, mo, ml, a, s);
+        case 2: return dispatch_mode<2>(mode, mc, mo, ml, a, s);
+        case 4: return dispatch_mode<4>(mode, mc, mo, ml, a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+size_t step2d_smem_bytes(int R, int mode) {
+    auto pick = [&](auto r_tag) -> size_t {
+        constexpr int RR = decltype(r_tag)::value;
+        switch (mode) {
+            case MODE_PLAIN: return Layout2D<RR, MODE_PLAIN>::BYTES;
+            case MODE_SAVE_LAP: return Layout2D<RR, MODE_SAVE_LAP>::BYTES;
+            default: return Layout2D<RR, MODE_GRAD>::BYTES;
+        }
+    };
+    switch (R) {
+        case 1: return pick(std::integral_constant<int, 1>{});
+        case 2: return pick(std::integral_constant<int, 2>{});
+        default: return pick(std::integral_constant<int, 4>{});
+    }
+}
+
+}  // namespace wfd

@@ -1,0 +1,368 @@
+"""Python host API of the GB300 finite-difference acoustic wave path.
+
+PyTorch tensors in, PyTorch tensors out; every call goes through the C ABI of
+libwavefd.so (include/wavefd.h) on the current CUDA stream. There is no CPU
+path: tensors must live on a CUDA device.
+
+Mapping to the reference (cmpmech/neuralmech):
+  * ``step2d_order2``  <- padded_step, projects/18_simple_wave_fd/step2D_wave.cu:59-81
+    as driven by 2D_wave_cuda_padding.py:66-76 (same arguments, u2 may alias u0);
+  * ``wave_forward``   <- cuwave ``measure(sim, sources, indicator, sensors)``
+    (projects/18_fwi/plate.py:140-142): one forward per shot, traces stacked
+    (shot, step, receiver); differentiable through ``torch.autograd``;
+  * ``misfit_gradient`` <- cuwave ``misfit_gradient(sim, sources, gamma, sensors,
+    observed) -> (cost, gradient)`` (projects/18_fwi/2D_fwi.py:40), here with
+    respect to the velocity (and optionally the wavelets);
+  * ``stable_dt``      <- cuwave ``stable_dt(dx, c, order)`` (projects/18_fwi/helper.py:52).
+
+Discretisation (shared with the FP64 oracle):
+  u_{n+1} = g (2 u_n + (v dt)^2 L u_n + src_scale w_n) - g^2 u_{n-1}
+on the interior; the outer ring of order/2 cells stays 0; L is the central
+Laplacian of space order 2, 4 or 8; g the product of the per-axis
+exponential (Cerjan) sponge profiles; traces[s, n, r] = u_{n+1}(rec[s, r]).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+# ---------------------------------------------------------------- descriptors
+@dataclass(frozen=True)
+class Grid:
+    """Simulation descriptor (the role of cuwave's ``ScalarWave``).
+
+    shape    (nz, nx) or (nz, ny, nx) cells
+    spacing  (dz, dx) or (dz, dy, dx)
+    dt, nt   time step and number of steps
+    order    space order (2, 4, 8)
+    sponge   sponge width in cells: one int for every face, or one
+             (low, high) pair per axis
+    sponge_strength  alpha W of the taper exp(-(alpha d)^2), d the depth into
+             the layer (1 .. W); 0.3 gives the classic Cerjan wall factor 0.914
+    """
+    shape: tuple
+    spacing: tuple
+    dt: float
+    nt: int
+    order: int = 8
+    sponge: object = 20
+    sponge_strength: float = 0.3
+    src_scale: float = 1.0
+    ckpt_every: int = 0
+    ckpt_bf16: bool = True
+    lap_bf16: bool = False
+    shots_per_cta: int = 0
+
+    @property
+    def ndim(self) -> int:
+        return len(self.shape)
+
+    def sponge_widths(self):
+        if isinstance(self.sponge, int):
+            return [(self.sponge, self.sponge)] * self.ndim
+        w = [tuple(p) for p in self.sponge]
+        if len(w) != self.ndim:
+            raise ValueError("sponge needs one (low, high) pair per axis")
+        return w
+
+
+def fd_weights(order: int) -> np.ndarray:
+    """Central second-derivative weights a_0..a_R of space order ``order``."""
+    R = order // 2
+    a = np.zeros(R + 1)
+    for k in range(1, R + 1):
+        a[k] = 2.0 * (1 if k % 2 else -1) * math.factorial(R) ** 2 / (
+            k * k * math.factorial(R - k) * math.factorial(R + k))
+    a[0] = -2.0 * a[1:].sum()
+    return a
+
+
+def stable_dt(spacing, vmax: float, order: int = 8) -> float:
+    """Largest stable leapfrog step: vmax dt sqrt(sum_axis S / h^2) <= 2,
+    S = |a_0| + 2 sum |a_k| (0.5547 h / vmax in 2D, 0.4529 in 3D, order 8)."""
+    a = fd_weights(order)
+    S = abs(a[0]) + 2 * np.abs(a[1:]).sum()
+    return 2.0 / (vmax * math.sqrt(S * sum(1.0 / h**2 for h in spacing)))
+
+
+def sponge_profile(n: int, low: int, high: int, strength: float = 0.3) -> np.ndarray:
+    """1D exponential sponge factors g[0..n-1] (1 in the interior)."""
+    g = np.ones(n, dtype=np.float64)
+    for w, idx in ((low, lambda d: w - d), (high, lambda d: n - 1 - (w - d))):
+        if w <= 0:
+            continue
+        a = strength / w
+        for d in range(1, w + 1):
+            i = idx(d)
+            if 0 <= i < n:
+                g[i] = math.exp(-(a * d) ** 2)
+    return g.astype(np.float32)
+
+
+def sponge_profiles(grid: Grid):
+    """(gz, gy, gx) FP32 profiles (gy None in 2D); None where the width is 0."""
+    widths = grid.sponge_widths()
+    prof = []
+    for n, (lo, hi) in zip(grid.shape, widths):
+        prof.append(None if lo == 0 and hi == 0 else sponge_profile(n, lo, hi, grid.sponge_strength))
+    if grid.ndim == 2:
+        return prof[0], None, prof[1]
+    return tuple(prof)
+
+
+def _problem(grid: Grid, nshot: int, nsrc: int, nrec: int, vmax: float) -> _lib.Problem:
+    if grid.ndim == 2:
+        nz, nx = grid.shape
+        ny = 1
+        dz, dx = grid.spacing
+        dy = 1.0
+    else:
+        nz, ny, nx = grid.shape
+        dz, dy, dx = grid.spacing
+    return _lib.Problem(grid.ndim, grid.order, nz, ny, nx, nshot, grid.nt, nsrc, nrec,
+                        grid.ckpt_every, int(grid.ckpt_bf16), int(grid.lap_bf16),
+                        grid.shots_per_cta, grid.dt, dz, dy, dx, grid.src_scale, vmax)
+
+
+# ---------------------------------------------------------------- argument prep
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _require_cuda(t: torch.Tensor, name: str):
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor (no CPU path)")
+
+
+def _positions(pos, nshot: int, ndim: int, device) -> torch.Tensor:
+    """(nshot, n, 3) int32 (z, y, x) from (n, ndim) or (nshot, n, ndim)."""
+    p = torch.as_tensor(pos, device=device)
+    if p.dim() == 2:
+        p = p.unsqueeze(0).expand(nshot, -1, -1)
+    if p.dim() != 3 or p.shape[0] != nshot or p.shape[2] != ndim:
+        raise ValueError(f"positions must be (n, {ndim}) or ({nshot}, n, {ndim})")
+    p = p.to(torch.int32)
+    if ndim == 2:
+        p = torch.stack([p[..., 0], torch.zeros_like(p[..., 0]), p[..., 1]], dim=-1)
+    return p.contiguous()
+
+
+def _wavelet(w, nshot: int, nt: int, nsrc: int, device) -> torch.Tensor:
+    """(nshot, nt, nsrc) FP32 from (nt,), (nshot, nt) or (nshot, nt, nsrc)."""
+    w = torch.as_tensor(w, device=device, dtype=torch.float32)
+    if w.dim() == 1:
+        w = w.view(1, -1, 1).expand(nshot, -1, nsrc)
+    elif w.dim() == 2:
+        w = w.unsqueeze(-1).expand(-1, -1, nsrc)
+    if tuple(w.shape) != (nshot, nt, nsrc):
+        raise ValueError(f"wavelet must broadcast to ({nshot}, {nt}, {nsrc})")
+    return w.contiguous()
+
+
+@dataclass
+class _Call:
+    grid: Grid
+    problem: _lib.Problem
+    vel: torch.Tensor
+    wavelet: torch.Tensor
+    src: torch.Tensor
+    rec: torch.Tensor
+    sponges: tuple = field(default_factory=tuple)
+
+
+def _prepare(vel, wavelet, src, rec, grid: Grid, nshot=None) -> _Call:
+    _require_cuda(vel, "vel")
+    if tuple(vel.shape) != tuple(grid.shape):
+        raise ValueError(f"vel has shape {tuple(vel.shape)}, grid {grid.shape}")
+    vel = vel.detach().to(torch.float32).contiguous()
+    dev = vel.device
+    src_t = torch.as_tensor(src)
+    if nshot is None:
+        nshot = src_t.shape[0] if src_t.dim() == 3 else 1
+    srcp = _positions(src, nshot, grid.ndim, dev)
+    recp = _positions(rec, nshot, grid.ndim, dev)
+    wav = _wavelet(wavelet, nshot, grid.nt, srcp.shape[1], dev)
+    vmax = float(vel.max())
+    prob = _problem(grid, nshot, srcp.shape[1], recp.shape[1], vmax)
+    gz, gy, gx = sponge_profiles(grid)
+    sp = tuple(None if g is None else torch.from_numpy(g).to(dev) for g in (gz, gy, gx))
+    return _Call(grid, prob, vel, wav, srcp, recp, sp)
+
+
+def workspace_bytes(grid: Grid, nshot: int, nsrc: int, nrec: int, with_gradient: bool) -> int:
+    lib = _lib.load()
+    n = ctypes.c_size_t(0)
+    _lib.check(lib.wfd_workspace_bytes(ctypes.byref(_problem(grid, nshot, nsrc, nrec, 0.0)),
+                                       int(with_gradient), ctypes.byref(n)), "wfd_workspace_bytes")
+    return n.value
+
+
+def _workspace(c: _Call, with_gradient: bool) -> torch.Tensor:
+    lib = _lib.load()
+    n = ctypes.c_size_t(0)
+    _lib.check(lib.wfd_workspace_bytes(ctypes.byref(c.problem), int(with_gradient), ctypes.byref(n)),
+               "wfd_workspace_bytes")
+    ws = torch.empty(n.value + 256, dtype=torch.uint8, device=c.vel.device)
+    off = (-ws.data_ptr()) % 256
+    return ws[off:off + n.value]
+
+
+def _status(ws: torch.Tensor, where: str):
+    _lib.check(_lib.load().wfd_status(_ptr(ws), _stream()), where)
+
+
+# ---------------------------------------------------------------- autograd
+class _WaveForward(torch.autograd.Function):
+    """Traces from (vel, wavelet); backward = the hand-written adjoint."""
+
+    @staticmethod
+    def forward(ctx, vel, wavelet, call: _Call, check: bool):
+        lib = _lib.load()
+        ws = _workspace(call, True)
+        c = call
+        traces = torch.empty((c.problem.nshot, c.problem.nt, c.problem.nrec),
+                             dtype=torch.float32, device=vel.device)
+        gz, gy, gx = c.sponges
+        _lib.check(lib.wfd_forward(ctypes.byref(c.problem), _ptr(c.vel), _ptr(gz), _ptr(gy), _ptr(gx),
+                                   _ptr(c.wavelet), _ptr(c.src), _ptr(c.rec), _ptr(traces), 1,
+                                   _ptr(ws), ws.numel(), _stream()), "wfd_forward")
+        if check:
+            _status(ws, "wfd_forward")
+        ctx.call = call
+        ctx.ws = ws
+        ctx.check = check
+        ctx.wavelet_shape = wavelet.shape
+        return traces
+
+    @staticmethod
+    def backward(ctx, dtraces):
+        lib = _lib.load()
+        c = ctx.call
+        if ctx.ws is None:  # a second backward: redo the checkpointed forward first
+            ctx.ws = _workspace(c, True)
+            gz, gy, gx = c.sponges
+            _lib.check(lib.wfd_forward(ctypes.byref(c.problem), _ptr(c.vel), _ptr(gz), _ptr(gy), _ptr(gx),
+                                       _ptr(c.wavelet), _ptr(c.src), _ptr(c.rec), None, 1,
+                                       _ptr(ctx.ws), ctx.ws.numel(), _stream()), "wfd_forward")
+        ws = ctx.ws
+        dtraces = dtraces.to(torch.float32).contiguous()
+        grad_vel = torch.empty_like(c.vel)
+        want_wav = ctx.needs_input_grad[1]
+        grad_wav = torch.empty_like(c.wavelet) if want_wav else None
+        gz, gy, gx = c.sponges
+        _lib.check(lib.wfd_backward(ctypes.byref(c.problem), _ptr(c.vel), _ptr(gz), _ptr(gy), _ptr(gx),
+                                    _ptr(c.wavelet), _ptr(c.src), _ptr(c.rec), _ptr(dtraces),
+                                    _ptr(grad_vel), _ptr(grad_wav), _ptr(ws), ws.numel(), _stream()),
+                   "wfd_backward")
+        if ctx.check:
+            _status(ws, "wfd_backward")
+        ctx.ws = None
+        gw = None
+        if want_wav:
+            gw = grad_wav
+            shape = ctx.wavelet_shape
+            if len(shape) == 1:
+                gw = gw.sum(dim=(0, 2))
+            elif len(shape) == 2:
+                gw = gw.sum(dim=2)
+        return (grad_vel if ctx.needs_input_grad[0] else None), gw, None, None
+
+
+# ---------------------------------------------------------------- public API
+def wave_forward(vel: torch.Tensor, wavelet, src, rec, grid: Grid, *, check: bool = True):
+    """Traces (nshot, nt, nrec) of every shot through the velocity ``vel``.
+
+    vel      (nz, nx) / (nz, ny, nx) CUDA tensor (m/s); differentiable
+    wavelet  (nt,), (nshot, nt) or (nshot, nt, nsrc); differentiable
+    src, rec (n, ndim) shared by all shots or (nshot, n, ndim) integer cells
+             (z, x) / (z, y, x), inside the interior (>= order/2 from every edge)
+    check    synchronise and raise on device-side errors (bad positions, timeouts)
+    """
+    wav_t = torch.as_tensor(wavelet, device=vel.device)
+    nshot = None
+    s = torch.as_tensor(src)
+    if s.dim() == 3:
+        nshot = s.shape[0]
+    elif wav_t.dim() >= 2:
+        nshot = wav_t.shape[0]
+    call = _prepare(vel, wav_t.detach(), src, rec, grid, nshot)
+    if torch.is_grad_enabled() and (vel.requires_grad or wav_t.requires_grad):
+        return _WaveForward.apply(vel, wav_t, call, check)
+    lib = _lib.load()
+    ws = _workspace(call, False)
+    p = call.problem
+    traces = torch.empty((p.nshot, p.nt, p.nrec), dtype=torch.float32, device=vel.device)
+    gz, gy, gx = call.sponges
+    _lib.check(lib.wfd_forward(ctypes.byref(p), _ptr(call.vel), _ptr(gz), _ptr(gy), _ptr(gx),
+                               _ptr(call.wavelet), _ptr(call.src), _ptr(call.rec), _ptr(traces), 0,
+                               _ptr(ws), ws.numel(), _stream()), "wfd_forward")
+    if check:
+        _status(ws, "wfd_forward")
+    return traces
+
+
+def misfit_gradient(vel: torch.Tensor, wavelet, src, rec, observed: torch.Tensor, grid: Grid, *,
+                    want_wavelet: bool = False, want_traces: bool = False, check: bool = True):
+    """(misfit, grad_vel[, grad_wavelet][, traces]) in one library call.
+
+    misfit = 1/2 sum (traces - observed)^2, accumulated in FP64 on the GPU
+    (a 0-d float64 tensor); grad_vel has vel's shape (0 on the fixed ring)."""
+    wav_t = torch.as_tensor(wavelet, device=vel.device)
+    nshot = observed.shape[0]
+    call = _prepare(vel, wav_t, src, rec, grid, nshot)
+    _require_cuda(observed, "observed")
+    p = call.problem
+    if tuple(observed.shape) != (p.nshot, p.nt, p.nrec):
+        raise ValueError(f"observed must be ({p.nshot}, {p.nt}, {p.nrec})")
+    obs = observed.to(torch.float32).contiguous()
+    lib = _lib.load()
+    ws = _workspace(call, True)
+    grad = torch.empty_like(call.vel)
+    gwav = torch.empty_like(call.wavelet) if want_wavelet else None
+    traces = torch.empty_like(obs) if want_traces else None
+    misfit = torch.zeros((), dtype=torch.float64, device=vel.device)
+    gz, gy, gx = call.sponges
+    _lib.check(lib.wfd_misfit_gradient(ctypes.byref(p), _ptr(call.vel), _ptr(gz), _ptr(gy), _ptr(gx),
+                                       _ptr(call.wavelet), _ptr(call.src), _ptr(call.rec), _ptr(obs),
+                                       _ptr(traces), _ptr(grad), _ptr(gwav), _ptr(misfit),
+                                       _ptr(ws), ws.numel(), _stream()), "wfd_misfit_gradient")
+    if check:
+        _status(ws, "wfd_misfit_gradient")
+    out = [misfit, grad]
+    if want_wavelet:
+        out.append(gwav)
+    if want_traces:
+        out.append(traces)
+    return tuple(out)
+
+
+def sum_sq(x: torch.Tensor) -> torch.Tensor:
+    """FP64 sum of squares of an FP32 CUDA tensor (gradient norms)."""
+    _require_cuda(x, "x")
+    x = x.to(torch.float32).contiguous()
+    out = torch.zeros((), dtype=torch.float64, device=x.device)
+    _lib.check(_lib.load().wfd_sum_sq(_ptr(x), x.numel(), _ptr(out), _stream()), "wfd_sum_sq")
+    return out
+
+
+def step2d_order2(u0, u1, u2, wavespeed: float, dt: float, dx: float, dy: float, N: int, M: int):
+    """padded_step (step2D_wave.cu:59-81): u2 <- -u0 + 2u1 + dt^2 c^2 Lap(u1) on
+    rows 1..N-2, columns 1..M-2 of (N, M_padded) FP32 CUDA tensors; u2 may be u0."""
+    for t, n in ((u0, "u0"), (u1, "u1"), (u2, "u2")):
+        _require_cuda(t, n)
+        if t.dtype != torch.float32 or not t.is_contiguous() or t.dim() != 2:
+            raise ValueError(f"{n} must be a contiguous 2D float32 tensor")
+    _lib.check(_lib.load().wfd_step2d_order2(_ptr(u0), _ptr(u1), _ptr(u2), wavespeed, dt, dx, dy,
+                                             N, M, u1.shape[1], _stream()), "wfd_step2d_order2")
+    return u2

@@ -1,0 +1,117 @@
+"""GPU parity of the forward path: the padded_step shim against the reference's
+own kernel (golden vectors), and the generic forward against the FP64 oracle.
+Tolerances: 1e-5 relative L2 against padded_step (FP32 vs FP32, different
+operation order); 1e-5 relative L2 against the FP64 oracle for FP32 traces.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN, rel_l2
+from helpers import oracle_geometry, small_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def test_step2d_order2_matches_padded_step(cuda):
+    from neuralmech_gb300 import step2d_order2
+    g = np.load(os.path.join(GOLDEN, "padded_step.npz"))
+    for ci in range(2):
+        N, M, MP, steps, c, dt, dx, dy = g[f"c{ci}_params"]
+        N, M, MP, steps = int(N), int(M), int(MP), int(steps)
+        a = torch.from_numpy(g[f"c{ci}_u0"]).to(cuda)
+        b = torch.from_numpy(g[f"c{ci}_u1"]).to(cuda)
+        for t in range(steps):
+            # the driver's in-place rotation: u0 = fd_step(u0, u1, u0); u1, u0 = u0, u1
+            a = step2d_order2(a, b, a, float(np.float32(c)), float(np.float32(dt)),
+                              float(np.float32(dx)), float(np.float32(dy)), N, M)
+            a, b = b, a
+            key = f"c{ci}_step{t}"
+            if key in g:
+                got = b.cpu().numpy()
+                assert rel_l2(got[:, :M], g[key][:, :M]) < 1e-5, (ci, t)
+                # padding columns and the ring are never written
+                assert np.array_equal(got[:, M:], g[key][:, M:])
+                assert np.array_equal(got[0], g[key][0]) and np.array_equal(got[-1], g[key][-1])
+
+
+def test_step2d_order2_separate_output(cuda):
+    from neuralmech_gb300 import step2d_order2
+    g = np.load(os.path.join(GOLDEN, "padded_step.npz"))
+    N, M, MP, steps, c, dt, dx, dy = g["c0_params"]
+    N, M = int(N), int(M)
+    u0 = torch.from_numpy(g["c0_u0"]).to(cuda)
+    u1 = torch.from_numpy(g["c0_u1"]).to(cuda)
+    u2 = torch.full_like(u0, 7.0)
+    step2d_order2(u0, u1, u2, float(c), float(dt), float(dx), float(dy), N, M)
+    got = u2.cpu().numpy()
+    assert rel_l2(got[1:-1, 1:M - 1], g["c0_step0"][1:-1, 1:M - 1]) < 1e-5
+    assert np.all(got[0] == 7.0) and np.all(got[:, 0] == 7.0) and np.all(got[:, M - 1:] == 7.0)
+
+
+@pytest.mark.parametrize("order", [2, 4, 8])
+@pytest.mark.parametrize("shape,sponge,nshot,spc", [
+    ((60, 150), 10, 3, 0),
+    ((37, 131), 0, 2, 1),
+    ((100, 260), (5, 12), 5, 2),
+    ((33, 40), 6, 1, 0),
+])
+def test_forward_matches_oracle(cuda, orc, order, shape, sponge, nshot, spc):
+    from neuralmech_gb300 import wave_forward
+    grid, v, wav, src, rec = small_problem(shape=shape, nshot=nshot, order=order,
+                                           sponge=sponge if isinstance(sponge, int) else [sponge, sponge],
+                                           nt=90, spc=spc, seed=order + nshot)
+    traces = wave_forward(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
+                          torch.from_numpy(src), torch.from_numpy(rec), grid)
+    ref = orc.forward(oracle_geometry(orc, grid, v, wav, src, rec))
+    assert traces.shape == ref.shape
+    assert np.isfinite(ref).all() and np.abs(ref).max() > 0
+    assert rel_l2(traces.cpu().numpy(), ref) < 1e-5
+
+
+def test_forward_many_sources_and_duplicates(cuda, orc):
+    from neuralmech_gb300 import wave_forward
+    grid, v, wav, src, rec = small_problem(shape=(70, 300), nshot=4, nsrc=5, nrec=40, nt=80)
+    src[:, 1] = src[:, 0]  # two sources on one cell (atomic injection)
+    rec[:, 3] = rec[:, 2]  # two receivers on one cell
+    traces = wave_forward(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
+                          torch.from_numpy(src), torch.from_numpy(rec), grid)
+    ref = orc.forward(oracle_geometry(orc, grid, v, wav, src, rec))
+    assert rel_l2(traces.cpu().numpy(), ref) < 1e-5
+    t = traces.cpu().numpy()
+    assert np.array_equal(t[:, :, 2], t[:, :, 3])
+
+
+def test_forward_positions_on_interior_edge(cuda, orc):
+    from neuralmech_gb300 import wave_forward
+    grid, v, wav, src, rec = small_problem(shape=(48, 140), nshot=1, nrec=4, nt=60)
+    R = grid.order // 2
+    src[0, 0] = [R, R]
+    rec[0] = [[R, R], [47 - R, 139 - R], [R, 139 - R], [47 - R, R]]
+    traces = wave_forward(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
+                          torch.from_numpy(src), torch.from_numpy(rec), grid)
+    ref = orc.forward(oracle_geometry(orc, grid, v, wav, src, rec))
+    assert rel_l2(traces.cpu().numpy(), ref) < 1e-5
+
+
+def test_forward_rejects_ring_positions(cuda):
+    from neuralmech_gb300 import wave_forward
+    from neuralmech_gb300._lib import WaveFDError
+    grid, v, wav, src, rec = small_problem(shape=(40, 140), nshot=1, nt=10)
+    rec[0, 0] = [1, 20]  # inside the fixed ring of order 8
+    with pytest.raises(WaveFDError):
+        wave_forward(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
+                     torch.from_numpy(src), torch.from_numpy(rec), grid)
+
+
+def test_forward_no_receivers_no_sources(cuda):
+    from neuralmech_gb300 import wave_forward
+    grid, v, wav, src, rec = small_problem(shape=(40, 140), nshot=2, nt=10)
+    out = wave_forward(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
+                       torch.from_numpy(src), torch.zeros((2, 0, 2), dtype=torch.int32), grid)
+    assert out.shape == (2, 10, 0)
+    out = wave_forward(torch.from_numpy(v).to(cuda), torch.zeros((2, 10, 0), device=cuda),
+                       torch.zeros((2, 0, 2), dtype=torch.int32), torch.from_numpy(rec), grid)
+    assert torch.count_nonzero(out) == 0

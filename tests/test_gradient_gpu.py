@@ -1,0 +1,115 @@
+"""GPU parity of the adjoint path (hand-written adjoint kernel behind
+torch.autograd.Function, checkpointed recomputation).
+
+Tolerances (relative L2 unless stated):
+  * velocity gradient vs the exact FP64 oracle gradient: 1e-4 with FP32
+    checkpoints and FP32 Laplacian store, 1e-3 with BF16 checkpoints;
+  * wavelet gradient vs the oracle: 1e-4 (FP32 storage);
+  * adjoint dot-product test <S w, y> = <w, S^T y>: 1e-5 relative difference;
+  * central finite differences of the FP64 misfit along 8 seeded directions:
+    1e-3 relative difference of the directional derivative.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+from helpers import oracle_geometry, small_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def _observed(orc, grid, v, wav, src, rec, seed=7):
+    """Observed data: the oracle's traces in a perturbed model."""
+    rng = np.random.default_rng(seed)
+    vt = (v * (1 + 0.05 * rng.standard_normal(v.shape).clip(-2, 2))).astype(np.float32)
+    return orc.forward(oracle_geometry(orc, grid, vt, wav, src, rec)).astype(np.float32)
+
+
+@pytest.mark.parametrize("order", [2, 8])
+@pytest.mark.parametrize("shape,nshot,nt,ckpt,spc", [
+    ((60, 150), 3, 100, 0, 0),
+    ((41, 133), 2, 77, 10, 1),
+    ((70, 260), 4, 64, 64, 2),
+])
+def test_gradient_matches_oracle_fp32(cuda, orc, order, shape, nshot, nt, ckpt, spc):
+    from neuralmech_gb300 import misfit_gradient
+    grid, v, wav, src, rec = small_problem(shape=shape, nshot=nshot, nt=nt, order=order,
+                                           ckpt_every=ckpt, spc=spc, seed=3)
+    obs = _observed(orc, grid, v, wav, src, rec)
+    J, g, gw = misfit_gradient(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
+                               torch.from_numpy(src), torch.from_numpy(rec),
+                               torch.from_numpy(obs).to(cuda), grid, want_wavelet=True)
+    Jr, gr, gwr, _ = orc.gradient(oracle_geometry(orc, grid, v, wav, src, rec), obs)
+    assert abs(J.item() - Jr) / Jr < 1e-5
+    assert rel_l2(g.cpu().numpy(), gr) < 1e-4
+    assert rel_l2(gw.cpu().numpy(), gwr) < 1e-4
+
+
+def test_gradient_bf16_checkpoints(cuda, orc):
+    from neuralmech_gb300 import misfit_gradient
+    grid, v, wav, src, rec = small_problem(shape=(80, 200), nshot=3, nt=150, ckpt_every=12,
+                                           ckpt_bf16=True, seed=5)
+    obs = _observed(orc, grid, v, wav, src, rec)
+    J, g = misfit_gradient(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
+                           torch.from_numpy(src), torch.from_numpy(rec),
+                           torch.from_numpy(obs).to(cuda), grid)
+    _, gr, _, _ = orc.gradient(oracle_geometry(orc, grid, v, wav, src, rec), obs)
+    err = rel_l2(g.cpu().numpy(), gr)
+    assert err < 1e-3, err
+
+
+def test_autograd_matches_fused_call(cuda, orc):
+    from neuralmech_gb300 import misfit_gradient, wave_forward
+    grid, v, wav, src, rec = small_problem(shape=(50, 140), nshot=2, nt=70, seed=11)
+    obs = torch.from_numpy(_observed(orc, grid, v, wav, src, rec)).to(cuda)
+    vel = torch.from_numpy(v).to(cuda).requires_grad_(True)
+    traces = wave_forward(vel, torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+                          torch.from_numpy(rec), grid)
+    loss = 0.5 * ((traces - obs) ** 2).sum()
+    loss.backward()
+    J, g = misfit_gradient(vel.detach(), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+                           torch.from_numpy(rec), obs, grid)
+    assert abs(loss.item() - J.item()) / J.item() < 1e-5
+    assert rel_l2(vel.grad.cpu().numpy(), g.cpu().numpy()) < 1e-6
+
+
+def test_adjoint_dot_product(cuda):
+    """<S w, y> = <w, S^T y> for the linear map S: wavelets -> traces."""
+    from neuralmech_gb300 import wave_forward
+    grid, v, wav, src, rec = small_problem(shape=(64, 180), nshot=3, nsrc=2, nrec=23, nt=110, seed=2)
+    rng = np.random.default_rng(0)
+    w = torch.from_numpy(rng.standard_normal(wav.shape).astype(np.float32)).to(cuda).requires_grad_(True)
+    y = torch.from_numpy(rng.standard_normal((3, 110, 23)).astype(np.float32)).to(cuda)
+    traces = wave_forward(torch.from_numpy(v).to(cuda), w, torch.from_numpy(src),
+                          torch.from_numpy(rec), grid)
+    traces.backward(y)
+    lhs = float((traces.double() * y.double()).sum())
+    rhs = float((w.detach().double() * w.grad.double()).sum())
+    assert abs(lhs - rhs) / max(abs(lhs), abs(rhs)) < 1e-5
+
+
+def test_gradient_finite_differences(cuda, orc):
+    """Directional derivative <grad, d> vs central differences of the FP64
+    oracle misfit along 8 seeded directions."""
+    from neuralmech_gb300 import misfit_gradient
+    grid, v, wav, src, rec = small_problem(shape=(48, 130), nshot=2, nt=90, seed=9)
+    obs = _observed(orc, grid, v, wav, src, rec)
+    J, g = misfit_gradient(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
+                           torch.from_numpy(src), torch.from_numpy(rec),
+                           torch.from_numpy(obs).to(cuda), grid)
+    g = g.cpu().numpy().astype(np.float64)
+    rng = np.random.default_rng(1)
+    geo = oracle_geometry(orc, grid, v, wav, src, rec)
+    from scipy.ndimage import gaussian_filter
+    for _ in range(8):
+        d = gaussian_filter(rng.standard_normal(v.shape), 3.0)
+        d *= 0.01 * np.abs(v).mean() / np.abs(d).max()
+        eps = 1.0
+        Js = []
+        for sgn in (1, -1):
+            geo.vel = v.astype(np.float64) + sgn * eps * d
+            Js.append(0.5 * ((orc.forward(geo) - obs) ** 2).sum())
+        fd = (Js[0] - Js[1]) / (2 * eps)
+        an = float((g * d).sum())
+        assert abs(fd - an) / abs(fd) < 1e-3, (fd, an)

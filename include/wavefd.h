@@ -36,6 +36,11 @@ extern "C" {
 #define WFD_ERR_TIMEOUT (-6)   /* a kernel gave up waiting for a TMA tile */
 #define WFD_ERR_STATE (-7)     /* wfd_backward without a preceding checkpointed forward */
 
+/* Checkpoint snapshot formats (bytes per cell). */
+#define WFD_CKPT_FP32 0 /* 4 */
+#define WFD_CKPT_BF16 1 /* 2, round to nearest even */
+#define WFD_CKPT_I16 2  /* 2 + 4/32: int16 with one FP32 scale per 32 cells (block max / 32767) */
+
 typedef struct wfd_problem {
     int32_t ndim;          /* 2 or 3 */
     int32_t order;         /* space order: 2, 4 or 8 */
@@ -44,7 +49,7 @@ typedef struct wfd_problem {
     int32_t nt;            /* time steps */
     int32_t nsrc, nrec;    /* sources / receivers per shot */
     int32_t ckpt_every;    /* steps between checkpoints; 0 = ceil(sqrt(nt)) */
-    int32_t ckpt_bf16;     /* 1: checkpoint snapshots stored as BF16, 0: FP32 */
+    int32_t ckpt_format;   /* checkpoint snapshots: WFD_CKPT_FP32, _BF16 or _I16 */
     int32_t lap_bf16;      /* 1: per-segment L u store in BF16, 0: FP32 */
     int32_t shots_per_cta; /* shots one CTA walks through per step; 0 = automatic */
     float dt;              /* time step */

@@ -129,6 +129,8 @@ int check_problem(const wfd_problem* p) {
     if (p->nshot > 65535 * 64) return fail(WFD_ERR_INVALID, "too many shots");
     if (!(p->dt > 0) || !(p->dx > 0) || !(p->dz > 0) || (p->ndim == 3 && !(p->dy > 0)))
         return fail(WFD_ERR_INVALID, "dt and spacings must be positive");
+    if (p->ckpt_format < WFD_CKPT_FP32 || p->ckpt_format > WFD_CKPT_I16)
+        return fail(WFD_ERR_INVALID, "unknown checkpoint format %d", p->ckpt_format);
     if (p->ckpt_every < 0 || p->shots_per_cta < 0)
         return fail(WFD_ERR_INVALID, "ckpt_every and shots_per_cta must be >= 0");
     if (p->vmax > 0) {
@@ -219,8 +221,9 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     L.rec_off = take((keys + 1) * 4);
     L.rec_ent = take((size_t)p->nshot * p->nrec * 8 + 8);
     if (grad) {
-        L.ckpt_field_bytes = (size_t)p->nshot * g.cells * (p->ckpt_bf16 ? 2 : 4);
-        L.lap_field_bytes = (size_t)p->nshot * g.cells * (p->lap_bf16 ? 2 : 4);
+        // per-field slots start on 256-byte boundaries (TMA bases, short4/float4 access)
+        L.ckpt_field_bytes = up256(ckpt_bytes(p->ckpt_format, (long long)p->nshot * g.cells));
+        L.lap_field_bytes = up256((size_t)p->nshot * g.cells * (p->lap_bf16 ? 2 : 4));
         L.Q0 = take(L.field_bytes);
         L.Q1 = take(L.field_bytes);
         L.G = take((size_t)g.cells * 4);
@@ -347,6 +350,7 @@ int common_checks(const wfd_problem* p, const float* vel, const float* wavelet, 
 
 int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
           const int32_t* src, const int32_t* rec, cudaStream_t s) {
+    WFD_CUDA(cudaMemsetAsync(w.err, 0, sizeof(unsigned), s));  // fresh status word
     WFD_CUDA(launch_vel_to_m(vel, w.m, g.nz, g.ny, g.nx, g.ld, p->dt / p->dx, s));
     WFD_CUDA(launch_build_lists(src, p->nshot, p->nsrc, g.nz, g.ny, g.nx, g.ld, g.R, g.tile_z,
                                 g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
@@ -373,8 +377,8 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
         const int bc = n & 1, bn = (n + 1) & 1;
         if (save && n % g.K == 0) {
             unsigned char* slot = w.ckpt + (size_t)(n / g.K) * 2 * L.ckpt_field_bytes;
-            WFD_CUDA(launch_pack(w.P[bn], slot, n_all, p->ckpt_bf16, s));
-            WFD_CUDA(launch_pack(w.P[bc], slot + L.ckpt_field_bytes, n_all, p->ckpt_bf16, s));
+            WFD_CUDA(launch_pack(w.P[bn], slot, n_all, p->ckpt_format, s));
+            WFD_CUDA(launch_pack(w.P[bc], slot + L.ckpt_field_bytes, n_all, p->ckpt_format, s));
         }
         const bool lap = save && n >= g.k0_last;
         StepArgs a = st.base(w.P[bn]);
@@ -451,8 +455,8 @@ int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Wor
         const int k0 = j * g.K, k1 = std::min(p->nt, k0 + g.K);
         if (j != g.nseg - 1) {
             const unsigned char* slot = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
-            WFD_CUDA(launch_unpack(slot, w.P[(k0 + 1) & 1], n_all, p->ckpt_bf16, s));
-            WFD_CUDA(launch_unpack(slot + L.ckpt_field_bytes, w.P[k0 & 1], n_all, p->ckpt_bf16, s));
+            WFD_CUDA(launch_unpack(slot, w.P[(k0 + 1) & 1], n_all, p->ckpt_format, s));
+            WFD_CUDA(launch_unpack(slot + L.ckpt_field_bytes, w.P[k0 & 1], n_all, p->ckpt_format, s));
             for (int k = k0; k < k1; ++k) {
                 const int bc = k & 1, bn = (k + 1) & 1;
                 StepArgs a = st.base(w.P[bn]);

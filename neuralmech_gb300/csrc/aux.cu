@@ -98,23 +98,57 @@ __global__ void gather_kernel(const float* __restrict__ u, long long shot_stride
     out[((long long)s * out_nt + out_t) * np + en.y] = v;
 }
 
-__global__ void pack_kernel(const float4* __restrict__ src, void* dst, long long n4, int to_bf16) {
+__global__ void pack_kernel(const float4* __restrict__ src, void* dst, long long n4, int fmt) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
          i += (long long)gridDim.x * blockDim.x) {
         const float4 v = src[i];
-        if (to_bf16)
+        if (fmt == 1)
             static_cast<uint2*>(dst)[i] = pack_bf16x4(v);
         else
             static_cast<float4*>(dst)[i] = v;
     }
 }
 
-__global__ void unpack_kernel(const void* src, float4* __restrict__ dst, long long n4,
-                              int from_bf16) {
+__global__ void unpack_kernel(const void* src, float4* __restrict__ dst, long long n4, int fmt) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
          i += (long long)gridDim.x * blockDim.x) {
-        dst[i] = from_bf16 ? unpack_bf16x4(static_cast<const uint2*>(src)[i])
-                           : static_cast<const float4*>(src)[i];
+        dst[i] = fmt == 1 ? unpack_bf16x4(static_cast<const uint2*>(src)[i])
+                          : static_cast<const float4*>(src)[i];
+    }
+}
+
+// Block-scaled int16: each block of 32 consecutive values (8 float4, 8 lanes)
+// stores round(v * 32767 / max|v|) and one FP32 scale max|v| / 32767. A warp
+// walks chunks of 32 float4 (4 blocks); the block max is a 3-step xor shuffle.
+__global__ void pack_i16_kernel(const float4* __restrict__ src, short4* __restrict__ q,
+                                float* __restrict__ scales, long long n4) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const long long nchunks = (n4 + 31) / 32;
+    for (long long c = warp; c < nchunks; c += nwarps) {
+        const long long i = c * 32 + lane;
+        const float4 v = i < n4 ? src[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float m = fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 4));
+        const float inv = m > 0.f ? 32767.f / m : 0.f;
+        if (i < n4) {
+            q[i] = make_short4(short(__float2int_rn(v.x * inv)), short(__float2int_rn(v.y * inv)),
+                               short(__float2int_rn(v.z * inv)), short(__float2int_rn(v.w * inv)));
+            if ((lane & 7) == 0) scales[i / 8] = m / 32767.f;
+        }
+    }
+}
+
+__global__ void unpack_i16_kernel(const short4* __restrict__ q, const float* __restrict__ scales,
+                                  float4* __restrict__ dst, long long n4) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
+         i += (long long)gridDim.x * blockDim.x) {
+        const short4 v = q[i];
+        const float sc = scales[i / 8];
+        dst[i] = make_float4(v.x * sc, v.y * sc, v.z * sc, v.w * sc);
     }
 }
 
@@ -212,15 +246,34 @@ cudaError_t launch_gather(const float* u, long long shot_stride, PointLists list
     return cudaGetLastError();
 }
 
-cudaError_t launch_pack(const float* src, void* dst, long long n, int to_bf16, cudaStream_t s) {
-    pack_kernel<<<grid_for(n / 4), 256, 0, s>>>(reinterpret_cast<const float4*>(src), dst, n / 4,
-                                                to_bf16);
+size_t ckpt_bytes(int format, long long n) {
+    if (format == 2) return (size_t)((n * 2 + 15) / 16 * 16) + (size_t)((n + 31) / 32) * 4;
+    return (size_t)n * (format == 1 ? 2 : 4);
+}
+
+cudaError_t launch_pack(const float* src, void* dst, long long n, int format, cudaStream_t s) {
+    if (format == 2) {
+        short4* q = static_cast<short4*>(dst);
+        float* sc = reinterpret_cast<float*>(static_cast<unsigned char*>(dst) + (n * 2 + 15) / 16 * 16);
+        pack_i16_kernel<<<grid_for(n / 4), 256, 0, s>>>(reinterpret_cast<const float4*>(src), q, sc,
+                                                        n / 4);
+    } else {
+        pack_kernel<<<grid_for(n / 4), 256, 0, s>>>(reinterpret_cast<const float4*>(src), dst,
+                                                    n / 4, format);
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_unpack(const void* src, float* dst, long long n, int from_bf16, cudaStream_t s) {
-    unpack_kernel<<<grid_for(n / 4), 256, 0, s>>>(src, reinterpret_cast<float4*>(dst), n / 4,
-                                                  from_bf16);
+cudaError_t launch_unpack(const void* src, float* dst, long long n, int format, cudaStream_t s) {
+    if (format == 2) {
+        const short4* q = static_cast<const short4*>(src);
+        const float* sc = reinterpret_cast<const float*>(static_cast<const unsigned char*>(src) +
+                                                         (n * 2 + 15) / 16 * 16);
+        unpack_i16_kernel<<<grid_for(n / 4), 256, 0, s>>>(q, sc, reinterpret_cast<float4*>(dst), n / 4);
+    } else {
+        unpack_kernel<<<grid_for(n / 4), 256, 0, s>>>(src, reinterpret_cast<float4*>(dst), n / 4,
+                                                      format);
+    }
     return cudaGetLastError();
 }
 

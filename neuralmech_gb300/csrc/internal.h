@@ -107,8 +107,11 @@ cudaError_t launch_build_lists(const int32_t* pos, int nshot, int np, int nz, in
 cudaError_t launch_gather(const float* u, long long shot_stride, PointLists lists, int ntiles,
                           int nshot, int np, const float* m, float scale, int div_m,
                           float* out, int out_nt, int out_t, cudaStream_t s);
-cudaError_t launch_pack(const float* src, void* dst, long long n, int to_bf16, cudaStream_t s);
-cudaError_t launch_unpack(const void* src, float* dst, long long n, int from_bf16, cudaStream_t s);
+// Checkpoint codec: format 0 FP32 copy, 1 BF16, 2 int16 + FP32 scale per 32
+// values (scales stored after the n int16 values). n is a multiple of 4.
+size_t ckpt_bytes(int format, long long n);
+cudaError_t launch_pack(const float* src, void* dst, long long n, int format, cudaStream_t s);
+cudaError_t launch_unpack(const void* src, float* dst, long long n, int format, cudaStream_t s);
 cudaError_t launch_residual_misfit(const float* d, const float* obs, float* res, long long n,
                                    double* misfit, cudaStream_t s);
 cudaError_t launch_grad_finalize(const float* G, const float* vel, float* grad_vel, int nz,

@@ -136,7 +136,7 @@ def fwi3d(n: int = 384, nt: int = 1500, nshot: int = 16, nrec_side: int = 64, se
     vmax = float(max(true.max(), init.max()))
     dt = cfl * dx / vmax
     grid = Grid((n, n, n), (dx, dx, dx), dt, nt, order=order, sponge=20, ckpt_every=ckpt_every,
-                ckpt_bf16=True)
+                ckpt_format="bf16")
     R = order // 2
     side = int(math.ceil(math.sqrt(nshot)))
     pos = _surface_line(n, side, R + n // 8, n - R - 1 - n // 8)
@@ -151,7 +151,7 @@ def fwi3d(n: int = 384, nt: int = 1500, nshot: int = 16, nrec_side: int = 64, se
 
 def batch_models(nmodels: int = 8, nshot: int = 128, sizes=(512, 1536, 64), steps=(1000, 3000),
                  freqs=(10.0, 25.0), seed: int = 0, dx: float = 10.0, cfl: float = 0.5,
-                 order: int = 8, ckpt_every: int = 0, ckpt_bf16: bool = True):
+                 order: int = 8, ckpt_every: int = 0, ckpt_format: str = "bf16"):
     """Uneven batch: nmodels seeded layered+anomaly models of random square size
     and step count, shots split as evenly as possible; each entry a Workload
     with its own observed-data model (vel_true) and smoothed start model."""
@@ -167,7 +167,7 @@ def batch_models(nmodels: int = 8, nshot: int = 128, sizes=(512, 1536, 64), step
                   ckpt_every=ckpt_every, order=order, name=f"batch{i}")
         g = w.grid
         w.grid = Grid(g.shape, g.spacing, g.dt, g.nt, order=g.order, sponge=g.sponge,
-                      ckpt_every=ckpt_every, ckpt_bf16=ckpt_bf16)
+                      ckpt_every=ckpt_every, ckpt_format=ckpt_format)
         out.append(w)
     return out
 

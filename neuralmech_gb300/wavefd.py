@@ -34,6 +34,9 @@ from . import _lib
 
 
 # ---------------------------------------------------------------- descriptors
+CKPT_FORMATS = {"fp32": 0, "bf16": 1, "i16": 2}
+
+
 @dataclass(frozen=True)
 class Grid:
     """Simulation descriptor (the role of cuwave's ``ScalarWave``).
@@ -46,6 +49,11 @@ class Grid:
              (low, high) pair per axis
     sponge_strength  alpha W of the taper exp(-(alpha d)^2), d the depth into
              the layer (1 .. W); 0.3 gives the classic Cerjan wall factor 0.914
+    ckpt_every   steps between checkpoints of the adjoint (0 = ceil(sqrt(nt)))
+    ckpt_format  checkpoint snapshots: "fp32", "bf16" or "i16" (int16 with one
+             FP32 scale per 32 cells)
+    lap_bf16     store the per-segment L u of the recomputed forward in BF16
+    shots_per_cta  shots one CTA walks through per step (0 = automatic)
     """
     shape: tuple
     spacing: tuple
@@ -56,7 +64,7 @@ class Grid:
     sponge_strength: float = 0.3
     src_scale: float = 1.0
     ckpt_every: int = 0
-    ckpt_bf16: bool = True
+    ckpt_format: str = "bf16"
     lap_bf16: bool = False
     shots_per_cta: int = 0
 
@@ -127,7 +135,7 @@ def _problem(grid: Grid, nshot: int, nsrc: int, nrec: int, vmax: float) -> _lib.
         nz, ny, nx = grid.shape
         dz, dy, dx = grid.spacing
     return _lib.Problem(grid.ndim, grid.order, nz, ny, nx, nshot, grid.nt, nsrc, nrec,
-                        grid.ckpt_every, int(grid.ckpt_bf16), int(grid.lap_bf16),
+                        grid.ckpt_every, CKPT_FORMATS[grid.ckpt_format], int(grid.lap_bf16),
                         grid.shots_per_cta, grid.dt, dz, dy, dx, grid.src_scale, vmax)
 
 

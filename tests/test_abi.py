@@ -1,0 +1,102 @@
+"""CPU tests of the C ABI: libwavefd.so loads, exports every entry point that
+include/wavefd.h declares, and its host-only calls validate their arguments.
+No compute call is made (no GPU here)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    text = open(os.path.join(ROOT, "include", "wavefd.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(wfd_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declarations_exported():
+    from neuralmech_gb300 import _lib
+    lib = _lib.load()
+    names = _declared()
+    assert names, "no declarations parsed"
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in wavefd.h but not exported"
+    assert set(names) <= set(_lib.EXPORTS) | set(names)
+    assert set(_lib.EXPORTS) == set(names)
+
+
+def test_version_and_strerror():
+    from neuralmech_gb300 import _lib
+    lib = _lib.load()
+    assert lib.wfd_version() >> 16 == 1
+    for code in range(0, -8, -1):
+        assert lib.wfd_strerror(code).decode()
+    assert lib.wfd_strerror(-99).decode() == "unknown status"
+
+
+def _problem(**kw):
+    from neuralmech_gb300 import _lib
+    base = dict(ndim=2, order=8, nz=64, ny=1, nx=100, nshot=2, nt=50, nsrc=1, nrec=5,
+                ckpt_every=0, ckpt_format=1, lap_bf16=0, shots_per_cta=0, dt=1e-3, dz=10.0,
+                dy=1.0, dx=10.0, src_scale=1.0, vmax=3000.0)
+    base.update(kw)
+    return _lib.Problem(**base)
+
+
+def _ws(p, grad=1):
+    from neuralmech_gb300 import _lib
+    n = ctypes.c_size_t(0)
+    rc = _lib.load().wfd_workspace_bytes(ctypes.byref(p), grad, ctypes.byref(n))
+    return rc, n.value
+
+
+def test_workspace_bytes_grows_with_gradient():
+    rc0, n0 = _ws(_problem(), 0)
+    rc1, n1 = _ws(_problem(), 1)
+    assert rc0 == 0 and rc1 == 0 and 0 < n0 < n1
+    # two FP32 fields of 2 x 64 x 104 cells at least
+    assert n0 >= 2 * 2 * 64 * 104 * 4
+    # BF16 checkpoints take about half the FP32 checkpoint space
+    _, f32 = _ws(_problem(ckpt_format=0))
+    _, b16 = _ws(_problem(ckpt_format=1))
+    _, i16 = _ws(_problem(ckpt_format=2))
+    assert b16 < i16 < f32
+
+
+@pytest.mark.parametrize("bad,code", [
+    (dict(ndim=4), -1), (dict(order=6), -1), (dict(ny=3), -1), (dict(nz=8), -1),
+    (dict(nshot=0), -1), (dict(nt=0), -1), (dict(dt=0.0), -1), (dict(dx=-1.0), -1),
+    (dict(ckpt_format=3), -1), (dict(ckpt_every=-1), -1),
+    (dict(vmax=1e6), -4),
+])
+def test_invalid_problems_rejected(bad, code):
+    from neuralmech_gb300 import _lib
+    rc, _ = _ws(_problem(**bad))
+    assert rc == code
+    assert _lib.load().wfd_last_error().decode()
+
+
+def test_cfl_bound_matches_stable_dt():
+    from neuralmech_gb300 import stable_dt
+    dt = stable_dt((10.0, 10.0), 3000.0, 8)
+    assert abs(dt * 3000.0 / 10.0 - 0.5547) < 1e-3
+    assert _ws(_problem(dt=dt * 0.999))[0] == 0
+    assert _ws(_problem(dt=dt * 1.01))[0] == -4
+    dt3 = stable_dt((10.0, 10.0, 10.0), 3000.0, 8)
+    assert abs(dt3 * 3000.0 / 10.0 - 0.4529) < 1e-3
+
+
+def test_null_workspace_and_arguments_rejected():
+    from neuralmech_gb300 import _lib
+    lib = _lib.load()
+    p = _problem()
+    assert lib.wfd_forward(ctypes.byref(p), None, None, None, None, None, None, None, None, 0,
+                           None, 0, None) == -1
+    assert lib.wfd_status(None, None) == -2
+    assert lib.wfd_step2d_order2(None, None, None, 1.0, 1.0, 1.0, 1.0, 10, 10, 12, None) == -1
+    # misaligned row pitch for the TMA path (M_padded % 4 != 0) is refused before any launch
+    buf = ctypes.create_string_buffer(4096 + 16)
+    a = ctypes.c_void_p((ctypes.addressof(buf) + 15) // 16 * 16)
+    assert lib.wfd_step2d_order2(a, a, a, 1.0, 1.0, 1.0, 1.0, 10, 10, 13, None) == -1

@@ -1,0 +1,76 @@
+"""CPU tests of the Python host layer: argument shaping, sponge profiles, the
+synthetic workload generators, and the refusal of CPU tensors (there is no
+CPU path)."""
+import numpy as np
+import pytest
+import torch
+
+
+def test_positions_and_wavelet_broadcast():
+    from neuralmech_gb300.wavefd import _positions, _wavelet
+    p = _positions(np.array([[3, 7], [4, 9]]), 3, 2, "cpu")
+    assert p.shape == (3, 2, 3) and p.dtype == torch.int32
+    assert p[2, 1].tolist() == [4, 0, 9]
+    p3 = _positions(np.zeros((2, 5, 3)), 2, 3, "cpu")
+    assert p3.shape == (2, 5, 3)
+    with pytest.raises(ValueError):
+        _positions(np.zeros((2, 5, 2)), 3, 2, "cpu")
+    w = _wavelet(np.arange(10.0), 4, 10, 2, "cpu")
+    assert w.shape == (4, 10, 2) and float(w[3, 7, 1]) == 7.0
+    w2 = _wavelet(np.ones((4, 10)), 4, 10, 3, "cpu")
+    assert w2.shape == (4, 10, 3)
+    with pytest.raises(ValueError):
+        _wavelet(np.ones(9), 4, 10, 2, "cpu")
+
+
+def test_sponge_profile():
+    from neuralmech_gb300 import sponge_profile
+    g = sponge_profile(100, 20, 10, 0.3)
+    assert g.dtype == np.float32
+    assert np.all(g[20:90] == 1.0)
+    assert np.isclose(g[0], np.exp(-0.09)) and np.isclose(g[99], np.exp(-0.09))
+    assert np.all(np.diff(g[:21]) > 0) and np.all(np.diff(g[89:]) < 0)
+    assert np.all(sponge_profile(50, 0, 0) == 1.0)
+
+
+def test_grid_sponge_widths():
+    from neuralmech_gb300 import Grid, sponge_profiles
+    g = Grid((40, 60), (10.0, 10.0), 1e-3, 10, sponge=[(0, 8), (5, 5)])
+    gz, gy, gx = sponge_profiles(g)
+    assert gy is None and gz[0] == 1.0 and gz[-1] < 1.0 and gx[0] < 1.0
+    g0 = Grid((40, 60), (10.0, 10.0), 1e-3, 10, sponge=0)
+    assert all(p is None for p in sponge_profiles(g0))
+    with pytest.raises(ValueError):
+        Grid((40, 60), (10.0, 10.0), 1e-3, 10, sponge=[(1, 1)]).sponge_widths()
+
+
+def test_cpu_tensors_refused():
+    from neuralmech_gb300 import Grid, wave_forward
+    g = Grid((40, 60), (10.0, 10.0), 1e-3, 10)
+    with pytest.raises(ValueError, match="CUDA"):
+        wave_forward(torch.ones(40, 60), torch.zeros(10), [[10, 10]], [[10, 20]], g)
+
+
+def test_synthetic_workloads():
+    from neuralmech_gb300 import stable_dt
+    from neuralmech_gb300.synth import workload
+    w = workload("fwd256")
+    assert w.vel.shape == (256, 256) and w.src.shape == (1, 1, 2) and w.rec.shape == (1, 256, 2)
+    assert w.src[0, 0].tolist() == [5, 128]
+    assert set(np.unique(np.round(w.vel[[0, 100, 200], 5], -2))) <= {1400.0, 1500, 1600, 2300, 2400,
+                                                                     2500, 2600, 2700, 3200, 3300,
+                                                                     3400, 3500, 3600, 3700, 3800}
+    assert np.isclose(w.grid.dt * w.vel.max() / 10.0, 0.5)
+    assert w.grid.dt < stable_dt((10.0, 10.0), float(w.vel.max()), 8)
+    w2 = workload("fwd256")
+    assert np.array_equal(w.vel, w2.vel)  # seeded
+    f = workload("fwi1024", scale=0.125)
+    assert f.vel.shape == (128, 128) and f.vel_true is not None and f.src.shape[0] == 64
+    assert not np.array_equal(f.vel, f.vel_true)
+    d3 = workload("fwi384_3d", scale=0.1)
+    assert d3.vel.ndim == 3 and d3.src.shape[-1] == 3
+    assert np.isclose(d3.grid.dt * float(max(d3.vel.max(), d3.vel_true.max())) / 10.0, 0.45)
+    b = workload("batch8")
+    assert len(b) == 8 and sum(x.nshot for x in b) == 128
+    assert all(512 <= x.vel.shape[0] <= 1536 and x.vel.shape[0] % 64 == 0 for x in b)
+    assert all(1000 <= x.grid.nt <= 3000 for x in b)

@@ -1,0 +1,198 @@
+"""CPU tests of the oracle: pinned against the reference's own kernels
+(golden vectors from oracle/_ref, i.e. step2D_wave.cu / step1D_wave.cu compiled
+for the CPU), cross-checked with the NumPy slice-form restatement, and its
+adjoint gradient checked against finite differences in FP64."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, rel_l2
+
+
+def test_fd_weights_taylor(orc):
+    """Order-2R weights are exact on polynomials up to degree 2R+1."""
+    for order in (2, 4, 6, 8):
+        a = orc.fd_coeffs(order)
+        R = order // 2
+        for deg in range(0, 2 * R + 2):
+            # second derivative of x^deg at 0 from samples at k = -R..R (h = 1)
+            f = lambda k: float(k) ** deg
+            d2 = a[0] * f(0) + sum(a[k] * (f(k) + f(-k)) for k in range(1, R + 1))
+            exact = 2.0 if deg == 2 else 0.0
+            assert abs(d2 - exact) < 1e-9, (order, deg)
+        # residual of the first neglected term is nonzero
+        f = lambda k: float(k) ** (2 * R + 2)
+        assert abs(a[0] * f(0) + sum(a[k] * (f(k) + f(-k)) for k in range(1, R + 1))) > 1e-3
+    a8 = orc.fd_coeffs(8)
+    assert abs(abs(a8[0]) + 2 * np.abs(a8[1:]).sum() - 6.5016) < 1e-4
+
+
+def test_oracle_pinned_to_padded_step(orc):
+    """The FP64 oracle in order-2, constant-speed, Dirichlet form reproduces the
+    reference kernel padded_step (golden vectors) over several steps."""
+    g = np.load(os.path.join(GOLDEN, "padded_step.npz"))
+    for ci in range(2):
+        N, M, MP, steps, c, dt, dx, dy = g[f"c{ci}_params"]
+        N, M, steps = int(N), int(M), int(steps)
+        a = g[f"c{ci}_u0"][:, :M].astype(np.float64)
+        b = g[f"c{ci}_u1"][:, :M].astype(np.float64)
+        f32 = lambda x: float(np.float32(x))
+        w = (f32(c) * f32(dt)) ** 2
+        for t in range(steps):
+            orc.step(2, (f32(dx), 1.0, f32(dy)), a, b, a, w_const=w)
+            a, b = b, a
+            key = f"c{ci}_step{t}"
+            if key in g:
+                assert rel_l2(b, g[key][:, :M]) < 1e-5, (ci, t)
+
+
+def test_numpy_fd_step_is_reference_bitwise():
+    """The NumPy restatement of 2D_wave_cupy.py:54-62 equals padded_step's
+    host build bit for bit on the first step (same operation order, FP32)."""
+    from oracle import numpy_ref
+    g = np.load(os.path.join(GOLDEN, "padded_step.npz"))
+    N, M, MP, steps, c, dt, dx, dy = g["c0_params"]
+    M = int(M)
+    u0 = g["c0_u0"][:, :M].copy()
+    u1 = g["c0_u1"][:, :M].copy()
+    u2 = u0.copy()
+    numpy_ref.fd_step_order2(u0, u1, u2, np.float32(dt), np.float32(dx), np.float32(dy), np.float32(c))
+    assert rel_l2(u2, g["c0_step0"][:, :M]) < 1e-6
+
+
+def test_step1d_golden_vs_oracle(orc):
+    """step1D (step1D_wave.cu:4-17) as the 1-row special case of the oracle."""
+    g = np.load(os.path.join(GOLDEN, "step1d.npz"))
+    N, c, dt, dx = g["params"]
+    N = int(N)
+    # embed the 1D line as the middle row of a 3-row grid with no z coupling
+    f32 = lambda x: float(np.float32(x))
+    a = g["u0"].astype(np.float64)[None, :].repeat(3, 0)
+    b = a.copy()
+    for t in range(25):
+        n = a.copy()
+        orc.step(2, (1e30, 1.0, f32(dx)), a, b, n, w_const=(f32(c) * f32(dt)) ** 2)
+        n[0] = n[1]
+        n[2] = n[1]
+        a, b = b, n
+        if f"step{t}" in g:
+            assert rel_l2(b[1], g[f"step{t}"]) < 1e-5
+
+
+def test_mixed_step_golden_close_to_fp32(orc):
+    """mixed_step (FP16 storage) stays within FP16 accuracy of the FP32 path."""
+    g = np.load(os.path.join(GOLDEN, "mixed_step.npz"))
+    p = np.load(os.path.join(GOLDEN, "padded_step.npz"))
+    N, M, MP, steps, c, dt, dx, dy = g["c0_params"]
+    M, steps = int(M), int(steps)
+    last = f"c0_step{steps - 1}"
+    assert rel_l2(g[last][:, :M].astype(np.float32), p[last][:, :M]) < 2e-2
+
+
+def test_numpy_generic_matches_oracle_3d(orc):
+    from oracle import numpy_ref
+    rng = np.random.default_rng(0)
+    u = [rng.standard_normal((20, 21, 22)) for _ in range(2)]
+    w = rng.uniform(0.05, 0.2, (20, 21, 22))
+    gz, gy, gx = (rng.uniform(0.8, 1, n) for n in (20, 21, 22))
+    G = gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
+    a = u[0].copy()
+    numpy_ref.fd_step(u[0], u[1], a, w, (1.0, 1.1, 0.9), order=8, g=G)
+    b = u[0].copy()
+    orc.step(8, (1.0, 1.1, 0.9), u[0], u[1], b, w=w, sponge=(gz, gy, gx))
+    assert rel_l2(a, b) < 1e-14
+
+
+def _tiny(orc, order=8, ndim=2, nshot=2, nt=70, seed=0, ckpt=0):
+    from helpers import oracle_geometry, small_problem
+    shape = (36, 52) if ndim == 2 else (20, 22, 24)
+    grid, v, wav, src, rec = small_problem(shape=shape, nshot=nshot, nt=nt, order=order, sponge=6,
+                                           seed=seed, ckpt_every=ckpt, nrec=9)
+    geo = oracle_geometry(orc, grid, v.astype(np.float64), wav, src, rec)
+    rng = np.random.default_rng(seed + 1)
+    vt = v * (1 + 0.03 * rng.standard_normal(v.shape))
+    geo_t = oracle_geometry(orc, grid, vt, wav, src, rec)
+    obs = orc.forward(geo_t)
+    return geo, obs
+
+
+@pytest.mark.parametrize("order,ndim,ckpt", [(8, 2, 0), (2, 2, 7), (4, 3, 5)])
+def test_oracle_gradient_finite_differences(orc, order, ndim, ckpt):
+    """The oracle's adjoint gradient vs central differences of its own FP64
+    misfit (validates the adjoint derivation independently of the GPU)."""
+    geo, obs = _tiny(orc, order=order, ndim=ndim, ckpt=ckpt, nt=60 if ndim == 2 else 40)
+    J, g, gw, _ = orc.gradient(geo, obs)
+    rng = np.random.default_rng(3)
+    v0 = geo.vel.copy()
+    for _ in range(3):
+        d = rng.standard_normal(v0.shape)
+        d *= 1e-4 * np.abs(v0).mean() / np.abs(d).max()
+        Js = []
+        for sgn in (1, -1):
+            geo.vel = v0 + sgn * d
+            Js.append(0.5 * ((orc.forward(geo) - obs) ** 2).sum())
+        fd = (Js[0] - Js[1]) / 2
+        an = float((g * d).sum())
+        assert abs(fd - an) <= 1e-6 * abs(fd) + 1e-30, (fd, an)
+    geo.vel = v0
+    # wavelet gradient: the misfit is quadratic in the wavelet
+    dw = rng.standard_normal(geo.wavelet.shape) * 1e-3
+    w0 = geo.wavelet.copy()
+    Js = []
+    for sgn in (1, -1):
+        geo.wavelet = w0 + sgn * dw
+        Js.append(0.5 * ((orc.forward(geo) - obs) ** 2).sum())
+    geo.wavelet = w0
+    fd = (Js[0] - Js[1]) / 2
+    assert abs(fd - float((gw * dw).sum())) <= 1e-8 * abs(fd)
+
+
+def test_oracle_checkpoint_interval_invariance(orc):
+    geo, obs = _tiny(orc, nt=50)
+    res = []
+    for k in (1, 7, 50, 0):
+        geo.ckpt_every = k
+        res.append(orc.gradient(geo, obs)[1])
+    for r in res[1:]:
+        assert rel_l2(r, res[0]) < 1e-13
+
+
+def test_oracle_homogeneous_greens_function(orc):
+    """Known answer: in a homogeneous 2D medium, far from the source and before
+    any boundary reflection, the trace is the 2D Green's function of
+    u_tt - c^2 Lap u = delta(x) delta(t), G = H(t - r/c) / (2 pi c^2 sqrt(t^2 - r^2/c^2)),
+    convolved with the injected wavelet.
+    With u_tt = c^2 Lap u + f, a discrete source adds w_n * dt^2 / h^2 per step.
+    """
+    from neuralmech_gb300.synth import ricker
+    n, h, c = 401, 5.0, 2000.0
+    dt = 0.4 * h / c
+    nt = 300
+    f = 20.0
+    wav = ricker(f, nt, dt).astype(np.float64)
+    sz, sx = 200, 200
+    r_cells = 60
+    geo = orc.Geometry(vel=np.full((n, n), c), wavelet=wav[None, :, None],
+                       src=np.array([[[sz, 0, sx]]], dtype=np.int32),
+                       rec=np.array([[[sz, 0, sx + r_cells]]], dtype=np.int32), dt=dt,
+                       h=(h, 1.0, h), order=8, sponge=None, src_scale=dt * dt / (h * h))
+    tr = orc.forward(geo)[0, :, 0]
+    # trace_n = u(t_{n+1}); u(t) = 1/(2 pi c^2) int_0^acosh(ct/r) w(t - (r/c) cosh s) ds
+    # (tau = (r/c) cosh s removes the 1/sqrt singularity of G)
+    r = r_cells * h
+    t = (np.arange(nt) + 1) * dt
+    t0 = 1.5 / f
+
+    def w(tt):
+        a = (math.pi * f * (tt - t0)) ** 2
+        return np.where(tt >= 0, (1 - 2 * a) * np.exp(-a), 0.0)
+
+    ana = np.zeros(nt)
+    for i, ti in enumerate(t):
+        if ti * c > r:
+            s = np.linspace(0.0, math.acosh(ti * c / r), 4001)
+            ana[i] = np.trapezoid(w(ti - (r / c) * np.cosh(s)), s) / (2 * math.pi * c * c)
+    win = (t > r / c) & (t < r / c + t0 + 2 / f)
+    assert rel_l2(tr[win], ana[win]) < 0.05

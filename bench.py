@@ -1,0 +1,404 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 wave path: the batched FWI gradient.
+
+One step = one misfit gradient (forward with checkpoints + checkpointed
+adjoint) of the fwi1024 workload: 1024 x 1024 grid, 2000 time steps, 64 shots
+along the surface in one batched call, 1024 receivers, order 8 + 20-cell
+sponge, checkpoints every 45 steps (BF16), seeded synthetic layered + anomaly
+models (no dataset exists for this path).
+
+Metric: counted cell-updates per second, forward + adjoint: 2 x shots x
+interior cells x steps per gradient (recomputed forward steps are not
+counted). Algorithmic bytes: 16 B per forward update, 20 B per adjoint update
+(16 B + the stored L u read for the imaging term), i.e. 36 B per (cell, step)
+pair; "% HBM" = those bytes / time / measured HBM copy bandwidth.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU (torchrun, one process per GPU): every rank runs the full 64-shot
+gradient of its own shot set (weak scaling) and the gradients and misfits are
+summed with one all-reduce per step.
+
+--impl reference times the reference's CPU path for this workload on the host
+cores: the FP64 C++/OpenMP restatement in oracle/ (the reference's own solver
+package is not installable here and its in-tree kernels are GPU-only), on a
+bounded sample of each step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_PATH = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "Gcell-updates/s fwd+adj (% HBM peak); FWI grad shots/s batched vs plain, 1 GPU"
+UNIT = "Gcell-updates/s"
+# algorithmic bytes per cell-update, per kernel phase
+ALG_BYTES = {"forward": 16.0, "recompute": 20.0, "adjoint": 20.0}
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink grid and steps (testing only)")
+    ap.add_argument("--plain-shots", type=int, default=4)
+    ap.add_argument("--cpu-sample-steps", type=int, default=200)
+    ap.add_argument("--no-extras", action="store_true", help="skip e2e, plain and CPU legs")
+    ap.add_argument("--once", action="store_true",
+                    help="run one gradient and exit (the command profiled by ncu)")
+    ap.add_argument("--nt", type=int, default=0, help="override the number of time steps (profiling)")
+    ap.add_argument("--shots", type=int, default=0, help="use the first N shots (profiling)")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_per_update():
+    """ncu DRAM bytes per cell-update per phase kernel (profiles/dram_traffic.txt)."""
+    out = {}
+    try:
+        with open(TRAFFIC_PATH) as f:
+            for line in f:
+                line = line.split("#", 1)[0].strip()
+                if "=" in line:
+                    k, v = (x.strip() for x in line.split("=", 1))
+                    out[k] = float(v)
+    except OSError:
+        pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(scale: float, nt: int = 0, shots: int = 0):
+    from neuralmech_gb300 import Grid
+    from neuralmech_gb300.synth import workload as wl
+    w = wl("fwi1024", scale=scale)
+    if nt:
+        g = w.grid
+        w.grid = Grid(g.shape, g.spacing, g.dt, nt, order=g.order, sponge=g.sponge,
+                      ckpt_every=min(g.ckpt_every, nt), ckpt_format=g.ckpt_format)
+        w.wavelet = w.wavelet[:nt].copy()
+    if shots:
+        w.src, w.rec = w.src[:shots].copy(), w.rec[:shots].copy()
+    return w
+
+
+def counted_updates(w) -> float:
+    R = w.grid.order // 2
+    interior = int(np.prod([n - 2 * R for n in w.grid.shape]))
+    return 2.0 * w.nshot * interior * w.grid.nt, interior
+
+
+def cpu_gradient_sample(w, steps: int, nshot: int = 1):
+    """FP64 oracle gradient of the first `nshot` shots over `steps` time steps
+    of the workload's grid: (counted updates, seconds, description)."""
+    import oracle
+    from neuralmech_gb300 import Grid, sponge_profiles
+    oracle.build()
+    g = w.grid
+    sub = Grid(g.shape, g.spacing, g.dt, steps, order=g.order, sponge=g.sponge,
+               ckpt_every=min(g.ckpt_every or 45, steps))
+    gz, _, gx = sponge_profiles(sub)
+    p3 = lambda p: np.stack([p[..., 0], 0 * p[..., 0], p[..., 1]], -1).astype(np.int32)
+    wav = np.broadcast_to(w.wavelet[:steps], (nshot, steps)).astype(np.float64)[:, :, None].copy()
+    geo = oracle.Geometry(vel=w.vel.astype(np.float64), wavelet=wav, src=p3(w.src[:nshot]),
+                          rec=p3(w.rec[:nshot]), dt=float(np.float32(g.dt)),
+                          h=(g.spacing[0], 1.0, g.spacing[1]), order=g.order,
+                          sponge=(gz.astype(np.float64), None, gx.astype(np.float64)),
+                          ckpt_every=sub.ckpt_every)
+    obs = np.zeros((nshot, steps, w.rec.shape[1]))
+    t0 = time.perf_counter()
+    oracle.gradient(geo, obs)
+    dt = time.perf_counter() - t0
+    R = g.order // 2
+    interior = int(np.prod([n - 2 * R for n in g.shape]))
+    desc = (f"FP64 C++/OpenMP oracle gradient (forward + checkpointed adjoint), {nshot} shot, "
+            f"{g.shape[0]}x{g.shape[1]} grid, {steps} of {g.nt} steps")
+    return 2.0 * nshot * interior * steps, dt, desc
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    w = workload(args.scale, args.nt, args.shots)
+    cores = os.cpu_count()
+    steps = max(10, int(args.cpu_sample_steps * args.scale)) if args.scale < 1 else args.cpu_sample_steps
+    for _ in range(args.warmup):
+        cpu_gradient_sample(w, steps)
+    tot_u, tot_t, desc = 0.0, 0.0, ""
+    for _ in range(args.steps):
+        u, t, desc = cpu_gradient_sample(w, steps)
+        tot_u += u
+        tot_t += t
+    value = tot_u / tot_t / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_t / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config_of(w, args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": desc + " per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_of(w, args):
+    g = w.grid
+    return {"workload": (f"fwi1024: 2D FWI gradient, {g.shape[0]}x{g.shape[1]}, {g.nt} steps, "
+                         f"{w.nshot} shots in one batched call, {w.rec.shape[1]} receivers, order {g.order}, "
+                         f"20-cell sponge, checkpoints every {g.ckpt_every} ({g.ckpt_format})"),
+            "grid": list(g.shape), "nt": g.nt, "nshot": w.nshot, "nrec": int(w.rec.shape[1]),
+            "ckpt_every": g.ckpt_every, "ckpt_format": g.ckpt_format, "order": g.order,
+            "l2": "inputs larger than L2 (multi-GB state and checkpoints per step)",
+            "parallelism": f"{args.gpus} GPU(s), shots batched per GPU, gradient all-reduce"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+
+    from neuralmech_gb300 import _lib, misfit_gradient, wave_forward
+    from neuralmech_gb300.wavefd import Grid
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+    lib = _lib.load()
+
+    w = workload(args.scale, args.nt, args.shots)
+    g = w.grid
+    vel = torch.from_numpy(w.vel).to(dev)
+    wav = torch.from_numpy(w.wavelet).to(dev)
+    src = torch.from_numpy(w.src)
+    rec = torch.from_numpy(w.rec)
+    observed = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, g)
+
+    def step():
+        J, grad = misfit_gradient(vel, wav, src, rec, observed, g, check=False)
+        if world > 1:
+            dist.all_reduce(grad)
+            dist.all_reduce(J)
+        return J, grad
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up; the first call also checks the device status word (bounded TMA
+    # waits, positions), the timed calls skip that synchronising read
+    misfit_gradient(vel, wav, src, rec, observed, g, check=True)
+    if args.once:
+        torch.cuda.synchronize()
+        return 0
+    for _ in range(max(args.warmup - 1, 0)):
+        step()
+    barrier()
+
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    launches0 = lib.wfd_kernel_launches()
+    _lib.check(lib.wfd_profile_begin(), "wfd_profile_begin")
+    barrier()
+    clocks.start()
+    e0.record(stream)
+    for _ in range(args.steps):
+        J, grad = step()
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    phases = _lib.PhaseTimes()
+    _lib.check(lib.wfd_profile_end(ctypes.byref(phases)), "wfd_profile_end")
+    launches = lib.wfd_kernel_launches() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    t = torch.tensor([ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t)
+    if not torch.isfinite(grad).all() or not np.isfinite(float(J)):
+        raise RuntimeError("non-finite gradient or misfit in the timed region")
+    misfit_gradient(vel, wav, src, rec, observed, g, check=True)  # status after the timed region
+
+    updates, interior = counted_updates(w)
+    value = updates * world / (ms / 1e3) / 1e9
+    hbm, peak_src = peaks()
+    alg_gbs = updates * 18.0 / (ms / 1e3) / 1e9  # 36 B per (cell, step) pair
+
+    # roofline of the dominant kernel (largest device-time phase)
+    names = ["forward", "recompute", "adjoint"]
+    share = {n: phases.ms[i] for i, n in enumerate(names)}
+    dom = max(share, key=share.get)
+    i = names.index(dom)
+    per_launch_ms = phases.ms[i] / max(1, phases.launches[i])
+    bytes_per_launch = ALG_BYTES[dom] * w.nshot * interior
+    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
+    tr = traffic_per_update().get(f"{dom}_bytes_per_cell_update")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": None if tr is None else tr * w.nshot * interior,
+                "kernel": f"step2d_kernel ({dom} phase)", "peak_source": peak_src,
+                "alg_bytes_per_launch": bytes_per_launch, "ms_per_launch": per_launch_ms}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered + Gaussian anomaly models)",
+        "config": config_of(w, args), "roofline": roofline, "clocks": clk, "gpu_launches": int(launches),
+        "shots_per_s": w.nshot * world / (ms / 1e3),
+        "hbm_alg_gbs": alg_gbs, "hbm_frac_measured": alg_gbs / hbm, "hbm_frac_8tbs": alg_gbs / 8000.0,
+        "phase_ms_per_step": {n: phases.ms[k] / args.steps for k, n in enumerate(names)},
+        "phase_share": {n: phases.ms[k] / max(1e-9, sum(phases.ms)) for k, n in enumerate(names)},
+    }
+
+    if not args.no_extras:
+        # end to end through the public API, host buffers, copies inside the timed region
+        host = {"vel": torch.from_numpy(w.vel).pin_memory(), "wav": torch.from_numpy(w.wavelet).pin_memory(),
+                "obs": observed.cpu().pin_memory()}
+        grad_h = torch.empty(g.shape, dtype=torch.float32).pin_memory()
+        J_h = torch.empty((), dtype=torch.float64).pin_memory()
+        h2d = sum(x.numel() * x.element_size() for x in host.values()) + src.numel() * 4 + rec.numel() * 4
+        d2h = grad_h.numel() * 4 + 8
+
+        def e2e_step():
+            v = host["vel"].to(dev, non_blocking=True)
+            wv = host["wav"].to(dev, non_blocking=True)
+            ob = host["obs"].to(dev, non_blocking=True)
+            J2, g2 = misfit_gradient(v, wv, src.to(dev, non_blocking=True), rec.to(dev, non_blocking=True),
+                                     ob, g, check=False)
+            if world > 1:
+                dist.all_reduce(g2)
+                dist.all_reduce(J2)
+            grad_h.copy_(g2, non_blocking=True)
+            J_h.copy_(J2, non_blocking=True)
+
+        e2e_step()
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        barrier()
+        ms_e2e = e0.elapsed_time(e1) / args.steps
+        t = torch.tensor([ms_e2e], device=dev)
+        if world > 1:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t)
+        line["e2e"] = {"value": updates * world / (ms_e2e / 1e3) / 1e9, "unit": UNIT,
+                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e}
+
+        # plain: one shot per call (per-shot forward/adjoint, one launch per step)
+        P = min(args.plain_shots, w.nshot)
+        gp = Grid(g.shape, g.spacing, g.dt, g.nt, order=g.order, sponge=g.sponge, ckpt_every=g.ckpt_every,
+                  ckpt_format=g.ckpt_format, shots_per_cta=1)
+        misfit_gradient(vel, wav, src[:1], rec[:1], observed[:1].contiguous(), gp, check=False)
+        barrier()
+        e0.record(stream)
+        for s in range(P):
+            misfit_gradient(vel, wav, src[s:s + 1], rec[s:s + 1], observed[s:s + 1].contiguous(), gp, check=False)
+        e1.record(stream)
+        barrier()
+        plain_sps = P / (e0.elapsed_time(e1) / 1e3)
+        line["plain_shots_per_s"] = plain_sps
+        line["batched_vs_plain"] = line["shots_per_s"] / world / plain_sps
+
+        if rank == 0 and world == 1:
+            steps = args.cpu_sample_steps if args.scale >= 1 else max(10, int(args.cpu_sample_steps * args.scale))
+            u, tcpu, desc = cpu_gradient_sample(w, steps)
+            line["cpu_baseline"] = {"value": u / tcpu / 1e9, "unit": UNIT, "cores": os.cpu_count(),
+                                    "kind": "port", "sample": desc}
+
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

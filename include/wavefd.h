@@ -129,6 +129,22 @@ int wfd_status(void* workspace, void* stream);
  * (gradient norms). */
 int wfd_sum_sq(const float* x, int64_t n, double* out, void* stream);
 
+/* Number of kernels this library has launched in this process (monotonic),
+ * for launch accounting by benchmarks. */
+uint64_t wfd_kernel_launches(void);
+
+/* Device time per phase of the calls made on this thread between
+ * wfd_profile_begin() and wfd_profile_end(): CUDA events are recorded on the
+ * call's stream around the forward time loop, each recomputed segment and each
+ * adjoint segment (NVTX ranges mark the same phases for external profilers).
+ * wfd_profile_end synchronises those events and sums them. */
+typedef struct wfd_phase_times {
+    double ms[3];        /* forward, recompute, adjoint */
+    int64_t launches[3]; /* step-kernel launches in each phase */
+} wfd_phase_times;
+int wfd_profile_begin(void);
+int wfd_profile_end(wfd_phase_times* out);
+
 /*
  * One order-2, constant-speed, Dirichlet step with the reference kernel's
  * exact signature and semantics: padded_step, projects/18_simple_wave_fd/

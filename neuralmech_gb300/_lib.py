@@ -26,7 +26,13 @@ WFD_ERR_STATE = -7
 EXPORTS = (
     "wfd_strerror", "wfd_last_error", "wfd_version", "wfd_workspace_bytes", "wfd_forward",
     "wfd_backward", "wfd_misfit_gradient", "wfd_status", "wfd_sum_sq", "wfd_step2d_order2",
+    "wfd_kernel_launches", "wfd_profile_begin", "wfd_profile_end",
 )
+
+
+class PhaseTimes(ctypes.Structure):
+    """Mirror of ``wfd_phase_times``: forward, recompute, adjoint."""
+    _fields_ = [("ms", ctypes.c_double * 3), ("launches", ctypes.c_int64 * 3)]
 
 
 class Problem(ctypes.Structure):
@@ -84,8 +90,12 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         lib.wfd_sum_sq.argtypes = [f, ctypes.c_int64, d, vp]
         lib.wfd_step2d_order2.argtypes = [f, f, f, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                           ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
+        lib.wfd_kernel_launches.argtypes = []
+        lib.wfd_kernel_launches.restype = ctypes.c_uint64
+        lib.wfd_profile_begin.argtypes = []
+        lib.wfd_profile_end.argtypes = [ctypes.POINTER(PhaseTimes)]
         for name in EXPORTS:
-            if name not in ("wfd_strerror", "wfd_last_error"):
+            if name not in ("wfd_strerror", "wfd_last_error", "wfd_kernel_launches"):
                 getattr(lib, name).restype = ctypes.c_int
         _lib = lib
         return lib

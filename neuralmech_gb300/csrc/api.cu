@@ -2,6 +2,9 @@
 // layout, TMA descriptors, and the time loops of the forward, the
 // checkpointed adjoint and the misfit gradient. Host code only; all device
 // work is in stencil2d.cu / stencil3d.cu / aux.cu.
+#include <nvtx3/nvToolsExt.h>
+
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -15,8 +18,56 @@
 using namespace wfd;
 
 namespace {
+std::atomic<uint64_t> g_launches{0};
+}
+
+void wfd::count_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+
+namespace {
 
 thread_local std::string g_last_error;
+
+// ------------------------------------------------------------------ phase timing
+enum Phase { PH_FORWARD = 0, PH_RECOMPUTE = 1, PH_ADJOINT = 2 };
+const char* const kPhaseName[3] = {"wfd forward", "wfd recompute", "wfd adjoint"};
+
+struct PhaseRecord {
+    int phase;
+    cudaEvent_t start, stop;
+    int launches;
+};
+thread_local bool g_profiling = false;
+thread_local std::vector<PhaseRecord> g_records;
+
+// Marks one phase: an NVTX range always, CUDA events on the stream while
+// profiling is on.
+class PhaseScope {
+   public:
+    PhaseScope(int phase, cudaStream_t s, int launches) : s_(s) {
+        nvtxRangePushA(kPhaseName[phase]);
+        if (g_profiling) {
+            rec_.phase = phase;
+            rec_.launches = launches;
+            if (cudaEventCreate(&rec_.start) == cudaSuccess &&
+                cudaEventCreate(&rec_.stop) == cudaSuccess) {
+                cudaEventRecord(rec_.start, s_);
+                active_ = true;
+            }
+        }
+    }
+    ~PhaseScope() {
+        if (active_) {
+            cudaEventRecord(rec_.stop, s_);
+            g_records.push_back(rec_);
+        }
+        nvtxRangePop();
+    }
+
+   private:
+    cudaStream_t s_;
+    PhaseRecord rec_{};
+    bool active_ = false;
+};
 
 int fail(int status, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
 int fail(int status, const char* fmt, ...) {
@@ -373,6 +424,7 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
     for (int b = 0; b < 2; ++b)
         if ((rc = st.map_pair(w.P[b], w.P[b], &mc[b], &mo[b]))) return rc;
     const long long n_all = (long long)p->nshot * g.cells;
+    PhaseScope scope(PH_FORWARD, s, p->nt);
     for (int n = 0; n < p->nt; ++n) {
         const int bc = n & 1, bn = (n + 1) & 1;
         if (save && n % g.K == 0) {
@@ -450,10 +502,14 @@ int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Wor
         return st.launch(mode, qc[bc], qo[bn], with_grad ? lm[slot] : qc[bc], a);
     };
 
-    if ((rc = adjoint_step(p->nt, false, 0))) return rc;
+    {
+        PhaseScope scope(PH_ADJOINT, s, 1);
+        if ((rc = adjoint_step(p->nt, false, 0))) return rc;
+    }
     for (int j = g.nseg - 1; j >= 0; --j) {
         const int k0 = j * g.K, k1 = std::min(p->nt, k0 + g.K);
         if (j != g.nseg - 1) {
+            PhaseScope scope(PH_RECOMPUTE, s, k1 - k0);
             const unsigned char* slot = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
             WFD_CUDA(launch_unpack(slot, w.P[(k0 + 1) & 1], n_all, p->ckpt_format, s));
             WFD_CUDA(launch_unpack(slot + L.ckpt_field_bytes, w.P[k0 & 1], n_all, p->ckpt_format, s));
@@ -471,6 +527,7 @@ int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Wor
                 if ((rc = st.launch(MODE_SAVE_LAP, pc[bc], po[bn], pc[bc], a))) return rc;
             }
         }
+        PhaseScope scope(PH_ADJOINT, s, k1 - std::max(k0, 1));
         for (int k = k1 - 1; k >= std::max(k0, 1); --k)
             if ((rc = adjoint_step(k, true, k - k0))) return rc;
     }
@@ -580,6 +637,37 @@ int wfd_status(void* workspace, void* stream) {
     if (h & DEV_ERR_BAD_POSITION)
         return fail(WFD_ERR_POSITION, "device: a source/receiver lies outside the interior");
     return WFD_OK;
+}
+
+uint64_t wfd_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int wfd_profile_begin(void) {
+    for (auto& r : g_records) {
+        cudaEventDestroy(r.start);
+        cudaEventDestroy(r.stop);
+    }
+    g_records.clear();
+    g_profiling = true;
+    return WFD_OK;
+}
+
+int wfd_profile_end(wfd_phase_times* out) {
+    g_profiling = false;
+    if (!out) return fail(WFD_ERR_INVALID, "out is NULL");
+    *out = wfd_phase_times{};
+    int rc = WFD_OK;
+    for (auto& r : g_records) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(r.stop) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, r.start, r.stop) != cudaSuccess)
+            rc = fail(WFD_ERR_CUDA, "phase event timing failed");
+        out->ms[r.phase] += ms;
+        out->launches[r.phase] += r.launches;
+        cudaEventDestroy(r.start);
+        cudaEventDestroy(r.stop);
+    }
+    g_records.clear();
+    return rc;
 }
 
 int wfd_sum_sq(const float* x, int64_t n, double* out, void* stream) {

@@ -213,6 +213,7 @@ int grid_for(long long n, int block = 256) {
 cudaError_t launch_vel_to_m(const float* vel, float* m, int nz, int ny, int nx, int ld,
                             float scale, cudaStream_t s) {
     vel_to_m_kernel<<<grid_for((long long)nz * ny * ld), 256, 0, s>>>(vel, m, nz, ny, nx, ld, scale);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -226,13 +227,18 @@ cudaError_t launch_build_lists(const int32_t* pos, int nshot, int np, int nz, in
     if (e != cudaSuccess) return e;
     const long long npts = (long long)nshot * np;
     const int blocks = int((npts + 255) / 256);
-    if (npts > 0)
+    if (npts > 0) {
         count_kernel<<<blocks, 256, 0, s>>>(pos, nshot, np, nz, ny, nx, R, tile_z, tile_y, tile_x,
                                             tiles_y, tiles_x, ntiles, counts, err);
+        count_launch();
+    }
     scan_kernel<<<1, 1024, 0, s>>>(counts, off, int(nkeys));
-    if (npts > 0)
+    count_launch();
+    if (npts > 0) {
         fill_kernel<<<blocks, 256, 0, s>>>(pos, nshot, np, nz, ny, nx, ld, R, tile_z, tile_y,
                                            tile_x, tiles_y, tiles_x, ntiles, counts, off, ent);
+        count_launch();
+    }
     return cudaGetLastError();
 }
 
@@ -243,6 +249,7 @@ cudaError_t launch_gather(const float* u, long long shot_stride, PointLists list
     const dim3 grid((np + 127) / 128, nshot);
     gather_kernel<<<grid, 128, 0, s>>>(u, shot_stride, lists.off, lists.ent, ntiles, np, m, scale,
                                        div_m, out, out_nt, out_t);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -257,9 +264,11 @@ cudaError_t launch_pack(const float* src, void* dst, long long n, int format, cu
         float* sc = reinterpret_cast<float*>(static_cast<unsigned char*>(dst) + (n * 2 + 15) / 16 * 16);
         pack_i16_kernel<<<grid_for(n / 4), 256, 0, s>>>(reinterpret_cast<const float4*>(src), q, sc,
                                                         n / 4);
+        count_launch();
     } else {
         pack_kernel<<<grid_for(n / 4), 256, 0, s>>>(reinterpret_cast<const float4*>(src), dst,
                                                     n / 4, format);
+        count_launch();
     }
     return cudaGetLastError();
 }
@@ -270,9 +279,11 @@ cudaError_t launch_unpack(const void* src, float* dst, long long n, int format, 
         const float* sc = reinterpret_cast<const float*>(static_cast<const unsigned char*>(src) +
                                                          (n * 2 + 15) / 16 * 16);
         unpack_i16_kernel<<<grid_for(n / 4), 256, 0, s>>>(q, sc, reinterpret_cast<float4*>(dst), n / 4);
+        count_launch();
     } else {
         unpack_kernel<<<grid_for(n / 4), 256, 0, s>>>(src, reinterpret_cast<float4*>(dst), n / 4,
                                                       format);
+        count_launch();
     }
     return cudaGetLastError();
 }
@@ -280,11 +291,13 @@ cudaError_t launch_unpack(const void* src, float* dst, long long n, int format, 
 cudaError_t launch_residual_misfit(const float* d, const float* obs, float* res, long long n,
                                    double* misfit, cudaStream_t s) {
     residual_misfit_kernel<<<grid_for(n), 256, 0, s>>>(d, obs, res, n, misfit);
+    count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_sum_sq(const float* x, long long n, double* out, cudaStream_t s) {
     sum_sq_kernel<<<grid_for(n), 256, 0, s>>>(x, n, out);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -292,6 +305,7 @@ cudaError_t launch_grad_finalize(const float* G, const float* vel, float* grad_v
                                  int ny, int nx, int ld, int R, cudaStream_t s) {
     grad_finalize_kernel<<<grid_for((long long)nz * ny * nx), 256, 0, s>>>(G, vel, grad_vel, nz,
                                                                          ny, nx, ld, R);
+    count_launch();
     return cudaGetLastError();
 }
 

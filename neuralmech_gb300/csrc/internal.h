@@ -97,6 +97,9 @@ cudaError_t launch_step3d(int R, int mode, const CUtensorMap& map_cur, const CUt
 size_t step3d_smem_bytes(int R, int mode);
 bool step3d_available();
 
+// Counts kernel launches (wfd_kernel_launches); every launcher calls it.
+void count_launch(int n = 1);
+
 // ---------------------------------------------------------------- helpers (aux.cu)
 cudaError_t launch_vel_to_m(const float* vel, float* m, int nz, int ny, int nx, int ld,
                             float scale, cudaStream_t s);

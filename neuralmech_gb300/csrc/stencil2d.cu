@@ -262,6 +262,7 @@ cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUte
     }
     const dim3 grid(a.tiles_x * a.tiles_z, (a.nshot + a.shots_per_cta - 1) / a.shots_per_cta);
     step2d_kernel<R, MODE><<<grid, T2_THREADS, L::BYTES, s>>>(mc, mo, ml, a);
+    count_launch();
     return cudaGetLastError();
 }
 

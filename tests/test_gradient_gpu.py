@@ -10,7 +10,8 @@ Tolerances (relative L2 unless stated):
   * wavelet gradient vs the oracle: 1e-4 (FP32 storage);
   * adjoint dot-product test <S w, y> = <w, S^T y>: 1e-5 relative difference;
   * central finite differences of the FP64 misfit along 8 seeded directions:
-    1e-3 relative difference of the directional derivative.
+    1e-3 relative difference of the directional derivative, plus 1e-4 |g||d|
+    for directions nearly orthogonal to the gradient.
 """
 import numpy as np
 import pytest
@@ -122,4 +123,6 @@ def test_gradient_finite_differences(cuda, orc):
             Js.append(0.5 * ((orc.forward(geo) - obs) ** 2).sum())
         fd = (Js[0] - Js[1]) / (2 * eps)
         an = float((g * d).sum())
-        assert abs(fd - an) / abs(fd) < 1e-3, (fd, an)
+        # relative to |fd|, and to |g||d| for directions nearly orthogonal to g
+        bound = 1e-3 * abs(fd) + 1e-4 * np.linalg.norm(g) * np.linalg.norm(d)
+        assert abs(fd - an) < bound, (fd, an)

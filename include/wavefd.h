@@ -120,6 +120,25 @@ int wfd_misfit_gradient(const wfd_problem* p, const float* vel, const float* spo
                         float* traces, float* grad_vel, float* grad_wavelet, double* misfit,
                         void* workspace, size_t workspace_bytes, void* stream);
 
+/*
+ * Allocation-free variant of wfd_forward (no checkpoints): the same forward,
+ * with its scratch in a 64 MiB array that the library holds on every device it
+ * is loaded on, for callers that cannot allocate device memory (a host
+ * framework that owns the device pool, a plugin that receives only input and
+ * output buffers, a loop that cannot take cudaMalloc's implicit
+ * synchronisation). No counterpart in the reference: an addition of this
+ * library. Problems whose forward scratch (wfd_workspace_bytes,
+ * with_gradient = 0) exceeds 64 MiB return WFD_ERR_WORKSPACE. The first call on
+ * a device looks up the array's device address with cudaGetSymbolAddress; make
+ * it before any stream capture. All calls share the array: calls that overlap
+ * on the GPU race, so serialise them; each call clears what must start at zero.
+ * Device-side errors of the last call are not reported by wfd_status (the
+ * status word lives in the static array); check positions on the host.
+ */
+int wfd_forward_static(const wfd_problem* p, const float* vel, const float* sponge_z,
+                       const float* sponge_y, const float* sponge_x, const float* wavelet,
+                       const int32_t* src, const int32_t* rec, float* traces, void* stream);
+
 /* Synchronises `stream`, returns the first device-side error recorded in the
  * workspace since the last call (WFD_ERR_TIMEOUT, WFD_ERR_POSITION) or 0, and
  * clears it. */

@@ -80,6 +80,12 @@ int fail(int status, const char* fmt, ...) {
     return status;
 }
 
+}  // namespace
+
+int wfd::set_error(int status, const char* message) { return fail(status, "%s", message); }
+
+namespace {
+
 #define WFD_CUDA(call)                                                                      \
     do {                                                                                    \
         cudaError_t e_ = (call);                                                            \

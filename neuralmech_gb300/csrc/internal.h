@@ -100,6 +100,9 @@ bool step3d_available();
 // Counts kernel launches (wfd_kernel_launches); every launcher calls it.
 void count_launch(int n = 1);
 
+// Records `message` as the calling thread's wfd_last_error() and returns status.
+int set_error(int status, const char* message);
+
 // ---------------------------------------------------------------- helpers (aux.cu)
 cudaError_t launch_vel_to_m(const float* vel, float* m, int nz, int ny, int nx, int ld,
                             float scale, cudaStream_t s);

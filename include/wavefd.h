@@ -52,6 +52,10 @@ typedef struct wfd_problem {
     int32_t ckpt_format;   /* checkpoint snapshots: WFD_CKPT_FP32, _BF16 or _I16 */
     int32_t lap_bf16;      /* 1: per-segment L u store in BF16, 0: FP32 */
     int32_t shots_per_cta; /* shots one CTA walks through per step; 0 = automatic */
+    int32_t group_shots;   /* run the shots in sequential groups of this many, all
+                              groups sharing one workspace sized for a group (forward
+                              without checkpoints and wfd_misfit_gradient only);
+                              0 = all shots at once */
     float dt;              /* time step */
     float dz, dy, dx;      /* grid spacing (dy ignored in 2D) */
     float src_scale;       /* factor on every injected wavelet sample */

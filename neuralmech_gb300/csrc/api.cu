@@ -183,13 +183,14 @@ int check_problem(const wfd_problem* p) {
         return fail(WFD_ERR_INVALID, "more than 2^31 cells per shot");
     if (p->nshot < 1 || p->nt < 1 || p->nsrc < 0 || p->nrec < 0)
         return fail(WFD_ERR_INVALID, "nshot, nt must be >= 1 and nsrc, nrec >= 0");
-    if (p->nshot > 65535 * 64) return fail(WFD_ERR_INVALID, "too many shots");
+    if (p->nshot > 65535 * 64 || (p->ndim == 3 && p->nshot > 65535))
+        return fail(WFD_ERR_INVALID, "too many shots");
     if (!(p->dt > 0) || !(p->dx > 0) || !(p->dz > 0) || (p->ndim == 3 && !(p->dy > 0)))
         return fail(WFD_ERR_INVALID, "dt and spacings must be positive");
     if (p->ckpt_format < WFD_CKPT_FP32 || p->ckpt_format > WFD_CKPT_I16)
         return fail(WFD_ERR_INVALID, "unknown checkpoint format %d", p->ckpt_format);
-    if (p->ckpt_every < 0 || p->shots_per_cta < 0)
-        return fail(WFD_ERR_INVALID, "ckpt_every and shots_per_cta must be >= 0");
+    if (p->ckpt_every < 0 || p->shots_per_cta < 0 || p->group_shots < 0)
+        return fail(WFD_ERR_INVALID, "ckpt_every, shots_per_cta and group_shots must be >= 0");
     if (p->vmax > 0) {
         double a[5];
         fd_weights(p->order, a);
@@ -224,7 +225,9 @@ Geom make_geom(const wfd_problem* p) {
     g.tiles_y = cdiv(g.ny, g.tile_y);
     g.tiles_x = cdiv(g.nx, g.tile_x);
     g.ntiles = g.tiles_z * g.tiles_y * g.tiles_x;
-    if (p->shots_per_cta > 0) {
+    if (g.ndim == 3) {
+        g.spc = 1;  // a 3D CTA marches one shot's column
+    } else if (p->shots_per_cta > 0) {
         g.spc = std::min(p->shots_per_cta, p->nshot);
     } else {
         // enough CTAs for ~6 waves of 2 resident CTAs on 152 SMs, otherwise
@@ -235,7 +238,7 @@ Geom make_geom(const wfd_problem* p) {
         while (2LL * s <= spc && 2 * s <= p->nshot) s *= 2;
         g.spc = s;
     }
-    while ((p->nshot + g.spc - 1) / g.spc > 65535) g.spc *= 2;
+    while (g.ndim == 2 && (p->nshot + g.spc - 1) / g.spc > 65535) g.spc *= 2;
     g.K = p->ckpt_every > 0 ? std::min(p->ckpt_every, p->nt)
                             : std::max(1, (int)std::ceil(std::sqrt((double)p->nt)));
     g.nseg = cdiv(p->nt, g.K);
@@ -342,6 +345,21 @@ struct Stepper {
     unsigned* err;
     const float* m;
     const float *gz, *gy, *gx;
+    CUtensorMap map_m{};  // 3D only: tiles of the model m
+
+    int init() {
+        if (g.ndim != 3) return WFD_OK;
+        EncodeTiled enc = encoder();
+        if (!enc) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+        const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+        const cuuint64_t strides[2] = {(cuuint64_t)g.ld * 4, (cuuint64_t)g.plane * 4};
+        const cuuint32_t box[3] = {T3_TX, T3_TY, 1}, estr[3] = {1, 1, 1};
+        CUresult r = enc(&map_m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(m), dims,
+                         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled (m) failed (%d)", (int)r);
+        return WFD_OK;
+    }
 
     StepArgs base(float* u_new) const {
         StepArgs a{};
@@ -389,7 +407,7 @@ struct Stepper {
     int launch(int mode, const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
                const StepArgs& a) const {
         cudaError_t e = g.ndim == 2 ? launch_step2d(g.R, mode, mc, mo, ml, a, s)
-                                    : launch_step3d(g.R, mode, mc, mo, ml, a, s);
+                                    : launch_step3d(g.R, mode, mc, mo, ml, map_m, a, s);
         if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "step launch failed: %s", cudaGetErrorString(e));
         return WFD_OK;
     }
@@ -405,9 +423,22 @@ int common_checks(const wfd_problem* p, const float* vel, const float* wavelet, 
     return WFD_OK;
 }
 
+// Shots per sequential group (all of them when group_shots is 0 or >= nshot).
+int group_size(const wfd_problem* p) {
+    return (p->group_shots > 0 && p->group_shots < p->nshot) ? p->group_shots : p->nshot;
+}
+
+// The problem restricted to shots [g0, g0 + count).
+wfd_problem group_problem(const wfd_problem* p, int g0) {
+    wfd_problem q = *p;
+    q.nshot = std::min(group_size(p), p->nshot - g0);
+    q.group_shots = 0;
+    return q;
+}
+
 int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
-          const int32_t* src, const int32_t* rec, cudaStream_t s) {
-    WFD_CUDA(cudaMemsetAsync(w.err, 0, sizeof(unsigned), s));  // fresh status word
+          const int32_t* src, const int32_t* rec, cudaStream_t s, bool clear_status = true) {
+    if (clear_status) WFD_CUDA(cudaMemsetAsync(w.err, 0, sizeof(unsigned), s));  // fresh status word
     WFD_CUDA(launch_vel_to_m(vel, w.m, g.nz, g.ny, g.nx, g.ld, p->dt / p->dx, s));
     WFD_CUDA(launch_build_lists(src, p->nshot, p->nsrc, g.nz, g.ny, g.nx, g.ld, g.R, g.tile_z,
                                 g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
@@ -463,13 +494,15 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
     return WFD_OK;
 }
 
+// Adjoint of one (group of) shots. zero_G starts a new gradient sum; finalize
+// turns the sum into dJ/dv (the last group of a grouped call).
 int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                  const Stepper& st, const float* wavelet, const float* dtraces, float* grad_vel,
-                 float* grad_wavelet, const float* vel) {
+                 float* grad_wavelet, const float* vel, bool zero_G = true, bool finalize = true) {
     cudaStream_t s = st.s;
     WFD_CUDA(cudaMemsetAsync(w.Q[0], 0, L.field_bytes, s));
     WFD_CUDA(cudaMemsetAsync(w.Q[1], 0, L.field_bytes, s));
-    WFD_CUDA(cudaMemsetAsync(w.G, 0, (size_t)g.cells * 4, s));
+    if (zero_G) WFD_CUDA(cudaMemsetAsync(w.G, 0, (size_t)g.cells * 4, s));
     int rc;
     CUtensorMap pc[2], po[2], qc[2], qo[2];
     for (int b = 0; b < 2; ++b) {
@@ -540,7 +573,7 @@ int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Wor
     if (grad_wavelet && p->nsrc > 0)  // q_1 at the sources -> d J / d w_0
         WFD_CUDA(launch_gather(w.Q[1], g.cells, w.src, g.ntiles, p->nshot, p->nsrc, w.m,
                                p->src_scale, 1, grad_wavelet, p->nt, 0, s));
-    WFD_CUDA(launch_grad_finalize(w.G, vel, grad_vel, g.nz, g.ny, g.nx, g.ld, g.R, s));
+    if (finalize) WFD_CUDA(launch_grad_finalize(w.G, vel, grad_vel, g.nz, g.ny, g.nx, g.ld, g.R, s));
     return WFD_OK;
 }
 
@@ -570,8 +603,9 @@ int wfd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes) 
     int rc = check_problem(p);
     if (rc) return rc;
     if (!bytes) return fail(WFD_ERR_INVALID, "bytes is NULL");
-    const Geom g = make_geom(p);
-    *bytes = make_layout(p, g, with_gradient != 0).total;
+    const wfd_problem q = group_problem(p, 0);  // the workspace serves one group at a time
+    const Geom g = make_geom(&q);
+    *bytes = make_layout(&q, g, with_gradient != 0).total;
     return WFD_OK;
 }
 
@@ -581,14 +615,28 @@ int wfd_forward(const wfd_problem* p, const float* vel, const float* sponge_z,
                 void* workspace, size_t workspace_bytes, void* stream) {
     int rc = common_checks(p, vel, wavelet, src, rec);
     if (rc) return rc;
-    const Geom g = make_geom(p);
-    const Layout L = make_layout(p, g, save_checkpoints != 0);
+    const int G = group_size(p);
+    if (save_checkpoints && G < p->nshot)
+        return fail(WFD_ERR_INVALID, "a checkpointed forward cannot be split into shot groups");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // one layout, sized for a full group, serves every group
+    const wfd_problem first = group_problem(p, 0);
+    const Layout L = make_layout(&first, make_geom(&first), save_checkpoints != 0);
     if ((rc = check_workspace(workspace, workspace_bytes, L.total))) return rc;
     const Work w = carve(workspace, L, save_checkpoints != 0);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if ((rc = setup(p, g, w, vel, src, rec, s))) return rc;
-    Stepper st{p, g, s, w.err, w.m, sponge_z, p->ndim == 3 ? sponge_y : nullptr, sponge_x};
-    return run_forward(p, g, L, w, st, wavelet, traces, save_checkpoints != 0);
+    for (int g0 = 0; g0 < p->nshot; g0 += G) {
+        const wfd_problem q = group_problem(p, g0);
+        const Geom g = make_geom(&q);
+        if ((rc = setup(&q, g, w, vel, src + 3L * g0 * p->nsrc, rec + 3L * g0 * p->nrec, s, g0 == 0)))
+            return rc;
+        Stepper st{&q, g, s, w.err, w.m, sponge_z, p->ndim == 3 ? sponge_y : nullptr, sponge_x};
+        if ((rc = st.init())) return rc;
+        if ((rc = run_forward(&q, g, L, w, st, wavelet + (long long)g0 * p->nt * p->nsrc,
+                              traces ? traces + (long long)g0 * p->nt * p->nrec : nullptr,
+                              save_checkpoints != 0)))
+            return rc;
+    }
+    return WFD_OK;
 }
 
 int wfd_backward(const wfd_problem* p, const float* vel, const float* sponge_z,
@@ -599,12 +647,15 @@ int wfd_backward(const wfd_problem* p, const float* vel, const float* sponge_z,
     if (rc) return rc;
     if (!grad_vel || (p->nrec > 0 && !dtraces))
         return fail(WFD_ERR_INVALID, "grad_vel/dtraces is NULL");
+    if (group_size(p) < p->nshot)
+        return fail(WFD_ERR_INVALID, "wfd_backward cannot be split into shot groups");
     const Geom g = make_geom(p);
     const Layout L = make_layout(p, g, true);
     if ((rc = check_workspace(workspace, workspace_bytes, L.total))) return rc;
     const Work w = carve(workspace, L, true);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     Stepper st{p, g, s, w.err, w.m, sponge_z, p->ndim == 3 ? sponge_y : nullptr, sponge_x};
+    if ((rc = st.init())) return rc;
     return run_backward(p, g, L, w, st, wavelet, dtraces, grad_vel, grad_wavelet, vel);
 }
 
@@ -617,19 +668,37 @@ int wfd_misfit_gradient(const wfd_problem* p, const float* vel, const float* spo
     if (rc) return rc;
     if (!grad_vel || !misfit || (p->nrec > 0 && !observed))
         return fail(WFD_ERR_INVALID, "grad_vel/misfit/observed is NULL");
-    const Geom g = make_geom(p);
-    const Layout L = make_layout(p, g, true);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    WFD_CUDA(cudaMemsetAsync(misfit, 0, sizeof(double), s));
+    const int G = group_size(p);
+    // one layout, sized for a full group, serves every group (the gradient
+    // accumulator keeps its address across groups)
+    const wfd_problem first = group_problem(p, 0);
+    const Layout L = make_layout(&first, make_geom(&first), true);
     if ((rc = check_workspace(workspace, workspace_bytes, L.total))) return rc;
     const Work w = carve(workspace, L, true);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if ((rc = setup(p, g, w, vel, src, rec, s))) return rc;
-    Stepper st{p, g, s, w.err, w.m, sponge_z, p->ndim == 3 ? sponge_y : nullptr, sponge_x};
-    float* d = traces ? traces : w.res;
-    if ((rc = run_forward(p, g, L, w, st, wavelet, d, true))) return rc;
-    const long long ntr = (long long)p->nshot * p->nt * p->nrec;
-    WFD_CUDA(cudaMemsetAsync(misfit, 0, sizeof(double), s));
-    if (ntr > 0) WFD_CUDA(launch_residual_misfit(d, observed, w.res, ntr, misfit, s));
-    return run_backward(p, g, L, w, st, wavelet, w.res, grad_vel, grad_wavelet, vel);
+    for (int g0 = 0; g0 < p->nshot; g0 += G) {
+        // one group: forward with checkpoints, residual, adjoint; the gradient
+        // and the misfit accumulate over the groups
+        const wfd_problem q = group_problem(p, g0);
+        const Geom g = make_geom(&q);
+        const int32_t* gsrc = src + 3L * g0 * p->nsrc;
+        const int32_t* grec = rec + 3L * g0 * p->nrec;
+        const float* gwav = wavelet + (long long)g0 * p->nt * p->nsrc;
+        const long long toff = (long long)g0 * p->nt * p->nrec;
+        if ((rc = setup(&q, g, w, vel, gsrc, grec, s, g0 == 0))) return rc;
+        Stepper st{&q, g, s, w.err, w.m, sponge_z, p->ndim == 3 ? sponge_y : nullptr, sponge_x};
+        if ((rc = st.init())) return rc;
+        float* d = traces ? traces + toff : w.res;
+        if ((rc = run_forward(&q, g, L, w, st, gwav, d, true))) return rc;
+        const long long ntr = (long long)q.nshot * q.nt * q.nrec;
+        if (ntr > 0) WFD_CUDA(launch_residual_misfit(d, observed + toff, w.res, ntr, misfit, s));
+        if ((rc = run_backward(&q, g, L, w, st, gwav, w.res, grad_vel,
+                               grad_wavelet ? grad_wavelet + (long long)g0 * p->nt * p->nsrc : nullptr,
+                               vel, g0 == 0, g0 + G >= p->nshot)))
+            return rc;
+    }
+    return WFD_OK;
 }
 
 int wfd_status(void* workspace, void* stream) {

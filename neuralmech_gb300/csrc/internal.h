@@ -82,18 +82,22 @@ cudaError_t launch_step2d(int R, int mode, const CUtensorMap& map_cur, const CUt
 size_t step2d_smem_bytes(int R, int mode);
 
 // ---------------------------------------------------------------- 3D tiles
-// One CTA marches along z through a (TY x TX) column of the grid, 4 x cells
-// per thread, a register queue of 2R+1 planes per cell.
+// One CTA (one shot) marches along z through a (TY x TX) column of the grid
+// for T3_ZCHUNK output planes; a thread owns 4 x cells and keeps the 2R + 1
+// z taps of each in registers.
 constexpr int T3_TX = 64;
 constexpr int T3_TY = 16;
 constexpr int T3_XH = 4;
 constexpr int T3_W = T3_TX + 2 * T3_XH;
 constexpr int T3_THREADS = (T3_TX / 4) * T3_TY;  // 256
 constexpr int T3_ZCHUNK = 64;                    // planes per CTA (z blocking)
-constexpr int T3_STAGES = 4;
 
+// map_cur: u_n planes (box T3_W x (T3_TY + 2R) x 1 x 1); map_old, map_lap:
+// output-plane tiles (box T3_TX x T3_TY x 1 x 1); map_m: the model m
+// ([z][y][ld], box T3_TX x T3_TY x 1).
 cudaError_t launch_step3d(int R, int mode, const CUtensorMap& map_cur, const CUtensorMap& map_old,
-                          const CUtensorMap& map_lap, const StepArgs& a, cudaStream_t s);
+                          const CUtensorMap& map_lap, const CUtensorMap& map_m, const StepArgs& a,
+                          cudaStream_t s);
 size_t step3d_smem_bytes(int R, int mode);
 bool step3d_available();
 

@@ -1,16 +1,311 @@
-// 3D time-step kernel of the acoustic wave path (sm_103a): not built yet.
+// 3D time-step kernel of the acoustic wave path (sm_103a).
+//
+// Same update as the 2D kernel,
+//   u_{n+1} = g (2 u_n + m L u_n) - g^2 u_{n-1},  g = gz[z] gy[y] gx[x],
+// on fields [shot][z][y][ld] FP32 (x fastest, ld a multiple of 8).
+//
+// Per CTA (256 threads = 16 lanes along x x 16 rows along y): one shot, one
+// 64 x 16 (x, y) column, marching along z through T3_ZCHUNK output planes.
+//   * u_n planes, each with a halo of R rows in y and 4 columns in x, arrive by
+//     TMA (cp.async.bulk.tensor.4d) into a ring of NB = 8 shared-memory
+//     buffers, four planes ahead of use. A thread keeps the 2R + 1 z-taps of
+//     its 4 cells in a register queue; the x and y taps come from the staged
+//     plane of the output z.
+//   * u_{n-1}, m and (MODE_GRAD) the stored L u of the output plane arrive by
+//     TMA into a ring of NBO = 4 buffers, four planes ahead.
+//   * All mbarrier waits are bounded (status bit on give-up, never a trap).
+//   * Point lists are bucketed by (z chunk, y tile, x tile). At each output
+//     plane the CTA samples receivers from the staged u_n plane, and after its
+//     stores injects into u_{n+1}.
+//   * MODE_SAVE_LAP stores L u_n; MODE_GRAD adds q_{k+1} L u_k into the
+//     gradient with 16-byte vector atomics.
 #include "common.cuh"
 #include "internal.h"
 
 namespace wfd {
+namespace {
 
-bool step3d_available() { return false; }
+__host__ __device__ constexpr int align3(int v, int a) { return (v + a - 1) / a * a; }
 
-cudaError_t launch_step3d(int, int, const CUtensorMap&, const CUtensorMap&, const CUtensorMap&,
-                          const StepArgs&, cudaStream_t) {
-    return cudaErrorNotSupported;
+constexpr int NB = 8;   // u_n plane ring
+constexpr int NBO = 4;  // u_{n-1} / m / L u plane ring
+constexpr int LANES_X = T3_TX / 4;  // 16
+
+template <int R, int MODE>
+struct Layout3D {
+    static constexpr int H = T3_TY + 2 * R;
+    static constexpr int CUR = H * T3_W * 4;  // TMA box bytes of one u_n plane
+    static constexpr int CUR_AL = align3(CUR, 128);
+    static constexpr int TILE = T3_TY * T3_TX * 4;  // one FP32 output-plane tile
+    static constexpr int OLD_GROUP = 2 * TILE + (MODE == MODE_GRAD ? TILE : 0);  // old, m, lap
+    static constexpr int BYTES = NB * CUR_AL + NBO * OLD_GROUP + (NB + NBO) * 8 + 128;
+};
+
+__device__ __forceinline__ float comp(const float4& v, int e) {
+    return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
 }
 
-size_t step3d_smem_bytes(int, int) { return 0; }
+template <int R, int MODE>
+__global__ void __launch_bounds__(T3_THREADS, 2)
+    step3d_kernel(const __grid_constant__ CUtensorMap map_cur,
+                  const __grid_constant__ CUtensorMap map_old,
+                  const __grid_constant__ CUtensorMap map_lap,
+                  const __grid_constant__ CUtensorMap map_m, const StepArgs a) {
+    using L = Layout3D<R, MODE>;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* base = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    unsigned char* cur_ring = base;
+    unsigned char* old_ring = base + NB * L::CUR_AL;
+    uint64_t* bc = reinterpret_cast<uint64_t*>(old_ring + NBO * L::OLD_GROUP);
+    uint64_t* bo = bc + NB;
+
+    const int tid = threadIdx.x, lane = tid % LANES_X, row = tid / LANES_X;
+    const int tile = blockIdx.x;
+    const int s = blockIdx.y;
+    const int ntiles = a.tiles_x * a.tiles_y * a.tiles_z;
+    const int tx_i = tile % a.tiles_x;
+    const int ty_i = (tile / a.tiles_x) % a.tiles_y;
+    const int tz_i = tile / (a.tiles_x * a.tiles_y);
+    const int x0 = tx_i * T3_TX, y0 = ty_i * T3_TY, z0 = tz_i * T3_ZCHUNK;
+    const int zc = min(T3_ZCHUNK, a.nz - z0);  // output planes of this CTA
+    const int total = zc + 2 * R;               // u_n planes it stages
+
+    const uint32_t lap_bytes = MODE == MODE_GRAD ? uint32_t(T3_TY * T3_TX * (a.lap_bf16 ? 2 : 4)) : 0u;
+    auto cur_buf = [&](int p) { return reinterpret_cast<float*>(cur_ring + (p % NB) * L::CUR_AL); };
+    auto old_buf = [&](int zr) { return reinterpret_cast<float*>(old_ring + (zr % NBO) * L::OLD_GROUP); };
+    auto m_buf = [&](int zr) { return reinterpret_cast<float*>(old_ring + (zr % NBO) * L::OLD_GROUP + L::TILE); };
+    auto lap_buf = [&](int zr) { return old_ring + (zr % NBO) * L::OLD_GROUP + 2 * L::TILE; };
+
+    // staged plane p holds u_n at z = z0 - R + p; old group zr holds output plane z0 + zr
+    auto issue_cur = [&](int p) {
+        uint64_t* bar = &bc[p % NB];
+        mbar_arrive_expect_tx(bar, uint32_t(L::CUR));
+        tma_load_4d(cur_buf(p), &map_cur, x0 - T3_XH, y0 - R, z0 - R + p, s, bar);
+    };
+    auto issue_old = [&](int zr) {
+        uint64_t* bar = &bo[zr % NBO];
+        mbar_arrive_expect_tx(bar, uint32_t(2 * L::TILE) + lap_bytes);
+        tma_load_4d(old_buf(zr), &map_old, x0, y0, z0 + zr, s, bar);
+        tma_load_3d(m_buf(zr), &map_m, x0, y0, z0 + zr, bar);
+        if (MODE == MODE_GRAD) tma_load_4d(lap_buf(zr), &map_lap, x0, y0, z0 + zr, s, bar);
+    };
+
+    if (tid == 0) {
+        for (int b = 0; b < NB; ++b) mbar_init(&bc[b], 1);
+        for (int b = 0; b < NBO; ++b) mbar_init(&bo[b], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int p = 0; p < min(NB, total); ++p) issue_cur(p);
+
+    // ---- per-thread constants
+    const int x = x0 + 4 * lane;
+    const int y = y0 + row;
+    float gxe[4];
+    bool xin[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        gxe[e] = (a.gx != nullptr && x + e < a.nx) ? __ldg(a.gx + x + e) : 1.f;
+        xin[e] = x + e >= R && x + e < a.nx - R;
+    }
+    const bool all_x = xin[0] && xin[1] && xin[2] && xin[3];
+    const bool yin = y >= R && y < a.ny - R;
+    const float gyv = (a.gy != nullptr && y < a.ny) ? __ldg(a.gy + y) : 1.f;
+    float* un = a.u_new + (long long)s * a.shot_stride;
+    const int col = T3_XH + 4 * lane;  // staged column of this thread's first cell
+
+    // ---- register queue of the z taps: V[j] = u_n at z = zout - R + j
+    float4 V[2 * R + 1];
+#pragma unroll
+    for (int p = 0; p < 2 * R; ++p) {
+        if (!mbar_wait(&bc[p % NB], (p / NB) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
+        V[p + 1] = *reinterpret_cast<const float4*>(cur_buf(p) + (row + R) * T3_W + col);
+    }
+    __syncthreads();  // planes 0 .. R-1 are consumed
+    if (tid == 0) {
+        for (int p = NB; p < min(NB + R, total); ++p) issue_cur(p);
+        for (int zr = 0; zr < min(NBO, zc); ++zr) issue_old(zr);
+    }
+
+    const int lo_s = a.smp.off ? a.smp.off[s * ntiles + tile] : 0;
+    const int hi_s = a.smp.off ? a.smp.off[s * ntiles + tile + 1] : 0;
+    const int lo_i = a.inj.off ? a.inj.off[s * ntiles + tile] : 0;
+    const int hi_i = a.inj.off ? a.inj.off[s * ntiles + tile + 1] : 0;
+
+    for (int zr = 0; zr < zc; ++zr) {
+        const int z = z0 + zr;
+        const int pn = zr + 2 * R;  // newest staged plane needed
+        if (!mbar_wait(&bc[pn % NB], (pn / NB) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
+#pragma unroll
+        for (int j = 0; j < 2 * R; ++j) V[j] = V[j + 1];
+        V[2 * R] = *reinterpret_cast<const float4*>(cur_buf(pn) + (row + R) * T3_W + col);
+        if (!mbar_wait(&bo[zr % NBO], (zr / NBO) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
+
+        const float* pl = cur_buf(zr + R);  // u_n at the output plane, with halo
+        const float* prow = pl + (row + R) * T3_W + 4 * lane;
+        const float4 lv = *reinterpret_cast<const float4*>(prow);
+        const float4 cv = V[R];
+        const float4 rv = *reinterpret_cast<const float4*>(prow + 2 * T3_XH);
+        const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y, cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
+        float4 ym[R], yp[R];
+#pragma unroll
+        for (int k = 1; k <= R; ++k) {
+            ym[k - 1] = *reinterpret_cast<const float4*>(pl + (row + R - k) * T3_W + col);
+            yp[k - 1] = *reinterpret_cast<const float4*>(pl + (row + R + k) * T3_W + col);
+        }
+        const int ti = row * T3_TX + 4 * lane;
+        const float4 ov = *reinterpret_cast<const float4*>(old_buf(zr) + ti);
+        const float4 mv = *reinterpret_cast<const float4*>(m_buf(zr) + ti);
+        const float gz = (a.gz != nullptr && z < a.nz) ? __ldg(a.gz + z) : 1.f;
+        float lap[4], nv[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            float acc = a.c0 * w[4 + e];
+#pragma unroll
+            for (int k = 1; k <= R; ++k) {
+                acc = fmaf(a.cx[k - 1], w[4 + e - k] + w[4 + e + k], acc);
+                acc = fmaf(a.cy[k - 1], comp(ym[k - 1], e) + comp(yp[k - 1], e), acc);
+                acc = fmaf(a.cz[k - 1], comp(V[R - k], e) + comp(V[R + k], e), acc);
+            }
+            lap[e] = acc;
+            const float g = gz * gyv * gxe[e];
+            nv[e] = g * fmaf(comp(mv, e), acc, 2.f * w[4 + e]) - (g * g) * comp(ov, e);
+        }
+        const bool rin = yin && z >= R && z < a.nz - R;
+        const long long off = (long long)z * a.plane + (long long)y * a.ld + x;
+        if (rin && all_x) {
+            *reinterpret_cast<float4*>(un + off) = make_float4(nv[0], nv[1], nv[2], nv[3]);
+        } else if (rin) {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (xin[e]) un[off + e] = nv[e];
+        }
+        if (MODE == MODE_SAVE_LAP && rin) {
+            const long long lo = (long long)s * a.shot_stride + off;
+            const float4 lp = make_float4(lap[0], lap[1], lap[2], lap[3]);
+            if (all_x) {
+                if (a.lap_bf16)
+                    *reinterpret_cast<uint2*>(static_cast<__nv_bfloat16*>(a.lap) + lo) = pack_bf16x4(lp);
+                else
+                    *reinterpret_cast<float4*>(static_cast<float*>(a.lap) + lo) = lp;
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (xin[e]) {
+                        if (a.lap_bf16)
+                            static_cast<__nv_bfloat16*>(a.lap)[lo + e] = __float2bfloat16_rn(lap[e]);
+                        else
+                            static_cast<float*>(a.lap)[lo + e] = lap[e];
+                    }
+            }
+        }
+        if (MODE == MODE_GRAD && rin) {
+            const unsigned char* lb = lap_buf(zr);
+            const float4 lu = a.lap_bf16
+                                  ? unpack_bf16x4(*reinterpret_cast<const uint2*>(
+                                        reinterpret_cast<const __nv_bfloat16*>(lb) + ti))
+                                  : *reinterpret_cast<const float4*>(reinterpret_cast<const float*>(lb) + ti);
+            float* gp = a.grad + off;
+            if (all_x) {
+                atomicAdd(reinterpret_cast<float4*>(gp),
+                          make_float4(cv.x * lu.x, cv.y * lu.y, cv.z * lu.z, cv.w * lu.w));
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (xin[e]) atomicAdd(gp + e, comp(cv, e) * comp(lu, e));
+            }
+        }
+        // sampling of u_n at this plane
+        for (int j = lo_s + tid; j < hi_s; j += T3_THREADS) {
+            const int2 en = a.smp.ent[j];
+            const int pz = en.x / int(a.plane);
+            if (pz != z) continue;
+            const int rem = en.x - pz * int(a.plane);
+            const int py = rem / a.ld, px = rem - py * a.ld;
+            float v = pl[(py - y0 + R) * T3_W + (px - x0 + T3_XH)] * a.smp_scale;
+            if (a.smp_div_m) v /= a.m[en.x];
+            a.smp_out[((long long)s * a.smp_nt + a.smp_t) * a.smp_np + en.y] = v;
+        }
+        __syncthreads();  // plane zr + R and old group zr fully read; stores of plane z done
+        if (tid == 0) {
+            fence_proxy_async_smem();
+            if (zr + NB + R < total) issue_cur(zr + NB + R);
+            if (zr + NBO < zc) issue_old(zr + NBO);
+        }
+        for (int j = lo_i + tid; j < hi_i; j += T3_THREADS) {
+            const int2 en = a.inj.ent[j];
+            const int pz = en.x / int(a.plane);
+            if (pz != z) continue;
+            const int rem = en.x - pz * int(a.plane);
+            const int py = rem / a.ld, px = rem - py * a.ld;
+            float v = a.inj_val[((long long)s * a.inj_nt + a.inj_t) * a.inj_np + en.y] * a.inj_scale;
+            if (a.inj_times_m) v *= a.m[en.x];
+            const float g = (a.gz ? a.gz[pz] : 1.f) * (a.gy ? a.gy[py] : 1.f) * (a.gx ? a.gx[px] : 1.f);
+            atomicAdd(un + en.x, g * v);
+        }
+    }
+}
+
+template <int R, int MODE>
+cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
+                        const CUtensorMap& mm, const StepArgs& a, cudaStream_t s) {
+    using L = Layout3D<R, MODE>;
+    static int configured_device = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (configured_device != dev) {
+        cudaError_t e = cudaFuncSetAttribute(step3d_kernel<R, MODE>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
+        if (e != cudaSuccess) return e;
+        configured_device = dev;
+    }
+    const dim3 grid(a.tiles_x * a.tiles_y * a.tiles_z, a.nshot);
+    step3d_kernel<R, MODE><<<grid, T3_THREADS, L::BYTES, s>>>(mc, mo, ml, mm, a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <int R>
+cudaError_t dispatch(int mode, const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
+                     const CUtensorMap& mm, const StepArgs& a, cudaStream_t s) {
+    switch (mode) {
+        case MODE_PLAIN: return launch_impl<R, MODE_PLAIN>(mc, mo, ml, mm, a, s);
+        case MODE_SAVE_LAP: return launch_impl<R, MODE_SAVE_LAP>(mc, mo, ml, mm, a, s);
+        case MODE_GRAD: return launch_impl<R, MODE_GRAD>(mc, mo, ml, mm, a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+bool step3d_available() { return true; }
+
+cudaError_t launch_step3d(int R, int mode, const CUtensorMap& mc, const CUtensorMap& mo,
+                          const CUtensorMap& ml, const CUtensorMap& mm, const StepArgs& a,
+                          cudaStream_t s) {
+    if (a.nshot > 65535) return cudaErrorInvalidValue;
+    switch (R) {
+        case 1: return dispatch<1>(mode, mc, mo, ml, mm, a, s);
+        case 2: return dispatch<2>(mode, mc, mo, ml, mm, a, s);
+        case 4: return dispatch<4>(mode, mc, mo, ml, mm, a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+size_t step3d_smem_bytes(int R, int mode) {
+    switch (R * 4 + mode) {
+        case 4 + MODE_PLAIN: return Layout3D<1, MODE_PLAIN>::BYTES;
+        case 4 + MODE_SAVE_LAP: return Layout3D<1, MODE_SAVE_LAP>::BYTES;
+        case 4 + MODE_GRAD: return Layout3D<1, MODE_GRAD>::BYTES;
+        case 8 + MODE_PLAIN: return Layout3D<2, MODE_PLAIN>::BYTES;
+        case 8 + MODE_SAVE_LAP: return Layout3D<2, MODE_SAVE_LAP>::BYTES;
+        case 8 + MODE_GRAD: return Layout3D<2, MODE_GRAD>::BYTES;
+        case 16 + MODE_PLAIN: return Layout3D<4, MODE_PLAIN>::BYTES;
+        case 16 + MODE_SAVE_LAP: return Layout3D<4, MODE_SAVE_LAP>::BYTES;
+        default: return Layout3D<4, MODE_GRAD>::BYTES;
+    }
+}
 
 }  // namespace wfd

@@ -54,6 +54,9 @@ class Grid:
              FP32 scale per 32 cells)
     lap_bf16     store the per-segment L u of the recomputed forward in BF16
     shots_per_cta  shots one CTA walks through per step (0 = automatic)
+    group_shots  run the shots of a misfit gradient (or of a forward without
+             autograd) in sequential groups of this many, sharing one workspace
+             sized for a group (0 = all at once)
     """
     shape: tuple
     spacing: tuple
@@ -67,6 +70,7 @@ class Grid:
     ckpt_format: str = "bf16"
     lap_bf16: bool = False
     shots_per_cta: int = 0
+    group_shots: int = 0
 
     @property
     def ndim(self) -> int:
@@ -136,7 +140,7 @@ def _problem(grid: Grid, nshot: int, nsrc: int, nrec: int, vmax: float) -> _lib.
         dz, dy, dx = grid.spacing
     return _lib.Problem(grid.ndim, grid.order, nz, ny, nx, nshot, grid.nt, nsrc, nrec,
                         grid.ckpt_every, CKPT_FORMATS[grid.ckpt_format], int(grid.lap_bf16),
-                        grid.shots_per_cta, grid.dt, dz, dy, dx, grid.src_scale, vmax)
+                        grid.shots_per_cta, grid.group_shots, grid.dt, dz, dy, dx, grid.src_scale, vmax)
 
 
 # ---------------------------------------------------------------- argument prep
@@ -237,6 +241,7 @@ class _WaveForward(torch.autograd.Function):
     @staticmethod
     def forward(ctx, vel, wavelet, call: _Call, check: bool):
         lib = _lib.load()
+        call.problem.group_shots = 0  # the checkpointed forward keeps every shot's state
         ws = _workspace(call, True)
         c = call
         traces = torch.empty((c.problem.nshot, c.problem.nt, c.problem.nrec),

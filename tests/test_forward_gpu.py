@@ -115,3 +115,19 @@ def test_forward_no_receivers_no_sources(cuda):
     out = wave_forward(torch.from_numpy(v).to(cuda), torch.zeros((2, 10, 0), device=cuda),
                        torch.zeros((2, 0, 2), dtype=torch.int32), torch.from_numpy(rec), grid)
     assert torch.count_nonzero(out) == 0
+
+
+@pytest.mark.parametrize("order", [2, 4, 8])
+@pytest.mark.parametrize("shape,nshot,sponge", [
+    ((70, 20, 72), 2, 5),     # two z chunks, two x tiles, two y tiles
+    ((30, 37, 41), 1, 0),     # odd sizes, one chunk
+])
+def test_forward_3d_matches_oracle(cuda, orc, order, shape, nshot, sponge):
+    from neuralmech_gb300 import wave_forward
+    grid, v, wav, src, rec = small_problem(shape=shape, nshot=nshot, order=order, sponge=sponge,
+                                           nt=50, nrec=25, seed=order + 7)
+    traces = wave_forward(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
+                          torch.from_numpy(src), torch.from_numpy(rec), grid)
+    ref = orc.forward(oracle_geometry(orc, grid, v, wav, src, rec))
+    assert np.abs(ref).max() > 0
+    assert rel_l2(traces.cpu().numpy(), ref) < 1e-5

@@ -126,3 +126,42 @@ def test_gradient_finite_differences(cuda, orc):
         # relative to |fd|, and to |g||d| for directions nearly orthogonal to g
         bound = 1e-3 * abs(fd) + 1e-4 * np.linalg.norm(g) * np.linalg.norm(d)
         assert abs(fd - an) < bound, (fd, an)
+
+
+@pytest.mark.parametrize("order,fmt,tol", [(8, "fp32", 1e-4), (4, "fp32", 1e-4), (8, "bf16", 5e-3)])
+def test_gradient_3d_matches_oracle(cuda, orc, order, fmt, tol):
+    from neuralmech_gb300 import misfit_gradient
+    grid, v, wav, src, rec = small_problem(shape=(68, 22, 70), nshot=2, nt=48, order=order, sponge=5,
+                                           ckpt_every=10, ckpt_format=fmt, nrec=30, seed=4)
+    obs = _observed(orc, grid, v, wav, src, rec)
+    J, g, gw = misfit_gradient(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
+                               torch.from_numpy(src), torch.from_numpy(rec),
+                               torch.from_numpy(obs).to(cuda), grid, want_wavelet=True)
+    Jr, gr, gwr, _ = orc.gradient(oracle_geometry(orc, grid, v, wav, src, rec), obs)
+    assert abs(J.item() - Jr) / Jr < 2e-4
+    err = rel_l2(g.cpu().numpy(), gr)
+    print(f"3D order {order} checkpoint {fmt}: gradient rel L2 {err:.3e}")
+    assert err < tol
+    if fmt == "fp32":
+        assert rel_l2(gw.cpu().numpy(), gwr) < 1e-4
+
+
+def test_shot_groups_match_one_batch(cuda, orc):
+    """group_shots runs the shots in sequential groups on one workspace; the
+    misfit, gradient, traces and wavelet gradient equal the one-batch call."""
+    import dataclasses
+    from neuralmech_gb300 import misfit_gradient, wave_forward
+    grid, v, wav, src, rec = small_problem(shape=(50, 150), nshot=5, nt=70, ckpt_every=9, seed=13)
+    obs = torch.from_numpy(_observed(orc, grid, v, wav, src, rec)).to(cuda)
+    args = (torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+            torch.from_numpy(rec))
+    J1, g1, w1, t1 = misfit_gradient(*args, obs, grid, want_wavelet=True, want_traces=True)
+    grouped = dataclasses.replace(grid, group_shots=2)
+    J2, g2, w2, t2 = misfit_gradient(*args, obs, grouped, want_wavelet=True, want_traces=True)
+    assert abs(J1.item() - J2.item()) <= 1e-12 * J1.item()
+    assert rel_l2(g2.cpu().numpy(), g1.cpu().numpy()) < 1e-6
+    assert rel_l2(w2.cpu().numpy(), w1.cpu().numpy()) < 1e-6
+    assert torch.equal(t1, t2)
+    f1 = wave_forward(*args, grid)
+    f2 = wave_forward(*args, grouped)
+    assert torch.equal(f1, f2)

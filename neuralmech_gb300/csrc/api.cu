@@ -183,7 +183,7 @@ int check_problem(const wfd_problem* p) {
         return fail(WFD_ERR_INVALID, "more than 2^31 cells per shot");
     if (p->nshot < 1 || p->nt < 1 || p->nsrc < 0 || p->nrec < 0)
         return fail(WFD_ERR_INVALID, "nshot, nt must be >= 1 and nsrc, nrec >= 0");
-    if (p->nshot > 65535 * 64 || (p->ndim == 3 && p->nshot > 65535))
+    if (p->nshot > 65535 || (p->ndim == 2 && p->nshot > 65535 * T2_MAX_SPC))
         return fail(WFD_ERR_INVALID, "too many shots");
     if (!(p->dt > 0) || !(p->dx > 0) || !(p->dz > 0) || (p->ndim == 3 && !(p->dy > 0)))
         return fail(WFD_ERR_INVALID, "dt and spacings must be positive");
@@ -228,7 +228,7 @@ Geom make_geom(const wfd_problem* p) {
     if (g.ndim == 3) {
         g.spc = 1;  // a 3D CTA marches one shot's column
     } else if (p->shots_per_cta > 0) {
-        g.spc = std::min(p->shots_per_cta, p->nshot);
+        g.spc = std::min(std::min(p->shots_per_cta, p->nshot), T2_MAX_SPC);
     } else {
         // enough CTAs for ~6 waves of 2 resident CTAs on 152 SMs, otherwise
         // as many shots per CTA as possible (m and the gradient amortise over them)
@@ -236,9 +236,9 @@ Geom make_geom(const wfd_problem* p) {
         long long spc = (long long)g.ntiles * p->nshot / target;
         int s = 1;
         while (2LL * s <= spc && 2 * s <= p->nshot) s *= 2;
-        g.spc = s;
+        g.spc = std::min(s, T2_MAX_SPC);
     }
-    while (g.ndim == 2 && (p->nshot + g.spc - 1) / g.spc > 65535) g.spc *= 2;
+    // (the shot count is bounded so that nshot / T2_MAX_SPC CTA rows fit gridDim.y)
     g.K = p->ckpt_every > 0 ? std::min(p->ckpt_every, p->nt)
                             : std::max(1, (int)std::ceil(std::sqrt((double)p->nt)));
     g.nseg = cdiv(p->nt, g.K);

@@ -24,6 +24,7 @@ constexpr int T2_W = T2_TX + 2 * T2_XH;  // staged row length (floats)
 constexpr int T2_RB = 4;
 constexpr int T2_TZ = 8 * T2_RB;         // 32 rows
 constexpr int T2_STAGES = 2;
+constexpr int T2_MAX_SPC = 64;  // shots one 2D CTA may walk through
 
 // What a step kernel does besides the stencil update.
 enum StepMode : int {

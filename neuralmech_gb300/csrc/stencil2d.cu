@@ -85,6 +85,14 @@ __global__ void __launch_bounds__(T2_THREADS, 2)
         if (MODE == MODE_GRAD) tma_load_3d(lap_buf(b), &map_lap, x0, z0, s0 + i, &bars[b]);
     };
 
+    // point-list ranges of this tile for every shot of the CTA, staged once
+    // (one global read each instead of a dependent read per shot and list)
+    __shared__ int2 smp_range[T2_MAX_SPC], inj_range[T2_MAX_SPC];
+    if (tid < ns) {
+        const int k = (s0 + tid) * ntiles + tile;
+        smp_range[tid] = a.smp.off ? make_int2(a.smp.off[k], a.smp.off[k + 1]) : make_int2(0, 0);
+        inj_range[tid] = a.inj.off ? make_int2(a.inj.off[k], a.inj.off[k + 1]) : make_int2(0, 0);
+    }
     if (tid == 0) {
         for (int b = 0; b < T2_STAGES; ++b) mbar_init(&bars[b], 1);
         fence_mbar_init();
@@ -205,8 +213,8 @@ __global__ void __launch_bounds__(T2_THREADS, 2)
 
         // sampling of the staged level u_n (receivers of the previous step,
         // or the adjoint field at the sources)
-        if (a.smp.off != nullptr) {
-            const int lo = a.smp.off[s * ntiles + tile], hi = a.smp.off[s * ntiles + tile + 1];
+        {
+            const int lo = smp_range[i].x, hi = smp_range[i].y;
             for (int j = lo + tid; j < hi; j += T2_THREADS) {
                 const int2 en = a.smp.ent[j];
                 const int z = en.x / a.ld, xx = en.x - z * a.ld;
@@ -221,8 +229,8 @@ __global__ void __launch_bounds__(T2_THREADS, 2)
             issue(i + T2_STAGES);
         }
         // injection into u_{n+1}, after every store of this shot
-        if (a.inj.off != nullptr) {
-            const int lo = a.inj.off[s * ntiles + tile], hi = a.inj.off[s * ntiles + tile + 1];
+        {
+            const int lo = inj_range[i].x, hi = inj_range[i].y;
             for (int j = lo + tid; j < hi; j += T2_THREADS) {
                 const int2 en = a.inj.ent[j];
                 const int z = en.x / a.ld, xx = en.x - z * a.ld;
@@ -240,9 +248,13 @@ __global__ void __launch_bounds__(T2_THREADS, 2)
         for (int r = 0; r < T2_RB; ++r) {
             if (!zin[r]) continue;
             float* gp = a.grad + (long long)(zb + r) * a.ld + x;
+            if (all_x) {
+                atomicAdd(reinterpret_cast<float4*>(gp), gacc[r]);  // one 16-byte reduction
+            } else {
 #pragma unroll
-            for (int e = 0; e < 4; ++e)
-                if (xin[e]) atomicAdd(gp + e, comp(gacc[r], e));
+                for (int e = 0; e < 4; ++e)
+                    if (xin[e]) atomicAdd(gp + e, comp(gacc[r], e));
+            }
         }
     }
 }

@@ -128,7 +128,7 @@ def test_gradient_finite_differences(cuda, orc):
         assert abs(fd - an) < bound, (fd, an)
 
 
-@pytest.mark.parametrize("order,fmt,tol", [(8, "fp32", 1e-4), (4, "fp32", 1e-4), (8, "bf16", 5e-3)])
+@pytest.mark.parametrize("order,fmt,tol", [(8, "fp32", 2e-4), (4, "fp32", 2e-4), (8, "bf16", 5e-3)])
 def test_gradient_3d_matches_oracle(cuda, orc, order, fmt, tol):
     from neuralmech_gb300 import misfit_gradient
     grid, v, wav, src, rec = small_problem(shape=(68, 22, 70), nshot=2, nt=48, order=order, sponge=5,

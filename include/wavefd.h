@@ -56,6 +56,7 @@ typedef struct wfd_problem {
                               groups sharing one workspace sized for a group (forward
                               without checkpoints and wfd_misfit_gradient only);
                               0 = all shots at once */
+    int32_t tile_rows;     /* 2D tile height: 16 or 32 rows (0 = 32) */
     float dt;              /* time step */
     float dz, dy, dx;      /* grid spacing (dy ignored in 2D) */
     float src_scale;       /* factor on every injected wavelet sample */

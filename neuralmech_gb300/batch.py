@@ -1,0 +1,109 @@
+"""Uneven multi-model batches in one CUDA graph.
+
+A batch holds several velocity models of different grid sizes and step
+counts, each with its own shots, wavelets, receivers and observed traces.
+This is the fwi workload family of many surveys at once (e.g. 8 models
+512^2..1536^2, 1000..3000 steps, 128 shots in total).
+
+``BatchFWI`` works in four steps:
+  * it chooses each model's kernel configuration with the autotuner;
+  * it allocates every workspace and output once;
+  * it captures one CUDA graph in which each model's checkpointed
+    forward + adjoint (``wfd_misfit_gradient``) runs on its own stream branch,
+    forked from and joined to the capturing stream, so the GPU overlaps the
+    models' step kernels;
+  * ``run()`` replays that graph: one host call per batch gradient.
+
+Inputs live in tensors owned by the batch. ``set_velocity`` / ``set_observed``
+update them in place, so the next replay sees the new values.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import torch
+
+from . import autotune as _autotune
+from .wavefd import Grid, _misfit_gradient_into, _prepare, _workspace
+
+
+@dataclasses.dataclass
+class _Model:
+    call: object
+    observed: torch.Tensor
+    ws: torch.Tensor
+    grad: torch.Tensor
+    misfit: torch.Tensor
+    stream: torch.cuda.Stream
+
+
+class BatchFWI:
+    """Misfit gradients of many models (uneven sizes) from one graph replay.
+
+    models: sequence of dicts with keys vel (nz, nx) CUDA tensor, wavelet,
+    src, rec (as for ``wave_forward``), observed (nshot, nt, nrec) CUDA tensor
+    and grid (``Grid``). ``autotune`` picks tile_rows / shots_per_cta per
+    model; ``graph=False`` runs the same calls eagerly on the streams.
+    """
+
+    def __init__(self, models, *, autotune: bool = True, graph: bool = True, tune_kw=None):
+        if not models:
+            raise ValueError("empty batch")
+        self.device = models[0]["vel"].device
+        self.models = []
+        for m in models:
+            grid: Grid = m["grid"]
+            obs = m["observed"].to(torch.float32).contiguous()
+            nshot = obs.shape[0]
+            if autotune:
+                grid = _autotune.tuned(grid, nshot, vel=m["vel"], **(tune_kw or {}))
+            call = _prepare(m["vel"], torch.as_tensor(m["wavelet"], device=self.device), m["src"], m["rec"],
+                            grid, nshot)
+            call.vel = call.vel.clone()  # the batch owns its inputs (set_velocity updates them)
+            self.models.append(_Model(call, obs, _workspace(call, True), torch.empty_like(call.vel),
+                                      torch.zeros((), dtype=torch.float64, device=self.device),
+                                      torch.cuda.Stream(device=self.device)))
+        self.configs = [(x.call.grid.tile_rows, x.call.grid.shots_per_cta) for x in self.models]
+        self.graph = None
+        self._launch()  # eager run: sets kernel attributes, validates arguments
+        torch.cuda.synchronize(self.device)
+        if graph:
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph):
+                self._launch()
+
+    def _launch(self):
+        main = torch.cuda.current_stream(self.device)
+        for m in self.models:
+            m.stream.wait_stream(main)
+            with torch.cuda.stream(m.stream):
+                _misfit_gradient_into(m.call, m.observed, m.ws, m.grad, m.misfit)
+        for m in self.models:
+            main.wait_stream(m.stream)
+
+    def set_velocity(self, i: int, vel: torch.Tensor):
+        self.models[i].call.vel.copy_(vel)
+
+    def set_observed(self, i: int, observed: torch.Tensor):
+        self.models[i].observed.copy_(observed)
+
+    def run(self):
+        """(misfits float64 [n_models], [grad_vel per model]) of the current inputs."""
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._launch()
+        return torch.stack([m.misfit for m in self.models]), [m.grad for m in self.models]
+
+    @property
+    def cell_updates(self) -> float:
+        """Counted cell-updates (forward + adjoint) of one batch gradient."""
+        tot = 0.0
+        for m in self.models:
+            g = m.call.grid
+            R = g.order // 2
+            inner = 1
+            for n in g.shape:
+                inner *= n - 2 * R
+            tot += 2.0 * m.call.problem.nshot * inner * g.nt
+        return tot

@@ -189,6 +189,8 @@ int check_problem(const wfd_problem* p) {
         return fail(WFD_ERR_INVALID, "dt and spacings must be positive");
     if (p->ckpt_format < WFD_CKPT_FP32 || p->ckpt_format > WFD_CKPT_I16)
         return fail(WFD_ERR_INVALID, "unknown checkpoint format %d", p->ckpt_format);
+    if (p->tile_rows != 0 && p->tile_rows != 16 && p->tile_rows != 32)
+        return fail(WFD_ERR_INVALID, "tile_rows must be 0, 16 or 32");
     if (p->ckpt_every < 0 || p->shots_per_cta < 0 || p->group_shots < 0)
         return fail(WFD_ERR_INVALID, "ckpt_every, shots_per_cta and group_shots must be >= 0");
     if (p->vmax > 0) {
@@ -217,7 +219,9 @@ Geom make_geom(const wfd_problem* p) {
     g.plane = (long long)g.ny * g.ld;
     g.cells = (long long)g.nz * g.plane;
     if (g.ndim == 2) {
-        g.tile_z = T2_TZ; g.tile_y = 1; g.tile_x = T2_TX;
+        g.tile_z = p->tile_rows > 0 ? p->tile_rows : T2_TZ;
+        g.tile_y = 1;
+        g.tile_x = T2_TX;
     } else {
         g.tile_z = T3_ZCHUNK; g.tile_y = T3_TY; g.tile_x = T3_TX;
     }
@@ -384,8 +388,8 @@ struct Stepper {
     int map_pair(const float* cur, const float* old, CUtensorMap* mc, CUtensorMap* mo) const {
         int rc;
         if (g.ndim == 2) {
-            const cuuint32_t bc[3] = {T2_W, cuuint32_t(T2_TZ + 2 * g.R), 1};
-            const cuuint32_t bo[3] = {T2_TX, T2_TZ, 1};
+            const cuuint32_t bc[3] = {T2_W, cuuint32_t(g.tile_z + 2 * g.R), 1};
+            const cuuint32_t bo[3] = {T2_TX, cuuint32_t(g.tile_z), 1};
             if ((rc = make_field_map(mc, cur, false, 2, g.nz, 1, g.nx, g.ld, p->nshot, bc))) return rc;
             return make_field_map(mo, old, false, 2, g.nz, 1, g.nx, g.ld, p->nshot, bo);
         }
@@ -397,7 +401,7 @@ struct Stepper {
 
     int lap_map(const void* lap, bool bf16, CUtensorMap* ml) const {
         if (g.ndim == 2) {
-            const cuuint32_t b[3] = {T2_TX, T2_TZ, 1};
+            const cuuint32_t b[3] = {T2_TX, cuuint32_t(g.tile_z), 1};
             return make_field_map(ml, lap, bf16, 2, g.nz, 1, g.nx, g.ld, p->nshot, b);
         }
         const cuuint32_t b[4] = {T3_TX, T3_TY, 1, 1};
@@ -406,7 +410,7 @@ struct Stepper {
 
     int launch(int mode, const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
                const StepArgs& a) const {
-        cudaError_t e = g.ndim == 2 ? launch_step2d(g.R, mode, mc, mo, ml, a, s)
+        cudaError_t e = g.ndim == 2 ? launch_step2d(g.R, mode, g.tile_z, mc, mo, ml, a, s)
                                     : launch_step3d(g.R, mode, mc, mo, ml, map_m, a, s);
         if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "step launch failed: %s", cudaGetErrorString(e));
         return WFD_OK;
@@ -782,7 +786,7 @@ int wfd_step2d_order2(const float* u0, const float* u1, float* u2, float wavespe
     int rc;
     if ((rc = make_field_map(&mc, u1, false, 2, N, 1, M, M_padded, 1, bc))) return rc;
     if ((rc = make_field_map(&mo, u0, false, 2, N, 1, M, M_padded, 1, bo))) return rc;
-    cudaError_t e = launch_step2d(1, MODE_PLAIN, mc, mo, mc, a, static_cast<cudaStream_t>(stream));
+    cudaError_t e = launch_step2d(1, MODE_PLAIN, T2_TZ, mc, mo, mc, a, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "step launch failed: %s", cudaGetErrorString(e));
     return WFD_OK;
 }

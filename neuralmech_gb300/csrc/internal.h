@@ -14,15 +14,15 @@ enum : unsigned {
 
 // ---------------------------------------------------------------- 2D tiles
 // One CTA = 256 threads = 8 warps. A lane owns 4 consecutive x cells (one
-// float4); a warp owns RB consecutive rows; the CTA tile is TX x TZ cells.
+// float4); a warp owns RB consecutive rows; the CTA tile is TX x (8 RB) cells,
+// RB = 4 (32 rows, the default) or 2 (16 rows).
 // u_n is staged with a halo of R rows and XH = 4 columns (XH keeps every TMA
 // x coordinate 16-byte aligned for any R <= 4).
 constexpr int T2_THREADS = 256;
 constexpr int T2_TX = 128;
 constexpr int T2_XH = 4;
 constexpr int T2_W = T2_TX + 2 * T2_XH;  // staged row length (floats)
-constexpr int T2_RB = 4;
-constexpr int T2_TZ = 8 * T2_RB;         // 32 rows
+constexpr int T2_TZ = 32;  // default tile rows; 16 is the other variant
 constexpr int T2_STAGES = 2;
 constexpr int T2_MAX_SPC = 64;  // shots one 2D CTA may walk through
 
@@ -75,12 +75,14 @@ struct StepArgs {
     unsigned* err;
 };
 
-// Launches one time step of the 2D kernel of half-width R (1, 2, 4) and mode.
-// map_cur: u_n (box T2_W x (T2_TZ + 2R) x 1); map_old: u_{n-1} (box T2_TX x T2_TZ x 1);
-// map_lap: Laplacian store (box T2_TX x T2_TZ x 1), used by MODE_GRAD only.
-cudaError_t launch_step2d(int R, int mode, const CUtensorMap& map_cur, const CUtensorMap& map_old,
-                          const CUtensorMap& map_lap, const StepArgs& a, cudaStream_t s);
-size_t step2d_smem_bytes(int R, int mode);
+// Launches one time step of the 2D kernel of half-width R (1, 2, 4), mode and
+// tile height tile_rows (16 or 32).
+// map_cur: u_n (box T2_W x (tile_rows + 2R) x 1); map_old: u_{n-1} (box
+// T2_TX x tile_rows x 1); map_lap: Laplacian store (box T2_TX x tile_rows x 1),
+// used by MODE_GRAD only.
+cudaError_t launch_step2d(int R, int mode, int tile_rows, const CUtensorMap& map_cur,
+                          const CUtensorMap& map_old, const CUtensorMap& map_lap, const StepArgs& a,
+                          cudaStream_t s);
 
 // ---------------------------------------------------------------- 3D tiles
 // One CTA (one shot) marches along z through a (TY x TX) column of the grid

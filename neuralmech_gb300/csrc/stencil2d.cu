@@ -10,15 +10,15 @@
 // Layout in HBM: each field is [shot][z][ld] FP32, ld a multiple of 8; the
 // model m is [z][ld], shared by all shots. u_{n+1} overwrites u_{n-1} in place.
 //
-// Per CTA (256 threads): a 128 x 32 tile of one shot at a time, over
+// Per CTA (256 threads): a 128 x TZ tile (TZ = 32 or 16 rows) of one shot at a time, over
 // `shots_per_cta` shots of the batch. For each shot a TMA bulk-tensor load
 // brings u_n with a halo of R rows and 4 columns and the u_{n-1} tile into
 // shared memory; two stages are in flight so the next shot's tiles load while
 // this one computes. m, the sponge factors and the gradient accumulator stay
 // in registers across the shots, so m is read once per tile per step and the
 // gradient written once per tile per step. Lane l owns x = x0 + 4l .. +3
-// (float4 loads/stores); warp w owns rows z0 + 4w .. +3, with the vertical
-// taps held in a register window.
+// (float4 loads/stores); warp w owns rows z0 + RB w .. + RB - 1, with the
+// vertical taps held in a register window.
 //
 // Fused per-step point work, bucketed by tile (PointLists):
 //   * sampling of the staged u_n at receivers (traces of the previous step),
@@ -33,12 +33,13 @@ namespace {
 
 __host__ __device__ constexpr int align_up(int v, int a) { return (v + a - 1) / a * a; }
 
-template <int R, int MODE>
+template <int R, int MODE, int RB>
 struct Layout2D {
-    static constexpr int H = T2_TZ + 2 * R;
+    static constexpr int TZ = 8 * RB;  // tile rows: 8 warps x RB rows
+    static constexpr int H = TZ + 2 * R;
     static constexpr int CUR = H * T2_W * 4;  // TMA box bytes of u_n
-    static constexpr int OLD = T2_TZ * T2_TX * 4;
-    static constexpr int LAP = MODE == MODE_GRAD ? T2_TZ * T2_TX * 4 : 0;
+    static constexpr int OLD = TZ * T2_TX * 4;
+    static constexpr int LAP = MODE == MODE_GRAD ? TZ * T2_TX * 4 : 0;
     // every TMA destination starts on a 128-byte boundary
     static constexpr int CUR_AL = align_up(CUR, 128);
     static constexpr int OLD_AL = align_up(OLD, 128);
@@ -50,12 +51,13 @@ __device__ __forceinline__ float comp(const float4& v, int e) {
     return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
 }
 
-template <int R, int MODE>
-__global__ void __launch_bounds__(T2_THREADS, 2)
+template <int R, int MODE, int RB>
+__global__ void __launch_bounds__(T2_THREADS, RB == 2 ? 3 : 2)
     step2d_kernel(const __grid_constant__ CUtensorMap map_cur,
                   const __grid_constant__ CUtensorMap map_old,
                   const __grid_constant__ CUtensorMap map_lap, const StepArgs a) {
-    using L = Layout2D<R, MODE>;
+    using L = Layout2D<R, MODE, RB>;
+    constexpr int TZ = L::TZ;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
@@ -65,13 +67,13 @@ __global__ void __launch_bounds__(T2_THREADS, 2)
     const int tile = blockIdx.x;
     const int ntiles = a.tiles_x * a.tiles_z;
     const int x0 = (tile % a.tiles_x) * T2_TX;
-    const int z0 = (tile / a.tiles_x) * T2_TZ;
+    const int z0 = (tile / a.tiles_x) * TZ;
     const int s0 = blockIdx.y * a.shots_per_cta;
     const int ns = min(a.nshot - s0, a.shots_per_cta);
     if (ns <= 0) return;
 
     const uint32_t lap_bytes =
-        MODE == MODE_GRAD ? uint32_t(T2_TZ * T2_TX * (a.lap_bf16 ? 2 : 4)) : 0u;
+        MODE == MODE_GRAD ? uint32_t(TZ * T2_TX * (a.lap_bf16 ? 2 : 4)) : 0u;
     const uint32_t stage_tx = uint32_t(L::CUR + L::OLD) + lap_bytes;
     auto cur_buf = [&](int b) { return reinterpret_cast<float*>(base + b * L::STAGE); };
     auto old_buf = [&](int b) { return reinterpret_cast<float*>(base + b * L::STAGE + L::CUR_AL); };
@@ -103,12 +105,12 @@ __global__ void __launch_bounds__(T2_THREADS, 2)
 
     // ---- per-thread constants, reused for every shot of the CTA
     const int x = x0 + 4 * lane;
-    const int zb = z0 + warp * T2_RB;
-    float4 mrow[T2_RB];
-    float gzr[T2_RB];
-    bool zin[T2_RB];
+    const int zb = z0 + warp * RB;
+    float4 mrow[RB];
+    float gzr[RB];
+    bool zin[RB];
 #pragma unroll
-    for (int r = 0; r < T2_RB; ++r) {
+    for (int r = 0; r < RB; ++r) {
         const int z = zb + r;
         if (a.m != nullptr && z < a.nz && x < a.ld)
             mrow[r] = __ldg(reinterpret_cast<const float4*>(a.m + (long long)z * a.ld + x));
@@ -126,9 +128,9 @@ __global__ void __launch_bounds__(T2_THREADS, 2)
     }
     const bool all_x = xin[0] && xin[1] && xin[2] && xin[3];
 
-    float4 gacc[T2_RB];
+    float4 gacc[RB];
 #pragma unroll
-    for (int r = 0; r < T2_RB; ++r) gacc[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int r = 0; r < RB; ++r) gacc[r] = make_float4(0.f, 0.f, 0.f, 0.f);
 
     for (int i = 0; i < ns; ++i) {
         const int s = s0 + i, b = i % T2_STAGES;
@@ -137,22 +139,22 @@ __global__ void __launch_bounds__(T2_THREADS, 2)
         const float* old = old_buf(b);
         float* un = a.u_new + (long long)s * a.shot_stride;
 
-        float4 V[T2_RB + 2 * R];
+        float4 V[RB + 2 * R];
 #pragma unroll
-        for (int j = 0; j < T2_RB + 2 * R; ++j)
-            V[j] = *reinterpret_cast<const float4*>(cur + (warp * T2_RB + j) * T2_W + T2_XH +
+        for (int j = 0; j < RB + 2 * R; ++j)
+            V[j] = *reinterpret_cast<const float4*>(cur + (warp * RB + j) * T2_W + T2_XH +
                                                     4 * lane);
 #pragma unroll
-        for (int r = 0; r < T2_RB; ++r) {
+        for (int r = 0; r < RB; ++r) {
             const int z = zb + r;
-            const float* row = cur + (warp * T2_RB + r + R) * T2_W + 4 * lane;
+            const float* row = cur + (warp * RB + r + R) * T2_W + 4 * lane;
             const float4 lv = *reinterpret_cast<const float4*>(row);
             const float4 cv = V[r + R];
             const float4 rv = *reinterpret_cast<const float4*>(row + 2 * T2_XH);
             const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y,
                                  cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
             const float4 ov =
-                *reinterpret_cast<const float4*>(old + (warp * T2_RB + r) * T2_TX + 4 * lane);
+                *reinterpret_cast<const float4*>(old + (warp * RB + r) * T2_TX + 4 * lane);
             float lap[4], nv[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -198,7 +200,7 @@ __global__ void __launch_bounds__(T2_THREADS, 2)
             }
             if (MODE == MODE_GRAD && zin[r]) {
                 const unsigned char* lb = lap_buf(b);
-                const int li = (warp * T2_RB + r) * T2_TX + 4 * lane;
+                const int li = (warp * RB + r) * T2_TX + 4 * lane;
                 const float4 lu =
                     a.lap_bf16 ? unpack_bf16x4(*reinterpret_cast<const uint2*>(
                                      reinterpret_cast<const __nv_bfloat16*>(lb) + li))
@@ -245,7 +247,7 @@ __global__ void __launch_bounds__(T2_THREADS, 2)
 
     if (MODE == MODE_GRAD) {
 #pragma unroll
-        for (int r = 0; r < T2_RB; ++r) {
+        for (int r = 0; r < RB; ++r) {
             if (!zin[r]) continue;
             float* gp = a.grad + (long long)(zb + r) * a.ld + x;
             if (all_x) {
@@ -259,61 +261,56 @@ __global__ void __launch_bounds__(T2_THREADS, 2)
     }
 }
 
-template <int R, int MODE>
+template <int R, int MODE, int RB>
 cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
                         const StepArgs& a, cudaStream_t s) {
-    using L = Layout2D<R, MODE>;
+    using L = Layout2D<R, MODE, RB>;
     static int configured_device = -1;
     int dev = 0;
     cudaGetDevice(&dev);
     if (configured_device != dev) {
-        cudaError_t e = cudaFuncSetAttribute(step2d_kernel<R, MODE>,
+        cudaError_t e = cudaFuncSetAttribute(step2d_kernel<R, MODE, RB>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
         if (e != cudaSuccess) return e;
         configured_device = dev;
     }
     const dim3 grid(a.tiles_x * a.tiles_z, (a.nshot + a.shots_per_cta - 1) / a.shots_per_cta);
-    step2d_kernel<R, MODE><<<grid, T2_THREADS, L::BYTES, s>>>(mc, mo, ml, a);
+    step2d_kernel<R, MODE, RB><<<grid, T2_THREADS, L::BYTES, s>>>(mc, mo, ml, a);
     count_launch();
     return cudaGetLastError();
 }
 
-template <int R>
+template <int R, int RB>
 cudaError_t dispatch_mode(int mode, const CUtensorMap& mc, const CUtensorMap& mo,
                           const CUtensorMap& ml, const StepArgs& a, cudaStream_t s) {
     switch (mode) {
-        case MODE_PLAIN: return launch_impl<R, MODE_PLAIN>(mc, mo, ml, a, s);
-        case MODE_SAVE_LAP: return launch_impl<R, MODE_SAVE_LAP>(mc, mo, ml, a, s);
-        case MODE_GRAD: return launch_impl<R, MODE_GRAD>(mc, mo, ml, a, s);
+        case MODE_PLAIN: return launch_impl<R, MODE_PLAIN, RB>(mc, mo, ml, a, s);
+        case MODE_SAVE_LAP: return launch_impl<R, MODE_SAVE_LAP, RB>(mc, mo, ml, a, s);
+        case MODE_GRAD: return launch_impl<R, MODE_GRAD, RB>(mc, mo, ml, a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int RB>
+cudaError_t dispatch_r(int R, int mode, const CUtensorMap& mc, const CUtensorMap& mo,
+                       const CUtensorMap& ml, const StepArgs& a, cudaStream_t s) {
+    switch (R) {
+        case 1: return dispatch_mode<1, RB>(mode, mc, mo, ml, a, s);
+        case 2: return dispatch_mode<2, RB>(mode, mc, mo, ml, a, s);
+        case 4: return dispatch_mode<4, RB>(mode, mc, mo, ml, a, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
 }  // namespace
 
-cudaError_t launch_step2d(int R, int mode, const CUtensorMap& mc, const CUtensorMap& mo,
-                          const CUtensorMap& ml, const StepArgs& a, cudaStream_t s) {
-    switch (R) {
-        case 1: return dispatch_mode<1>(mode, mc, mo, ml, a, s);
-        case 2: return dispatch_mode<2>(mode, mc, mo, ml, a, s);
-        case 4: return dispatch_mode<4>(mode, mc, mo, ml, a, s);
+cudaError_t launch_step2d(int R, int mode, int tile_rows, const CUtensorMap& mc,
+                          const CUtensorMap& mo, const CUtensorMap& ml, const StepArgs& a,
+                          cudaStream_t s) {
+    switch (tile_rows) {
+        case 16: return dispatch_r<2>(R, mode, mc, mo, ml, a, s);
+        case 32: return dispatch_r<4>(R, mode, mc, mo, ml, a, s);
         default: return cudaErrorInvalidValue;
-    }
-}
-
-size_t step2d_smem_bytes(int R, int mode) {
-    auto pick = [&](auto r_tag) -> size_t {
-        constexpr int RR = decltype(r_tag)::value;
-        switch (mode) {
-            case MODE_PLAIN: return Layout2D<RR, MODE_PLAIN>::BYTES;
-            case MODE_SAVE_LAP: return Layout2D<RR, MODE_SAVE_LAP>::BYTES;
-            default: return Layout2D<RR, MODE_GRAD>::BYTES;
-        }
-    };
-    switch (R) {
-        case 1: return pick(std::integral_constant<int, 1>{});
-        case 2: return pick(std::integral_constant<int, 2>{});
-        default: return pick(std::integral_constant<int, 4>{});
     }
 }
 

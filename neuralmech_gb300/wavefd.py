@@ -57,6 +57,7 @@ class Grid:
     group_shots  run the shots of a misfit gradient (or of a forward without
              autograd) in sequential groups of this many, sharing one workspace
              sized for a group (0 = all at once)
+    tile_rows    2D tile height, 16 or 32 rows (0 = 32)
     """
     shape: tuple
     spacing: tuple
@@ -71,6 +72,7 @@ class Grid:
     lap_bf16: bool = False
     shots_per_cta: int = 0
     group_shots: int = 0
+    tile_rows: int = 0
 
     @property
     def ndim(self) -> int:
@@ -140,7 +142,7 @@ def _problem(grid: Grid, nshot: int, nsrc: int, nrec: int, vmax: float) -> _lib.
         dz, dy, dx = grid.spacing
     return _lib.Problem(grid.ndim, grid.order, nz, ny, nx, nshot, grid.nt, nsrc, nrec,
                         grid.ckpt_every, CKPT_FORMATS[grid.ckpt_format], int(grid.lap_bf16),
-                        grid.shots_per_cta, grid.group_shots, grid.dt, dz, dy, dx, grid.src_scale, vmax)
+                        grid.shots_per_cta, grid.group_shots, grid.tile_rows, grid.dt, dz, dy, dx, grid.src_scale, vmax)
 
 
 # ---------------------------------------------------------------- argument prep
@@ -339,17 +341,12 @@ def misfit_gradient(vel: torch.Tensor, wavelet, src, rec, observed: torch.Tensor
     if tuple(observed.shape) != (p.nshot, p.nt, p.nrec):
         raise ValueError(f"observed must be ({p.nshot}, {p.nt}, {p.nrec})")
     obs = observed.to(torch.float32).contiguous()
-    lib = _lib.load()
     ws = _workspace(call, True)
     grad = torch.empty_like(call.vel)
     gwav = torch.empty_like(call.wavelet) if want_wavelet else None
     traces = torch.empty_like(obs) if want_traces else None
     misfit = torch.zeros((), dtype=torch.float64, device=vel.device)
-    gz, gy, gx = call.sponges
-    _lib.check(lib.wfd_misfit_gradient(ctypes.byref(p), _ptr(call.vel), _ptr(gz), _ptr(gy), _ptr(gx),
-                                       _ptr(call.wavelet), _ptr(call.src), _ptr(call.rec), _ptr(obs),
-                                       _ptr(traces), _ptr(grad), _ptr(gwav), _ptr(misfit),
-                                       _ptr(ws), ws.numel(), _stream()), "wfd_misfit_gradient")
+    _misfit_gradient_into(call, obs, ws, grad, misfit, gwav, traces)
     if check:
         _status(ws, "wfd_misfit_gradient")
     out = [misfit, grad]
@@ -358,6 +355,16 @@ def misfit_gradient(vel: torch.Tensor, wavelet, src, rec, observed: torch.Tensor
     if want_traces:
         out.append(traces)
     return tuple(out)
+
+
+def _misfit_gradient_into(call: _Call, obs, ws, grad, misfit, gwav=None, traces=None):
+    """wfd_misfit_gradient into caller buffers on the current stream (no
+    allocation, no synchronisation: safe inside CUDA-graph capture)."""
+    gz, gy, gx = call.sponges
+    _lib.check(_lib.load().wfd_misfit_gradient(
+        ctypes.byref(call.problem), _ptr(call.vel), _ptr(gz), _ptr(gy), _ptr(gx), _ptr(call.wavelet),
+        _ptr(call.src), _ptr(call.rec), _ptr(obs), _ptr(traces), _ptr(grad), _ptr(gwav), _ptr(misfit),
+        _ptr(ws), ws.numel(), _stream()), "wfd_misfit_gradient")
 
 
 def sum_sq(x: torch.Tensor) -> torch.Tensor:

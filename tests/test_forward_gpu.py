@@ -52,17 +52,18 @@ def test_step2d_order2_separate_output(cuda):
 
 
 @pytest.mark.parametrize("order", [2, 4, 8])
-@pytest.mark.parametrize("shape,sponge,nshot,spc", [
-    ((60, 150), 10, 3, 0),
-    ((37, 131), 0, 2, 1),
-    ((100, 260), (5, 12), 5, 2),
-    ((33, 40), 6, 1, 0),
+@pytest.mark.parametrize("shape,sponge,nshot,spc,rows", [
+    ((60, 150), 10, 3, 0, 0),
+    ((37, 131), 0, 2, 1, 16),
+    ((100, 260), (5, 12), 5, 2, 0),
+    ((100, 260), (5, 12), 5, 3, 16),
+    ((33, 40), 6, 1, 0, 0),
 ])
-def test_forward_matches_oracle(cuda, orc, order, shape, sponge, nshot, spc):
+def test_forward_matches_oracle(cuda, orc, order, shape, sponge, nshot, spc, rows):
     from neuralmech_gb300 import wave_forward
     grid, v, wav, src, rec = small_problem(shape=shape, nshot=nshot, order=order,
                                            sponge=sponge if isinstance(sponge, int) else [sponge, sponge],
-                                           nt=90, spc=spc, seed=order + nshot)
+                                           nt=90, spc=spc, seed=order + nshot, tile_rows=rows)
     traces = wave_forward(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
                           torch.from_numpy(src), torch.from_numpy(rec), grid)
     ref = orc.forward(oracle_geometry(orc, grid, v, wav, src, rec))

@@ -31,15 +31,15 @@ def _observed(orc, grid, v, wav, src, rec, seed=7):
 
 
 @pytest.mark.parametrize("order", [2, 8])
-@pytest.mark.parametrize("shape,nshot,nt,ckpt,spc", [
-    ((60, 150), 3, 100, 0, 0),
-    ((41, 133), 2, 77, 10, 1),
-    ((70, 260), 4, 64, 64, 2),
+@pytest.mark.parametrize("shape,nshot,nt,ckpt,spc,rows", [
+    ((60, 150), 3, 100, 0, 0, 0),
+    ((41, 133), 2, 77, 10, 1, 16),
+    ((70, 260), 4, 64, 64, 2, 0),
 ])
-def test_gradient_matches_oracle_fp32(cuda, orc, order, shape, nshot, nt, ckpt, spc):
+def test_gradient_matches_oracle_fp32(cuda, orc, order, shape, nshot, nt, ckpt, spc, rows):
     from neuralmech_gb300 import misfit_gradient
     grid, v, wav, src, rec = small_problem(shape=shape, nshot=nshot, nt=nt, order=order,
-                                           ckpt_every=ckpt, spc=spc, seed=3)
+                                           ckpt_every=ckpt, spc=spc, seed=3, tile_rows=rows)
     obs = _observed(orc, grid, v, wav, src, rec)
     J, g, gw = misfit_gradient(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
                                torch.from_numpy(src), torch.from_numpy(rec),

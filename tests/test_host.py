@@ -74,3 +74,23 @@ def test_synthetic_workloads():
     assert len(b) == 8 and sum(x.nshot for x in b) == 128
     assert all(512 <= x.vel.shape[0] <= 1536 and x.vel.shape[0] % 64 == 0 for x in b)
     assert all(1000 <= x.grid.nt <= 3000 for x in b)
+
+
+def test_autotune_selection_and_cache(tmp_path):
+    from neuralmech_gb300 import Grid, autotune
+    g = Grid((256, 512), (10.0, 10.0), 1e-3, 10)
+    calls = []
+
+    def fake(cfg):
+        calls.append(cfg)
+        return abs(cfg["shots_per_cta"] - 4) + (0.5 if cfg["tile_rows"] == 32 else 0.0) + 1.0
+
+    path = str(tmp_path / "cache.json")
+    best = autotune.tune(g, 12, timer=fake, path=path)
+    assert best == {"tile_rows": 16, "shots_per_cta": 4}
+    n = len(calls)
+    assert n == len(autotune.candidates(12))
+    assert autotune.tune(g, 12, timer=fake, path=path) == best and len(calls) == n
+    assert autotune.tune(g, 12, timer=fake, path=path, refresh=True) == best and len(calls) == 2 * n
+    g3 = Grid((32, 32, 32), (10.0,) * 3, 1e-3, 10)
+    assert autotune.tune(g3, 4, timer=fake, path=path) == {"tile_rows": 0, "shots_per_cta": 0}

@@ -57,6 +57,8 @@ typedef struct wfd_problem {
                               without checkpoints and wfd_misfit_gradient only);
                               0 = all shots at once */
     int32_t tile_rows;     /* 2D tile height: 16 or 32 rows (0 = 32) */
+    int32_t step_block;    /* 2D time steps per kernel launch: 1 or 2 (0 = 1); 2 keeps
+                              u_{n+1} in shared memory between the two steps */
     float dt;              /* time step */
     float dz, dy, dx;      /* grid spacing (dy ignored in 2D) */
     float src_scale;       /* factor on every injected wavelet sample */

@@ -145,6 +145,7 @@ int make_field_map(CUtensorMap* map, const void* base, bool bf16, int ndim, int 
 // ------------------------------------------------------------------ geometry
 struct Geom {
     int ndim, R, nz, ny, nx, ld;
+    int sb;                  // time steps per launch (2D: 1 or 2)
     long long plane, cells;  // z stride; cells per shot (padded)
     int tile_z, tile_y, tile_x, tiles_z, tiles_y, tiles_x, ntiles;
     int spc;                 // shots per CTA
@@ -191,6 +192,8 @@ int check_problem(const wfd_problem* p) {
         return fail(WFD_ERR_INVALID, "unknown checkpoint format %d", p->ckpt_format);
     if (p->tile_rows != 0 && p->tile_rows != 16 && p->tile_rows != 32)
         return fail(WFD_ERR_INVALID, "tile_rows must be 0, 16 or 32");
+    if (p->step_block < 0 || p->step_block > 2 || (p->step_block == 2 && p->ndim != 2))
+        return fail(WFD_ERR_INVALID, "step_block must be 0, 1 or 2 (2: 2D only)");
     if (p->ckpt_every < 0 || p->shots_per_cta < 0 || p->group_shots < 0)
         return fail(WFD_ERR_INVALID, "ckpt_every, shots_per_cta and group_shots must be >= 0");
     if (p->vmax > 0) {
@@ -218,7 +221,12 @@ Geom make_geom(const wfd_problem* p) {
     g.ld = (p->nx + 7) / 8 * 8;
     g.plane = (long long)g.ny * g.ld;
     g.cells = (long long)g.nz * g.plane;
-    if (g.ndim == 2) {
+    g.sb = (p->ndim == 2 && p->step_block == 2) ? 2 : 1;
+    if (g.ndim == 2 && g.sb == 2) {
+        g.tile_z = K2_TZ;
+        g.tile_y = 1;
+        g.tile_x = K2_TX;
+    } else if (g.ndim == 2) {
         g.tile_z = p->tile_rows > 0 ? p->tile_rows : T2_TZ;
         g.tile_y = 1;
         g.tile_x = T2_TX;
@@ -229,8 +237,8 @@ Geom make_geom(const wfd_problem* p) {
     g.tiles_y = cdiv(g.ny, g.tile_y);
     g.tiles_x = cdiv(g.nx, g.tile_x);
     g.ntiles = g.tiles_z * g.tiles_y * g.tiles_x;
-    if (g.ndim == 3) {
-        g.spc = 1;  // a 3D CTA marches one shot's column
+    if (g.ndim == 3 || g.sb == 2) {
+        g.spc = 1;  // a 3D or two-step CTA works on one shot
     } else if (p->shots_per_cta > 0) {
         g.spc = std::min(std::min(p->shots_per_cta, p->nshot), T2_MAX_SPC);
     } else {
@@ -262,8 +270,10 @@ Geom make_geom(const wfd_problem* p) {
 
 // ------------------------------------------------------------------ workspace
 struct Layout {
-    size_t err, m, P0, P1, counts, src_off, src_ent, rec_off, rec_ent;
-    size_t Q0, Q1, G, ckpt, lap, res, total;
+    int nbuf;  // field buffers per direction: 2 (in place) or 4 (two-step blocking)
+    size_t err, m, P[4], counts, src_off, src_ent, rec_off, rec_ent;
+    size_t srce_off, srce_ent, rece_off, rece_ent;  // extended-region lists (two-step)
+    size_t Q[4], G, ckpt, lap, res, total;
     size_t field_bytes, ckpt_field_bytes, lap_field_bytes;
 };
 
@@ -275,21 +285,26 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     auto take = [&](size_t bytes) { size_t at = o; o = up256(o + bytes); return at; };
     const size_t keys = (size_t)p->nshot * g.ntiles;
     L.field_bytes = (size_t)p->nshot * g.cells * 4;
+    L.nbuf = g.sb == 2 ? 4 : 2;
     L.err = take(256);
     L.m = take((size_t)g.cells * 4);
-    L.P0 = take(L.field_bytes);
-    L.P1 = take(L.field_bytes);
+    for (int b = 0; b < L.nbuf; ++b) L.P[b] = take(L.field_bytes);
     L.counts = take(keys * 4);
     L.src_off = take((keys + 1) * 4);
     L.src_ent = take((size_t)p->nshot * p->nsrc * 8 + 8);
     L.rec_off = take((keys + 1) * 4);
     L.rec_ent = take((size_t)p->nshot * p->nrec * 8 + 8);
+    if (g.sb == 2) {  // a point joins up to 4 extended tile regions
+        L.srce_off = take((keys + 1) * 4);
+        L.srce_ent = take((size_t)p->nshot * p->nsrc * 32 + 8);
+        L.rece_off = take((keys + 1) * 4);
+        L.rece_ent = take((size_t)p->nshot * p->nrec * 32 + 8);
+    }
     if (grad) {
         // per-field slots start on 256-byte boundaries (TMA bases, short4/float4 access)
         L.ckpt_field_bytes = up256(ckpt_bytes(p->ckpt_format, (long long)p->nshot * g.cells));
         L.lap_field_bytes = up256((size_t)p->nshot * g.cells * (p->lap_bf16 ? 2 : 4));
-        L.Q0 = take(L.field_bytes);
-        L.Q1 = take(L.field_bytes);
+        for (int b = 0; b < L.nbuf; ++b) L.Q[b] = take(L.field_bytes);
         L.G = take((size_t)g.cells * 4);
         L.ckpt = take((size_t)g.nseg * 2 * L.ckpt_field_bytes);
         L.lap = take((size_t)g.K * L.lap_field_bytes);
@@ -301,9 +316,9 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
 
 struct Work {
     unsigned* err;
-    float *m, *P[2], *Q[2], *G, *res;
+    float *m, *P[4], *Q[4], *G, *res;
     int* counts;
-    PointLists src, rec;
+    PointLists src, rec, src_e, rec_e;
     unsigned char *ckpt, *lap;
 };
 
@@ -312,16 +327,20 @@ Work carve(void* ws, const Layout& L, bool grad) {
     Work w{};
     w.err = reinterpret_cast<unsigned*>(b + L.err);
     w.m = reinterpret_cast<float*>(b + L.m);
-    w.P[0] = reinterpret_cast<float*>(b + L.P0);
-    w.P[1] = reinterpret_cast<float*>(b + L.P1);
+    for (int k = 0; k < L.nbuf; ++k) w.P[k] = reinterpret_cast<float*>(b + L.P[k]);
     w.counts = reinterpret_cast<int*>(b + L.counts);
     w.src.off = reinterpret_cast<int*>(b + L.src_off);
     w.src.ent = reinterpret_cast<int2*>(b + L.src_ent);
     w.rec.off = reinterpret_cast<int*>(b + L.rec_off);
     w.rec.ent = reinterpret_cast<int2*>(b + L.rec_ent);
+    if (L.nbuf == 4) {
+        w.src_e.off = reinterpret_cast<int*>(b + L.srce_off);
+        w.src_e.ent = reinterpret_cast<int2*>(b + L.srce_ent);
+        w.rec_e.off = reinterpret_cast<int*>(b + L.rece_off);
+        w.rec_e.ent = reinterpret_cast<int2*>(b + L.rece_ent);
+    }
     if (grad) {
-        w.Q[0] = reinterpret_cast<float*>(b + L.Q0);
-        w.Q[1] = reinterpret_cast<float*>(b + L.Q1);
+        for (int k = 0; k < L.nbuf; ++k) w.Q[k] = reinterpret_cast<float*>(b + L.Q[k]);
         w.G = reinterpret_cast<float*>(b + L.G);
         w.ckpt = b + L.ckpt;
         w.lap = b + L.lap;
@@ -349,9 +368,22 @@ struct Stepper {
     unsigned* err;
     const float* m;
     const float *gz, *gy, *gx;
-    CUtensorMap map_m{};  // 3D only: tiles of the model m
+    CUtensorMap map_m{};  // 3D: tiles of the model m; 2D two-step: m on the extended tile
 
     int init() {
+        if (g.ndim == 2 && g.sb == 2) {
+            EncodeTiled enc = encoder();
+            if (!enc) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+            const cuuint64_t dims[2] = {(cuuint64_t)g.nx, (cuuint64_t)g.nz};
+            const cuuint64_t strides[1] = {(cuuint64_t)g.ld * 4};
+            const cuuint32_t box[2] = {K2_EW, cuuint32_t(K2_TZ + 2 * g.R)}, estr[2] = {1, 1};
+            CUresult r = enc(&map_m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(m), dims,
+                             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled (m) failed (%d)", (int)r);
+            return WFD_OK;
+        }
         if (g.ndim != 3) return WFD_OK;
         EncodeTiled enc = encoder();
         if (!enc) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
@@ -408,6 +440,27 @@ struct Stepper {
         return make_field_map(ml, lap, bf16, 3, g.nz, g.ny, g.nx, g.ld, p->nshot, b);
     }
 
+    // two-step kernel: u_n box (2R rows / 8 columns of halo) and u_{n-1} box (R / 4)
+    int map_k2(const float* buf, CUtensorMap* mu, CUtensorMap* mo) const {
+        const cuuint32_t bu[3] = {K2_UW, cuuint32_t(K2_TZ + 4 * g.R), 1};
+        const cuuint32_t bo[3] = {K2_EW, cuuint32_t(K2_TZ + 2 * g.R), 1};
+        int rc;
+        if ((rc = make_field_map(mu, buf, false, 2, g.nz, 1, g.nx, g.ld, p->nshot, bu))) return rc;
+        return make_field_map(mo, buf, false, 2, g.nz, 1, g.nx, g.ld, p->nshot, bo);
+    }
+
+    int lap_map_k2(const void* lap, bool bf16, CUtensorMap* ml) const {
+        const cuuint32_t b[3] = {K2_TX, K2_TZ, 1};
+        return make_field_map(ml, lap, bf16, 2, g.nz, 1, g.nx, g.ld, p->nshot, b);
+    }
+
+    int launch_k2(int mode, const CUtensorMap& mu, const CUtensorMap& mo, const CUtensorMap& l1,
+                  const CUtensorMap& l2, const Step2Args& q) const {
+        cudaError_t e = launch_step2d_k2(g.R, mode, mu, mo, map_m, l1, l2, q, s);
+        if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "two-step launch failed: %s", cudaGetErrorString(e));
+        return WFD_OK;
+    }
+
     int launch(int mode, const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
                const StepArgs& a) const {
         cudaError_t e = g.ndim == 2 ? launch_step2d(g.R, mode, g.tile_z, mc, mo, ml, a, s)
@@ -450,17 +503,34 @@ int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
     WFD_CUDA(launch_build_lists(rec, p->nshot, p->nrec, g.nz, g.ny, g.nx, g.ld, g.R, g.tile_z,
                                 g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
                                 const_cast<int*>(w.rec.off), const_cast<int2*>(w.rec.ent), w.err, s));
+    if (g.sb == 2) {  // points inside each tile's extended region (R rows, 4 columns)
+        WFD_CUDA(launch_build_lists(src, p->nshot, p->nsrc, g.nz, g.ny, g.nx, g.ld, g.R, g.tile_z,
+                                    g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
+                                    const_cast<int*>(w.src_e.off), const_cast<int2*>(w.src_e.ent),
+                                    w.err, s, g.R, 4));
+        WFD_CUDA(launch_build_lists(rec, p->nshot, p->nrec, g.nz, g.ny, g.nx, g.ld, g.R, g.tile_z,
+                                    g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
+                                    const_cast<int*>(w.rec_e.off), const_cast<int2*>(w.rec_e.ent),
+                                    w.err, s, g.R, 4));
+    }
     return WFD_OK;
 }
+
+int run_forward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
+                   const Stepper& st, const float* wavelet, float* traces, bool save);
+int run_backward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
+                    const Stepper& st, const float* wavelet, const float* dtraces, float* grad_vel,
+                    float* grad_wavelet, const float* vel, bool zero_G, bool finalize);
 
 // Forward time loop. With save: checkpoints every K steps and the L u store of
 // the last segment (which the backward then does not recompute).
 int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                 const Stepper& st, const float* wavelet, float* traces, bool save) {
+    if (g.sb == 2) return run_forward_k2(p, g, L, w, st, wavelet, traces, save);
     cudaStream_t s = st.s;
     WFD_CUDA(cudaMemsetAsync(w.P[0], 0, L.field_bytes, s));
     WFD_CUDA(cudaMemsetAsync(w.P[1], 0, L.field_bytes, s));
-    CUtensorMap mc[2], mo[2], ml;
+    CUtensorMap mc[2], mo[2];
     int rc;
     for (int b = 0; b < 2; ++b)
         if ((rc = st.map_pair(w.P[b], w.P[b], &mc[b], &mo[b]))) return rc;
@@ -498,11 +568,217 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
     return WFD_OK;
 }
 
+// ------------------------------------------------------------------ two-step loops
+// Buffers rotate through four slots: a launch reads (u_{n-1}, u_n) from two of
+// them and writes (u_{n+1}, u_{n+2}) to the other two (one step: u_{n+1} only).
+struct Levels {
+    int old_, cur;
+    void free_pair(int& f0, int& f1) const {
+        int k = 0, f[2] = {0, 0};
+        for (int b = 0; b < 4 && k < 2; ++b)
+            if (b != old_ && b != cur) f[k++] = b;
+        f0 = f[0];
+        f1 = f[1];
+    }
+    void advance(bool two, int f0, int f1) {
+        if (two) {
+            old_ = f0;
+            cur = f1;
+        } else {
+            old_ = cur;
+            cur = f0;
+        }
+    }
+};
+
+int run_forward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
+                   const Stepper& st, const float* wavelet, float* traces, bool save) {
+    cudaStream_t s = st.s;
+    for (int b = 0; b < 4; ++b) WFD_CUDA(cudaMemsetAsync(w.P[b], 0, L.field_bytes, s));
+    CUtensorMap mu[4], mo[4], none{};
+    int rc;
+    for (int b = 0; b < 4; ++b)
+        if ((rc = st.map_k2(w.P[b], &mu[b], &mo[b]))) return rc;
+    const long long n_all = (long long)p->nshot * g.cells;
+    Levels lv{0, 1};
+    PhaseScope scope(PH_FORWARD, s, (p->nt + 1) / 2);
+    for (int n = 0; n < p->nt;) {
+        if (save && n % g.K == 0) {
+            unsigned char* slot = w.ckpt + (size_t)(n / g.K) * 2 * L.ckpt_field_bytes;
+            WFD_CUDA(launch_pack(w.P[lv.old_], slot, n_all, p->ckpt_format, s));
+            WFD_CUDA(launch_pack(w.P[lv.cur], slot + L.ckpt_field_bytes, n_all, p->ckpt_format, s));
+        }
+        // a launch never spans a checkpoint (nor the start of the stored last segment)
+        const bool two = n + 1 < p->nt && !(save && (n + 1) % g.K == 0);
+        const bool lap = save && n >= g.k0_last;
+        int f0, f1;
+        lv.free_pair(f0, f1);
+        Step2Args q{};
+        q.a = st.base(w.P[f1]);
+        q.u_mid = w.P[f0];
+        q.two_steps = two;
+        q.inj_t1 = -1;
+        q.a.inj_t = -1;
+        if (p->nsrc > 0) {
+            q.inj_e = w.src_e;
+            q.inj_t1 = n;
+            q.a.inj = w.src;
+            q.a.inj_val = wavelet;
+            q.a.inj_np = p->nsrc; q.a.inj_nt = p->nt; q.a.inj_t = two ? n + 1 : -1;
+            q.a.inj_scale = p->src_scale;
+        }
+        q.smp_t1 = -1;
+        q.a.smp_t = -1;
+        if (traces && p->nrec > 0) {
+            q.a.smp = w.rec;
+            q.a.smp_out = traces;
+            q.a.smp_np = p->nrec; q.a.smp_nt = p->nt;
+            q.a.smp_scale = 1.f;
+            q.smp_t1 = n - 1;
+            q.a.smp_t = two ? n : -1;
+        }
+        if (lap) {
+            q.lap1 = w.lap + (size_t)(n - g.k0_last) * L.lap_field_bytes;
+            if (two) q.a.lap = w.lap + (size_t)(n + 1 - g.k0_last) * L.lap_field_bytes;
+            q.a.lap_bf16 = p->lap_bf16;
+        }
+        if ((rc = st.launch_k2(lap ? MODE_SAVE_LAP : MODE_PLAIN, mu[lv.cur], mo[lv.old_], none, none, q)))
+            return rc;
+        lv.advance(two, f0, f1);
+        n += two ? 2 : 1;
+    }
+    if (traces && p->nrec > 0)
+        WFD_CUDA(launch_gather(w.P[lv.cur], g.cells, w.rec, g.ntiles, p->nshot, p->nrec, nullptr, 1.f, 0,
+                               traces, p->nt, p->nt - 1, s));
+    return WFD_OK;
+}
+
+int run_backward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
+                    const Stepper& st, const float* wavelet, const float* dtraces, float* grad_vel,
+                    float* grad_wavelet, const float* vel, bool zero_G, bool finalize) {
+    cudaStream_t s = st.s;
+    for (int b = 0; b < 4; ++b) WFD_CUDA(cudaMemsetAsync(w.Q[b], 0, L.field_bytes, s));
+    if (zero_G) WFD_CUDA(cudaMemsetAsync(w.G, 0, (size_t)g.cells * 4, s));
+    int rc;
+    CUtensorMap pu[4], po[4], qu[4], qo[4], none{};
+    for (int b = 0; b < 4; ++b) {
+        if ((rc = st.map_k2(w.P[b], &pu[b], &po[b]))) return rc;
+        if ((rc = st.map_k2(w.Q[b], &qu[b], &qo[b]))) return rc;
+    }
+    std::vector<CUtensorMap> lm(g.K);
+    for (int k = 0; k < g.K; ++k)
+        if ((rc = st.lap_map_k2(w.lap + (size_t)k * L.lap_field_bytes, p->lap_bf16, &lm[k]))) return rc;
+    const long long n_all = (long long)p->nshot * g.cells;
+
+    // adjoint launch at k: q_k (and q_{k-1} when two) from (q_{k+2}, q_{k+1})
+    Levels ql{0, 1};
+    auto adjoint = [&](int k, bool two, bool grad, int k0) -> int {
+        int f0, f1;
+        ql.free_pair(f0, f1);
+        Step2Args q{};
+        q.a = st.base(w.Q[f1]);
+        q.u_mid = w.Q[f0];
+        q.two_steps = two;
+        q.inj_t1 = -1;
+        q.a.inj_t = -1;
+        if (p->nrec > 0) {
+            q.inj_e = w.rec_e;
+            q.inj_t1 = k - 1;
+            q.a.inj = w.rec;
+            q.a.inj_val = dtraces;
+            q.a.inj_np = p->nrec; q.a.inj_nt = p->nt; q.a.inj_t = two ? k - 2 : -1;
+            q.a.inj_scale = 1.f;
+            q.a.inj_times_m = 1;
+        }
+        q.smp_t1 = -1;
+        q.a.smp_t = -1;
+        if (grad_wavelet && p->nsrc > 0 && k <= p->nt - 1) {
+            q.a.smp = w.src;
+            q.a.smp_out = grad_wavelet;
+            q.a.smp_np = p->nsrc; q.a.smp_nt = p->nt;
+            q.a.smp_scale = p->src_scale;
+            q.a.smp_div_m = 1;
+            q.smp_t1 = k;
+            q.a.smp_t = two ? k - 1 : -1;
+        }
+        int mode = MODE_PLAIN;
+        const CUtensorMap* l1 = &none;
+        const CUtensorMap* l2 = &none;
+        if (grad) {
+            mode = MODE_GRAD;
+            q.a.grad = w.G;
+            q.a.lap_bf16 = p->lap_bf16;
+            l1 = &lm[k - k0];
+            if (two) l2 = &lm[k - 1 - k0];
+        }
+        const int r = st.launch_k2(mode, qu[ql.cur], qo[ql.old_], *l1, *l2, q);
+        ql.advance(two, f0, f1);
+        return r;
+    };
+
+    {
+        PhaseScope scope(PH_ADJOINT, s, 1);
+        if ((rc = adjoint(p->nt, false, false, 0))) return rc;  // q_nt: its gradient term is 0
+    }
+    for (int j = g.nseg - 1; j >= 0; --j) {
+        const int k0 = j * g.K, k1 = std::min(p->nt, k0 + g.K);
+        if (j != g.nseg - 1) {
+            PhaseScope scope(PH_RECOMPUTE, s, (k1 - k0 + 1) / 2);
+            const unsigned char* slot = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
+            WFD_CUDA(launch_unpack(slot, w.P[0], n_all, p->ckpt_format, s));
+            WFD_CUDA(launch_unpack(slot + L.ckpt_field_bytes, w.P[1], n_all, p->ckpt_format, s));
+            Levels lv{0, 1};
+            for (int k = k0; k < k1;) {
+                const bool two = k + 1 < k1;
+                int f0, f1;
+                lv.free_pair(f0, f1);
+                Step2Args q{};
+                q.a = st.base(w.P[f1]);
+                q.u_mid = w.P[f0];
+                q.two_steps = two;
+                q.inj_t1 = -1;
+                q.a.inj_t = -1;
+                if (p->nsrc > 0) {
+                    q.inj_e = w.src_e;
+                    q.inj_t1 = k;
+                    q.a.inj = w.src;
+                    q.a.inj_val = wavelet;
+                    q.a.inj_np = p->nsrc; q.a.inj_nt = p->nt; q.a.inj_t = two ? k + 1 : -1;
+                    q.a.inj_scale = p->src_scale;
+                }
+                q.smp_t1 = -1;
+                q.a.smp_t = -1;
+                q.lap1 = w.lap + (size_t)(k - k0) * L.lap_field_bytes;
+                if (two) q.a.lap = w.lap + (size_t)(k + 1 - k0) * L.lap_field_bytes;
+                q.a.lap_bf16 = p->lap_bf16;
+                if ((rc = st.launch_k2(MODE_SAVE_LAP, pu[lv.cur], po[lv.old_], none, none, q))) return rc;
+                lv.advance(two, f0, f1);
+                k += two ? 2 : 1;
+            }
+        }
+        PhaseScope scope(PH_ADJOINT, s, (k1 - std::max(k0, 1) + 1) / 2);
+        const int kmin = std::max(k0, 1);
+        for (int k = k1 - 1; k >= kmin;) {
+            const bool two = k - 1 >= kmin;
+            if ((rc = adjoint(k, two, true, k0))) return rc;
+            k -= two ? 2 : 1;
+        }
+    }
+    if (grad_wavelet && p->nsrc > 0)  // q_1 at the sources -> d J / d w_0
+        WFD_CUDA(launch_gather(w.Q[ql.cur], g.cells, w.src, g.ntiles, p->nshot, p->nsrc, w.m,
+                               p->src_scale, 1, grad_wavelet, p->nt, 0, s));
+    if (finalize) WFD_CUDA(launch_grad_finalize(w.G, vel, grad_vel, g.nz, g.ny, g.nx, g.ld, g.R, s));
+    return WFD_OK;
+}
+
 // Adjoint of one (group of) shots. zero_G starts a new gradient sum; finalize
 // turns the sum into dJ/dv (the last group of a grouped call).
 int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                  const Stepper& st, const float* wavelet, const float* dtraces, float* grad_vel,
                  float* grad_wavelet, const float* vel, bool zero_G = true, bool finalize = true) {
+    if (g.sb == 2)
+        return run_backward_k2(p, g, L, w, st, wavelet, dtraces, grad_vel, grad_wavelet, vel, zero_G,
+                               finalize);
     cudaStream_t s = st.s;
     WFD_CUDA(cudaMemsetAsync(w.Q[0], 0, L.field_bytes, s));
     WFD_CUDA(cudaMemsetAsync(w.Q[1], 0, L.field_bytes, s));

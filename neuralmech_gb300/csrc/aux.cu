@@ -31,9 +31,16 @@ __device__ __forceinline__ bool decode(const int32_t* pos, int nz, int ny, int n
     return zok && yok && xok;
 }
 
+// Range of tiles (along one axis) whose region [t*T - h, (t+1)*T + h) holds v.
+__device__ __forceinline__ void tile_span(int v, int T, int h, int ntile, int& lo, int& hi) {
+    lo = v - h >= 0 ? (v - h) / T : 0;                  // smallest t with (t+1) T + h > v
+    hi = min(ntile - 1, (v + h) / T);                   // largest t with t T - h <= v
+    if (h == 0) lo = hi = v / T;
+}
+
 __global__ void count_kernel(const int32_t* __restrict__ pos, int nshot, int np, int nz, int ny,
                              int nx, int R, int tz, int ty, int tx, int tiles_y, int tiles_x,
-                             int ntiles, int* counts, unsigned* err) {
+                             int ntiles, int* counts, unsigned* err, int hz, int hx) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= (long long)nshot * np) return;
     const int s = int(i / np);
@@ -42,8 +49,14 @@ __global__ void count_kernel(const int32_t* __restrict__ pos, int nshot, int np,
         report(err, DEV_ERR_BAD_POSITION);
         return;
     }
-    const int t = ((z / tz) * tiles_y + (y / ty)) * tiles_x + (x / tx);
-    atomicAdd(&counts[(long long)s * ntiles + t], 1);
+    int zl, zh, xl, xh;
+    tile_span(z, tz, hz, (nz + tz - 1) / tz, zl, zh);
+    tile_span(x, tx, hx, tiles_x, xl, xh);
+    for (int a = zl; a <= zh; ++a)
+        for (int b = xl; b <= xh; ++b) {
+            const int t = (a * tiles_y + (y / ty)) * tiles_x + b;
+            atomicAdd(&counts[(long long)s * ntiles + t], 1);
+        }
 }
 
 // Exclusive scan of counts into off[0..n] in one block; counts reset to 0 so
@@ -74,15 +87,22 @@ __global__ void scan_kernel(int* counts, int* off, int n) {
 
 __global__ void fill_kernel(const int32_t* __restrict__ pos, int nshot, int np, int nz, int ny,
                             int nx, int ld, int R, int tz, int ty, int tx, int tiles_y,
-                            int tiles_x, int ntiles, int* cursor, const int* off, int2* ent) {
+                            int tiles_x, int ntiles, int* cursor, const int* off, int2* ent, int hz,
+                            int hx) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= (long long)nshot * np) return;
     const int s = int(i / np), p = int(i % np);
     int z, y, x;
     if (!decode(pos + 3 * i, nz, ny, nx, R, z, y, x)) return;
-    const long long key = (long long)s * ntiles + ((z / tz) * tiles_y + (y / ty)) * tiles_x + x / tx;
-    const int slot = off[key] + atomicAdd(&cursor[key], 1);
-    ent[slot] = make_int2(int(((long long)z * ny + y) * ld + x), p);
+    int zl, zh, xl, xh;
+    tile_span(z, tz, hz, (nz + tz - 1) / tz, zl, zh);
+    tile_span(x, tx, hx, tiles_x, xl, xh);
+    for (int a = zl; a <= zh; ++a)
+        for (int b = xl; b <= xh; ++b) {
+            const long long key = (long long)s * ntiles + (a * tiles_y + (y / ty)) * tiles_x + b;
+            const int slot = off[key] + atomicAdd(&cursor[key], 1);
+            ent[slot] = make_int2(int(((long long)z * ny + y) * ld + x), p);
+        }
 }
 
 __global__ void gather_kernel(const float* __restrict__ u, long long shot_stride, const int* off,
@@ -220,7 +240,7 @@ cudaError_t launch_vel_to_m(const float* vel, float* m, int nz, int ny, int nx, 
 cudaError_t launch_build_lists(const int32_t* pos, int nshot, int np, int nz, int ny, int nx,
                                int ld, int R, int tile_z, int tile_y, int tile_x, int tiles_z,
                                int tiles_y, int tiles_x, int* counts, int* off, int2* ent,
-                               unsigned* err, cudaStream_t s) {
+                               unsigned* err, cudaStream_t s, int halo_z, int halo_x) {
     const int ntiles = tiles_z * tiles_y * tiles_x;
     const long long nkeys = (long long)nshot * ntiles;
     cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * nkeys, s);
@@ -229,14 +249,15 @@ cudaError_t launch_build_lists(const int32_t* pos, int nshot, int np, int nz, in
     const int blocks = int((npts + 255) / 256);
     if (npts > 0) {
         count_kernel<<<blocks, 256, 0, s>>>(pos, nshot, np, nz, ny, nx, R, tile_z, tile_y, tile_x,
-                                            tiles_y, tiles_x, ntiles, counts, err);
+                                            tiles_y, tiles_x, ntiles, counts, err, halo_z, halo_x);
         count_launch();
     }
     scan_kernel<<<1, 1024, 0, s>>>(counts, off, int(nkeys));
     count_launch();
     if (npts > 0) {
         fill_kernel<<<blocks, 256, 0, s>>>(pos, nshot, np, nz, ny, nx, ld, R, tile_z, tile_y,
-                                           tile_x, tiles_y, tiles_x, ntiles, counts, off, ent);
+                                           tile_x, tiles_y, tiles_x, ntiles, counts, off, ent, halo_z,
+                                           halo_x);
         count_launch();
     }
     return cudaGetLastError();

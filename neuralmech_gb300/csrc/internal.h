@@ -84,6 +84,33 @@ cudaError_t launch_step2d(int R, int mode, int tile_rows, const CUtensorMap& map
                           const CUtensorMap& map_old, const CUtensorMap& map_lap, const StepArgs& a,
                           cudaStream_t s);
 
+// ---------------------------------------------------------------- 2D, two steps per launch
+// Tile T = K2_TX x K2_TZ cells; u_n is staged on T plus 2R rows / 8 columns
+// (K2_UW wide), u_{n-1} and m on E = T plus R rows / 4 columns (K2_EW wide).
+constexpr int K2_TX = 120;
+constexpr int K2_TZ = 32;
+constexpr int K2_EW = K2_TX + 8;
+constexpr int K2_UW = K2_TX + 16;
+constexpr int K2_THREADS = 256;
+
+struct Step2Args {
+    StepArgs a;         // step 2: u_new = u_{n+2}, inj/inj_t (tile lists), smp/smp_t
+                        // (samples u_{n+1}), lap (its L u store); a.smp also serves step 1
+    float* u_mid;       // u_{n+1} output on the tile
+    PointLists inj_e;   // step-1 injection: points inside the tile's extended region E
+    int inj_t1;         // step-1 injection time index (-1: none)
+    int smp_t1;         // step-1 sampling time index of u_n (-1: none)
+    void* lap1;         // step-1 L u store (MODE_SAVE_LAP)
+    int two_steps;      // 0: step 1 only (u_{n+1} to u_mid)
+};
+
+// map_u: u_n (box K2_UW x (K2_TZ + 4R) x 1); map_o: u_{n-1} (box K2_EW x (K2_TZ + 2R) x 1);
+// map_m: m (2D, box K2_EW x (K2_TZ + 2R)); map_l1 / map_l2: stored L u of the two
+// steps (box K2_TX x K2_TZ x 1, MODE_GRAD).
+cudaError_t launch_step2d_k2(int R, int mode, const CUtensorMap& map_u, const CUtensorMap& map_o,
+                             const CUtensorMap& map_m, const CUtensorMap& map_l1,
+                             const CUtensorMap& map_l2, const Step2Args& p, cudaStream_t s);
+
 // ---------------------------------------------------------------- 3D tiles
 // One CTA (one shot) marches along z through a (TY x TX) column of the grid
 // for T3_ZCHUNK output planes; a thread owns 4 x cells and keeps the 2R + 1
@@ -113,10 +140,13 @@ int set_error(int status, const char* message);
 // ---------------------------------------------------------------- helpers (aux.cu)
 cudaError_t launch_vel_to_m(const float* vel, float* m, int nz, int ny, int nx, int ld,
                             float scale, cudaStream_t s);
+// Per-(shot, tile) point lists. With halo_z / halo_x > 0 a point joins every
+// tile whose region grown by that halo contains it (at most 4 in 2D); ent must
+// then hold 4 entries per point.
 cudaError_t launch_build_lists(const int32_t* pos, int nshot, int np, int nz, int ny, int nx,
                                int ld, int R, int tile_z, int tile_y, int tile_x, int tiles_z,
                                int tiles_y, int tiles_x, int* counts, int* off, int2* ent,
-                               unsigned* err, cudaStream_t s);
+                               unsigned* err, cudaStream_t s, int halo_z = 0, int halo_x = 0);
 cudaError_t launch_gather(const float* u, long long shot_stride, PointLists lists, int ntiles,
                           int nshot, int np, const float* m, float scale, int div_m,
                           float* out, int out_nt, int out_t, cudaStream_t s);

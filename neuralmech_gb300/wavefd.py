@@ -58,6 +58,7 @@ class Grid:
              autograd) in sequential groups of this many, sharing one workspace
              sized for a group (0 = all at once)
     tile_rows    2D tile height, 16 or 32 rows (0 = 32)
+    step_block   2D time steps per kernel launch, 1 or 2 (0 = 1)
     """
     shape: tuple
     spacing: tuple
@@ -73,6 +74,7 @@ class Grid:
     shots_per_cta: int = 0
     group_shots: int = 0
     tile_rows: int = 0
+    step_block: int = 0
 
     @property
     def ndim(self) -> int:
@@ -142,7 +144,7 @@ def _problem(grid: Grid, nshot: int, nsrc: int, nrec: int, vmax: float) -> _lib.
         dz, dy, dx = grid.spacing
     return _lib.Problem(grid.ndim, grid.order, nz, ny, nx, nshot, grid.nt, nsrc, nrec,
                         grid.ckpt_every, CKPT_FORMATS[grid.ckpt_format], int(grid.lap_bf16),
-                        grid.shots_per_cta, grid.group_shots, grid.tile_rows, grid.dt, dz, dy, dx, grid.src_scale, vmax)
+                        grid.shots_per_cta, grid.group_shots, grid.tile_rows, grid.step_block, grid.dt, dz, dy, dx, grid.src_scale, vmax)
 
 
 # ---------------------------------------------------------------- argument prep

@@ -132,3 +132,32 @@ def test_forward_3d_matches_oracle(cuda, orc, order, shape, nshot, sponge):
     ref = orc.forward(oracle_geometry(orc, grid, v, wav, src, rec))
     assert np.abs(ref).max() > 0
     assert rel_l2(traces.cpu().numpy(), ref) < 1e-5
+
+
+@pytest.mark.parametrize("order", [2, 4, 8])
+@pytest.mark.parametrize("shape,nshot,nt,sponge", [
+    ((70, 250), 3, 91, 8),    # odd step count: a one-step launch at the end
+    ((40, 130), 2, 60, 0),
+    ((100, 370), 4, 75, (5, 11)),
+])
+def test_forward_two_step_blocking(cuda, orc, order, shape, nshot, nt, sponge):
+    """step_block=2 (two steps per launch, u_{n+1} kept in shared memory) against
+    the FP64 oracle; sources and receivers sit on and around tile seams, where
+    the injections of neighbouring tiles' extended regions must agree."""
+    from neuralmech_gb300 import wave_forward
+    grid, v, wav, src, rec = small_problem(shape=shape, nshot=nshot, nt=nt, order=order,
+                                           sponge=sponge if isinstance(sponge, int) else [sponge, sponge],
+                                           nsrc=3, nrec=20, step_block=2, seed=order * 3 + nshot)
+    R = order // 2
+    seams_x = [x for x in (116, 117, 119, 120, 121, 123, 124, 239, 240, 243) if R <= x < shape[1] - R]
+    seams_z = [z for z in (28, 29, 31, 32, 33, 35, 36, 63, 64, 65) if R <= z < shape[0] - R]
+    for s in range(nshot):
+        for i in range(3):
+            src[s, i] = [seams_z[(s + i) % len(seams_z)], seams_x[(2 * s + i) % len(seams_x)]]
+        for i in range(min(10, rec.shape[1])):
+            rec[s, i] = [seams_z[(i + s) % len(seams_z)], seams_x[(i * 3 + s) % len(seams_x)]]
+    traces = wave_forward(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
+                          torch.from_numpy(src), torch.from_numpy(rec), grid)
+    ref = orc.forward(oracle_geometry(orc, grid, v, wav, src, rec))
+    assert np.abs(ref).max() > 0
+    assert rel_l2(traces.cpu().numpy(), ref) < 1e-5

@@ -2,8 +2,9 @@
 
 For a problem key (architecture, grid shape, order, shots) it times a short
 forward (`steps` time steps) for every candidate:
-  * tile_rows (16 or 32);
-  * shots_per_cta (1, 2, 4, ... up to 32 and the shot count).
+  * one step per launch: tile_rows (16 or 32) x shots_per_cta (1, 2, 4, ...
+    up to 32 and the shot count);
+  * two steps per launch (step_block 2, 120 x 32 tiles, one shot per CTA).
 
 It keeps the fastest, and caches the choice in a JSON file (default
 ``~/.cache/neuralmech_gb300/autotune.json``, or ``$WAVEFD_AUTOTUNE_CACHE``).
@@ -50,7 +51,8 @@ def candidates(nshot: int):
     spcs = [s for s in (1, 2, 4, 8, 16, 32) if s <= max(1, nshot)]
     if nshot <= 32 and nshot not in spcs:
         spcs.append(nshot)
-    return [{"tile_rows": tr, "shots_per_cta": s} for tr in (32, 16) for s in spcs]
+    one = [{"tile_rows": tr, "shots_per_cta": s, "step_block": 1} for tr in (32, 16) for s in spcs]
+    return one + [{"tile_rows": 0, "shots_per_cta": 0, "step_block": 2}]
 
 
 def select(timings: dict) -> dict:
@@ -61,11 +63,11 @@ def select(timings: dict) -> dict:
 
 def tune(grid, nshot: int, vel=None, steps: int = 16, device=None, path: str | None = None,
          timer=None, refresh: bool = False) -> dict:
-    """Best {tile_rows, shots_per_cta} for `grid` with `nshot` shots (2D).
+    """Best {tile_rows, shots_per_cta, step_block} for `grid` with `nshot` shots (2D).
 
     `timer(config) -> seconds` replaces the GPU timing (used by tests)."""
     if grid.ndim != 2:
-        return {"tile_rows": 0, "shots_per_cta": 0}
+        return {"tile_rows": 0, "shots_per_cta": 0, "step_block": 0}
     import torch
     path = path or cache_path()
     arch = "cpu-timer" if timer else torch.cuda.get_device_name(device)
@@ -114,6 +116,6 @@ def _gpu_timer(grid, nshot, vel, steps, device):
 
 
 def tuned(grid, nshot: int, **kw):
-    """`grid` with its tile_rows / shots_per_cta replaced by the tuned choice."""
+    """`grid` with tile_rows / shots_per_cta / step_block replaced by the tuned choice."""
     best = tune(grid, nshot, **kw)
     return dataclasses.replace(grid, **best) if grid.ndim == 2 else grid

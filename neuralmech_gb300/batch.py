@@ -63,7 +63,8 @@ class BatchFWI:
             self.models.append(_Model(call, obs, _workspace(call, True), torch.empty_like(call.vel),
                                       torch.zeros((), dtype=torch.float64, device=self.device),
                                       torch.cuda.Stream(device=self.device)))
-        self.configs = [(x.call.grid.tile_rows, x.call.grid.shots_per_cta) for x in self.models]
+        self.configs = [(x.call.grid.tile_rows, x.call.grid.shots_per_cta, x.call.grid.step_block)
+                        for x in self.models]
         self.graph = None
         self._launch()  # eager run: sets kernel attributes, validates arguments
         torch.cuda.synchronize(self.device)

@@ -93,8 +93,26 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
             if (two) tma_load_3d(const_cast<unsigned char*>(L2), &map_l2, x0, z0, s, bar);
         }
     }
-    // per-thread constants while the tiles land
+    // per-thread constants and point-list ranges while the tiles land: every
+    // global read the CTA depends on is issued here, before the TMA wait
+    __shared__ int2 rng[4];  // sampling, step-1 (extended) injection, step-2 injection
+    if (tid < 3) {
+        const PointLists& pl = tid == 0 ? a.smp : tid == 1 ? p.inj_e : a.inj;
+        const int k = s * ntiles + tile;
+        rng[tid] = pl.off != nullptr ? make_int2(pl.off[k], pl.off[k + 1]) : make_int2(0, 0);
+    }
     const int ex = x0 - 4 + 4 * lane;  // global x of this lane's first E column
+    float gz1[L::RB1], gz2[L::RB2];
+#pragma unroll
+    for (int r = 0; r < L::RB1; ++r) {
+        const int z = z0 - R + warp * L::RB1 + r;
+        gz1[r] = (a.gz != nullptr && z >= 0 && z < a.nz) ? __ldg(a.gz + z) : 1.f;
+    }
+#pragma unroll
+    for (int r = 0; r < L::RB2; ++r) {
+        const int z = z0 + warp * L::RB2 + r;
+        gz2[r] = (a.gz != nullptr && z < a.nz) ? __ldg(a.gz + z) : 1.f;
+    }
     float gxe[4];
     bool xin[4];
 #pragma unroll
@@ -110,6 +128,7 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
     const long long lap_shot = (long long)s * a.shot_stride;
 
     if (!mbar_wait(bar, 0)) report(a.err, DEV_ERR_TMA_TIMEOUT);
+    __syncthreads();  // rng visible to every thread
 
     // ---------------------------------------------------------------- step 1 on E
     {
@@ -132,7 +151,7 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
             const float4 ov = f4(orow);
             const float4 mv = f4(M + er * K2_EW + 4 * lane);
             const bool zin = z >= R && z < a.nz - R;
-            const float gz = (a.gz != nullptr && z >= 0 && z < a.nz) ? __ldg(a.gz + z) : 1.f;
+            const float gz = gz1[r];
             float nv[4], lap[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -162,8 +181,8 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
         }
     }
     // sampling of u_n (receivers owned by this tile)
-    if (p.smp_t1 >= 0 && a.smp.off != nullptr) {
-        const int lo = a.smp.off[s * ntiles + tile], hi = a.smp.off[s * ntiles + tile + 1];
+    if (p.smp_t1 >= 0) {
+        const int lo = rng[0].x, hi = rng[0].y;
         for (int j = lo + tid; j < hi; j += K2_THREADS) {
             const int2 en = a.smp.ent[j];
             const int z = en.x / a.ld, xx = en.x - z * a.ld;
@@ -174,8 +193,8 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
     }
     __syncthreads();  // u_{n+1} on E complete in O
     // injection of step n into u_{n+1}, every point inside E (neighbours' too)
-    if (p.inj_e.off != nullptr && p.inj_t1 >= 0) {
-        const int lo = p.inj_e.off[s * ntiles + tile], hi = p.inj_e.off[s * ntiles + tile + 1];
+    if (p.inj_t1 >= 0 && rng[1].y > rng[1].x) {
+        const int lo = rng[1].x, hi = rng[1].y;
         for (int j = lo + tid; j < hi; j += K2_THREADS) {
             const int2 en = p.inj_e.ent[j];
             const int z = en.x / a.ld, xx = en.x - z * a.ld;
@@ -230,7 +249,7 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
             const float4 lv = f4(nrow - 4), rv = f4(nrow + 4);
             const float w[12] = {lv.x, lv.y, lv.z, lv.w, c1.x, c1.y, c1.z, c1.w, rv.x, rv.y, rv.z, rv.w};
             const float4 mv = f4(M + er * K2_EW + 4 * lane);
-            const float gz = (a.gz != nullptr && z < a.nz) ? __ldg(a.gz + z) : 1.f;
+            const float gz = gz2[r];
             float nv[4], lap[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -277,8 +296,8 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
     }
     if (two) {
         // sampling of u_{n+1} (receivers of this tile), from shared memory
-        if (a.smp_t >= 0 && a.smp.off != nullptr) {
-            const int lo = a.smp.off[s * ntiles + tile], hi = a.smp.off[s * ntiles + tile + 1];
+        if (a.smp_t >= 0) {
+            const int lo = rng[0].x, hi = rng[0].y;
             for (int j = lo + tid; j < hi; j += K2_THREADS) {
                 const int2 en = a.smp.ent[j];
                 const int z = en.x / a.ld, xx = en.x - z * a.ld;
@@ -288,8 +307,8 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
             }
         }
         __syncthreads();  // every u_{n+2} store of the tile is done
-        if (a.inj.off != nullptr && a.inj_t >= 0) {
-            const int lo = a.inj.off[s * ntiles + tile], hi = a.inj.off[s * ntiles + tile + 1];
+        if (a.inj_t >= 0) {
+            const int lo = rng[2].x, hi = rng[2].y;
             for (int j = lo + tid; j < hi; j += K2_THREADS) {
                 const int2 en = a.inj.ent[j];
                 const int z = en.x / a.ld, xx = en.x - z * a.ld;

@@ -83,14 +83,20 @@ def test_autotune_selection_and_cache(tmp_path):
 
     def fake(cfg):
         calls.append(cfg)
+        if cfg["step_block"] == 2:
+            return 9.0
         return abs(cfg["shots_per_cta"] - 4) + (0.5 if cfg["tile_rows"] == 32 else 0.0) + 1.0
 
     path = str(tmp_path / "cache.json")
     best = autotune.tune(g, 12, timer=fake, path=path)
-    assert best == {"tile_rows": 16, "shots_per_cta": 4}
+    assert best == {"tile_rows": 16, "shots_per_cta": 4, "step_block": 1}
     n = len(calls)
     assert n == len(autotune.candidates(12))
     assert autotune.tune(g, 12, timer=fake, path=path) == best and len(calls) == n
     assert autotune.tune(g, 12, timer=fake, path=path, refresh=True) == best and len(calls) == 2 * n
     g3 = Grid((32, 32, 32), (10.0,) * 3, 1e-3, 10)
-    assert autotune.tune(g3, 4, timer=fake, path=path) == {"tile_rows": 0, "shots_per_cta": 0}
+    assert autotune.tune(g3, 4, timer=fake, path=path) == {"tile_rows": 0, "shots_per_cta": 0, "step_block": 0}
+    # a faster two-step candidate wins
+    best2 = autotune.tune(Grid((64, 512), (10.0, 10.0), 1e-3, 10), 2, path=path,
+                          timer=lambda c: 0.5 if c["step_block"] == 2 else 1.0)
+    assert best2["step_block"] == 2

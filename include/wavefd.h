@@ -146,6 +146,32 @@ int wfd_forward_static(const wfd_problem* p, const float* vel, const float* spon
                        const float* sponge_y, const float* sponge_x, const float* wavelet,
                        const int32_t* src, const int32_t* rec, float* traces, void* stream);
 
+/*
+ * Analytic signal h = x + i H[x] of `ntraces` traces of `nt` samples each
+ * (traces [ntraces][nt] FP32 -> out [ntraces][nt] interleaved (re, im) FP32).
+ * H is the periodic discrete Hilbert transform, the one scipy.signal.hilbert
+ * applies through its FFT, given as the circular-convolution kernel
+ * hilbert_kernel[nt], g = ifft(-i sign(k)) (sign 0 at k = 0 and, for even nt,
+ * at nt / 2). Replaces the cupyx.scipy.signal.hilbert call of
+ * projects/18_fwi/2D_tfm.py:37 for the delay and sum below. nt <= 18000.
+ */
+int wfd_analytic_signal(const float* traces, int64_t ntraces, int nt, const float* hilbert_kernel,
+                        float* out, void* stream);
+
+/*
+ * Total focusing method (projects/18_fwi/tfm.py:12-36, tfm_kernel): for each of
+ * npix pixels (xp, yp),
+ *   image = | sum_e sum_r h_er((t0 + |p - x_e| / c + |p - x_r| / c) / dt) |,
+ * h [E][E][nt] interleaved complex FP32 analytic traces (emitter, receiver,
+ * sample), x_e = (xe[e], ye[e]), linear interpolation in time, pairs whose
+ * sample index reaches nt - 1 skipped. reciprocity = 1 sums the upper triangle
+ * r >= e with weight 2 off the diagonal, as the reference kernel does (valid
+ * when h_er = h_re). E <= 256.
+ */
+int wfd_tfm(const float* h, int E, const float* xe, const float* ye, int nt, float dt, float t0,
+            float c, const float* xp, const float* yp, int npix, int reciprocity, float* image,
+            void* stream);
+
 /* Synchronises `stream`, returns the first device-side error recorded in the
  * workspace since the last call (WFD_ERR_TIMEOUT, WFD_ERR_POSITION) or 0, and
  * clears it. */

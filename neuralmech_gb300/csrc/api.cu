@@ -1031,6 +1031,31 @@ int wfd_sum_sq(const float* x, int64_t n, double* out, void* stream) {
     return WFD_OK;
 }
 
+int wfd_analytic_signal(const float* traces, int64_t ntraces, int nt, const float* hilbert_kernel,
+                        float* out, void* stream) {
+    if (!traces || !hilbert_kernel || !out) return fail(WFD_ERR_INVALID, "NULL argument");
+    if (ntraces < 0 || nt < 2 || nt > 18000) return fail(WFD_ERR_INVALID, "need 2 <= nt <= 18000");
+    if (ntraces == 0) return WFD_OK;
+    if (ntraces > 0x7fffffffLL) return fail(WFD_ERR_INVALID, "too many traces");
+    if (reinterpret_cast<uintptr_t>(out) % 8) return fail(WFD_ERR_INVALID, "out must be 8-byte aligned");
+    WFD_CUDA(launch_analytic(traces, ntraces, nt, hilbert_kernel, reinterpret_cast<float2*>(out),
+                             static_cast<cudaStream_t>(stream)));
+    return WFD_OK;
+}
+
+int wfd_tfm(const float* h, int E, const float* xe, const float* ye, int nt, float dt, float t0,
+            float c, const float* xp, const float* yp, int npix, int reciprocity, float* image,
+            void* stream) {
+    if (!h || !xe || !ye || !xp || !yp || !image) return fail(WFD_ERR_INVALID, "NULL argument");
+    if (E < 1 || E > 256 || nt < 2 || npix < 0) return fail(WFD_ERR_INVALID, "need 1 <= E <= 256, nt >= 2");
+    if (!(dt > 0) || !(c > 0)) return fail(WFD_ERR_INVALID, "dt and c must be positive");
+    if (reinterpret_cast<uintptr_t>(h) % 8) return fail(WFD_ERR_INVALID, "h must be 8-byte aligned");
+    if (npix == 0) return WFD_OK;
+    WFD_CUDA(launch_tfm(reinterpret_cast<const float2*>(h), E, xe, ye, nt, dt, t0, c, xp, yp, npix,
+                        reciprocity, image, static_cast<cudaStream_t>(stream)));
+    return WFD_OK;
+}
+
 int wfd_step2d_order2(const float* u0, const float* u1, float* u2, float wavespeed, float dt,
                       float dx, float dy, int N, int M, int M_padded, void* stream) {
     if (!u0 || !u1 || !u2) return fail(WFD_ERR_INVALID, "NULL field");

@@ -161,4 +161,11 @@ cudaError_t launch_grad_finalize(const float* G, const float* vel, float* grad_v
                                  int ny, int nx, int ld, int R, cudaStream_t s);
 cudaError_t launch_sum_sq(const float* x, long long n, double* out, cudaStream_t s);
 
+// ---------------------------------------------------------------- imaging (imaging.cu)
+cudaError_t launch_analytic(const float* traces, long long ntr, int nt, const float* g, float2* h,
+                            cudaStream_t s);
+cudaError_t launch_tfm(const float2* h, int E, const float* xe, const float* ye, int nt, float dt,
+                       float t0, float c, const float* xp, const float* yp, int P, int reciprocity,
+                       float* image, cudaStream_t s);
+
 }  // namespace wfd

@@ -34,8 +34,12 @@ def orc():
 
 
 def rel_l2(a, b):
-    a = np.asarray(a, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
+    a = np.asarray(a)
+    b = np.asarray(b)
+    if np.iscomplexobj(a) or np.iscomplexobj(b):
+        a, b = a.astype(np.complex128), b.astype(np.complex128)
+    else:
+        a, b = a.astype(np.float64), b.astype(np.float64)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 

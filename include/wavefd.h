@@ -98,6 +98,18 @@ int wfd_forward(const wfd_problem* p, const float* vel, const float* sponge_z,
                 void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * wfd_forward without checkpoints that also returns the final wavefield
+ * u_final [nshot][nz][ny][nx] (u_nt of every shot, the fixed ring included):
+ * cuwave `simulate(sim, source, indicator)` returning the field
+ * (projects/18_fwi/2D_scalar_wave_forward_B_hai.py:30). Workspace as for
+ * wfd_forward(save_checkpoints = 0); no shot groups.
+ */
+int wfd_forward_final(const wfd_problem* p, const float* vel, const float* sponge_z,
+                      const float* sponge_y, const float* sponge_x, const float* wavelet,
+                      const int32_t* src, const int32_t* rec, float* traces, float* u_final,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * Adjoint of the forward above for a trace cotangent `dtraces`
  * ([nshot][nt][nrec]): grad_vel [nz][ny][nx] = (dF/dvel)^T dtraces (summed over
  * shots; 0 on the fixed ring) and, when grad_wavelet is not NULL,

@@ -517,16 +517,20 @@ int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
 }
 
 int run_forward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
-                   const Stepper& st, const float* wavelet, float* traces, bool save);
+                   const Stepper& st, const float* wavelet, float* traces, bool save,
+                   int* final_buf);
 int run_backward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                     const Stepper& st, const float* wavelet, const float* dtraces, float* grad_vel,
                     float* grad_wavelet, const float* vel, bool zero_G, bool finalize);
 
 // Forward time loop. With save: checkpoints every K steps and the L u store of
 // the last segment (which the backward then does not recompute).
+// final_buf (optional) receives the index of the buffer that holds u_nt.
 int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
-                const Stepper& st, const float* wavelet, float* traces, bool save) {
-    if (g.sb == 2) return run_forward_k2(p, g, L, w, st, wavelet, traces, save);
+                const Stepper& st, const float* wavelet, float* traces, bool save,
+                int* final_buf = nullptr) {
+    if (g.sb == 2) return run_forward_k2(p, g, L, w, st, wavelet, traces, save, final_buf);
+    if (final_buf) *final_buf = p->nt & 1;
     cudaStream_t s = st.s;
     WFD_CUDA(cudaMemsetAsync(w.P[0], 0, L.field_bytes, s));
     WFD_CUDA(cudaMemsetAsync(w.P[1], 0, L.field_bytes, s));
@@ -592,7 +596,8 @@ struct Levels {
 };
 
 int run_forward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
-                   const Stepper& st, const float* wavelet, float* traces, bool save) {
+                   const Stepper& st, const float* wavelet, float* traces, bool save,
+                   int* final_buf) {
     cudaStream_t s = st.s;
     for (int b = 0; b < 4; ++b) WFD_CUDA(cudaMemsetAsync(w.P[b], 0, L.field_bytes, s));
     CUtensorMap mu[4], mo[4], none{};
@@ -650,6 +655,7 @@ int run_forward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const W
     if (traces && p->nrec > 0)
         WFD_CUDA(launch_gather(w.P[lv.cur], g.cells, w.rec, g.ntiles, p->nshot, p->nrec, nullptr, 1.f, 0,
                                traces, p->nt, p->nt - 1, s));
+    if (final_buf) *final_buf = lv.cur;
     return WFD_OK;
 }
 
@@ -916,6 +922,30 @@ int wfd_forward(const wfd_problem* p, const float* vel, const float* sponge_z,
                               save_checkpoints != 0)))
             return rc;
     }
+    return WFD_OK;
+}
+
+int wfd_forward_final(const wfd_problem* p, const float* vel, const float* sponge_z,
+                      const float* sponge_y, const float* sponge_x, const float* wavelet,
+                      const int32_t* src, const int32_t* rec, float* traces, float* u_final,
+                      void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = common_checks(p, vel, wavelet, src, rec);
+    if (rc) return rc;
+    if (!u_final) return fail(WFD_ERR_INVALID, "u_final is NULL");
+    if (group_size(p) < p->nshot) return fail(WFD_ERR_INVALID, "no shot groups with u_final");
+    const Geom g = make_geom(p);
+    const Layout L = make_layout(p, g, false);
+    if ((rc = check_workspace(workspace, workspace_bytes, L.total))) return rc;
+    const Work w = carve(workspace, L, false);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if ((rc = setup(p, g, w, vel, src, rec, s))) return rc;
+    Stepper st{p, g, s, w.err, w.m, sponge_z, p->ndim == 3 ? sponge_y : nullptr, sponge_x};
+    if ((rc = st.init())) return rc;
+    int fb = 0;
+    if ((rc = run_forward(p, g, L, w, st, wavelet, traces, false, &fb))) return rc;
+    // strip the row padding: rows of ld floats -> rows of nx floats
+    WFD_CUDA(cudaMemcpy2DAsync(u_final, (size_t)g.nx * 4, w.P[fb], (size_t)g.ld * 4, (size_t)g.nx * 4,
+                               (size_t)p->nshot * g.nz * g.ny, cudaMemcpyDeviceToDevice, s));
     return WFD_OK;
 }
 

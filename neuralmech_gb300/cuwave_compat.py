@@ -1,0 +1,237 @@
+"""cuwave-shaped adapter: the reference drivers' call sequence on this library.
+
+projects/18_fwi (plate.py, helper.py, 2D_fwi.py) and projects/16_neuralopt
+drive the pip package cuwave through a small surface:
+  ScalarWave(Nx, dx, N, dt, threads, precision, space_order, wavespeed, density),
+  line, shots, point_source, Sensors, sineburst, stable_dt, simulate, measure,
+  misfit, misfit_gradient, resample, Adam.
+This module offers the same names and call shapes over PyTorch tensors, with
+every time step in the library's CUDA kernels. cuwave's own equations are
+not available (the package is absent), so the choices below are this
+module's own. They are written here so callers can judge parity:
+
+* Material indicator gamma (the reference's "indicator", 1 = solid, ~1e-4 =
+  void; plate.py:132-137, helper.py:30-43). It scales the stiffness at
+  constant density: c(x) = wavespeed * sqrt(gamma(x)). misfit_gradient returns
+  d misfit / d gamma = d misfit / d c * wavespeed / (2 sqrt(gamma)).
+* Grid. The nodes of ScalarWave((nx, ny), (dx, dy)) sit at x = -dx + i dx
+  (helper.py:240-242: one ghost node outside [0, L] on each side). The library's
+  order-2R stencil holds a ring of R cells fixed, so the adapter pads R - 1
+  more ghost nodes on every side; the physical nodes, the array on the plate
+  edge included, are then updated. Indicators are read where the reference
+  drivers put them, in [:nx, :ny] of an array of shape Nx or larger
+  (helper.py:76-77, 2D_fwi.py:176), and their edge values extend into the
+  margin. Gradients come back in the indicator's shape and place. Nx_padded
+  rounds each axis up to a multiple of 8.
+* Coordinates map to the nearest node, as cuwave's point sources and sensors
+  do. point_source divides the signal by the cell volume dx dy
+  (projects/9_structural_optimization/README.md:87) and scales it by dt^2
+  (the source term of u_tt = c^2 Lap u + f).
+* sineburst(t, A, f, cycles) is a Hann-windowed tone burst
+  A sin(2 pi f t) sin^2(pi f t / cycles) on 0 <= t <= cycles / f.
+* Array axes follow the reference (x first); they map onto the library's
+  (z, x) axes unchanged.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from .wavefd import Grid, misfit_gradient as _misfit_gradient, stable_dt as _stable_dt, wave_forward
+from .wavefd import wave_forward_final
+
+
+@dataclass
+class ScalarWave:
+    """Simulation descriptor (cuwave.scalar.ScalarWave's arguments)."""
+    Nx: tuple
+    dx: tuple
+    N: int
+    dt: float
+    threads: tuple = (4, 128)
+    precision: str = "float32"
+    space_order: int = 2
+    wavespeed: float = 1.0
+    density: float = 1.0
+    damping: int = 0  # sponge width in cells on every face (0: reflecting plate)
+    device: str = "cuda"
+
+    @property
+    def dtype(self):
+        return torch.float32
+
+    @property
+    def margin(self) -> int:
+        return self.space_order // 2 - 1
+
+    @property
+    def grid_shape(self) -> tuple:
+        return tuple(n + 2 * self.margin for n in self.Nx)
+
+    @property
+    def Nx_padded(self) -> tuple:
+        return tuple((n + 7) // 8 * 8 for n in self.grid_shape)
+
+    def grid(self) -> Grid:
+        return Grid(self.grid_shape, tuple(self.dx), self.dt, self.N, order=self.space_order,
+                    sponge=self.damping, src_scale=1.0)
+
+    def node(self, coord) -> tuple:
+        """Nearest node (padded grid index) of a physical coordinate."""
+        return tuple(int(round(c / h)) + 1 + self.margin for c, h in zip(coord, self.dx))
+
+    def velocity(self, indicator) -> torch.Tensor:
+        """c = wavespeed sqrt(gamma) on the padded grid; gamma is read from
+        [:nx, :ny] of the indicator and extends into the margin."""
+        g = torch.as_tensor(indicator, device=self.device, dtype=torch.float32)
+        nx, ny = self.Nx
+        if g.dim() != 2 or g.shape[0] < nx or g.shape[1] < ny:
+            raise ValueError(f"indicator of shape {tuple(g.shape)} does not cover {self.Nx}")
+        g = g[:nx, :ny]
+        m = self.margin
+        if m:
+            g = torch.nn.functional.pad(g[None, None], (m, m, m, m), mode="replicate")[0, 0]
+        return self.wavespeed * torch.sqrt(g.clamp_min(0.0))
+
+
+def stable_dt(dx, c: float, order: int) -> float:
+    return _stable_dt(tuple(dx), c, order)
+
+
+def sineburst(t, amplitude: float, frequency: float, cycles: float) -> np.ndarray:
+    t = np.asarray(t, dtype=np.float64)
+    on = (t >= 0) & (t <= cycles / frequency)
+    s = amplitude * np.sin(2 * math.pi * frequency * t) * np.sin(math.pi * frequency * t / cycles) ** 2
+    return np.where(on, s, 0.0).astype(np.float32)
+
+
+def line(a, b, n: int) -> np.ndarray:
+    """n points evenly spaced from a to b."""
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return a[None, :] + np.linspace(0.0, 1.0, n)[:, None] * (b - a)[None, :]
+
+
+@dataclass
+class Source:
+    nodes: np.ndarray   # (nsrc, 2) padded-grid indices
+    signal: np.ndarray  # (N, nsrc)
+
+
+def point_source(sim: ScalarWave, coords, signal) -> Source:
+    coords = np.atleast_2d(np.asarray(coords, dtype=np.float64))
+    nodes = np.array([sim.node(c) for c in coords], dtype=np.int32)
+    sig = np.asarray(signal, dtype=np.float64).reshape(sim.N, -1)
+    if sig.shape[1] == 1 and len(nodes) > 1:
+        sig = np.repeat(sig, len(nodes), axis=1)
+    vol = float(np.prod(sim.dx))
+    return Source(nodes, (sig * sim.dt * sim.dt / vol).astype(np.float32))
+
+
+class _SourceList(list):
+    def __getitem__(self, i):
+        r = super().__getitem__(i)
+        return _SourceList(r) if isinstance(i, slice) else r
+
+
+def shots(sim: ScalarWave, coords, signal):
+    """One point source per coordinate (every element fires once)."""
+    return _SourceList(point_source(sim, c, signal) for c in np.asarray(coords))
+
+
+@dataclass
+class Sensors:
+    sim: ScalarWave
+    coords: np.ndarray
+    nodes: np.ndarray = field(init=False)
+
+    def __post_init__(self):
+        self.nodes = np.array([self.sim.node(c) for c in np.atleast_2d(self.coords)], dtype=np.int32)
+
+
+def _batch(sim, sources, sensors):
+    srcs = list(sources) if isinstance(sources, (list, tuple)) else [sources]
+    nsrc = max(len(s.nodes) for s in srcs)
+    if any(len(s.nodes) != nsrc for s in srcs):
+        raise ValueError("every shot needs the same number of source points")
+    src = np.stack([s.nodes for s in srcs])
+    wav = np.stack([s.signal for s in srcs])  # (nshot, N, nsrc)
+    rec = np.repeat(sensors.nodes[None], len(srcs), axis=0)
+    return src, wav, rec
+
+
+def measure(sim: ScalarWave, sources, indicator, sensors: Sensors):
+    """Records of every shot: a list of (N, nsensors) tensors (plate.py:140-142)."""
+    src, wav, rec = _batch(sim, sources, sensors)
+    vel = sim.velocity(indicator)
+    tr = wave_forward(vel, torch.from_numpy(wav).to(vel.device), src, rec, sim.grid())
+    return list(tr.unbind(0))
+
+
+def simulate(sim: ScalarWave, source: Source, indicator, sensors: Sensors | None = None):
+    """Final field u_N of one shot on the physical nodes (shape Nx); with
+    sensors also the record (N, nsensors)
+    (2D_scalar_wave_forward_B_hai.py:30, 4_analog_rnn.py:125-128)."""
+    s = sensors if sensors is not None else Sensors(sim, np.zeros((0, 2)))
+    src, wav, rec = _batch(sim, source, s)
+    vel = sim.velocity(indicator)
+    rec_t = torch.from_numpy(rec) if rec.shape[1] > 0 else torch.zeros((1, 0, 2), dtype=torch.int32)
+    traces, final = wave_forward_final(vel, torch.from_numpy(wav).to(vel.device), src, rec_t, sim.grid())
+    m = sim.margin
+    u = final[0, m:m + sim.Nx[0], m:m + sim.Nx[1]]
+    return (u, traces[0]) if sensors is not None else u
+
+
+def resample(record, dt_obs: float, dt: float, N: int):
+    """Linear interpolation of a record (steps first) onto N steps of dt."""
+    r = torch.as_tensor(record)
+    t = torch.arange(N, dtype=torch.float64, device=r.device) * dt
+    pos = (t / dt_obs).clamp(0, r.shape[0] - 1)
+    k = pos.floor().long().clamp(max=r.shape[0] - 2)
+    w = (pos - k).to(r.dtype).view(-1, *([1] * (r.dim() - 1)))
+    return (1 - w) * r[k] + w * r[k + 1]
+
+
+def misfit_gradient(sim: ScalarWave, sources, indicator, sensors: Sensors, observed):
+    """(cost, d cost / d indicator) with cost = 1/2 sum over shots of
+    |record - observed|^2 (2D_fwi.py:40). The gradient has the indicator's
+    shape, nonzero in [:nx, :ny] only."""
+    src, wav, rec = _batch(sim, sources, sensors)
+    gamma = torch.as_tensor(indicator, device=sim.device, dtype=torch.float32)
+    vel = sim.velocity(gamma)
+    obs = torch.stack([torch.as_tensor(o, device=vel.device, dtype=torch.float32) for o in observed])
+    J, gv = _misfit_gradient(vel, torch.from_numpy(wav).to(vel.device), src, rec, obs, sim.grid())
+    # c = w sqrt(gamma): d cost / d gamma = d cost / d c * w^2 / (2 c)
+    g_pad = gv * (sim.wavespeed ** 2) / (2.0 * vel.clamp_min(1e-6 * sim.wavespeed))
+    m = sim.margin
+    out = torch.zeros_like(gamma)
+    out[:sim.Nx[0], :sim.Nx[1]] = g_pad[m:m + sim.Nx[0], m:m + sim.Nx[1]]
+    return J, out
+
+
+def misfit(sim: ScalarWave, sources, indicator, sensors: Sensors, observed):
+    records = measure(sim, sources, indicator, sensors)
+    return sum(0.5 * float(((r - torch.as_tensor(o, device=r.device)) ** 2).sum()) for r, o in
+               zip(records, observed))
+
+
+class Adam:
+    """Adam on a tensor parameter (2D_fwi.py:34-41: step(x, grad) -> new x)."""
+
+    def __init__(self, lr: float = 0.1, betas=(0.9, 0.999), eps: float = 1e-8):
+        self.lr, self.b1, self.b2, self.eps = lr, betas[0], betas[1], eps
+        self.m = self.v = None
+        self.t = 0
+
+    def step(self, x: torch.Tensor, grad: torch.Tensor) -> torch.Tensor:
+        if self.m is None:
+            self.m = torch.zeros_like(grad)
+            self.v = torch.zeros_like(grad)
+        self.t += 1
+        self.m.mul_(self.b1).add_(grad, alpha=1 - self.b1)
+        self.v.mul_(self.b2).addcmul_(grad, grad, value=1 - self.b2)
+        mh = self.m / (1 - self.b1 ** self.t)
+        vh = self.v / (1 - self.b2 ** self.t)
+        return x - self.lr * mh / (vh.sqrt() + self.eps)

@@ -329,6 +329,28 @@ def wave_forward(vel: torch.Tensor, wavelet, src, rec, grid: Grid, *, check: boo
     return traces
 
 
+def wave_forward_final(vel: torch.Tensor, wavelet, src, rec, grid: Grid, *, check: bool = True):
+    """(traces, u_final): the forward plus the last wavefield u_nt of every
+    shot, shaped (nshot,) + grid.shape (no autograd)."""
+    wav_t = torch.as_tensor(wavelet, device=vel.device)
+    s = torch.as_tensor(src)
+    nshot = s.shape[0] if s.dim() == 3 else (wav_t.shape[0] if wav_t.dim() >= 2 else None)
+    call = _prepare(vel, wav_t, src, rec, grid, nshot)
+    call.problem.group_shots = 0
+    p = call.problem
+    ws = _workspace(call, False)
+    traces = torch.empty((p.nshot, p.nt, p.nrec), dtype=torch.float32, device=vel.device)
+    final = torch.empty((p.nshot,) + tuple(grid.shape), dtype=torch.float32, device=vel.device)
+    gz, gy, gx = call.sponges
+    _lib.check(_lib.load().wfd_forward_final(ctypes.byref(p), _ptr(call.vel), _ptr(gz), _ptr(gy), _ptr(gx),
+                                             _ptr(call.wavelet), _ptr(call.src), _ptr(call.rec),
+                                             _ptr(traces), _ptr(final), _ptr(ws), ws.numel(), _stream()),
+               "wfd_forward_final")
+    if check:
+        _status(ws, "wfd_forward_final")
+    return traces, final
+
+
 def misfit_gradient(vel: torch.Tensor, wavelet, src, rec, observed: torch.Tensor, grid: Grid, *,
                     want_wavelet: bool = False, want_traces: bool = False, check: bool = True):
     """(misfit, grad_vel[, grad_wavelet][, traces]) in one library call.

@@ -1,0 +1,103 @@
+"""The cuwave-shaped adapter (projects/18_fwi call sequence on this library)."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+
+
+def test_geometry_and_helpers():
+    from neuralmech_gb300 import cuwave_compat as cw
+    sim = cw.ScalarWave((64, 80), (1 / 61, 1 / 77), 100, 1e-3, space_order=8)
+    assert sim.margin == 3 and sim.grid_shape == (70, 86) and sim.Nx_padded == (72, 88)
+    # node i of the physical grid sits at x = -dx + i dx; the margin shifts it
+    assert sim.node((0.0, 0.0)) == (4, 4)
+    assert sim.node((1.0, 1.0)) == (61 + 4, 77 + 4)  # the last physical interior node
+    R = 4
+    assert sim.node((1.0, 1.0))[1] < sim.grid_shape[1] - R  # updated by the order-8 stencil
+    pts = cw.line((0.1, 1.0), (0.9, 1.0), 5)
+    assert pts.shape == (5, 2) and np.allclose(pts[:, 1], 1.0) and np.isclose(pts[2, 0], 0.5)
+    t = np.linspace(0, 0.5, 1001)
+    s = cw.sineburst(t, 2.0, 10.0, 2)
+    assert np.all(s[t > 0.2] == 0) and np.abs(s).max() <= 2.0 and np.abs(s).max() > 1.5
+    src = cw.point_source(sim, (0.5, 1.0), np.ones(100))
+    assert np.allclose(src.signal, 1e-6 / (1 / 61 * 1 / 77))
+
+
+def test_resample_and_adam():
+    from neuralmech_gb300 import cuwave_compat as cw
+    r = torch.arange(10, dtype=torch.float32)[:, None].repeat(1, 3)
+    assert torch.allclose(cw.resample(r, 1.0, 1.0, 10), r)
+    half = cw.resample(r, 1.0, 0.5, 19)
+    assert torch.allclose(half[:, 0], torch.arange(19, dtype=torch.float32) / 2)
+    opt = cw.Adam(lr=0.1)
+    x = torch.zeros(3)
+    x = opt.step(x, torch.tensor([1.0, -2.0, 0.0]))
+    assert torch.allclose(x, torch.tensor([-0.1, 0.1, 0.0]), atol=1e-6)
+
+
+def _plate(cuda, order=4, n=72, N=260, E=8):
+    from neuralmech_gb300 import cuwave_compat as cw
+    L = 1.0
+    dx = (L / (n - 3), L / (n - 3))
+    dt = 0.9 * cw.stable_dt(dx, 1.0, order)
+    sim = cw.ScalarWave((n, n), dx, N, dt, space_order=order, wavespeed=1.0, density=1.0)
+    t = np.arange(N) * dt
+    elements = cw.line((0.1, L), (0.9, L), E)
+    sources = cw.shots(sim, elements, cw.sineburst(t, 1.0, 12.0, 2))
+    sensors = cw.Sensors(sim, elements)
+    gamma_true = torch.ones(sim.Nx_padded, device=cuda)
+    xx, yy = np.meshgrid(np.arange(n) * dx[0] - dx[0], np.arange(n) * dx[1] - dx[1], indexing="ij")
+    void = (xx - 0.5) ** 2 + (yy - 0.55) ** 2 < 0.08 ** 2
+    gamma_true[:n, :n][torch.from_numpy(void).to(cuda)] = 1e-4
+    return cw, sim, sources, sensors, gamma_true
+
+
+@pytest.mark.gpu
+def test_plate_fwi_flow(cuda):
+    """plate.py + 2D_fwi.py on the adapter: measure with the void, then Adam on
+    the indicator from gamma = 1 lowers the misfit."""
+    cw, sim, sources, sensors, gamma_true = _plate(cuda)
+    observed = cw.measure(sim, sources, gamma_true, sensors)
+    assert len(observed) == 8 and observed[0].shape == (sim.N, 8)
+    gamma = torch.ones(sim.Nx_padded, device=cuda)
+    opt = cw.Adam(lr=0.05)
+    costs = []
+    for _ in range(6):
+        cost, grad = cw.misfit_gradient(sim, sources[::2], gamma, sensors, observed[::2])
+        assert grad.shape == gamma.shape and torch.isfinite(grad).all()
+        assert torch.count_nonzero(grad[sim.Nx[0]:]) == 0
+        costs.append(float(cost))
+        gamma = torch.clamp(opt.step(gamma, grad), 1e-3, 1.0)
+    assert costs[-1] < 0.9 * costs[0], costs
+    c2 = cw.misfit(sim, sources[::2], gamma, sensors, observed[::2])
+    assert np.isfinite(c2)
+
+
+@pytest.mark.gpu
+def test_indicator_gradient_finite_difference(cuda):
+    cw, sim, sources, sensors, gamma_true = _plate(cuda, order=8, N=220)
+    observed = cw.measure(sim, sources[:3], gamma_true, sensors)
+    gamma = torch.ones(sim.Nx_padded, device=cuda) * 0.8
+    cost, grad = cw.misfit_gradient(sim, sources[:3], gamma, sensors, observed)
+    n = sim.Nx[0]
+    d = torch.zeros_like(gamma)
+    d[20:50, 25:55] = 0.02
+    costs = [cw.misfit(sim, sources[:3], gamma + s * d, sensors, observed) for s in (1, -1)]
+    fd = (costs[0] - costs[1]) / 2
+    an = float((grad * d).sum())
+    assert abs(fd - an) < 2e-2 * abs(fd), (fd, an)
+    del n
+
+
+@pytest.mark.gpu
+def test_simulate_matches_measure(cuda):
+    cw, sim, sources, sensors, gamma_true = _plate(cuda, N=120)
+    u, record = cw.simulate(sim, sources[3], gamma_true, sensors)
+    assert u.shape == sim.Nx and torch.isfinite(u).all() and u.abs().max() > 0
+    ref = cw.measure(sim, sources[3:4], gamma_true, sensors)[0]
+    assert rel_l2(record.cpu().numpy(), ref.cpu().numpy()) < 1e-6
+    # the last recorded sample is the final field at the sensor nodes
+    m = sim.margin
+    nodes = sensors.nodes - m
+    assert rel_l2(u[nodes[:, 0], nodes[:, 1]].cpu().numpy(), record[-1].cpu().numpy()) < 1e-6

@@ -213,8 +213,8 @@ def misfit_gradient(sim: ScalarWave, sources, indicator, sensors: Sensors, obser
 
 def misfit(sim: ScalarWave, sources, indicator, sensors: Sensors, observed):
     records = measure(sim, sources, indicator, sensors)
-    return sum(0.5 * float(((r - torch.as_tensor(o, device=r.device)) ** 2).sum()) for r, o in
-               zip(records, observed))
+    return sum(0.5 * float(((r.double() - torch.as_tensor(o, device=r.device).double()) ** 2).sum())
+               for r, o in zip(records, observed))
 
 
 class Adam:

@@ -75,19 +75,37 @@ def test_plate_fwi_flow(cuda):
 
 
 @pytest.mark.gpu
-def test_indicator_gradient_finite_difference(cuda):
-    cw, sim, sources, sensors, gamma_true = _plate(cuda, order=8, N=220)
-    observed = cw.measure(sim, sources[:3], gamma_true, sensors)
+def test_indicator_gradient_finite_difference(cuda, orc):
+    """d misfit / d gamma of the adapter (GPU) against central differences of
+    the same misfit computed by the FP64 oracle on the adapter's own grid,
+    positions and scaled wavelets. (FP32 traces bound the gradient's precision
+    by the residual-to-data ratio; the observed model differs by 10 % so that
+    the residuals are not a cancellation of nearly equal traces.)"""
+    cw, sim, sources, sensors, _ = _plate(cuda, order=8, N=220)
     gamma = torch.ones(sim.Nx_padded, device=cuda) * 0.8
-    cost, grad = cw.misfit_gradient(sim, sources[:3], gamma, sensors, observed)
-    n = sim.Nx[0]
-    d = torch.zeros_like(gamma)
-    d[20:50, 25:55] = 0.02
-    costs = [cw.misfit(sim, sources[:3], gamma + s * d, sensors, observed) for s in (1, -1)]
-    fd = (costs[0] - costs[1]) / 2
-    an = float((grad * d).sum())
-    assert abs(fd - an) < 2e-2 * abs(fd), (fd, an)
-    del n
+    g_obs = gamma.clone()
+    g_obs[30:40, 30:45] *= 1.1
+    shots = sources[:3]
+    observed = cw.measure(sim, shots, g_obs, sensors)
+    cost, grad = cw.misfit_gradient(sim, shots, gamma, sensors, observed)
+
+    src, wav, rec = cw._batch(sim, shots, sensors)
+    p3 = lambda p: np.stack([p[..., 0], 0 * p[..., 0], p[..., 1]], -1).astype(np.int32)
+    obs = torch.stack(observed).cpu().numpy().astype(np.float64)
+
+    def J(gm):
+        v = sim.velocity(gm).cpu().numpy().astype(np.float64)
+        geo = orc.Geometry(vel=v, wavelet=wav.astype(np.float64), src=p3(src), rec=p3(rec),
+                           dt=float(np.float32(sim.dt)), h=(sim.dx[0], 1.0, sim.dx[1]), order=8,
+                           sponge=None, src_scale=1.0)
+        return 0.5 * float(((orc.forward(geo) - obs) ** 2).sum())
+
+    # gradient test along the steepest-descent direction: <g, d> = |g||d|, no
+    # cancellation between cells of opposite sign in the projection
+    d = 1e-3 * grad / grad.abs().max()
+    fd = (J(gamma + d) - J(gamma - d)) / 2
+    an = float((grad.double() * d.double()).sum())
+    assert abs(fd - an) < 2e-3 * abs(fd), (fd, an)
 
 
 @pytest.mark.gpu

@@ -14,6 +14,14 @@ counted). Algorithmic bytes: 16 B per forward update, 20 B per adjoint update
 pair; "% HBM" = those bytes / time / measured HBM copy bandwidth.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload fwi1024|fwd2048|fwi384_3d|batch8]
+
+The other workloads (not the headline) print the same JSON line for:
+  fwd2048    2D forward, 2048^2, 4000 steps, one shot (16 B per update);
+  fwi384_3d  3D FWI gradient, 384^3, 1500 steps, 16 shots in two sequential
+             groups of 8, BF16 checkpoints every 39 (18 B per counted update);
+  batch8     8 models 512^2..1536^2, 1000..3000 steps, 128 shots, one
+             graph-captured batch gradient (18 B per counted update).
 
 Multi-GPU (torchrun, one process per GPU): every rank runs the full 64-shot
 gradient of its own shot set (weak scaling) and the gradients and misfits are
@@ -64,6 +72,7 @@ def parse():
                     help="run one gradient and exit (the command profiled by ncu)")
     ap.add_argument("--nt", type=int, default=0, help="override the number of time steps (profiling)")
     ap.add_argument("--shots", type=int, default=0, help="use the first N shots (profiling)")
+    ap.add_argument("--workload", default="fwi1024", choices=["fwi1024", "fwd2048", "fwi384_3d", "batch8"])
     return ap.parse_args()
 
 
@@ -231,10 +240,88 @@ def config_of(w, args):
             "parallelism": f"{args.gpus} GPU(s), shots batched per GPU, gradient all-reduce"}
 
 
+def run_other(args):
+    """fwd2048 / fwi384_3d / batch8: the kernel-level JSON line (no e2e leg)."""
+    import dataclasses
+
+    import torch
+
+    from neuralmech_gb300 import _lib, misfit_gradient, wave_forward
+    from neuralmech_gb300.synth import workload as wl
+
+    dev = torch.device("cuda", 0)
+    lib = _lib.load()
+    if args.workload == "batch8":
+        from neuralmech_gb300.batch import BatchFWI
+        models = []
+        for w in wl("batch8"):
+            v = torch.from_numpy(w.vel).to(dev)
+            wav = torch.from_numpy(w.wavelet).to(dev)
+            src, rec = torch.from_numpy(w.src), torch.from_numpy(w.rec)
+            obs = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, w.grid)
+            models.append(dict(vel=v, wavelet=wav, src=src, rec=rec, observed=obs, grid=w.grid))
+        batch = BatchFWI(models, autotune=True)
+        step = batch.run
+        updates, bpu = batch.cell_updates, 18.0
+        cfg = {"workload": "batch8: 8 models 512^2..1536^2, 1000..3000 steps, 128 shots, Ricker 10..25 Hz, "
+                           "one graph-captured batch gradient (streams per model), autotuned kernels",
+               "models": [[list(m.call.grid.shape), m.call.grid.nt, m.call.problem.nshot] for m in batch.models],
+               "configs": batch.configs}
+    else:
+        w = wl(args.workload)
+        g = w.grid
+        if args.nt:
+            g = dataclasses.replace(g, nt=args.nt, ckpt_every=min(g.ckpt_every or args.nt, args.nt))
+            w.wavelet = w.wavelet[:args.nt]
+        v = torch.from_numpy(w.vel).to(dev)
+        wav = torch.from_numpy(w.wavelet).to(dev)
+        src, rec = torch.from_numpy(w.src), torch.from_numpy(w.rec)
+        R = g.order // 2
+        interior = float(np.prod([n - 2 * R for n in g.shape]))
+        if args.workload == "fwd2048":
+            step = lambda: wave_forward(v, wav, src, rec, g, check=False)
+            updates, bpu = w.nshot * interior * g.nt, 16.0
+            cfg = {"workload": f"fwd2048: 2D forward {g.shape[0]}^2, {g.nt} steps, 1 shot, "
+                               f"{w.rec.shape[1]} receivers, order 8, 20-cell sponge"}
+        else:
+            g = dataclasses.replace(g, group_shots=8)
+            obs = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, g)
+            step = lambda: misfit_gradient(v, wav, src, rec, obs, g, check=False)
+            updates, bpu = 2.0 * w.nshot * interior * g.nt, 18.0
+            cfg = {"workload": f"fwi384_3d: 3D FWI gradient {g.shape[0]}^3, {g.nt} steps, {w.nshot} shots "
+                               f"in groups of 8, {w.rec.shape[1]} receivers per shot, BF16 checkpoints every "
+                               f"{g.ckpt_every}"}
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0)
+    n0 = lib.wfd_kernel_launches()
+    clocks.start()
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    hbm, src_kind = peaks()
+    gbs = updates * bpu / (ms / 1e3) / 1e9
+    line = {"metric": METRIC, "value": updates / (ms / 1e3) / 1e9, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "hbm_alg_gbs": gbs, "hbm_frac_measured": gbs / hbm, "peak_source": src_kind, "clocks": clk,
+            "gpu_launches": int(lib.wfd_kernel_launches() - n0)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "fwi1024":
+        return run_other(args)
 
     import torch
     import torch.distributed as dist

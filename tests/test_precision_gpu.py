@@ -1,0 +1,48 @@
+"""Precision at the benchmark's scale: the fwi1024 grid and time axis
+(1024 x 1024, 2000 steps, order 8, 20-cell sponge, checkpoints every 45) for
+two of its 64 shots, against the FP64 oracle.
+
+* Forward traces: 1e-5 relative L2 (the benchmark spec's bound against the reference
+  solver; measured 5.7e-7).
+* Gradient: on this workload the residuals are ~3.5e-4 of the traces (the
+  2000-step record ends before the deep reflections return), so FP32
+  trace rounding (~6e-7), magnified by that ratio, sets the gradient error
+  (~4e-3) for every checkpoint format. The test states this: BF16 and int16
+  checkpoint storage stay within 5% of the FP32-checkpoint error, and that
+  error stays below 1e-2.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+from helpers import oracle_geometry
+
+pytestmark = pytest.mark.gpu
+
+
+def test_fwi1024_two_shots_against_fp64(cuda, orc):
+    from neuralmech_gb300 import misfit_gradient, synth, wave_forward
+    w = synth.workload("fwi1024")
+    sel = [0, 63]
+    src, rec = w.src[sel], w.rec[sel]
+    wav = np.repeat(w.wavelet[None], 2, 0).astype(np.float32)
+    g = w.grid
+    obs = orc.forward(oracle_geometry(orc, g, w.vel_true, wav[:, :, None], src, rec)).astype(np.float32)
+    geo = oracle_geometry(orc, g, w.vel, wav[:, :, None], src, rec)
+    Jr, gr, _, _ = orc.gradient(geo, obs)
+    args = (torch.from_numpy(w.vel).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+            torch.from_numpy(rec))
+    tr = wave_forward(*args, g).cpu().numpy()
+    e_tr = rel_l2(tr, orc.forward(geo))
+    errs = {}
+    for fmt in ("fp32", "i16", "bf16"):
+        J, gv = misfit_gradient(*args, torch.from_numpy(obs).to(cuda), dataclasses.replace(g, ckpt_format=fmt))
+        errs[fmt] = rel_l2(gv.cpu().numpy(), gr)
+    print(f"fwi1024 (2 shots): traces rel L2 {e_tr:.2e}; gradient rel L2 {errs}")
+    assert e_tr < 1e-5
+    assert errs["fp32"] < 1e-2
+    for fmt in ("i16", "bf16"):
+        assert abs(errs[fmt] - errs["fp32"]) < 0.05 * errs["fp32"]

@@ -54,8 +54,15 @@ TRAFFIC_PATH = os.path.join(ROOT, "profiles", "dram_traffic.txt")
 FALLBACK_HBM_GBS = 6800.0
 METRIC = "Gcell-updates/s fwd+adj (% HBM peak); FWI grad shots/s batched vs plain, 1 GPU"
 UNIT = "Gcell-updates/s"
-# algorithmic bytes per cell-update, per kernel phase
+# algorithmic bytes per cell-update, per kernel phase: u_n, u_{n-1} and m read,
+# u_{n+1} written; the recompute adds the L u write unless the levels u_k
+# themselves are kept (the 2D one-step default), the adjoint the L u or u_k read
 ALG_BYTES = {"forward": 16.0, "recompute": 20.0, "adjoint": 20.0}
+
+
+def alg_bytes(grid, phase: str) -> float:
+    ustore = grid.ndim == 2 and grid.step_block != 2 and grid.lap_store == "auto"
+    return 16.0 if (phase == "recompute" and ustore) else ALG_BYTES[phase]
 
 
 def parse():
@@ -404,7 +411,7 @@ def main():
     dom = max(share, key=share.get)
     i = names.index(dom)
     per_launch_ms = phases.ms[i] / max(1, phases.launches[i])
-    bytes_per_launch = ALG_BYTES[dom] * w.nshot * interior
+    bytes_per_launch = alg_bytes(g, dom) * w.nshot * interior
     achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
     tr = traffic_per_update().get(f"{dom}_bytes_per_cell_update")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,

@@ -41,6 +41,13 @@ extern "C" {
 #define WFD_CKPT_BF16 1 /* 2, round to nearest even */
 #define WFD_CKPT_I16 2  /* 2 + 4/32: int16 with one FP32 scale per 32 cells (block max / 32767) */
 
+/* What the checkpointed adjoint keeps of each recomputed step for its imaging
+ * term q_{k+1} L u_k. */
+#define WFD_LAP_AUTO 0 /* 2D one-step kernel: the level u_k itself (FP32, written by the
+                          recompute anyway) and the adjoint forms L u_k; otherwise FP32 L u_k */
+#define WFD_LAP_BF16 1 /* L u_k in BF16 */
+#define WFD_LAP_FP32 2 /* L u_k in FP32 */
+
 typedef struct wfd_problem {
     int32_t ndim;          /* 2 or 3 */
     int32_t order;         /* space order: 2, 4 or 8 */
@@ -50,7 +57,7 @@ typedef struct wfd_problem {
     int32_t nsrc, nrec;    /* sources / receivers per shot */
     int32_t ckpt_every;    /* steps between checkpoints; 0 = ceil(sqrt(nt)) */
     int32_t ckpt_format;   /* checkpoint snapshots: WFD_CKPT_FP32, _BF16 or _I16 */
-    int32_t lap_bf16;      /* 1: per-segment L u store in BF16, 0: FP32 */
+    int32_t lap_store;     /* WFD_LAP_AUTO, _BF16 or _FP32 */
     int32_t shots_per_cta; /* shots one CTA walks through per step; 0 = automatic */
     int32_t group_shots;   /* run the shots in sequential groups of this many, all
                               groups sharing one workspace sized for a group (forward

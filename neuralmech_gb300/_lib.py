@@ -44,7 +44,7 @@ class Problem(ctypes.Structure):
         ("nshot", ctypes.c_int32), ("nt", ctypes.c_int32),
         ("nsrc", ctypes.c_int32), ("nrec", ctypes.c_int32),
         ("ckpt_every", ctypes.c_int32), ("ckpt_format", ctypes.c_int32),
-        ("lap_bf16", ctypes.c_int32), ("shots_per_cta", ctypes.c_int32),
+        ("lap_store", ctypes.c_int32), ("shots_per_cta", ctypes.c_int32),
         ("group_shots", ctypes.c_int32), ("tile_rows", ctypes.c_int32),
         ("step_block", ctypes.c_int32),
         ("dt", ctypes.c_float), ("dz", ctypes.c_float), ("dy", ctypes.c_float),

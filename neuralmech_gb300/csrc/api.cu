@@ -150,6 +150,8 @@ struct Geom {
     int tile_z, tile_y, tile_x, tiles_z, tiles_y, tiles_x, ntiles;
     int spc;                 // shots per CTA
     int K, nseg, k0_last;    // checkpoint interval, segments, first step of the last segment
+    bool ustore;             // the adjoint forms L u_k from stored levels u_k (2D, one step)
+    bool lap_bf16;           // stored L u_k in BF16 (when !ustore)
     float c0, cz[4], cy[4], cx[4];
 };
 
@@ -190,6 +192,8 @@ int check_problem(const wfd_problem* p) {
         return fail(WFD_ERR_INVALID, "dt and spacings must be positive");
     if (p->ckpt_format < WFD_CKPT_FP32 || p->ckpt_format > WFD_CKPT_I16)
         return fail(WFD_ERR_INVALID, "unknown checkpoint format %d", p->ckpt_format);
+    if (p->lap_store < WFD_LAP_AUTO || p->lap_store > WFD_LAP_FP32)
+        return fail(WFD_ERR_INVALID, "unknown lap_store %d", p->lap_store);
     if (p->tile_rows != 0 && p->tile_rows != 16 && p->tile_rows != 32)
         return fail(WFD_ERR_INVALID, "tile_rows must be 0, 16 or 32");
     if (p->step_block < 0 || p->step_block > 2 || (p->step_block == 2 && p->ndim != 2))
@@ -211,7 +215,9 @@ int check_problem(const wfd_problem* p) {
     return WFD_OK;
 }
 
-Geom make_geom(const wfd_problem* p) {
+// tile_rows > 0 overrides the problem's 2D tile height (the u-store adjoint
+// runs on 16-row tiles: its second staged tile must leave room for two stages).
+Geom make_geom(const wfd_problem* p, int tile_rows = 0) {
     Geom g{};
     g.ndim = p->ndim;
     g.R = p->order / 2;
@@ -227,7 +233,7 @@ Geom make_geom(const wfd_problem* p) {
         g.tile_y = 1;
         g.tile_x = K2_TX;
     } else if (g.ndim == 2) {
-        g.tile_z = p->tile_rows > 0 ? p->tile_rows : T2_TZ;
+        g.tile_z = tile_rows > 0 ? tile_rows : p->tile_rows > 0 ? p->tile_rows : T2_TZ;
         g.tile_y = 1;
         g.tile_x = T2_TX;
     } else {
@@ -255,6 +261,8 @@ Geom make_geom(const wfd_problem* p) {
                             : std::max(1, (int)std::ceil(std::sqrt((double)p->nt)));
     g.nseg = cdiv(p->nt, g.K);
     g.k0_last = (g.nseg - 1) * g.K;
+    g.ustore = g.ndim == 2 && g.sb == 1 && p->lap_store == WFD_LAP_AUTO;
+    g.lap_bf16 = p->lap_store == WFD_LAP_BF16;
     double a[5] = {0, 0, 0, 0, 0};
     fd_weights(p->order, a);
     const double sz = (double)p->dx * p->dx / ((double)p->dz * p->dz);
@@ -268,13 +276,20 @@ Geom make_geom(const wfd_problem* p) {
     return g;
 }
 
+// Geometry of the adjoint launches: 16-row tiles for the u-store adjoint.
+Geom adjoint_geom(const wfd_problem* p, const Geom& g) {
+    return g.ustore && g.tile_z != 16 ? make_geom(p, 16) : g;
+}
+
 // ------------------------------------------------------------------ workspace
 struct Layout {
     int nbuf;  // field buffers per direction: 2 (in place) or 4 (two-step blocking)
     size_t err, m, P[4], counts, src_off, src_ent, rec_off, rec_ent;
     size_t srce_off, srce_ent, rece_off, rece_ent;  // extended-region lists (two-step)
+    size_t asrc_off, asrc_ent, arec_off, arec_ent;  // adjoint-geometry lists (u store)
     size_t Q[4], G, ckpt, lap, res, total;
     size_t field_bytes, ckpt_field_bytes, lap_field_bytes;
+    int nlap;  // slots of the lap region: K stored L u_k, or K + 2 levels u_k (u store)
 };
 
 size_t up256(size_t v) { return (v + 255) / 256 * 256; }
@@ -283,7 +298,9 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     Layout L{};
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o = up256(o + bytes); return at; };
-    const size_t keys = (size_t)p->nshot * g.ntiles;
+    const Geom ga = adjoint_geom(p, g);
+    const bool alists = grad && ga.tile_z != g.tile_z;
+    const size_t keys = (size_t)p->nshot * std::max(g.ntiles, alists ? ga.ntiles : 0);
     L.field_bytes = (size_t)p->nshot * g.cells * 4;
     L.nbuf = g.sb == 2 ? 4 : 2;
     L.err = take(256);
@@ -300,14 +317,22 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
         L.rece_off = take((keys + 1) * 4);
         L.rece_ent = take((size_t)p->nshot * p->nrec * 32 + 8);
     }
+    if (alists) {
+        const size_t akeys = (size_t)p->nshot * ga.ntiles;
+        L.asrc_off = take((akeys + 1) * 4);
+        L.asrc_ent = take((size_t)p->nshot * p->nsrc * 8 + 8);
+        L.arec_off = take((akeys + 1) * 4);
+        L.arec_ent = take((size_t)p->nshot * p->nrec * 8 + 8);
+    }
     if (grad) {
         // per-field slots start on 256-byte boundaries (TMA bases, short4/float4 access)
         L.ckpt_field_bytes = up256(ckpt_bytes(p->ckpt_format, (long long)p->nshot * g.cells));
-        L.lap_field_bytes = up256((size_t)p->nshot * g.cells * (p->lap_bf16 ? 2 : 4));
+        L.lap_field_bytes = up256((size_t)p->nshot * g.cells * (g.lap_bf16 ? 2 : 4));
+        L.nlap = g.ustore ? g.K + 2 : g.K;
         for (int b = 0; b < L.nbuf; ++b) L.Q[b] = take(L.field_bytes);
         L.G = take((size_t)g.cells * 4);
         L.ckpt = take((size_t)g.nseg * 2 * L.ckpt_field_bytes);
-        L.lap = take((size_t)g.K * L.lap_field_bytes);
+        L.lap = take((size_t)L.nlap * L.lap_field_bytes);
         L.res = take((size_t)p->nshot * p->nt * p->nrec * 4 + 4);
     }
     L.total = o;
@@ -319,7 +344,12 @@ struct Work {
     float *m, *P[4], *Q[4], *G, *res;
     int* counts;
     PointLists src, rec, src_e, rec_e;
+    PointLists src_a, rec_a;  // lists of the adjoint geometry (== src, rec unless u store)
     unsigned char *ckpt, *lap;
+    bool own_alists;          // src_a / rec_a are separate lists that setup() builds
+    float* slot(const Layout& L, int i) const {  // u-store level slot i
+        return reinterpret_cast<float*>(lap + (size_t)i * L.lap_field_bytes);
+    }
 };
 
 Work carve(void* ws, const Layout& L, bool grad) {
@@ -338,6 +368,15 @@ Work carve(void* ws, const Layout& L, bool grad) {
         w.src_e.ent = reinterpret_cast<int2*>(b + L.srce_ent);
         w.rec_e.off = reinterpret_cast<int*>(b + L.rece_off);
         w.rec_e.ent = reinterpret_cast<int2*>(b + L.rece_ent);
+    }
+    w.src_a = w.src;
+    w.rec_a = w.rec;
+    if (L.asrc_off) {
+        w.own_alists = true;
+        w.src_a.off = reinterpret_cast<int*>(b + L.asrc_off);
+        w.src_a.ent = reinterpret_cast<int2*>(b + L.asrc_ent);
+        w.rec_a.off = reinterpret_cast<int*>(b + L.arec_off);
+        w.rec_a.ent = reinterpret_cast<int2*>(b + L.arec_ent);
     }
     if (grad) {
         for (int k = 0; k < L.nbuf; ++k) w.Q[k] = reinterpret_cast<float*>(b + L.Q[k]);
@@ -513,6 +552,17 @@ int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
                                     const_cast<int*>(w.rec_e.off), const_cast<int2*>(w.rec_e.ent),
                                     w.err, s, g.R, 4));
     }
+    if (w.own_alists) {  // the u-store adjoint's 16-row tiles
+        const Geom a = adjoint_geom(p, g);
+        WFD_CUDA(launch_build_lists(src, p->nshot, p->nsrc, a.nz, a.ny, a.nx, a.ld, a.R, a.tile_z,
+                                    a.tile_y, a.tile_x, a.tiles_z, a.tiles_y, a.tiles_x, w.counts,
+                                    const_cast<int*>(w.src_a.off), const_cast<int2*>(w.src_a.ent),
+                                    w.err, s));
+        WFD_CUDA(launch_build_lists(rec, p->nshot, p->nrec, a.nz, a.ny, a.nx, a.ld, a.R, a.tile_z,
+                                    a.tile_y, a.tile_x, a.tiles_z, a.tiles_y, a.tiles_x, w.counts,
+                                    const_cast<int*>(w.rec_a.off), const_cast<int2*>(w.rec_a.ent),
+                                    w.err, s));
+    }
     return WFD_OK;
 }
 
@@ -530,25 +580,41 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
                 const Stepper& st, const float* wavelet, float* traces, bool save,
                 int* final_buf = nullptr) {
     if (g.sb == 2) return run_forward_k2(p, g, L, w, st, wavelet, traces, save, final_buf);
-    if (final_buf) *final_buf = p->nt & 1;
     cudaStream_t s = st.s;
-    WFD_CUDA(cudaMemsetAsync(w.P[0], 0, L.field_bytes, s));
-    WFD_CUDA(cudaMemsetAsync(w.P[1], 0, L.field_bytes, s));
-    CUtensorMap mc[2], mo[2];
+    // Level u_k lives in P[k & 1] (u_{k+1} overwrites u_{k-1} in place), except
+    // that with the u store the levels of the last segment, from u_{k0_last - 1}
+    // on, go to the store's slots k - k0_last + 1 for the adjoint to read.
+    const bool us = save && g.ustore;
+    const int nslot = us ? L.nlap : 0;
+    auto loc = [&](int k) -> int { return us && k >= g.k0_last - 1 ? 2 + (k - g.k0_last + 1) : (k & 1); };
+    std::vector<float*> buf(2 + nslot);
+    buf[0] = w.P[0];
+    buf[1] = w.P[1];
+    for (int i = 0; i < nslot; ++i) buf[2 + i] = w.slot(L, i);
+    if (final_buf) {
+        if (us) return fail(WFD_ERR_INVALID, "internal: final level requested from a u-store forward");
+        *final_buf = p->nt & 1;
+    }
+    if (us)  // the fixed outer ring of every slot (the kernel writes the interior only)
+        WFD_CUDA(launch_zero_ring2d(w.slot(L, 0), L.lap_field_bytes / 4, nslot, g.cells, p->nshot,
+                                    g.nz, g.nx, g.ld, g.R, s));
+    WFD_CUDA(cudaMemsetAsync(buf[loc(-1)], 0, L.field_bytes, s));
+    WFD_CUDA(cudaMemsetAsync(buf[loc(0)], 0, L.field_bytes, s));
+    std::vector<CUtensorMap> mc(buf.size()), mo(buf.size());
     int rc;
-    for (int b = 0; b < 2; ++b)
-        if ((rc = st.map_pair(w.P[b], w.P[b], &mc[b], &mo[b]))) return rc;
+    for (size_t b = 0; b < buf.size(); ++b)
+        if ((rc = st.map_pair(buf[b], buf[b], &mc[b], &mo[b]))) return rc;
     const long long n_all = (long long)p->nshot * g.cells;
     PhaseScope scope(PH_FORWARD, s, p->nt);
     for (int n = 0; n < p->nt; ++n) {
-        const int bc = n & 1, bn = (n + 1) & 1;
+        const int bo = loc(n - 1), bc = loc(n), bn = loc(n + 1);
         if (save && n % g.K == 0) {
             unsigned char* slot = w.ckpt + (size_t)(n / g.K) * 2 * L.ckpt_field_bytes;
-            WFD_CUDA(launch_pack(w.P[bn], slot, n_all, p->ckpt_format, s));
-            WFD_CUDA(launch_pack(w.P[bc], slot + L.ckpt_field_bytes, n_all, p->ckpt_format, s));
+            WFD_CUDA(launch_pack(buf[bo], slot, n_all, p->ckpt_format, s));
+            WFD_CUDA(launch_pack(buf[bc], slot + L.ckpt_field_bytes, n_all, p->ckpt_format, s));
         }
-        const bool lap = save && n >= g.k0_last;
-        StepArgs a = st.base(w.P[bn]);
+        const bool lap = save && !g.ustore && n >= g.k0_last;
+        StepArgs a = st.base(buf[bn]);
         a.inj = w.src;
         a.inj_val = wavelet;
         a.inj_np = p->nsrc; a.inj_nt = p->nt; a.inj_t = n;
@@ -562,12 +628,12 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
         }
         if (lap) {
             a.lap = w.lap + (size_t)(n - g.k0_last) * L.lap_field_bytes;
-            a.lap_bf16 = p->lap_bf16;
+            a.lap_bf16 = g.lap_bf16;
         }
-        if ((rc = st.launch(lap ? MODE_SAVE_LAP : MODE_PLAIN, mc[bc], mo[bn], mc[bc], a))) return rc;
+        if ((rc = st.launch(lap ? MODE_SAVE_LAP : MODE_PLAIN, mc[bc], mo[bo], mc[bc], a))) return rc;
     }
     if (traces && p->nrec > 0)
-        WFD_CUDA(launch_gather(w.P[p->nt & 1], g.cells, w.rec, g.ntiles, p->nshot, p->nrec, nullptr,
+        WFD_CUDA(launch_gather(buf[loc(p->nt)], g.cells, w.rec, g.ntiles, p->nshot, p->nrec, nullptr,
                                1.f, 0, traces, p->nt, p->nt - 1, s));
     return WFD_OK;
 }
@@ -645,7 +711,7 @@ int run_forward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const W
         if (lap) {
             q.lap1 = w.lap + (size_t)(n - g.k0_last) * L.lap_field_bytes;
             if (two) q.a.lap = w.lap + (size_t)(n + 1 - g.k0_last) * L.lap_field_bytes;
-            q.a.lap_bf16 = p->lap_bf16;
+            q.a.lap_bf16 = g.lap_bf16;
         }
         if ((rc = st.launch_k2(lap ? MODE_SAVE_LAP : MODE_PLAIN, mu[lv.cur], mo[lv.old_], none, none, q)))
             return rc;
@@ -673,7 +739,7 @@ int run_backward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const 
     }
     std::vector<CUtensorMap> lm(g.K);
     for (int k = 0; k < g.K; ++k)
-        if ((rc = st.lap_map_k2(w.lap + (size_t)k * L.lap_field_bytes, p->lap_bf16, &lm[k]))) return rc;
+        if ((rc = st.lap_map_k2(w.lap + (size_t)k * L.lap_field_bytes, g.lap_bf16, &lm[k]))) return rc;
     const long long n_all = (long long)p->nshot * g.cells;
 
     // adjoint launch at k: q_k (and q_{k-1} when two) from (q_{k+2}, q_{k+1})
@@ -713,7 +779,7 @@ int run_backward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const 
         if (grad) {
             mode = MODE_GRAD;
             q.a.grad = w.G;
-            q.a.lap_bf16 = p->lap_bf16;
+            q.a.lap_bf16 = g.lap_bf16;
             l1 = &lm[k - k0];
             if (two) l2 = &lm[k - 1 - k0];
         }
@@ -756,7 +822,7 @@ int run_backward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const 
                 q.a.smp_t = -1;
                 q.lap1 = w.lap + (size_t)(k - k0) * L.lap_field_bytes;
                 if (two) q.a.lap = w.lap + (size_t)(k + 1 - k0) * L.lap_field_bytes;
-                q.a.lap_bf16 = p->lap_bf16;
+                q.a.lap_bf16 = g.lap_bf16;
                 if ((rc = st.launch_k2(MODE_SAVE_LAP, pu[lv.cur], po[lv.old_], none, none, q))) return rc;
                 lv.advance(two, f0, f1);
                 k += two ? 2 : 1;
@@ -777,6 +843,91 @@ int run_backward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const 
     return WFD_OK;
 }
 
+// Adjoint with the u store (2D, one step per launch). Segment j restores
+// (u_{k0-1}, u_k0) into slots 0 and 1 and recomputes u_{k0+1} .. u_{k1-1} into
+// slots 2 .. k1 - k0 (each step writes a new slot: nothing else is stored); the
+// adjoint step k then stages u_k from slot k - k0 + 1 next to q_{k+1} and forms
+// L u_k itself (MODE_GRAD_U) on 16-row tiles, the recompute on the forward's.
+int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
+                        const Stepper& st, const float* wavelet, const float* dtraces,
+                        float* grad_vel, float* grad_wavelet, const float* vel, bool zero_G,
+                        bool finalize) {
+    cudaStream_t s = st.s;
+    const Geom ga = adjoint_geom(p, g);
+    Stepper sa = st;
+    sa.g = ga;
+    WFD_CUDA(cudaMemsetAsync(w.Q[0], 0, L.field_bytes, s));
+    WFD_CUDA(cudaMemsetAsync(w.Q[1], 0, L.field_bytes, s));
+    if (zero_G) WFD_CUDA(cudaMemsetAsync(w.G, 0, (size_t)g.cells * 4, s));
+    int rc;
+    CUtensorMap qc[2], qo[2];
+    for (int b = 0; b < 2; ++b)
+        if ((rc = sa.map_pair(w.Q[b], w.Q[b], &qc[b], &qo[b]))) return rc;
+    // per slot: u_k as the recompute's u_n / u_{n-1} tiles and as the adjoint's staged u_k
+    std::vector<CUtensorMap> uc(L.nlap), uo(L.nlap), ua(L.nlap), unused(L.nlap);
+    for (int i = 0; i < L.nlap; ++i) {
+        if ((rc = st.map_pair(w.slot(L, i), w.slot(L, i), &uc[i], &uo[i]))) return rc;
+        if ((rc = sa.map_pair(w.slot(L, i), w.slot(L, i), &ua[i], &unused[i]))) return rc;
+    }
+    const long long n_all = (long long)p->nshot * g.cells;
+
+    // q_k from (q_{k+1}, q_{k+2}); with the gradient term q_{k+1} L u_k, u_k in slot `slot`
+    auto adjoint_step = [&](int k, int slot) -> int {
+        const int bc = (k + 1) & 1, bn = k & 1;
+        StepArgs a = sa.base(w.Q[bn]);
+        if (p->nrec > 0) {
+            a.inj = w.rec_a;
+            a.inj_val = dtraces;
+            a.inj_np = p->nrec; a.inj_nt = p->nt; a.inj_t = k - 1;
+            a.inj_scale = 1.f;
+            a.inj_times_m = 1;
+        }
+        if (grad_wavelet && k <= p->nt - 1 && p->nsrc > 0) {
+            a.smp = w.src_a;
+            a.smp_out = grad_wavelet;
+            a.smp_np = p->nsrc; a.smp_nt = p->nt; a.smp_t = k;
+            a.smp_scale = p->src_scale;
+            a.smp_div_m = 1;
+        }
+        if (slot < 0) return sa.launch(MODE_PLAIN, qc[bc], qo[bn], qc[bc], a);
+        a.grad = w.G;
+        return sa.launch(MODE_GRAD_U, qc[bc], qo[bn], ua[slot], a);
+    };
+
+    {
+        PhaseScope scope(PH_ADJOINT, s, 1);
+        if ((rc = adjoint_step(p->nt, -1))) return rc;  // q_nt: its gradient term is 0
+    }
+    for (int j = g.nseg - 1; j >= 0; --j) {
+        const int k0 = j * g.K, k1 = std::min(p->nt, k0 + g.K);
+        if (j != g.nseg - 1) {  // the forward left the last segment's levels in the slots
+            PhaseScope scope(PH_RECOMPUTE, s, k1 - k0 - 1);
+            const unsigned char* ck = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
+            WFD_CUDA(launch_unpack(ck, w.slot(L, 0), n_all, p->ckpt_format, s));
+            WFD_CUDA(launch_unpack(ck + L.ckpt_field_bytes, w.slot(L, 1), n_all, p->ckpt_format, s));
+            for (int k = k0; k + 1 < k1; ++k) {
+                const int i = k - k0 + 1;  // slot of u_k
+                StepArgs a = st.base(w.slot(L, i + 1));
+                if (p->nsrc > 0) {
+                    a.inj = w.src;
+                    a.inj_val = wavelet;
+                    a.inj_np = p->nsrc; a.inj_nt = p->nt; a.inj_t = k;
+                    a.inj_scale = p->src_scale;
+                }
+                if ((rc = st.launch(MODE_PLAIN, uc[i], uo[i - 1], uc[i], a))) return rc;
+            }
+        }
+        PhaseScope scope(PH_ADJOINT, s, k1 - std::max(k0, 1));
+        for (int k = k1 - 1; k >= std::max(k0, 1); --k)
+            if ((rc = adjoint_step(k, k - k0 + 1))) return rc;
+    }
+    if (grad_wavelet && p->nsrc > 0)  // q_1 at the sources -> d J / d w_0
+        WFD_CUDA(launch_gather(w.Q[1], ga.cells, w.src_a, ga.ntiles, p->nshot, p->nsrc, w.m,
+                               p->src_scale, 1, grad_wavelet, p->nt, 0, s));
+    if (finalize) WFD_CUDA(launch_grad_finalize(w.G, vel, grad_vel, g.nz, g.ny, g.nx, g.ld, g.R, s));
+    return WFD_OK;
+}
+
 // Adjoint of one (group of) shots. zero_G starts a new gradient sum; finalize
 // turns the sum into dJ/dv (the last group of a grouped call).
 int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
@@ -785,6 +936,9 @@ int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Wor
     if (g.sb == 2)
         return run_backward_k2(p, g, L, w, st, wavelet, dtraces, grad_vel, grad_wavelet, vel, zero_G,
                                finalize);
+    if (g.ustore)
+        return run_backward_ustore(p, g, L, w, st, wavelet, dtraces, grad_vel, grad_wavelet, vel,
+                                   zero_G, finalize);
     cudaStream_t s = st.s;
     WFD_CUDA(cudaMemsetAsync(w.Q[0], 0, L.field_bytes, s));
     WFD_CUDA(cudaMemsetAsync(w.Q[1], 0, L.field_bytes, s));
@@ -797,7 +951,7 @@ int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Wor
     }
     std::vector<CUtensorMap> lm(g.K);
     for (int k = 0; k < g.K; ++k)
-        if ((rc = st.lap_map(w.lap + (size_t)k * L.lap_field_bytes, p->lap_bf16, &lm[k]))) return rc;
+        if ((rc = st.lap_map(w.lap + (size_t)k * L.lap_field_bytes, g.lap_bf16, &lm[k]))) return rc;
     const long long n_all = (long long)p->nshot * g.cells;
 
     auto adjoint_step = [&](int k, bool with_grad, int slot) -> int {
@@ -821,7 +975,7 @@ int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Wor
         if (with_grad) {
             mode = MODE_GRAD;
             a.lap = w.lap + (size_t)slot * L.lap_field_bytes;
-            a.lap_bf16 = p->lap_bf16;
+            a.lap_bf16 = g.lap_bf16;
             a.grad = w.G;
         }
         return st.launch(mode, qc[bc], qo[bn], with_grad ? lm[slot] : qc[bc], a);
@@ -848,7 +1002,7 @@ int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Wor
                     a.inj_scale = p->src_scale;
                 }
                 a.lap = w.lap + (size_t)(k - k0) * L.lap_field_bytes;
-                a.lap_bf16 = p->lap_bf16;
+                a.lap_bf16 = g.lap_bf16;
                 if ((rc = st.launch(MODE_SAVE_LAP, pc[bc], po[bn], pc[bc], a))) return rc;
             }
         }

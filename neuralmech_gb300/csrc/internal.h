@@ -31,6 +31,8 @@ enum StepMode : int {
     MODE_PLAIN = 0,     // update only
     MODE_SAVE_LAP = 1,  // update + store L u_n (forward recompute)
     MODE_GRAD = 2,      // update + accumulate q_{k+1} * L u_k into the gradient (adjoint)
+    MODE_GRAD_U = 3,    // as MODE_GRAD, with L u_k computed in the kernel from a staged u_k
+                        // tile (2D one-step kernel; the map_lap box is then the u_n box)
 };
 
 // A set of points (sources or receivers) bucketed by the tile that owns them.
@@ -147,6 +149,9 @@ cudaError_t launch_build_lists(const int32_t* pos, int nshot, int np, int nz, in
                                int ld, int R, int tile_z, int tile_y, int tile_x, int tiles_z,
                                int tiles_y, int tiles_x, int* counts, int* off, int2* ent,
                                unsigned* err, cudaStream_t s, int halo_z = 0, int halo_x = 0);
+// Zeroes the R-cell outer ring of nslot x nshot 2D fields (slot / shot strides in floats).
+cudaError_t launch_zero_ring2d(float* base, long long slot_stride, int nslot, long long shot_stride,
+                               int nshot, int nz, int nx, int ld, int R, cudaStream_t s);
 cudaError_t launch_gather(const float* u, long long shot_stride, PointLists lists, int ntiles,
                           int nshot, int np, const float* m, float scale, int div_m,
                           float* out, int out_nt, int out_t, cudaStream_t s);

@@ -24,7 +24,11 @@
 //   * sampling of the staged u_n at receivers (traces of the previous step),
 //   * injection into u_{n+1} (sources, or m-scaled residuals in the adjoint),
 //   * MODE_SAVE_LAP: L u_n stored (FP32 or BF16) for the adjoint's imaging term,
-//   * MODE_GRAD: q_{k+1} L u_k accumulated into the gradient.
+//   * MODE_GRAD: q_{k+1} L u_k accumulated into the gradient;
+//   * MODE_GRAD_U: the same with u_k staged (with its halo) instead of L u_k,
+//     and L u_k formed in the kernel: the recompute then stores nothing but
+//     the levels it writes anyway. This mode runs on 16-row tiles: with the
+//     third tile, two stages of 32-row tiles would leave one CTA per SM.
 #include "common.cuh"
 #include "internal.h"
 
@@ -39,12 +43,15 @@ struct Layout2D {
     static constexpr int H = TZ + 2 * R;
     static constexpr int CUR = H * T2_W * 4;  // TMA box bytes of u_n
     static constexpr int OLD = TZ * T2_TX * 4;
-    static constexpr int LAP = MODE == MODE_GRAD ? TZ * T2_TX * 4 : 0;
+    static constexpr int LAP = MODE == MODE_GRAD ? TZ * T2_TX * 4 : MODE == MODE_GRAD_U ? H * T2_W * 4 : 0;
     // every TMA destination starts on a 128-byte boundary
     static constexpr int CUR_AL = align_up(CUR, 128);
     static constexpr int OLD_AL = align_up(OLD, 128);
     static constexpr int STAGE = align_up(CUR_AL + OLD_AL + LAP, 128);
-    static constexpr int BYTES = T2_STAGES * STAGE + 64 + 128;  // + barriers + alignment slack
+    // TMA stages in flight per CTA: three for the u-store adjoint, whose three
+    // tiles per shot make a stage the longest to arrive
+    static constexpr int STAGES = MODE == MODE_GRAD_U ? 3 : T2_STAGES;
+    static constexpr int BYTES = STAGES * STAGE + 64 + 128;  // + barriers + alignment slack
 };
 
 __device__ __forceinline__ float comp(const float4& v, int e) {
@@ -52,7 +59,7 @@ __device__ __forceinline__ float comp(const float4& v, int e) {
 }
 
 template <int R, int MODE, int RB>
-__global__ void __launch_bounds__(T2_THREADS, RB == 2 ? 3 : 2)
+__global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ? 3 : 2)
     step2d_kernel(const __grid_constant__ CUtensorMap map_cur,
                   const __grid_constant__ CUtensorMap map_old,
                   const __grid_constant__ CUtensorMap map_lap, const StepArgs a) {
@@ -61,7 +68,7 @@ __global__ void __launch_bounds__(T2_THREADS, RB == 2 ? 3 : 2)
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    uint64_t* bars = reinterpret_cast<uint64_t*>(base + T2_STAGES * L::STAGE);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base + L::STAGES * L::STAGE);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tile = blockIdx.x;
@@ -73,18 +80,22 @@ __global__ void __launch_bounds__(T2_THREADS, RB == 2 ? 3 : 2)
     if (ns <= 0) return;
 
     const uint32_t lap_bytes =
-        MODE == MODE_GRAD ? uint32_t(TZ * T2_TX * (a.lap_bf16 ? 2 : 4)) : 0u;
+        MODE == MODE_GRAD     ? uint32_t(TZ * T2_TX * (a.lap_bf16 ? 2 : 4))
+        : MODE == MODE_GRAD_U ? uint32_t(L::CUR)
+                              : 0u;
     const uint32_t stage_tx = uint32_t(L::CUR + L::OLD) + lap_bytes;
     auto cur_buf = [&](int b) { return reinterpret_cast<float*>(base + b * L::STAGE); };
     auto old_buf = [&](int b) { return reinterpret_cast<float*>(base + b * L::STAGE + L::CUR_AL); };
     auto lap_buf = [&](int b) { return base + b * L::STAGE + L::CUR_AL + L::OLD_AL; };
 
     auto issue = [&](int i) {  // called by thread 0 only
-        const int b = i % T2_STAGES;
+        const int b = i % L::STAGES;
         mbar_arrive_expect_tx(&bars[b], stage_tx);
         tma_load_3d(cur_buf(b), &map_cur, x0 - T2_XH, z0 - R, s0 + i, &bars[b]);
         tma_load_3d(old_buf(b), &map_old, x0, z0, s0 + i, &bars[b]);
         if (MODE == MODE_GRAD) tma_load_3d(lap_buf(b), &map_lap, x0, z0, s0 + i, &bars[b]);
+        if (MODE == MODE_GRAD_U)  // u_k with the halo of u_n
+            tma_load_3d(lap_buf(b), &map_lap, x0 - T2_XH, z0 - R, s0 + i, &bars[b]);
     };
 
     // point-list ranges of this tile for every shot of the CTA, staged once
@@ -96,12 +107,12 @@ __global__ void __launch_bounds__(T2_THREADS, RB == 2 ? 3 : 2)
         inj_range[tid] = a.inj.off ? make_int2(a.inj.off[k], a.inj.off[k + 1]) : make_int2(0, 0);
     }
     if (tid == 0) {
-        for (int b = 0; b < T2_STAGES; ++b) mbar_init(&bars[b], 1);
+        for (int b = 0; b < L::STAGES; ++b) mbar_init(&bars[b], 1);
         fence_mbar_init();
     }
     __syncthreads();
     if (tid == 0)
-        for (int i = 0; i < min(ns, T2_STAGES); ++i) issue(i);
+        for (int i = 0; i < min(ns, L::STAGES); ++i) issue(i);
 
     // ---- per-thread constants, reused for every shot of the CTA
     const int x = x0 + 4 * lane;
@@ -133,11 +144,48 @@ __global__ void __launch_bounds__(T2_THREADS, RB == 2 ? 3 : 2)
     for (int r = 0; r < RB; ++r) gacc[r] = make_float4(0.f, 0.f, 0.f, 0.f);
 
     for (int i = 0; i < ns; ++i) {
-        const int s = s0 + i, b = i % T2_STAGES;
-        if (!mbar_wait(&bars[b], (i / T2_STAGES) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
+        const int s = s0 + i, b = i % L::STAGES;
+        if (!mbar_wait(&bars[b], (i / L::STAGES) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
         const float* cur = cur_buf(b);
         const float* old = old_buf(b);
         float* un = a.u_new + (long long)s * a.shot_stride;
+
+        // MODE_GRAD_U: L u_k of this thread's cells from the staged u_k tile,
+        // times q_{k+1} at the cells into the gradient sum (before the q
+        // window is loaded, so that the two register windows never coexist)
+        if (MODE == MODE_GRAD_U) {
+            const float* ut = reinterpret_cast<const float*>(lap_buf(b));
+            float4 W[RB + 2 * R];
+#pragma unroll
+            for (int j = 0; j < RB + 2 * R; ++j)
+                W[j] = *reinterpret_cast<const float4*>(ut + (warp * RB + j) * T2_W + T2_XH + 4 * lane);
+#pragma unroll
+            for (int r = 0; r < RB; ++r) {
+                if (!zin[r]) continue;
+                const float* row = ut + (warp * RB + r + R) * T2_W + 4 * lane;
+                const float4 lv = *reinterpret_cast<const float4*>(row);
+                const float4 cv = W[r + R];
+                const float4 rv = *reinterpret_cast<const float4*>(row + 2 * T2_XH);
+                const float4 qv =
+                    *reinterpret_cast<const float4*>(cur + (warp * RB + r + R) * T2_W + T2_XH + 4 * lane);
+                const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y, cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
+                float l4[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    float acc = a.c0 * w[4 + e];
+#pragma unroll
+                    for (int k = 1; k <= R; ++k) {
+                        acc = fmaf(a.cx[k - 1], w[4 + e - k] + w[4 + e + k], acc);
+                        acc = fmaf(a.cz[k - 1], comp(W[r + R - k], e) + comp(W[r + R + k], e), acc);
+                    }
+                    l4[e] = xin[e] ? comp(qv, e) * acc : 0.f;
+                }
+                gacc[r].x += l4[0];
+                gacc[r].y += l4[1];
+                gacc[r].z += l4[2];
+                gacc[r].w += l4[3];
+            }
+        }
 
         float4 V[RB + 2 * R];
 #pragma unroll
@@ -226,9 +274,9 @@ __global__ void __launch_bounds__(T2_THREADS, RB == 2 ? 3 : 2)
             }
         }
         __syncthreads();  // stage b fully read; this shot's u_{n+1} stores done
-        if (tid == 0 && i + T2_STAGES < ns) {
+        if (tid == 0 && i + L::STAGES < ns) {
             fence_proxy_async_smem();
-            issue(i + T2_STAGES);
+            issue(i + L::STAGES);
         }
         // injection into u_{n+1}, after every store of this shot
         {
@@ -245,7 +293,7 @@ __global__ void __launch_bounds__(T2_THREADS, RB == 2 ? 3 : 2)
         }
     }
 
-    if (MODE == MODE_GRAD) {
+    if (MODE == MODE_GRAD || MODE == MODE_GRAD_U) {
 #pragma unroll
         for (int r = 0; r < RB; ++r) {
             if (!zin[r]) continue;
@@ -287,6 +335,7 @@ cudaError_t dispatch_mode(int mode, const CUtensorMap& mc, const CUtensorMap& mo
         case MODE_PLAIN: return launch_impl<R, MODE_PLAIN, RB>(mc, mo, ml, a, s);
         case MODE_SAVE_LAP: return launch_impl<R, MODE_SAVE_LAP, RB>(mc, mo, ml, a, s);
         case MODE_GRAD: return launch_impl<R, MODE_GRAD, RB>(mc, mo, ml, a, s);
+        case MODE_GRAD_U: return launch_impl<R, MODE_GRAD_U, RB>(mc, mo, ml, a, s);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -35,6 +35,7 @@ from . import _lib
 
 # ---------------------------------------------------------------- descriptors
 CKPT_FORMATS = {"fp32": 0, "bf16": 1, "i16": 2}
+LAP_STORES = {"auto": 0, "bf16": 1, "fp32": 2}
 
 
 @dataclass(frozen=True)
@@ -52,7 +53,10 @@ class Grid:
     ckpt_every   steps between checkpoints of the adjoint (0 = ceil(sqrt(nt)))
     ckpt_format  checkpoint snapshots: "fp32", "bf16" or "i16" (int16 with one
              FP32 scale per 32 cells)
-    lap_bf16     store the per-segment L u of the recomputed forward in BF16
+    lap_store    what the adjoint keeps of each recomputed step for its imaging
+             term: "auto" (2D one-step kernel: the level u_k, which the
+             recompute writes anyway, with L u_k formed by the adjoint; else
+             FP32 L u_k), "fp32" or "bf16" (L u_k stored in that type)
     shots_per_cta  shots one CTA walks through per step (0 = automatic)
     group_shots  run the shots of a misfit gradient (or of a forward without
              autograd) in sequential groups of this many, sharing one workspace
@@ -70,7 +74,7 @@ class Grid:
     src_scale: float = 1.0
     ckpt_every: int = 0
     ckpt_format: str = "bf16"
-    lap_bf16: bool = False
+    lap_store: str = "auto"
     shots_per_cta: int = 0
     group_shots: int = 0
     tile_rows: int = 0
@@ -143,7 +147,7 @@ def _problem(grid: Grid, nshot: int, nsrc: int, nrec: int, vmax: float) -> _lib.
         nz, ny, nx = grid.shape
         dz, dy, dx = grid.spacing
     return _lib.Problem(grid.ndim, grid.order, nz, ny, nx, nshot, grid.nt, nsrc, nrec,
-                        grid.ckpt_every, CKPT_FORMATS[grid.ckpt_format], int(grid.lap_bf16),
+                        grid.ckpt_every, CKPT_FORMATS[grid.ckpt_format], LAP_STORES[grid.lap_store],
                         grid.shots_per_cta, grid.group_shots, grid.tile_rows, grid.step_block, grid.dt, dz, dy, dx, grid.src_scale, vmax)
 
 

@@ -10,7 +10,7 @@ from neuralmech_gb300.synth import add_anomalies, layered, ricker
 
 def small_problem(shape=(60, 150), nshot=3, nsrc=1, nrec=17, nt=120, order=8, sponge=10,
                   seed=0, dx=10.0, cfl=0.45, freq=25.0, ckpt_every=0, ckpt_format="fp32",
-                  lap_bf16=False, spc=0, src_scale=1.0, tile_rows=0, step_block=0):
+                  lap_store="auto", spc=0, src_scale=1.0, tile_rows=0, step_block=0):
     rng = np.random.default_rng(seed)
     nd = len(shape)
     n0 = shape[0]
@@ -19,7 +19,7 @@ def small_problem(shape=(60, 150), nshot=3, nsrc=1, nrec=17, nt=120, order=8, sp
     h = (dx,) * nd
     dt = cfl * dx / float(v.max())
     grid = Grid(tuple(shape), h, dt, nt, order=order, sponge=sponge, ckpt_every=ckpt_every,
-                ckpt_format=ckpt_format, lap_bf16=lap_bf16, shots_per_cta=spc, src_scale=src_scale,
+                ckpt_format=ckpt_format, lap_store=lap_store, shots_per_cta=spc, src_scale=src_scale,
                 tile_rows=tile_rows, step_block=step_block)
     R = order // 2
     lo = [R] * nd

@@ -39,7 +39,7 @@ def test_version_and_strerror():
 def _problem(**kw):
     from neuralmech_gb300 import _lib
     base = dict(ndim=2, order=8, nz=64, ny=1, nx=100, nshot=2, nt=50, nsrc=1, nrec=5,
-                ckpt_every=0, ckpt_format=1, lap_bf16=0, shots_per_cta=0, dt=1e-3, dz=10.0,
+                ckpt_every=0, ckpt_format=1, lap_store=0, shots_per_cta=0, dt=1e-3, dz=10.0,
                 dy=1.0, dx=10.0, src_scale=1.0, vmax=3000.0)
     base.update(kw)
     return _lib.Problem(**base)

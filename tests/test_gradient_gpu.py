@@ -50,24 +50,52 @@ def test_gradient_matches_oracle_fp32(cuda, orc, order, shape, nshot, nt, ckpt, 
     assert rel_l2(gw.cpu().numpy(), gwr) < 1e-4
 
 
-@pytest.mark.parametrize("fmt,lap_bf16,tol", [
-    ("fp32", False, 1e-4),
-    ("i16", False, 2e-4),
-    ("bf16", False, 5e-3),
-    ("fp32", True, 5e-3),
+@pytest.mark.parametrize("fmt,lap_store,tol", [
+    ("fp32", "auto", 1e-4),
+    ("fp32", "fp32", 1e-4),
+    ("i16", "auto", 2e-4),
+    ("bf16", "auto", 5e-3),
+    ("fp32", "bf16", 5e-3),
 ])
-def test_gradient_checkpoint_formats(cuda, orc, fmt, lap_bf16, tol):
+def test_gradient_checkpoint_formats(cuda, orc, fmt, lap_store, tol):
     from neuralmech_gb300 import misfit_gradient
     grid, v, wav, src, rec = small_problem(shape=(80, 200), nshot=3, nt=150, ckpt_every=12,
-                                           ckpt_format=fmt, lap_bf16=lap_bf16, seed=5)
+                                           ckpt_format=fmt, lap_store=lap_store, seed=5)
     obs = _observed(orc, grid, v, wav, src, rec)
     J, g = misfit_gradient(torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda),
                            torch.from_numpy(src), torch.from_numpy(rec),
                            torch.from_numpy(obs).to(cuda), grid)
     _, gr, _, _ = orc.gradient(oracle_geometry(orc, grid, v, wav, src, rec), obs)
     err = rel_l2(g.cpu().numpy(), gr)
-    print(f"checkpoint {fmt} lap_bf16={lap_bf16}: gradient rel L2 {err:.3e}")
+    print(f"checkpoint {fmt} lap_store={lap_store}: gradient rel L2 {err:.3e}")
     assert err < tol, err
+
+
+@pytest.mark.parametrize("order,shape,nt,ckpt,rows,group", [
+    (8, (90, 260), 100, 13, 0, 0),
+    (4, (48, 136), 60, 60, 0, 2),
+    (8, (64, 200), 75, 0, 16, 0),
+])
+def test_u_store_matches_lap_store(cuda, orc, order, shape, nt, ckpt, rows, group):
+    """The u-store adjoint (levels u_k kept, L u_k formed in the adjoint
+    kernel) against the stored-FP32-L u adjoint: the same arithmetic per cell,
+    so the gradients agree to FP32 summation-order noise (1e-6)."""
+    import dataclasses
+    from neuralmech_gb300 import misfit_gradient
+    grid, v, wav, src, rec = small_problem(shape=shape, nshot=5, nt=nt, order=order, ckpt_every=ckpt,
+                                           seed=21, tile_rows=rows)
+    grid = dataclasses.replace(grid, group_shots=group)
+    obs = _observed(orc, grid, v, wav, src, rec)
+    args = (torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+            torch.from_numpy(rec), torch.from_numpy(obs).to(cuda))
+    out = {}
+    for store in ("auto", "fp32"):
+        out[store] = misfit_gradient(*args, dataclasses.replace(grid, lap_store=store), want_wavelet=True)
+    Ja, ga, gwa = out["auto"]
+    Jf, gf, gwf = out["fp32"]
+    assert abs(Ja.item() - Jf.item()) <= 1e-6 * abs(Jf.item())
+    assert rel_l2(ga.cpu().numpy(), gf.cpu().numpy()) < 1e-6
+    assert rel_l2(gwa.cpu().numpy(), gwf.cpu().numpy()) < 1e-6
 
 
 def test_autograd_matches_fused_call(cuda, orc):

@@ -79,6 +79,9 @@ def parse():
                     help="run one gradient and exit (the command profiled by ncu)")
     ap.add_argument("--nt", type=int, default=0, help="override the number of time steps (profiling)")
     ap.add_argument("--shots", type=int, default=0, help="use the first N shots (profiling)")
+    ap.add_argument("--level-store-frac", type=float, default=0.55,
+                    help="fraction of the GPU's memory for the forward levels the adjoint keeps "
+                         "instead of recomputing them (0: recompute all but the last segment)")
     ap.add_argument("--workload", default="fwi1024", choices=["fwi1024", "fwd2048", "fwi384_3d", "batch8"])
     return ap.parse_args()
 
@@ -174,6 +177,13 @@ def workload(scale: float, nt: int = 0, shots: int = 0):
     return w
 
 
+def kept_segments(g) -> int:
+    """Segments whose forward levels the adjoint keeps (the last one at least)."""
+    K = g.ckpt_every or int(np.ceil(np.sqrt(g.nt)))
+    nseg = -(-g.nt // K)
+    return min(nseg, max(1, (g.store_levels - 2) // K))
+
+
 def counted_updates(w) -> float:
     R = w.grid.order // 2
     interior = int(np.prod([n - 2 * R for n in w.grid.shape]))
@@ -243,6 +253,8 @@ def config_of(w, args):
                          f"20-cell sponge, checkpoints every {g.ckpt_every} ({g.ckpt_format})"),
             "grid": list(g.shape), "nt": g.nt, "nshot": w.nshot, "nrec": int(w.rec.shape[1]),
             "ckpt_every": g.ckpt_every, "ckpt_format": g.ckpt_format, "order": g.order,
+            "store_levels": g.store_levels,
+            "kept_segments": kept_segments(g),
             "l2": "inputs larger than L2 (multi-GB state and checkpoints per step)",
             "parallelism": f"{args.gpus} GPU(s), shots batched per GPU, gradient all-reduce"}
 
@@ -333,7 +345,9 @@ def main():
     import torch
     import torch.distributed as dist
 
-    from neuralmech_gb300 import _lib, misfit_gradient, wave_forward
+    import dataclasses
+
+    from neuralmech_gb300 import _lib, levels_for_budget, misfit_gradient, wave_forward
     from neuralmech_gb300.wavefd import Grid
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -346,6 +360,9 @@ def main():
     lib = _lib.load()
 
     w = workload(args.scale, args.nt, args.shots)
+    if args.level_store_frac > 0:  # kept forward levels instead of recomputed ones
+        budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
+        w.grid = dataclasses.replace(w.grid, store_levels=levels_for_budget(w.grid, w.nshot, budget))
     g = w.grid
     vel = torch.from_numpy(w.vel).to(dev)
     wav = torch.from_numpy(w.wavelet).to(dev)

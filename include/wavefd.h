@@ -66,6 +66,11 @@ typedef struct wfd_problem {
     int32_t tile_rows;     /* 2D tile height: 16 or 32 rows (0 = 32) */
     int32_t step_block;    /* 2D time steps per kernel launch: 1 or 2 (0 = 1); 2 keeps
                               u_{n+1} in shared memory between the two steps */
+    int32_t store_levels;  /* WFD_LAP_AUTO path: FP32 levels (fields of nshot x cells)
+                              the workspace may hold. The forward keeps the levels of
+                              its last floor((store_levels - 2) / K) segments, K the
+                              checkpoint interval, and the adjoint recomputes only
+                              the others; 0 (or <= K + 2) = the last segment only */
     float dt;              /* time step */
     float dz, dy, dx;      /* grid spacing (dy ignored in 2D) */
     float src_scale;       /* factor on every injected wavelet sample */

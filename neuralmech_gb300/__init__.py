@@ -5,8 +5,8 @@ Host side: Python over PyTorch tensors. Device side: hand-written sm_103a CUDA
 kernels in libwavefd.so behind the C ABI of include/wavefd.h.
 """
 from . import autotune
-from .wavefd import (Grid, fd_weights, misfit_gradient, sponge_profile, sponge_profiles,
-                     stable_dt, step2d_order2, sum_sq, wave_forward, workspace_bytes)
+from .wavefd import (Grid, fd_weights, levels_for_budget, misfit_gradient, sponge_profile,
+                     sponge_profiles, stable_dt, step2d_order2, sum_sq, wave_forward, workspace_bytes)
 
-__all__ = ["autotune", "Grid", "fd_weights", "misfit_gradient", "sponge_profile", "sponge_profiles",
+__all__ = ["autotune", "Grid", "fd_weights", "levels_for_budget", "misfit_gradient", "sponge_profile", "sponge_profiles",
            "stable_dt", "step2d_order2", "sum_sq", "wave_forward", "workspace_bytes"]

@@ -151,6 +151,7 @@ struct Geom {
     int spc;                 // shots per CTA
     int K, nseg, k0_last;    // checkpoint interval, segments, first step of the last segment
     bool ustore;             // the adjoint forms L u_k from stored levels u_k (2D, one step)
+    int jstore, k0_store;    // u store: the forward keeps the levels of segments >= jstore
     bool lap_bf16;           // stored L u_k in BF16 (when !ustore)
     float c0, cz[4], cy[4], cx[4];
 };
@@ -198,8 +199,9 @@ int check_problem(const wfd_problem* p) {
         return fail(WFD_ERR_INVALID, "tile_rows must be 0, 16 or 32");
     if (p->step_block < 0 || p->step_block > 2 || (p->step_block == 2 && p->ndim != 2))
         return fail(WFD_ERR_INVALID, "step_block must be 0, 1 or 2 (2: 2D only)");
-    if (p->ckpt_every < 0 || p->shots_per_cta < 0 || p->group_shots < 0)
-        return fail(WFD_ERR_INVALID, "ckpt_every, shots_per_cta and group_shots must be >= 0");
+    if (p->ckpt_every < 0 || p->shots_per_cta < 0 || p->group_shots < 0 || p->store_levels < 0)
+        return fail(WFD_ERR_INVALID,
+                    "ckpt_every, shots_per_cta, group_shots and store_levels must be >= 0");
     if (p->vmax > 0) {
         double a[5];
         fd_weights(p->order, a);
@@ -262,6 +264,10 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0) {
     g.nseg = cdiv(p->nt, g.K);
     g.k0_last = (g.nseg - 1) * g.K;
     g.ustore = g.ndim == 2 && g.sb == 1 && p->lap_store == WFD_LAP_AUTO;
+    g.jstore = g.nseg - 1;
+    if (g.ustore && p->store_levels > g.K + 2)
+        g.jstore = std::max(0, g.nseg - (p->store_levels - 2) / g.K);
+    g.k0_store = g.jstore * g.K;
     g.lap_bf16 = p->lap_store == WFD_LAP_BF16;
     double a[5] = {0, 0, 0, 0, 0};
     fd_weights(p->order, a);
@@ -289,7 +295,8 @@ struct Layout {
     size_t asrc_off, asrc_ent, arec_off, arec_ent;  // adjoint-geometry lists (u store)
     size_t Q[4], G, ckpt, lap, res, total;
     size_t field_bytes, ckpt_field_bytes, lap_field_bytes;
-    int nlap;  // slots of the lap region: K stored L u_k, or K + 2 levels u_k (u store)
+    int nlap;  // slots of the lap region: K stored L u_k, or levels u_k (u store): from
+               // u_{k0_store - 1} to u_nt, and at least K + 2 for a recomputed segment
 };
 
 size_t up256(size_t v) { return (v + 255) / 256 * 256; }
@@ -328,7 +335,7 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
         // per-field slots start on 256-byte boundaries (TMA bases, short4/float4 access)
         L.ckpt_field_bytes = up256(ckpt_bytes(p->ckpt_format, (long long)p->nshot * g.cells));
         L.lap_field_bytes = up256((size_t)p->nshot * g.cells * (g.lap_bf16 ? 2 : 4));
-        L.nlap = g.ustore ? g.K + 2 : g.K;
+        L.nlap = g.ustore ? std::max(g.K + 2, p->nt - g.k0_store + 2) : g.K;
         for (int b = 0; b < L.nbuf; ++b) L.Q[b] = take(L.field_bytes);
         L.G = take((size_t)g.cells * 4);
         L.ckpt = take((size_t)g.nseg * 2 * L.ckpt_field_bytes);
@@ -582,11 +589,12 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
     if (g.sb == 2) return run_forward_k2(p, g, L, w, st, wavelet, traces, save, final_buf);
     cudaStream_t s = st.s;
     // Level u_k lives in P[k & 1] (u_{k+1} overwrites u_{k-1} in place), except
-    // that with the u store the levels of the last segment, from u_{k0_last - 1}
-    // on, go to the store's slots k - k0_last + 1 for the adjoint to read.
+    // that with the u store the levels of the kept segments, from
+    // u_{k0_store - 1} on, go to the store's slots k - k0_store + 1 for the
+    // adjoint to read.
     const bool us = save && g.ustore;
     const int nslot = us ? L.nlap : 0;
-    auto loc = [&](int k) -> int { return us && k >= g.k0_last - 1 ? 2 + (k - g.k0_last + 1) : (k & 1); };
+    auto loc = [&](int k) -> int { return us && k >= g.k0_store - 1 ? 2 + (k - g.k0_store + 1) : (k & 1); };
     std::vector<float*> buf(2 + nslot);
     buf[0] = w.P[0];
     buf[1] = w.P[1];
@@ -608,7 +616,7 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
     PhaseScope scope(PH_FORWARD, s, p->nt);
     for (int n = 0; n < p->nt; ++n) {
         const int bo = loc(n - 1), bc = loc(n), bn = loc(n + 1);
-        if (save && n % g.K == 0) {
+        if (save && n % g.K == 0 && !(us && n >= g.k0_store)) {  // (kept segments need none)
             unsigned char* slot = w.ckpt + (size_t)(n / g.K) * 2 * L.ckpt_field_bytes;
             WFD_CUDA(launch_pack(buf[bo], slot, n_all, p->ckpt_format, s));
             WFD_CUDA(launch_pack(buf[bc], slot + L.ckpt_field_bytes, n_all, p->ckpt_format, s));
@@ -843,11 +851,13 @@ int run_backward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const 
     return WFD_OK;
 }
 
-// Adjoint with the u store (2D, one step per launch). Segment j restores
-// (u_{k0-1}, u_k0) into slots 0 and 1 and recomputes u_{k0+1} .. u_{k1-1} into
-// slots 2 .. k1 - k0 (each step writes a new slot: nothing else is stored); the
-// adjoint step k then stages u_k from slot k - k0 + 1 next to q_{k+1} and forms
-// L u_k itself (MODE_GRAD_U) on 16-row tiles, the recompute on the forward's.
+// Adjoint with the u store (2D, one step per launch). The forward left the
+// levels of segments >= jstore in the slots (u_k in slot k - k0_store + 1).
+// Every earlier segment j restores (u_{k0-1}, u_k0) into slots 0 and 1 and
+// recomputes u_{k0+1} .. u_{k1-1} into slots 2 .. k1 - k0 (each step writes a
+// new slot: nothing else is stored). The adjoint step k stages u_k from its
+// slot next to q_{k+1} and forms L u_k itself (MODE_GRAD_U) on 16-row tiles;
+// the recompute runs on the forward's tiles.
 int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                         const Stepper& st, const float* wavelet, const float* dtraces,
                         float* grad_vel, float* grad_wavelet, const float* vel, bool zero_G,
@@ -900,7 +910,8 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
     }
     for (int j = g.nseg - 1; j >= 0; --j) {
         const int k0 = j * g.K, k1 = std::min(p->nt, k0 + g.K);
-        if (j != g.nseg - 1) {  // the forward left the last segment's levels in the slots
+        const int base = j >= g.jstore ? g.k0_store : k0;  // u_k is in slot k - base + 1
+        if (j < g.jstore) {
             PhaseScope scope(PH_RECOMPUTE, s, k1 - k0 - 1);
             const unsigned char* ck = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
             WFD_CUDA(launch_unpack(ck, w.slot(L, 0), n_all, p->ckpt_format, s));
@@ -919,7 +930,7 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
         }
         PhaseScope scope(PH_ADJOINT, s, k1 - std::max(k0, 1));
         for (int k = k1 - 1; k >= std::max(k0, 1); --k)
-            if ((rc = adjoint_step(k, k - k0 + 1))) return rc;
+            if ((rc = adjoint_step(k, k - base + 1))) return rc;
     }
     if (grad_wavelet && p->nsrc > 0)  // q_1 at the sources -> d J / d w_0
         WFD_CUDA(launch_gather(w.Q[1], ga.cells, w.src_a, ga.ntiles, p->nshot, p->nsrc, w.m,
@@ -1037,7 +1048,7 @@ const char* wfd_strerror(int status) {
 
 const char* wfd_last_error(void) { return g_last_error.c_str(); }
 
-int wfd_version(void) { return (1 << 16) | 0; }
+int wfd_version(void) { return (2 << 16) | 0; }
 
 int wfd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes) {
     int rc = check_problem(p);

@@ -63,6 +63,10 @@ class Grid:
              sized for a group (0 = all at once)
     tile_rows    2D tile height, 16 or 32 rows (0 = 32)
     step_block   2D time steps per kernel launch, 1 or 2 (0 = 1)
+    store_levels FP32 levels the adjoint's workspace may hold (lap_store "auto"):
+             the forward keeps the levels of its last (store_levels - 2) // K
+             segments and only the earlier ones are recomputed (0: the last
+             segment only); see levels_for_budget()
     """
     shape: tuple
     spacing: tuple
@@ -79,6 +83,7 @@ class Grid:
     group_shots: int = 0
     tile_rows: int = 0
     step_block: int = 0
+    store_levels: int = 0
 
     @property
     def ndim(self) -> int:
@@ -102,6 +107,14 @@ def fd_weights(order: int) -> np.ndarray:
             k * k * math.factorial(R - k) * math.factorial(R + k))
     a[0] = -2.0 * a[1:].sum()
     return a
+
+
+def levels_for_budget(grid: Grid, nshot: int, budget_bytes: float) -> int:
+    """store_levels that fit `budget_bytes` of FP32 levels (nshot fields of the
+    grid, rows padded to 8 cells)."""
+    nx = grid.shape[-1]
+    cells = int(np.prod(grid.shape[:-1])) * ((nx + 7) // 8 * 8)
+    return max(0, int(budget_bytes // (4 * cells * nshot)))
 
 
 def stable_dt(spacing, vmax: float, order: int = 8) -> float:
@@ -148,7 +161,7 @@ def _problem(grid: Grid, nshot: int, nsrc: int, nrec: int, vmax: float) -> _lib.
         dz, dy, dx = grid.spacing
     return _lib.Problem(grid.ndim, grid.order, nz, ny, nx, nshot, grid.nt, nsrc, nrec,
                         grid.ckpt_every, CKPT_FORMATS[grid.ckpt_format], LAP_STORES[grid.lap_store],
-                        grid.shots_per_cta, grid.group_shots, grid.tile_rows, grid.step_block, grid.dt, dz, dy, dx, grid.src_scale, vmax)
+                        grid.shots_per_cta, grid.group_shots, grid.tile_rows, grid.step_block, grid.store_levels, grid.dt, dz, dy, dx, grid.src_scale, vmax)
 
 
 # ---------------------------------------------------------------- argument prep

@@ -30,7 +30,7 @@ def test_header_declarations_exported():
 def test_version_and_strerror():
     from neuralmech_gb300 import _lib
     lib = _lib.load()
-    assert lib.wfd_version() >> 16 == 1
+    assert lib.wfd_version() >> 16 == 2
     for code in range(0, -8, -1):
         assert lib.wfd_strerror(code).decode()
     assert lib.wfd_strerror(-99).decode() == "unknown status"
@@ -65,11 +65,29 @@ def test_workspace_bytes_grows_with_gradient():
     assert b16 < i16 < f32
 
 
+def test_workspace_holds_the_kept_levels():
+    """store_levels: the forward keeps the last floor((S - 2) / K) segments'
+    levels, u_{k0 - 1} .. u_nt, one FP32 field of nshot x nz x ld each."""
+    field = 2 * 64 * 104 * 4
+    slot = (field + 255) // 256 * 256
+    _, n0 = _ws(_problem(nt=100, ckpt_every=10))
+    _, n1 = _ws(_problem(nt=100, ckpt_every=10, store_levels=12))  # = K + 2: the minimum
+    _, n4 = _ws(_problem(nt=100, ckpt_every=10, store_levels=45))  # 4 segments: 42 levels
+    _, n9 = _ws(_problem(nt=100, ckpt_every=10, store_levels=10 ** 6))  # all 10 segments
+    assert n1 == n0
+    assert n4 - n0 == (42 - 12) * slot
+    assert n9 - n0 == (102 - 12) * slot
+    # the L u stores (FP32, BF16) do not use it
+    _, f0 = _ws(_problem(nt=100, ckpt_every=10, lap_store=2))
+    _, f9 = _ws(_problem(nt=100, ckpt_every=10, lap_store=2, store_levels=10 ** 6))
+    assert f0 == f9
+
+
 @pytest.mark.parametrize("bad,code", [
     (dict(ndim=4), -1), (dict(order=6), -1), (dict(ny=3), -1), (dict(nz=8), -1),
     (dict(nshot=0), -1), (dict(nt=0), -1), (dict(dt=0.0), -1), (dict(dx=-1.0), -1),
-    (dict(ckpt_format=3), -1), (dict(ckpt_every=-1), -1),
-    (dict(vmax=1e6), -4),
+    (dict(ckpt_format=3), -1), (dict(ckpt_every=-1), -1), (dict(lap_store=3), -1),
+    (dict(store_levels=-1), -1), (dict(vmax=1e6), -4),
 ])
 def test_invalid_problems_rejected(bad, code):
     from neuralmech_gb300 import _lib
@@ -100,3 +118,21 @@ def test_null_workspace_and_arguments_rejected():
     buf = ctypes.create_string_buffer(4096 + 16)
     a = ctypes.c_void_p((ctypes.addressof(buf) + 15) // 16 * 16)
     assert lib.wfd_step2d_order2(a, a, a, 1.0, 1.0, 1.0, 1.0, 10, 10, 13, None) == -1
+
+
+def test_problem_struct_mirrors_header():
+    """_lib.Problem has the fields of wfd_problem in the header's order and types."""
+    import re
+    from neuralmech_gb300 import _lib
+    src = open(os.path.join(ROOT, "include", "wavefd.h")).read()
+    body = re.search(r"typedef struct wfd_problem \{(.*?)\} wfd_problem;", src, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        ctype, names = decl.split(None, 1)
+        fields += [(n.strip(), ctype) for n in names.split(",")]
+    mirror = [(n, {ctypes.c_int32: "int32_t", ctypes.c_float: "float"}[t]) for n, t in _lib.Problem._fields_]
+    assert mirror == fields

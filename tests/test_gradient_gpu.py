@@ -98,6 +98,34 @@ def test_u_store_matches_lap_store(cuda, orc, order, shape, nt, ckpt, rows, grou
     assert rel_l2(gwa.cpu().numpy(), gwf.cpu().numpy()) < 1e-6
 
 
+@pytest.mark.parametrize("nt,ckpt,levels", [(100, 13, 30), (100, 13, 10 ** 6), (61, 20, 45)])
+def test_kept_levels_match_recompute(cuda, orc, nt, ckpt, levels):
+    """store_levels: the forward keeps the levels of its last segments and the
+    adjoint recomputes only the others. With FP32 checkpoints the recompute
+    reproduces the kept levels exactly, so the gradients agree to summation
+    order (1e-6); with BF16 checkpoints the kept levels are the exact forward
+    ones, and the gradient is no further from the FP64 oracle than before."""
+    import dataclasses
+    from neuralmech_gb300 import misfit_gradient
+    grid, v, wav, src, rec = small_problem(shape=(72, 210), nshot=4, nt=nt, ckpt_every=ckpt, seed=8)
+    obs = _observed(orc, grid, v, wav, src, rec)
+    args = (torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+            torch.from_numpy(rec), torch.from_numpy(obs).to(cuda))
+    _, gr, gwr, _ = orc.gradient(oracle_geometry(orc, grid, v, wav, src, rec), obs)
+    res = {}
+    for fmt in ("fp32", "bf16"):
+        for lv in (0, levels):
+            g = dataclasses.replace(grid, ckpt_format=fmt, store_levels=lv)
+            res[fmt, lv] = misfit_gradient(*args, g, want_wavelet=True)
+    for k in (1, 2):
+        assert rel_l2(res["fp32", levels][k].cpu().numpy(), res["fp32", 0][k].cpu().numpy()) < 1e-6
+    e_rec = rel_l2(res["bf16", 0][1].cpu().numpy(), gr)
+    e_kept = rel_l2(res["bf16", levels][1].cpu().numpy(), gr)
+    print(f"bf16 checkpoints: gradient rel L2 {e_rec:.2e} recomputed, {e_kept:.2e} with kept levels")
+    assert e_kept <= 1.05 * e_rec
+    assert rel_l2(res["bf16", levels][2].cpu().numpy(), gwr) < 5e-3
+
+
 def test_autograd_matches_fused_call(cuda, orc):
     from neuralmech_gb300 import misfit_gradient, wave_forward
     grid, v, wav, src, rec = small_problem(shape=(50, 140), nshot=2, nt=70, seed=11)

@@ -459,6 +459,7 @@ struct Stepper {
         a.tiles_x = g.tiles_x; a.tiles_y = g.tiles_y; a.tiles_z = g.tiles_z;
         a.c0 = g.c0;
         for (int k = 0; k < 4; ++k) { a.cz[k] = g.cz[k]; a.cy[k] = g.cy[k]; a.cx[k] = g.cx[k]; }
+        a.zero_ring = 1;  // the wave path's ring is 0 in every level
         a.err = err;
         return a;
     }
@@ -603,9 +604,6 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
         if (us) return fail(WFD_ERR_INVALID, "internal: final level requested from a u-store forward");
         *final_buf = p->nt & 1;
     }
-    if (us)  // the fixed outer ring of every slot (the kernel writes the interior only)
-        WFD_CUDA(launch_zero_ring2d(w.slot(L, 0), L.lap_field_bytes / 4, nslot, g.cells, p->nshot,
-                                    g.nz, g.nx, g.ld, g.R, s));
     WFD_CUDA(cudaMemsetAsync(buf[loc(-1)], 0, L.field_bytes, s));
     WFD_CUDA(cudaMemsetAsync(buf[loc(0)], 0, L.field_bytes, s));
     std::vector<CUtensorMap> mc(buf.size()), mo(buf.size());

@@ -237,47 +237,6 @@ cudaError_t launch_vel_to_m(const float* vel, float* m, int nz, int ny, int nx, 
     return cudaGetLastError();
 }
 
-namespace {
-
-// Zeroes the fixed outer ring (R cells wide) of nslot x nshot 2D fields
-// [nz][ld]; slot i, shot j starts at base + i slot_stride + j shot_stride.
-__global__ void zero_ring2d_kernel(float* base, long long slot_stride, int nslot,
-                                   long long shot_stride, int nshot, int nz, int nx, int ld, int R) {
-    const int rows = 2 * R * nx;                // the R top and R bottom rows
-    const int ring = rows + 2 * R * (nz - 2 * R);  // + R cells at each end of the other rows
-    const long long total = (long long)nslot * nshot * ring;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const long long f = i / ring;
-        int c = int(i - f * ring), z, x;
-        if (c < rows) {
-            const int r = c / nx;
-            x = c - r * nx;
-            z = r < R ? r : nz - 2 * R + r;
-        } else {
-            c -= rows;
-            const int r = c / (2 * R), e = c - r * (2 * R);
-            z = R + r;
-            x = e < R ? e : nx - 2 * R + e;
-        }
-        const long long slot = f / nshot, shot = f - slot * nshot;
-        base[slot * slot_stride + shot * shot_stride + (long long)z * ld + x] = 0.f;
-    }
-}
-
-}  // namespace
-
-cudaError_t launch_zero_ring2d(float* base, long long slot_stride, int nslot, long long shot_stride,
-                               int nshot, int nz, int nx, int ld, int R, cudaStream_t s) {
-    const long long total = (long long)nslot * nshot * (2 * R * nx + 2 * R * (nz - 2 * R));
-    if (total <= 0) return cudaSuccess;
-    const int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 16);
-    zero_ring2d_kernel<<<blocks, 256, 0, s>>>(base, slot_stride, nslot, shot_stride, nshot, nz, nx,
-                                              ld, R);
-    count_launch();
-    return cudaGetLastError();
-}
-
 cudaError_t launch_build_lists(const int32_t* pos, int nshot, int np, int nz, int ny, int nx,
                                int ld, int R, int tile_z, int tile_y, int tile_x, int tiles_z,
                                int tiles_y, int tiles_x, int* counts, int* off, int2* ent,

@@ -74,6 +74,8 @@ struct StepArgs {
     void* lap;                 // [nshot][cells] FP32 or BF16
     int lap_bf16;
     float* grad;               // [cells], MODE_GRAD accumulation target
+    int zero_ring;             // 2D one-step kernel: also write the fixed ring (and the row
+                               // padding) of u_new, as 0; else leave those cells untouched
     unsigned* err;
 };
 
@@ -149,9 +151,6 @@ cudaError_t launch_build_lists(const int32_t* pos, int nshot, int np, int nz, in
                                int ld, int R, int tile_z, int tile_y, int tile_x, int tiles_z,
                                int tiles_y, int tiles_x, int* counts, int* off, int2* ent,
                                unsigned* err, cudaStream_t s, int halo_z = 0, int halo_x = 0);
-// Zeroes the R-cell outer ring of nslot x nshot 2D fields (slot / shot strides in floats).
-cudaError_t launch_zero_ring2d(float* base, long long slot_stride, int nslot, long long shot_stride,
-                               int nshot, int nz, int nx, int ld, int R, cudaStream_t s);
 cudaError_t launch_gather(const float* u, long long shot_stride, PointLists lists, int ntiles,
                           int nshot, int np, const float* m, float scale, int div_m,
                           float* out, int out_nt, int out_t, cudaStream_t s);

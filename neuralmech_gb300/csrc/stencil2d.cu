@@ -8,7 +8,9 @@
 // which is the R = 1, g = 1, constant-m case.
 //
 // Layout in HBM: each field is [shot][z][ld] FP32, ld a multiple of 8; the
-// model m is [z][ld], shared by all shots. u_{n+1} overwrites u_{n-1} in place.
+// model m is [z][ld], shared by all shots. u_{n+1} overwrites u_{n-1} in place
+// (or goes to a fresh buffer: the kernel writes every cell of its tile, the
+// fixed ring as 0).
 //
 // Per CTA (256 threads): a 128 x TZ tile (TZ = 32 or 16 rows) of one shot at a time, over
 // `shots_per_cta` shots of the batch. For each shot a TMA bulk-tensor load
@@ -56,6 +58,39 @@ struct Layout2D {
 
 __device__ __forceinline__ float comp(const float4& v, int e) {
     return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+}
+
+// L u at the four cells of a row: horizontal taps from (lv, cv, rv), vertical
+// taps from the register window V (centre row C). The cells go in pairs
+// through the packed FP32x2 arithmetic of sm_100+, with the operations and
+// their order of the scalar form c0 u + sum_k cx_k (u_{x-k} + u_{x+k}) +
+// cz_k (u_{z-k} + u_{z+k}), accumulated k = 1 .. R with x before z.
+template <int R, int N>
+__device__ __forceinline__ float4 lap_row(const float4& lv, const float4& cv, const float4& rv,
+                                          const float4 (&V)[N], int C, const StepArgs& a) {
+    const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y, cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
+    const float2 c0 = make_float2(a.c0, a.c0);
+    float2 lo = __fmul2_rn(c0, make_float2(cv.x, cv.y));
+    float2 hi = __fmul2_rn(c0, make_float2(cv.z, cv.w));
+#pragma unroll
+    for (int k = 1; k <= R; ++k) {
+        const float2 cx = make_float2(a.cx[k - 1], a.cx[k - 1]);
+        const float2 cz = make_float2(a.cz[k - 1], a.cz[k - 1]);
+        float2 xl, xh;
+        if (k % 2 == 0) {  // the x taps form aligned register pairs
+            xl = __fadd2_rn(make_float2(w[4 - k], w[5 - k]), make_float2(w[4 + k], w[5 + k]));
+            xh = __fadd2_rn(make_float2(w[6 - k], w[7 - k]), make_float2(w[6 + k], w[7 + k]));
+        } else {
+            xl = make_float2(w[4 - k] + w[4 + k], w[5 - k] + w[5 + k]);
+            xh = make_float2(w[6 - k] + w[6 + k], w[7 - k] + w[7 + k]);
+        }
+        lo = __ffma2_rn(cx, xl, lo);
+        hi = __ffma2_rn(cx, xh, hi);
+        const float4 up = V[C - k], dn = V[C + k];
+        lo = __ffma2_rn(cz, __fadd2_rn(make_float2(up.x, up.y), make_float2(dn.x, dn.y)), lo);
+        hi = __ffma2_rn(cz, __fadd2_rn(make_float2(up.z, up.w), make_float2(dn.z, dn.w)), hi);
+    }
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
 }
 
 template <int R, int MODE, int RB>
@@ -168,18 +203,10 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ?
                 const float4 rv = *reinterpret_cast<const float4*>(row + 2 * T2_XH);
                 const float4 qv =
                     *reinterpret_cast<const float4*>(cur + (warp * RB + r + R) * T2_W + T2_XH + 4 * lane);
-                const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y, cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
+                const float4 lu = lap_row<R>(lv, cv, rv, W, r + R, a);
                 float l4[4];
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    float acc = a.c0 * w[4 + e];
-#pragma unroll
-                    for (int k = 1; k <= R; ++k) {
-                        acc = fmaf(a.cx[k - 1], w[4 + e - k] + w[4 + e + k], acc);
-                        acc = fmaf(a.cz[k - 1], comp(W[r + R - k], e) + comp(W[r + R + k], e), acc);
-                    }
-                    l4[e] = xin[e] ? comp(qv, e) * acc : 0.f;
-                }
+                for (int e = 0; e < 4; ++e) l4[e] = xin[e] ? comp(qv, e) * comp(lu, e) : 0.f;
                 gacc[r].x += l4[0];
                 gacc[r].y += l4[1];
                 gacc[r].z += l4[2];
@@ -199,27 +226,28 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ?
             const float4 lv = *reinterpret_cast<const float4*>(row);
             const float4 cv = V[r + R];
             const float4 rv = *reinterpret_cast<const float4*>(row + 2 * T2_XH);
-            const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y,
-                                 cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
             const float4 ov =
                 *reinterpret_cast<const float4*>(old + (warp * RB + r) * T2_TX + 4 * lane);
+            const float4 l = lap_row<R>(lv, cv, rv, V, r + R, a);
             float lap[4], nv[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-                float acc = a.c0 * w[4 + e];
-#pragma unroll
-                for (int k = 1; k <= R; ++k) {
-                    acc = fmaf(a.cx[k - 1], w[4 + e - k] + w[4 + e + k], acc);
-                    acc = fmaf(a.cz[k - 1], comp(V[r + R - k], e) + comp(V[r + R + k], e), acc);
-                }
+                const float acc = comp(l, e);
                 lap[e] = acc;
                 const float g = gzr[r] * gxe[e];
-                const float c = w[4 + e];
+                const float c = comp(cv, e);
                 nv[e] = g * fmaf(comp(mrow[r], e), acc, 2.f * c) - (g * g) * comp(ov, e);
             }
             const long long off = (long long)z * a.ld + x;
             if (zin[r] && all_x) {
                 *reinterpret_cast<float4*>(un + off) = make_float4(nv[0], nv[1], nv[2], nv[3]);
+            } else if (a.zero_ring) {
+                // the fixed ring (and the row padding) as 0, so that a level
+                // written to a fresh buffer needs no separate clearing
+                if (z < a.nz && x < a.ld)  // (ld is a multiple of 8: x + 3 < ld)
+                    *reinterpret_cast<float4*>(un + off) =
+                        make_float4(zin[r] && xin[0] ? nv[0] : 0.f, zin[r] && xin[1] ? nv[1] : 0.f,
+                                    zin[r] && xin[2] ? nv[2] : 0.f, zin[r] && xin[3] ? nv[3] : 0.f);
             } else if (zin[r]) {
 #pragma unroll
                 for (int e = 0; e < 4; ++e)

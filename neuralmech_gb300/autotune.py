@@ -4,7 +4,8 @@ For a problem key (architecture, grid shape, order, shots) it times a short
 forward (`steps` time steps) for every candidate:
   * one step per launch: tile_rows (16 or 32) x shots_per_cta (1, 2, 4, ...
     up to 32 and the shot count);
-  * two steps per launch (step_block 2, 120 x 32 tiles, one shot per CTA).
+  * two steps per launch (step_block 2, 120 x 32 tiles) x shots_per_cta
+    (automatic, 1, 2, 4, ...).
 
 It keeps the fastest, and caches the choice in a JSON file (default
 ``~/.cache/neuralmech_gb300/autotune.json``, or ``$WAVEFD_AUTOTUNE_CACHE``).
@@ -52,7 +53,8 @@ def candidates(nshot: int):
     if nshot <= 32 and nshot not in spcs:
         spcs.append(nshot)
     one = [{"tile_rows": tr, "shots_per_cta": s, "step_block": 1} for tr in (32, 16) for s in spcs]
-    return one + [{"tile_rows": 0, "shots_per_cta": 0, "step_block": 2}]
+    two = [{"tile_rows": 0, "shots_per_cta": s, "step_block": 2} for s in [0] + spcs]
+    return one + two
 
 
 def select(timings: dict) -> dict:

@@ -199,6 +199,8 @@ int check_problem(const wfd_problem* p) {
         return fail(WFD_ERR_INVALID, "tile_rows must be 0, 16 or 32");
     if (p->step_block < 0 || p->step_block > 2 || (p->step_block == 2 && p->ndim != 2))
         return fail(WFD_ERR_INVALID, "step_block must be 0, 1 or 2 (2: 2D only)");
+    if (p->step_block == 2 && p->lap_store != WFD_LAP_AUTO)
+        return fail(WFD_ERR_INVALID, "step_block 2 keeps the levels u_k: lap_store must be WFD_LAP_AUTO");
     if (p->ckpt_every < 0 || p->shots_per_cta < 0 || p->group_shots < 0 || p->store_levels < 0)
         return fail(WFD_ERR_INVALID,
                     "ckpt_every, shots_per_cta, group_shots and store_levels must be >= 0");
@@ -217,9 +219,10 @@ int check_problem(const wfd_problem* p) {
     return WFD_OK;
 }
 
-// tile_rows > 0 overrides the problem's 2D tile height (the u-store adjoint
-// runs on 16-row tiles: its second staged tile must leave room for two stages).
-Geom make_geom(const wfd_problem* p, int tile_rows = 0) {
+// tile_rows > 0 overrides the problem's 2D tile height and step_block >= 1
+// its steps per launch (the u-store adjoint runs one step per launch on
+// 16-row tiles: its third staged tile must leave room for the stages).
+Geom make_geom(const wfd_problem* p, int tile_rows = 0, int step_block = 0) {
     Geom g{};
     g.ndim = p->ndim;
     g.R = p->order / 2;
@@ -229,7 +232,8 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0) {
     g.ld = (p->nx + 7) / 8 * 8;
     g.plane = (long long)g.ny * g.ld;
     g.cells = (long long)g.nz * g.plane;
-    g.sb = (p->ndim == 2 && p->step_block == 2) ? 2 : 1;
+    const int sb = step_block > 0 ? step_block : p->step_block;
+    g.sb = (p->ndim == 2 && sb == 2) ? 2 : 1;
     if (g.ndim == 2 && g.sb == 2) {
         g.tile_z = K2_TZ;
         g.tile_y = 1;
@@ -245,8 +249,8 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0) {
     g.tiles_y = cdiv(g.ny, g.tile_y);
     g.tiles_x = cdiv(g.nx, g.tile_x);
     g.ntiles = g.tiles_z * g.tiles_y * g.tiles_x;
-    if (g.ndim == 3 || g.sb == 2) {
-        g.spc = 1;  // a 3D or two-step CTA works on one shot
+    if (g.ndim == 3) {
+        g.spc = 1;  // a 3D CTA works on one shot
     } else if (p->shots_per_cta > 0) {
         g.spc = std::min(std::min(p->shots_per_cta, p->nshot), T2_MAX_SPC);
     } else {
@@ -263,7 +267,7 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0) {
                             : std::max(1, (int)std::ceil(std::sqrt((double)p->nt)));
     g.nseg = cdiv(p->nt, g.K);
     g.k0_last = (g.nseg - 1) * g.K;
-    g.ustore = g.ndim == 2 && g.sb == 1 && p->lap_store == WFD_LAP_AUTO;
+    g.ustore = g.ndim == 2 && p->lap_store == WFD_LAP_AUTO;
     g.jstore = g.nseg - 1;
     if (g.ustore && p->store_levels > g.K + 2)
         g.jstore = std::max(0, g.nseg - (p->store_levels - 2) / g.K);
@@ -284,14 +288,14 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0) {
 
 // Geometry of the adjoint launches: 16-row tiles for the u-store adjoint.
 Geom adjoint_geom(const wfd_problem* p, const Geom& g) {
-    return g.ustore && g.tile_z != 16 ? make_geom(p, 16) : g;
+    return g.ustore && (g.tile_z != 16 || g.sb != 1) ? make_geom(p, 16, 1) : g;
 }
 
 // ------------------------------------------------------------------ workspace
 struct Layout {
-    int nbuf;  // field buffers per direction: 2 (in place) or 4 (two-step blocking)
+    int nbuf;  // forward field buffers: 2 (in place) or 4 (two-step blocking)
     size_t err, m, P[4], counts, src_off, src_ent, rec_off, rec_ent;
-    size_t srce_off, srce_ent, rece_off, rece_ent;  // extended-region lists (two-step)
+    size_t srce_off, srce_ent;  // extended-region source lists (two-step)
     size_t asrc_off, asrc_ent, arec_off, arec_ent;  // adjoint-geometry lists (u store)
     size_t Q[4], G, ckpt, lap, res, total;
     size_t field_bytes, ckpt_field_bytes, lap_field_bytes;
@@ -306,7 +310,7 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o = up256(o + bytes); return at; };
     const Geom ga = adjoint_geom(p, g);
-    const bool alists = grad && ga.tile_z != g.tile_z;
+    const bool alists = grad && (ga.tile_z != g.tile_z || ga.tile_x != g.tile_x);
     const size_t keys = (size_t)p->nshot * std::max(g.ntiles, alists ? ga.ntiles : 0);
     L.field_bytes = (size_t)p->nshot * g.cells * 4;
     L.nbuf = g.sb == 2 ? 4 : 2;
@@ -321,8 +325,6 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     if (g.sb == 2) {  // a point joins up to 4 extended tile regions
         L.srce_off = take((keys + 1) * 4);
         L.srce_ent = take((size_t)p->nshot * p->nsrc * 32 + 8);
-        L.rece_off = take((keys + 1) * 4);
-        L.rece_ent = take((size_t)p->nshot * p->nrec * 32 + 8);
     }
     if (alists) {
         const size_t akeys = (size_t)p->nshot * ga.ntiles;
@@ -336,7 +338,7 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
         L.ckpt_field_bytes = up256(ckpt_bytes(p->ckpt_format, (long long)p->nshot * g.cells));
         L.lap_field_bytes = up256((size_t)p->nshot * g.cells * (g.lap_bf16 ? 2 : 4));
         L.nlap = g.ustore ? std::max(g.K + 2, p->nt - g.k0_store + 2) : g.K;
-        for (int b = 0; b < L.nbuf; ++b) L.Q[b] = take(L.field_bytes);
+        for (int b = 0; b < 2; ++b) L.Q[b] = take(L.field_bytes);  // (the adjoint is one-step)
         L.G = take((size_t)g.cells * 4);
         L.ckpt = take((size_t)g.nseg * 2 * L.ckpt_field_bytes);
         L.lap = take((size_t)L.nlap * L.lap_field_bytes);
@@ -350,7 +352,7 @@ struct Work {
     unsigned* err;
     float *m, *P[4], *Q[4], *G, *res;
     int* counts;
-    PointLists src, rec, src_e, rec_e;
+    PointLists src, rec, src_e;
     PointLists src_a, rec_a;  // lists of the adjoint geometry (== src, rec unless u store)
     unsigned char *ckpt, *lap;
     bool own_alists;          // src_a / rec_a are separate lists that setup() builds
@@ -373,8 +375,6 @@ Work carve(void* ws, const Layout& L, bool grad) {
     if (L.nbuf == 4) {
         w.src_e.off = reinterpret_cast<int*>(b + L.srce_off);
         w.src_e.ent = reinterpret_cast<int2*>(b + L.srce_ent);
-        w.rec_e.off = reinterpret_cast<int*>(b + L.rece_off);
-        w.rec_e.ent = reinterpret_cast<int2*>(b + L.rece_ent);
     }
     w.src_a = w.src;
     w.rec_a = w.rec;
@@ -386,7 +386,7 @@ Work carve(void* ws, const Layout& L, bool grad) {
         w.rec_a.ent = reinterpret_cast<int2*>(b + L.arec_ent);
     }
     if (grad) {
-        for (int k = 0; k < L.nbuf; ++k) w.Q[k] = reinterpret_cast<float*>(b + L.Q[k]);
+        for (int k = 0; k < 2; ++k) w.Q[k] = reinterpret_cast<float*>(b + L.Q[k]);
         w.G = reinterpret_cast<float*>(b + L.G);
         w.ckpt = b + L.ckpt;
         w.lap = b + L.lap;
@@ -424,9 +424,8 @@ struct Stepper {
             const cuuint64_t strides[1] = {(cuuint64_t)g.ld * 4};
             const cuuint32_t box[2] = {K2_EW, cuuint32_t(K2_TZ + 2 * g.R)}, estr[2] = {1, 1};
             CUresult r = enc(&map_m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(m), dims,
-                             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
             if (r != CUDA_SUCCESS) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled (m) failed (%d)", (int)r);
             return WFD_OK;
         }
@@ -496,14 +495,8 @@ struct Stepper {
         return make_field_map(mo, buf, false, 2, g.nz, 1, g.nx, g.ld, p->nshot, bo);
     }
 
-    int lap_map_k2(const void* lap, bool bf16, CUtensorMap* ml) const {
-        const cuuint32_t b[3] = {K2_TX, K2_TZ, 1};
-        return make_field_map(ml, lap, bf16, 2, g.nz, 1, g.nx, g.ld, p->nshot, b);
-    }
-
-    int launch_k2(int mode, const CUtensorMap& mu, const CUtensorMap& mo, const CUtensorMap& l1,
-                  const CUtensorMap& l2, const Step2Args& q) const {
-        cudaError_t e = launch_step2d_k2(g.R, mode, mu, mo, map_m, l1, l2, q, s);
+    int launch_k2(const CUtensorMap& mu, const CUtensorMap& mo, const Step2Args& q) const {
+        cudaError_t e = launch_step2d_k2(g.R, mu, mo, map_m, q, s);
         if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "two-step launch failed: %s", cudaGetErrorString(e));
         return WFD_OK;
     }
@@ -555,10 +548,6 @@ int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
                                     g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
                                     const_cast<int*>(w.src_e.off), const_cast<int2*>(w.src_e.ent),
                                     w.err, s, g.R, 4));
-        WFD_CUDA(launch_build_lists(rec, p->nshot, p->nrec, g.nz, g.ny, g.nx, g.ld, g.R, g.tile_z,
-                                    g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
-                                    const_cast<int*>(w.rec_e.off), const_cast<int2*>(w.rec_e.ent),
-                                    w.err, s, g.R, 4));
     }
     if (w.own_alists) {  // the u-store adjoint's 16-row tiles
         const Geom a = adjoint_geom(p, g);
@@ -574,51 +563,86 @@ int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
     return WFD_OK;
 }
 
-int run_forward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
-                   const Stepper& st, const float* wavelet, float* traces, bool save,
-                   int* final_buf);
-int run_backward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
-                    const Stepper& st, const float* wavelet, const float* dtraces, float* grad_vel,
-                    float* grad_wavelet, const float* vel, bool zero_G, bool finalize);
 
-// Forward time loop. With save: checkpoints every K steps and the L u store of
-// the last segment (which the backward then does not recompute).
-// final_buf (optional) receives the index of the buffer that holds u_nt.
+// Forward time loop. With save: checkpoints every K steps and, for the
+// adjoint's imaging term, either the kept levels (u store) or the L u store
+// of the last segment (which the backward then does not recompute).
+// final_buf (optional) receives the index of the buffer P[] that holds u_nt.
+//
+// Level u_k lives in P[k % nP]: nP = 2 with one step per launch (u_{k+1}
+// overwrites u_{k-1} in place), nP = 4 with two (a launch reads u_{k-1}, u_k
+// and writes u_{k+1}, u_{k+2}, none of which alias). With the u store the
+// levels of the kept segments, from u_{k0_store - 1} on, go to the store's
+// slots k - k0_store + 1 for the adjoint to read instead.
 int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                 const Stepper& st, const float* wavelet, float* traces, bool save,
                 int* final_buf = nullptr) {
-    if (g.sb == 2) return run_forward_k2(p, g, L, w, st, wavelet, traces, save, final_buf);
     cudaStream_t s = st.s;
-    // Level u_k lives in P[k & 1] (u_{k+1} overwrites u_{k-1} in place), except
-    // that with the u store the levels of the kept segments, from
-    // u_{k0_store - 1} on, go to the store's slots k - k0_store + 1 for the
-    // adjoint to read.
     const bool us = save && g.ustore;
+    const int np = L.nbuf;
     const int nslot = us ? L.nlap : 0;
-    auto loc = [&](int k) -> int { return us && k >= g.k0_store - 1 ? 2 + (k - g.k0_store + 1) : (k & 1); };
-    std::vector<float*> buf(2 + nslot);
-    buf[0] = w.P[0];
-    buf[1] = w.P[1];
-    for (int i = 0; i < nslot; ++i) buf[2 + i] = w.slot(L, i);
+    auto loc = [&](int k) -> int {
+        return us && k >= g.k0_store - 1 ? np + (k - g.k0_store + 1) : ((k % np) + np) % np;
+    };
+    std::vector<float*> buf(np + nslot);
+    for (int b = 0; b < np; ++b) buf[b] = w.P[b];
+    for (int i = 0; i < nslot; ++i) buf[np + i] = w.slot(L, i);
     if (final_buf) {
         if (us) return fail(WFD_ERR_INVALID, "internal: final level requested from a u-store forward");
-        *final_buf = p->nt & 1;
+        *final_buf = loc(p->nt);
     }
     WFD_CUDA(cudaMemsetAsync(buf[loc(-1)], 0, L.field_bytes, s));
     WFD_CUDA(cudaMemsetAsync(buf[loc(0)], 0, L.field_bytes, s));
     std::vector<CUtensorMap> mc(buf.size()), mo(buf.size());
     int rc;
     for (size_t b = 0; b < buf.size(); ++b)
-        if ((rc = st.map_pair(buf[b], buf[b], &mc[b], &mo[b]))) return rc;
+        if ((rc = g.sb == 2 ? st.map_k2(buf[b], &mc[b], &mo[b]) : st.map_pair(buf[b], buf[b], &mc[b], &mo[b])))
+            return rc;
     const long long n_all = (long long)p->nshot * g.cells;
-    PhaseScope scope(PH_FORWARD, s, p->nt);
-    for (int n = 0; n < p->nt; ++n) {
-        const int bo = loc(n - 1), bc = loc(n), bn = loc(n + 1);
-        if (save && n % g.K == 0 && !(us && n >= g.k0_store)) {  // (kept segments need none)
-            unsigned char* slot = w.ckpt + (size_t)(n / g.K) * 2 * L.ckpt_field_bytes;
-            WFD_CUDA(launch_pack(buf[bo], slot, n_all, p->ckpt_format, s));
-            WFD_CUDA(launch_pack(buf[bc], slot + L.ckpt_field_bytes, n_all, p->ckpt_format, s));
+    auto checkpoint = [&](int n) -> int {  // (u_{n-1}, u_n) at the start of segment n / K
+        if (!save || n % g.K != 0 || (us && n >= g.k0_store)) return WFD_OK;  // (kept segments need none)
+        unsigned char* slot = w.ckpt + (size_t)(n / g.K) * 2 * L.ckpt_field_bytes;
+        WFD_CUDA(launch_pack(buf[loc(n - 1)], slot, n_all, p->ckpt_format, s));
+        WFD_CUDA(launch_pack(buf[loc(n)], slot + L.ckpt_field_bytes, n_all, p->ckpt_format, s));
+        return WFD_OK;
+    };
+    PhaseScope scope(PH_FORWARD, s, g.sb == 2 ? (p->nt + 1) / 2 : p->nt);
+    for (int n = 0; n < p->nt;) {
+        if (g.sb == 2) {
+            // u_{n+1} and u_{n+2} from (u_{n-1}, u_n); no buffer the launch reads is written
+            const bool two = n + 1 < p->nt;
+            Step2Args q{};
+            q.a = st.base(buf[loc(two ? n + 2 : n + 1)]);
+            q.u_mid = buf[loc(n + 1)];
+            q.two_steps = two;
+            q.inj_t1 = -1;
+            q.a.inj_t = -1;
+            if (p->nsrc > 0) {
+                q.inj_e = w.src_e;
+                q.inj_t1 = n;
+                q.a.inj = w.src;
+                q.a.inj_val = wavelet;
+                q.a.inj_np = p->nsrc; q.a.inj_nt = p->nt; q.a.inj_t = two ? n + 1 : -1;
+                q.a.inj_scale = p->src_scale;
+            }
+            q.smp_t1 = -1;
+            q.a.smp_t = -1;
+            if (traces && p->nrec > 0) {
+                q.a.smp = w.rec;
+                q.a.smp_out = traces;
+                q.a.smp_np = p->nrec; q.a.smp_nt = p->nt;
+                q.a.smp_scale = 1.f;
+                q.smp_t1 = n - 1;
+                q.a.smp_t = two ? n : -1;
+            }
+            if ((rc = st.launch_k2(mc[loc(n)], mo[loc(n - 1)], q))) return rc;
+            for (int k = n; k < n + (two ? 2 : 1); ++k)  // (every level read there is still held)
+                if ((rc = checkpoint(k))) return rc;
+            n += two ? 2 : 1;
+            continue;
         }
+        if ((rc = checkpoint(n))) return rc;
+        const int bo = loc(n - 1), bc = loc(n), bn = loc(n + 1);
         const bool lap = save && !g.ustore && n >= g.k0_last;
         StepArgs a = st.base(buf[bn]);
         a.inj = w.src;
@@ -637,215 +661,11 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
             a.lap_bf16 = g.lap_bf16;
         }
         if ((rc = st.launch(lap ? MODE_SAVE_LAP : MODE_PLAIN, mc[bc], mo[bo], mc[bc], a))) return rc;
+        ++n;
     }
     if (traces && p->nrec > 0)
         WFD_CUDA(launch_gather(buf[loc(p->nt)], g.cells, w.rec, g.ntiles, p->nshot, p->nrec, nullptr,
                                1.f, 0, traces, p->nt, p->nt - 1, s));
-    return WFD_OK;
-}
-
-// ------------------------------------------------------------------ two-step loops
-// Buffers rotate through four slots: a launch reads (u_{n-1}, u_n) from two of
-// them and writes (u_{n+1}, u_{n+2}) to the other two (one step: u_{n+1} only).
-struct Levels {
-    int old_, cur;
-    void free_pair(int& f0, int& f1) const {
-        int k = 0, f[2] = {0, 0};
-        for (int b = 0; b < 4 && k < 2; ++b)
-            if (b != old_ && b != cur) f[k++] = b;
-        f0 = f[0];
-        f1 = f[1];
-    }
-    void advance(bool two, int f0, int f1) {
-        if (two) {
-            old_ = f0;
-            cur = f1;
-        } else {
-            old_ = cur;
-            cur = f0;
-        }
-    }
-};
-
-int run_forward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
-                   const Stepper& st, const float* wavelet, float* traces, bool save,
-                   int* final_buf) {
-    cudaStream_t s = st.s;
-    for (int b = 0; b < 4; ++b) WFD_CUDA(cudaMemsetAsync(w.P[b], 0, L.field_bytes, s));
-    CUtensorMap mu[4], mo[4], none{};
-    int rc;
-    for (int b = 0; b < 4; ++b)
-        if ((rc = st.map_k2(w.P[b], &mu[b], &mo[b]))) return rc;
-    const long long n_all = (long long)p->nshot * g.cells;
-    Levels lv{0, 1};
-    PhaseScope scope(PH_FORWARD, s, (p->nt + 1) / 2);
-    for (int n = 0; n < p->nt;) {
-        if (save && n % g.K == 0) {
-            unsigned char* slot = w.ckpt + (size_t)(n / g.K) * 2 * L.ckpt_field_bytes;
-            WFD_CUDA(launch_pack(w.P[lv.old_], slot, n_all, p->ckpt_format, s));
-            WFD_CUDA(launch_pack(w.P[lv.cur], slot + L.ckpt_field_bytes, n_all, p->ckpt_format, s));
-        }
-        // a launch never spans a checkpoint (nor the start of the stored last segment)
-        const bool two = n + 1 < p->nt && !(save && (n + 1) % g.K == 0);
-        const bool lap = save && n >= g.k0_last;
-        int f0, f1;
-        lv.free_pair(f0, f1);
-        Step2Args q{};
-        q.a = st.base(w.P[f1]);
-        q.u_mid = w.P[f0];
-        q.two_steps = two;
-        q.inj_t1 = -1;
-        q.a.inj_t = -1;
-        if (p->nsrc > 0) {
-            q.inj_e = w.src_e;
-            q.inj_t1 = n;
-            q.a.inj = w.src;
-            q.a.inj_val = wavelet;
-            q.a.inj_np = p->nsrc; q.a.inj_nt = p->nt; q.a.inj_t = two ? n + 1 : -1;
-            q.a.inj_scale = p->src_scale;
-        }
-        q.smp_t1 = -1;
-        q.a.smp_t = -1;
-        if (traces && p->nrec > 0) {
-            q.a.smp = w.rec;
-            q.a.smp_out = traces;
-            q.a.smp_np = p->nrec; q.a.smp_nt = p->nt;
-            q.a.smp_scale = 1.f;
-            q.smp_t1 = n - 1;
-            q.a.smp_t = two ? n : -1;
-        }
-        if (lap) {
-            q.lap1 = w.lap + (size_t)(n - g.k0_last) * L.lap_field_bytes;
-            if (two) q.a.lap = w.lap + (size_t)(n + 1 - g.k0_last) * L.lap_field_bytes;
-            q.a.lap_bf16 = g.lap_bf16;
-        }
-        if ((rc = st.launch_k2(lap ? MODE_SAVE_LAP : MODE_PLAIN, mu[lv.cur], mo[lv.old_], none, none, q)))
-            return rc;
-        lv.advance(two, f0, f1);
-        n += two ? 2 : 1;
-    }
-    if (traces && p->nrec > 0)
-        WFD_CUDA(launch_gather(w.P[lv.cur], g.cells, w.rec, g.ntiles, p->nshot, p->nrec, nullptr, 1.f, 0,
-                               traces, p->nt, p->nt - 1, s));
-    if (final_buf) *final_buf = lv.cur;
-    return WFD_OK;
-}
-
-int run_backward_k2(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
-                    const Stepper& st, const float* wavelet, const float* dtraces, float* grad_vel,
-                    float* grad_wavelet, const float* vel, bool zero_G, bool finalize) {
-    cudaStream_t s = st.s;
-    for (int b = 0; b < 4; ++b) WFD_CUDA(cudaMemsetAsync(w.Q[b], 0, L.field_bytes, s));
-    if (zero_G) WFD_CUDA(cudaMemsetAsync(w.G, 0, (size_t)g.cells * 4, s));
-    int rc;
-    CUtensorMap pu[4], po[4], qu[4], qo[4], none{};
-    for (int b = 0; b < 4; ++b) {
-        if ((rc = st.map_k2(w.P[b], &pu[b], &po[b]))) return rc;
-        if ((rc = st.map_k2(w.Q[b], &qu[b], &qo[b]))) return rc;
-    }
-    std::vector<CUtensorMap> lm(g.K);
-    for (int k = 0; k < g.K; ++k)
-        if ((rc = st.lap_map_k2(w.lap + (size_t)k * L.lap_field_bytes, g.lap_bf16, &lm[k]))) return rc;
-    const long long n_all = (long long)p->nshot * g.cells;
-
-    // adjoint launch at k: q_k (and q_{k-1} when two) from (q_{k+2}, q_{k+1})
-    Levels ql{0, 1};
-    auto adjoint = [&](int k, bool two, bool grad, int k0) -> int {
-        int f0, f1;
-        ql.free_pair(f0, f1);
-        Step2Args q{};
-        q.a = st.base(w.Q[f1]);
-        q.u_mid = w.Q[f0];
-        q.two_steps = two;
-        q.inj_t1 = -1;
-        q.a.inj_t = -1;
-        if (p->nrec > 0) {
-            q.inj_e = w.rec_e;
-            q.inj_t1 = k - 1;
-            q.a.inj = w.rec;
-            q.a.inj_val = dtraces;
-            q.a.inj_np = p->nrec; q.a.inj_nt = p->nt; q.a.inj_t = two ? k - 2 : -1;
-            q.a.inj_scale = 1.f;
-            q.a.inj_times_m = 1;
-        }
-        q.smp_t1 = -1;
-        q.a.smp_t = -1;
-        if (grad_wavelet && p->nsrc > 0 && k <= p->nt - 1) {
-            q.a.smp = w.src;
-            q.a.smp_out = grad_wavelet;
-            q.a.smp_np = p->nsrc; q.a.smp_nt = p->nt;
-            q.a.smp_scale = p->src_scale;
-            q.a.smp_div_m = 1;
-            q.smp_t1 = k;
-            q.a.smp_t = two ? k - 1 : -1;
-        }
-        int mode = MODE_PLAIN;
-        const CUtensorMap* l1 = &none;
-        const CUtensorMap* l2 = &none;
-        if (grad) {
-            mode = MODE_GRAD;
-            q.a.grad = w.G;
-            q.a.lap_bf16 = g.lap_bf16;
-            l1 = &lm[k - k0];
-            if (two) l2 = &lm[k - 1 - k0];
-        }
-        const int r = st.launch_k2(mode, qu[ql.cur], qo[ql.old_], *l1, *l2, q);
-        ql.advance(two, f0, f1);
-        return r;
-    };
-
-    {
-        PhaseScope scope(PH_ADJOINT, s, 1);
-        if ((rc = adjoint(p->nt, false, false, 0))) return rc;  // q_nt: its gradient term is 0
-    }
-    for (int j = g.nseg - 1; j >= 0; --j) {
-        const int k0 = j * g.K, k1 = std::min(p->nt, k0 + g.K);
-        if (j != g.nseg - 1) {
-            PhaseScope scope(PH_RECOMPUTE, s, (k1 - k0 + 1) / 2);
-            const unsigned char* slot = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
-            WFD_CUDA(launch_unpack(slot, w.P[0], n_all, p->ckpt_format, s));
-            WFD_CUDA(launch_unpack(slot + L.ckpt_field_bytes, w.P[1], n_all, p->ckpt_format, s));
-            Levels lv{0, 1};
-            for (int k = k0; k < k1;) {
-                const bool two = k + 1 < k1;
-                int f0, f1;
-                lv.free_pair(f0, f1);
-                Step2Args q{};
-                q.a = st.base(w.P[f1]);
-                q.u_mid = w.P[f0];
-                q.two_steps = two;
-                q.inj_t1 = -1;
-                q.a.inj_t = -1;
-                if (p->nsrc > 0) {
-                    q.inj_e = w.src_e;
-                    q.inj_t1 = k;
-                    q.a.inj = w.src;
-                    q.a.inj_val = wavelet;
-                    q.a.inj_np = p->nsrc; q.a.inj_nt = p->nt; q.a.inj_t = two ? k + 1 : -1;
-                    q.a.inj_scale = p->src_scale;
-                }
-                q.smp_t1 = -1;
-                q.a.smp_t = -1;
-                q.lap1 = w.lap + (size_t)(k - k0) * L.lap_field_bytes;
-                if (two) q.a.lap = w.lap + (size_t)(k + 1 - k0) * L.lap_field_bytes;
-                q.a.lap_bf16 = g.lap_bf16;
-                if ((rc = st.launch_k2(MODE_SAVE_LAP, pu[lv.cur], po[lv.old_], none, none, q))) return rc;
-                lv.advance(two, f0, f1);
-                k += two ? 2 : 1;
-            }
-        }
-        PhaseScope scope(PH_ADJOINT, s, (k1 - std::max(k0, 1) + 1) / 2);
-        const int kmin = std::max(k0, 1);
-        for (int k = k1 - 1; k >= kmin;) {
-            const bool two = k - 1 >= kmin;
-            if ((rc = adjoint(k, two, true, k0))) return rc;
-            k -= two ? 2 : 1;
-        }
-    }
-    if (grad_wavelet && p->nsrc > 0)  // q_1 at the sources -> d J / d w_0
-        WFD_CUDA(launch_gather(w.Q[ql.cur], g.cells, w.src, g.ntiles, p->nshot, p->nsrc, w.m,
-                               p->src_scale, 1, grad_wavelet, p->nt, 0, s));
-    if (finalize) WFD_CUDA(launch_grad_finalize(w.G, vel, grad_vel, g.nz, g.ny, g.nx, g.ld, g.R, s));
     return WFD_OK;
 }
 
@@ -874,7 +694,9 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
     // per slot: u_k as the recompute's u_n / u_{n-1} tiles and as the adjoint's staged u_k
     std::vector<CUtensorMap> uc(L.nlap), uo(L.nlap), ua(L.nlap), unused(L.nlap);
     for (int i = 0; i < L.nlap; ++i) {
-        if ((rc = st.map_pair(w.slot(L, i), w.slot(L, i), &uc[i], &uo[i]))) return rc;
+        if ((rc = g.sb == 2 ? st.map_k2(w.slot(L, i), &uc[i], &uo[i])
+                            : st.map_pair(w.slot(L, i), w.slot(L, i), &uc[i], &uo[i])))
+            return rc;
         if ((rc = sa.map_pair(w.slot(L, i), w.slot(L, i), &ua[i], &unused[i]))) return rc;
     }
     const long long n_all = (long long)p->nshot * g.cells;
@@ -910,20 +732,42 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
         const int k0 = j * g.K, k1 = std::min(p->nt, k0 + g.K);
         const int base = j >= g.jstore ? g.k0_store : k0;  // u_k is in slot k - base + 1
         if (j < g.jstore) {
-            PhaseScope scope(PH_RECOMPUTE, s, k1 - k0 - 1);
+            PhaseScope scope(PH_RECOMPUTE, s, g.sb == 2 ? (k1 - k0) / 2 : k1 - k0 - 1);
             const unsigned char* ck = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
             WFD_CUDA(launch_unpack(ck, w.slot(L, 0), n_all, p->ckpt_format, s));
             WFD_CUDA(launch_unpack(ck + L.ckpt_field_bytes, w.slot(L, 1), n_all, p->ckpt_format, s));
-            for (int k = k0; k + 1 < k1; ++k) {
-                const int i = k - k0 + 1;  // slot of u_k
-                StepArgs a = st.base(w.slot(L, i + 1));
-                if (p->nsrc > 0) {
-                    a.inj = w.src;
-                    a.inj_val = wavelet;
-                    a.inj_np = p->nsrc; a.inj_nt = p->nt; a.inj_t = k;
-                    a.inj_scale = p->src_scale;
+            for (int k = k0; k + 1 < k1;) {  // u_{k+1} (and u_{k+2}) up to u_{k1-1}
+                const int i = k - k0 + 1;     // slot of u_k
+                const bool two = g.sb == 2 && k + 2 < k1;
+                if (g.sb == 2) {
+                    Step2Args q{};
+                    q.a = st.base(w.slot(L, i + (two ? 2 : 1)));
+                    q.u_mid = w.slot(L, i + 1);
+                    q.two_steps = two;
+                    q.inj_t1 = -1;
+                    q.a.inj_t = -1;
+                    q.smp_t1 = -1;
+                    q.a.smp_t = -1;
+                    if (p->nsrc > 0) {
+                        q.inj_e = w.src_e;
+                        q.inj_t1 = k;
+                        q.a.inj = w.src;
+                        q.a.inj_val = wavelet;
+                        q.a.inj_np = p->nsrc; q.a.inj_nt = p->nt; q.a.inj_t = two ? k + 1 : -1;
+                        q.a.inj_scale = p->src_scale;
+                    }
+                    if ((rc = st.launch_k2(uc[i], uo[i - 1], q))) return rc;
+                } else {
+                    StepArgs a = st.base(w.slot(L, i + 1));
+                    if (p->nsrc > 0) {
+                        a.inj = w.src;
+                        a.inj_val = wavelet;
+                        a.inj_np = p->nsrc; a.inj_nt = p->nt; a.inj_t = k;
+                        a.inj_scale = p->src_scale;
+                    }
+                    if ((rc = st.launch(MODE_PLAIN, uc[i], uo[i - 1], uc[i], a))) return rc;
                 }
-                if ((rc = st.launch(MODE_PLAIN, uc[i], uo[i - 1], uc[i], a))) return rc;
+                k += two ? 2 : 1;
             }
         }
         PhaseScope scope(PH_ADJOINT, s, k1 - std::max(k0, 1));
@@ -942,9 +786,6 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
 int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                  const Stepper& st, const float* wavelet, const float* dtraces, float* grad_vel,
                  float* grad_wavelet, const float* vel, bool zero_G = true, bool finalize = true) {
-    if (g.sb == 2)
-        return run_backward_k2(p, g, L, w, st, wavelet, dtraces, grad_vel, grad_wavelet, vel, zero_G,
-                               finalize);
     if (g.ustore)
         return run_backward_ustore(p, g, L, w, st, wavelet, dtraces, grad_vel, grad_wavelet, vel,
                                    zero_G, finalize);

@@ -114,4 +114,74 @@ __device__ __forceinline__ float4 unpack_bf16x4(uint2 p) {
     return make_float4(a.x, a.y, b.x, b.y);
 }
 
+// ---------------------------------------------------------------- 2D stencil rows
+// The launchers' copy of the arguments with the duplicated weight pairs set.
+inline StepArgs with_weight_pairs(StepArgs a) {
+    a.c0p = make_float2(a.c0, a.c0);
+    for (int k = 0; k < 4; ++k) {
+        a.czp[k] = make_float2(a.cz[k], a.cz[k]);
+        a.cxp[k] = make_float2(a.cx[k], a.cx[k]);
+    }
+    return a;
+}
+
+// A thread owns 4 consecutive cells of a row (a float4); lv and rv are the
+// float4s to its left and right, V a register window of the rows above and
+// below.
+__device__ __forceinline__ float comp(const float4& v, int e) {
+    return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+}
+
+// L u at the four cells of a row: horizontal taps from (lv, cv, rv), vertical
+// taps from the register window V (centre row C). The cells go in pairs
+// through the packed FP32x2 arithmetic of sm_100+, with the operations and
+// their order of the scalar form c0 u + sum_k cx_k (u_{x-k} + u_{x+k}) +
+// cz_k (u_{z-k} + u_{z+k}), accumulated k = 1 .. R with x before z.
+template <int R, int N>
+__device__ __forceinline__ float4 lap_row(const float4& lv, const float4& cv, const float4& rv,
+                                          const float4 (&V)[N], int C, const StepArgs& a) {
+    const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y, cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
+    float2 lo = __fmul2_rn(a.c0p, make_float2(cv.x, cv.y));
+    float2 hi = __fmul2_rn(a.c0p, make_float2(cv.z, cv.w));
+#pragma unroll
+    for (int k = 1; k <= R; ++k) {
+        const float2 cx = a.cxp[k - 1];
+        const float2 cz = a.czp[k - 1];
+        float2 xl, xh;
+        if (k % 2 == 0) {  // the x taps form aligned register pairs
+            xl = __fadd2_rn(make_float2(w[4 - k], w[5 - k]), make_float2(w[4 + k], w[5 + k]));
+            xh = __fadd2_rn(make_float2(w[6 - k], w[7 - k]), make_float2(w[6 + k], w[7 + k]));
+        } else {
+            xl = make_float2(w[4 - k] + w[4 + k], w[5 - k] + w[5 + k]);
+            xh = make_float2(w[6 - k] + w[6 + k], w[7 - k] + w[7 + k]);
+        }
+        lo = __ffma2_rn(cx, xl, lo);
+        hi = __ffma2_rn(cx, xh, hi);
+        const float4 up = V[C - k], dn = V[C + k];
+        lo = __ffma2_rn(cz, __fadd2_rn(make_float2(up.x, up.y), make_float2(dn.x, dn.y)), lo);
+        hi = __ffma2_rn(cz, __fadd2_rn(make_float2(up.z, up.w), make_float2(dn.z, dn.w)), hi);
+    }
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
+// u_{n+1} = m L u_n + 2 u_n - u_{n-1} at 4 interior cells outside the sponge
+// (g = 1), in packed pairs: the general update g (m L u + 2 u) - g^2 u_{n-1}
+// with g = 1, value for value.
+__device__ __forceinline__ float4 leap_plain(const float4& m, const float4& l, const float4& c,
+                                             const float4& o) {
+    const float2 lo = __fadd2_rn(__ffma2_rn(make_float2(m.x, m.y), make_float2(l.x, l.y),
+                                            __fadd2_rn(make_float2(c.x, c.y), make_float2(c.x, c.y))),
+                                 make_float2(-o.x, -o.y));
+    const float2 hi = __fadd2_rn(__ffma2_rn(make_float2(m.z, m.w), make_float2(l.z, l.w),
+                                            __fadd2_rn(make_float2(c.z, c.w), make_float2(c.z, c.w))),
+                                 make_float2(-o.z, -o.w));
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
+// A compile-time flag for generic lambdas (the plain-tile and general bodies).
+template <bool B>
+struct Flag {
+    static constexpr bool value = B;
+};
+
 }  // namespace wfd

@@ -58,6 +58,8 @@ struct StepArgs {
     int tiles_x, tiles_y, tiles_z;
     float c0;                  // centre weight (all axes)
     float cz[4], cy[4], cx[4]; // axis weights for k = 1..R, already scaled by (dx/h)^2
+    float2 c0p, czp[4], cxp[4]; // 2D: the same as duplicated pairs, operands of the packed
+                                // FP32x2 arithmetic (set by the 2D launchers)
     // injection into u_new: u += g * scale * val (* m at the cell when inj_times_m)
     PointLists inj;
     const float* inj_val;      // [nshot][inj_nt][inj_np]
@@ -92,28 +94,26 @@ cudaError_t launch_step2d(int R, int mode, int tile_rows, const CUtensorMap& map
 // Tile T = K2_TX x K2_TZ cells; u_n is staged on T plus 2R rows / 8 columns
 // (K2_UW wide), u_{n-1} and m on E = T plus R rows / 4 columns (K2_EW wide).
 constexpr int K2_TX = 120;
-constexpr int K2_TZ = 32;
+constexpr int K2_TZ = 24;  // (two stages and the m tile fit two CTAs per SM)
 constexpr int K2_EW = K2_TX + 8;
 constexpr int K2_UW = K2_TX + 16;
 constexpr int K2_THREADS = 256;
 
 struct Step2Args {
     StepArgs a;         // step 2: u_new = u_{n+2}, inj/inj_t (tile lists), smp/smp_t
-                        // (samples u_{n+1}), lap (its L u store); a.smp also serves step 1
+                        // (samples u_{n+1}); a.smp also serves step 1
     float* u_mid;       // u_{n+1} output on the tile
     PointLists inj_e;   // step-1 injection: points inside the tile's extended region E
     int inj_t1;         // step-1 injection time index (-1: none)
     int smp_t1;         // step-1 sampling time index of u_n (-1: none)
-    void* lap1;         // step-1 L u store (MODE_SAVE_LAP)
     int two_steps;      // 0: step 1 only (u_{n+1} to u_mid)
 };
 
 // map_u: u_n (box K2_UW x (K2_TZ + 4R) x 1); map_o: u_{n-1} (box K2_EW x (K2_TZ + 2R) x 1);
-// map_m: m (2D, box K2_EW x (K2_TZ + 2R)); map_l1 / map_l2: stored L u of the two
-// steps (box K2_TX x K2_TZ x 1, MODE_GRAD).
-cudaError_t launch_step2d_k2(int R, int mode, const CUtensorMap& map_u, const CUtensorMap& map_o,
-                             const CUtensorMap& map_m, const CUtensorMap& map_l1,
-                             const CUtensorMap& map_l2, const Step2Args& p, cudaStream_t s);
+// map_m: m ([nz][ld], box K2_EW x (K2_TZ + 2R)).
+// Plain steps only (no L u store, no gradient term); a.shots_per_cta shots per CTA.
+cudaError_t launch_step2d_k2(int R, const CUtensorMap& map_u, const CUtensorMap& map_o,
+                             const CUtensorMap& map_m, const Step2Args& p, cudaStream_t s);
 
 // ---------------------------------------------------------------- 3D tiles
 // One CTA (one shot) marches along z through a (TY x TX) column of the grid

@@ -56,43 +56,6 @@ struct Layout2D {
     static constexpr int BYTES = STAGES * STAGE + 64 + 128;  // + barriers + alignment slack
 };
 
-__device__ __forceinline__ float comp(const float4& v, int e) {
-    return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
-}
-
-// L u at the four cells of a row: horizontal taps from (lv, cv, rv), vertical
-// taps from the register window V (centre row C). The cells go in pairs
-// through the packed FP32x2 arithmetic of sm_100+, with the operations and
-// their order of the scalar form c0 u + sum_k cx_k (u_{x-k} + u_{x+k}) +
-// cz_k (u_{z-k} + u_{z+k}), accumulated k = 1 .. R with x before z.
-template <int R, int N>
-__device__ __forceinline__ float4 lap_row(const float4& lv, const float4& cv, const float4& rv,
-                                          const float4 (&V)[N], int C, const StepArgs& a) {
-    const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y, cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
-    const float2 c0 = make_float2(a.c0, a.c0);
-    float2 lo = __fmul2_rn(c0, make_float2(cv.x, cv.y));
-    float2 hi = __fmul2_rn(c0, make_float2(cv.z, cv.w));
-#pragma unroll
-    for (int k = 1; k <= R; ++k) {
-        const float2 cx = make_float2(a.cx[k - 1], a.cx[k - 1]);
-        const float2 cz = make_float2(a.cz[k - 1], a.cz[k - 1]);
-        float2 xl, xh;
-        if (k % 2 == 0) {  // the x taps form aligned register pairs
-            xl = __fadd2_rn(make_float2(w[4 - k], w[5 - k]), make_float2(w[4 + k], w[5 + k]));
-            xh = __fadd2_rn(make_float2(w[6 - k], w[7 - k]), make_float2(w[6 + k], w[7 + k]));
-        } else {
-            xl = make_float2(w[4 - k] + w[4 + k], w[5 - k] + w[5 + k]);
-            xh = make_float2(w[6 - k] + w[6 + k], w[7 - k] + w[7 + k]);
-        }
-        lo = __ffma2_rn(cx, xl, lo);
-        hi = __ffma2_rn(cx, xh, hi);
-        const float4 up = V[C - k], dn = V[C + k];
-        lo = __ffma2_rn(cz, __fadd2_rn(make_float2(up.x, up.y), make_float2(dn.x, dn.y)), lo);
-        hi = __ffma2_rn(cz, __fadd2_rn(make_float2(up.z, up.w), make_float2(dn.z, dn.w)), hi);
-    }
-    return make_float4(lo.x, lo.y, hi.x, hi.y);
-}
-
 template <int R, int MODE, int RB>
 __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ? 3 : 2)
     step2d_kernel(const __grid_constant__ CUtensorMap map_cur,
@@ -339,7 +302,8 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ?
 
 template <int R, int MODE, int RB>
 cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
-                        const StepArgs& a, cudaStream_t s) {
+                        const StepArgs& a_in, cudaStream_t s) {
+    const StepArgs a = with_weight_pairs(a_in);
     using L = Layout2D<R, MODE, RB>;
     static int configured_device = -1;
     int dev = 0;

@@ -81,7 +81,7 @@ def parse():
     ap.add_argument("--shots", type=int, default=0, help="use the first N shots (profiling)")
     ap.add_argument("--step-block", type=int, default=1, choices=[1, 2],
                     help="time steps per launch of the forward and the recompute")
-    ap.add_argument("--level-store-frac", type=float, default=0.55,
+    ap.add_argument("--level-store-frac", type=float, default=0.65,
                     help="fraction of the GPU's memory for the forward levels the adjoint keeps "
                          "instead of recomputing them (0: recompute all but the last segment)")
     ap.add_argument("--workload", default="fwi1024", choices=["fwi1024", "fwd2048", "fwi384_3d", "batch8"])

@@ -340,7 +340,8 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
         L.nlap = g.ustore ? std::max(g.K + 2, p->nt - g.k0_store + 2) : g.K;
         for (int b = 0; b < 2; ++b) L.Q[b] = take(L.field_bytes);  // (the adjoint is one-step)
         L.G = take((size_t)g.cells * 4);
-        L.ckpt = take((size_t)g.nseg * 2 * L.ckpt_field_bytes);
+        // (segments whose levels the forward keeps need no checkpoint)
+        L.ckpt = take((size_t)(g.ustore ? g.jstore : g.nseg) * 2 * L.ckpt_field_bytes);
         L.lap = take((size_t)L.nlap * L.lap_field_bytes);
         L.res = take((size_t)p->nshot * p->nt * p->nrec * 4 + 4);
     }

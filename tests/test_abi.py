@@ -74,9 +74,14 @@ def test_workspace_holds_the_kept_levels():
     _, n1 = _ws(_problem(nt=100, ckpt_every=10, store_levels=12))  # = K + 2: the minimum
     _, n4 = _ws(_problem(nt=100, ckpt_every=10, store_levels=45))  # 4 segments: 42 levels
     _, n9 = _ws(_problem(nt=100, ckpt_every=10, store_levels=10 ** 6))  # all 10 segments
+    # FP32 checkpoints of the 10 segments: one pair less per kept segment
+    ck = 2 * ((field + 255) // 256 * 256)
+    _, c0 = _ws(_problem(nt=100, ckpt_every=10, ckpt_format=0))
+    _, c4 = _ws(_problem(nt=100, ckpt_every=10, ckpt_format=0, store_levels=45))
     assert n1 == n0
-    assert n4 - n0 == (42 - 12) * slot
-    assert n9 - n0 == (102 - 12) * slot
+    assert c4 - c0 == (42 - 12) * slot - 3 * ck  # 4 kept segments: the last one kept anyway
+    _, c9 = _ws(_problem(nt=100, ckpt_every=10, ckpt_format=0, store_levels=10 ** 6))
+    assert c9 - c0 == (102 - 12) * slot - 9 * ck
     # the L u stores (FP32, BF16) do not use it
     _, f0 = _ws(_problem(nt=100, ckpt_every=10, lap_store=2))
     _, f9 = _ws(_problem(nt=100, ckpt_every=10, lap_store=2, store_levels=10 ** 6))

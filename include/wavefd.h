@@ -233,6 +233,37 @@ int wfd_profile_end(wfd_phase_times* out);
 int wfd_step2d_order2(const float* u0, const float* u1, float* u2, float wavespeed, float dt,
                       float dx, float dy, int N, int M, int M_padded, void* stream);
 
+/*
+ * The same step with the field stored in FP16: mixed_step,
+ * projects/18_simple_wave_fd/step2D_wave.cu:85-124, launched as in
+ * 2D_wave_cuda_mixed.py. u0, u1, u2 are [N][M_padded] IEEE binary16 (raw
+ * 16-bit patterns), M_padded even and > M, pointers 4-byte aligned; FP32
+ * arithmetic, round to nearest even on store. u2 may alias u0.
+ */
+int wfd_step2d_mixed(const void* u0, const void* u1, void* u2, float wavespeed, float dt, float dx,
+                     float dy, int N, int M, int M_padded, void* stream);
+
+/*
+ * The same step with the field stored as int16 plus one FP32 scale per block
+ * of 32 values along a row, u = s q: scaled_step, step2D_wave.cu:128-183, as
+ * driven by 2D_wave_cuda_scaled.py. q* are [N][M_padded] int16 (8-byte
+ * aligned), s* are [N][M_padded / 32] FP32, M_padded a multiple of 64. Each
+ * new block's scale is its largest magnitude / 32767 and q = rint(u / s).
+ * Interior rows are written in full (boundary columns and padding as 0);
+ * rows 0 and N - 1 are left untouched. q2/s2 may alias q0/s0.
+ */
+int wfd_step2d_scaled(const int16_t* q0, const float* s0, const int16_t* q1, const float* s1,
+                      int16_t* q2, float* s2, float wavespeed, float dt, float dx, float dy, int N,
+                      int M, int M_padded, void* stream);
+
+/*
+ * The 1D 3-point step: step1D, projects/18_simple_wave_fd/step1D_wave.cu:4-17.
+ * u0, u1, u2 are FP32 [N]; cells 1..N-2 of u2 receive
+ * -u0 + 2 u1 + dt^2 c^2 (u1[i-1] - 2 u1[i] + u1[i+1]) / dx^2. u2 may alias u0.
+ */
+int wfd_step1d(const float* u0, const float* u1, float* u2, float wavespeed, float dt, float dx,
+               int N, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,7 +27,8 @@ EXPORTS = (
     "wfd_strerror", "wfd_last_error", "wfd_version", "wfd_workspace_bytes", "wfd_forward",
     "wfd_backward", "wfd_misfit_gradient", "wfd_status", "wfd_sum_sq", "wfd_step2d_order2",
     "wfd_kernel_launches", "wfd_profile_begin", "wfd_profile_end", "wfd_forward_static",
-    "wfd_analytic_signal", "wfd_tfm", "wfd_forward_final",
+    "wfd_analytic_signal", "wfd_tfm", "wfd_forward_final", "wfd_step2d_mixed", "wfd_step2d_scaled",
+    "wfd_step1d",
 )
 
 
@@ -98,6 +99,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         lib.wfd_analytic_signal.argtypes = [f, ctypes.c_int64, ctypes.c_int, f, f, vp]
         F, I = ctypes.c_float, ctypes.c_int
         lib.wfd_tfm.argtypes = [f, I, f, f, I, F, F, F, f, f, I, I, f, vp]
+        lib.wfd_step2d_mixed.argtypes = [vp, vp, vp, F, F, F, F, I, I, I, vp]
+        lib.wfd_step2d_scaled.argtypes = [vp, f, vp, f, vp, f, F, F, F, F, I, I, I, vp]
+        lib.wfd_step1d.argtypes = [f, f, f, F, F, F, I, vp]
         lib.wfd_kernel_launches.argtypes = []
         lib.wfd_kernel_launches.restype = ctypes.c_uint64
         lib.wfd_profile_begin.argtypes = []

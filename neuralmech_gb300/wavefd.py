@@ -417,6 +417,45 @@ def sum_sq(x: torch.Tensor) -> torch.Tensor:
     return out
 
 
+def _check_fields(dtype, names_tensors, dim):
+    for n, t in names_tensors:
+        _require_cuda(t, n)
+        if t.dtype != dtype or not t.is_contiguous() or t.dim() != dim:
+            raise ValueError(f"{n} must be a contiguous {dim}D {dtype} tensor")
+
+
+def step2d_mixed(u0, u1, u2, wavespeed: float, dt: float, dx: float, dy: float, N: int, M: int):
+    """mixed_step (step2D_wave.cu:85-124): the padded_step update on (N, M_padded)
+    float16 CUDA tensors, FP32 arithmetic; u2 may be u0."""
+    _check_fields(torch.float16, (("u0", u0), ("u1", u1), ("u2", u2)), 2)
+    _lib.check(_lib.load().wfd_step2d_mixed(_ptr(u0), _ptr(u1), _ptr(u2), wavespeed, dt, dx, dy,
+                                            N, M, u1.shape[1], _stream()), "wfd_step2d_mixed")
+    return u2
+
+
+def step2d_scaled(q0, s0, q1, s1, q2, s2, wavespeed: float, dt: float, dx: float, dy: float, N: int,
+                  M: int):
+    """scaled_step (step2D_wave.cu:128-183): the padded_step update on int16
+    fields q (N, M_padded) with one float32 scale per 32 values, s (N, M_padded / 32),
+    u = s q; (q2, s2) may be (q0, s0)."""
+    _check_fields(torch.int16, (("q0", q0), ("q1", q1), ("q2", q2)), 2)
+    _check_fields(torch.float32, (("s0", s0), ("s1", s1), ("s2", s2)), 2)
+    if s1.shape[1] * 32 != q1.shape[1]:
+        raise ValueError("s must have M_padded / 32 columns")
+    _lib.check(_lib.load().wfd_step2d_scaled(_ptr(q0), _ptr(s0), _ptr(q1), _ptr(s1), _ptr(q2), _ptr(s2),
+                                             wavespeed, dt, dx, dy, N, M, q1.shape[1], _stream()),
+               "wfd_step2d_scaled")
+    return q2, s2
+
+
+def step1d(u0, u1, u2, wavespeed: float, dt: float, dx: float):
+    """step1D (step1D_wave.cu:4-17) on (N,) float32 CUDA tensors; u2 may be u0."""
+    _check_fields(torch.float32, (("u0", u0), ("u1", u1), ("u2", u2)), 1)
+    _lib.check(_lib.load().wfd_step1d(_ptr(u0), _ptr(u1), _ptr(u2), wavespeed, dt, dx, u1.shape[0],
+                                      _stream()), "wfd_step1d")
+    return u2
+
+
 def step2d_order2(u0, u1, u2, wavespeed: float, dt: float, dx: float, dy: float, N: int, M: int):
     """padded_step (step2D_wave.cu:59-81): u2 <- -u0 + 2u1 + dt^2 c^2 Lap(u1) on
     rows 1..N-2, columns 1..M-2 of (N, M_padded) FP32 CUDA tensors; u2 may be u0."""

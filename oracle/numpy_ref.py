@@ -66,3 +66,51 @@ def fd_step(u0, u1, u2, w, h, order=8, g=None):
         gi = g[inner]
         u2[inner] = gi * (2 * u1[inner] + wi * lap) - gi * gi * u0[inner]
     return u2
+
+
+def _update_order2(u0, u1c, il, ir, jl, jr, k, dx2, dy2):
+    """-u0 + 2 u1 + k ((il - 2u1 + ir)/dx2 + (jl - 2u1 + jr)/dy2), FP32, the
+    operation order of step2D_wave.cu:108-113 and 162-167."""
+    two = np.float32(2) * u1c
+    li = (il - two) + ir
+    lj = (jl - two) + jr
+    return (-u0 + two) + k * (li / dx2 + lj / dy2)
+
+
+def scaled_step(q0, s0, q1, s1, c, dt, dx, dy, N, M):
+    """scaled_step (projects/18_simple_wave_fd/step2D_wave.cu:128-183) restated
+    on NumPy: int16 fields q [N][Mp] with one FP32 scale per 32 values of a row,
+    s [N][Mp/32], u = s q. Returns (q2, s2) for rows 1..N-2 (rows 0 and N-1 are
+    copied from q0/s0, which the in-place driver passes as q2/s2). The
+    reference's shuffles only move decoded neighbour values between threads:
+    here each neighbour is decoded with its own block's scale, as they are."""
+    f32 = np.float32
+    Mp = q1.shape[1]
+    k = f32(dt) * f32(dt) * f32(c) * f32(c)
+    dx2, dy2 = f32(dx) * f32(dx), f32(dy) * f32(dy)
+    u0 = np.repeat(s0, 32, axis=1) * q0.astype(f32)
+    u1 = np.repeat(s1, 32, axis=1) * q1.astype(f32)
+    zero = np.zeros((N, 1), f32)
+    jl = np.concatenate([zero, u1[:, :-1]], axis=1)  # j - 1 (0 at j = 0)
+    jr = np.concatenate([u1[:, 1:], zero], axis=1)   # j + 1 (0 past M_padded)
+    q2, s2 = q0.copy(), s0.copy()
+    v = _update_order2(u0[1:-1], u1[1:-1], u1[:-2], u1[2:], jl[1:-1], jr[1:-1], k, dx2, dy2)
+    j = np.arange(Mp)[None, :]
+    v = np.where((j == 0) | (j >= M - 1), f32(0), v).astype(f32)
+    m = np.abs(v).reshape(N - 2, Mp // 32, 32).max(axis=2)
+    with np.errstate(divide="ignore"):
+        inv = np.where(m > 0, f32(32767) / np.where(m > 0, m, f32(1)), f32(0)).astype(f32)
+    q2[1:-1] = np.rint(v * np.repeat(inv, 32, axis=1)).astype(np.int16)
+    s2[1:-1] = (m / f32(32767)).astype(f32)
+    return q2, s2
+
+
+def scaled_encode(u):
+    """A field [N][Mp] as (q, s): per 32-value block, s = max|u| / 32767 and
+    q = rint(u * 32767 / max|u|) (the encoding of step2D_wave.cu:175-182)."""
+    f32 = np.float32
+    N, Mp = u.shape
+    m = np.abs(u).reshape(N, Mp // 32, 32).max(axis=2).astype(f32)
+    m = np.where(m < f32(2.0**-100), f32(0), m)  # (32767 / m must stay finite: such blocks encode as 0)
+    inv = np.where(m > 0, f32(32767) / np.where(m > 0, m, f32(1)), f32(0)).astype(f32)
+    return np.rint(u.astype(f32) * np.repeat(inv, 32, axis=1)).astype(np.int16), (m / f32(32767)).astype(f32)

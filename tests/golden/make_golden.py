@@ -12,6 +12,9 @@ Outputs (small .npz files, committed):
                    a multiple of 32 as in the driver)
   mixed_step.npz   the same for mixed_step (FP16 storage)
   step1d.npz       the same for step1D
+  scaled_step.npz  the same for scaled_step (int16 + FP32 scale per 32 values),
+                   from the NumPy restatement oracle.numpy_ref.scaled_step (the
+                   kernel's warp shuffles do not run in the CPU build)
 """
 from __future__ import annotations
 
@@ -97,7 +100,33 @@ def main():
         if t in (0, 1, 24):
             out[f"step{t}"] = b.copy()
     np.savez_compressed(os.path.join(HERE, "step1d.npz"), **out)
+    scaled_golden()
     print("golden vectors written to", HERE)
+
+
+def scaled_golden():
+    """scaled_step golden vectors from the NumPy restatement (oracle.numpy_ref):
+    the reference kernel's warp shuffles do not run in the CPU build."""
+    from oracle import numpy_ref as nr
+    out = {}
+    for ci, (N, M, L, steps, seed) in enumerate(CASES):
+        MP = (M + 63) // 64 * 64
+        dx, dy = L[0] / (N - 1), L[1] / (M - 1)
+        c = 1.0
+        dt = 0.95 * min(dx, dy) / c / math.sqrt(2)
+        u = initial(N, MP, MP, L, seed)
+        u[:, M:] = 0
+        q, s = nr.scaled_encode(u)
+        a, b = (q.copy(), s.copy()), (q.copy(), s.copy())
+        out[f"c{ci}_q0"], out[f"c{ci}_s0"] = q.copy(), s.copy()
+        out[f"c{ci}_params"] = np.array([N, M, MP, steps, c, dt, dx, dy], dtype=np.float64)
+        for t in range(steps):
+            a = nr.scaled_step(a[0], a[1], b[0], b[1], np.float32(c), np.float32(dt), np.float32(dx),
+                               np.float32(dy), N, M)
+            a, b = b, a
+            if t in (0, 1, steps - 1):
+                out[f"c{ci}_step{t}_q"], out[f"c{ci}_step{t}_s"] = b[0].copy(), b[1].copy()
+    np.savez_compressed(os.path.join(HERE, "scaled_step.npz"), **out)
 
 
 if __name__ == "__main__":

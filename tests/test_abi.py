@@ -141,3 +141,20 @@ def test_problem_struct_mirrors_header():
         fields += [(n.strip(), ctype) for n in names.split(",")]
     mirror = [(n, {ctypes.c_int32: "int32_t", ctypes.c_float: "float"}[t]) for n, t in _lib.Problem._fields_]
     assert mirror == fields
+
+
+def test_dropin_arguments_rejected():
+    """The reduced-precision and 1D drop-ins check their arguments on the host
+    (no launch is made here)."""
+    from neuralmech_gb300 import _lib
+    lib = _lib.load()
+    p = ctypes.c_void_p(256)  # never dereferenced: every call below fails its checks first
+    assert lib.wfd_step1d(p, p, p, 1.0, 1e-3, 1e-2, 2, None) == -1
+    assert lib.wfd_step1d(None, p, p, 1.0, 1e-3, 1e-2, 100, None) == -1
+    assert lib.wfd_step2d_mixed(p, p, p, 1.0, 1e-3, 1e-2, 1e-2, 64, 64, 64, None) == -1  # M_padded <= M
+    assert lib.wfd_step2d_mixed(p, p, p, 1.0, 1e-3, 1e-2, 1e-2, 64, 60, 63, None) == -1  # odd M_padded
+    assert lib.wfd_step2d_mixed(ctypes.c_void_p(258), p, p, 1.0, 1e-3, 1e-2, 1e-2, 64, 60, 64, None) == -1
+    assert lib.wfd_step2d_scaled(p, p, p, p, p, p, 1.0, 1e-3, 1e-2, 1e-2, 64, 60, 96, None) == -1  # % 64
+    assert lib.wfd_step2d_scaled(ctypes.c_void_p(260), p, p, p, p, p, 1.0, 1e-3, 1e-2, 1e-2, 64, 60, 64,
+                                 None) == -1  # q not 8-byte aligned
+    assert "64" in lib.wfd_last_error().decode() or "aligned" in lib.wfd_last_error().decode()

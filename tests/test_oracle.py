@@ -196,3 +196,36 @@ def test_oracle_homogeneous_greens_function(orc):
             ana[i] = np.trapezoid(w(ti - (r / c) * np.cosh(s)), s) / (2 * math.pi * c * c)
     win = (t > r / c) & (t < r / c + t0 + 2 / f)
     assert rel_l2(tr[win], ana[win]) < 0.05
+
+
+def test_scaled_step_restatement_tracks_fp32():
+    """The NumPy restatement of scaled_step (the golden source for
+    wfd_step2d_scaled) stays within int16 quantisation of the FP32 slice step
+    (pinned to padded_step above) on the same field, and its encoding round
+    trips to 1/65534 of each block's largest magnitude."""
+    from oracle import numpy_ref as nr
+    N, M, MP = 48, 90, 128
+    dx, dy = 1.0 / (N - 1), 2.0 / (M - 1)
+    dt = 0.95 * min(dx, dy) / math.sqrt(2)
+    f32 = np.float32
+    x = np.linspace(0, 1, N)[:, None]
+    y = np.linspace(0, 2, M)[None, :]
+    u = np.zeros((N, MP), f32)
+    u[:, :M] = np.exp(-((x - 0.5) ** 2 + (y - 0.9) ** 2) / (2 * 0.1**2))
+    u[0] = u[-1] = 0
+    u[:, 0] = 0
+    u[:, M - 1:] = 0
+    q, s = nr.scaled_encode(u)
+    dec = np.repeat(s, 32, axis=1) * q
+    blockmax = np.repeat(np.abs(u).reshape(N, MP // 32, 32).max(axis=2), 32, axis=1)
+    assert np.all(np.abs(dec - u) <= blockmax / 65534 * 1.0001 + 1e-30)
+    a, b = (q.copy(), s.copy()), (q.copy(), s.copy())
+    fa, fb = u[:, :M].copy(), u[:, :M].copy()
+    for _ in range(12):
+        a = nr.scaled_step(a[0], a[1], b[0], b[1], 1.0, dt, dx, dy, N, M)
+        a, b = b, a
+        fa = nr.fd_step_order2(fa, fb, fa, f32(dt), f32(dx), f32(dy), f32(1.0))
+        fa, fb = fb, fa
+    got = (np.repeat(b[1], 32, axis=1) * b[0])[:, :M]
+    assert np.linalg.norm(got - fb) / np.linalg.norm(fb) < 2e-4
+    assert np.all(b[0][:, M - 1:] == 0) and np.all(b[0][1:-1, 0] == 0)

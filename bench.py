@@ -79,6 +79,8 @@ def parse():
                     help="run one gradient and exit (the command profiled by ncu)")
     ap.add_argument("--nt", type=int, default=0, help="override the number of time steps (profiling)")
     ap.add_argument("--shots", type=int, default=0, help="use the first N shots (profiling)")
+    ap.add_argument("--field-format", default="fp32", choices=["fp32", "fp16", "i16"],
+                    help="fwd2048: storage of the wavefields (arithmetic stays FP32)")
     ap.add_argument("--step-block", type=int, default=1, choices=[1, 2],
                     help="time steps per launch of the forward and the recompute")
     ap.add_argument("--level-store-frac", type=float, default=0.65,
@@ -300,10 +302,16 @@ def run_other(args):
         R = g.order // 2
         interior = float(np.prod([n - 2 * R for n in g.shape]))
         if args.workload == "fwd2048":
+            g = dataclasses.replace(g, field_format=args.field_format)
             step = lambda: wave_forward(v, wav, src, rec, g, check=False)
             updates, bpu = w.nshot * interior * g.nt, 16.0
             cfg = {"workload": f"fwd2048: 2D forward {g.shape[0]}^2, {g.nt} steps, 1 shot, "
-                               f"{w.rec.shape[1]} receivers, order 8, 20-cell sponge"}
+                               f"{w.rec.shape[1]} receivers, order 8, 20-cell sponge",
+                   "field_format": g.field_format}
+            if g.field_format != "fp32":  # the storage error against the FP32 forward
+                ref = wave_forward(v, wav, src, rec, dataclasses.replace(g, field_format="fp32"))
+                got = step()
+                cfg["traces_rel_l2_vs_fp32"] = float((got - ref).norm() / ref.norm())
         else:
             g = dataclasses.replace(g, group_shots=8)
             obs = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, g)

@@ -41,6 +41,13 @@ extern "C" {
 #define WFD_CKPT_BF16 1 /* 2, round to nearest even */
 #define WFD_CKPT_I16 2  /* 2 + 4/32: int16 with one FP32 scale per 32 cells (block max / 32767) */
 
+/* Storage of the wavefields (wfd_problem.field_format). Reduced precision is
+ * a 2D forward-only mode (no checkpoints, no gradient); arithmetic stays FP32. */
+#define WFD_FIELD_FP32 0 /* 4 bytes per cell */
+#define WFD_FIELD_FP16 1 /* IEEE binary16, round to nearest even (mixed_step's format) */
+#define WFD_FIELD_I16 2  /* int16 with one FP32 scale per 32 cells along x, scale = block
+                            max / 32767 (scaled_step's format) */
+
 /* What the checkpointed adjoint keeps of each recomputed step for its imaging
  * term q_{k+1} L u_k. */
 #define WFD_LAP_AUTO 0 /* 2D one-step kernel: the level u_k itself (FP32, written by the
@@ -71,6 +78,7 @@ typedef struct wfd_problem {
                               its last floor((store_levels - 2) / K) segments, K the
                               checkpoint interval, and the adjoint recomputes only
                               the others; 0 (or <= K + 2) = the last segment only */
+    int32_t field_format;  /* WFD_FIELD_FP32, _FP16 or _I16 */
     float dt;              /* time step */
     float dz, dy, dx;      /* grid spacing (dy ignored in 2D) */
     float src_scale;       /* factor on every injected wavelet sample */

@@ -142,6 +142,21 @@ int make_field_map(CUtensorMap* map, const void* base, bool bf16, int ndim, int 
     return WFD_OK;
 }
 
+// 3D tiled map (x fastest) of any element type, zero fill out of range.
+int make_map3(CUtensorMap* map, const void* base, CUtensorMapDataType dt, const cuuint64_t* dims,
+              const cuuint64_t* strides, const cuuint32_t* box) {
+    EncodeTiled enc = encoder();
+    if (!enc) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(map, dt, 3, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return WFD_OK;
+}
+
+int scale_blocks(int ld) { return ((ld + 31) / 32 + 3) / 4 * 4; }  // per row, a multiple of 4
+
 // ------------------------------------------------------------------ geometry
 struct Geom {
     int ndim, R, nz, ny, nx, ld;
@@ -195,6 +210,10 @@ int check_problem(const wfd_problem* p) {
         return fail(WFD_ERR_INVALID, "unknown checkpoint format %d", p->ckpt_format);
     if (p->lap_store < WFD_LAP_AUTO || p->lap_store > WFD_LAP_FP32)
         return fail(WFD_ERR_INVALID, "unknown lap_store %d", p->lap_store);
+    if (p->field_format < WFD_FIELD_FP32 || p->field_format > WFD_FIELD_I16)
+        return fail(WFD_ERR_INVALID, "unknown field_format %d", p->field_format);
+    if (p->field_format != WFD_FIELD_FP32 && (p->ndim != 2 || p->step_block == 2))
+        return fail(WFD_ERR_INVALID, "reduced-precision fields: 2D, one step per launch only");
     if (p->tile_rows != 0 && p->tile_rows != 16 && p->tile_rows != 32)
         return fail(WFD_ERR_INVALID, "tile_rows must be 0, 16 or 32");
     if (p->step_block < 0 || p->step_block > 2 || (p->step_block == 2 && p->ndim != 2))
@@ -238,6 +257,10 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0, int step_block = 0) {
         g.tile_z = K2_TZ;
         g.tile_y = 1;
         g.tile_x = K2_TX;
+    } else if (g.ndim == 2 && p->field_format != WFD_FIELD_FP32) {
+        g.tile_z = 32;  // the reduced-precision kernel's 128 x 32 tile
+        g.tile_y = 1;
+        g.tile_x = T2_TX;
     } else if (g.ndim == 2) {
         g.tile_z = tile_rows > 0 ? tile_rows : p->tile_rows > 0 ? p->tile_rows : T2_TZ;
         g.tile_y = 1;
@@ -299,6 +322,7 @@ struct Layout {
     size_t asrc_off, asrc_ent, arec_off, arec_ent;  // adjoint-geometry lists (u store)
     size_t Q[4], G, ckpt, lap, res, total;
     size_t field_bytes, ckpt_field_bytes, lap_field_bytes;
+    size_t S[2], scale_bytes;  // reduced-precision fields: the int16 block scales
     int nlap;  // slots of the lap region: K stored L u_k, or levels u_k (u store): from
                // u_{k0_store - 1} to u_nt, and at least K + 2 for a recomputed segment
 };
@@ -312,11 +336,15 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     const Geom ga = adjoint_geom(p, g);
     const bool alists = grad && (ga.tile_z != g.tile_z || ga.tile_x != g.tile_x);
     const size_t keys = (size_t)p->nshot * std::max(g.ntiles, alists ? ga.ntiles : 0);
-    L.field_bytes = (size_t)p->nshot * g.cells * 4;
+    L.field_bytes = (size_t)p->nshot * g.cells * (p->field_format == WFD_FIELD_FP32 ? 4 : 2);
     L.nbuf = g.sb == 2 ? 4 : 2;
     L.err = take(256);
     L.m = take((size_t)g.cells * 4);
     for (int b = 0; b < L.nbuf; ++b) L.P[b] = take(L.field_bytes);
+    if (p->field_format == WFD_FIELD_I16) {
+        L.scale_bytes = (size_t)p->nshot * g.nz * scale_blocks(g.ld) * 4;
+        for (int b = 0; b < 2; ++b) L.S[b] = take(L.scale_bytes);
+    }
     L.counts = take(keys * 4);
     L.src_off = take((keys + 1) * 4);
     L.src_ent = take((size_t)p->nshot * p->nsrc * 8 + 8);
@@ -352,6 +380,7 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
 struct Work {
     unsigned* err;
     float *m, *P[4], *Q[4], *G, *res;
+    float* S[2];  // int16 block scales of P[0], P[1] (reduced-precision fields)
     int* counts;
     PointLists src, rec, src_e;
     PointLists src_a, rec_a;  // lists of the adjoint geometry (== src, rec unless u store)
@@ -368,6 +397,8 @@ Work carve(void* ws, const Layout& L, bool grad) {
     w.err = reinterpret_cast<unsigned*>(b + L.err);
     w.m = reinterpret_cast<float*>(b + L.m);
     for (int k = 0; k < L.nbuf; ++k) w.P[k] = reinterpret_cast<float*>(b + L.P[k]);
+    if (L.S[0])
+        for (int k = 0; k < 2; ++k) w.S[k] = reinterpret_cast<float*>(b + L.S[k]);
     w.counts = reinterpret_cast<int*>(b + L.counts);
     w.src.off = reinterpret_cast<int*>(b + L.src_off);
     w.src.ent = reinterpret_cast<int2*>(b + L.src_ent);
@@ -575,9 +606,16 @@ int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
 // and writes u_{k+1}, u_{k+2}, none of which alias). With the u store the
 // levels of the kept segments, from u_{k0_store - 1} on, go to the store's
 // slots k - k0_store + 1 for the adjoint to read instead.
+int run_forward_lp(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
+                   const Stepper& st, const float* wavelet, float* traces, int* final_buf);
+
 int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                 const Stepper& st, const float* wavelet, float* traces, bool save,
                 int* final_buf = nullptr) {
+    if (p->field_format != WFD_FIELD_FP32) {
+        if (save) return fail(WFD_ERR_INVALID, "reduced-precision fields are a forward-only mode");
+        return run_forward_lp(p, g, L, w, st, wavelet, traces, final_buf);
+    }
     cudaStream_t s = st.s;
     const bool us = save && g.ustore;
     const int np = L.nbuf;
@@ -667,6 +705,69 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
     if (traces && p->nrec > 0)
         WFD_CUDA(launch_gather(buf[loc(p->nt)], g.cells, w.rec, g.ntiles, p->nshot, p->nrec, nullptr,
                                1.f, 0, traces, p->nt, p->nt - 1, s));
+    return WFD_OK;
+}
+
+// Forward with reduced-precision fields (FP16 or block-scaled int16): u_{n+1}
+// over u_{n-1} in two buffers, the sources added and the receivers sampled in
+// the step kernel (traces[n] = the stored u_{n+1}).
+int run_forward_lp(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
+                   const Stepper& st, const float* wavelet, float* traces, int* final_buf) {
+    cudaStream_t s = st.s;
+    if (final_buf) *final_buf = p->nt & 1;
+    const bool i16 = p->field_format == WFD_FIELD_I16;
+    for (int b = 0; b < 2; ++b) {
+        WFD_CUDA(cudaMemsetAsync(w.P[b], 0, L.field_bytes, s));
+        if (i16) WFD_CUDA(cudaMemsetAsync(w.S[b], 0, L.scale_bytes, s));
+    }
+    const int nblk = scale_blocks(g.ld);
+    CUtensorMap mcur[2], mold[2], mcs[2]{}, mos[2]{};
+    // (int16 cells travel as 16-bit patterns: the copy does not look at them)
+    const CUtensorMapDataType dt = i16 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    const cuuint64_t fdims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.nz, (cuuint64_t)p->nshot};
+    const cuuint64_t fstr[2] = {(cuuint64_t)g.ld * 2, (cuuint64_t)g.nz * g.ld * 2};
+    const cuuint64_t sdims[3] = {(cuuint64_t)nblk, (cuuint64_t)g.nz, (cuuint64_t)p->nshot};
+    const cuuint64_t sstr[2] = {(cuuint64_t)nblk * 4, (cuuint64_t)g.nz * nblk * 4};
+    const cuuint32_t bcur[3] = {144, cuuint32_t(32 + 2 * g.R), 1}, bold[3] = {128, 32, 1};
+    const cuuint32_t bcs[3] = {12, cuuint32_t(32 + 2 * g.R), 1}, bos[3] = {4, 32, 1};
+    int rc;
+    for (int b = 0; b < 2; ++b) {
+        if ((rc = make_map3(&mcur[b], w.P[b], dt, fdims, fstr, bcur))) return rc;
+        if ((rc = make_map3(&mold[b], w.P[b], dt, fdims, fstr, bold))) return rc;
+        if (i16) {
+            if ((rc = make_map3(&mcs[b], w.S[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, sdims, sstr, bcs))) return rc;
+            if ((rc = make_map3(&mos[b], w.S[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, sdims, sstr, bos))) return rc;
+        }
+    }
+    PhaseScope scope(PH_FORWARD, s, p->nt);
+    for (int n = 0; n < p->nt; ++n) {
+        const int bc = n & 1, bn = (n + 1) & 1;
+        LpArgs q{};
+        q.a = st.base(nullptr);
+        q.a.inj = w.src;
+        q.a.inj_val = wavelet;
+        q.a.inj_np = p->nsrc; q.a.inj_nt = p->nt; q.a.inj_t = n;
+        q.a.inj_scale = p->src_scale;
+        if (p->nsrc == 0) q.a.inj.off = nullptr;
+        if (traces && p->nrec > 0) {
+            q.a.smp = w.rec;
+            q.a.smp_out = traces;
+            q.a.smp_np = p->nrec; q.a.smp_nt = p->nt; q.a.smp_t = n;
+            q.a.smp_scale = 1.f;
+        }
+        q.cur = w.P[bc];
+        q.old = w.P[bn];
+        q.nw = w.P[bn];
+        if (i16) {
+            q.scur = w.S[bc];
+            q.sold = w.S[bn];
+            q.snw = w.S[bn];
+        }
+        q.nblk = nblk;
+        q.sstride = (long long)g.nz * nblk;
+        cudaError_t e = launch_step2d_lp(g.R, p->field_format, mcur[bc], mold[bn], mcs[bc], mos[bn], q, s);
+        if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "reduced-precision step failed: %s", cudaGetErrorString(e));
+    }
     return WFD_OK;
 }
 
@@ -894,6 +995,8 @@ int wfd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes) 
     int rc = check_problem(p);
     if (rc) return rc;
     if (!bytes) return fail(WFD_ERR_INVALID, "bytes is NULL");
+    if (with_gradient && p->field_format != WFD_FIELD_FP32)
+        return fail(WFD_ERR_INVALID, "reduced-precision fields are a forward-only mode");
     const wfd_problem q = group_problem(p, 0);  // the workspace serves one group at a time
     const Geom g = make_geom(&q);
     *bytes = make_layout(&q, g, with_gradient != 0).total;
@@ -909,6 +1012,8 @@ int wfd_forward(const wfd_problem* p, const float* vel, const float* sponge_z,
     const int G = group_size(p);
     if (save_checkpoints && G < p->nshot)
         return fail(WFD_ERR_INVALID, "a checkpointed forward cannot be split into shot groups");
+    if (save_checkpoints && p->field_format != WFD_FIELD_FP32)
+        return fail(WFD_ERR_INVALID, "reduced-precision fields are a forward-only mode");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     // one layout, sized for a full group, serves every group
     const wfd_problem first = group_problem(p, 0);
@@ -948,6 +1053,11 @@ int wfd_forward_final(const wfd_problem* p, const float* vel, const float* spong
     if ((rc = st.init())) return rc;
     int fb = 0;
     if ((rc = run_forward(p, g, L, w, st, wavelet, traces, false, &fb))) return rc;
+    if (p->field_format != WFD_FIELD_FP32) {  // decode, rows of nx cells
+        WFD_CUDA(launch_decode_field(p->field_format, w.P[fb], w.S[fb], u_final, (long long)p->nshot * g.nz,
+                                     g.nx, g.ld, scale_blocks(g.ld), s));
+        return WFD_OK;
+    }
     // strip the row padding: rows of ld floats -> rows of nx floats
     WFD_CUDA(cudaMemcpy2DAsync(u_final, (size_t)g.nx * 4, w.P[fb], (size_t)g.ld * 4, (size_t)g.nx * 4,
                                (size_t)p->nshot * g.nz * g.ny, cudaMemcpyDeviceToDevice, s));
@@ -962,6 +1072,8 @@ int wfd_backward(const wfd_problem* p, const float* vel, const float* sponge_z,
     if (rc) return rc;
     if (!grad_vel || (p->nrec > 0 && !dtraces))
         return fail(WFD_ERR_INVALID, "grad_vel/dtraces is NULL");
+    if (p->field_format != WFD_FIELD_FP32)
+        return fail(WFD_ERR_INVALID, "reduced-precision fields are a forward-only mode");
     if (group_size(p) < p->nshot)
         return fail(WFD_ERR_INVALID, "wfd_backward cannot be split into shot groups");
     const Geom g = make_geom(p);
@@ -983,6 +1095,8 @@ int wfd_misfit_gradient(const wfd_problem* p, const float* vel, const float* spo
     if (rc) return rc;
     if (!grad_vel || !misfit || (p->nrec > 0 && !observed))
         return fail(WFD_ERR_INVALID, "grad_vel/misfit/observed is NULL");
+    if (p->field_format != WFD_FIELD_FP32)
+        return fail(WFD_ERR_INVALID, "reduced-precision fields are a forward-only mode");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     WFD_CUDA(cudaMemsetAsync(misfit, 0, sizeof(double), s));
     const int G = group_size(p);

@@ -81,6 +81,33 @@ struct StepArgs {
     unsigned* err;
 };
 
+// Reduced-precision storage step (stencil2d_lp.cu): fields [shot][z][ld] of
+// FP16 or int16 (fmt WFD_FIELD_FP16 / _I16), int16 with scales
+// [shot][z][nblk] FP32 (one per 32 cells along x). a carries the geometry,
+// weights, m, sponge and point lists (a.shot_stride in cells); a.inj_t is the
+// step's source sample, a.smp_t the trace index of u_{n+1}.
+struct LpArgs {
+    StepArgs a;
+    const void* cur;  // u_n (read-only in the launch)
+    const float* scur;
+    const void* old;  // u_{n-1}
+    const float* sold;
+    void* nw;         // u_{n+1} (may alias old)
+    float* snw;
+    int nblk;         // scale blocks per row: ceil(ld / 32) rounded up to 4
+    long long sstride;  // scales per shot: nz * nblk
+};
+// map_cur: u_n (16-bit, box 144 x (32 + 2R) x 1 at x0 - 8); map_old: u_{n-1}
+// (box 128 x 32 x 1); map_cs / map_os (int16 only): their scale rows (FP32,
+// [shot][z][nblk] with nblk a multiple of 4; boxes 12 x (32 + 2R) x 1 at block
+// x0/32 - 4 and 4 x 32 x 1 at block x0/32).
+cudaError_t launch_step2d_lp(int R, int fmt, const CUtensorMap& map_cur, const CUtensorMap& map_old,
+                             const CUtensorMap& map_cs, const CUtensorMap& map_os, const LpArgs& p,
+                             cudaStream_t s);
+// u_final[row][x] (FP32, nx per row) from a reduced-precision field.
+cudaError_t launch_decode_field(int fmt, const void* f, const float* sc, float* out, long long nrows, int nx,
+                                int ld, int nblk, cudaStream_t s);
+
 // Launches one time step of the 2D kernel of half-width R (1, 2, 4), mode and
 // tile height tile_rows (16 or 32).
 // map_cur: u_n (box T2_W x (tile_rows + 2R) x 1); map_old: u_{n-1} (box

@@ -36,6 +36,7 @@ from . import _lib
 # ---------------------------------------------------------------- descriptors
 CKPT_FORMATS = {"fp32": 0, "bf16": 1, "i16": 2}
 LAP_STORES = {"auto": 0, "bf16": 1, "fp32": 2}
+FIELD_FORMATS = {"fp32": 0, "fp16": 1, "i16": 2}
 
 
 @dataclass(frozen=True)
@@ -67,6 +68,9 @@ class Grid:
              the forward keeps the levels of its last (store_levels - 2) // K
              segments and only the earlier ones are recomputed (0: the last
              segment only); see levels_for_budget()
+    field_format storage of the wavefields in a forward without gradient (2D):
+             "fp32", "fp16" or "i16" (int16 with one FP32 scale per 32 cells
+             along x); arithmetic is FP32 in every format
     """
     shape: tuple
     spacing: tuple
@@ -84,6 +88,7 @@ class Grid:
     tile_rows: int = 0
     step_block: int = 0
     store_levels: int = 0
+    field_format: str = "fp32"
 
     @property
     def ndim(self) -> int:
@@ -161,7 +166,8 @@ def _problem(grid: Grid, nshot: int, nsrc: int, nrec: int, vmax: float) -> _lib.
         dz, dy, dx = grid.spacing
     return _lib.Problem(grid.ndim, grid.order, nz, ny, nx, nshot, grid.nt, nsrc, nrec,
                         grid.ckpt_every, CKPT_FORMATS[grid.ckpt_format], LAP_STORES[grid.lap_store],
-                        grid.shots_per_cta, grid.group_shots, grid.tile_rows, grid.step_block, grid.store_levels, grid.dt, dz, dy, dx, grid.src_scale, vmax)
+                        grid.shots_per_cta, grid.group_shots, grid.tile_rows, grid.step_block, grid.store_levels,
+                        FIELD_FORMATS[grid.field_format], grid.dt, dz, dy, dx, grid.src_scale, vmax)
 
 
 # ---------------------------------------------------------------- argument prep
@@ -332,6 +338,8 @@ def wave_forward(vel: torch.Tensor, wavelet, src, rec, grid: Grid, *, check: boo
         nshot = wav_t.shape[0]
     call = _prepare(vel, wav_t.detach(), src, rec, grid, nshot)
     if torch.is_grad_enabled() and (vel.requires_grad or wav_t.requires_grad):
+        if grid.field_format != "fp32":
+            raise ValueError("reduced-precision field storage is a forward-only mode: use fp32 for gradients")
         return _WaveForward.apply(vel, wav_t, call, check)
     lib = _lib.load()
     ws = _workspace(call, False)

@@ -92,7 +92,8 @@ def test_workspace_holds_the_kept_levels():
     (dict(ndim=4), -1), (dict(order=6), -1), (dict(ny=3), -1), (dict(nz=8), -1),
     (dict(nshot=0), -1), (dict(nt=0), -1), (dict(dt=0.0), -1), (dict(dx=-1.0), -1),
     (dict(ckpt_format=3), -1), (dict(ckpt_every=-1), -1), (dict(lap_store=3), -1),
-    (dict(store_levels=-1), -1), (dict(vmax=1e6), -4),
+    (dict(store_levels=-1), -1), (dict(field_format=3), -1), (dict(field_format=1, ndim=3, ny=64), -1),
+    (dict(field_format=2, step_block=2), -1), (dict(vmax=1e6), -4),
 ])
 def test_invalid_problems_rejected(bad, code):
     from neuralmech_gb300 import _lib
@@ -158,3 +159,14 @@ def test_dropin_arguments_rejected():
     assert lib.wfd_step2d_scaled(ctypes.c_void_p(260), p, p, p, p, p, 1.0, 1e-3, 1e-2, 1e-2, 64, 60, 64,
                                  None) == -1  # q not 8-byte aligned
     assert "64" in lib.wfd_last_error().decode() or "aligned" in lib.wfd_last_error().decode()
+
+
+def test_reduced_precision_fields_halve_the_forward_workspace():
+    _, f32 = _ws(_problem(), 0)
+    _, f16 = _ws(_problem(field_format=1), 0)
+    _, i16 = _ws(_problem(field_format=2), 0)
+    field = 2 * 64 * 104 * 4
+    assert f32 - f16 >= 2 * field // 2 - 512  # two levels of 2 instead of 4 bytes
+    assert f16 < i16 < f32
+    rc, _ = _ws(_problem(field_format=1), 1)  # no gradient workspace: forward-only
+    assert rc == -1

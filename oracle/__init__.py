@@ -63,6 +63,9 @@ def lib():
         _lib.orc_step.argtypes = [P, d, ctypes.c_double, d, d, d, d, d, d]
         _lib.orc_forward.argtypes = [P, d, d, d, d, d, i32, i32, d, d]
         _lib.orc_gradient.argtypes = [P, d, d, d, d, d, i32, i32, d, d, d, d, d]
+        _lib.orc_stag_coeffs.argtypes = [ctypes.c_int, d]
+        _lib.orc_vd_forward.argtypes = [P, d, d, d, d, d, i32, i32, d, d]
+        _lib.orc_vd_gradient.argtypes = [P, d, d, d, d, d, i32, i32, d, d, d, d, d, d]
         for f in (_lib.orc_fd_coeffs, _lib.orc_step, _lib.orc_forward, _lib.orc_gradient):
             f.restype = ctypes.c_int
     return _lib
@@ -172,3 +175,63 @@ def step(order: int, h: tuple, uo, uc, un, w=None, w_const: float = 0.0, sponge=
                         _dp(uo), _dp(uc), _dp(un))
     assert rc == 0
     return un
+
+
+def stag_coeffs(order: int) -> np.ndarray:
+    """Staggered first-derivative weights c_1..c_R of order ``order`` (unit grid)."""
+    c = np.zeros(5)
+    if lib().orc_stag_coeffs(order, _dp(c)) != 0:
+        raise ValueError(f"unsupported order {order}")
+    return c[1: order // 2 + 1].copy()
+
+
+@dataclass
+class VdGeometry:
+    """Inputs of one variable-density oracle run (2D; kappa, rho per cell)."""
+    kappa: np.ndarray          # (nz, nx) bulk modulus
+    rho: np.ndarray            # (nz, nx) density
+    wavelet: np.ndarray        # (nshot, nt, nsrc)
+    src: np.ndarray            # (nshot, nsrc, 3) int (z, 0, x)
+    rec: np.ndarray            # (nshot, nrec, 3) int
+    dt: float
+    h: tuple                   # (dz, dx)
+    order: int = 8
+    sponge: tuple | None = None  # (gz, gx)
+    src_scale: float = 1.0
+
+
+def _vd_args(g: VdGeometry):
+    nz, nx = g.kappa.shape
+    nshot, nt, nsrc = g.wavelet.shape
+    p = _Problem(2, g.order, nz, 1, nx, nshot, nt, nsrc, g.rec.shape[1], 0, g.dt, g.h[0], 1.0, g.h[1],
+                 g.src_scale)
+    f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+    gz, gx = (None, None) if g.sponge is None else g.sponge
+    return (p, f(g.kappa), f(g.rho), f(gz), f(gx), f(g.wavelet), np.ascontiguousarray(g.src, dtype=np.int32),
+            np.ascontiguousarray(g.rec, dtype=np.int32))
+
+
+def vd_forward(g: VdGeometry, want_final: bool = False):
+    """Variable-density traces (nshot, nt, nrec) in FP64; optionally the final fields."""
+    p, kap, rho, gz, gx, wav, src, rec = _vd_args(g)
+    traces = np.zeros((p.nshot, p.nt, p.nrec))
+    final = np.zeros((p.nshot,) + g.kappa.shape) if want_final else None
+    rc = lib().orc_vd_forward(ctypes.byref(p), _dp(kap), _dp(rho), _dp(gz), _dp(gx), _dp(wav), _ip(src), _ip(rec),
+                              _dp(traces), _dp(final))
+    if rc != 0:
+        raise ValueError(f"orc_vd_forward failed ({rc})")
+    return (traces, final) if want_final else traces
+
+
+def vd_gradient(g: VdGeometry, observed: np.ndarray):
+    """(misfit, grad_kappa, grad_rho, grad_wavelet, traces) in FP64."""
+    p, kap, rho, gz, gx, wav, src, rec = _vd_args(g)
+    obs = np.ascontiguousarray(observed, dtype=np.float64)
+    gk, gr, gw = np.zeros(g.kappa.shape), np.zeros(g.kappa.shape), np.zeros(wav.shape)
+    traces = np.zeros((p.nshot, p.nt, p.nrec))
+    J = ctypes.c_double(0.0)
+    rc = lib().orc_vd_gradient(ctypes.byref(p), _dp(kap), _dp(rho), _dp(gz), _dp(gx), _dp(wav), _ip(src), _ip(rec),
+                               _dp(obs), _dp(gk), _dp(gr), _dp(gw), _dp(traces), ctypes.byref(J))
+    if rc != 0:
+        raise ValueError(f"orc_vd_gradient failed ({rc})")
+    return J.value, gk, gr, gw, traces

@@ -339,4 +339,243 @@ int orc_gradient(const orc_problem* p, const double* vel, const double* gz, cons
     return 0;
 }
 
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Variable density (2D): the conservative acoustic operator
+//     p_tt = kappa div(b grad p) + s,   b = 1 / rho,
+// the two-phase medium of cuwave's AcousticWave (projects/8_physics_drivers/
+// waveND.py:52-65; 1_benchmark_2D/README.md:141-144: 1/rho and 1/kappa are the
+// interpolated quantities). Staggered differences of order 2R on a unit grid,
+//     (D f)_j = sum_k c_k (f_{j+k} - f_{j-k+1})   at the half point j + 1/2,
+// c_k = 1/(2k-1) prod_{m != k} (2m-1)^2 / ((2m-1)^2 - (2k-1)^2), fluxes
+// F = b_half D u with b_half the mean of the two cells' b, and
+//     Lb u = sum_k c_k (Fx_{x+k-1} - Fx_{x-k}) + sz sum_k c_k (Fz_{z+k-1} - Fz_{z-k}),
+// sz = (dx/dz)^2. Fields and b are zero outside the grid. The update on the
+// interior is u_{n+1} = g (2 u_n + k Lb u_n + s w_n) - g^2 u_{n-1}, k = kappa dt^2/dx^2;
+// k b = (c dt / dx)^2 recovers the constant-density scaling.
+//
+// Lb = -Dx^T Bx Dx - sz Dz^T Bz Dz is symmetric, so the adjoint in q = k g mu is
+// the same update with k-weighted residuals injected, and
+//     dJ/dk_c      = sum_n q_{n+1,c} (Lb u_n)_c / k_c,
+//     dJ/dbx_{z,j} = -sum_n (Dx q_{n+1})_{z,j} (Dx u_n)_{z,j},  dJ/dbz likewise times sz,
+//     dJ/db_c      = (dJ/dbx_{x-1} + dJ/dbx_x + dJ/dbz_{z-1} + dJ/dbz_z) / 2,
+//     dJ/dkappa = dJ/dk dt^2 / dx^2,  dJ/drho = -dJ/db / rho^2.
+// The forward states are kept in full (FP64, small problems).
+namespace {
+
+void stag_coeffs(int R, double* c) {
+    for (int k = 1; k <= R; ++k) {
+        double v = 1.0 / (2 * k - 1);
+        for (int m = 1; m <= R; ++m)
+            if (m != k) {
+                const double a = (2 * m - 1) * (2 * m - 1), b = (2 * k - 1) * (2 * k - 1);
+                v *= a / (a - b);
+            }
+        c[k] = v;
+    }
+}
+
+struct VdGrid {
+    int R, nz, nx;
+    double c[5], sz;
+};
+
+// value of a zero-extended field
+inline double at(const VdGrid& g, const double* f, int z, int x) {
+    return (z < 0 || z >= g.nz || x < 0 || x >= g.nx) ? 0.0 : f[(long)z * g.nx + x];
+}
+inline double dx_half(const VdGrid& g, const double* f, int z, int j) {  // (Dx f) at (z, j + 1/2)
+    double s = 0;
+    for (int k = 1; k <= g.R; ++k) s += g.c[k] * (at(g, f, z, j + k) - at(g, f, z, j - k + 1));
+    return s;
+}
+inline double dz_half(const VdGrid& g, const double* f, int i, int x) {  // (Dz f) at (i + 1/2, x)
+    double s = 0;
+    for (int k = 1; k <= g.R; ++k) s += g.c[k] * (at(g, f, i + k, x) - at(g, f, i - k + 1, x));
+    return s;
+}
+inline double bx_half(const VdGrid& g, const double* b, int z, int j) {
+    return 0.5 * (at(g, b, z, j) + at(g, b, z, j + 1));
+}
+inline double bz_half(const VdGrid& g, const double* b, int i, int x) {
+    return 0.5 * (at(g, b, i, x) + at(g, b, i + 1, x));
+}
+inline double lb(const VdGrid& g, const double* b, const double* u, int z, int x) {
+    double s = 0;
+    for (int k = 1; k <= g.R; ++k) {
+        const int j1 = x + k - 1, j0 = x - k;
+        s += g.c[k] * (bx_half(g, b, z, j1) * dx_half(g, u, z, j1) - bx_half(g, b, z, j0) * dx_half(g, u, z, j0));
+        const int i1 = z + k - 1, i0 = z - k;
+        s += g.sz * g.c[k] *
+             (bz_half(g, b, i1, x) * dz_half(g, u, i1, x) - bz_half(g, b, i0, x) * dz_half(g, u, i0, x));
+    }
+    return s;
+}
+
+void vd_step(const VdGrid& g, const Grid& gg, const Sponge& sp, const double* k, const double* b,
+             const double* uo, const double* uc, double* un, double* lb_out) {
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < g.nz; ++z)
+        for (int x = 0; x < g.nx; ++x) {
+            if (!interior(gg, z, 0, x)) continue;
+            const long c = (long)z * g.nx + x;
+            const double L = lb(g, b, uc, z, x);
+            const double s = sp.at(z, 0, x);
+            un[c] = s * (2.0 * uc[c] + k[c] * L) - s * s * uo[c];
+            if (lb_out) lb_out[c] = L;
+        }
+}
+
+VdGrid make_vd(const orc_problem& p) {
+    VdGrid g{};
+    g.R = p.order / 2;
+    g.nz = p.nz;
+    g.nx = p.nx;
+    stag_coeffs(g.R, g.c);
+    g.sz = (p.dx * p.dx) / (p.dz * p.dz);
+    return g;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_stag_coeffs(int order, double* c) {
+    if (order != 2 && order != 4 && order != 8) return -1;
+    stag_coeffs(order / 2, c);
+    return 0;
+}
+
+// Variable-density forward: traces[s][n][r] = u_{n+1}(rec); u_final optional.
+int orc_vd_forward(const orc_problem* p, const double* kappa, const double* rho, const double* gz,
+                   const double* gx, const double* wavelet, const int32_t* src, const int32_t* rec,
+                   double* traces, double* u_final) {
+    if (p->ndim != 2) return -1;
+    const Grid gg = make_grid(*p);
+    const VdGrid g = make_vd(*p);
+    if (!positions_ok(gg, src, (long)p->nshot * p->nsrc) || !positions_ok(gg, rec, (long)p->nshot * p->nrec))
+        return -2;
+    const long N = gg.ncell;
+    std::vector<double> k(N), b(N), ua(N), ub(N);
+    for (long c = 0; c < N; ++c) {
+        k[c] = kappa[c] * p->dt * p->dt / (p->dx * p->dx);
+        b[c] = 1.0 / rho[c];
+    }
+    const Sponge sp{gz, nullptr, gx};
+    for (int s = 0; s < p->nshot; ++s) {
+        std::fill(ua.begin(), ua.end(), 0.0);
+        std::fill(ub.begin(), ub.end(), 0.0);
+        double *uo = ua.data(), *uc = ub.data();
+        const int32_t* sp_pos = src + 3L * s * p->nsrc;
+        const int32_t* rp_pos = rec + 3L * s * p->nrec;
+        for (int n = 0; n < p->nt; ++n) {
+            vd_step(g, gg, sp, k.data(), b.data(), uo, uc, uo, nullptr);
+            for (int i = 0; i < p->nsrc; ++i) {
+                const int32_t* q = sp_pos + 3 * i;
+                uo[cell_of(gg, q)] += sp.at(q[0], 0, q[2]) * p->src_scale * wavelet[((long)s * p->nt + n) * p->nsrc + i];
+            }
+            for (int r = 0; r < p->nrec; ++r)
+                traces[((long)s * p->nt + n) * p->nrec + r] = uo[cell_of(gg, rp_pos + 3 * r)];
+            std::swap(uo, uc);
+        }
+        if (u_final) std::memcpy(u_final + (long)s * N, uc, sizeof(double) * N);
+    }
+    return 0;
+}
+
+// Misfit J = 1/2 sum (d - d_obs)^2 and its gradient w.r.t. kappa, rho (summed
+// over shots) and the wavelets (optional), from the exact discrete adjoint.
+int orc_vd_gradient(const orc_problem* p, const double* kappa, const double* rho, const double* gz,
+                    const double* gx, const double* wavelet, const int32_t* src, const int32_t* rec,
+                    const double* observed, double* grad_kappa, double* grad_rho, double* grad_wavelet,
+                    double* traces, double* misfit) {
+    if (p->ndim != 2) return -1;
+    const Grid gg = make_grid(*p);
+    const VdGrid g = make_vd(*p);
+    if (!positions_ok(gg, src, (long)p->nshot * p->nsrc) || !positions_ok(gg, rec, (long)p->nshot * p->nrec))
+        return -2;
+    const long N = gg.ncell;
+    const int nt = p->nt;
+    std::vector<double> k(N), b(N);
+    for (long c = 0; c < N; ++c) {
+        k[c] = kappa[c] * p->dt * p->dt / (p->dx * p->dx);
+        b[c] = 1.0 / rho[c];
+    }
+    const Sponge sp{gz, nullptr, gx};
+    std::vector<double> GK(N, 0.0), GBX(N, 0.0), GBZ(N, 0.0);  // half points (z, x + 1/2), (z + 1/2, x)
+    std::vector<double> U((size_t)(nt + 1) * N), qa(N), qb(N), L(N);
+    std::vector<double> d((size_t)nt * p->nrec), res((size_t)nt * p->nrec);
+    double J = 0.0;
+    for (int s = 0; s < p->nshot; ++s) {
+        const int32_t* sp_pos = src + 3L * s * p->nsrc;
+        const int32_t* rp_pos = rec + 3L * s * p->nrec;
+        const double* wav = wavelet + (long)s * nt * p->nsrc;
+        // forward, every level kept: U[n] = u_n, n = 0 .. nt (u_0 = u_{-1} = 0)
+        std::fill(U.begin(), U.begin() + N, 0.0);
+        std::vector<double> um(N, 0.0);
+        for (int n = 0; n < nt; ++n) {
+            double* un = &U[(size_t)(n + 1) * N];
+            const double* uc = &U[(size_t)n * N];
+            const double* uo = n == 0 ? um.data() : &U[(size_t)(n - 1) * N];
+            std::fill(un, un + N, 0.0);
+            vd_step(g, gg, sp, k.data(), b.data(), uo, uc, un, nullptr);
+            for (int i = 0; i < p->nsrc; ++i) {
+                const int32_t* q = sp_pos + 3 * i;
+                un[cell_of(gg, q)] += sp.at(q[0], 0, q[2]) * p->src_scale * wav[n * p->nsrc + i];
+            }
+            for (int r = 0; r < p->nrec; ++r) d[(size_t)n * p->nrec + r] = un[cell_of(gg, rp_pos + 3 * r)];
+        }
+        const double* obs = observed + (long)s * nt * p->nrec;
+        for (size_t i = 0; i < d.size(); ++i) {
+            res[i] = d[i] - obs[i];
+            J += 0.5 * res[i] * res[i];
+        }
+        if (traces) std::memcpy(traces + (long)s * nt * p->nrec, d.data(), sizeof(double) * d.size());
+        // adjoint: q_k = g (2 q_{k+1} + k Lb q_{k+1} + k P^T r_{k-1}) - g^2 q_{k+2}
+        std::fill(qa.begin(), qa.end(), 0.0);
+        std::fill(qb.begin(), qb.end(), 0.0);
+        double *qo = qa.data(), *qc = qb.data();
+        auto adjoint_step = [&](int kk) {
+            vd_step(g, gg, sp, k.data(), b.data(), qo, qc, qo, nullptr);
+            for (int r = 0; r < p->nrec; ++r) {
+                const int32_t* q = rp_pos + 3 * r;
+                const long c = cell_of(gg, q);
+                qo[c] += sp.at(q[0], 0, q[2]) * k[c] * res[(size_t)(kk - 1) * p->nrec + r];
+            }
+            std::swap(qo, qc);
+        };
+        double* gw = grad_wavelet ? grad_wavelet + (long)s * nt * p->nsrc : nullptr;
+        adjoint_step(nt);
+        for (int n = nt - 1; n >= 0; --n) {
+            // qc = q_{n+1}: the terms of u_n
+            const double* u = &U[(size_t)n * N];
+#pragma omp parallel for schedule(static)
+            for (int z = 0; z < g.nz; ++z)
+                for (int x = 0; x < g.nx; ++x) {
+                    const long c = (long)z * g.nx + x;
+                    if (interior(gg, z, 0, x)) GK[c] += qc[c] * lb(g, b.data(), u, z, x);
+                    GBX[c] -= dx_half(g, qc, z, x) * dx_half(g, u, z, x);
+                    GBZ[c] -= g.sz * dz_half(g, qc, z, x) * dz_half(g, u, z, x);
+                }
+            if (gw)
+                for (int i = 0; i < p->nsrc; ++i) {
+                    const long c = cell_of(gg, sp_pos + 3 * i);
+                    gw[n * p->nsrc + i] = p->src_scale * qc[c] / k[c];
+                }
+            if (n >= 1) adjoint_step(n);
+        }
+    }
+    for (int z = 0; z < g.nz; ++z)
+        for (int x = 0; x < g.nx; ++x) {
+            const long c = (long)z * g.nx + x;
+            grad_kappa[c] = interior(gg, z, 0, x) ? GK[c] / k[c] * p->dt * p->dt / (p->dx * p->dx) : 0.0;
+            const double db = 0.5 * ((x > 0 ? GBX[c - 1] : 0.0) + GBX[c] + (z > 0 ? GBZ[c - g.nx] : 0.0) + GBZ[c]);
+            grad_rho[c] = -db / (rho[c] * rho[c]);
+        }
+    *misfit = J;
+    return 0;
+}
+
 }  // extern "C"

@@ -229,3 +229,77 @@ def test_scaled_step_restatement_tracks_fp32():
     got = (np.repeat(b[1], 32, axis=1) * b[0])[:, :M]
     assert np.linalg.norm(got - fb) / np.linalg.norm(fb) < 2e-4
     assert np.all(b[0][:, M - 1:] == 0) and np.all(b[0][1:-1, 0] == 0)
+
+
+def test_staggered_weights_taylor(orc):
+    """sum_k c_k (2k-1)^(2j+1) = 1 for j = 0 and 0 for 0 < j < R: exact first
+    derivatives of the odd monomials up to degree 2R - 1 at the half point."""
+    for order in (2, 4, 8):
+        c = orc.stag_coeffs(order)
+        R = order // 2
+        for j in range(R):
+            terms = [c[k - 1] * (2 * k - 1) ** (2 * j + 1) for k in range(1, R + 1)]
+            assert abs(sum(terms) - (1.0 if j == 0 else 0.0)) < 1e-14 * sum(abs(t) for t in terms)
+
+
+def _vd_case(orc, order, sponge=True, seed=0):
+    rng = np.random.default_rng(seed)
+    nz, nx, nt = 34, 46, 70
+    kap = 2.0e9 * (1 + 0.2 * rng.random((nz, nx)))
+    rho = 1000.0 * (1 + 0.5 * rng.random((nz, nx)))
+    rho[10:16, 15:30] = 2600.0  # a dense inclusion: a sharp interface
+    dt, h = 1e-4, (6.0, 5.0)
+    wav = np.zeros((2, nt, 1))
+    wav[:, :12, 0] = np.sin(0.5 * np.arange(12))[None] * np.array([[1.0], [0.7]])
+    src = np.array([[[17, 0, 23]], [[12, 0, 9]]])
+    rec = np.array([[[8, 0, 10], [22, 0, 36], [12, 0, 30]]] * 2)
+    sp = None
+    if sponge:
+        from neuralmech_gb300 import sponge_profile
+        sp = (sponge_profile(nz, 6, 6).astype(np.float64), sponge_profile(nx, 6, 6).astype(np.float64))
+    return orc.VdGeometry(kap, rho, wav, src, rec, dt, h, order=order, sponge=sp)
+
+
+def test_vd_constant_density_order2_is_the_scalar_step(orc):
+    """At order 2 the staggered operator with constant rho is the 5-point
+    Laplacian: the variable-density oracle equals the scalar one with v^2 = kappa/rho."""
+    g = _vd_case(orc, 2)
+    g.rho = np.full_like(g.rho, 1500.0)
+    vel = np.sqrt(g.kappa / g.rho)
+    t_vd = orc.vd_forward(g)
+    gs = orc.Geometry(vel=vel, wavelet=g.wavelet, src=g.src, rec=g.rec, dt=g.dt, h=(g.h[0], 1.0, g.h[1]), order=2,
+                      sponge=(g.sponge[0], None, g.sponge[1]))
+    t_sc = orc.forward(gs)
+    assert rel_l2(t_vd, t_sc) < 1e-12
+
+
+@pytest.mark.parametrize("order", [2, 8])
+def test_vd_gradient_finite_differences(orc, order):
+    """The variable-density adjoint gradient w.r.t. kappa and rho (every cell,
+    the fixed ring included: rho there enters the boundary fluxes) against
+    central differences of the FP64 misfit."""
+    g = _vd_case(orc, order)
+    obs = orc.vd_forward(orc.VdGeometry(**{**g.__dict__, "kappa": g.kappa * 1.03}))
+    J, gk, gr, gw, _ = orc.vd_gradient(g, obs)
+    rng = np.random.default_rng(4)
+    for name, grad in (("kappa", gk), ("rho", gr)):
+        base = getattr(g, name)
+        d = rng.standard_normal(base.shape) * base
+        eps = 1e-6
+
+        def Jof(v):
+            t = orc.vd_forward(orc.VdGeometry(**{**g.__dict__, name: v}))
+            return 0.5 * ((t - obs) ** 2).sum()
+
+        fd = (Jof(base + eps * d) - Jof(base - eps * d)) / (2 * eps)
+        an = float((grad * d).sum())
+        assert abs(fd - an) < 1e-6 * abs(fd), (name, fd, an)
+    # wavelet gradient: one sample
+    wav = g.wavelet.copy()
+    eps = 1e-6
+    wp, wm = wav.copy(), wav.copy()
+    wp[1, 5, 0] += eps
+    wm[1, 5, 0] -= eps
+    Jp = 0.5 * ((orc.vd_forward(orc.VdGeometry(**{**g.__dict__, "wavelet": wp})) - obs) ** 2).sum()
+    Jm = 0.5 * ((orc.vd_forward(orc.VdGeometry(**{**g.__dict__, "wavelet": wm})) - obs) ** 2).sum()
+    assert abs((Jp - Jm) / (2 * eps) - gw[1, 5, 0]) < 1e-6 * abs(gw[1, 5, 0])

@@ -242,6 +242,31 @@ int wfd_step2d_order2(const float* u0, const float* u1, float* u2, float wavespe
                       float dx, float dy, int N, int M, int M_padded, void* stream);
 
 /*
+ * Variable density (2D): the conservative acoustic operator
+ *     u_{n+1} = g (2 u_n + k Lb u_n + src_scale * w_n) - g^2 u_{n-1},
+ *     k = kappa dt^2 / dx^2,  Lb u = Dx^- (b Dx^+ u) + (dx/dz)^2 Dz^- (b Dz^+ u),
+ * b = 1 / rho averaged onto the half points, Dx^+ / Dx^- the order-`order`
+ * staggered differences on a unit grid (fields and b zero outside the grid);
+ * the two-phase medium of cuwave's AcousticWave (projects/8_physics_drivers/
+ * waveND.py:52-65), which has no counterpart in this repository's reference
+ * kernels. kappa and rho are [nz][nx] FP32 device arrays; the other arguments
+ * and the workspace rules are those of wfd_forward / wfd_misfit_gradient
+ * (2D, step_block 0/1, lap_store WFD_LAP_AUTO, FP32 fields, no shot groups;
+ * store_levels keeps forward levels as in the constant-density path).
+ * wfd_vd_misfit_gradient returns dJ/dkappa and dJ/drho, each [nz][nx] and
+ * summed over the shots, and optionally dJ/dwavelet.
+ */
+int wfd_vd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes);
+int wfd_vd_forward(const wfd_problem* p, const float* kappa, const float* rho, const float* sponge_z,
+                   const float* sponge_x, const float* wavelet, const int32_t* src, const int32_t* rec,
+                   float* traces, void* workspace, size_t workspace_bytes, void* stream);
+int wfd_vd_misfit_gradient(const wfd_problem* p, const float* kappa, const float* rho, const float* sponge_z,
+                           const float* sponge_x, const float* wavelet, const int32_t* src, const int32_t* rec,
+                           const float* observed, float* traces, float* grad_kappa, float* grad_rho,
+                           float* grad_wavelet, double* misfit, void* workspace, size_t workspace_bytes,
+                           void* stream);
+
+/*
  * The same step with the field stored in FP16: mixed_step,
  * projects/18_simple_wave_fd/step2D_wave.cu:85-124, launched as in
  * 2D_wave_cuda_mixed.py. u0, u1, u2 are [N][M_padded] IEEE binary16 (raw

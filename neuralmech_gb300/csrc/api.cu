@@ -169,7 +169,23 @@ struct Geom {
     int jstore, k0_store;    // u store: the forward keeps the levels of segments >= jstore
     bool lap_bf16;           // stored L u_k in BF16 (when !ustore)
     float c0, cz[4], cy[4], cx[4];
+    bool vd;                 // variable density (2D): 128 x 16 tiles, staggered operator
+    float cs[4], vd_sz;      // staggered first-derivative weights, (dx/dz)^2
 };
+
+// Staggered first-derivative weights of order 2R on a unit grid:
+// c_k = 1/(2k-1) prod_{m != k} (2m-1)^2 / ((2m-1)^2 - (2k-1)^2).
+void stag_weights(int R, double* c) {
+    for (int k = 1; k <= R; ++k) {
+        double v = 1.0 / (2 * k - 1);
+        for (int m = 1; m <= R; ++m)
+            if (m != k) {
+                const double a = (2 * m - 1) * (2 * m - 1), b = (2 * k - 1) * (2 * k - 1);
+                v *= a / (a - b);
+            }
+        c[k] = v;
+    }
+}
 
 int cdiv(long long a, long long b) { return int((a + b - 1) / b); }
 
@@ -241,8 +257,9 @@ int check_problem(const wfd_problem* p) {
 // tile_rows > 0 overrides the problem's 2D tile height and step_block >= 1
 // its steps per launch (the u-store adjoint runs one step per launch on
 // 16-row tiles: its third staged tile must leave room for the stages).
-Geom make_geom(const wfd_problem* p, int tile_rows = 0, int step_block = 0) {
+Geom make_geom(const wfd_problem* p, int tile_rows = 0, int step_block = 0, bool vd = false) {
     Geom g{};
+    g.vd = vd;
     g.ndim = p->ndim;
     g.R = p->order / 2;
     g.nz = p->nz;
@@ -253,7 +270,12 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0, int step_block = 0) {
     g.cells = (long long)g.nz * g.plane;
     const int sb = step_block > 0 ? step_block : p->step_block;
     g.sb = (p->ndim == 2 && sb == 2) ? 2 : 1;
-    if (g.ndim == 2 && g.sb == 2) {
+    if (vd) {
+        g.sb = 1;
+        g.tile_z = 16;  // the variable-density kernel's 128 x 16 tile
+        g.tile_y = 1;
+        g.tile_x = T2_TX;
+    } else if (g.ndim == 2 && g.sb == 2) {
         g.tile_z = K2_TZ;
         g.tile_y = 1;
         g.tile_x = K2_TX;
@@ -306,6 +328,12 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0, int step_block = 0) {
         g.cy[k - 1] = k <= g.R ? float(a[k] * sy) : 0.f;
         g.cx[k - 1] = k <= g.R ? float(a[k]) : 0.f;
     }
+    if (vd) {
+        double c[5] = {0, 0, 0, 0, 0};
+        stag_weights(g.R, c);
+        for (int k = 1; k <= 4; ++k) g.cs[k - 1] = k <= g.R ? float(c[k]) : 0.f;
+        g.vd_sz = float(sz);
+    }
     return g;
 }
 
@@ -323,6 +351,7 @@ struct Layout {
     size_t Q[4], G, ckpt, lap, res, total;
     size_t field_bytes, ckpt_field_bytes, lap_field_bytes;
     size_t S[2], scale_bytes;  // reduced-precision fields: the int16 block scales
+    size_t b, Gbx, Gbz;        // variable density: b = 1/rho, half-point gradient sums
     int nlap;  // slots of the lap region: K stored L u_k, or levels u_k (u store): from
                // u_{k0_store - 1} to u_nt, and at least K + 2 for a recomputed segment
 };
@@ -340,6 +369,7 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     L.nbuf = g.sb == 2 ? 4 : 2;
     L.err = take(256);
     L.m = take((size_t)g.cells * 4);
+    if (g.vd) L.b = take((size_t)g.cells * 4);
     for (int b = 0; b < L.nbuf; ++b) L.P[b] = take(L.field_bytes);
     if (p->field_format == WFD_FIELD_I16) {
         L.scale_bytes = (size_t)p->nshot * g.nz * scale_blocks(g.ld) * 4;
@@ -368,6 +398,10 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
         L.nlap = g.ustore ? std::max(g.K + 2, p->nt - g.k0_store + 2) : g.K;
         for (int b = 0; b < 2; ++b) L.Q[b] = take(L.field_bytes);  // (the adjoint is one-step)
         L.G = take((size_t)g.cells * 4);
+        if (g.vd) {
+            L.Gbx = take((size_t)g.cells * 4);
+            L.Gbz = take((size_t)g.cells * 4);
+        }
         // (segments whose levels the forward keeps need no checkpoint)
         L.ckpt = take((size_t)(g.ustore ? g.jstore : g.nseg) * 2 * L.ckpt_field_bytes);
         L.lap = take((size_t)L.nlap * L.lap_field_bytes);
@@ -381,6 +415,9 @@ struct Work {
     unsigned* err;
     float *m, *P[4], *Q[4], *G, *res;
     float* S[2];  // int16 block scales of P[0], P[1] (reduced-precision fields)
+    float *b, *Gbx, *Gbz;  // variable density (workspace)
+    const float* rho;      // variable density: the caller's rho, for setup and the gradient
+    float* grad_rho;       // variable density: dJ/drho output
     int* counts;
     PointLists src, rec, src_e;
     PointLists src_a, rec_a;  // lists of the adjoint geometry (== src, rec unless u store)
@@ -396,6 +433,11 @@ Work carve(void* ws, const Layout& L, bool grad) {
     Work w{};
     w.err = reinterpret_cast<unsigned*>(b + L.err);
     w.m = reinterpret_cast<float*>(b + L.m);
+    if (L.b) w.b = reinterpret_cast<float*>(b + L.b);
+    if (L.Gbx) {
+        w.Gbx = reinterpret_cast<float*>(b + L.Gbx);
+        w.Gbz = reinterpret_cast<float*>(b + L.Gbz);
+    }
     for (int k = 0; k < L.nbuf; ++k) w.P[k] = reinterpret_cast<float*>(b + L.P[k]);
     if (L.S[0])
         for (int k = 0; k < 2; ++k) w.S[k] = reinterpret_cast<float*>(b + L.S[k]);
@@ -448,7 +490,21 @@ struct Stepper {
     const float *gz, *gy, *gx;
     CUtensorMap map_m{};  // 3D: tiles of the model m; 2D two-step: m on the extended tile
 
+    const float* bfield = nullptr;  // variable density: b = 1/rho
+
     int init() {
+        if (g.vd) {  // b on the tile with R rows / 8 columns of halo (and one more row)
+            EncodeTiled enc = encoder();
+            if (!enc) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+            const cuuint64_t dims[2] = {(cuuint64_t)g.nx, (cuuint64_t)g.nz};
+            const cuuint64_t strides[1] = {(cuuint64_t)g.ld * 4};
+            const cuuint32_t box[2] = {T2_TX + 16, cuuint32_t(16 + 2 * g.R + 1)}, estr[2] = {1, 1};
+            CUresult r = enc(&map_m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(bfield), dims,
+                             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled (b) failed (%d)", (int)r);
+            return WFD_OK;
+        }
         if (g.ndim == 2 && g.sb == 2) {
             EncodeTiled enc = encoder();
             if (!enc) return fail(WFD_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
@@ -491,12 +547,22 @@ struct Stepper {
         a.c0 = g.c0;
         for (int k = 0; k < 4; ++k) { a.cz[k] = g.cz[k]; a.cy[k] = g.cy[k]; a.cx[k] = g.cx[k]; }
         a.zero_ring = 1;  // the wave path's ring is 0 in every level
+        if (g.vd) {
+            for (int k = 0; k < 4; ++k) a.cs[k] = g.cs[k];
+            a.vd_sz = g.vd_sz;
+        }
         a.err = err;
         return a;
     }
 
     int map_pair(const float* cur, const float* old, CUtensorMap* mc, CUtensorMap* mo) const {
         int rc;
+        if (g.vd) {  // the field with 2R rows / 8 columns of halo
+            const cuuint32_t bc[3] = {T2_TX + 16, cuuint32_t(16 + 4 * g.R), 1};
+            const cuuint32_t bo[3] = {T2_TX, 16, 1};
+            if ((rc = make_field_map(mc, cur, false, 2, g.nz, 1, g.nx, g.ld, p->nshot, bc))) return rc;
+            return make_field_map(mo, old, false, 2, g.nz, 1, g.nx, g.ld, p->nshot, bo);
+        }
         if (g.ndim == 2) {
             const cuuint32_t bc[3] = {T2_W, cuuint32_t(g.tile_z + 2 * g.R), 1};
             const cuuint32_t bo[3] = {T2_TX, cuuint32_t(g.tile_z), 1};
@@ -535,8 +601,9 @@ struct Stepper {
 
     int launch(int mode, const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
                const StepArgs& a) const {
-        cudaError_t e = g.ndim == 2 ? launch_step2d(g.R, mode, g.tile_z, mc, mo, ml, a, s)
-                                    : launch_step3d(g.R, mode, mc, mo, ml, map_m, a, s);
+        cudaError_t e = g.vd           ? launch_step2d_vd(g.R, mode, mc, mo, ml, map_m, a, s)
+                        : g.ndim == 2 ? launch_step2d(g.R, mode, g.tile_z, mc, mo, ml, a, s)
+                                      : launch_step3d(g.R, mode, mc, mo, ml, map_m, a, s);
         if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "step launch failed: %s", cudaGetErrorString(e));
         return WFD_OK;
     }
@@ -568,7 +635,11 @@ wfd_problem group_problem(const wfd_problem* p, int g0) {
 int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
           const int32_t* src, const int32_t* rec, cudaStream_t s, bool clear_status = true) {
     if (clear_status) WFD_CUDA(cudaMemsetAsync(w.err, 0, sizeof(unsigned), s));  // fresh status word
-    WFD_CUDA(launch_vel_to_m(vel, w.m, g.nz, g.ny, g.nx, g.ld, p->dt / p->dx, s));
+    if (g.vd)  // vel is kappa: k = kappa dt^2 / dx^2, b = 1 / rho
+        WFD_CUDA(launch_vd_params(vel, w.rho, w.m, w.b, g.nz, g.nx, g.ld,
+                                  float((double)p->dt * p->dt / ((double)p->dx * p->dx)), s));
+    else
+        WFD_CUDA(launch_vel_to_m(vel, w.m, g.nz, g.ny, g.nx, g.ld, p->dt / p->dx, s));
     WFD_CUDA(launch_build_lists(src, p->nshot, p->nsrc, g.nz, g.ny, g.nx, g.ld, g.R, g.tile_z,
                                 g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
                                 const_cast<int*>(w.src.off), const_cast<int2*>(w.src.ent), w.err, s));
@@ -788,7 +859,13 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
     sa.g = ga;
     WFD_CUDA(cudaMemsetAsync(w.Q[0], 0, L.field_bytes, s));
     WFD_CUDA(cudaMemsetAsync(w.Q[1], 0, L.field_bytes, s));
-    if (zero_G) WFD_CUDA(cudaMemsetAsync(w.G, 0, (size_t)g.cells * 4, s));
+    if (zero_G) {
+        WFD_CUDA(cudaMemsetAsync(w.G, 0, (size_t)g.cells * 4, s));
+        if (g.vd) {
+            WFD_CUDA(cudaMemsetAsync(w.Gbx, 0, (size_t)g.cells * 4, s));
+            WFD_CUDA(cudaMemsetAsync(w.Gbz, 0, (size_t)g.cells * 4, s));
+        }
+    }
     int rc;
     CUtensorMap qc[2], qo[2];
     for (int b = 0; b < 2; ++b)
@@ -823,6 +900,8 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
         }
         if (slot < 0) return sa.launch(MODE_PLAIN, qc[bc], qo[bn], qc[bc], a);
         a.grad = w.G;
+        a.grad_bx = w.Gbx;
+        a.grad_bz = w.Gbz;
         return sa.launch(MODE_GRAD_U, qc[bc], qo[bn], ua[slot], a);
     };
 
@@ -879,7 +958,11 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
     if (grad_wavelet && p->nsrc > 0)  // q_1 at the sources -> d J / d w_0
         WFD_CUDA(launch_gather(w.Q[1], ga.cells, w.src_a, ga.ntiles, p->nshot, p->nsrc, w.m,
                                p->src_scale, 1, grad_wavelet, p->nt, 0, s));
-    if (finalize) WFD_CUDA(launch_grad_finalize(w.G, vel, grad_vel, g.nz, g.ny, g.nx, g.ld, g.R, s));
+    if (finalize && g.vd)  // vel is kappa, grad_vel dJ/dkappa
+        WFD_CUDA(launch_vd_finalize(w.G, w.Gbx, w.Gbz, w.m, w.rho, grad_vel, w.grad_rho, g.nz, g.nx, g.ld, g.R,
+                                    float((double)p->dt * p->dt / ((double)p->dx * p->dx)), s));
+    else if (finalize)
+        WFD_CUDA(launch_grad_finalize(w.G, vel, grad_vel, g.nz, g.ny, g.nx, g.ld, g.R, s));
     return WFD_OK;
 }
 
@@ -1128,6 +1211,89 @@ int wfd_misfit_gradient(const wfd_problem* p, const float* vel, const float* spo
             return rc;
     }
     return WFD_OK;
+}
+
+// ------------------------------------------------------------------ variable density
+namespace {
+
+int vd_checks(const wfd_problem* p, const float* kappa, const float* rho, const float* wavelet,
+              const int32_t* src, const int32_t* rec) {
+    int rc = common_checks(p, kappa, wavelet, src, rec);
+    if (rc) return rc;
+    if (!rho) return fail(WFD_ERR_INVALID, "rho is NULL");
+    if (p->ndim != 2 || p->step_block == 2 || p->lap_store != WFD_LAP_AUTO ||
+        p->field_format != WFD_FIELD_FP32 || p->group_shots != 0)
+        return fail(WFD_ERR_INVALID,
+                    "variable density: 2D, one step per launch, lap_store auto, FP32 fields, no shot groups");
+    if (p->vmax > 0) {  // the staggered operator's bound: vmax dt sqrt((2 sum|c_k|)^2 sum 1/h^2) <= 2
+        double c[5] = {0, 0, 0, 0, 0};
+        stag_weights(p->order / 2, c);
+        double S = 0;
+        for (int k = 1; k <= p->order / 2; ++k) S += std::fabs(c[k]);
+        S = 4 * S * S;
+        const double inv2 = 1.0 / ((double)p->dz * p->dz) + 1.0 / ((double)p->dx * p->dx);
+        if (p->vmax * (double)p->dt * std::sqrt(inv2 * S) > 2.0)
+            return fail(WFD_ERR_UNSTABLE, "vmax*dt = %g exceeds the staggered CFL bound %g of order %d",
+                        p->vmax * (double)p->dt, 2.0 / std::sqrt(inv2 * S), p->order);
+    }
+    return WFD_OK;
+}
+
+}  // namespace
+
+int wfd_vd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes) {
+    int rc = check_problem(p);
+    if (rc) return rc;
+    if (!bytes) return fail(WFD_ERR_INVALID, "bytes is NULL");
+    const Geom g = make_geom(p, 0, 0, true);
+    *bytes = make_layout(p, g, with_gradient != 0).total;
+    return WFD_OK;
+}
+
+int wfd_vd_forward(const wfd_problem* p, const float* kappa, const float* rho, const float* sponge_z,
+                   const float* sponge_x, const float* wavelet, const int32_t* src, const int32_t* rec,
+                   float* traces, void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = vd_checks(p, kappa, rho, wavelet, src, rec);
+    if (rc) return rc;
+    const Geom g = make_geom(p, 0, 0, true);
+    const Layout L = make_layout(p, g, false);
+    if ((rc = check_workspace(workspace, workspace_bytes, L.total))) return rc;
+    Work w = carve(workspace, L, false);
+    w.rho = rho;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if ((rc = setup(p, g, w, kappa, src, rec, s))) return rc;
+    Stepper st{p, g, s, w.err, w.m, sponge_z, nullptr, sponge_x};
+    st.bfield = w.b;
+    if ((rc = st.init())) return rc;
+    return run_forward(p, g, L, w, st, wavelet, traces, false);
+}
+
+int wfd_vd_misfit_gradient(const wfd_problem* p, const float* kappa, const float* rho, const float* sponge_z,
+                           const float* sponge_x, const float* wavelet, const int32_t* src, const int32_t* rec,
+                           const float* observed, float* traces, float* grad_kappa, float* grad_rho,
+                           float* grad_wavelet, double* misfit, void* workspace, size_t workspace_bytes,
+                           void* stream) {
+    int rc = vd_checks(p, kappa, rho, wavelet, src, rec);
+    if (rc) return rc;
+    if (!grad_kappa || !grad_rho || !misfit || (p->nrec > 0 && !observed))
+        return fail(WFD_ERR_INVALID, "grad_kappa/grad_rho/misfit/observed is NULL");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    WFD_CUDA(cudaMemsetAsync(misfit, 0, sizeof(double), s));
+    const Geom g = make_geom(p, 0, 0, true);
+    const Layout L = make_layout(p, g, true);
+    if ((rc = check_workspace(workspace, workspace_bytes, L.total))) return rc;
+    Work w = carve(workspace, L, true);
+    w.rho = rho;
+    w.grad_rho = grad_rho;
+    if ((rc = setup(p, g, w, kappa, src, rec, s))) return rc;
+    Stepper st{p, g, s, w.err, w.m, sponge_z, nullptr, sponge_x};
+    st.bfield = w.b;
+    if ((rc = st.init())) return rc;
+    float* d = traces ? traces : w.res;
+    if ((rc = run_forward(p, g, L, w, st, wavelet, d, true))) return rc;
+    const long long ntr = (long long)p->nshot * p->nt * p->nrec;
+    if (ntr > 0) WFD_CUDA(launch_residual_misfit(d, observed, w.res, ntr, misfit, s));
+    return run_backward(p, g, L, w, st, wavelet, w.res, grad_kappa, grad_wavelet, kappa, true, true);
 }
 
 int wfd_status(void* workspace, void* stream) {

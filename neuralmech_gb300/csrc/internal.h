@@ -76,6 +76,10 @@ struct StepArgs {
     void* lap;                 // [nshot][cells] FP32 or BF16
     int lap_bf16;
     float* grad;               // [cells], MODE_GRAD accumulation target
+    // variable density (stencil2d_vd.cu): m holds k = kappa dt^2/dx^2
+    float cs[4];               // staggered first-derivative weights c_1..c_R
+    float vd_sz;               // (dx/dz)^2
+    float *grad_bx, *grad_bz;  // MODE_GRAD_U accumulators at the half points (z, x+1/2), (z+1/2, x)
     int zero_ring;             // 2D one-step kernel: also write the fixed ring (and the row
                                // padding) of u_new, as 0; else leave those cells untouched
     unsigned* err;
@@ -107,6 +111,17 @@ cudaError_t launch_step2d_lp(int R, int fmt, const CUtensorMap& map_cur, const C
 // u_final[row][x] (FP32, nx per row) from a reduced-precision field.
 cudaError_t launch_decode_field(int fmt, const void* f, const float* sc, float* out, long long nrows, int nx,
                                 int ld, int nblk, cudaStream_t s);
+
+// Variable-density step (stencil2d_vd.cu), mode MODE_PLAIN or MODE_GRAD_U on
+// 128 x 16 tiles. map_f: the field (box 144 x (16 + 4R) x 1 at x0 - 8, z0 - 2R);
+// map_o: u_{n-1} (box 128 x 16 x 1); map_u: u_k as map_f (MODE_GRAD_U); map_b:
+// b = 1/rho ([nz][ld], box 144 x (16 + 2R + 1) at x0 - 8, z0 - R).
+cudaError_t launch_step2d_vd(int R, int mode, const CUtensorMap& map_f, const CUtensorMap& map_o,
+                             const CUtensorMap& map_u, const CUtensorMap& map_b, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_vd_params(const float* kappa, const float* rho, float* k, float* b, int nz, int nx, int ld,
+                             float scale, cudaStream_t s);
+cudaError_t launch_vd_finalize(const float* G, const float* Gbx, const float* Gbz, const float* k, const float* rho,
+                               float* gkap, float* grho, int nz, int nx, int ld, int R, float scale, cudaStream_t s);
 
 // Launches one time step of the 2D kernel of half-width R (1, 2, 4), mode and
 // tile height tile_rows (16 or 32).

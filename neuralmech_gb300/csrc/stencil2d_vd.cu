@@ -1,0 +1,445 @@
+// Variable-density 2D time step (sm_103a): the conservative operator
+//     u_{n+1} = g (2 u_n + k Lb u_n) - g^2 u_{n-1},   k = kappa dt^2 / dx^2,
+//     Lb u = sum_k c_k (Fx_{x+k-1} - Fx_{x-k}) + sz sum_k c_k (Fz_{z+k-1} - Fz_{z-k}),
+//     Fx_j = bx_j (Dx u)_j,  (Dx u)_j = sum_k c_k (u_{j+k} - u_{j-k+1})  at x = j + 1/2,
+// b = 1 / rho, bx_j = (b_j + b_{j+1}) / 2 (likewise in z), c_k the order-2R
+// staggered first-derivative weights, sz = (dx/dz)^2; fields and b are zero
+// outside the grid. This is the two-phase medium of cuwave's AcousticWave
+// (projects/8_physics_drivers/waveND.py:52-65), which interpolates 1/rho and
+// 1/kappa between the phases (1_benchmark_2D/README.md:141-144).
+//
+// Per CTA (256 threads): a 128 x 16 tile of `shots_per_cta` shots. b on the
+// tile (plus R rows and 8 columns) is staged once by TMA with the first shot;
+// each shot's stage holds the field with a halo of 2R rows and 8 columns, the
+// u_{n-1} tile and, in MODE_GRAD_U, the level u_k with the same halo. For a
+// field, every thread forms the fluxes at its own half points (lanes 0 and 31
+// and warps 0 .. 2R-2 also the tile's halo ones) into shared memory, then the
+// divergence at its cells. MODE_GRAD_U does that for u_k (keeping L u_k and
+// the raw differences Dx u_k, Dz u_k of its half points in registers), then
+// for q_{k+1}, and accumulates
+//     G   += q_{k+1} Lb u_k            (cells, dJ/dk = G / k),
+//     Gbx -= (Dx q_{k+1}) (Dx u_k)     (half points (z, x + 1/2)),
+//     Gbz -= sz (Dz q_{k+1}) (Dz u_k)  (half points (z + 1/2, x)).
+// Sampling and injection are those of the constant-density kernel (k in the
+// role of m).
+#include <algorithm>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace wfd {
+namespace {
+
+constexpr int VD_TX = 128, VD_TZ = 16, VD_RB = 2, VD_THREADS = 256;
+constexpr int VD_W = VD_TX + 16;  // staged columns: x0 - 8 .. x0 + 135
+constexpr int VD_FXW = VD_TX + 8; // flux columns: half points x0 - 4 .. x0 + 131
+
+__host__ __device__ constexpr int al128(int v) { return (v + 127) / 128 * 128; }
+
+template <int R, int MODE>
+struct LayoutVD {
+    static constexpr int FH = VD_TZ + 4 * R;      // staged field rows: z0 - 2R ..
+    static constexpr int BH = VD_TZ + 2 * R + 1;  // staged b rows: z0 - R ..
+    static constexpr int ZH = VD_TZ + 2 * R;      // flux rows in z: half rows z0 - R ..
+    static constexpr int F = FH * VD_W * 4;
+    static constexpr int O = VD_TZ * VD_TX * 4;
+    static constexpr int U = MODE == MODE_GRAD_U ? F : 0;
+    static constexpr int O_OFF = al128(F);
+    static constexpr int U_OFF = O_OFF + al128(O);
+    static constexpr int STAGE = U_OFF + al128(U);
+    static constexpr int STAGES = 2;
+    static constexpr int B_OFF = STAGES * STAGE;
+    static constexpr int B = BH * VD_W * 4;
+    static constexpr int FX_OFF = B_OFF + al128(B);
+    static constexpr int FX = VD_TZ * VD_FXW * 4;
+    static constexpr int FZ_OFF = FX_OFF + al128(FX);
+    static constexpr int FZ = ZH * VD_TX * 4;
+    static constexpr int BAR_OFF = FZ_OFF + al128(FZ);
+    static constexpr int BYTES = BAR_OFF + 64 + 128;
+};
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, const float4& v) { *reinterpret_cast<float4*>(p) = v; }
+
+// Raw staggered x differences at the 4 half points whose window w[12] spans
+// the cells 4 left of the first half point's left cell to 7 right of it:
+// (Dx f)_{j+e} = sum_k c_k (w[4 + e + k] - w[5 + e - k]).
+template <int R>
+__device__ __forceinline__ float4 dx4(const float* w, const StepArgs& a) {
+    float d[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        float s = 0.f;
+#pragma unroll
+        for (int k = 1; k <= R; ++k) s = fmaf(a.cs[k - 1], w[4 + e + k] - w[5 + e - k], s);
+        d[e] = s;
+    }
+    return make_float4(d[0], d[1], d[2], d[3]);
+}
+
+template <int R, int MODE>
+__global__ void __launch_bounds__(VD_THREADS, MODE == MODE_PLAIN ? 2 : 1)
+    step2d_vd_kernel(const __grid_constant__ CUtensorMap map_f, const __grid_constant__ CUtensorMap map_o,
+                     const __grid_constant__ CUtensorMap map_u, const __grid_constant__ CUtensorMap map_b,
+                     const StepArgs a) {
+    using L = LayoutVD<R, MODE>;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* base = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base + L::BAR_OFF);
+    const float* B = reinterpret_cast<const float*>(base + L::B_OFF);
+    float* FX = reinterpret_cast<float*>(base + L::FX_OFF);
+    float* FZ = reinterpret_cast<float*>(base + L::FZ_OFF);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tile = blockIdx.x;
+    const int ntiles = a.tiles_x * a.tiles_z;
+    const int x0 = (tile % a.tiles_x) * VD_TX, z0 = (tile / a.tiles_x) * VD_TZ;
+    const int s0 = blockIdx.y * a.shots_per_cta;
+    const int ns = min(a.nshot - s0, a.shots_per_cta);
+    if (ns <= 0) return;
+
+    auto stage = [&](int b) { return base + b * L::STAGE; };
+    auto issue = [&](int i) {  // thread 0 only
+        const int b = i % L::STAGES;
+        mbar_arrive_expect_tx(&bars[b], uint32_t(L::F + L::O + L::U + (i == 0 ? L::B : 0)));
+        tma_load_3d(stage(b), &map_f, x0 - 8, z0 - 2 * R, s0 + i, &bars[b]);
+        tma_load_3d(stage(b) + L::O_OFF, &map_o, x0, z0, s0 + i, &bars[b]);
+        if (MODE == MODE_GRAD_U) tma_load_3d(stage(b) + L::U_OFF, &map_u, x0 - 8, z0 - 2 * R, s0 + i, &bars[b]);
+        if (i == 0) tma_load_2d(const_cast<float*>(B), &map_b, x0 - 8, z0 - R, &bars[b]);
+    };
+
+    __shared__ int2 smp_range[T2_MAX_SPC], inj_range[T2_MAX_SPC];
+    if (tid < ns) {
+        const int k = (s0 + tid) * ntiles + tile;
+        smp_range[tid] = a.smp.off ? make_int2(a.smp.off[k], a.smp.off[k + 1]) : make_int2(0, 0);
+        inj_range[tid] = a.inj.off ? make_int2(a.inj.off[k], a.inj.off[k + 1]) : make_int2(0, 0);
+    }
+    if (tid == 0) {
+        for (int b = 0; b < L::STAGES; ++b) mbar_init(&bars[b], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int i = 0; i < min(ns, L::STAGES); ++i) issue(i);
+
+    // ---- per-thread constants
+    const int x = x0 + 4 * lane;
+    const int zb = z0 + warp * VD_RB;
+    float4 krow[VD_RB];
+    float gzr[VD_RB];
+    bool zin[VD_RB];
+#pragma unroll
+    for (int r = 0; r < VD_RB; ++r) {
+        const int z = zb + r;
+        krow[r] = (z < a.nz && x < a.ld) ? __ldg(reinterpret_cast<const float4*>(a.m + (long long)z * a.ld + x))
+                                         : make_float4(0.f, 0.f, 0.f, 0.f);
+        gzr[r] = (a.gz != nullptr && z < a.nz) ? __ldg(a.gz + z) : 1.f;
+        zin[r] = z >= R && z < a.nz - R;
+    }
+    float gxe[4];
+    bool xin[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        gxe[e] = (a.gx != nullptr && x + e < a.nx) ? __ldg(a.gx + x + e) : 1.f;
+        xin[e] = x + e >= R && x + e < a.nx - R;
+    }
+    const bool all_x = xin[0] && xin[1] && xin[2] && xin[3];
+
+    float4 gk[VD_RB], gbx[VD_RB], gbz[VD_RB];
+#pragma unroll
+    for (int r = 0; r < VD_RB; ++r) {
+        gk[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+        gbx[r] = gk[r];
+        gbz[r] = gk[r];
+    }
+
+    // Fluxes of the staged field T into FX / FZ; the raw differences of the
+    // thread's own half points to dxr, dzr.
+    auto fluxes = [&](const float* T, float4* dxr, float4* dzr) {
+        auto trow = [&](int fr) { return T + fr * VD_W; };  // staged row of z = z0 - 2R + fr
+        auto brow = [&](int br) { return B + br * VD_W; };  // staged b row of z = z0 - R + br
+        // x: own half points x .. x + 3 of the rows zb, zb + 1
+#pragma unroll
+        for (int r = 0; r < VD_RB; ++r) {
+            const int fr = warp * VD_RB + r + 2 * R, br = warp * VD_RB + r + R;
+            const float4 p0 = ld4(trow(fr) + 4 * lane + 4), p1 = ld4(trow(fr) + 4 * lane + 8),
+                         p2 = ld4(trow(fr) + 4 * lane + 12);
+            const float w[12] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w, p2.x, p2.y, p2.z, p2.w};
+            const float4 d = dx4<R>(w, a);
+            const float4 b0 = ld4(brow(br) + 4 * lane + 8), b1 = ld4(brow(br) + 4 * lane + 12);
+            const float4 bx = make_float4(0.5f * (b0.x + b0.y), 0.5f * (b0.y + b0.z), 0.5f * (b0.z + b0.w),
+                                          0.5f * (b0.w + b1.x));
+            dxr[r] = d;
+            st4(FX + (warp * VD_RB + r) * VD_FXW + 4 + 4 * lane,
+                make_float4(bx.x * d.x, bx.y * d.y, bx.z * d.z, bx.w * d.w));
+            if (lane == 0 || lane == 31) {  // the tile's halo half points x0 - 4 .. x0 - 1, x0 + 128 .. x0 + 131
+                const int c0 = lane == 0 ? 0 : 4 * lane + 8;  // first staged column of the window
+                const float4 h0 = ld4(trow(fr) + c0), h1 = ld4(trow(fr) + c0 + 4), h2 = ld4(trow(fr) + c0 + 8);
+                const float hw[12] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w, h2.x, h2.y, h2.z, h2.w};
+                const float4 hd = dx4<R>(hw, a);
+                const float4 c4 = ld4(brow(br) + c0 + 4), c5 = ld4(brow(br) + c0 + 8);
+                const float4 hb = make_float4(0.5f * (c4.x + c4.y), 0.5f * (c4.y + c4.z), 0.5f * (c4.z + c4.w),
+                                              0.5f * (c4.w + c5.x));
+                st4(FX + (warp * VD_RB + r) * VD_FXW + (lane == 0 ? 0 : VD_TX + 4),
+                    make_float4(hb.x * hd.x, hb.y * hd.y, hb.z * hd.z, hb.w * hd.w));
+            }
+        }
+        // z: own half rows zb, zb + 1 from a window of field rows zb - R + 1 .. zb + R
+        {
+            float4 W[VD_RB + 2 * R - 1];
+#pragma unroll
+            for (int j = 0; j < VD_RB + 2 * R - 1; ++j) W[j] = ld4(trow(warp * VD_RB + R + 1 + j) + 8 + 4 * lane);
+#pragma unroll
+            for (int r = 0; r < VD_RB; ++r) {
+                float d[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    float s = 0.f;
+#pragma unroll
+                    for (int k = 1; k <= R; ++k) s = fmaf(a.cs[k - 1], comp(W[r + R - 1 + k], e) - comp(W[r + R - k], e), s);
+                    d[e] = s;
+                }
+                const int br = warp * VD_RB + r + R;
+                const float4 b0 = ld4(brow(br) + 8 + 4 * lane), b1 = ld4(brow(br + 1) + 8 + 4 * lane);
+                dzr[r] = make_float4(d[0], d[1], d[2], d[3]);
+                st4(FZ + (warp * VD_RB + r + R) * VD_TX + 4 * lane,
+                    make_float4(0.5f * (b0.x + b1.x) * d[0], 0.5f * (b0.y + b1.y) * d[1],
+                                0.5f * (b0.z + b1.z) * d[2], 0.5f * (b0.w + b1.w) * d[3]));
+            }
+        }
+        // z halo half rows: FZ rows 0 .. R-1 (warps 0 .. R-1) and VD_TZ + R .. VD_TZ + 2R - 2
+        if (warp < 2 * R - 1) {
+            const int f = warp < R ? warp : VD_TZ + warp;  // FZ row: half row z0 - R + f
+            float d[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int k = 1; k <= R; ++k) {
+                const float4 up = ld4(trow(f + R + k) + 8 + 4 * lane), dn = ld4(trow(f + R + 1 - k) + 8 + 4 * lane);
+                d[0] = fmaf(a.cs[k - 1], up.x - dn.x, d[0]);
+                d[1] = fmaf(a.cs[k - 1], up.y - dn.y, d[1]);
+                d[2] = fmaf(a.cs[k - 1], up.z - dn.z, d[2]);
+                d[3] = fmaf(a.cs[k - 1], up.w - dn.w, d[3]);
+            }
+            const float4 b0 = ld4(brow(f) + 8 + 4 * lane), b1 = ld4(brow(f + 1) + 8 + 4 * lane);
+            st4(FZ + f * VD_TX + 4 * lane,
+                make_float4(0.5f * (b0.x + b1.x) * d[0], 0.5f * (b0.y + b1.y) * d[1], 0.5f * (b0.z + b1.z) * d[2],
+                            0.5f * (b0.w + b1.w) * d[3]));
+        }
+    };
+
+    // Lb of the fluxes at the thread's cells (rows zb, zb + 1)
+    auto divergence = [&](float4* out) {
+        float4 Z[VD_RB + 2 * R - 1];  // FZ rows warp RB .. (half rows zb - R .. zb + RB + R - 2)
+#pragma unroll
+        for (int j = 0; j < VD_RB + 2 * R - 1; ++j) Z[j] = ld4(FZ + (warp * VD_RB + j) * VD_TX + 4 * lane);
+#pragma unroll
+        for (int r = 0; r < VD_RB; ++r) {
+            const float* fx = FX + (warp * VD_RB + r) * VD_FXW + 4 * lane;
+            const float4 p0 = ld4(fx), p1 = ld4(fx + 4), p2 = ld4(fx + 8);
+            const float w[12] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w, p2.x, p2.y, p2.z, p2.w};
+            float l[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                float sx = 0.f, sz = 0.f;
+#pragma unroll
+                for (int k = 1; k <= R; ++k) {
+                    sx = fmaf(a.cs[k - 1], w[3 + e + k] - w[4 + e - k], sx);
+                    sz = fmaf(a.cs[k - 1], comp(Z[r + R + k - 1], e) - comp(Z[r + R - k], e), sz);
+                }
+                l[e] = fmaf(a.vd_sz, sz, sx);
+            }
+            out[r] = make_float4(l[0], l[1], l[2], l[3]);
+        }
+    };
+
+    for (int i = 0; i < ns; ++i) {
+        const int s = s0 + i, b = i % L::STAGES;
+        if (!mbar_wait(&bars[b], (i / L::STAGES) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
+        const float* F = reinterpret_cast<const float*>(stage(b));
+        const float* O = reinterpret_cast<const float*>(stage(b) + L::O_OFF);
+        float* un = a.u_new + (long long)s * a.shot_stride;
+
+        float4 lbu[MODE == MODE_GRAD_U ? VD_RB : 1], dxu[MODE == MODE_GRAD_U ? VD_RB : 1],
+            dzu[MODE == MODE_GRAD_U ? VD_RB : 1];
+        if (MODE == MODE_GRAD_U) {
+            fluxes(reinterpret_cast<const float*>(stage(b) + L::U_OFF), dxu, dzu);
+            __syncthreads();
+            divergence(lbu);
+            __syncthreads();  // the flux buffers are free again
+        }
+        float4 dxq[VD_RB], dzq[VD_RB], lb[VD_RB];
+        fluxes(F, dxq, dzq);
+        __syncthreads();
+        divergence(lb);
+
+#pragma unroll
+        for (int r = 0; r < VD_RB; ++r) {
+            const int z = zb + r;
+            const float4 cv = ld4(F + (warp * VD_RB + r + 2 * R) * VD_W + 8 + 4 * lane);
+            const float4 ov = ld4(O + (warp * VD_RB + r) * VD_TX + 4 * lane);
+            float nv[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const float g = gzr[r] * gxe[e];
+                nv[e] = g * fmaf(comp(krow[r], e), comp(lb[r], e), 2.f * comp(cv, e)) - (g * g) * comp(ov, e);
+            }
+            const long long off = (long long)z * a.ld + x;
+            if (zin[r] && all_x) {
+                st4(un + off, make_float4(nv[0], nv[1], nv[2], nv[3]));
+            } else if (a.zero_ring) {
+                if (z < a.nz && x < a.ld)
+                    st4(un + off, make_float4(zin[r] && xin[0] ? nv[0] : 0.f, zin[r] && xin[1] ? nv[1] : 0.f,
+                                              zin[r] && xin[2] ? nv[2] : 0.f, zin[r] && xin[3] ? nv[3] : 0.f));
+            } else if (zin[r]) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (xin[e]) un[off + e] = nv[e];
+            }
+            if (MODE == MODE_GRAD_U) {
+                if (zin[r]) {
+                    gk[r].x += xin[0] ? cv.x * lbu[r].x : 0.f;
+                    gk[r].y += xin[1] ? cv.y * lbu[r].y : 0.f;
+                    gk[r].z += xin[2] ? cv.z * lbu[r].z : 0.f;
+                    gk[r].w += xin[3] ? cv.w * lbu[r].w : 0.f;
+                }
+                gbx[r].x -= dxq[r].x * dxu[r].x;
+                gbx[r].y -= dxq[r].y * dxu[r].y;
+                gbx[r].z -= dxq[r].z * dxu[r].z;
+                gbx[r].w -= dxq[r].w * dxu[r].w;
+                gbz[r].x -= a.vd_sz * dzq[r].x * dzu[r].x;
+                gbz[r].y -= a.vd_sz * dzq[r].y * dzu[r].y;
+                gbz[r].z -= a.vd_sz * dzq[r].z * dzu[r].z;
+                gbz[r].w -= a.vd_sz * dzq[r].w * dzu[r].w;
+            }
+        }
+
+        // sampling of the staged level (receivers of the previous step, or the
+        // adjoint field at the sources)
+        {
+            const int lo = smp_range[i].x, hi = smp_range[i].y;
+            for (int j = lo + tid; j < hi; j += VD_THREADS) {
+                const int2 en = a.smp.ent[j];
+                const int z = en.x / a.ld, xx = en.x - z * a.ld;
+                float v = F[(z - z0 + 2 * R) * VD_W + (xx - x0 + 8)] * a.smp_scale;
+                if (a.smp_div_m) v /= a.m[en.x];
+                a.smp_out[((long long)s * a.smp_nt + a.smp_t) * a.smp_np + en.y] = v;
+            }
+        }
+        __syncthreads();  // stage b fully read, fluxes consumed, this shot's stores done
+        if (tid == 0 && i + L::STAGES < ns) {
+            fence_proxy_async_smem();
+            issue(i + L::STAGES);
+        }
+        {
+            const int lo = inj_range[i].x, hi = inj_range[i].y;
+            for (int j = lo + tid; j < hi; j += VD_THREADS) {
+                const int2 en = a.inj.ent[j];
+                const int z = en.x / a.ld, xx = en.x - z * a.ld;
+                float v = a.inj_val[((long long)s * a.inj_nt + a.inj_t) * a.inj_np + en.y] * a.inj_scale;
+                if (a.inj_times_m) v *= a.m[en.x];
+                const float g = (a.gz ? a.gz[z] : 1.f) * (a.gx ? a.gx[xx] : 1.f);
+                atomicAdd(un + en.x, g * v);
+            }
+        }
+    }
+
+    if (MODE == MODE_GRAD_U) {
+#pragma unroll
+        for (int r = 0; r < VD_RB; ++r) {
+            const int z = zb + r;
+            if (z >= a.nz || x >= a.ld) continue;
+            const long long off = (long long)z * a.ld + x;
+            atomicAdd(reinterpret_cast<float4*>(a.grad + off), gk[r]);
+            atomicAdd(reinterpret_cast<float4*>(a.grad_bx + off), gbx[r]);
+            atomicAdd(reinterpret_cast<float4*>(a.grad_bz + off), gbz[r]);
+        }
+    }
+}
+
+template <int R, int MODE>
+cudaError_t launch_impl(const CUtensorMap& mf, const CUtensorMap& mo, const CUtensorMap& mu,
+                        const CUtensorMap& mb, const StepArgs& a, cudaStream_t s) {
+    using L = LayoutVD<R, MODE>;
+    static int configured_device = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (configured_device != dev) {
+        cudaError_t e = cudaFuncSetAttribute(step2d_vd_kernel<R, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             L::BYTES);
+        if (e != cudaSuccess) return e;
+        configured_device = dev;
+    }
+    const dim3 grid(a.tiles_x * a.tiles_z, (a.nshot + a.shots_per_cta - 1) / a.shots_per_cta);
+    step2d_vd_kernel<R, MODE><<<grid, VD_THREADS, L::BYTES, s>>>(mf, mo, mu, mb, a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <int R>
+cudaError_t dispatch(int mode, const CUtensorMap& mf, const CUtensorMap& mo, const CUtensorMap& mu,
+                     const CUtensorMap& mb, const StepArgs& a, cudaStream_t s) {
+    switch (mode) {
+        case MODE_PLAIN: return launch_impl<R, MODE_PLAIN>(mf, mo, mu, mb, a, s);
+        case MODE_GRAD_U: return launch_impl<R, MODE_GRAD_U>(mf, mo, mu, mb, a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// k = kappa dt^2 / dx^2 and b = 1 / rho on [nz][ld] (0 in the row padding).
+__global__ void vd_params_kernel(const float* kappa, const float* rho, float* k, float* b, int nz, int nx, int ld,
+                                 float scale) {
+    const long long n = (long long)nz * ld;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long z = i / ld;
+        const int x = int(i - z * ld);
+        const long long c = z * nx + x;
+        k[i] = x < nx ? kappa[c] * scale : 0.f;
+        b[i] = x < nx ? 1.f / rho[c] : 0.f;
+    }
+}
+
+// dJ/dkappa = G / k * scale on the interior; dJ/drho = -(Gbx_{x-1} + Gbx_x + Gbz_{z-1} + Gbz_z) / 2 / rho^2.
+__global__ void vd_finalize_kernel(const float* G, const float* Gbx, const float* Gbz, const float* k,
+                                   const float* rho, float* gkap, float* grho, int nz, int nx, int ld, int R,
+                                   float scale) {
+    const long long n = (long long)nz * nx;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int z = int(i / nx), x = int(i - (long long)z * nx);
+        const long long c = (long long)z * ld + x;
+        const bool in = z >= R && z < nz - R && x >= R && x < nx - R;
+        gkap[i] = in ? G[c] / k[c] * scale : 0.f;
+        const float db = 0.5f * ((x > 0 ? Gbx[c - 1] : 0.f) + Gbx[c] + (z > 0 ? Gbz[c - ld] : 0.f) + Gbz[c]);
+        grho[i] = -db / (rho[i] * rho[i]);
+    }
+}
+
+int blocks_for(long long n) { return (int)std::min<long long>(std::max<long long>((n + 255) / 256, 1), 152LL * 32); }
+
+}  // namespace
+
+cudaError_t launch_step2d_vd(int R, int mode, const CUtensorMap& map_f, const CUtensorMap& map_o,
+                             const CUtensorMap& map_u, const CUtensorMap& map_b, const StepArgs& a, cudaStream_t s) {
+    switch (R) {
+        case 1: return dispatch<1>(mode, map_f, map_o, map_u, map_b, a, s);
+        case 2: return dispatch<2>(mode, map_f, map_o, map_u, map_b, a, s);
+        case 4: return dispatch<4>(mode, map_f, map_o, map_u, map_b, a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_vd_params(const float* kappa, const float* rho, float* k, float* b, int nz, int nx, int ld,
+                             float scale, cudaStream_t s) {
+    vd_params_kernel<<<blocks_for((long long)nz * ld), 256, 0, s>>>(kappa, rho, k, b, nz, nx, ld, scale);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vd_finalize(const float* G, const float* Gbx, const float* Gbz, const float* k, const float* rho,
+                               float* gkap, float* grho, int nz, int nx, int ld, int R, float scale, cudaStream_t s) {
+    vd_finalize_kernel<<<blocks_for((long long)nz * nx), 256, 0, s>>>(G, Gbx, Gbz, k, rho, gkap, grho, nz, nx, ld, R,
+                                                                      scale);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace wfd

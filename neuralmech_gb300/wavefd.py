@@ -474,3 +474,74 @@ def step2d_order2(u0, u1, u2, wavespeed: float, dt: float, dx: float, dy: float,
     _lib.check(_lib.load().wfd_step2d_order2(_ptr(u0), _ptr(u1), _ptr(u2), wavespeed, dt, dx, dy,
                                              N, M, u1.shape[1], _stream()), "wfd_step2d_order2")
     return u2
+
+
+# ---------------------------------------------------------------- variable density
+def _vd_prepare(kappa, rho, wavelet, src, rec, grid: Grid, nshot=None):
+    if grid.ndim != 2:
+        raise ValueError("variable density is 2D")
+    _require_cuda(rho, "rho")
+    if tuple(rho.shape) != tuple(grid.shape):
+        raise ValueError(f"rho has shape {tuple(rho.shape)}, grid {grid.shape}")
+    rho = rho.detach().to(torch.float32).contiguous()
+    call = _prepare(kappa, torch.as_tensor(wavelet, device=kappa.device), src, rec, grid, nshot)
+    call.problem.vmax = float(torch.sqrt((call.vel / rho).max()))
+    return call, rho
+
+
+def _vd_workspace(call: _Call, with_gradient: bool) -> torch.Tensor:
+    lib = _lib.load()
+    n = ctypes.c_size_t(0)
+    _lib.check(lib.wfd_vd_workspace_bytes(ctypes.byref(call.problem), int(with_gradient), ctypes.byref(n)),
+               "wfd_vd_workspace_bytes")
+    ws = torch.empty(n.value + 256, dtype=torch.uint8, device=call.vel.device)
+    off = (-ws.data_ptr()) % 256
+    return ws[off:off + n.value]
+
+
+def vd_forward(kappa: torch.Tensor, rho: torch.Tensor, wavelet, src, rec, grid: Grid, *, check: bool = True):
+    """Traces (nshot, nt, nrec) of the variable-density acoustic medium
+    p_tt = kappa div(grad p / rho) + s (2D, staggered order-`grid.order`
+    operator; kappa, rho (nz, nx) CUDA tensors)."""
+    call, rho = _vd_prepare(kappa, rho, wavelet, src, rec, grid)
+    p = call.problem
+    ws = _vd_workspace(call, False)
+    traces = torch.empty((p.nshot, p.nt, p.nrec), dtype=torch.float32, device=kappa.device)
+    gz, _, gx = call.sponges
+    _lib.check(_lib.load().wfd_vd_forward(ctypes.byref(p), _ptr(call.vel), _ptr(rho), _ptr(gz), _ptr(gx),
+                                          _ptr(call.wavelet), _ptr(call.src), _ptr(call.rec), _ptr(traces),
+                                          _ptr(ws), ws.numel(), _stream()), "wfd_vd_forward")
+    if check:
+        _status(ws, "wfd_vd_forward")
+    return traces
+
+
+def vd_misfit_gradient(kappa: torch.Tensor, rho: torch.Tensor, wavelet, src, rec, observed: torch.Tensor,
+                       grid: Grid, *, want_wavelet: bool = False, want_traces: bool = False, check: bool = True):
+    """(misfit, dJ/dkappa, dJ/drho[, dJ/dwavelet][, traces]) of the
+    variable-density medium, misfit = 1/2 sum (traces - observed)^2 (FP64)."""
+    call, rho = _vd_prepare(kappa, rho, wavelet, src, rec, grid, observed.shape[0])
+    p = call.problem
+    _require_cuda(observed, "observed")
+    if tuple(observed.shape) != (p.nshot, p.nt, p.nrec):
+        raise ValueError(f"observed must be ({p.nshot}, {p.nt}, {p.nrec})")
+    obs = observed.to(torch.float32).contiguous()
+    ws = _vd_workspace(call, True)
+    gk = torch.empty_like(call.vel)
+    gr = torch.empty_like(call.vel)
+    gwav = torch.empty_like(call.wavelet) if want_wavelet else None
+    traces = torch.empty_like(obs) if want_traces else None
+    misfit = torch.zeros((), dtype=torch.float64, device=kappa.device)
+    gz, _, gx = call.sponges
+    _lib.check(_lib.load().wfd_vd_misfit_gradient(
+        ctypes.byref(p), _ptr(call.vel), _ptr(rho), _ptr(gz), _ptr(gx), _ptr(call.wavelet), _ptr(call.src),
+        _ptr(call.rec), _ptr(obs), _ptr(traces), _ptr(gk), _ptr(gr), _ptr(gwav), _ptr(misfit), _ptr(ws),
+        ws.numel(), _stream()), "wfd_vd_misfit_gradient")
+    if check:
+        _status(ws, "wfd_vd_misfit_gradient")
+    out = [misfit, gk, gr]
+    if want_wavelet:
+        out.append(gwav)
+    if want_traces:
+        out.append(traces)
+    return tuple(out)

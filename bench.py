@@ -86,7 +86,8 @@ def parse():
     ap.add_argument("--level-store-frac", type=float, default=0.65,
                     help="fraction of the GPU's memory for the forward levels the adjoint keeps "
                          "instead of recomputing them (0: recompute all but the last segment)")
-    ap.add_argument("--workload", default="fwi1024", choices=["fwi1024", "fwd2048", "fwi384_3d", "batch8"])
+    ap.add_argument("--workload", default="fwi1024",
+                    choices=["fwi1024", "fwd2048", "fwi384_3d", "batch8", "vd1024"])
     return ap.parse_args()
 
 
@@ -269,7 +270,7 @@ def run_other(args):
 
     import torch
 
-    from neuralmech_gb300 import _lib, misfit_gradient, wave_forward
+    from neuralmech_gb300 import _lib, levels_for_budget, misfit_gradient, wave_forward
     from neuralmech_gb300.synth import workload as wl
 
     dev = torch.device("cuda", 0)
@@ -291,7 +292,7 @@ def run_other(args):
                "models": [[list(m.call.grid.shape), m.call.grid.nt, m.call.problem.nshot] for m in batch.models],
                "configs": batch.configs}
     else:
-        w = wl(args.workload)
+        w = wl("fwi1024" if args.workload == "vd1024" else args.workload)
         g = w.grid
         if args.nt:
             g = dataclasses.replace(g, nt=args.nt, ckpt_every=min(g.ckpt_every or args.nt, args.nt))
@@ -301,7 +302,25 @@ def run_other(args):
         src, rec = torch.from_numpy(w.src), torch.from_numpy(w.rec)
         R = g.order // 2
         interior = float(np.prod([n - 2 * R for n in g.shape]))
-        if args.workload == "fwd2048":
+        if args.workload == "vd1024":
+            # the fwi1024 models with Gardner densities rho = 310 v^0.25 and kappa = rho v^2
+            from neuralmech_gb300.wavefd import vd_forward, vd_misfit_gradient
+            if args.level_store_frac > 0:
+                budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
+                g = dataclasses.replace(g, store_levels=levels_for_budget(g, w.nshot, budget))
+            rho_of = lambda v: 310.0 * np.power(v.astype(np.float64), 0.25)
+            r0, r1 = rho_of(w.vel), rho_of(w.vel_true)
+            kap = torch.from_numpy((r0 * w.vel.astype(np.float64) ** 2).astype(np.float32)).to(dev)
+            rho = torch.from_numpy(r0.astype(np.float32)).to(dev)
+            obs = vd_forward(torch.from_numpy((r1 * w.vel_true.astype(np.float64) ** 2).astype(np.float32)).to(dev),
+                             torch.from_numpy(r1.astype(np.float32)).to(dev), wav, src, rec, g)
+            step = lambda: vd_misfit_gradient(kap, rho, wav, src, rec, obs, g, check=False)
+            updates, bpu = 2.0 * w.nshot * interior * g.nt, 18.0
+            cfg = {"workload": f"vd1024: 2D variable-density FWI gradient (kappa, rho) {g.shape[0]}^2, {g.nt} steps, "
+                               f"{w.nshot} shots, {w.rec.shape[1]} receivers, order 8 staggered, 20-cell sponge, "
+                               f"Gardner densities, BF16 checkpoints every {g.ckpt_every}",
+                   "store_levels": g.store_levels}
+        elif args.workload == "fwd2048":
             g = dataclasses.replace(g, field_format=args.field_format)
             step = lambda: wave_forward(v, wav, src, rec, g, check=False)
             updates, bpu = w.nshot * interior * g.nt, 16.0

@@ -31,6 +31,13 @@ module's own. They are written here so callers can judge parity:
   A sin(2 pi f t) sin^2(pi f t / cycles) on 0 <= t <= cycles / f.
 * Array axes follow the reference (x first); they map onto the library's
   (z, x) axes unchanged.
+* AcousticWave(..., rho1, rho2, kappa1, kappa2): the two-phase medium
+  u_tt = kappa div(grad u / rho) + f of projects/8_physics_drivers/
+  waveND.py:52-65. Like cuwave (1_benchmark_2D/README.md:141-144) it
+  interpolates 1/rho and 1/kappa linearly in the indicator (0: rho1, kappa1;
+  1: rho2, kappa2), and source samples are scaled by the indicator at their
+  node, so that nothing is injected into a hole. misfit_gradient returns
+  d misfit / d gamma through kappa, rho and the source scaling.
 """
 from __future__ import annotations
 
@@ -41,7 +48,7 @@ import numpy as np
 import torch
 
 from .wavefd import Grid, misfit_gradient as _misfit_gradient, stable_dt as _stable_dt, wave_forward
-from .wavefd import wave_forward_final
+from .wavefd import vd_forward, vd_misfit_gradient, wave_forward_final
 
 
 @dataclass
@@ -235,3 +242,79 @@ class Adam:
         mh = self.m / (1 - self.b1 ** self.t)
         vh = self.v / (1 - self.b2 ** self.t)
         return x - self.lr * mh / (vh.sqrt() + self.eps)
+
+
+@dataclass
+class AcousticWave(ScalarWave):
+    """Two-phase acoustic descriptor (cuwave.acoustic.AcousticWave's arguments)."""
+    rho1: float = 1.204
+    rho2: float = 2643.0
+    kappa1: float = 1.419e5
+    kappa2: float = 6.87e8
+
+    def indicator(self, indicator) -> torch.Tensor:
+        """gamma on the padded grid: read from [:nx, :ny], edges extended."""
+        g = torch.as_tensor(indicator, device=self.device, dtype=torch.float32)
+        nx, ny = self.Nx
+        if g.dim() != 2 or g.shape[0] < nx or g.shape[1] < ny:
+            raise ValueError(f"indicator of shape {tuple(g.shape)} does not cover {self.Nx}")
+        g = g[:nx, :ny]
+        m = self.margin
+        if m:
+            g = torch.nn.functional.pad(g[None, None], (m, m, m, m), mode="replicate")[0, 0]
+        return g
+
+    def materials(self, indicator):
+        """(kappa, rho) on the padded grid from 1/rho and 1/kappa linear in gamma."""
+        g = self.indicator(indicator).double()
+        inv_rho = (1 - g) / self.rho1 + g / self.rho2
+        inv_kap = (1 - g) / self.kappa1 + g / self.kappa2
+        return (1 / inv_kap).float(), (1 / inv_rho).float()
+
+    def velocity(self, indicator) -> torch.Tensor:
+        kap, rho = self.materials(indicator)
+        return torch.sqrt(kap / rho)
+
+
+def _scaled_sources(sim: AcousticWave, sources, indicator):
+    """Source signals times the indicator at each source node."""
+    g = sim.indicator(indicator)
+    srcs = list(sources) if isinstance(sources, (list, tuple)) else [sources]
+    out = []
+    for s in srcs:
+        w = torch.as_tensor(np.asarray(g.detach().cpu())[s.nodes[:, 0], s.nodes[:, 1]], dtype=torch.float32)
+        out.append(Source(s.nodes, (s.signal * w.numpy()[None, :]).astype(np.float32)))
+    return _SourceList(out)
+
+
+def acoustic_measure(sim: AcousticWave, sources, indicator, sensors: Sensors):
+    kap, rho = sim.materials(indicator)
+    src, wav, rec = _batch(sim, _scaled_sources(sim, sources, indicator), sensors)
+    tr = vd_forward(kap, rho, torch.from_numpy(wav).to(kap.device), src, rec, sim.grid())
+    return list(tr.unbind(0))
+
+
+def acoustic_misfit_gradient(sim: AcousticWave, sources, indicator, sensors: Sensors, observed):
+    """(cost, d cost / d indicator) for the two-phase medium."""
+    gamma = torch.as_tensor(indicator, device=sim.device, dtype=torch.float32)
+    kap, rho = sim.materials(gamma)
+    scaled = _scaled_sources(sim, sources, gamma)
+    src, wav, rec = _batch(sim, scaled, sensors)
+    obs = torch.stack([torch.as_tensor(o, device=kap.device, dtype=torch.float32) for o in observed])
+    J, gk, gr, gw = vd_misfit_gradient(kap, rho, torch.from_numpy(wav).to(kap.device), src, rec, obs, sim.grid(),
+                                       want_wavelet=True)
+    # kappa = 1 / ((1-g)/k1 + g/k2): d kappa / d g = -kappa^2 (1/k2 - 1/k1); rho likewise
+    dk = -kap.double() ** 2 * (1 / sim.kappa2 - 1 / sim.kappa1)
+    dr = -rho.double() ** 2 * (1 / sim.rho2 - 1 / sim.rho1)
+    g_pad = (gk.double() * dk + gr.double() * dr)
+    # the source samples scale with gamma at their nodes: + sum_n dJ/dw_n * signal_n
+    srcs = list(sources) if isinstance(sources, (list, tuple)) else [sources]
+    for si, s in enumerate(srcs):
+        sig = torch.from_numpy(s.signal).to(kap.device).double()  # (N, nsrc)
+        contrib = (gw[si].double() * sig).sum(0)
+        for j, (a, b) in enumerate(s.nodes):
+            g_pad[a, b] += contrib[j]
+    m = sim.margin
+    out = torch.zeros_like(gamma)
+    out[:sim.Nx[0], :sim.Nx[1]] = g_pad[m:m + sim.Nx[0], m:m + sim.Nx[1]].float()
+    return J, out

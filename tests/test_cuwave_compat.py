@@ -119,3 +119,41 @@ def test_simulate_matches_measure(cuda):
     m = sim.margin
     nodes = sensors.nodes - m
     assert rel_l2(u[nodes[:, 0], nodes[:, 1]].cpu().numpy(), record[-1].cpu().numpy()) < 1e-6
+
+
+@pytest.mark.gpu
+def test_acoustic_indicator_gradient(cuda, orc):
+    """The two-phase AcousticWave adapter: d misfit / d gamma (through kappa,
+    rho and the source scaling) against central differences of the same
+    misfit computed by the FP64 variable-density oracle on the adapter's own
+    padded grid, positions and signals, along the steepest-descent direction."""
+    from neuralmech_gb300 import cuwave_compat as cw
+    n, N, E = 60, 200, 6
+    dx = (1.0 / (n - 3), 1.0 / (n - 3))
+    dt = 0.8 * cw.stable_dt(dx, float(np.sqrt(6.87e8 / 2643.0)), 8)
+    sim = cw.AcousticWave((n, n), dx, N, dt, space_order=8, rho1=1.204, rho2=2643.0, kappa1=1.419e5, kappa2=6.87e8)
+    t = np.arange(N) * dt
+    elements = cw.line((0.1, 1.0), (0.9, 1.0), E)
+    sources = cw.shots(sim, elements, cw.sineburst(t, 1.0, 8.0 / (N * dt), 2))[:3]
+    sensors = cw.Sensors(sim, elements)
+    gamma = torch.full((n, n), 0.8, device=cuda)
+    g_obs = gamma.clone()
+    g_obs[20:32, 25:40] = 0.95
+    observed = cw.acoustic_measure(sim, sources, g_obs, sensors)
+    cost, grad = cw.acoustic_misfit_gradient(sim, sources, gamma, sensors, observed)
+    assert torch.isfinite(grad).all() and grad.abs().max() > 0
+    obs = torch.stack(observed).cpu().numpy().astype(np.float64)
+    p3 = lambda p: np.stack([p[..., 0], 0 * p[..., 0], p[..., 1]], -1).astype(np.int32)
+
+    def J(gm):
+        kap, rho = (a.cpu().numpy().astype(np.float64) for a in sim.materials(gm))
+        src, wav, rec = cw._batch(sim, cw._scaled_sources(sim, sources, gm), sensors)
+        geo = orc.VdGeometry(kap, rho, wav.astype(np.float64), p3(src), p3(rec), float(np.float32(sim.dt)),
+                             tuple(sim.dx), order=8)
+        return 0.5 * float(((orc.vd_forward(geo) - obs) ** 2).sum())
+
+    d = 1e-3 * grad / grad.abs().max()
+    fd = (J(gamma + d) - J(gamma - d)) / 2
+    an = float((grad.double() * d.double()).sum())
+    print("acoustic adapter: fd", fd, "analytic", an)
+    assert abs(fd - an) < 5e-3 * abs(fd), (fd, an)

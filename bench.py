@@ -81,6 +81,8 @@ def parse():
     ap.add_argument("--shots", type=int, default=0, help="use the first N shots (profiling)")
     ap.add_argument("--field-format", default="fp32", choices=["fp32", "fp16", "i16"],
                     help="fwd2048: storage of the wavefields (arithmetic stays FP32)")
+    ap.add_argument("--adjoint", default="checkpoint", choices=["checkpoint", "reconstruct"],
+                    help="how the gradient obtains the forward levels")
     ap.add_argument("--step-block", type=int, default=1, choices=[1, 2],
                     help="time steps per launch of the forward and the recompute")
     ap.add_argument("--level-store-frac", type=float, default=0.65,
@@ -258,7 +260,7 @@ def config_of(w, args):
                          f"20-cell sponge, checkpoints every {g.ckpt_every} ({g.ckpt_format})"),
             "grid": list(g.shape), "nt": g.nt, "nshot": w.nshot, "nrec": int(w.rec.shape[1]),
             "ckpt_every": g.ckpt_every, "ckpt_format": g.ckpt_format, "order": g.order,
-            "store_levels": g.store_levels, "step_block": g.step_block,
+            "store_levels": g.store_levels, "step_block": g.step_block, "adjoint": g.adjoint,
             "kept_segments": kept_segments(g),
             "l2": "inputs larger than L2 (multi-GB state and checkpoints per step)",
             "parallelism": f"{args.gpus} GPU(s), shots batched per GPU, gradient all-reduce"}
@@ -389,7 +391,7 @@ def main():
     lib = _lib.load()
 
     w = workload(args.scale, args.nt, args.shots)
-    w.grid = dataclasses.replace(w.grid, step_block=args.step_block)
+    w.grid = dataclasses.replace(w.grid, step_block=args.step_block, adjoint=args.adjoint)
     if args.level_store_frac > 0:  # kept forward levels instead of recomputed ones
         budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
         w.grid = dataclasses.replace(w.grid, store_levels=levels_for_budget(w.grid, w.nshot, budget))

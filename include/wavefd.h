@@ -48,6 +48,16 @@ extern "C" {
 #define WFD_FIELD_I16 2  /* int16 with one FP32 scale per 32 cells along x, scale = block
                             max / 32767 (scaled_step's format) */
 
+/* How the adjoint obtains the forward levels u_k (wfd_problem.adjoint_mode). */
+#define WFD_ADJOINT_CHECKPOINT 0  /* checkpoints (and kept levels), segments recomputed */
+#define WFD_ADJOINT_RECONSTRUCT 1 /* time reversal: u_{k} = 2 u_{k+1} + m L u_{k+1} + s w_{k+1}
+                                     - u_{k+2} from the last two levels, exact where the
+                                     update is undamped; the damped frame (recon_band cells
+                                     along every edge) is restored from per-step copies the
+                                     forward saves. No checkpoints (2D, one step per launch,
+                                     FP32 fields; the reference's reconstruction_sensitivity,
+                                     projects/4_specialized_nns/analog_rnn_train.py:142) */
+
 /* What the checkpointed adjoint keeps of each recomputed step for its imaging
  * term q_{k+1} L u_k. */
 #define WFD_LAP_AUTO 0 /* 2D one-step kernel: the level u_k itself (FP32, written by the
@@ -79,6 +89,10 @@ typedef struct wfd_problem {
                               checkpoint interval, and the adjoint recomputes only
                               the others; 0 (or <= K + 2) = the last segment only */
     int32_t field_format;  /* WFD_FIELD_FP32, _FP16 or _I16 */
+    int32_t adjoint_mode;  /* WFD_ADJOINT_CHECKPOINT or WFD_ADJOINT_RECONSTRUCT */
+    int32_t recon_band;    /* WFD_ADJOINT_RECONSTRUCT: width in cells of the frame along
+                              every edge where the sponge damps (0: no sponge); the
+                              forward saves that frame of every level */
     float dt;              /* time step */
     float dz, dy, dx;      /* grid spacing (dy ignored in 2D) */
     float src_scale;       /* factor on every injected wavelet sample */

@@ -48,7 +48,7 @@ class Problem(ctypes.Structure):
         ("lap_store", ctypes.c_int32), ("shots_per_cta", ctypes.c_int32),
         ("group_shots", ctypes.c_int32), ("tile_rows", ctypes.c_int32),
         ("step_block", ctypes.c_int32), ("store_levels", ctypes.c_int32),
-        ("field_format", ctypes.c_int32),
+        ("field_format", ctypes.c_int32), ("adjoint_mode", ctypes.c_int32), ("recon_band", ctypes.c_int32),
         ("dt", ctypes.c_float), ("dz", ctypes.c_float), ("dy", ctypes.c_float),
         ("dx", ctypes.c_float), ("src_scale", ctypes.c_float), ("vmax", ctypes.c_float),
     ]

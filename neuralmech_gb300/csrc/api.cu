@@ -170,6 +170,8 @@ struct Geom {
     bool lap_bf16;           // stored L u_k in BF16 (when !ustore)
     float c0, cz[4], cy[4], cx[4];
     bool vd;                 // variable density (2D): 128 x 16 tiles, staggered operator
+    bool recon;              // the reconstruction adjoint (time reversal, saved frames)
+    int band_w, band_cl, band_cr;  // its damped frame: W rows / columns [0, cl), [cr, ld)
     float cs[4], vd_sz;      // staggered first-derivative weights, (dx/dz)^2
 };
 
@@ -230,6 +232,13 @@ int check_problem(const wfd_problem* p) {
         return fail(WFD_ERR_INVALID, "unknown field_format %d", p->field_format);
     if (p->field_format != WFD_FIELD_FP32 && (p->ndim != 2 || p->step_block == 2))
         return fail(WFD_ERR_INVALID, "reduced-precision fields: 2D, one step per launch only");
+    if (p->adjoint_mode < WFD_ADJOINT_CHECKPOINT || p->adjoint_mode > WFD_ADJOINT_RECONSTRUCT)
+        return fail(WFD_ERR_INVALID, "unknown adjoint_mode %d", p->adjoint_mode);
+    if (p->adjoint_mode == WFD_ADJOINT_RECONSTRUCT &&
+        (p->ndim != 2 || p->step_block == 2 || p->lap_store != WFD_LAP_AUTO || p->field_format != WFD_FIELD_FP32))
+        return fail(WFD_ERR_INVALID, "the reconstruction adjoint: 2D, one step per launch, lap_store auto, FP32");
+    if (p->recon_band < 0 || 2 * p->recon_band > std::min(p->nz, p->nx))
+        return fail(WFD_ERR_INVALID, "recon_band must lie in [0, min(nz, nx) / 2]");
     if (p->tile_rows != 0 && p->tile_rows != 16 && p->tile_rows != 32)
         return fail(WFD_ERR_INVALID, "tile_rows must be 0, 16 or 32");
     if (p->step_block < 0 || p->step_block > 2 || (p->step_block == 2 && p->ndim != 2))
@@ -318,6 +327,12 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0, int step_block = 0, bool
         g.jstore = std::max(0, g.nseg - (p->store_levels - 2) / g.K);
     g.k0_store = g.jstore * g.K;
     g.lap_bf16 = p->lap_store == WFD_LAP_BF16;
+    g.recon = p->adjoint_mode == WFD_ADJOINT_RECONSTRUCT;
+    if (g.recon) {
+        g.band_w = p->recon_band;
+        g.band_cl = (g.band_w + 3) / 4 * 4;
+        g.band_cr = g.band_w == 0 ? g.ld : std::max(g.band_cl, (g.nx - g.band_w) / 4 * 4);
+    }
     double a[5] = {0, 0, 0, 0, 0};
     fd_weights(p->order, a);
     const double sz = (double)p->dx * p->dx / ((double)p->dz * p->dz);
@@ -352,6 +367,7 @@ struct Layout {
     size_t field_bytes, ckpt_field_bytes, lap_field_bytes;
     size_t S[2], scale_bytes;  // reduced-precision fields: the int16 block scales
     size_t b, Gbx, Gbz;        // variable density: b = 1/rho, half-point gradient sums
+    size_t frames, frame_bytes;  // reconstruction adjoint: the damped frame of u_1 .. u_nt
     int nlap;  // slots of the lap region: K stored L u_k, or levels u_k (u store): from
                // u_{k0_store - 1} to u_nt, and at least K + 2 for a recomputed segment
 };
@@ -395,7 +411,7 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
         // per-field slots start on 256-byte boundaries (TMA bases, short4/float4 access)
         L.ckpt_field_bytes = up256(ckpt_bytes(p->ckpt_format, (long long)p->nshot * g.cells));
         L.lap_field_bytes = up256((size_t)p->nshot * g.cells * (g.lap_bf16 ? 2 : 4));
-        L.nlap = g.ustore ? std::max(g.K + 2, p->nt - g.k0_store + 2) : g.K;
+        L.nlap = g.recon ? 0 : g.ustore ? std::max(g.K + 2, p->nt - g.k0_store + 2) : g.K;
         for (int b = 0; b < 2; ++b) L.Q[b] = take(L.field_bytes);  // (the adjoint is one-step)
         L.G = take((size_t)g.cells * 4);
         if (g.vd) {
@@ -403,7 +419,11 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
             L.Gbz = take((size_t)g.cells * 4);
         }
         // (segments whose levels the forward keeps need no checkpoint)
-        L.ckpt = take((size_t)(g.ustore ? g.jstore : g.nseg) * 2 * L.ckpt_field_bytes);
+        L.ckpt = take(g.recon ? 0 : (size_t)(g.ustore ? g.jstore : g.nseg) * 2 * L.ckpt_field_bytes);
+        if (g.recon) {
+            L.frame_bytes = up256((size_t)band_cells(g.nz, g.ld, g.band_w, g.band_cl, g.band_cr) * p->nshot * 4);
+            L.frames = take((size_t)(p->nt + 1) * L.frame_bytes);
+        }
         L.lap = take((size_t)L.nlap * L.lap_field_bytes);
         L.res = take((size_t)p->nshot * p->nt * p->nrec * 4 + 4);
     }
@@ -418,6 +438,7 @@ struct Work {
     float *b, *Gbx, *Gbz;  // variable density (workspace)
     const float* rho;      // variable density: the caller's rho, for setup and the gradient
     float* grad_rho;       // variable density: dJ/drho output
+    unsigned char* frames; // reconstruction adjoint: frame n at frames + n frame_bytes
     int* counts;
     PointLists src, rec, src_e;
     PointLists src_a, rec_a;  // lists of the adjoint geometry (== src, rec unless u store)
@@ -463,6 +484,7 @@ Work carve(void* ws, const Layout& L, bool grad) {
         for (int k = 0; k < 2; ++k) w.Q[k] = reinterpret_cast<float*>(b + L.Q[k]);
         w.G = reinterpret_cast<float*>(b + L.G);
         w.ckpt = b + L.ckpt;
+        if (L.frames) w.frames = b + L.frames;
         w.lap = b + L.lap;
         w.res = reinterpret_cast<float*>(b + L.res);
     }
@@ -688,7 +710,8 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
         return run_forward_lp(p, g, L, w, st, wavelet, traces, final_buf);
     }
     cudaStream_t s = st.s;
-    const bool us = save && g.ustore;
+    const bool rc_mode = save && g.recon;  // reconstruction adjoint: frames, no checkpoints or slots
+    const bool us = save && g.ustore && !rc_mode;
     const int np = L.nbuf;
     const int nslot = us ? L.nlap : 0;
     auto loc = [&](int k) -> int {
@@ -710,7 +733,7 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
             return rc;
     const long long n_all = (long long)p->nshot * g.cells;
     auto checkpoint = [&](int n) -> int {  // (u_{n-1}, u_n) at the start of segment n / K
-        if (!save || n % g.K != 0 || (us && n >= g.k0_store)) return WFD_OK;  // (kept segments need none)
+        if (!save || rc_mode || n % g.K != 0 || (us && n >= g.k0_store)) return WFD_OK;  // (kept segments need none)
         unsigned char* slot = w.ckpt + (size_t)(n / g.K) * 2 * L.ckpt_field_bytes;
         WFD_CUDA(launch_pack(buf[loc(n - 1)], slot, n_all, p->ckpt_format, s));
         WFD_CUDA(launch_pack(buf[loc(n)], slot + L.ckpt_field_bytes, n_all, p->ckpt_format, s));
@@ -771,6 +794,9 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
             a.lap_bf16 = g.lap_bf16;
         }
         if ((rc = st.launch(lap ? MODE_SAVE_LAP : MODE_PLAIN, mc[bc], mo[bo], mc[bc], a))) return rc;
+        if (rc_mode)  // the damped frame of u_{n+1} (sources included: after the launch)
+            WFD_CUDA(launch_band(buf[bn], reinterpret_cast<float*>(w.frames + (size_t)(n + 1) * L.frame_bytes),
+                                 g.cells, p->nshot, g.nz, g.ld, g.band_w, g.band_cl, g.band_cr, true, s));
         ++n;
     }
     if (traces && p->nrec > 0)
@@ -966,11 +992,101 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
     return WFD_OK;
 }
 
+// Adjoint by time reversal (WFD_ADJOINT_RECONSTRUCT, 2D one step per launch).
+// The forward leaves u_{nt-1}, u_nt in P[(nt-1) & 1], P[nt & 1] and the damped
+// frame of every level in w.frames. Going back, u_k comes from inverting the
+// forward step k + 1 where it is undamped,
+//     u_k = 2 u_{k+1} + m L u_{k+1} + s w_{k+1} - u_{k+2}
+// (the step kernel without sponge factors, in place of u_{k+2}), and the frame
+// is restored from its copy; the adjoint step k then stages u_k as in the
+// u-store adjoint. No checkpoints, no recomputed segments.
+int run_backward_recon(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w, const Stepper& st,
+                       const float* wavelet, const float* dtraces, float* grad_vel, float* grad_wavelet,
+                       const float* vel) {
+    cudaStream_t s = st.s;
+    const Geom ga = adjoint_geom(p, g);
+    Stepper sa = st;
+    sa.g = ga;
+    Stepper rv = st;  // the reversal: no sponge factors
+    rv.gz = rv.gy = rv.gx = nullptr;
+    WFD_CUDA(cudaMemsetAsync(w.Q[0], 0, L.field_bytes, s));
+    WFD_CUDA(cudaMemsetAsync(w.Q[1], 0, L.field_bytes, s));
+    WFD_CUDA(cudaMemsetAsync(w.G, 0, (size_t)g.cells * 4, s));
+    if (g.vd) {
+        WFD_CUDA(cudaMemsetAsync(w.Gbx, 0, (size_t)g.cells * 4, s));
+        WFD_CUDA(cudaMemsetAsync(w.Gbz, 0, (size_t)g.cells * 4, s));
+    }
+    int rc;
+    CUtensorMap qc[2], qo[2], pc[2], po[2], pa[2], unused[2];
+    for (int b = 0; b < 2; ++b) {
+        if ((rc = sa.map_pair(w.Q[b], w.Q[b], &qc[b], &qo[b]))) return rc;
+        if ((rc = rv.map_pair(w.P[b], w.P[b], &pc[b], &po[b]))) return rc;
+        if ((rc = sa.map_pair(w.P[b], w.P[b], &pa[b], &unused[b]))) return rc;
+    }
+    auto adjoint_step = [&](int k, bool grad) -> int {  // q_k from (q_{k+1}, q_{k+2}); u_k in P[k & 1]
+        const int bc = (k + 1) & 1, bn = k & 1;
+        StepArgs a = sa.base(w.Q[bn]);
+        if (p->nrec > 0) {
+            a.inj = w.rec_a;
+            a.inj_val = dtraces;
+            a.inj_np = p->nrec; a.inj_nt = p->nt; a.inj_t = k - 1;
+            a.inj_scale = 1.f;
+            a.inj_times_m = 1;
+        }
+        if (grad_wavelet && k <= p->nt - 1 && p->nsrc > 0) {
+            a.smp = w.src_a;
+            a.smp_out = grad_wavelet;
+            a.smp_np = p->nsrc; a.smp_nt = p->nt; a.smp_t = k;
+            a.smp_scale = p->src_scale;
+            a.smp_div_m = 1;
+        }
+        if (!grad) return sa.launch(MODE_PLAIN, qc[bc], qo[bn], qc[bc], a);
+        a.grad = w.G;
+        a.grad_bx = w.Gbx;
+        a.grad_bz = w.Gbz;
+        return sa.launch(MODE_GRAD_U, qc[bc], qo[bn], pa[k & 1], a);
+    };
+    {
+        PhaseScope scope(PH_ADJOINT, s, 1);
+        if ((rc = adjoint_step(p->nt, false))) return rc;
+    }
+    PhaseScope scope(PH_ADJOINT, s, 2 * (p->nt - 1));
+    for (int k = p->nt - 1; k >= 1; --k) {
+        if (k < p->nt - 1) {  // u_k into P[k & 1] (which holds u_{k+2})
+            StepArgs a = rv.base(w.P[k & 1]);
+            if (p->nsrc > 0) {
+                a.inj = w.src;
+                a.inj_val = wavelet;
+                a.inj_np = p->nsrc; a.inj_nt = p->nt; a.inj_t = k + 1;
+                a.inj_scale = p->src_scale;
+            }
+            if ((rc = rv.launch(MODE_PLAIN, pc[(k + 1) & 1], po[k & 1], pc[(k + 1) & 1], a))) return rc;
+            WFD_CUDA(launch_band(w.P[k & 1], reinterpret_cast<float*>(w.frames + (size_t)k * L.frame_bytes), g.cells,
+                                 p->nshot, g.nz, g.ld, g.band_w, g.band_cl, g.band_cr, false, s));
+        }
+        if ((rc = adjoint_step(k, true))) return rc;
+    }
+    if (grad_wavelet && p->nsrc > 0)  // q_1 at the sources -> d J / d w_0
+        WFD_CUDA(launch_gather(w.Q[1], ga.cells, w.src_a, ga.ntiles, p->nshot, p->nsrc, w.m, p->src_scale, 1,
+                               grad_wavelet, p->nt, 0, s));
+    if (g.vd)
+        WFD_CUDA(launch_vd_finalize(w.G, w.Gbx, w.Gbz, w.m, w.rho, grad_vel, w.grad_rho, g.nz, g.nx, g.ld, g.R,
+                                    float((double)p->dt * p->dt / ((double)p->dx * p->dx)), s));
+    else
+        WFD_CUDA(launch_grad_finalize(w.G, vel, grad_vel, g.nz, g.ny, g.nx, g.ld, g.R, s));
+    return WFD_OK;
+}
+
 // Adjoint of one (group of) shots. zero_G starts a new gradient sum; finalize
 // turns the sum into dJ/dv (the last group of a grouped call).
 int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                  const Stepper& st, const float* wavelet, const float* dtraces, float* grad_vel,
                  float* grad_wavelet, const float* vel, bool zero_G = true, bool finalize = true) {
+    if (g.recon) {
+        if (!zero_G || !finalize)
+            return fail(WFD_ERR_INVALID, "the reconstruction adjoint does not run in shot groups");
+        return run_backward_recon(p, g, L, w, st, wavelet, dtraces, grad_vel, grad_wavelet, vel);
+    }
     if (g.ustore)
         return run_backward_ustore(p, g, L, w, st, wavelet, dtraces, grad_vel, grad_wavelet, vel,
                                    zero_G, finalize);

@@ -2,6 +2,8 @@
 // lists, gathers, checkpoint packing, FP64 misfit / norm reductions.
 // All are launched once per call (or once per checkpoint), not per cell-step,
 // except the checkpoint pack which runs every ckpt_every steps.
+#include <algorithm>
+
 #include "common.cuh"
 #include "internal.h"
 
@@ -233,6 +235,55 @@ int grid_for(long long n, int block = 256) {
 cudaError_t launch_vel_to_m(const float* vel, float* m, int nz, int ny, int nx, int ld,
                             float scale, cudaStream_t s) {
     vel_to_m_kernel<<<grid_for((long long)nz * ny * ld), 256, 0, s>>>(vel, m, nz, ny, nx, ld, scale);
+    count_launch();
+    return cudaGetLastError();
+}
+
+namespace {
+
+// Copies the damped frame of nshot fields [z][ld] to (save) or from a compact
+// store: rows [0, W) and [nz - W, nz) in full, the other rows' columns
+// [0, cl) and [cr, ld).
+__global__ void band_kernel(float* field, float* store, long long shot_stride, int nshot, int nz, int ld, int W,
+                            int cl, int cr, int save) {
+    const long long rows = 2LL * W * ld, side = (long long)(cl + ld - cr);
+    const long long B = rows + (long long)(nz - 2 * W) * side;
+    const long long n = B * nshot;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long s = i / B;
+        long long j = i - s * B;
+        int z, x;
+        if (j < rows) {
+            const int r = int(j / ld);
+            x = int(j - (long long)r * ld);
+            z = r < W ? r : nz - 2 * W + r;
+        } else {
+            j -= rows;
+            const int r = int(j / side), c = int(j - (long long)r * side);
+            z = W + r;
+            x = c < cl ? c : cr + (c - cl);
+        }
+        float* f = field + s * shot_stride + (long long)z * ld + x;
+        if (save)
+            store[i] = *f;
+        else
+            *f = store[i];
+    }
+}
+
+}  // namespace
+
+long long band_cells(int nz, int ld, int W, int cl, int cr) {
+    return 2LL * W * ld + (long long)(nz - 2 * W) * (cl + ld - cr);
+}
+
+cudaError_t launch_band(float* field, float* store, long long shot_stride, int nshot, int nz, int ld, int W,
+                        int cl, int cr, bool save, cudaStream_t s) {
+    const long long n = band_cells(nz, ld, W, cl, cr) * nshot;
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+    band_kernel<<<blocks, 256, 0, s>>>(field, store, shot_stride, nshot, nz, ld, W, cl, cr, save ? 1 : 0);
     count_launch();
     return cudaGetLastError();
 }

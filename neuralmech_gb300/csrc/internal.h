@@ -193,6 +193,12 @@ cudaError_t launch_build_lists(const int32_t* pos, int nshot, int np, int nz, in
                                int ld, int R, int tile_z, int tile_y, int tile_x, int tiles_z,
                                int tiles_y, int tiles_x, int* counts, int* off, int2* ent,
                                unsigned* err, cudaStream_t s, int halo_z = 0, int halo_x = 0);
+// The damped frame of fields [z][ld]: rows [0, W), [nz - W, nz), and columns
+// [0, cl), [cr, ld) of the other rows, saved to / restored from a compact store
+// (band_cells per shot, shots contiguous).
+long long band_cells(int nz, int ld, int W, int cl, int cr);
+cudaError_t launch_band(float* field, float* store, long long shot_stride, int nshot, int nz, int ld, int W,
+                        int cl, int cr, bool save, cudaStream_t s);
 cudaError_t launch_gather(const float* u, long long shot_stride, PointLists lists, int ntiles,
                           int nshot, int np, const float* m, float scale, int div_m,
                           float* out, int out_nt, int out_t, cudaStream_t s);

@@ -37,6 +37,7 @@ from . import _lib
 CKPT_FORMATS = {"fp32": 0, "bf16": 1, "i16": 2}
 LAP_STORES = {"auto": 0, "bf16": 1, "fp32": 2}
 FIELD_FORMATS = {"fp32": 0, "fp16": 1, "i16": 2}
+ADJOINT_MODES = {"checkpoint": 0, "reconstruct": 1}
 
 
 @dataclass(frozen=True)
@@ -71,6 +72,10 @@ class Grid:
     field_format storage of the wavefields in a forward without gradient (2D):
              "fp32", "fp16" or "i16" (int16 with one FP32 scale per 32 cells
              along x); arithmetic is FP32 in every format
+    adjoint      how the gradient obtains the forward levels (2D): "checkpoint"
+             (checkpoints, kept levels, recomputed segments) or "reconstruct"
+             (time reversal from the last two levels; the sponge frame of every
+             level is saved by the forward instead of checkpoints)
     """
     shape: tuple
     spacing: tuple
@@ -89,6 +94,7 @@ class Grid:
     step_block: int = 0
     store_levels: int = 0
     field_format: str = "fp32"
+    adjoint: str = "checkpoint"
 
     @property
     def ndim(self) -> int:
@@ -167,7 +173,9 @@ def _problem(grid: Grid, nshot: int, nsrc: int, nrec: int, vmax: float) -> _lib.
     return _lib.Problem(grid.ndim, grid.order, nz, ny, nx, nshot, grid.nt, nsrc, nrec,
                         grid.ckpt_every, CKPT_FORMATS[grid.ckpt_format], LAP_STORES[grid.lap_store],
                         grid.shots_per_cta, grid.group_shots, grid.tile_rows, grid.step_block, grid.store_levels,
-                        FIELD_FORMATS[grid.field_format], grid.dt, dz, dy, dx, grid.src_scale, vmax)
+                        FIELD_FORMATS[grid.field_format], ADJOINT_MODES[grid.adjoint],
+                        max(max(w) for w in grid.sponge_widths()) if grid.adjoint == "reconstruct" else 0,
+                        grid.dt, dz, dy, dx, grid.src_scale, vmax)
 
 
 # ---------------------------------------------------------------- argument prep

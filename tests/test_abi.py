@@ -93,7 +93,9 @@ def test_workspace_holds_the_kept_levels():
     (dict(nshot=0), -1), (dict(nt=0), -1), (dict(dt=0.0), -1), (dict(dx=-1.0), -1),
     (dict(ckpt_format=3), -1), (dict(ckpt_every=-1), -1), (dict(lap_store=3), -1),
     (dict(store_levels=-1), -1), (dict(field_format=3), -1), (dict(field_format=1, ndim=3, ny=64), -1),
-    (dict(field_format=2, step_block=2), -1), (dict(vmax=1e6), -4),
+    (dict(field_format=2, step_block=2), -1), (dict(adjoint_mode=2), -1),
+    (dict(adjoint_mode=1, step_block=2), -1), (dict(adjoint_mode=1, recon_band=40), -1),
+    (dict(vmax=1e6), -4),
 ])
 def test_invalid_problems_rejected(bad, code):
     from neuralmech_gb300 import _lib
@@ -170,3 +172,15 @@ def test_reduced_precision_fields_halve_the_forward_workspace():
     assert f16 < i16 < f32
     rc, _ = _ws(_problem(field_format=1), 1)  # no gradient workspace: forward-only
     assert rc == -1
+
+
+def test_reconstruction_workspace_keeps_frames_not_checkpoints():
+    """adjoint_mode reconstruct: no checkpoints or level slots; the damped
+    frame (recon_band cells along every edge) of every level instead."""
+    _, ck = _ws(_problem(nt=100, ckpt_every=10, ckpt_format=0))
+    _, r0 = _ws(_problem(nt=100, adjoint_mode=1, recon_band=0))
+    _, r6 = _ws(_problem(nt=100, adjoint_mode=1, recon_band=6))
+    assert r0 < ck and r0 < r6
+    # frame of one shot: 2 * 6 full rows of ld = 104 and 52 rows of 8 + (104 - 92) columns
+    frame = 2 * (2 * 6 * 104 + (64 - 12) * (8 + 104 - 92)) * 4
+    assert r6 - r0 == 101 * ((frame + 255) // 256 * 256)

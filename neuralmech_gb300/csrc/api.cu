@@ -222,6 +222,9 @@ int check_problem(const wfd_problem* p) {
         return fail(WFD_ERR_INVALID, "nshot, nt must be >= 1 and nsrc, nrec >= 0");
     if (p->nshot > 65535 || (p->ndim == 2 && p->nshot > 65535 * T2_MAX_SPC))
         return fail(WFD_ERR_INVALID, "too many shots");
+    if (p->ndim == 3 && (long long)cdiv(p->nz, T3_ZCHUNK) * cdiv(p->ny, T3_TY) * cdiv(p->nx, T3_TX) > 65535)
+        return fail(WFD_ERR_INVALID, "3D grid has more than 65535 (%d x %d x %d)-cell columns", T3_ZCHUNK,
+                    T3_TY, T3_TX);
     if (!(p->dt > 0) || !(p->dx > 0) || !(p->dz > 0) || (p->ndim == 3 && !(p->dy > 0)))
         return fail(WFD_ERR_INVALID, "dt and spacings must be positive");
     if (p->ckpt_format < WFD_CKPT_FP32 || p->ckpt_format > WFD_CKPT_I16)

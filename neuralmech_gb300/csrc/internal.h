@@ -58,8 +58,8 @@ struct StepArgs {
     int tiles_x, tiles_y, tiles_z;
     float c0;                  // centre weight (all axes)
     float cz[4], cy[4], cx[4]; // axis weights for k = 1..R, already scaled by (dx/h)^2
-    float2 c0p, czp[4], cxp[4]; // 2D: the same as duplicated pairs, operands of the packed
-                                // FP32x2 arithmetic (set by the 2D launchers)
+    float2 c0p, czp[4], cyp[4], cxp[4]; // the same as duplicated pairs, operands of the
+                                        // packed FP32x2 arithmetic (set by the launchers)
     // injection into u_new: u += g * scale * val (* m at the cell when inj_times_m)
     PointLists inj;
     const float* inj_val;      // [nshot][inj_nt][inj_np]
@@ -167,6 +167,7 @@ constexpr int T3_XH = 4;
 constexpr int T3_W = T3_TX + 2 * T3_XH;
 constexpr int T3_THREADS = (T3_TX / 4) * T3_TY;  // 256
 constexpr int T3_ZCHUNK = 64;                    // planes per CTA (z blocking)
+constexpr int T3_UNROLL = 1;                     // output planes per turn of the z-tap queue
 
 // map_cur: u_n planes (box T3_W x (T3_TY + 2R) x 1 x 1); map_old, map_lap:
 // output-plane tiles (box T3_TX x T3_TY x 1 x 1); map_m: the model m

@@ -6,6 +6,9 @@
 //
 // Per CTA (256 threads = 16 lanes along x x 16 rows along y): one shot, one
 // 64 x 16 (x, y) column, marching along z through T3_ZCHUNK output planes.
+// The shot is the fastest grid index: the CTAs of all shots of one column run
+// together, so m and (MODE_GRAD) the gradient tile are read from DRAM once
+// per column and served from L2 to the other shots.
 //   * u_n planes, each with a halo of R rows in y and 4 columns in x, arrive by
 //     TMA (cp.async.bulk.tensor.4d) into a ring of NB = 8 shared-memory
 //     buffers, four planes ahead of use. A thread keeps the 2R + 1 z-taps of
@@ -41,9 +44,8 @@ struct Layout3D {
     static constexpr int BYTES = NB * CUR_AL + NBO * OLD_GROUP + (NB + NBO) * 8 + 128;
 };
 
-__device__ __forceinline__ float comp(const float4& v, int e) {
-    return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
-}
+__device__ __forceinline__ float2 lo2(const float4& v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4& v) { return make_float2(v.z, v.w); }
 
 template <int R, int MODE>
 __global__ void __launch_bounds__(T3_THREADS, 2)
@@ -52,6 +54,8 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
                   const __grid_constant__ CUtensorMap map_lap,
                   const __grid_constant__ CUtensorMap map_m, const StepArgs a) {
     using L = Layout3D<R, MODE>;
+    constexpr int U = T3_UNROLL;  // output planes per turn of the register queue
+    constexpr int Q = 2 * R + U;  // register queue of staged planes
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
@@ -61,8 +65,8 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
     uint64_t* bo = bc + NB;
 
     const int tid = threadIdx.x, lane = tid % LANES_X, row = tid / LANES_X;
-    const int tile = blockIdx.x;
-    const int s = blockIdx.y;
+    const int s = blockIdx.x;
+    const int tile = blockIdx.y;
     const int ntiles = a.tiles_x * a.tiles_y * a.tiles_z;
     const int tx_i = tile % a.tiles_x;
     const int ty_i = (tile / a.tiles_x) % a.tiles_y;
@@ -116,12 +120,16 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
     float* un = a.u_new + (long long)s * a.shot_stride;
     const int col = T3_XH + 4 * lane;  // staged column of this thread's first cell
 
-    // ---- register queue of the z taps: V[j] = u_n at z = zout - R + j
-    float4 V[2 * R + 1];
+    // ---- register queue of the z taps. The plane loop is unrolled U times:
+    // at the start of a group of U output planes zr0 .. zr0 + U - 1, V[j]
+    // holds staged plane zr0 + j (j < 2R); output plane zr0 + u loads plane
+    // zr0 + 2R + u into V[2R + u] and takes its z taps from V[u .. u + 2R];
+    // after the group the queue moves down by U.
+    float4 V[Q];
 #pragma unroll
     for (int p = 0; p < 2 * R; ++p) {
         if (!mbar_wait(&bc[p % NB], (p / NB) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
-        V[p + 1] = *reinterpret_cast<const float4*>(cur_buf(p) + (row + R) * T3_W + col);
+        V[p] = *reinterpret_cast<const float4*>(cur_buf(p) + (row + R) * T3_W + col);
     }
     __syncthreads();  // planes 0 .. R-1 are consumed
     if (tid == 0) {
@@ -134,117 +142,136 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
     const int lo_i = a.inj.off ? a.inj.off[s * ntiles + tile] : 0;
     const int hi_i = a.inj.off ? a.inj.off[s * ntiles + tile + 1] : 0;
 
-    for (int zr = 0; zr < zc; ++zr) {
-        const int z = z0 + zr;
-        const int pn = zr + 2 * R;  // newest staged plane needed
-        if (!mbar_wait(&bc[pn % NB], (pn / NB) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
+    for (int zr0 = 0; zr0 < zc; zr0 += U) {
 #pragma unroll
-        for (int j = 0; j < 2 * R; ++j) V[j] = V[j + 1];
-        V[2 * R] = *reinterpret_cast<const float4*>(cur_buf(pn) + (row + R) * T3_W + col);
-        if (!mbar_wait(&bo[zr % NBO], (zr / NBO) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
+        for (int u = 0; u < U; ++u) {
+            const int zr = zr0 + u;
+            if (zr >= zc) break;
+            const int z = z0 + zr;
+            const int pn = zr + 2 * R;  // newest staged plane needed
+            if (!mbar_wait(&bc[pn % NB], (pn / NB) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
+            V[u + 2 * R] = *reinterpret_cast<const float4*>(cur_buf(pn) + (row + R) * T3_W + col);
+            if (!mbar_wait(&bo[zr % NBO], (zr / NBO) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
 
-        const float* pl = cur_buf(zr + R);  // u_n at the output plane, with halo
-        const float* prow = pl + (row + R) * T3_W + 4 * lane;
-        const float4 lv = *reinterpret_cast<const float4*>(prow);
-        const float4 cv = V[R];
-        const float4 rv = *reinterpret_cast<const float4*>(prow + 2 * T3_XH);
-        const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y, cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
-        float4 ym[R], yp[R];
-#pragma unroll
-        for (int k = 1; k <= R; ++k) {
-            ym[k - 1] = *reinterpret_cast<const float4*>(pl + (row + R - k) * T3_W + col);
-            yp[k - 1] = *reinterpret_cast<const float4*>(pl + (row + R + k) * T3_W + col);
-        }
-        const int ti = row * T3_TX + 4 * lane;
-        const float4 ov = *reinterpret_cast<const float4*>(old_buf(zr) + ti);
-        const float4 mv = *reinterpret_cast<const float4*>(m_buf(zr) + ti);
-        const float gz = (a.gz != nullptr && z < a.nz) ? __ldg(a.gz + z) : 1.f;
-        float lap[4], nv[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            float acc = a.c0 * w[4 + e];
+            const float* pl = cur_buf(zr + R);  // u_n at the output plane, with halo
+            const float* prow = pl + (row + R) * T3_W + 4 * lane;
+            const float4 lv = *reinterpret_cast<const float4*>(prow);
+            const float4 cv = V[u + R];
+            const float4 rv = *reinterpret_cast<const float4*>(prow + 2 * T3_XH);
+            const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y, cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
+            // L u in packed pairs: c0 u + sum_k cx_k (x taps) + cy_k (y taps) + cz_k (z taps)
+            float2 lo = __fmul2_rn(a.c0p, lo2(cv));
+            float2 hi = __fmul2_rn(a.c0p, hi2(cv));
 #pragma unroll
             for (int k = 1; k <= R; ++k) {
-                acc = fmaf(a.cx[k - 1], w[4 + e - k] + w[4 + e + k], acc);
-                acc = fmaf(a.cy[k - 1], comp(ym[k - 1], e) + comp(yp[k - 1], e), acc);
-                acc = fmaf(a.cz[k - 1], comp(V[R - k], e) + comp(V[R + k], e), acc);
+                float2 xl, xh;
+                if (k % 2 == 0) {  // the x taps form aligned register pairs
+                    xl = __fadd2_rn(make_float2(w[4 - k], w[5 - k]), make_float2(w[4 + k], w[5 + k]));
+                    xh = __fadd2_rn(make_float2(w[6 - k], w[7 - k]), make_float2(w[6 + k], w[7 + k]));
+                } else {
+                    xl = make_float2(w[4 - k] + w[4 + k], w[5 - k] + w[5 + k]);
+                    xh = make_float2(w[6 - k] + w[6 + k], w[7 - k] + w[7 + k]);
+                }
+                lo = __ffma2_rn(a.cxp[k - 1], xl, lo);
+                hi = __ffma2_rn(a.cxp[k - 1], xh, hi);
+                const float4 ym = *reinterpret_cast<const float4*>(pl + (row + R - k) * T3_W + col);
+                const float4 yp = *reinterpret_cast<const float4*>(pl + (row + R + k) * T3_W + col);
+                lo = __ffma2_rn(a.cyp[k - 1], __fadd2_rn(lo2(ym), lo2(yp)), lo);
+                hi = __ffma2_rn(a.cyp[k - 1], __fadd2_rn(hi2(ym), hi2(yp)), hi);
+                const float4 zm = V[u + R - k], zp = V[u + R + k];
+                lo = __ffma2_rn(a.czp[k - 1], __fadd2_rn(lo2(zm), lo2(zp)), lo);
+                hi = __ffma2_rn(a.czp[k - 1], __fadd2_rn(hi2(zm), hi2(zp)), hi);
             }
-            lap[e] = acc;
-            const float g = gz * gyv * gxe[e];
-            nv[e] = g * fmaf(comp(mv, e), acc, 2.f * w[4 + e]) - (g * g) * comp(ov, e);
-        }
-        const bool rin = yin && z >= R && z < a.nz - R;
-        const long long off = (long long)z * a.plane + (long long)y * a.ld + x;
-        if (rin && all_x) {
-            *reinterpret_cast<float4*>(un + off) = make_float4(nv[0], nv[1], nv[2], nv[3]);
-        } else if (rin) {
-#pragma unroll
-            for (int e = 0; e < 4; ++e)
-                if (xin[e]) un[off + e] = nv[e];
-        }
-        if (MODE == MODE_SAVE_LAP && rin) {
-            const long long lo = (long long)s * a.shot_stride + off;
-            const float4 lp = make_float4(lap[0], lap[1], lap[2], lap[3]);
-            if (all_x) {
-                if (a.lap_bf16)
-                    *reinterpret_cast<uint2*>(static_cast<__nv_bfloat16*>(a.lap) + lo) = pack_bf16x4(lp);
-                else
-                    *reinterpret_cast<float4*>(static_cast<float*>(a.lap) + lo) = lp;
-            } else {
-#pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    if (xin[e]) {
-                        if (a.lap_bf16)
-                            static_cast<__nv_bfloat16*>(a.lap)[lo + e] = __float2bfloat16_rn(lap[e]);
-                        else
-                            static_cast<float*>(a.lap)[lo + e] = lap[e];
-                    }
-            }
-        }
-        if (MODE == MODE_GRAD && rin) {
-            const unsigned char* lb = lap_buf(zr);
-            const float4 lu = a.lap_bf16
-                                  ? unpack_bf16x4(*reinterpret_cast<const uint2*>(
-                                        reinterpret_cast<const __nv_bfloat16*>(lb) + ti))
-                                  : *reinterpret_cast<const float4*>(reinterpret_cast<const float*>(lb) + ti);
-            float* gp = a.grad + off;
-            if (all_x) {
-                atomicAdd(reinterpret_cast<float4*>(gp),
-                          make_float4(cv.x * lu.x, cv.y * lu.y, cv.z * lu.z, cv.w * lu.w));
-            } else {
+            const int ti = row * T3_TX + 4 * lane;
+            const float4 ov = *reinterpret_cast<const float4*>(old_buf(zr) + ti);
+            const float4 mv = *reinterpret_cast<const float4*>(m_buf(zr) + ti);
+            const float gz = (a.gz != nullptr && z < a.nz) ? __ldg(a.gz + z) : 1.f;
+            // u_{n+1} = g (m L u + 2 u) - g^2 u_{n-1}
+            const float gyz = gz * gyv;
+            const float2 gl = __fmul2_rn(make_float2(gyz, gyz), make_float2(gxe[0], gxe[1]));
+            const float2 gh = __fmul2_rn(make_float2(gyz, gyz), make_float2(gxe[2], gxe[3]));
+            const float2 tl = __ffma2_rn(lo2(mv), lo, __fadd2_rn(lo2(cv), lo2(cv)));
+            const float2 th = __ffma2_rn(hi2(mv), hi, __fadd2_rn(hi2(cv), hi2(cv)));
+            const float2 nl = __ffma2_rn(gl, tl, __fmul2_rn(__fmul2_rn(gl, gl), make_float2(-ov.x, -ov.y)));
+            const float2 nh = __ffma2_rn(gh, th, __fmul2_rn(__fmul2_rn(gh, gh), make_float2(-ov.z, -ov.w)));
+            const float nv[4] = {nl.x, nl.y, nh.x, nh.y};
+            const float lap[4] = {lo.x, lo.y, hi.x, hi.y};
+
+            const bool rin = yin && z >= R && z < a.nz - R;
+            const long long off = (long long)z * a.plane + (long long)y * a.ld + x;
+            if (rin && all_x) {
+                *reinterpret_cast<float4*>(un + off) = make_float4(nv[0], nv[1], nv[2], nv[3]);
+            } else if (rin) {
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
-                    if (xin[e]) atomicAdd(gp + e, comp(cv, e) * comp(lu, e));
+                    if (xin[e]) un[off + e] = nv[e];
+            }
+            if (MODE == MODE_SAVE_LAP && rin) {
+                const long long lo_i64 = (long long)s * a.shot_stride + off;
+                const float4 lp = make_float4(lap[0], lap[1], lap[2], lap[3]);
+                if (all_x) {
+                    if (a.lap_bf16)
+                        *reinterpret_cast<uint2*>(static_cast<__nv_bfloat16*>(a.lap) + lo_i64) = pack_bf16x4(lp);
+                    else
+                        *reinterpret_cast<float4*>(static_cast<float*>(a.lap) + lo_i64) = lp;
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        if (xin[e]) {
+                            if (a.lap_bf16)
+                                static_cast<__nv_bfloat16*>(a.lap)[lo_i64 + e] = __float2bfloat16_rn(lap[e]);
+                            else
+                                static_cast<float*>(a.lap)[lo_i64 + e] = lap[e];
+                        }
+                }
+            }
+            if (MODE == MODE_GRAD && rin) {
+                const unsigned char* lb = lap_buf(zr);
+                const float4 lu = a.lap_bf16
+                                      ? unpack_bf16x4(*reinterpret_cast<const uint2*>(
+                                            reinterpret_cast<const __nv_bfloat16*>(lb) + ti))
+                                      : *reinterpret_cast<const float4*>(reinterpret_cast<const float*>(lb) + ti);
+                float* gp = a.grad + off;
+                if (all_x) {
+                    const float2 pl2 = __fmul2_rn(lo2(cv), lo2(lu)), ph2 = __fmul2_rn(hi2(cv), hi2(lu));
+                    atomicAdd(reinterpret_cast<float4*>(gp), make_float4(pl2.x, pl2.y, ph2.x, ph2.y));
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        if (xin[e]) atomicAdd(gp + e, comp(cv, e) * comp(lu, e));
+                }
+            }
+            // sampling of u_n at this plane
+            for (int j = lo_s + tid; j < hi_s; j += T3_THREADS) {
+                const int2 en = a.smp.ent[j];
+                const int pz = en.x / int(a.plane);
+                if (pz != z) continue;
+                const int rem = en.x - pz * int(a.plane);
+                const int py = rem / a.ld, px = rem - py * a.ld;
+                float v = pl[(py - y0 + R) * T3_W + (px - x0 + T3_XH)] * a.smp_scale;
+                if (a.smp_div_m) v /= a.m[en.x];
+                a.smp_out[((long long)s * a.smp_nt + a.smp_t) * a.smp_np + en.y] = v;
+            }
+            __syncthreads();  // plane zr + R and old group zr fully read; stores of plane z done
+            if (tid == 0) {
+                fence_proxy_async_smem();
+                if (zr + NB + R < total) issue_cur(zr + NB + R);
+                if (zr + NBO < zc) issue_old(zr + NBO);
+            }
+            for (int j = lo_i + tid; j < hi_i; j += T3_THREADS) {
+                const int2 en = a.inj.ent[j];
+                const int pz = en.x / int(a.plane);
+                if (pz != z) continue;
+                const int rem = en.x - pz * int(a.plane);
+                const int py = rem / a.ld, px = rem - py * a.ld;
+                float v = a.inj_val[((long long)s * a.inj_nt + a.inj_t) * a.inj_np + en.y] * a.inj_scale;
+                if (a.inj_times_m) v *= a.m[en.x];
+                const float g = (a.gz ? a.gz[pz] : 1.f) * (a.gy ? a.gy[py] : 1.f) * (a.gx ? a.gx[px] : 1.f);
+                atomicAdd(un + en.x, g * v);
             }
         }
-        // sampling of u_n at this plane
-        for (int j = lo_s + tid; j < hi_s; j += T3_THREADS) {
-            const int2 en = a.smp.ent[j];
-            const int pz = en.x / int(a.plane);
-            if (pz != z) continue;
-            const int rem = en.x - pz * int(a.plane);
-            const int py = rem / a.ld, px = rem - py * a.ld;
-            float v = pl[(py - y0 + R) * T3_W + (px - x0 + T3_XH)] * a.smp_scale;
-            if (a.smp_div_m) v /= a.m[en.x];
-            a.smp_out[((long long)s * a.smp_nt + a.smp_t) * a.smp_np + en.y] = v;
-        }
-        __syncthreads();  // plane zr + R and old group zr fully read; stores of plane z done
-        if (tid == 0) {
-            fence_proxy_async_smem();
-            if (zr + NB + R < total) issue_cur(zr + NB + R);
-            if (zr + NBO < zc) issue_old(zr + NBO);
-        }
-        for (int j = lo_i + tid; j < hi_i; j += T3_THREADS) {
-            const int2 en = a.inj.ent[j];
-            const int pz = en.x / int(a.plane);
-            if (pz != z) continue;
-            const int rem = en.x - pz * int(a.plane);
-            const int py = rem / a.ld, px = rem - py * a.ld;
-            float v = a.inj_val[((long long)s * a.inj_nt + a.inj_t) * a.inj_np + en.y] * a.inj_scale;
-            if (a.inj_times_m) v *= a.m[en.x];
-            const float g = (a.gz ? a.gz[pz] : 1.f) * (a.gy ? a.gy[py] : 1.f) * (a.gx ? a.gx[px] : 1.f);
-            atomicAdd(un + en.x, g * v);
-        }
+#pragma unroll
+        for (int j = 0; j < 2 * R; ++j) V[j] = V[j + U];
     }
 }
 
@@ -261,8 +288,8 @@ cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUte
         if (e != cudaSuccess) return e;
         configured_device = dev;
     }
-    const dim3 grid(a.tiles_x * a.tiles_y * a.tiles_z, a.nshot);
-    step3d_kernel<R, MODE><<<grid, T3_THREADS, L::BYTES, s>>>(mc, mo, ml, mm, a);
+    const dim3 grid(a.nshot, a.tiles_x * a.tiles_y * a.tiles_z);
+    step3d_kernel<R, MODE><<<grid, T3_THREADS, L::BYTES, s>>>(mc, mo, ml, mm, with_weight_pairs(a));
     count_launch();
     return cudaGetLastError();
 }
@@ -285,7 +312,7 @@ bool step3d_available() { return true; }
 cudaError_t launch_step3d(int R, int mode, const CUtensorMap& mc, const CUtensorMap& mo,
                           const CUtensorMap& ml, const CUtensorMap& mm, const StepArgs& a,
                           cudaStream_t s) {
-    if (a.nshot > 65535) return cudaErrorInvalidValue;
+    if ((long long)a.tiles_x * a.tiles_y * a.tiles_z > 65535) return cudaErrorInvalidValue;
     switch (R) {
         case 1: return dispatch<1>(mode, mc, mo, ml, mm, a, s);
         case 2: return dispatch<2>(mode, mc, mo, ml, mm, a, s);

@@ -41,7 +41,7 @@ struct Layout3D {
     static constexpr int CUR_AL = align3(CUR, 128);
     static constexpr int TILE = T3_TY * T3_TX * 4;  // one FP32 output-plane tile
     static constexpr int OLD_GROUP = 2 * TILE + (MODE == MODE_GRAD ? TILE : 0);  // old, m, lap
-    static constexpr int BYTES = NB * CUR_AL + NBO * OLD_GROUP + (NB + NBO) * 8 + 128;
+    static constexpr int BYTES = NB * CUR_AL + NBO * OLD_GROUP + (NB + NBO) * 8 + T3_ZCHUNK * 4 + 128;
 };
 
 __device__ __forceinline__ float2 lo2(const float4& v) { return make_float2(v.x, v.y); }
@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
     unsigned char* old_ring = base + NB * L::CUR_AL;
     uint64_t* bc = reinterpret_cast<uint64_t*>(old_ring + NBO * L::OLD_GROUP);
     uint64_t* bo = bc + NB;
+    float* gzs = reinterpret_cast<float*>(bo + NBO);  // gz of the CTA's output planes
 
     const int tid = threadIdx.x, lane = tid % LANES_X, row = tid / LANES_X;
     const int s = blockIdx.x;
@@ -103,6 +104,7 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
     __syncthreads();
     if (tid == 0)
         for (int p = 0; p < min(NB, total); ++p) issue_cur(p);
+    if (tid < zc) gzs[tid] = a.gz != nullptr ? __ldg(a.gz + z0 + tid) : 1.f;
 
     // ---- per-thread constants
     const int x = x0 + 4 * lane;
@@ -159,9 +161,11 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
             const float4 cv = V[u + R];
             const float4 rv = *reinterpret_cast<const float4*>(prow + 2 * T3_XH);
             const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y, cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
-            // L u in packed pairs: c0 u + sum_k cx_k (x taps) + cy_k (y taps) + cz_k (z taps)
+            // L u in packed pairs: (c0 u + sum_k cx_k (x taps)) + sum_k cy_k (y taps)
+            // + sum_k cz_k (z taps), the three sums in independent chains
             float2 lo = __fmul2_rn(a.c0p, lo2(cv));
             float2 hi = __fmul2_rn(a.c0p, hi2(cv));
+            float2 loy = make_float2(0.f, 0.f), hiy = loy, loz = loy, hiz = loy;
 #pragma unroll
             for (int k = 1; k <= R; ++k) {
                 float2 xl, xh;
@@ -176,16 +180,18 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
                 hi = __ffma2_rn(a.cxp[k - 1], xh, hi);
                 const float4 ym = *reinterpret_cast<const float4*>(pl + (row + R - k) * T3_W + col);
                 const float4 yp = *reinterpret_cast<const float4*>(pl + (row + R + k) * T3_W + col);
-                lo = __ffma2_rn(a.cyp[k - 1], __fadd2_rn(lo2(ym), lo2(yp)), lo);
-                hi = __ffma2_rn(a.cyp[k - 1], __fadd2_rn(hi2(ym), hi2(yp)), hi);
+                loy = __ffma2_rn(a.cyp[k - 1], __fadd2_rn(lo2(ym), lo2(yp)), loy);
+                hiy = __ffma2_rn(a.cyp[k - 1], __fadd2_rn(hi2(ym), hi2(yp)), hiy);
                 const float4 zm = V[u + R - k], zp = V[u + R + k];
-                lo = __ffma2_rn(a.czp[k - 1], __fadd2_rn(lo2(zm), lo2(zp)), lo);
-                hi = __ffma2_rn(a.czp[k - 1], __fadd2_rn(hi2(zm), hi2(zp)), hi);
+                loz = __ffma2_rn(a.czp[k - 1], __fadd2_rn(lo2(zm), lo2(zp)), loz);
+                hiz = __ffma2_rn(a.czp[k - 1], __fadd2_rn(hi2(zm), hi2(zp)), hiz);
             }
+            lo = __fadd2_rn(__fadd2_rn(lo, loy), loz);
+            hi = __fadd2_rn(__fadd2_rn(hi, hiy), hiz);
             const int ti = row * T3_TX + 4 * lane;
             const float4 ov = *reinterpret_cast<const float4*>(old_buf(zr) + ti);
             const float4 mv = *reinterpret_cast<const float4*>(m_buf(zr) + ti);
-            const float gz = (a.gz != nullptr && z < a.nz) ? __ldg(a.gz + z) : 1.f;
+            const float gz = gzs[zr];
             // u_{n+1} = g (m L u + 2 u) - g^2 u_{n-1}
             const float gyz = gz * gyv;
             const float2 gl = __fmul2_rn(make_float2(gyz, gyz), make_float2(gxe[0], gxe[1]));

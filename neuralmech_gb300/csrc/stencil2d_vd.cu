@@ -42,7 +42,9 @@ struct LayoutVD {
     static constexpr int BH = VD_TZ + 2 * R + 1;  // staged b rows: z0 - R ..
     static constexpr int ZH = VD_TZ + 2 * R;      // flux rows in z: half rows z0 - R ..
     static constexpr int F = FH * VD_W * 4;
-    static constexpr int O = VD_TZ * VD_TX * 4;
+    // u_{n-1} tile: staged in the forward; the adjoint reads it from global
+    // memory at the update, which keeps two adjoint CTAs within one SM
+    static constexpr int O = MODE == MODE_GRAD_U ? 0 : VD_TZ * VD_TX * 4;
     static constexpr int U = MODE == MODE_GRAD_U ? F : 0;
     static constexpr int O_OFF = al128(F);
     static constexpr int U_OFF = O_OFF + al128(O);
@@ -78,7 +80,7 @@ __device__ __forceinline__ float4 dx4(const float* w, const StepArgs& a) {
 }
 
 template <int R, int MODE>
-__global__ void __launch_bounds__(VD_THREADS, MODE == MODE_PLAIN ? 2 : 1)
+__global__ void __launch_bounds__(VD_THREADS, 2)
     step2d_vd_kernel(const __grid_constant__ CUtensorMap map_f, const __grid_constant__ CUtensorMap map_o,
                      const __grid_constant__ CUtensorMap map_u, const __grid_constant__ CUtensorMap map_b,
                      const StepArgs a) {
@@ -104,7 +106,7 @@ __global__ void __launch_bounds__(VD_THREADS, MODE == MODE_PLAIN ? 2 : 1)
         const int b = i % L::STAGES;
         mbar_arrive_expect_tx(&bars[b], uint32_t(L::F + L::O + L::U + (i == 0 ? L::B : 0)));
         tma_load_3d(stage(b), &map_f, x0 - 8, z0 - 2 * R, s0 + i, &bars[b]);
-        tma_load_3d(stage(b) + L::O_OFF, &map_o, x0, z0, s0 + i, &bars[b]);
+        if (MODE != MODE_GRAD_U) tma_load_3d(stage(b) + L::O_OFF, &map_o, x0, z0, s0 + i, &bars[b]);
         if (MODE == MODE_GRAD_U) tma_load_3d(stage(b) + L::U_OFF, &map_u, x0 - 8, z0 - 2 * R, s0 + i, &bars[b]);
         if (i == 0) tma_load_2d(const_cast<float*>(B), &map_b, x0 - 8, z0 - R, &bars[b]);
     };
@@ -276,14 +278,19 @@ __global__ void __launch_bounds__(VD_THREADS, MODE == MODE_PLAIN ? 2 : 1)
         for (int r = 0; r < VD_RB; ++r) {
             const int z = zb + r;
             const float4 cv = ld4(F + (warp * VD_RB + r + 2 * R) * VD_W + 8 + 4 * lane);
-            const float4 ov = ld4(O + (warp * VD_RB + r) * VD_TX + 4 * lane);
+            const long long off = (long long)z * a.ld + x;
+            float4 ov;
+            if (MODE != MODE_GRAD_U)
+                ov = ld4(O + (warp * VD_RB + r) * VD_TX + 4 * lane);
+            else  // (plain load: u_new is this level's buffer, each cell read here and written below)
+                ov = (z < a.nz && x < a.ld) ? *reinterpret_cast<const float4*>(un + off)
+                                            : make_float4(0.f, 0.f, 0.f, 0.f);
             float nv[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 const float g = gzr[r] * gxe[e];
                 nv[e] = g * fmaf(comp(krow[r], e), comp(lb[r], e), 2.f * comp(cv, e)) - (g * g) * comp(ov, e);
             }
-            const long long off = (long long)z * a.ld + x;
             if (zin[r] && all_x) {
                 st4(un + off, make_float4(nv[0], nv[1], nv[2], nv[3]));
             } else if (a.zero_ring) {

@@ -99,18 +99,19 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ?
     // point-list ranges of this tile for every shot of the CTA, staged once
     // (one global read each instead of a dependent read per shot and list)
     __shared__ int2 smp_range[T2_MAX_SPC], inj_range[T2_MAX_SPC];
+    // the first stages are issued before the point-list ranges are read, so
+    // that the two memory latencies overlap
+    if (tid == 0) {
+        for (int b = 0; b < L::STAGES; ++b) mbar_init(&bars[b], 1);
+        fence_mbar_init();
+        for (int i = 0; i < min(ns, L::STAGES); ++i) issue(i);
+    }
     if (tid < ns) {
         const int k = (s0 + tid) * ntiles + tile;
         smp_range[tid] = a.smp.off ? make_int2(a.smp.off[k], a.smp.off[k + 1]) : make_int2(0, 0);
         inj_range[tid] = a.inj.off ? make_int2(a.inj.off[k], a.inj.off[k + 1]) : make_int2(0, 0);
     }
-    if (tid == 0) {
-        for (int b = 0; b < L::STAGES; ++b) mbar_init(&bars[b], 1);
-        fence_mbar_init();
-    }
     __syncthreads();
-    if (tid == 0)
-        for (int i = 0; i < min(ns, L::STAGES); ++i) issue(i);
 
     // ---- per-thread constants, reused for every shot of the CTA
     const int x = x0 + 4 * lane;

@@ -101,19 +101,20 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
     // point-list ranges of this tile for every shot of the CTA, staged once:
     // sampling, step-1 (extended region) injection, step-2 injection
     __shared__ int2 smp_rng[T2_MAX_SPC], inje_rng[T2_MAX_SPC], inj_rng[T2_MAX_SPC];
+    // the first stages are issued before the point-list ranges are read, so
+    // that the two memory latencies overlap
+    if (tid == 0) {
+        for (int b = 0; b < L::STAGES; ++b) mbar_init(&bars[b], 1);
+        fence_mbar_init();
+        for (int i = 0; i < min(ns, L::STAGES); ++i) issue(i);
+    }
     if (tid < ns) {
         const int k = (s0 + tid) * ntiles + tile;
         smp_rng[tid] = a.smp.off ? make_int2(a.smp.off[k], a.smp.off[k + 1]) : make_int2(0, 0);
         inje_rng[tid] = p.inj_e.off ? make_int2(p.inj_e.off[k], p.inj_e.off[k + 1]) : make_int2(0, 0);
         inj_rng[tid] = a.inj.off ? make_int2(a.inj.off[k], a.inj.off[k + 1]) : make_int2(0, 0);
     }
-    if (tid == 0) {
-        for (int b = 0; b < L::STAGES; ++b) mbar_init(&bars[b], 1);
-        fence_mbar_init();
-    }
     __syncthreads();
-    if (tid == 0)
-        for (int i = 0; i < min(ns, L::STAGES); ++i) issue(i);
 
     // ---- per-thread constants, reused for every shot of the CTA
     const int ex = x0 - 4 + 4 * lane;  // global x of this lane's first E column

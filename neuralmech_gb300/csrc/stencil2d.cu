@@ -106,14 +106,8 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ?
         fence_mbar_init();
         for (int i = 0; i < min(ns, L::STAGES); ++i) issue(i);
     }
-    if (tid < ns) {
-        const int k = (s0 + tid) * ntiles + tile;
-        smp_range[tid] = a.smp.off ? make_int2(a.smp.off[k], a.smp.off[k + 1]) : make_int2(0, 0);
-        inj_range[tid] = a.inj.off ? make_int2(a.inj.off[k], a.inj.off[k + 1]) : make_int2(0, 0);
-    }
-    __syncthreads();
-
-    // ---- per-thread constants, reused for every shot of the CTA
+    // ---- per-thread constants, reused for every shot of the CTA (loaded before
+    // the barrier below, so that their latency overlaps the range reads)
     const int x = x0 + 4 * lane;
     const int zb = z0 + warp * RB;
     float4 mrow[RB];
@@ -137,6 +131,13 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ?
         xin[e] = x + e >= R && x + e < a.nx - R;
     }
     const bool all_x = xin[0] && xin[1] && xin[2] && xin[3];
+
+    if (tid < ns) {
+        const int k = (s0 + tid) * ntiles + tile;
+        smp_range[tid] = a.smp.off ? make_int2(a.smp.off[k], a.smp.off[k + 1]) : make_int2(0, 0);
+        inj_range[tid] = a.inj.off ? make_int2(a.inj.off[k], a.inj.off[k + 1]) : make_int2(0, 0);
+    }
+    __syncthreads();
 
     float4 gacc[RB];
 #pragma unroll

@@ -140,13 +140,9 @@ __global__ void __launch_bounds__(LP_THREADS, 2)
         fence_mbar_init();
         for (int i = 0; i < min(ns, LP_STAGES); ++i) issue(i);
     }
-    if (tid < ns) {
-        const int k = (s0 + tid) * ntiles + tile;
-        smp_range[tid] = a.smp.off ? make_int2(a.smp.off[k], a.smp.off[k + 1]) : make_int2(0, 0);
-        inj_range[tid] = a.inj.off ? make_int2(a.inj.off[k], a.inj.off[k + 1]) : make_int2(0, 0);
-    }
-    __syncthreads();
 
+    // ---- per-thread constants (loaded before the barrier below, so that their
+    // latency overlaps the range reads)
     const int x = x0 + 4 * lane;
     const int zb = z0 + warp * LP_RB;
     float4 mrow[LP_RB];
@@ -169,6 +165,14 @@ __global__ void __launch_bounds__(LP_THREADS, 2)
         xin[e] = x + e >= R && x + e < a.nx - R;
     }
     const bool x_ok = x < a.ld;
+
+    if (tid < ns) {
+        const int k = (s0 + tid) * ntiles + tile;
+        smp_range[tid] = a.smp.off ? make_int2(a.smp.off[k], a.smp.off[k + 1]) : make_int2(0, 0);
+        inj_range[tid] = a.inj.off ? make_int2(a.inj.off[k], a.inj.off[k + 1]) : make_int2(0, 0);
+    }
+    __syncthreads();
+
     // staged columns of this lane: centre 8 + 4l, left 4 + 4l, right 12 + 4l;
     // their scale blocks in the staged scale rows (block 4t - 4 at index 0)
     const int cc = LP_XH + 4 * lane;

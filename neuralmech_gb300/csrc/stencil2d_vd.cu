@@ -119,14 +119,9 @@ __global__ void __launch_bounds__(VD_THREADS, 2)
         fence_mbar_init();
         for (int i = 0; i < min(ns, L::STAGES); ++i) issue(i);
     }
-    if (tid < ns) {
-        const int k = (s0 + tid) * ntiles + tile;
-        smp_range[tid] = a.smp.off ? make_int2(a.smp.off[k], a.smp.off[k + 1]) : make_int2(0, 0);
-        inj_range[tid] = a.inj.off ? make_int2(a.inj.off[k], a.inj.off[k + 1]) : make_int2(0, 0);
-    }
-    __syncthreads();
 
-    // ---- per-thread constants
+    // ---- per-thread constants (loaded before the barrier below, so that their
+    // latency overlaps the range reads)
     const int x = x0 + 4 * lane;
     const int zb = z0 + warp * VD_RB;
     float4 krow[VD_RB];
@@ -148,6 +143,13 @@ __global__ void __launch_bounds__(VD_THREADS, 2)
         xin[e] = x + e >= R && x + e < a.nx - R;
     }
     const bool all_x = xin[0] && xin[1] && xin[2] && xin[3];
+
+    if (tid < ns) {
+        const int k = (s0 + tid) * ntiles + tile;
+        smp_range[tid] = a.smp.off ? make_int2(a.smp.off[k], a.smp.off[k + 1]) : make_int2(0, 0);
+        inj_range[tid] = a.inj.off ? make_int2(a.inj.off[k], a.inj.off[k + 1]) : make_int2(0, 0);
+    }
+    __syncthreads();
 
     float4 gk[VD_RB], gbx[VD_RB], gbz[VD_RB];
 #pragma unroll

@@ -10,12 +10,13 @@
 // together, so m and (MODE_GRAD) the gradient tile are read from DRAM once
 // per column and served from L2 to the other shots.
 //   * u_n planes, each with a halo of R rows in y and 4 columns in x, arrive by
-//     TMA (cp.async.bulk.tensor.4d) into a ring of NB = 8 shared-memory
+//     TMA (cp.async.bulk.tensor.4d) into a ring of NB = 4 + R shared-memory
 //     buffers, four planes ahead of use. A thread keeps the 2R + 1 z-taps of
 //     its 4 cells in a register queue; the x and y taps come from the staged
 //     plane of the output z.
-//   * u_{n-1}, m and (MODE_GRAD) the stored L u of the output plane arrive by
-//     TMA into a ring of NBO = 4 buffers, four planes ahead.
+//   * u_{n-1}, m and (MODE_GRAD) the stored L u of output plane zr arrive by
+//     TMA into a ring of NBO = 4 buffers, on the mbarrier of staged plane
+//     zr + 2R (the plane that output first needs): one wait per plane.
 //   * All mbarrier waits are bounded (status bit on give-up, never a trap).
 //   * Point lists are bucketed by (z chunk, y tile, x tile). At each output
 //     plane the CTA samples receivers from the staged u_n plane, and after its
@@ -30,18 +31,18 @@ namespace {
 
 __host__ __device__ constexpr int align3(int v, int a) { return (v + a - 1) / a * a; }
 
-constexpr int NB = 8;   // u_n plane ring
-constexpr int NBO = 4;  // u_{n-1} / m / L u plane ring
+constexpr int NBO = 4;  // u_{n-1} / m / L u tile ring (the u_n ring has NBO + R buffers)
 constexpr int LANES_X = T3_TX / 4;  // 16
 
 template <int R, int MODE>
 struct Layout3D {
+    static constexpr int NB = NBO + R;  // u_n plane ring
     static constexpr int H = T3_TY + 2 * R;
     static constexpr int CUR = H * T3_W * 4;  // TMA box bytes of one u_n plane
     static constexpr int CUR_AL = align3(CUR, 128);
     static constexpr int TILE = T3_TY * T3_TX * 4;  // one FP32 output-plane tile
     static constexpr int OLD_GROUP = 2 * TILE + (MODE == MODE_GRAD ? TILE : 0);  // old, m, lap
-    static constexpr int BYTES = NB * CUR_AL + NBO * OLD_GROUP + (NB + NBO) * 8 + T3_ZCHUNK * 4 + 128;
+    static constexpr int BYTES = NB * CUR_AL + NBO * OLD_GROUP + NB * 8 + T3_ZCHUNK * 4 + 128;
 };
 
 __device__ __forceinline__ float2 lo2(const float4& v) { return make_float2(v.x, v.y); }
@@ -54,6 +55,7 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
                   const __grid_constant__ CUtensorMap map_lap,
                   const __grid_constant__ CUtensorMap map_m, const StepArgs a) {
     using L = Layout3D<R, MODE>;
+    constexpr int NB = L::NB;
     constexpr int U = T3_UNROLL;  // output planes per turn of the register queue
     constexpr int Q = 2 * R + U;  // register queue of staged planes
     extern __shared__ unsigned char smem_raw[];
@@ -62,8 +64,7 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
     unsigned char* cur_ring = base;
     unsigned char* old_ring = base + NB * L::CUR_AL;
     uint64_t* bc = reinterpret_cast<uint64_t*>(old_ring + NBO * L::OLD_GROUP);
-    uint64_t* bo = bc + NB;
-    float* gzs = reinterpret_cast<float*>(bo + NBO);  // gz of the CTA's output planes
+    float* gzs = reinterpret_cast<float*>(bc + NB);  // gz of the CTA's output planes
 
     const int tid = threadIdx.x, lane = tid % LANES_X, row = tid / LANES_X;
     const int s = blockIdx.x;
@@ -82,28 +83,27 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
     auto m_buf = [&](int zr) { return reinterpret_cast<float*>(old_ring + (zr % NBO) * L::OLD_GROUP + L::TILE); };
     auto lap_buf = [&](int zr) { return old_ring + (zr % NBO) * L::OLD_GROUP + 2 * L::TILE; };
 
-    // staged plane p holds u_n at z = z0 - R + p; old group zr holds output plane z0 + zr
-    auto issue_cur = [&](int p) {
+    // staged plane p holds u_n at z = z0 - R + p; old group zr holds output
+    // plane z0 + zr and travels with staged plane zr + 2R (p < total <=> zr < zc)
+    auto issue = [&](int p) {
         uint64_t* bar = &bc[p % NB];
-        mbar_arrive_expect_tx(bar, uint32_t(L::CUR));
+        const int zr = p - 2 * R;
+        mbar_arrive_expect_tx(bar, uint32_t(L::CUR) + (zr >= 0 ? uint32_t(2 * L::TILE) + lap_bytes : 0u));
         tma_load_4d(cur_buf(p), &map_cur, x0 - T3_XH, y0 - R, z0 - R + p, s, bar);
-    };
-    auto issue_old = [&](int zr) {
-        uint64_t* bar = &bo[zr % NBO];
-        mbar_arrive_expect_tx(bar, uint32_t(2 * L::TILE) + lap_bytes);
-        tma_load_4d(old_buf(zr), &map_old, x0, y0, z0 + zr, s, bar);
-        tma_load_3d(m_buf(zr), &map_m, x0, y0, z0 + zr, bar);
-        if (MODE == MODE_GRAD) tma_load_4d(lap_buf(zr), &map_lap, x0, y0, z0 + zr, s, bar);
+        if (zr >= 0) {
+            tma_load_4d(old_buf(zr), &map_old, x0, y0, z0 + zr, s, bar);
+            tma_load_3d(m_buf(zr), &map_m, x0, y0, z0 + zr, bar);
+            if (MODE == MODE_GRAD) tma_load_4d(lap_buf(zr), &map_lap, x0, y0, z0 + zr, s, bar);
+        }
     };
 
     if (tid == 0) {
         for (int b = 0; b < NB; ++b) mbar_init(&bc[b], 1);
-        for (int b = 0; b < NBO; ++b) mbar_init(&bo[b], 1);
         fence_mbar_init();
     }
     __syncthreads();
     if (tid == 0)
-        for (int p = 0; p < min(NB, total); ++p) issue_cur(p);
+        for (int p = 0; p < min(NB, total); ++p) issue(p);
     if (tid < zc) gzs[tid] = a.gz != nullptr ? __ldg(a.gz + z0 + tid) : 1.f;
 
     // ---- per-thread constants
@@ -135,8 +135,7 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
     }
     __syncthreads();  // planes 0 .. R-1 are consumed
     if (tid == 0) {
-        for (int p = NB; p < min(NB + R, total); ++p) issue_cur(p);
-        for (int zr = 0; zr < min(NBO, zc); ++zr) issue_old(zr);
+        for (int p = NB; p < min(NB + R, total); ++p) issue(p);
     }
 
     const int lo_s = a.smp.off ? a.smp.off[s * ntiles + tile] : 0;
@@ -153,7 +152,6 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
             const int pn = zr + 2 * R;  // newest staged plane needed
             if (!mbar_wait(&bc[pn % NB], (pn / NB) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
             V[u + 2 * R] = *reinterpret_cast<const float4*>(cur_buf(pn) + (row + R) * T3_W + col);
-            if (!mbar_wait(&bo[zr % NBO], (zr / NBO) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
 
             const float* pl = cur_buf(zr + R);  // u_n at the output plane, with halo
             const float* prow = pl + (row + R) * T3_W + 4 * lane;
@@ -261,8 +259,7 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
             __syncthreads();  // plane zr + R and old group zr fully read; stores of plane z done
             if (tid == 0) {
                 fence_proxy_async_smem();
-                if (zr + NB + R < total) issue_cur(zr + NB + R);
-                if (zr + NBO < zc) issue_old(zr + NBO);
+                if (zr + NB + R < total) issue(zr + NB + R);
             }
             for (int j = lo_i + tid; j < hi_i; j += T3_THREADS) {
                 const int2 en = a.inj.ent[j];

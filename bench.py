@@ -79,6 +79,7 @@ def parse():
                     help="run one gradient and exit (the command profiled by ncu)")
     ap.add_argument("--nt", type=int, default=0, help="override the number of time steps (profiling)")
     ap.add_argument("--shots", type=int, default=0, help="use the first N shots (profiling)")
+    ap.add_argument("--ckpt-every", type=int, default=0, help="override the checkpoint interval (profiling)")
     ap.add_argument("--field-format", default="fp32", choices=["fp32", "fp16", "i16"],
                     help="fwd2048: storage of the wavefields (arithmetic stays FP32)")
     ap.add_argument("--adjoint", default="checkpoint", choices=["checkpoint", "reconstruct"],
@@ -277,6 +278,7 @@ def run_other(args):
 
     dev = torch.device("cuda", 0)
     lib = _lib.load()
+    graph_kernels = 0
     if args.workload == "batch8":
         from neuralmech_gb300.batch import BatchFWI
         models = []
@@ -287,6 +289,7 @@ def run_other(args):
             obs = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, w.grid)
             models.append(dict(vel=v, wavelet=wav, src=src, rec=rec, observed=obs, grid=w.grid))
         batch = BatchFWI(models, autotune=True)
+        graph_kernels = batch.graph_kernels  # replays launch these without a host call each
         step = batch.run
         updates, bpu = batch.cell_updates, 18.0
         cfg = {"workload": "batch8: 8 models 512^2..1536^2, 1000..3000 steps, 128 shots, Ricker 10..25 Hz, "
@@ -294,11 +297,19 @@ def run_other(args):
                "models": [[list(m.call.grid.shape), m.call.grid.nt, m.call.problem.nshot] for m in batch.models],
                "configs": batch.configs}
     else:
-        w = wl("fwi1024" if args.workload == "vd1024" else args.workload)
+        w = wl("fwi1024" if args.workload == "vd1024" else args.workload, scale=args.scale)
+        if args.shots:
+            w.src = w.src[:args.shots].copy()
+            if w.wavelet.ndim == 2:
+                w.wavelet = w.wavelet[:args.shots].copy()
+            if w.rec.ndim == 3:
+                w.rec = w.rec[:args.shots].copy()
         g = w.grid
         if args.nt:
             g = dataclasses.replace(g, nt=args.nt, ckpt_every=min(g.ckpt_every or args.nt, args.nt))
-            w.wavelet = w.wavelet[:args.nt]
+            w.wavelet = w.wavelet[..., :args.nt]
+        if args.ckpt_every:
+            g = dataclasses.replace(g, ckpt_every=args.ckpt_every)
         v = torch.from_numpy(w.vel).to(dev)
         wav = torch.from_numpy(w.wavelet).to(dev)
         src, rec = torch.from_numpy(w.src), torch.from_numpy(w.rec)
@@ -341,6 +352,11 @@ def run_other(args):
             cfg = {"workload": f"fwi384_3d: 3D FWI gradient {g.shape[0]}^3, {g.nt} steps, {w.nshot} shots "
                                f"in groups of 8, {w.rec.shape[1]} receivers per shot, BF16 checkpoints every "
                                f"{g.ckpt_every}"}
+    if args.once:  # one step, no timing: the command profiled by ncu
+        step()
+        torch.cuda.synchronize()
+        print(json.dumps({"once": args.workload, "config": cfg}), flush=True)
+        return 0
     for _ in range(max(1, args.warmup)):
         step()
     torch.cuda.synchronize()
@@ -361,7 +377,7 @@ def run_other(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
             "hbm_alg_gbs": gbs, "hbm_frac_measured": gbs / hbm, "peak_source": src_kind, "clocks": clk,
-            "gpu_launches": int(lib.wfd_kernel_launches() - n0)}
+            "gpu_launches": int(lib.wfd_kernel_launches() - n0) + graph_kernels * args.steps}
     print(json.dumps(line), flush=True)
     return 0
 

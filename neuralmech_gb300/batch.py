@@ -23,6 +23,7 @@ import dataclasses
 
 import torch
 
+from . import _lib
 from . import autotune as _autotune
 from .wavefd import Grid, _misfit_gradient_into, _prepare, _workspace
 
@@ -68,10 +69,15 @@ class BatchFWI:
         self.graph = None
         self._launch()  # eager run: sets kernel attributes, validates arguments
         torch.cuda.synchronize(self.device)
+        # kernels of one replay: what the library launched while the graph was captured
+        self.graph_kernels = 0
         if graph:
+            lib = _lib.load()
+            n0 = lib.wfd_kernel_launches()
             self.graph = torch.cuda.CUDAGraph()
             with torch.cuda.graph(self.graph):
                 self._launch()
+            self.graph_kernels = int(lib.wfd_kernel_launches() - n0)
 
     def _launch(self):
         main = torch.cuda.current_stream(self.device)

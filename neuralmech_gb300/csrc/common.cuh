@@ -42,6 +42,15 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                  : "memory");
 }
 
+// Programmatic dependent launch (sm_90+): a kernel launched with programmatic
+// stream serialisation may start while the previous kernel of the stream
+// finishes. grid_dependency_wait() blocks the calling thread until that kernel
+// has completed and its memory is visible; launch_dependents() lets the next
+// kernel of the stream start its CTAs once every CTA of this grid has called
+// it (or exited).
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t done;
     asm volatile(

@@ -99,12 +99,18 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ?
     // point-list ranges of this tile for every shot of the CTA, staged once
     // (one global read each instead of a dependent read per shot and list)
     __shared__ int2 smp_range[T2_MAX_SPC], inj_range[T2_MAX_SPC];
-    // the first stages are issued before the point-list ranges are read, so
-    // that the two memory latencies overlap
+    // launched as a programmatic dependent: everything above touches only
+    // registers and shared memory; every global access comes after the wait
     if (tid == 0) {
         for (int b = 0; b < L::STAGES; ++b) mbar_init(&bars[b], 1);
         fence_mbar_init();
+    }
+    grid_dependency_wait();
+    // the first stages are issued before the point-list ranges are read, so
+    // that the two memory latencies overlap
+    if (tid == 0) {
         for (int i = 0; i < min(ns, L::STAGES); ++i) issue(i);
+        launch_dependents();  // the next step's CTAs may take SM slots this grid frees
     }
     // ---- per-thread constants, reused for every shot of the CTA (loaded before
     // the barrier below, so that their latency overlaps the range reads)
@@ -316,10 +322,19 @@ cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUte
         if (e != cudaSuccess) return e;
         configured_device = dev;
     }
-    const dim3 grid(a.tiles_x * a.tiles_z, (a.nshot + a.shots_per_cta - 1) / a.shots_per_cta);
-    step2d_kernel<R, MODE, RB><<<grid, T2_THREADS, L::BYTES, s>>>(mc, mo, ml, a);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(a.tiles_x * a.tiles_z, (a.nshot + a.shots_per_cta - 1) / a.shots_per_cta);
+    cfg.blockDim = dim3(T2_THREADS);
+    cfg.dynamicSmemBytes = L::BYTES;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, step2d_kernel<R, MODE, RB>, mc, mo, ml, a);
     count_launch();
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int R, int RB>

@@ -322,17 +322,8 @@ cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUte
         if (e != cudaSuccess) return e;
         configured_device = dev;
     }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(a.tiles_x * a.tiles_z, (a.nshot + a.shots_per_cta - 1) / a.shots_per_cta);
-    cfg.blockDim = dim3(T2_THREADS);
-    cfg.dynamicSmemBytes = L::BYTES;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, step2d_kernel<R, MODE, RB>, mc, mo, ml, a);
+    const dim3 grid(a.tiles_x * a.tiles_z, (a.nshot + a.shots_per_cta - 1) / a.shots_per_cta);
+    const cudaError_t e = launch_pdl(step2d_kernel<R, MODE, RB>, grid, dim3(T2_THREADS), L::BYTES, s, mc, mo, ml, a);
     count_launch();
     return e != cudaSuccess ? e : cudaGetLastError();
 }

@@ -133,12 +133,17 @@ __global__ void __launch_bounds__(LP_THREADS, 2)
     };
 
     __shared__ int2 smp_range[T2_MAX_SPC], inj_range[T2_MAX_SPC];
-    // the first stages are issued before the point-list ranges are read, so
-    // that the two memory latencies overlap
+    // launched as a programmatic dependent: every global access comes after the wait
     if (tid == 0) {
         for (int b = 0; b < LP_STAGES; ++b) mbar_init(&bars[b], 1);
         fence_mbar_init();
+    }
+    grid_dependency_wait();
+    // the first stages are issued before the point-list ranges are read, so
+    // that the two memory latencies overlap
+    if (tid == 0) {
         for (int i = 0; i < min(ns, LP_STAGES); ++i) issue(i);
+        launch_dependents();
     }
 
     // ---- per-thread constants (loaded before the barrier below, so that their
@@ -291,9 +296,9 @@ cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUte
     LpArgs p = p_in;
     p.a = with_weight_pairs(p_in.a);
     const dim3 grid(p.a.tiles_x * p.a.tiles_z, (p.a.nshot + p.a.shots_per_cta - 1) / p.a.shots_per_cta);
-    step2d_lp_kernel<R, FMT><<<grid, LP_THREADS, L::BYTES, s>>>(mc, mo, mcs, mos, p);
+    const cudaError_t e = launch_pdl(step2d_lp_kernel<R, FMT>, grid, dim3(LP_THREADS), L::BYTES, s, mc, mo, mcs, mos, p);
     count_launch();
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int FMT>

@@ -112,12 +112,17 @@ __global__ void __launch_bounds__(VD_THREADS, 2)
     };
 
     __shared__ int2 smp_range[T2_MAX_SPC], inj_range[T2_MAX_SPC];
-    // the first stages are issued before the point-list ranges are read, so
-    // that the two memory latencies overlap
+    // launched as a programmatic dependent: every global access comes after the wait
     if (tid == 0) {
         for (int b = 0; b < L::STAGES; ++b) mbar_init(&bars[b], 1);
         fence_mbar_init();
+    }
+    grid_dependency_wait();
+    // the first stages are issued before the point-list ranges are read, so
+    // that the two memory latencies overlap
+    if (tid == 0) {
         for (int i = 0; i < min(ns, L::STAGES); ++i) issue(i);
+        launch_dependents();
     }
 
     // ---- per-thread constants (loaded before the barrier below, so that their
@@ -380,9 +385,9 @@ cudaError_t launch_impl(const CUtensorMap& mf, const CUtensorMap& mo, const CUte
         configured_device = dev;
     }
     const dim3 grid(a.tiles_x * a.tiles_z, (a.nshot + a.shots_per_cta - 1) / a.shots_per_cta);
-    step2d_vd_kernel<R, MODE><<<grid, VD_THREADS, L::BYTES, s>>>(mf, mo, mu, mb, a);
+    const cudaError_t e = launch_pdl(step2d_vd_kernel<R, MODE>, grid, dim3(VD_THREADS), L::BYTES, s, mf, mo, mu, mb, a);
     count_launch();
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int R>

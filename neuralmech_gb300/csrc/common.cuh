@@ -150,6 +150,7 @@ inline StepArgs with_weight_pairs(StepArgs a) {
     for (int k = 0; k < 4; ++k) {
         a.czp[k] = make_float2(a.cz[k], a.cz[k]);
         a.cyp[k] = make_float2(a.cy[k], a.cy[k]);
+        a.csp[k] = make_float2(a.cs[k], a.cs[k]);
         a.cxp[k] = make_float2(a.cx[k], a.cx[k]);
     }
     return a;

@@ -78,6 +78,7 @@ struct StepArgs {
     float* grad;               // [cells], MODE_GRAD accumulation target
     // variable density (stencil2d_vd.cu): m holds k = kappa dt^2/dx^2
     float cs[4];               // staggered first-derivative weights c_1..c_R
+    float2 csp[4];             // the same as duplicated pairs (set by the launchers)
     float vd_sz;               // (dx/dz)^2
     float *grad_bx, *grad_bz;  // MODE_GRAD_U accumulators at the half points (z, x+1/2), (z+1/2, x)
     int zero_ring;             // 2D one-step kernel: also write the fixed ring (and the row

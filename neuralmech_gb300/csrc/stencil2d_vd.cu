@@ -63,21 +63,31 @@ struct LayoutVD {
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, const float4& v) { *reinterpret_cast<float4*>(p) = v; }
 
+// Packed FP32x2 staggered sums, rounding as the scalar form
+// s = fmaf(c_k, hi_k - lo_k, s), k = 1 .. R: each difference is one rounded
+// subtraction (hi + (-1) lo, exact multiply), then a fused multiply-add.
+__device__ __forceinline__ float2 psub(float2 hi, float2 lo) {
+    return __ffma2_rn(lo, make_float2(-1.f, -1.f), hi);
+}
+
 // Raw staggered x differences at the 4 half points whose window w[12] spans
 // the cells 4 left of the first half point's left cell to 7 right of it:
-// (Dx f)_{j+e} = sum_k c_k (w[4 + e + k] - w[5 + e - k]).
+// (Dx f)_{j+e} = sum_k c_k (w[4 + e + k] - w[5 + e - k]), in pairs e, e + 1
+// (the two operands of a pair sit one register apart, so the differences are
+// scalar and the multiply-adds packed).
 template <int R>
 __device__ __forceinline__ float4 dx4(const float* w, const StepArgs& a) {
-    float d[4];
+    float2 lo = make_float2(0.f, 0.f), hi = lo;
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        float s = 0.f;
-#pragma unroll
-        for (int k = 1; k <= R; ++k) s = fmaf(a.cs[k - 1], w[4 + e + k] - w[5 + e - k], s);
-        d[e] = s;
+    for (int k = 1; k <= R; ++k) {
+        lo = __ffma2_rn(a.csp[k - 1], make_float2(w[4 + k] - w[5 - k], w[5 + k] - w[6 - k]), lo);
+        hi = __ffma2_rn(a.csp[k - 1], make_float2(w[6 + k] - w[7 - k], w[7 + k] - w[8 - k]), hi);
     }
-    return make_float4(d[0], d[1], d[2], d[3]);
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
 }
+
+__device__ __forceinline__ float2 lo2v(const float4& v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2v(const float4& v) { return make_float2(v.z, v.w); }
 
 template <int R, int MODE>
 __global__ void __launch_bounds__(VD_THREADS, 2)
@@ -202,38 +212,37 @@ __global__ void __launch_bounds__(VD_THREADS, 2)
             for (int j = 0; j < VD_RB + 2 * R - 1; ++j) W[j] = ld4(trow(warp * VD_RB + R + 1 + j) + 8 + 4 * lane);
 #pragma unroll
             for (int r = 0; r < VD_RB; ++r) {
-                float d[4];
+                float2 dl = make_float2(0.f, 0.f), dh = dl;
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    float s = 0.f;
-#pragma unroll
-                    for (int k = 1; k <= R; ++k) s = fmaf(a.cs[k - 1], comp(W[r + R - 1 + k], e) - comp(W[r + R - k], e), s);
-                    d[e] = s;
+                for (int k = 1; k <= R; ++k) {
+                    const float4 up = W[r + R - 1 + k], dn = W[r + R - k];
+                    dl = __ffma2_rn(a.csp[k - 1], psub(lo2v(up), lo2v(dn)), dl);
+                    dh = __ffma2_rn(a.csp[k - 1], psub(hi2v(up), hi2v(dn)), dh);
                 }
                 const int br = warp * VD_RB + r + R;
                 const float4 b0 = ld4(brow(br) + 8 + 4 * lane), b1 = ld4(brow(br + 1) + 8 + 4 * lane);
-                dzr[r] = make_float4(d[0], d[1], d[2], d[3]);
-                st4(FZ + (warp * VD_RB + r + R) * VD_TX + 4 * lane,
-                    make_float4(0.5f * (b0.x + b1.x) * d[0], 0.5f * (b0.y + b1.y) * d[1],
-                                0.5f * (b0.z + b1.z) * d[2], 0.5f * (b0.w + b1.w) * d[3]));
+                dzr[r] = make_float4(dl.x, dl.y, dh.x, dh.y);
+                const float2 h = make_float2(0.5f, 0.5f);
+                const float2 fl = __fmul2_rn(__fmul2_rn(h, __fadd2_rn(lo2v(b0), lo2v(b1))), dl);
+                const float2 fh = __fmul2_rn(__fmul2_rn(h, __fadd2_rn(hi2v(b0), hi2v(b1))), dh);
+                st4(FZ + (warp * VD_RB + r + R) * VD_TX + 4 * lane, make_float4(fl.x, fl.y, fh.x, fh.y));
             }
         }
         // z halo half rows: FZ rows 0 .. R-1 (warps 0 .. R-1) and VD_TZ + R .. VD_TZ + 2R - 2
         if (warp < 2 * R - 1) {
             const int f = warp < R ? warp : VD_TZ + warp;  // FZ row: half row z0 - R + f
-            float d[4] = {0.f, 0.f, 0.f, 0.f};
+            float2 dl = make_float2(0.f, 0.f), dh = dl;
 #pragma unroll
             for (int k = 1; k <= R; ++k) {
                 const float4 up = ld4(trow(f + R + k) + 8 + 4 * lane), dn = ld4(trow(f + R + 1 - k) + 8 + 4 * lane);
-                d[0] = fmaf(a.cs[k - 1], up.x - dn.x, d[0]);
-                d[1] = fmaf(a.cs[k - 1], up.y - dn.y, d[1]);
-                d[2] = fmaf(a.cs[k - 1], up.z - dn.z, d[2]);
-                d[3] = fmaf(a.cs[k - 1], up.w - dn.w, d[3]);
+                dl = __ffma2_rn(a.csp[k - 1], psub(lo2v(up), lo2v(dn)), dl);
+                dh = __ffma2_rn(a.csp[k - 1], psub(hi2v(up), hi2v(dn)), dh);
             }
             const float4 b0 = ld4(brow(f) + 8 + 4 * lane), b1 = ld4(brow(f + 1) + 8 + 4 * lane);
-            st4(FZ + f * VD_TX + 4 * lane,
-                make_float4(0.5f * (b0.x + b1.x) * d[0], 0.5f * (b0.y + b1.y) * d[1], 0.5f * (b0.z + b1.z) * d[2],
-                            0.5f * (b0.w + b1.w) * d[3]));
+            const float2 h = make_float2(0.5f, 0.5f);
+            const float2 fl = __fmul2_rn(__fmul2_rn(h, __fadd2_rn(lo2v(b0), lo2v(b1))), dl);
+            const float2 fh = __fmul2_rn(__fmul2_rn(h, __fadd2_rn(hi2v(b0), hi2v(b1))), dh);
+            st4(FZ + f * VD_TX + 4 * lane, make_float4(fl.x, fl.y, fh.x, fh.y));
         }
     };
 
@@ -247,18 +256,19 @@ __global__ void __launch_bounds__(VD_THREADS, 2)
             const float* fx = FX + (warp * VD_RB + r) * VD_FXW + 4 * lane;
             const float4 p0 = ld4(fx), p1 = ld4(fx + 4), p2 = ld4(fx + 8);
             const float w[12] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w, p2.x, p2.y, p2.z, p2.w};
-            float l[4];
+            // l = sz * (sum_k c_k (Z up - Z down)) + sum_k c_k (w right - w left), in pairs
+            float2 xl = make_float2(0.f, 0.f), xh = xl, zl = xl, zh = xl;
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                float sx = 0.f, sz = 0.f;
-#pragma unroll
-                for (int k = 1; k <= R; ++k) {
-                    sx = fmaf(a.cs[k - 1], w[3 + e + k] - w[4 + e - k], sx);
-                    sz = fmaf(a.cs[k - 1], comp(Z[r + R + k - 1], e) - comp(Z[r + R - k], e), sz);
-                }
-                l[e] = fmaf(a.vd_sz, sz, sx);
+            for (int k = 1; k <= R; ++k) {
+                xl = __ffma2_rn(a.csp[k - 1], make_float2(w[3 + k] - w[4 - k], w[4 + k] - w[5 - k]), xl);
+                xh = __ffma2_rn(a.csp[k - 1], make_float2(w[5 + k] - w[6 - k], w[6 + k] - w[7 - k]), xh);
+                const float4 up = Z[r + R + k - 1], dn = Z[r + R - k];
+                zl = __ffma2_rn(a.csp[k - 1], psub(lo2v(up), lo2v(dn)), zl);
+                zh = __ffma2_rn(a.csp[k - 1], psub(hi2v(up), hi2v(dn)), zh);
             }
-            out[r] = make_float4(l[0], l[1], l[2], l[3]);
+            const float2 szp = make_float2(a.vd_sz, a.vd_sz);
+            const float2 ll = __ffma2_rn(szp, zl, xl), lh = __ffma2_rn(szp, zh, xh);
+            out[r] = make_float4(ll.x, ll.y, lh.x, lh.y);
         }
     };
 
@@ -280,6 +290,17 @@ __global__ void __launch_bounds__(VD_THREADS, 2)
         float4 dxq[VD_RB], dzq[VD_RB], lb[VD_RB];
         fluxes(F, dxq, dzq);
         __syncthreads();
+        // MODE_GRAD_U: u_{n-1} comes from global memory (plain loads: u_new is
+        // this level's buffer, each cell read here and written below); issued
+        // before the divergence so that their latency overlaps it
+        float4 ovg[MODE == MODE_GRAD_U ? VD_RB : 1];
+        if (MODE == MODE_GRAD_U) {
+#pragma unroll
+            for (int r = 0; r < VD_RB; ++r)
+                ovg[r] = (zb + r < a.nz && x < a.ld)
+                             ? *reinterpret_cast<const float4*>(un + (long long)(zb + r) * a.ld + x)
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
         divergence(lb);
 
 #pragma unroll
@@ -287,12 +308,7 @@ __global__ void __launch_bounds__(VD_THREADS, 2)
             const int z = zb + r;
             const float4 cv = ld4(F + (warp * VD_RB + r + 2 * R) * VD_W + 8 + 4 * lane);
             const long long off = (long long)z * a.ld + x;
-            float4 ov;
-            if (MODE != MODE_GRAD_U)
-                ov = ld4(O + (warp * VD_RB + r) * VD_TX + 4 * lane);
-            else  // (plain load: u_new is this level's buffer, each cell read here and written below)
-                ov = (z < a.nz && x < a.ld) ? *reinterpret_cast<const float4*>(un + off)
-                                            : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 ov = MODE != MODE_GRAD_U ? ld4(O + (warp * VD_RB + r) * VD_TX + 4 * lane) : ovg[r];
             float nv[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -385,7 +401,8 @@ cudaError_t launch_impl(const CUtensorMap& mf, const CUtensorMap& mo, const CUte
         configured_device = dev;
     }
     const dim3 grid(a.tiles_x * a.tiles_z, (a.nshot + a.shots_per_cta - 1) / a.shots_per_cta);
-    const cudaError_t e = launch_pdl(step2d_vd_kernel<R, MODE>, grid, dim3(VD_THREADS), L::BYTES, s, mf, mo, mu, mb, a);
+    const cudaError_t e = launch_pdl(step2d_vd_kernel<R, MODE>, grid, dim3(VD_THREADS), L::BYTES, s, mf, mo, mu, mb,
+                                      with_weight_pairs(a));
     count_launch();
     return e != cudaSuccess ? e : cudaGetLastError();
 }

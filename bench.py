@@ -288,14 +288,17 @@ def run_other(args):
             src, rec = torch.from_numpy(w.src), torch.from_numpy(w.rec)
             obs = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, w.grid)
             models.append(dict(vel=v, wavelet=wav, src=src, rec=rec, observed=obs, grid=w.grid))
-        batch = BatchFWI(models, autotune=True)
+        budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
+        batch = BatchFWI(models, autotune=True, level_budget=budget)
         graph_kernels = batch.graph_kernels  # replays launch these without a host call each
         step = batch.run
         updates, bpu = batch.cell_updates, 18.0
         cfg = {"workload": "batch8: 8 models 512^2..1536^2, 1000..3000 steps, 128 shots, Ricker 10..25 Hz, "
-                           "one graph-captured batch gradient (streams per model), autotuned kernels",
+                           "one graph-captured batch gradient (streams per model), autotuned kernels, "
+                           f"kept forward levels in {args.level_store_frac:.0%} of the GPU's memory",
                "models": [[list(m.call.grid.shape), m.call.grid.nt, m.call.problem.nshot] for m in batch.models],
-               "configs": batch.configs}
+               "configs": batch.configs,
+               "store_levels": [m.call.grid.store_levels for m in batch.models]}
     else:
         w = wl("fwi1024" if args.workload == "vd1024" else args.workload, scale=args.scale)
         if args.shots:

@@ -25,7 +25,24 @@ import torch
 
 from . import _lib
 from . import autotune as _autotune
-from .wavefd import Grid, _misfit_gradient_into, _prepare, _workspace
+from .wavefd import Grid, _misfit_gradient_into, _prepare, _workspace, levels_for_budget
+
+
+def _level_shares(models, budget: float) -> list:
+    """Bytes of kept forward levels per model (see BatchFWI)."""
+    if budget <= 0:
+        return [0.0] * len(models)
+    want = []
+    for m in models:
+        g = m["grid"]
+        nx = g.shape[-1]
+        cells = 1
+        for n in g.shape[:-1]:
+            cells *= n
+        cells *= (nx + 7) // 8 * 8
+        want.append(4.0 * cells * m["observed"].shape[0] * (g.nt + 1))
+    total = sum(want)
+    return [min(w, budget * w / total) for w in want]
 
 
 @dataclasses.dataclass
@@ -45,19 +62,29 @@ class BatchFWI:
     src, rec (as for ``wave_forward``), observed (nshot, nt, nrec) CUDA tensor
     and grid (``Grid``). ``autotune`` picks tile_rows / shots_per_cta per
     model; ``graph=False`` runs the same calls eagerly on the streams.
+    ``level_budget`` (bytes) is shared among the models' adjoints for the
+    forward levels they keep instead of recomputing (``Grid.store_levels``),
+    in proportion to the levels each would keep with unlimited memory (a
+    kept level saves one recomputed step of its model, whatever its size, so
+    any split that no model can use up saves the same work); 0 keeps each
+    model's own ``store_levels``.
     """
 
-    def __init__(self, models, *, autotune: bool = True, graph: bool = True, tune_kw=None):
+    def __init__(self, models, *, autotune: bool = True, graph: bool = True, tune_kw=None,
+                 level_budget: float = 0.0):
         if not models:
             raise ValueError("empty batch")
         self.device = models[0]["vel"].device
         self.models = []
-        for m in models:
+        shares = _level_shares(models, level_budget)
+        for m, share in zip(models, shares):
             grid: Grid = m["grid"]
             obs = m["observed"].to(torch.float32).contiguous()
             nshot = obs.shape[0]
             if autotune:
                 grid = _autotune.tuned(grid, nshot, vel=m["vel"], **(tune_kw or {}))
+            if share > 0:
+                grid = dataclasses.replace(grid, store_levels=levels_for_budget(grid, nshot, share))
             call = _prepare(m["vel"], torch.as_tensor(m["wavelet"], device=self.device), m["src"], m["rec"],
                             grid, nshot)
             call.vel = call.vel.clone()  # the batch owns its inputs (set_velocity updates them)

@@ -53,6 +53,29 @@ def test_batch_graph_matches_single_calls(cuda, orc, tmp_path, monkeypatch):
     assert batch.cell_updates > 0
 
 
+def test_batch_level_budget_keeps_levels(cuda, orc, tmp_path, monkeypatch):
+    """A shared budget of kept forward levels: every model keeps some levels
+    (fewer recomputed segments) and the gradients equal the per-model calls
+    that recompute (FP32 checkpoints: the recomputed levels are the kept ones)."""
+    from neuralmech_gb300 import misfit_gradient
+    from neuralmech_gb300.batch import BatchFWI
+    monkeypatch.setenv("WAVEFD_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    models = _models(orc, cuda)
+    level_bytes = [4 * m["grid"].shape[0] * ((m["grid"].shape[1] + 7) // 8 * 8) * m["observed"].shape[0]
+                   for m in models]
+    budget = 0.5 * sum(b * (m["grid"].nt + 1) for b, m in zip(level_bytes, models))
+    batch = BatchFWI(models, autotune=False, level_budget=budget)
+    for x, m in zip(batch.models, models):
+        K = m["grid"].ckpt_every
+        assert x.call.grid.store_levels >= 2 * K + 2  # at least one segment beyond the last
+    J, grads = batch.run()
+    torch.cuda.synchronize()
+    for i, m in enumerate(models):
+        Jr, gr = misfit_gradient(m["vel"], m["wavelet"], m["src"], m["rec"], m["observed"], m["grid"])
+        assert abs(J[i].item() - Jr.item()) <= 1e-9 * Jr.item()
+        assert rel_l2(grads[i].cpu().numpy(), gr.cpu().numpy()) < 1e-6
+
+
 def test_autotune_on_gpu_picks_a_valid_config(cuda, tmp_path, monkeypatch):
     from neuralmech_gb300 import Grid, autotune
     g = Grid((128, 256), (10.0, 10.0), 1e-3, 8)

@@ -337,12 +337,13 @@ def run_other(args):
                                f"Gardner densities, BF16 checkpoints every {g.ckpt_every}",
                    "store_levels": g.store_levels}
         elif args.workload == "fwd2048":
-            g = dataclasses.replace(g, field_format=args.field_format)
+            g = dataclasses.replace(g, field_format=args.field_format,
+                                    step_block=args.step_block if args.field_format == "fp32" else 1)
             step = lambda: wave_forward(v, wav, src, rec, g, check=False)
             updates, bpu = w.nshot * interior * g.nt, 16.0
             cfg = {"workload": f"fwd2048: 2D forward {g.shape[0]}^2, {g.nt} steps, 1 shot, "
                                f"{w.rec.shape[1]} receivers, order 8, 20-cell sponge",
-                   "field_format": g.field_format}
+                   "field_format": g.field_format, "step_block": g.step_block}
             if g.field_format != "fp32":  # the storage error against the FP32 forward
                 ref = wave_forward(v, wav, src, rec, dataclasses.replace(g, field_format="fp32"))
                 got = step()

@@ -101,12 +101,17 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
     // point-list ranges of this tile for every shot of the CTA, staged once:
     // sampling, step-1 (extended region) injection, step-2 injection
     __shared__ int2 smp_rng[T2_MAX_SPC], inje_rng[T2_MAX_SPC], inj_rng[T2_MAX_SPC];
-    // the first stages are issued before the point-list ranges are read, so
-    // that the two memory latencies overlap
+    // launched as a programmatic dependent: every global access comes after the wait
     if (tid == 0) {
         for (int b = 0; b < L::STAGES; ++b) mbar_init(&bars[b], 1);
         fence_mbar_init();
+    }
+    grid_dependency_wait();
+    // the first stages are issued before the point-list ranges are read, so
+    // that the two memory latencies overlap
+    if (tid == 0) {
         for (int i = 0; i < min(ns, L::STAGES); ++i) issue(i);
+        launch_dependents();
     }
     if (tid < ns) {
         const int k = (s0 + tid) * ntiles + tile;
@@ -327,9 +332,9 @@ cudaError_t launch_impl(const CUtensorMap& mu, const CUtensorMap& mo, const CUte
         configured_device = dev;
     }
     const dim3 grid(p.a.tiles_x * p.a.tiles_z, (p.a.nshot + p.a.shots_per_cta - 1) / p.a.shots_per_cta);
-    step2d_k2_kernel<R><<<grid, K2_THREADS, L::BYTES, s>>>(mu, mo, mm, p);
+    const cudaError_t e = launch_pdl(step2d_k2_kernel<R>, grid, dim3(K2_THREADS), L::BYTES, s, mu, mo, mm, p);
     count_launch();
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 }  // namespace

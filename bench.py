@@ -86,6 +86,8 @@ def parse():
                     help="how the gradient obtains the forward levels")
     ap.add_argument("--step-block", type=int, default=1, choices=[1, 2],
                     help="time steps per launch of the forward and the recompute")
+    ap.add_argument("--group-shots", type=int, default=8,
+                    help="fwi384_3d: shots per sequential group (0: all 16 at once)")
     ap.add_argument("--level-store-frac", type=float, default=0.65,
                     help="fraction of the GPU's memory for the forward levels the adjoint keeps "
                          "instead of recomputing them (0: recompute all but the last segment)")
@@ -349,12 +351,13 @@ def run_other(args):
                 got = step()
                 cfg["traces_rel_l2_vs_fp32"] = float((got - ref).norm() / ref.norm())
         else:
-            g = dataclasses.replace(g, group_shots=8)
+            g = dataclasses.replace(g, group_shots=args.group_shots)
             obs = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, g)
             step = lambda: misfit_gradient(v, wav, src, rec, obs, g, check=False)
             updates, bpu = 2.0 * w.nshot * interior * g.nt, 18.0
             cfg = {"workload": f"fwi384_3d: 3D FWI gradient {g.shape[0]}^3, {g.nt} steps, {w.nshot} shots "
-                               f"in groups of 8, {w.rec.shape[1]} receivers per shot, BF16 checkpoints every "
+                               f"in groups of {args.group_shots or w.nshot}, {w.rec.shape[1]} receivers per shot, "
+                               f"BF16 checkpoints every "
                                f"{g.ckpt_every}"}
     if args.once:  # one step, no timing: the command profiled by ncu
         step()

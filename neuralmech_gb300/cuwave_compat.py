@@ -8,7 +8,7 @@ drive the pip package cuwave through a small surface:
 This module offers the same names and call shapes over PyTorch tensors, with
 every time step in the library's CUDA kernels. cuwave's own equations are
 not available (the package is absent), so the choices below are this
-module's own. They are written here so callers can judge parity:
+module's own. They are written here so callers can check parity:
 
 * Material indicator gamma (the reference's "indicator", 1 = solid, ~1e-4 =
   void; plate.py:132-137, helper.py:30-43). It scales the stiffness at

@@ -2,8 +2,8 @@
 (1024 x 1024, 2000 steps, order 8, 20-cell sponge, checkpoints every 45) for
 two of its 64 shots, against the FP64 oracle.
 
-* Forward traces: 1e-5 relative L2 (the benchmark spec's bound against the reference
-  solver; measured 5.7e-7).
+* Forward traces: 1e-5 relative L2 (the trace tolerance of this path against
+  the reference solver; measured 5.7e-7).
 * Gradient: on this workload the residuals are ~3.5e-4 of the traces (the
   2000-step record ends before the deep reflections return), so FP32
   trace rounding (~6e-7), magnified by that ratio, sets the gradient error

@@ -84,6 +84,8 @@ def parse():
                     help="fwd2048: storage of the wavefields (arithmetic stays FP32)")
     ap.add_argument("--adjoint", default="checkpoint", choices=["checkpoint", "reconstruct"],
                     help="how the gradient obtains the forward levels")
+    ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 16, 32],
+                    help="fwd2048: 2D tile height of the one-step kernel (0: the library default)")
     ap.add_argument("--step-block", type=int, default=1, choices=[1, 2],
                     help="time steps per launch of the forward and the recompute")
     ap.add_argument("--group-shots", type=int, default=8,
@@ -339,13 +341,13 @@ def run_other(args):
                                f"Gardner densities, BF16 checkpoints every {g.ckpt_every}",
                    "store_levels": g.store_levels}
         elif args.workload == "fwd2048":
-            g = dataclasses.replace(g, field_format=args.field_format,
+            g = dataclasses.replace(g, field_format=args.field_format, tile_rows=args.tile_rows,
                                     step_block=args.step_block if args.field_format == "fp32" else 1)
             step = lambda: wave_forward(v, wav, src, rec, g, check=False)
             updates, bpu = w.nshot * interior * g.nt, 16.0
             cfg = {"workload": f"fwd2048: 2D forward {g.shape[0]}^2, {g.nt} steps, 1 shot, "
                                f"{w.rec.shape[1]} receivers, order 8, 20-cell sponge",
-                   "field_format": g.field_format, "step_block": g.step_block}
+                   "field_format": g.field_format, "step_block": g.step_block, "tile_rows": g.tile_rows or 32}
             if g.field_format != "fp32":  # the storage error against the FP32 forward
                 ref = wave_forward(v, wav, src, rec, dataclasses.replace(g, field_format="fp32"))
                 got = step()

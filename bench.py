@@ -14,14 +14,20 @@ counted). Algorithmic bytes: 16 B per forward update, 20 B per adjoint update
 pair; "% HBM" = those bytes / time / measured HBM copy bandwidth.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload fwi1024|fwd2048|fwi384_3d|batch8]
+                  [--workload fwi1024|fwd2048|fwi384_3d|batch8|vd1024|temporal]
 
 The other workloads (not the headline) print the same JSON line for:
   fwd2048    2D forward, 2048^2, 4000 steps, one shot (16 B per update);
   fwi384_3d  3D FWI gradient, 384^3, 1500 steps, 16 shots in two sequential
              groups of 8, BF16 checkpoints every 39 (18 B per counted update);
   batch8     8 models 512^2..1536^2, 1000..3000 steps, 128 shots, one
-             graph-captured batch gradient (18 B per counted update).
+             graph-captured batch gradient (18 B per counted update);
+  vd1024     the fwi1024 models with densities, (kappa, rho) gradient;
+  temporal   the padded_step drop-in problem of the reference's temporal
+             driver (8000 x 16000, order 2, Dirichlet): one step = one
+             wfd_temporal_step launch (8 updates), 2 B per update (each
+             launch reads and writes both levels once); the eight-launch
+             wfd_step2d_order2 rate is reported beside it.
 
 Multi-GPU (torchrun, one process per GPU): every rank runs the full 64-shot
 gradient of its own shot set (weak scaling) and the gradients and misfits are
@@ -37,6 +43,7 @@ from __future__ import annotations
 import argparse
 import ctypes
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -94,7 +101,7 @@ def parse():
                     help="fraction of the GPU's memory for the forward levels the adjoint keeps "
                          "instead of recomputing them (0: recompute all but the last segment)")
     ap.add_argument("--workload", default="fwi1024",
-                    choices=["fwi1024", "fwd2048", "fwi384_3d", "batch8", "vd1024"])
+                    choices=["fwi1024", "fwd2048", "fwi384_3d", "batch8", "vd1024", "temporal"])
     return ap.parse_args()
 
 
@@ -283,7 +290,48 @@ def run_other(args):
     dev = torch.device("cuda", 0)
     lib = _lib.load()
     graph_kernels = 0
-    if args.workload == "batch8":
+    extra = {}
+    if args.workload == "temporal":
+        from neuralmech_gb300 import step2d_order2
+        from neuralmech_gb300.wavefd import temporal_step
+        N, M = 8000, 16000  # 2D_wave_cuda_temporal.py:26
+        Mp = (M + 31) // 32 * 32
+        dx, dy = 1.0 / (N - 1), 2.0 / (M - 1)
+        dt = 0.95 * min(dx, dy) / math.sqrt(2)
+        x = torch.linspace(0, 1, N, device=dev)[:, None]
+        y = torch.linspace(0, 2, M, device=dev)[None, :]
+        u0 = torch.zeros((N, Mp), device=dev)
+        u0[:, :M] = torch.exp(-(x - 0.5) ** 2 / (2 * 0.02 ** 2)) * torch.exp(-(y - 0.5) ** 2 / (2 * 0.02 ** 2))
+        bufs = [u0, u0.clone(), torch.empty_like(u0), torch.empty_like(u0)]
+        state = {"k": 0}
+
+        def step():  # the driver's two pairs of arrays, swapped every launch
+            a, b = (0, 1) if state["k"] % 2 == 0 else (2, 3)
+            c, d = (2, 3) if state["k"] % 2 == 0 else (0, 1)
+            temporal_step(bufs[a], bufs[b], bufs[c], bufs[d], 1.0, dt, dx, dy, N, M)
+            state["k"] += 1
+
+        def padded8():
+            p, q = bufs[0], bufs[1]
+            for _ in range(8):
+                p = step2d_order2(p, q, p, 1.0, dt, dx, dy, N, M)
+                p, q = q, p
+        for _ in range(3):
+            padded8()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            padded8()
+        e1.record()
+        torch.cuda.synchronize()
+        inner = (N - 2) * (M - 2)
+        extra["padded_step_gcells"] = 8 * inner * 5 / (e0.elapsed_time(e1) / 1e3) / 1e9
+        updates, bpu = 8.0 * inner, 16.0 / 8
+        cfg = {"workload": f"temporal: wfd_temporal_step, {N} x {M} (M_padded {Mp}), order 2, Dirichlet, "
+                           "8 updates per launch; bytes: both levels read and written once per launch",
+               "l2": "inputs larger than L2 (4 x 512 MB)"}
+    elif args.workload == "batch8":
         from neuralmech_gb300.batch import BatchFWI
         models = []
         for w in wl("batch8"):
@@ -387,6 +435,7 @@ def run_other(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
             "hbm_alg_gbs": gbs, "hbm_frac_measured": gbs / hbm, "peak_source": src_kind, "clocks": clk,
             "gpu_launches": int(lib.wfd_kernel_launches() - n0) + graph_kernels * args.steps}
+    line.update(extra)
     print(json.dumps(line), flush=True)
     return 0
 

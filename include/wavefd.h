@@ -304,6 +304,22 @@ int wfd_step2d_scaled(const int16_t* q0, const float* s0, const int16_t* q1, con
                       int M, int M_padded, void* stream);
 
 /*
+ * Eight padded_step updates in one launch, with temporal_step's arguments and
+ * results: projects/18_simple_wave_fd/step2D_wave.cu:244-304, launched as in
+ * 2D_wave_cuda_temporal.py:68-79. u0 = u_{n-1}, u1 = u_n are [N][M_padded]
+ * FP32; v0 receives u_{n+7} and v1 u_{n+8} on every cell i < N, j < M (the
+ * padding columns are left untouched; boundary cells keep their u0 / u1
+ * values). Each cell follows padded_step's expression in its operation order
+ * (IEEE, no contraction), so the result equals eight launches of the
+ * reference's padded_step source evaluated that way, value for value (the
+ * reference states temporal_step is bit-identical to padded_step). v0 and v1 must
+ * not overlap each other, u0 or u1; M_padded a multiple of 4, pointers 16-byte
+ * aligned.
+ */
+int wfd_temporal_step(const float* u0, const float* u1, float* v0, float* v1, float wavespeed, float dt,
+                      float dx, float dy, int N, int M, int M_padded, void* stream);
+
+/*
  * The 1D 3-point step: step1D, projects/18_simple_wave_fd/step1D_wave.cu:4-17.
  * u0, u1, u2 are FP32 [N]; cells 1..N-2 of u2 receive
  * -u0 + 2 u1 + dt^2 c^2 (u1[i-1] - 2 u1[i] + u1[i+1]) / dx^2. u2 may alias u0.

@@ -117,7 +117,118 @@ __global__ void scaled_kernel(const short* __restrict__ q0, const float* __restr
 
 float kcoef(float c, float dt) { return dt * dt * c * c; }  // as the reference: ((dt dt) c) c
 
+// Eight steps per launch (temporal_step): a CTA stages both levels of a
+// 160 x 48 window (a 144 x 32 output tile plus an 8-cell halo on every side)
+// by TMA, advances them in shared memory, and writes the tile of both final
+// levels. The cells a step can update shrink by one per step from the window
+// edges (the halo is the step count); global boundary cells and cells outside
+// the grid are never updated, exactly as eight padded_step launches.
+constexpr int TT_TX = 144, TT_TZ = 32, TT_H = 8, TT_STEPS = 8;
+constexpr int TT_W = TT_TX + 2 * TT_H;   // 160 staged columns (40 float4)
+constexpr int TT_WZ = TT_TZ + 2 * TT_H;  // 48 staged rows
+constexpr int TT_THREADS = 256;
+constexpr int TT_LEVEL = TT_WZ * TT_W * 4;  // bytes of one staged level
+constexpr int TT_BYTES = 2 * TT_LEVEL + 16 + 128;
+
+__global__ void __launch_bounds__(TT_THREADS)
+    temporal_kernel(const __grid_constant__ CUtensorMap map_u0, const __grid_constant__ CUtensorMap map_u1,
+                    float* __restrict__ v0, float* __restrict__ v1, float k, float dx2, float dy2, int N,
+                    int M, int Mp) {
+    extern __shared__ unsigned char smem_raw[];
+    float* base = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    float* lev[2] = {base, base + TT_WZ * TT_W};
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * TT_WZ * TT_W);
+    const int tid = threadIdx.x;
+    const int j0 = blockIdx.x * TT_TX - TT_H, i0 = blockIdx.y * TT_TZ - TT_H;  // window origin
+
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();  // no thread polls the barrier before it is initialised
+    grid_dependency_wait();
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, 2u * TT_LEVEL);
+        // (the maps are rank 3: x, rows, shot; one shot here)
+        tma_load_3d(lev[0], &map_u0, j0, i0, 0, bar);  // cells outside the grid arrive as 0
+        tma_load_3d(lev[1], &map_u1, j0, i0, 0, bar);
+        launch_dependents();
+    }
+    mbar_wait(bar, 0);  // bounded; every thread goes on to the same barriers either way
+
+    for (int st = 0; st < TT_STEPS; ++st) {
+        float* old = lev[st & 1];              // u_{n-1}, overwritten by u_{n+1}
+        const float* cur = lev[1 - (st & 1)];  // u_n
+        for (int g = tid; g < TT_WZ * (TT_W / 4); g += TT_THREADS) {
+            const int ti = g / (TT_W / 4), tj = 4 * (g - ti * (TT_W / 4));
+            const int i = i0 + ti;
+            if (ti <= st || ti >= TT_WZ - 1 - st || i <= 0 || i >= N - 1) continue;
+            const float* c = cur + ti * TT_W + tj;
+            const float4 cv = *reinterpret_cast<const float4*>(c);
+            const float4 up = *reinterpret_cast<const float4*>(c - TT_W);
+            const float4 dn = *reinterpret_cast<const float4*>(c + TT_W);
+            const float left = tj > 0 ? c[-1] : 0.f, right = tj + 4 < TT_W ? c[4] : 0.f;
+            float4 ov = *reinterpret_cast<const float4*>(old + ti * TT_W + tj);
+            const float cc[6] = {left, cv.x, cv.y, cv.z, cv.w, right};
+            const float uu[4] = {up.x, up.y, up.z, up.w}, dd[4] = {dn.x, dn.y, dn.z, dn.w};
+            float o[4] = {ov.x, ov.y, ov.z, ov.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int te = tj + e, j = j0 + te;
+                if (te > st && te < TT_W - 1 - st && j > 0 && j < M - 1)
+                    o[e] = update2d(o[e], cc[e + 1], uu[e], dd[e], cc[e], cc[e + 2], k, dx2, dy2);
+            }
+            *reinterpret_cast<float4*>(old + ti * TT_W + tj) = make_float4(o[0], o[1], o[2], o[3]);
+        }
+        __syncthreads();
+    }
+
+    // after the eight steps lev[0] holds u_{n+7} and lev[1] u_{n+8}
+    for (int g = tid; g < TT_TZ * (TT_TX / 4); g += TT_THREADS) {
+        const int r = g / (TT_TX / 4), q = 4 * (g - r * (TT_TX / 4));
+        const int i = i0 + TT_H + r, j = j0 + TT_H + q;
+        if (i >= N || j >= M) continue;
+        const float* a = lev[0] + (TT_H + r) * TT_W + TT_H + q;
+        const float* b = lev[1] + (TT_H + r) * TT_W + TT_H + q;
+        const size_t o = (size_t)i * Mp + j;
+        if (j + 3 < M) {
+            *reinterpret_cast<float4*>(v0 + o) = *reinterpret_cast<const float4*>(a);
+            *reinterpret_cast<float4*>(v1 + o) = *reinterpret_cast<const float4*>(b);
+        } else {
+            for (int e = 0; j + e < M; ++e) {
+                v0[o + e] = a[e];
+                v1[o + e] = b[e];
+            }
+        }
+    }
+}
+
 }  // namespace
+
+// the staged window of temporal_kernel: TMA box (columns, rows)
+void temporal_box(unsigned* cols, unsigned* rows) {
+    *cols = TT_W;
+    *rows = TT_WZ;
+}
+
+cudaError_t launch_temporal(const CUtensorMap& m0, const CUtensorMap& m1, float* v0, float* v1, float wavespeed,
+                            float dt, float dx, float dy, int N, int M, int Mp, cudaStream_t s) {
+    static int configured_device = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (configured_device != dev) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(temporal_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TT_BYTES);
+        if (e != cudaSuccess) return e;
+        configured_device = dev;
+    }
+    const dim3 grid((M + TT_TX - 1) / TT_TX, (N + TT_TZ - 1) / TT_TZ);
+    const cudaError_t e = launch_pdl(temporal_kernel, grid, dim3(TT_THREADS), TT_BYTES, s, m0, m1, v0, v1,
+                                     kcoef(wavespeed, dt), dx * dx, dy * dy, N, M, Mp);
+    count_launch();
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
 }  // namespace wfd
 
 using namespace wfd;

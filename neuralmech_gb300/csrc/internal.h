@@ -106,6 +106,11 @@ struct LpArgs {
 // (box 128 x 32 x 1); map_cs / map_os (int16 only): their scale rows (FP32,
 // [shot][z][nblk] with nblk a multiple of 4; boxes 12 x (32 + 2R) x 1 at block
 // x0/32 - 4 and 4 x 32 x 1 at block x0/32).
+// The eight-step drop-in (dropin.cu): maps over u0 and u1 ([N][Mp], extent M)
+// with the box temporal_box() gives.
+void temporal_box(unsigned* cols, unsigned* rows);
+cudaError_t launch_temporal(const CUtensorMap& m0, const CUtensorMap& m1, float* v0, float* v1, float wavespeed,
+                            float dt, float dx, float dy, int N, int M, int Mp, cudaStream_t s);
 cudaError_t launch_step2d_lp(int R, int fmt, const CUtensorMap& map_cur, const CUtensorMap& map_old,
                              const CUtensorMap& map_cs, const CUtensorMap& map_os, const LpArgs& p,
                              cudaStream_t s);

@@ -449,6 +449,16 @@ def step2d_mixed(u0, u1, u2, wavespeed: float, dt: float, dx: float, dy: float, 
     return u2
 
 
+def temporal_step(u0, u1, v0, v1, wavespeed: float, dt: float, dx: float, dy: float, N: int, M: int):
+    """temporal_step (step2D_wave.cu:244-304): eight padded_step updates in one
+    launch; from u0 = u_{n-1}, u1 = u_n ((N, M_padded) float32 CUDA tensors)
+    v0 receives u_{n+7} and v1 u_{n+8}. v0, v1 must be separate tensors."""
+    _check_fields(torch.float32, (("u0", u0), ("u1", u1), ("v0", v0), ("v1", v1)), 2)
+    _lib.check(_lib.load().wfd_temporal_step(_ptr(u0), _ptr(u1), _ptr(v0), _ptr(v1), wavespeed, dt, dx, dy,
+                                             N, M, u1.shape[1], _stream()), "wfd_temporal_step")
+    return v0, v1
+
+
 def step2d_scaled(q0, s0, q1, s1, q2, s2, wavespeed: float, dt: float, dx: float, dy: float, N: int,
                   M: int):
     """scaled_step (step2D_wave.cu:128-183): the padded_step update on int16

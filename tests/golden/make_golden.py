@@ -15,6 +15,11 @@ Outputs (small .npz files, committed):
   scaled_step.npz  the same for scaled_step (int16 + FP32 scale per 32 values),
                    from the NumPy restatement oracle.numpy_ref.scaled_step (the
                    kernel's warp shuffles do not run in the CPU build)
+  temporal_step.npz  two distinct levels (u0, u1) and the level pairs after 8
+                   and 16 padded_step updates: what one and two temporal_step
+                   launches return (step2D_wave.cu:244-304; the reference states
+                   the two kernels are bit-identical, README.md:38-40, and its
+                   block barriers do not run in the CPU build)
 """
 from __future__ import annotations
 
@@ -101,7 +106,34 @@ def main():
             out[f"step{t}"] = b.copy()
     np.savez_compressed(os.path.join(HERE, "step1d.npz"), **out)
     scaled_golden()
+    temporal_golden()
     print("golden vectors written to", HERE)
+
+
+def temporal_golden():
+    out = {}
+    cases = [(67, 150, (1.0, 2.0), 1), (40, 33, (1.0, 1.0), 2), (36, 300, (1.0, 3.0), 3)]
+    for ci, (N, M, L, seed) in enumerate(cases):
+        MP = (M + 31) // 32 * 32
+        dx, dy = L[0] / (N - 1), L[1] / (M - 1)
+        c = 1.0
+        dt = 0.95 * min(dx, dy) / c / math.sqrt(2)
+        u = initial(N, MP, MP, L, seed)
+        u[:, M:] = 0
+        a, b = u.copy(), u.copy()
+        step = lambda a, b: ref.padded_step(a, b, a, np.float32(c), np.float32(dt), np.float32(dx),
+                                            np.float32(dy), N, M)
+        for _ in range(3):  # two distinct levels to start from
+            a = step(a, b)
+            a, b = b, a
+        out[f"c{ci}_u0"], out[f"c{ci}_u1"] = a.copy(), b.copy()
+        out[f"c{ci}_params"] = np.array([N, M, MP, c, dt, dx, dy], dtype=np.float64)
+        for t in range(16):
+            a = step(a, b)
+            a, b = b, a
+            if t == 15 or (t == 7 and ci < 2):
+                out[f"c{ci}_after{t + 1}_v0"], out[f"c{ci}_after{t + 1}_v1"] = a.copy(), b.copy()
+    np.savez_compressed(os.path.join(HERE, "temporal_step.npz"), **out)
 
 
 def scaled_golden():

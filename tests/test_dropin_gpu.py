@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import ROOT
+from conftest import GOLDEN, ROOT
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(ROOT, "tests", "golden")
@@ -110,3 +110,76 @@ def test_storage_error_against_fp32(cuda):
     for fp16, int16 in errs.values():
         assert fp16 < 2e-2 and int16 < 2e-3
         assert int16 < fp16
+
+
+def test_temporal_step_matches_golden_bitwise(cuda):
+    """wfd_temporal_step: one launch = eight padded_step updates, two launches
+    = sixteen; v0 = u_{n+7}, v1 = u_{n+8} equal the reference's host build bit
+    for bit on every written cell, and the padding columns stay untouched."""
+    from neuralmech_gb300.wavefd import temporal_step
+    g = np.load(os.path.join(GOLDEN, "temporal_step.npz"))
+    for ci in range(3):
+        N, M, MP, c, dt, dx, dy = g[f"c{ci}_params"]
+        N, M = int(N), int(M)
+        args = (float(np.float32(c)), float(np.float32(dt)), float(np.float32(dx)), float(np.float32(dy)), N, M)
+        u0 = torch.from_numpy(g[f"c{ci}_u0"]).to(cuda)
+        u1 = torch.from_numpy(g[f"c{ci}_u1"]).to(cuda)
+        v0 = torch.full_like(u0, 7.0)
+        v1 = torch.full_like(u0, 7.0)
+        temporal_step(u0, u1, v0, v1, *args)
+        if f"c{ci}_after8_v0" in g:
+            assert np.array_equal(v0.cpu().numpy()[:, :M], g[f"c{ci}_after8_v0"][:, :M]), ci
+            assert np.array_equal(v1.cpu().numpy()[:, :M], g[f"c{ci}_after8_v1"][:, :M]), ci
+            assert torch.all(v0[:, M:] == 7.0) and torch.all(v1[:, M:] == 7.0)
+        w0, w1 = torch.empty_like(u0), torch.empty_like(u0)
+        temporal_step(v0, v1, w0, w1, *args)
+        assert np.array_equal(w0.cpu().numpy()[:, :M], g[f"c{ci}_after16_v0"][:, :M]), ci
+        assert np.array_equal(w1.cpu().numpy()[:, :M], g[f"c{ci}_after16_v1"][:, :M]), ci
+
+
+def test_temporal_step_many_tiles_bitwise(cuda):
+    """A grid of several CTA waves (1000 x 3000): two launches equal sixteen
+    padded_step updates restated in PyTorch FP32 (one rounded operation per
+    term, the kernel's order), value for value."""
+    from neuralmech_gb300.wavefd import temporal_step
+    N, M = 1000, 3000
+    Mp = (M + 31) // 32 * 32
+    f = np.float32
+    dx, dy = f(1.0 / (N - 1)), f(2.0 / (M - 1))
+    dt = f(0.95 * min(dx, dy) / math.sqrt(2))
+    k = torch.tensor(dt * dt * f(1.0) * f(1.0), device=cuda)
+    dx2, dy2 = torch.tensor(dx * dx, device=cuda), torch.tensor(dy * dy, device=cuda)
+    g = torch.Generator(device="cpu").manual_seed(5)
+    u0 = torch.zeros((N, Mp))
+    u0[:, :M] = torch.rand((N, M), generator=g) - 0.5
+    u1 = u0.clone()
+    u1[:, :M] += 0.01 * (torch.rand((N, M), generator=g) - 0.5)
+    u0, u1 = u0.to(cuda), u1.to(cuda)
+
+    def padded(a, b):  # the in-place padded_step update of a from b
+        c = b[1:-1, 1:M - 1]
+        two = 2.0 * c
+        li = (b[:-2, 1:M - 1] - two) + b[2:, 1:M - 1]
+        lj = (b[1:-1, :M - 2] - two) + b[1:-1, 2:M]
+        a[1:-1, 1:M - 1] = (-a[1:-1, 1:M - 1] + two) + k * (li / dx2 + lj / dy2)
+        return a
+
+    a, b = u0.clone(), u1.clone()
+    for _ in range(16):
+        a = padded(a, b)
+        a, b = b, a
+    v0, v1 = torch.empty_like(u0), torch.empty_like(u0)
+    w0, w1 = torch.empty_like(u0), torch.empty_like(u0)
+    args = (1.0, float(dt), float(dx), float(dy), N, M)
+    temporal_step(u0, u1, v0, v1, *args)
+    temporal_step(v0, v1, w0, w1, *args)
+    assert torch.equal(w0[:, :M], a[:, :M]) and torch.equal(w1[:, :M], b[:, :M])
+
+
+def test_temporal_step_rejects_overlapping_outputs(cuda):
+    from neuralmech_gb300 import _lib
+    from neuralmech_gb300.wavefd import temporal_step
+    u = torch.zeros((20, 64), device=cuda)
+    with pytest.raises(_lib.WaveFDError):
+        temporal_step(u, u.clone(), u, torch.zeros_like(u), 1.0, 1e-3, 0.1, 0.1, 20, 60)
+

@@ -62,6 +62,31 @@ def test_numpy_fd_step_is_reference_bitwise():
     assert rel_l2(u2, g["c0_step0"][:, :M]) < 1e-6
 
 
+def test_temporal_golden_is_padded_restatement():
+    """temporal_step's golden levels (eight and sixteen padded_step updates of
+    the reference's host build) equal the NumPy restatement of the padded_step
+    expression (oracle.numpy_ref._update_order2, FP32, the kernel's operation
+    order) bit for bit, on every cell the steps update."""
+    from oracle import numpy_ref
+    g = np.load(os.path.join(GOLDEN, "temporal_step.npz"))
+    f32 = np.float32
+    for ci in range(3):
+        N, M, MP, c, dt, dx, dy = g[f"c{ci}_params"]
+        N, M = int(N), int(M)
+        k = f32(dt) * f32(dt) * f32(c) * f32(c)
+        dx2, dy2 = f32(dx) * f32(dx), f32(dy) * f32(dy)
+        a, b = g[f"c{ci}_u0"].copy(), g[f"c{ci}_u1"].copy()
+        for t in range(16):
+            new = a.copy()
+            new[1:-1, 1:M - 1] = numpy_ref._update_order2(
+                a[1:-1, 1:M - 1], b[1:-1, 1:M - 1], b[:-2, 1:M - 1], b[2:, 1:M - 1], b[1:-1, :M - 2],
+                b[1:-1, 2:M], k, dx2, dy2)
+            a, b = b, new
+            key = f"c{ci}_after{t + 1}_v0"
+            if key in g:
+                assert np.array_equal(a, g[key]) and np.array_equal(b, g[f"c{ci}_after{t + 1}_v1"]), (ci, t)
+
+
 def test_step1d_golden_vs_oracle(orc):
     """step1D (step1D_wave.cu:4-17) as the 1-row special case of the oracle."""
     g = np.load(os.path.join(GOLDEN, "step1d.npz"))

@@ -27,7 +27,7 @@ The other workloads (not the headline) print the same JSON line for:
              driver (8000 x 16000, order 2, Dirichlet): one step = one
              wfd_temporal_step launch (8 updates), 2 B per update (each
              launch reads and writes both levels once); the eight-launch
-             wfd_step2d_order2 rate is reported beside it.
+             wfd_step2d_order2 and wfd_step2d_exact rates are reported beside it.
 
 Multi-GPU (torchrun, one process per GPU): every rank runs the full 64-shot
 gradient of its own shot set (weak scaling) and the gradients and misfits are
@@ -293,7 +293,7 @@ def run_other(args):
     extra = {}
     if args.workload == "temporal":
         from neuralmech_gb300 import step2d_order2
-        from neuralmech_gb300.wavefd import temporal_step
+        from neuralmech_gb300.wavefd import step2d_exact, temporal_step
         N, M = 8000, 16000  # 2D_wave_cuda_temporal.py:26
         Mp = (M + 31) // 32 * 32
         dx, dy = 1.0 / (N - 1), 2.0 / (M - 1)
@@ -311,22 +311,23 @@ def run_other(args):
             temporal_step(bufs[a], bufs[b], bufs[c], bufs[d], 1.0, dt, dx, dy, N, M)
             state["k"] += 1
 
-        def padded8():
-            p, q = bufs[0], bufs[1]
-            for _ in range(8):
-                p = step2d_order2(p, q, p, 1.0, dt, dx, dy, N, M)
-                p, q = q, p
-        for _ in range(3):
-            padded8()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(5):
-            padded8()
-        e1.record()
-        torch.cuda.synchronize()
         inner = (N - 2) * (M - 2)
-        extra["padded_step_gcells"] = 8 * inner * 5 / (e0.elapsed_time(e1) / 1e3) / 1e9
+        for name, fn in (("padded_step_gcells", step2d_order2), ("exact_step_gcells", step2d_exact)):
+            def eight():
+                p, q = bufs[0], bufs[1]
+                for _ in range(8):
+                    p = fn(p, q, p, 1.0, dt, dx, dy, N, M)
+                    p, q = q, p
+            for _ in range(3):
+                eight()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(5):
+                eight()
+            e1.record()
+            torch.cuda.synchronize()
+            extra[name] = 8 * inner * 5 / (e0.elapsed_time(e1) / 1e3) / 1e9
         updates, bpu = 8.0 * inner, 16.0 / 8
         cfg = {"workload": f"temporal: wfd_temporal_step, {N} x {M} (M_padded {Mp}), order 2, Dirichlet, "
                            "8 updates per launch; bytes: both levels read and written once per launch",

@@ -256,6 +256,18 @@ int wfd_step2d_order2(const float* u0, const float* u1, float* u2, float wavespe
                       float dx, float dy, int N, int M, int M_padded, void* stream);
 
 /*
+ * The same order-2 step evaluated as the reference kernels evaluate it, value
+ * for value, for any row stride: padded_step and shared_step
+ * (step2D_wave.cu:59-81, 187-240) with M_padded, basic_step and
+ * coalesced_step (step2D_wave.cu:8-55, launched as in 2D_wave_cuda_basic.py /
+ * 2D_wave_cuda_coalesced.py) with M_padded = M. Each cell follows the
+ * kernels' expression in its operation order (IEEE, no contraction); no
+ * alignment requirement. u2 may alias u0.
+ */
+int wfd_step2d_exact(const float* u0, const float* u1, float* u2, float wavespeed, float dt, float dx,
+                     float dy, int N, int M, int M_padded, void* stream);
+
+/*
  * Variable density (2D): the conservative acoustic operator
  *     u_{n+1} = g (2 u_n + k Lb u_n + src_scale * w_n) - g^2 u_{n-1},
  *     k = kappa dt^2 / dx^2,  Lb u = Dx^- (b Dx^+ u) + (dx/dz)^2 Dz^- (b Dz^+ u),

@@ -28,7 +28,7 @@ EXPORTS = (
     "wfd_backward", "wfd_misfit_gradient", "wfd_status", "wfd_sum_sq", "wfd_step2d_order2",
     "wfd_kernel_launches", "wfd_profile_begin", "wfd_profile_end", "wfd_forward_static",
     "wfd_analytic_signal", "wfd_tfm", "wfd_forward_final", "wfd_step2d_mixed", "wfd_step2d_scaled",
-    "wfd_temporal_step",
+    "wfd_temporal_step", "wfd_step2d_exact",
     "wfd_step1d", "wfd_vd_workspace_bytes", "wfd_vd_forward", "wfd_vd_misfit_gradient",
 )
 
@@ -103,6 +103,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         lib.wfd_tfm.argtypes = [f, I, f, f, I, F, F, F, f, f, I, I, f, vp]
         lib.wfd_step2d_mixed.argtypes = [vp, vp, vp, F, F, F, F, I, I, I, vp]
         lib.wfd_temporal_step.argtypes = [vp, vp, vp, vp, F, F, F, F, I, I, I, vp]
+        lib.wfd_step2d_exact.argtypes = [vp, vp, vp, F, F, F, F, I, I, I, vp]
         lib.wfd_step2d_scaled.argtypes = [vp, f, vp, f, vp, f, F, F, F, F, I, I, I, vp]
         lib.wfd_step1d.argtypes = [f, f, f, F, F, F, I, vp]
         lib.wfd_vd_workspace_bytes.argtypes = [P, ctypes.c_int, ctypes.POINTER(sz)]

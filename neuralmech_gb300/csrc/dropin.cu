@@ -41,6 +41,27 @@ __global__ void step1d_kernel(const float* __restrict__ u0, const float* __restr
     u2[i] = __fadd_rn(__fadd_rn(-u0[i], __fmul_rn(2.f, c)), __fmul_rn(k, lap));
 }
 
+// FP32 storage with any row stride (padded_step / shared_step with M_padded,
+// basic_step / coalesced_step with M_padded = M): a thread owns 4 consecutive
+// cells j .. j + 3 of row i, read and written as scalars (rows need not be
+// 16-byte aligned).
+__global__ void exact_kernel(const float* __restrict__ u0, const float* __restrict__ u1,
+                             float* __restrict__ u2, float k, float dx2, float dy2, int N, int M, int Mp) {
+    const int j = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i <= 0 || i >= N - 1 || j >= M - 1) return;
+    const size_t c = (size_t)i * Mp + j;
+    float w[6];  // u1 at j - 1 .. j + 4 of row i
+#pragma unroll
+    for (int e = 0; e < 6; ++e) w[e] = (j - 1 + e >= 0 && j - 1 + e < M) ? u1[c - 1 + e] : 0.f;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int je = j + e;
+        if (je == 0 || je >= M - 1) continue;  // the boundary columns (and beyond) stay untouched
+        u2[c + e] = update2d(u0[c + e], w[e + 1], u1[c + e - Mp], u1[c + e + Mp], w[e], w[e + 2], k, dx2, dy2);
+    }
+}
+
 // FP16 storage: a thread owns the pair (j, j + 1), j even, of row i, loaded and
 // stored as one __half2.
 __global__ void mixed_kernel(const __half* __restrict__ u0, const __half* __restrict__ u1,
@@ -247,6 +268,20 @@ int wfd_step1d(const float* u0, const float* u1, float* u2, float wavespeed, flo
     return e == cudaSuccess ? WFD_OK : set_error(WFD_ERR_CUDA, cudaGetErrorString(e));
 }
 
+int wfd_step2d_exact(const float* u0, const float* u1, float* u2, float wavespeed, float dt, float dx,
+                     float dy, int N, int M, int M_padded, void* stream) {
+    if (!u0 || !u1 || !u2) return set_error(WFD_ERR_INVALID, "NULL field");
+    if (N < 3 || M < 3 || M_padded < M) return set_error(WFD_ERR_INVALID, "need N, M >= 3 and M_padded >= M");
+    if ((long long)N * M_padded >= (1ll << 31)) return set_error(WFD_ERR_INVALID, "grid too large");
+    if ((N + 3) / 4 > 65535) return set_error(WFD_ERR_INVALID, "N too large (more than 262140 rows)");
+    const dim3 block(64, 4), grid(((M + 3) / 4 + 63) / 64, (N + 3) / 4);
+    exact_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(u0, u1, u2, kcoef(wavespeed, dt), dx * dx,
+                                                                        dy * dy, N, M, M_padded);
+    count_launch();
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? WFD_OK : set_error(WFD_ERR_CUDA, cudaGetErrorString(e));
+}
+
 int wfd_step2d_mixed(const void* u0, const void* u1, void* u2, float wavespeed, float dt, float dx,
                      float dy, int N, int M, int M_padded, void* stream) {
     if (!u0 || !u1 || !u2) return set_error(WFD_ERR_INVALID, "NULL field");
@@ -256,6 +291,7 @@ int wfd_step2d_mixed(const void* u0, const void* u1, void* u2, float wavespeed, 
         reinterpret_cast<uintptr_t>(u2) % 4)
         return set_error(WFD_ERR_INVALID, "fields must be 4-byte aligned");
     if ((long long)N * M_padded >= (1ll << 31)) return set_error(WFD_ERR_INVALID, "grid too large");
+    if ((N + 3) / 4 > 65535) return set_error(WFD_ERR_INVALID, "N too large (more than 262140 rows)");
     const dim3 block(128, 4), grid((M_padded / 2 + 127) / 128, (N + 3) / 4);
     mixed_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const __half*>(u0), static_cast<const __half*>(u1), static_cast<__half*>(u2),
@@ -274,6 +310,7 @@ int wfd_step2d_scaled(const int16_t* q0, const float* s0, const int16_t* q1, con
     for (const void* p : {(const void*)q0, (const void*)q1, (const void*)q2})
         if (reinterpret_cast<uintptr_t>(p) % 8) return set_error(WFD_ERR_INVALID, "q fields must be 8-byte aligned");
     if ((long long)N * M_padded >= (1ll << 31)) return set_error(WFD_ERR_INVALID, "grid too large");
+    if ((N + 3) / 4 > 65535) return set_error(WFD_ERR_INVALID, "N too large (more than 262140 rows)");
     const dim3 block(64, 4), grid((M_padded / 4 + 63) / 64, (N + 3) / 4);
     scaled_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(
         q0, s0, q1, s1, q2, s2, kcoef(wavespeed, dt), dx * dx, dy * dy, N, M, M_padded);

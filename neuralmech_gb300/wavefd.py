@@ -449,6 +449,16 @@ def step2d_mixed(u0, u1, u2, wavespeed: float, dt: float, dx: float, dy: float, 
     return u2
 
 
+def step2d_exact(u0, u1, u2, wavespeed: float, dt: float, dx: float, dy: float, N: int, M: int):
+    """padded_step / shared_step (M_padded = u1.shape[1]) or basic_step /
+    coalesced_step (M_padded = M) evaluated as the reference kernels evaluate
+    them, value for value; (N, M_padded) float32 CUDA tensors, u2 may be u0."""
+    _check_fields(torch.float32, (("u0", u0), ("u1", u1), ("u2", u2)), 2)
+    _lib.check(_lib.load().wfd_step2d_exact(_ptr(u0), _ptr(u1), _ptr(u2), wavespeed, dt, dx, dy,
+                                            N, M, u1.shape[1], _stream()), "wfd_step2d_exact")
+    return u2
+
+
 def temporal_step(u0, u1, v0, v1, wavespeed: float, dt: float, dx: float, dy: float, N: int, M: int):
     """temporal_step (step2D_wave.cu:244-304): eight padded_step updates in one
     launch; from u0 = u_{n-1}, u1 = u_n ((N, M_padded) float32 CUDA tensors)

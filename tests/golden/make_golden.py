@@ -107,7 +107,28 @@ def main():
     np.savez_compressed(os.path.join(HERE, "step1d.npz"), **out)
     scaled_golden()
     temporal_golden()
+    basic_golden()
     print("golden vectors written to", HERE)
+
+
+def basic_golden():
+    """basic_step and coalesced_step (unpadded rows, M_padded = M) from the
+    reference's host build: a few steps with the driver's in-place rotation."""
+    out = {}
+    for ci, (N, M, L, steps, seed) in enumerate(CASES):
+        dx, dy = L[0] / (N - 1), L[1] / (M - 1)
+        c = 1.0
+        dt = 0.95 * min(dx, dy) / c / math.sqrt(2)
+        u = initial(N, M, M, L, seed)
+        out[f"c{ci}_u0"] = u.copy()
+        out[f"c{ci}_params"] = np.array([N, M, steps, c, dt, dx, dy], dtype=np.float64)
+        for name, fn in (("basic", ref.basic_step), ("coalesced", ref.coalesced_step)):
+            a, b = u.copy(), u.copy()
+            for t in range(steps):
+                a = fn(a, b, a, np.float32(c), np.float32(dt), np.float32(dx), np.float32(dy))
+                a, b = b, a
+            out[f"c{ci}_{name}_last"] = b.copy()
+    np.savez_compressed(os.path.join(HERE, "basic_step.npz"), **out)
 
 
 def temporal_golden():

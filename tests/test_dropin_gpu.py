@@ -137,6 +137,42 @@ def test_temporal_step_matches_golden_bitwise(cuda):
         assert np.array_equal(w1.cpu().numpy()[:, :M], g[f"c{ci}_after16_v1"][:, :M]), ci
 
 
+def test_step2d_exact_matches_padded_step_bitwise(cuda):
+    """wfd_step2d_exact with M_padded: padded_step's host build value for value
+    over the golden runs (in-place rotation), padding columns untouched."""
+    from neuralmech_gb300.wavefd import step2d_exact
+    g = np.load(os.path.join(GOLDEN, "padded_step.npz"))
+    for ci in range(2):
+        N, M, MP, steps, c, dt, dx, dy = g[f"c{ci}_params"]
+        N, M, steps = int(N), int(M), int(steps)
+        a = torch.from_numpy(g[f"c{ci}_u0"]).to(cuda)
+        b = torch.from_numpy(g[f"c{ci}_u1"]).to(cuda)
+        for t in range(steps):
+            a = step2d_exact(a, b, a, float(np.float32(c)), float(np.float32(dt)), float(np.float32(dx)),
+                             float(np.float32(dy)), N, M)
+            a, b = b, a
+            if f"c{ci}_step{t}" in g:
+                assert np.array_equal(b.cpu().numpy(), g[f"c{ci}_step{t}"]), (ci, t)
+
+
+def test_step2d_exact_matches_basic_and_coalesced_step(cuda):
+    """Unpadded rows (M_padded = M, odd M: rows not 16-byte aligned):
+    basic_step's and coalesced_step's host builds value for value."""
+    from neuralmech_gb300.wavefd import step2d_exact
+    g = np.load(os.path.join(GOLDEN, "basic_step.npz"))
+    for ci in range(2):
+        N, M, steps, c, dt, dx, dy = g[f"c{ci}_params"]
+        N, M, steps = int(N), int(M), int(steps)
+        a = torch.from_numpy(g[f"c{ci}_u0"]).to(cuda)
+        b = a.clone()
+        for _ in range(steps):
+            a = step2d_exact(a, b, a, float(np.float32(c)), float(np.float32(dt)), float(np.float32(dx)),
+                             float(np.float32(dy)), N, M)
+            a, b = b, a
+        got = b.cpu().numpy()
+        assert np.array_equal(got, g[f"c{ci}_basic_last"]) and np.array_equal(got, g[f"c{ci}_coalesced_last"])
+
+
 def test_temporal_step_many_tiles_bitwise(cuda):
     """A grid of several CTA waves (1000 x 3000): two launches equal sixteen
     padded_step updates restated in PyTorch FP32 (one rounded operation per

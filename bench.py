@@ -14,7 +14,7 @@ counted). Algorithmic bytes: 16 B per forward update, 20 B per adjoint update
 pair; "% HBM" = those bytes / time / measured HBM copy bandwidth.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload fwi1024|fwd2048|fwi384_3d|batch8|vd1024|temporal]
+                  [--workload fwi1024|fwd2048|fwi384_3d|batch8|vd1024|temporal|fmc_tfm]
 
 The other workloads (not the headline) print the same JSON line for:
   fwd2048    2D forward, 2048^2, 4000 steps, one shot (16 B per update);
@@ -27,7 +27,11 @@ The other workloads (not the headline) print the same JSON line for:
              driver (8000 x 16000, order 2, Dirichlet): one step = one
              wfd_temporal_step launch (8 updates), 2 B per update (each
              launch reads and writes both levels once); the eight-launch
-             wfd_step2d_order2 and wfd_step2d_exact rates are reported beside it.
+             wfd_step2d_order2 and wfd_step2d_exact rates are reported beside it;
+  fmc_tfm    the ultrasonic plate pipeline: full matrix capture (32 elements
+             on a 512^2 plate, order 8, 2.5 traversals), analytic signal and
+             total focusing onto 512^2 pixels; value = capture cell-updates/s,
+             the per-stage times beside it.
 
 Multi-GPU (torchrun, one process per GPU): every rank runs the full 64-shot
 gradient of its own shot set (weak scaling) and the gradients and misfits are
@@ -101,7 +105,7 @@ def parse():
                     help="fraction of the GPU's memory for the forward levels the adjoint keeps "
                          "instead of recomputing them (0: recompute all but the last segment)")
     ap.add_argument("--workload", default="fwi1024",
-                    choices=["fwi1024", "fwd2048", "fwi384_3d", "batch8", "vd1024", "temporal"])
+                    choices=["fwi1024", "fwd2048", "fwi384_3d", "batch8", "vd1024", "temporal", "fmc_tfm"])
     return ap.parse_args()
 
 
@@ -332,6 +336,49 @@ def run_other(args):
         cfg = {"workload": f"temporal: wfd_temporal_step, {N} x {M} (M_padded {Mp}), order 2, Dirichlet, "
                            "8 updates per launch; bytes: both levels read and written once per launch",
                "l2": "inputs larger than L2 (4 x 512 MB)"}
+    elif args.workload == "fmc_tfm":
+        from neuralmech_gb300 import Grid
+        from neuralmech_gb300.cuwave_compat import sineburst, stable_dt
+        from neuralmech_gb300.imaging import analytic_signal, full_matrix_capture, tfm
+        n, E, c = 512, 32, 1.0  # projects/18_fwi/plate.py:19-32
+        h = 1.0 / (n - 3)
+        dt0 = 0.9 * stable_dt((h, h), c, 8)
+        nt = math.ceil(2.5 / dt0) + 1
+        dt = 2.5 / (nt - 1)
+        grid = Grid((n, n), (h, h), dt, nt, order=8, sponge=0)
+        cols = np.round(np.linspace(0.1, 0.9, E) * (n - 1)).astype(np.int32)
+        el_cells = np.stack([np.full(E, 4, np.int32), cols], axis=1)       # (z, x): the top edge
+        el_xy = np.stack([cols * h, np.full(E, 4 * h)], axis=1)            # (x, y) in plate units
+        vel = torch.full((n, n), c, device=dev)
+        rng = np.random.default_rng(0)
+        for _ in range(4):  # circular slow voids (synthetic stand-ins for the plate's voids)
+            zc, xc, r = rng.uniform(0.3, 0.8) * n, rng.uniform(0.3, 0.7) * n, rng.uniform(0.02, 0.05) * n
+            zz, xx = torch.meshgrid(torch.arange(n, device=dev), torch.arange(n, device=dev), indexing="ij")
+            vel[(zz - zc) ** 2 + (xx - xc) ** 2 < r * r] = 0.5 * c
+        wav = torch.from_numpy(sineburst(np.arange(nt) * dt, 1.0, 20.0, 2)).to(dev)
+        px = torch.linspace(0, 1, 512, device=dev)
+        X, Y = torch.meshgrid(px, px, indexing="ij")
+        t0 = 2 / (2 * 20.0)
+        stage_ms = {"capture": [], "analytic": [], "tfm": []}
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
+        def step():
+            evs[0].record()
+            traces = full_matrix_capture(vel, wav, el_cells, grid)          # (E, nt, E)
+            evs[1].record()
+            hs = analytic_signal(traces.permute(0, 2, 1).contiguous())       # (E, E, nt)
+            evs[2].record()
+            tfm(hs, el_xy, t0, dt, c, X, Y)
+            evs[3].record()
+            torch.cuda.synchronize()
+            for k, name in enumerate(("capture", "analytic", "tfm")):
+                stage_ms[name].append(evs[k].elapsed_time(evs[k + 1]))
+        R = 4
+        updates, bpu = float(E) * (n - 2 * R) ** 2 * nt, 16.0
+        extra["stage_ms"] = stage_ms  # averaged over the timed calls below
+        cfg = {"workload": f"fmc_tfm: full matrix capture, {E} elements on a {n}^2 plate, {nt} steps, order 8, "
+                           "4 slow voids; analytic signal; TFM onto 512^2 pixels with reciprocity",
+               "pixels": 512 * 512, "traces": E * E, "samples": nt}
     elif args.workload == "batch8":
         from neuralmech_gb300.batch import BatchFWI
         models = []
@@ -436,6 +483,8 @@ def run_other(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
             "hbm_alg_gbs": gbs, "hbm_frac_measured": gbs / hbm, "peak_source": src_kind, "clocks": clk,
             "gpu_launches": int(lib.wfd_kernel_launches() - n0) + graph_kernels * args.steps}
+    if "stage_ms" in extra:
+        extra["stage_ms"] = {k: sum(v[-args.steps:]) / args.steps for k, v in extra["stage_ms"].items()}
     line.update(extra)
     print(json.dumps(line), flush=True)
     return 0

@@ -147,7 +147,8 @@ float kcoef(float c, float dt) { return dt * dt * c * c; }  // as the reference:
 constexpr int TT_TX = 144, TT_TZ = 32, TT_H = 8, TT_STEPS = 8;
 constexpr int TT_W = TT_TX + 2 * TT_H;   // 160 staged columns (40 float4)
 constexpr int TT_WZ = TT_TZ + 2 * TT_H;  // 48 staged rows
-constexpr int TT_THREADS = 256;
+constexpr int TT_THREADS = 320;  // 8 rows x 40 float4 columns per pass
+constexpr int TT_PASSES = TT_WZ / 8;  // 6 row passes per step
 constexpr int TT_LEVEL = TT_WZ * TT_W * 4;  // bytes of one staged level
 constexpr int TT_BYTES = 2 * TT_LEVEL + 16 + 128;
 
@@ -177,11 +178,14 @@ __global__ void __launch_bounds__(TT_THREADS)
     }
     mbar_wait(bar, 0);  // bounded; every thread goes on to the same barriers either way
 
+    // a thread owns the float4 column tj of rows r0, r0 + 8, ..., r0 + 40
+    const int tj = 4 * (tid % (TT_W / 4)), r0 = tid / (TT_W / 4);
     for (int st = 0; st < TT_STEPS; ++st) {
         float* old = lev[st & 1];              // u_{n-1}, overwritten by u_{n+1}
         const float* cur = lev[1 - (st & 1)];  // u_n
-        for (int g = tid; g < TT_WZ * (TT_W / 4); g += TT_THREADS) {
-            const int ti = g / (TT_W / 4), tj = 4 * (g - ti * (TT_W / 4));
+#pragma unroll 3
+        for (int ps = 0; ps < TT_PASSES; ++ps) {
+            const int ti = r0 + 8 * ps;
             const int i = i0 + ti;
             if (ti <= st || ti >= TT_WZ - 1 - st || i <= 0 || i >= N - 1) continue;
             const float* c = cur + ti * TT_W + tj;

@@ -612,12 +612,21 @@ def main():
         h2d = sum(x.numel() * x.element_size() for x in host.values()) + src.numel() * 4 + rec.numel() * 4
         d2h = grad_h.numel() * 4 + 8
 
+        # the observed traces (most of the bytes) go up on a second stream while
+        # the forward runs; the call waits for them only before the residual
+        copy_stream = torch.cuda.Stream(device=dev)
+        ob = torch.empty(host["obs"].shape, dtype=torch.float32, device=dev)
+        ob_ready = torch.cuda.Event()
+
         def e2e_step():
+            copy_stream.wait_stream(torch.cuda.current_stream(dev))  # the previous step's reads of ob
+            with torch.cuda.stream(copy_stream):
+                ob.copy_(host["obs"], non_blocking=True)
+                ob_ready.record(copy_stream)
             v = host["vel"].to(dev, non_blocking=True)
             wv = host["wav"].to(dev, non_blocking=True)
-            ob = host["obs"].to(dev, non_blocking=True)
             J2, g2 = misfit_gradient(v, wv, src.to(dev, non_blocking=True), rec.to(dev, non_blocking=True),
-                                     ob, g, check=False)
+                                     ob, g, check=False, observed_ready=ob_ready)
             if world > 1:
                 dist.all_reduce(g2)
                 dist.all_reduce(J2)

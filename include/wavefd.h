@@ -174,6 +174,20 @@ int wfd_misfit_gradient(const wfd_problem* p, const float* vel, const float* spo
                         void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * wfd_misfit_gradient for observed traces that are still arriving: the call
+ * makes `stream` wait for `observed_ready` (a cudaEvent_t passed as void*,
+ * recorded by the caller after it enqueued the copy of `observed`, e.g. on a
+ * second stream) just before its first read of `observed`, which comes after
+ * the forward. A host-to-device copy of the observed data then overlaps the
+ * forward. No counterpart in the reference.
+ */
+int wfd_misfit_gradient_overlap(const wfd_problem* p, const float* vel, const float* sponge_z,
+                                const float* sponge_y, const float* sponge_x, const float* wavelet,
+                                const int32_t* src, const int32_t* rec, const float* observed,
+                                void* observed_ready, float* traces, float* grad_vel, float* grad_wavelet,
+                                double* misfit, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * Allocation-free variant of wfd_forward (no checkpoints): the same forward,
  * with its scratch in a 64 MiB array that the library holds on every device it
  * is loaded on, for callers that cannot allocate device memory (a host

@@ -28,7 +28,7 @@ EXPORTS = (
     "wfd_backward", "wfd_misfit_gradient", "wfd_status", "wfd_sum_sq", "wfd_step2d_order2",
     "wfd_kernel_launches", "wfd_profile_begin", "wfd_profile_end", "wfd_forward_static",
     "wfd_analytic_signal", "wfd_tfm", "wfd_forward_final", "wfd_step2d_mixed", "wfd_step2d_scaled",
-    "wfd_temporal_step", "wfd_step2d_exact",
+    "wfd_temporal_step", "wfd_step2d_exact", "wfd_misfit_gradient_overlap",
     "wfd_step1d", "wfd_vd_workspace_bytes", "wfd_vd_forward", "wfd_vd_misfit_gradient",
 )
 
@@ -92,6 +92,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         lib.wfd_forward.argtypes = [P, f, f, f, f, f, i32, i32, f, ctypes.c_int, vp, sz, vp]
         lib.wfd_backward.argtypes = [P, f, f, f, f, f, i32, i32, f, f, f, vp, sz, vp]
         lib.wfd_misfit_gradient.argtypes = [P, f, f, f, f, f, i32, i32, f, f, f, f, d, vp, sz, vp]
+        lib.wfd_misfit_gradient_overlap.argtypes = [P, f, f, f, f, f, i32, i32, f, vp, f, f, f, d, vp, sz, vp]
         lib.wfd_status.argtypes = [vp, vp]
         lib.wfd_sum_sq.argtypes = [f, ctypes.c_int64, d, vp]
         lib.wfd_step2d_order2.argtypes = [f, f, f, ctypes.c_float, ctypes.c_float, ctypes.c_float,

@@ -1288,11 +1288,15 @@ int wfd_backward(const wfd_problem* p, const float* vel, const float* sponge_z,
     return run_backward(p, g, L, w, st, wavelet, dtraces, grad_vel, grad_wavelet, vel);
 }
 
-int wfd_misfit_gradient(const wfd_problem* p, const float* vel, const float* sponge_z,
-                        const float* sponge_y, const float* sponge_x, const float* wavelet,
-                        const int32_t* src, const int32_t* rec, const float* observed,
-                        float* traces, float* grad_vel, float* grad_wavelet, double* misfit,
-                        void* workspace, size_t workspace_bytes, void* stream) {
+namespace {
+
+// The misfit gradient; when `observed_ready` is set, the stream waits for it
+// just before the first read of `observed` (after the forward).
+int misfit_gradient_impl(const wfd_problem* p, const float* vel, const float* sponge_z,
+                         const float* sponge_y, const float* sponge_x, const float* wavelet,
+                         const int32_t* src, const int32_t* rec, const float* observed,
+                         cudaEvent_t observed_ready, float* traces, float* grad_vel, float* grad_wavelet,
+                         double* misfit, void* workspace, size_t workspace_bytes, void* stream) {
     int rc = common_checks(p, vel, wavelet, src, rec);
     if (rc) return rc;
     if (!grad_vel || !misfit || (p->nrec > 0 && !observed))
@@ -1323,6 +1327,7 @@ int wfd_misfit_gradient(const wfd_problem* p, const float* vel, const float* spo
         float* d = traces ? traces + toff : w.res;
         if ((rc = run_forward(&q, g, L, w, st, gwav, d, true))) return rc;
         const long long ntr = (long long)q.nshot * q.nt * q.nrec;
+        if (observed_ready && g0 == 0) WFD_CUDA(cudaStreamWaitEvent(s, observed_ready, 0));
         if (ntr > 0) WFD_CUDA(launch_residual_misfit(d, observed + toff, w.res, ntr, misfit, s));
         if ((rc = run_backward(&q, g, L, w, st, gwav, w.res, grad_vel,
                                grad_wavelet ? grad_wavelet + (long long)g0 * p->nt * p->nsrc : nullptr,
@@ -1330,6 +1335,28 @@ int wfd_misfit_gradient(const wfd_problem* p, const float* vel, const float* spo
             return rc;
     }
     return WFD_OK;
+}
+
+}  // namespace
+
+int wfd_misfit_gradient(const wfd_problem* p, const float* vel, const float* sponge_z,
+                        const float* sponge_y, const float* sponge_x, const float* wavelet,
+                        const int32_t* src, const int32_t* rec, const float* observed,
+                        float* traces, float* grad_vel, float* grad_wavelet, double* misfit,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+    return misfit_gradient_impl(p, vel, sponge_z, sponge_y, sponge_x, wavelet, src, rec, observed, nullptr,
+                                traces, grad_vel, grad_wavelet, misfit, workspace, workspace_bytes, stream);
+}
+
+int wfd_misfit_gradient_overlap(const wfd_problem* p, const float* vel, const float* sponge_z,
+                                const float* sponge_y, const float* sponge_x, const float* wavelet,
+                                const int32_t* src, const int32_t* rec, const float* observed,
+                                void* observed_ready, float* traces, float* grad_vel, float* grad_wavelet,
+                                double* misfit, void* workspace, size_t workspace_bytes, void* stream) {
+    if (!observed_ready) return fail(WFD_ERR_INVALID, "observed_ready is NULL");
+    return misfit_gradient_impl(p, vel, sponge_z, sponge_y, sponge_x, wavelet, src, rec, observed,
+                                static_cast<cudaEvent_t>(observed_ready), traces, grad_vel, grad_wavelet, misfit,
+                                workspace, workspace_bytes, stream);
 }
 
 // ------------------------------------------------------------------ variable density

@@ -385,11 +385,16 @@ def wave_forward_final(vel: torch.Tensor, wavelet, src, rec, grid: Grid, *, chec
 
 
 def misfit_gradient(vel: torch.Tensor, wavelet, src, rec, observed: torch.Tensor, grid: Grid, *,
-                    want_wavelet: bool = False, want_traces: bool = False, check: bool = True):
+                    want_wavelet: bool = False, want_traces: bool = False, check: bool = True,
+                    observed_ready: torch.cuda.Event | None = None):
     """(misfit, grad_vel[, grad_wavelet][, traces]) in one library call.
 
     misfit = 1/2 sum (traces - observed)^2, accumulated in FP64 on the GPU
-    (a 0-d float64 tensor); grad_vel has vel's shape (0 on the fixed ring)."""
+    (a 0-d float64 tensor); grad_vel has vel's shape (0 on the fixed ring).
+    observed_ready: an event recorded after the (asynchronous) copy that fills
+    ``observed``; the call waits for it only after the forward, so the copy
+    overlaps the forward (``observed`` must then be a contiguous float32
+    tensor, read in place)."""
     wav_t = torch.as_tensor(wavelet, device=vel.device)
     nshot = observed.shape[0]
     call = _prepare(vel, wav_t, src, rec, grid, nshot)
@@ -397,13 +402,15 @@ def misfit_gradient(vel: torch.Tensor, wavelet, src, rec, observed: torch.Tensor
     p = call.problem
     if tuple(observed.shape) != (p.nshot, p.nt, p.nrec):
         raise ValueError(f"observed must be ({p.nshot}, {p.nt}, {p.nrec})")
+    if observed_ready is not None and (observed.dtype != torch.float32 or not observed.is_contiguous()):
+        raise ValueError("with observed_ready, observed must be a contiguous float32 tensor")
     obs = observed.to(torch.float32).contiguous()
     ws = _workspace(call, True)
     grad = torch.empty_like(call.vel)
     gwav = torch.empty_like(call.wavelet) if want_wavelet else None
     traces = torch.empty_like(obs) if want_traces else None
     misfit = torch.zeros((), dtype=torch.float64, device=vel.device)
-    _misfit_gradient_into(call, obs, ws, grad, misfit, gwav, traces)
+    _misfit_gradient_into(call, obs, ws, grad, misfit, gwav, traces, observed_ready)
     if check:
         _status(ws, "wfd_misfit_gradient")
     out = [misfit, grad]
@@ -414,14 +421,19 @@ def misfit_gradient(vel: torch.Tensor, wavelet, src, rec, observed: torch.Tensor
     return tuple(out)
 
 
-def _misfit_gradient_into(call: _Call, obs, ws, grad, misfit, gwav=None, traces=None):
+def _misfit_gradient_into(call: _Call, obs, ws, grad, misfit, gwav=None, traces=None, observed_ready=None):
     """wfd_misfit_gradient into caller buffers on the current stream (no
     allocation, no synchronisation: safe inside CUDA-graph capture)."""
     gz, gy, gx = call.sponges
-    _lib.check(_lib.load().wfd_misfit_gradient(
-        ctypes.byref(call.problem), _ptr(call.vel), _ptr(gz), _ptr(gy), _ptr(gx), _ptr(call.wavelet),
-        _ptr(call.src), _ptr(call.rec), _ptr(obs), _ptr(traces), _ptr(grad), _ptr(gwav), _ptr(misfit),
-        _ptr(ws), ws.numel(), _stream()), "wfd_misfit_gradient")
+    lib = _lib.load()
+    head = (ctypes.byref(call.problem), _ptr(call.vel), _ptr(gz), _ptr(gy), _ptr(gx), _ptr(call.wavelet),
+            _ptr(call.src), _ptr(call.rec), _ptr(obs))
+    tail = (_ptr(traces), _ptr(grad), _ptr(gwav), _ptr(misfit), _ptr(ws), ws.numel(), _stream())
+    if observed_ready is None:
+        _lib.check(lib.wfd_misfit_gradient(*head, *tail), "wfd_misfit_gradient")
+    else:
+        _lib.check(lib.wfd_misfit_gradient_overlap(*head, observed_ready._as_parameter_, *tail),
+                   "wfd_misfit_gradient_overlap")
 
 
 def sum_sq(x: torch.Tensor) -> torch.Tensor:

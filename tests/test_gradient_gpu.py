@@ -223,6 +223,28 @@ def test_3d_unequal_spacings_match_oracle(cuda, orc):
     assert rel_l2(g.cpu().numpy(), gr) < 2e-4
 
 
+def test_misfit_gradient_overlap_matches(cuda, orc):
+    """observed_ready: the observed traces copied on a second stream while the
+    forward runs give the same misfit and gradient as resident data."""
+    from neuralmech_gb300 import misfit_gradient
+    grid, v, wav, src, rec = small_problem(shape=(60, 150), nshot=3, nt=80, ckpt_every=9, seed=21)
+    obs = _observed(orc, grid, v, wav, src, rec)
+    args = (torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+            torch.from_numpy(rec))
+    J1, g1 = misfit_gradient(*args, torch.from_numpy(obs).to(cuda), grid)
+    host = torch.from_numpy(obs).pin_memory()
+    side = torch.cuda.Stream()
+    ob = torch.empty(host.shape, dtype=torch.float32, device=cuda)
+    ready = torch.cuda.Event()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        ob.copy_(host, non_blocking=True)
+        ready.record(side)
+    J2, g2 = misfit_gradient(*args, ob, grid, observed_ready=ready)
+    assert J2.item() == J1.item()
+    assert torch.equal(g2, g1) or rel_l2(g2.cpu().numpy(), g1.cpu().numpy()) < 1e-6
+
+
 def test_shot_groups_match_one_batch(cuda, orc):
     """group_shots runs the shots in sequential groups on one workspace; the
     misfit, gradient, traces and wavelet gradient equal the one-batch call."""

@@ -171,9 +171,9 @@ constexpr int T3_TX = 64;
 constexpr int T3_TY = 16;
 constexpr int T3_XH = 4;
 constexpr int T3_W = T3_TX + 2 * T3_XH;
-constexpr int T3_THREADS = (T3_TX / 4) * T3_TY;  // 256
+constexpr int T3_ROWS = 1;                       // tile rows per thread
+constexpr int T3_THREADS = (T3_TX / 4) * T3_TY / T3_ROWS;
 constexpr int T3_ZCHUNK = 64;                    // planes per CTA (z blocking)
-constexpr int T3_UNROLL = 1;                     // output planes per turn of the z-tap queue
 
 // map_cur: u_n planes (box T3_W x (T3_TY + 2R) x 1 x 1); map_old, map_lap:
 // output-plane tiles (box T3_TX x T3_TY x 1 x 1); map_m: the model m

@@ -48,16 +48,17 @@ struct Layout3D {
 __device__ __forceinline__ float2 lo2(const float4& v) { return make_float2(v.x, v.y); }
 __device__ __forceinline__ float2 hi2(const float4& v) { return make_float2(v.z, v.w); }
 
-template <int R, int MODE>
-__global__ void __launch_bounds__(T3_THREADS, 2)
+template <int R, int MODE, int TR>
+__global__ void __launch_bounds__(LANES_X * T3_TY / TR, 2)
     step3d_kernel(const __grid_constant__ CUtensorMap map_cur,
                   const __grid_constant__ CUtensorMap map_old,
                   const __grid_constant__ CUtensorMap map_lap,
                   const __grid_constant__ CUtensorMap map_m, const StepArgs a) {
     using L = Layout3D<R, MODE>;
     constexpr int NB = L::NB;
-    constexpr int U = T3_UNROLL;  // output planes per turn of the register queue
-    constexpr int Q = 2 * R + U;  // register queue of staged planes
+    constexpr int Q = 2 * R + 1;                 // z taps held in registers per row
+    constexpr int NTH = LANES_X * T3_TY / TR;    // threads
+    constexpr int YW = TR + 2 * R;               // staged rows a thread reads for its y taps
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
@@ -66,7 +67,8 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
     uint64_t* bc = reinterpret_cast<uint64_t*>(old_ring + NBO * L::OLD_GROUP);
     float* gzs = reinterpret_cast<float*>(bc + NB);  // gz of the CTA's output planes
 
-    const int tid = threadIdx.x, lane = tid % LANES_X, row = tid / LANES_X;
+    const int tid = threadIdx.x, lane = tid % LANES_X;
+    const int yr0 = (tid / LANES_X) * TR;  // first tile row of this thread
     const int s = blockIdx.x;
     const int tile = blockIdx.y;
     const int ntiles = a.tiles_x * a.tiles_y * a.tiles_z;
@@ -108,7 +110,6 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
 
     // ---- per-thread constants
     const int x = x0 + 4 * lane;
-    const int y = y0 + row;
     float gxe[4];
     bool xin[4];
 #pragma unroll
@@ -117,21 +118,26 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
         xin[e] = x + e >= R && x + e < a.nx - R;
     }
     const bool all_x = xin[0] && xin[1] && xin[2] && xin[3];
-    const bool yin = y >= R && y < a.ny - R;
-    const float gyv = (a.gy != nullptr && y < a.ny) ? __ldg(a.gy + y) : 1.f;
+    bool yin[TR];
+    float gyv[TR];
+#pragma unroll
+    for (int t = 0; t < TR; ++t) {
+        const int y = y0 + yr0 + t;
+        yin[t] = y >= R && y < a.ny - R;
+        gyv[t] = (a.gy != nullptr && y < a.ny) ? __ldg(a.gy + y) : 1.f;
+    }
     float* un = a.u_new + (long long)s * a.shot_stride;
     const int col = T3_XH + 4 * lane;  // staged column of this thread's first cell
 
-    // ---- register queue of the z taps. The plane loop is unrolled U times:
-    // at the start of a group of U output planes zr0 .. zr0 + U - 1, V[j]
-    // holds staged plane zr0 + j (j < 2R); output plane zr0 + u loads plane
-    // zr0 + 2R + u into V[2R + u] and takes its z taps from V[u .. u + 2R];
-    // after the group the queue moves down by U.
-    float4 V[Q];
+    // ---- register queues of the z taps, one per row: V[t][j] = u_n of row
+    // yr0 + t at z = zout - R + j
+    float4 V[TR][Q];
 #pragma unroll
     for (int p = 0; p < 2 * R; ++p) {
         if (!mbar_wait(&bc[p % NB], (p / NB) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
-        V[p] = *reinterpret_cast<const float4*>(cur_buf(p) + (row + R) * T3_W + col);
+#pragma unroll
+        for (int t = 0; t < TR; ++t)
+            V[t][p + 1] = *reinterpret_cast<const float4*>(cur_buf(p) + (yr0 + t + R) * T3_W + col);
     }
     __syncthreads();  // planes 0 .. R-1 are consumed
     if (tid == 0) {
@@ -143,20 +149,35 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
     const int lo_i = a.inj.off ? a.inj.off[s * ntiles + tile] : 0;
     const int hi_i = a.inj.off ? a.inj.off[s * ntiles + tile + 1] : 0;
 
-    for (int zr0 = 0; zr0 < zc; zr0 += U) {
+    for (int zr = 0; zr < zc; ++zr) {
+        const int z = z0 + zr;
+        const int pn = zr + 2 * R;  // newest staged plane needed
+        if (!mbar_wait(&bc[pn % NB], (pn / NB) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int zr = zr0 + u;
-            if (zr >= zc) break;
-            const int z = z0 + zr;
-            const int pn = zr + 2 * R;  // newest staged plane needed
-            if (!mbar_wait(&bc[pn % NB], (pn / NB) & 1)) report(a.err, DEV_ERR_TMA_TIMEOUT);
-            V[u + 2 * R] = *reinterpret_cast<const float4*>(cur_buf(pn) + (row + R) * T3_W + col);
+        for (int t = 0; t < TR; ++t) {
+#pragma unroll
+            for (int j = 0; j < 2 * R; ++j) V[t][j] = V[t][j + 1];
+            V[t][2 * R] = *reinterpret_cast<const float4*>(cur_buf(pn) + (yr0 + t + R) * T3_W + col);
+        }
 
-            const float* pl = cur_buf(zr + R);  // u_n at the output plane, with halo
-            const float* prow = pl + (row + R) * T3_W + 4 * lane;
+        const float* pl = cur_buf(zr + R);  // u_n at the output plane, with halo
+        // y taps: staged rows yr0 .. yr0 + TR + 2R - 1 (tile rows yr0 - R ..);
+        // the thread's own rows come from the queues
+        float4 Y[YW];
+#pragma unroll
+        for (int j = 0; j < YW; ++j) {
+            if (j >= R && j < R + TR)
+                Y[j] = V[j - R][R];
+            else
+                Y[j] = *reinterpret_cast<const float4*>(pl + (yr0 + j) * T3_W + col);
+        }
+        const float gz = gzs[zr];
+        const bool zin = z >= R && z < a.nz - R;
+#pragma unroll
+        for (int t = 0; t < TR; ++t) {
+            const float* prow = pl + (yr0 + t + R) * T3_W + 4 * lane;
             const float4 lv = *reinterpret_cast<const float4*>(prow);
-            const float4 cv = V[u + R];
+            const float4 cv = V[t][R];
             const float4 rv = *reinterpret_cast<const float4*>(prow + 2 * T3_XH);
             const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y, cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
             // L u in packed pairs: (c0 u + sum_k cx_k (x taps)) + sum_k cy_k (y taps)
@@ -176,22 +197,20 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
                 }
                 lo = __ffma2_rn(a.cxp[k - 1], xl, lo);
                 hi = __ffma2_rn(a.cxp[k - 1], xh, hi);
-                const float4 ym = *reinterpret_cast<const float4*>(pl + (row + R - k) * T3_W + col);
-                const float4 yp = *reinterpret_cast<const float4*>(pl + (row + R + k) * T3_W + col);
+                const float4 ym = Y[R + t - k], yp = Y[R + t + k];
                 loy = __ffma2_rn(a.cyp[k - 1], __fadd2_rn(lo2(ym), lo2(yp)), loy);
                 hiy = __ffma2_rn(a.cyp[k - 1], __fadd2_rn(hi2(ym), hi2(yp)), hiy);
-                const float4 zm = V[u + R - k], zp = V[u + R + k];
+                const float4 zm = V[t][R - k], zp = V[t][R + k];
                 loz = __ffma2_rn(a.czp[k - 1], __fadd2_rn(lo2(zm), lo2(zp)), loz);
                 hiz = __ffma2_rn(a.czp[k - 1], __fadd2_rn(hi2(zm), hi2(zp)), hiz);
             }
             lo = __fadd2_rn(__fadd2_rn(lo, loy), loz);
             hi = __fadd2_rn(__fadd2_rn(hi, hiy), hiz);
-            const int ti = row * T3_TX + 4 * lane;
+            const int ti = (yr0 + t) * T3_TX + 4 * lane;
             const float4 ov = *reinterpret_cast<const float4*>(old_buf(zr) + ti);
             const float4 mv = *reinterpret_cast<const float4*>(m_buf(zr) + ti);
-            const float gz = gzs[zr];
             // u_{n+1} = g (m L u + 2 u) - g^2 u_{n-1}
-            const float gyz = gz * gyv;
+            const float gyz = gz * gyv[t];
             const float2 gl = __fmul2_rn(make_float2(gyz, gyz), make_float2(gxe[0], gxe[1]));
             const float2 gh = __fmul2_rn(make_float2(gyz, gyz), make_float2(gxe[2], gxe[3]));
             const float2 tl = __ffma2_rn(lo2(mv), lo, __fadd2_rn(lo2(cv), lo2(cv)));
@@ -201,8 +220,8 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
             const float nv[4] = {nl.x, nl.y, nh.x, nh.y};
             const float lap[4] = {lo.x, lo.y, hi.x, hi.y};
 
-            const bool rin = yin && z >= R && z < a.nz - R;
-            const long long off = (long long)z * a.plane + (long long)y * a.ld + x;
+            const bool rin = yin[t] && zin;
+            const long long off = (long long)z * a.plane + (long long)(y0 + yr0 + t) * a.ld + x;
             if (rin && all_x) {
                 *reinterpret_cast<float4*>(un + off) = make_float4(nv[0], nv[1], nv[2], nv[3]);
             } else if (rin) {
@@ -245,36 +264,34 @@ __global__ void __launch_bounds__(T3_THREADS, 2)
                         if (xin[e]) atomicAdd(gp + e, comp(cv, e) * comp(lu, e));
                 }
             }
-            // sampling of u_n at this plane
-            for (int j = lo_s + tid; j < hi_s; j += T3_THREADS) {
-                const int2 en = a.smp.ent[j];
-                const int pz = en.x / int(a.plane);
-                if (pz != z) continue;
-                const int rem = en.x - pz * int(a.plane);
-                const int py = rem / a.ld, px = rem - py * a.ld;
-                float v = pl[(py - y0 + R) * T3_W + (px - x0 + T3_XH)] * a.smp_scale;
-                if (a.smp_div_m) v /= a.m[en.x];
-                a.smp_out[((long long)s * a.smp_nt + a.smp_t) * a.smp_np + en.y] = v;
-            }
-            __syncthreads();  // plane zr + R and old group zr fully read; stores of plane z done
-            if (tid == 0) {
-                fence_proxy_async_smem();
-                if (zr + NB + R < total) issue(zr + NB + R);
-            }
-            for (int j = lo_i + tid; j < hi_i; j += T3_THREADS) {
-                const int2 en = a.inj.ent[j];
-                const int pz = en.x / int(a.plane);
-                if (pz != z) continue;
-                const int rem = en.x - pz * int(a.plane);
-                const int py = rem / a.ld, px = rem - py * a.ld;
-                float v = a.inj_val[((long long)s * a.inj_nt + a.inj_t) * a.inj_np + en.y] * a.inj_scale;
-                if (a.inj_times_m) v *= a.m[en.x];
-                const float g = (a.gz ? a.gz[pz] : 1.f) * (a.gy ? a.gy[py] : 1.f) * (a.gx ? a.gx[px] : 1.f);
-                atomicAdd(un + en.x, g * v);
-            }
         }
-#pragma unroll
-        for (int j = 0; j < 2 * R; ++j) V[j] = V[j + U];
+        // sampling of u_n at this plane
+        for (int j = lo_s + tid; j < hi_s; j += NTH) {
+            const int2 en = a.smp.ent[j];
+            const int pz = en.x / int(a.plane);
+            if (pz != z) continue;
+            const int rem = en.x - pz * int(a.plane);
+            const int py = rem / a.ld, px = rem - py * a.ld;
+            float v = pl[(py - y0 + R) * T3_W + (px - x0 + T3_XH)] * a.smp_scale;
+            if (a.smp_div_m) v /= a.m[en.x];
+            a.smp_out[((long long)s * a.smp_nt + a.smp_t) * a.smp_np + en.y] = v;
+        }
+        __syncthreads();  // plane zr + R and old group zr fully read; stores of plane z done
+        if (tid == 0) {
+            fence_proxy_async_smem();
+            if (zr + NB + R < total) issue(zr + NB + R);
+        }
+        for (int j = lo_i + tid; j < hi_i; j += NTH) {
+            const int2 en = a.inj.ent[j];
+            const int pz = en.x / int(a.plane);
+            if (pz != z) continue;
+            const int rem = en.x - pz * int(a.plane);
+            const int py = rem / a.ld, px = rem - py * a.ld;
+            float v = a.inj_val[((long long)s * a.inj_nt + a.inj_t) * a.inj_np + en.y] * a.inj_scale;
+            if (a.inj_times_m) v *= a.m[en.x];
+            const float g = (a.gz ? a.gz[pz] : 1.f) * (a.gy ? a.gy[py] : 1.f) * (a.gx ? a.gx[px] : 1.f);
+            atomicAdd(un + en.x, g * v);
+        }
     }
 }
 
@@ -286,13 +303,13 @@ cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUte
     int dev = 0;
     cudaGetDevice(&dev);
     if (configured_device != dev) {
-        cudaError_t e = cudaFuncSetAttribute(step3d_kernel<R, MODE>,
+        cudaError_t e = cudaFuncSetAttribute(step3d_kernel<R, MODE, T3_ROWS>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
         if (e != cudaSuccess) return e;
         configured_device = dev;
     }
     const dim3 grid(a.nshot, a.tiles_x * a.tiles_y * a.tiles_z);
-    step3d_kernel<R, MODE><<<grid, T3_THREADS, L::BYTES, s>>>(mc, mo, ml, mm, with_weight_pairs(a));
+    step3d_kernel<R, MODE, T3_ROWS><<<grid, T3_THREADS, L::BYTES, s>>>(mc, mo, ml, mm, with_weight_pairs(a));
     count_launch();
     return cudaGetLastError();
 }

@@ -241,8 +241,8 @@ def test_misfit_gradient_overlap_matches(cuda, orc):
         ob.copy_(host, non_blocking=True)
         ready.record(side)
     J2, g2 = misfit_gradient(*args, ob, grid, observed_ready=ready)
-    assert J2.item() == J1.item()
-    assert torch.equal(g2, g1) or rel_l2(g2.cpu().numpy(), g1.cpu().numpy()) < 1e-6
+    assert abs(J2.item() - J1.item()) <= 1e-12 * J1.item()  # (FP64 atomic sums: order may differ)
+    assert rel_l2(g2.cpu().numpy(), g1.cpu().numpy()) < 1e-6
 
 
 def test_shot_groups_match_one_batch(cuda, orc):

@@ -282,181 +282,218 @@ def config_of(w, args):
             "parallelism": f"{args.gpus} GPU(s), shots batched per GPU, gradient all-reduce"}
 
 
-def run_other(args):
-    """fwd2048 / fwi384_3d / batch8: the kernel-level JSON line (no e2e leg)."""
+def _wl_temporal(args, dev):
+    """The order-2 drop-ins on the reference temporal driver's grid."""
+    import torch
+
+    extra, graph_kernels = {}, 0
+    from neuralmech_gb300 import step2d_order2
+    from neuralmech_gb300.wavefd import step2d_exact, temporal_step
+    N, M = 8000, 16000  # 2D_wave_cuda_temporal.py:26
+    Mp = (M + 31) // 32 * 32
+    dx, dy = 1.0 / (N - 1), 2.0 / (M - 1)
+    dt = 0.95 * min(dx, dy) / math.sqrt(2)
+    x = torch.linspace(0, 1, N, device=dev)[:, None]
+    y = torch.linspace(0, 2, M, device=dev)[None, :]
+    u0 = torch.zeros((N, Mp), device=dev)
+    u0[:, :M] = torch.exp(-(x - 0.5) ** 2 / (2 * 0.02 ** 2)) * torch.exp(-(y - 0.5) ** 2 / (2 * 0.02 ** 2))
+    bufs = [u0, u0.clone(), torch.empty_like(u0), torch.empty_like(u0)]
+    state = {"k": 0}
+
+    def step():  # the driver's two pairs of arrays, swapped every launch
+        a, b = (0, 1) if state["k"] % 2 == 0 else (2, 3)
+        c, d = (2, 3) if state["k"] % 2 == 0 else (0, 1)
+        temporal_step(bufs[a], bufs[b], bufs[c], bufs[d], 1.0, dt, dx, dy, N, M)
+        state["k"] += 1
+
+    inner = (N - 2) * (M - 2)
+    for name, fn in (("padded_step_gcells", step2d_order2), ("exact_step_gcells", step2d_exact)):
+        def eight():
+            p, q = bufs[0], bufs[1]
+            for _ in range(8):
+                p = fn(p, q, p, 1.0, dt, dx, dy, N, M)
+                p, q = q, p
+        for _ in range(3):
+            eight()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            eight()
+        e1.record()
+        torch.cuda.synchronize()
+        extra[name] = 8 * inner * 5 / (e0.elapsed_time(e1) / 1e3) / 1e9
+    updates, bpu = 8.0 * inner, 16.0 / 8
+    cfg = {"workload": f"temporal: wfd_temporal_step, {N} x {M} (M_padded {Mp}), order 2, Dirichlet, "
+                       "8 updates per launch; bytes: both levels read and written once per launch",
+           "l2": "inputs larger than L2 (4 x 512 MB)"}
+    return dict(step=step, updates=updates, bpu=bpu, cfg=cfg, extra=extra, graph_kernels=graph_kernels)
+
+
+def _wl_fmc_tfm(args, dev):
+    """Full matrix capture, analytic signal and TFM on the plate driver's sizes."""
+    import torch
+
+    extra, graph_kernels = {}, 0
+    from neuralmech_gb300 import Grid
+    from neuralmech_gb300.cuwave_compat import sineburst, stable_dt
+    from neuralmech_gb300.imaging import analytic_signal, full_matrix_capture, tfm
+    n, E, c = 512, 32, 1.0  # projects/18_fwi/plate.py:19-32
+    h = 1.0 / (n - 3)
+    dt0 = 0.9 * stable_dt((h, h), c, 8)
+    nt = math.ceil(2.5 / dt0) + 1
+    dt = 2.5 / (nt - 1)
+    grid = Grid((n, n), (h, h), dt, nt, order=8, sponge=0)
+    cols = np.round(np.linspace(0.1, 0.9, E) * (n - 1)).astype(np.int32)
+    el_cells = np.stack([np.full(E, 4, np.int32), cols], axis=1)       # (z, x): the top edge
+    el_xy = np.stack([cols * h, np.full(E, 4 * h)], axis=1)            # (x, y) in plate units
+    vel = torch.full((n, n), c, device=dev)
+    rng = np.random.default_rng(0)
+    for _ in range(4):  # circular slow voids (synthetic stand-ins for the plate's voids)
+        zc, xc, r = rng.uniform(0.3, 0.8) * n, rng.uniform(0.3, 0.7) * n, rng.uniform(0.02, 0.05) * n
+        zz, xx = torch.meshgrid(torch.arange(n, device=dev), torch.arange(n, device=dev), indexing="ij")
+        vel[(zz - zc) ** 2 + (xx - xc) ** 2 < r * r] = 0.5 * c
+    wav = torch.from_numpy(sineburst(np.arange(nt) * dt, 1.0, 20.0, 2)).to(dev)
+    px = torch.linspace(0, 1, 512, device=dev)
+    X, Y = torch.meshgrid(px, px, indexing="ij")
+    t0 = 2 / (2 * 20.0)
+    stage_ms = {"capture": [], "analytic": [], "tfm": []}
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
+    def step():
+        evs[0].record()
+        traces = full_matrix_capture(vel, wav, el_cells, grid)          # (E, nt, E)
+        evs[1].record()
+        hs = analytic_signal(traces.permute(0, 2, 1).contiguous())       # (E, E, nt)
+        evs[2].record()
+        tfm(hs, el_xy, t0, dt, c, X, Y)
+        evs[3].record()
+        torch.cuda.synchronize()
+        for k, name in enumerate(("capture", "analytic", "tfm")):
+            stage_ms[name].append(evs[k].elapsed_time(evs[k + 1]))
+    R = 4
+    updates, bpu = float(E) * (n - 2 * R) ** 2 * nt, 16.0
+    extra["stage_ms"] = stage_ms  # averaged over the timed calls below
+    cfg = {"workload": f"fmc_tfm: full matrix capture, {E} elements on a {n}^2 plate, {nt} steps, order 8, "
+                       "4 slow voids; analytic signal; TFM onto 512^2 pixels with reciprocity",
+           "pixels": 512 * 512, "traces": E * E, "samples": nt}
+    return dict(step=step, updates=updates, bpu=bpu, cfg=cfg, extra=extra, graph_kernels=graph_kernels)
+
+
+def _wl_batch8(args, dev):
+    """Eight uneven models in one graph-captured batch gradient."""
+    import torch
+
+    from neuralmech_gb300 import wave_forward
+    from neuralmech_gb300.batch import BatchFWI
+    from neuralmech_gb300.synth import workload as wl
+
+    extra = {}
+    models = []
+    for w in wl("batch8"):
+        v = torch.from_numpy(w.vel).to(dev)
+        wav = torch.from_numpy(w.wavelet).to(dev)
+        src, rec = torch.from_numpy(w.src), torch.from_numpy(w.rec)
+        obs = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, w.grid)
+        models.append(dict(vel=v, wavelet=wav, src=src, rec=rec, observed=obs, grid=w.grid))
+    budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
+    batch = BatchFWI(models, autotune=True, level_budget=budget)
+    graph_kernels = batch.graph_kernels  # replays launch these without a host call each
+    step = batch.run
+    updates, bpu = batch.cell_updates, 18.0
+    cfg = {"workload": "batch8: 8 models 512^2..1536^2, 1000..3000 steps, 128 shots, Ricker 10..25 Hz, "
+                       "one graph-captured batch gradient (streams per model), autotuned kernels, "
+                       f"kept forward levels in {args.level_store_frac:.0%} of the GPU's memory",
+           "models": [[list(m.call.grid.shape), m.call.grid.nt, m.call.problem.nshot] for m in batch.models],
+           "configs": batch.configs,
+           "store_levels": [m.call.grid.store_levels for m in batch.models]}
+    return dict(step=step, updates=updates, bpu=bpu, cfg=cfg, extra=extra, graph_kernels=graph_kernels)
+
+
+def _wl_grid(args, dev):
+    """vd1024 / fwd2048 / fwi384_3d: one grid, one library call per step."""
     import dataclasses
 
     import torch
 
-    from neuralmech_gb300 import _lib, levels_for_budget, misfit_gradient, wave_forward
+    from neuralmech_gb300 import levels_for_budget, misfit_gradient, wave_forward
     from neuralmech_gb300.synth import workload as wl
+
+    extra, graph_kernels = {}, 0
+    w = wl("fwi1024" if args.workload == "vd1024" else args.workload, scale=args.scale)
+    if args.shots:
+        w.src = w.src[:args.shots].copy()
+        if w.wavelet.ndim == 2:
+            w.wavelet = w.wavelet[:args.shots].copy()
+        if w.rec.ndim == 3:
+            w.rec = w.rec[:args.shots].copy()
+    g = w.grid
+    if args.nt:
+        g = dataclasses.replace(g, nt=args.nt, ckpt_every=min(g.ckpt_every or args.nt, args.nt))
+        w.wavelet = w.wavelet[..., :args.nt]
+    if args.ckpt_every:
+        g = dataclasses.replace(g, ckpt_every=args.ckpt_every)
+    v = torch.from_numpy(w.vel).to(dev)
+    wav = torch.from_numpy(w.wavelet).to(dev)
+    src, rec = torch.from_numpy(w.src), torch.from_numpy(w.rec)
+    R = g.order // 2
+    interior = float(np.prod([n - 2 * R for n in g.shape]))
+    if args.workload == "vd1024":
+        # the fwi1024 models with Gardner densities rho = 310 v^0.25 and kappa = rho v^2
+        from neuralmech_gb300.wavefd import vd_forward, vd_misfit_gradient
+        if args.level_store_frac > 0:
+            budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
+            g = dataclasses.replace(g, store_levels=levels_for_budget(g, w.nshot, budget))
+        rho_of = lambda v: 310.0 * np.power(v.astype(np.float64), 0.25)
+        r0, r1 = rho_of(w.vel), rho_of(w.vel_true)
+        kap = torch.from_numpy((r0 * w.vel.astype(np.float64) ** 2).astype(np.float32)).to(dev)
+        rho = torch.from_numpy(r0.astype(np.float32)).to(dev)
+        obs = vd_forward(torch.from_numpy((r1 * w.vel_true.astype(np.float64) ** 2).astype(np.float32)).to(dev),
+                         torch.from_numpy(r1.astype(np.float32)).to(dev), wav, src, rec, g)
+        step = lambda: vd_misfit_gradient(kap, rho, wav, src, rec, obs, g, check=False)
+        updates, bpu = 2.0 * w.nshot * interior * g.nt, 18.0
+        cfg = {"workload": f"vd1024: 2D variable-density FWI gradient (kappa, rho) {g.shape[0]}^2, {g.nt} steps, "
+                           f"{w.nshot} shots, {w.rec.shape[1]} receivers, order 8 staggered, 20-cell sponge, "
+                           f"Gardner densities, BF16 checkpoints every {g.ckpt_every}",
+               "store_levels": g.store_levels}
+    elif args.workload == "fwd2048":
+        g = dataclasses.replace(g, field_format=args.field_format, tile_rows=args.tile_rows,
+                                step_block=args.step_block if args.field_format == "fp32" else 1)
+        step = lambda: wave_forward(v, wav, src, rec, g, check=False)
+        updates, bpu = w.nshot * interior * g.nt, 16.0
+        cfg = {"workload": f"fwd2048: 2D forward {g.shape[0]}^2, {g.nt} steps, 1 shot, "
+                           f"{w.rec.shape[1]} receivers, order 8, 20-cell sponge",
+               "field_format": g.field_format, "step_block": g.step_block, "tile_rows": g.tile_rows or 32}
+        if g.field_format != "fp32":  # the storage error against the FP32 forward
+            ref = wave_forward(v, wav, src, rec, dataclasses.replace(g, field_format="fp32"))
+            got = step()
+            cfg["traces_rel_l2_vs_fp32"] = float((got - ref).norm() / ref.norm())
+    else:
+        g = dataclasses.replace(g, group_shots=args.group_shots)
+        obs = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, g)
+        step = lambda: misfit_gradient(v, wav, src, rec, obs, g, check=False)
+        updates, bpu = 2.0 * w.nshot * interior * g.nt, 18.0
+        cfg = {"workload": f"fwi384_3d: 3D FWI gradient {g.shape[0]}^3, {g.nt} steps, {w.nshot} shots "
+                           f"in groups of {args.group_shots or w.nshot}, {w.rec.shape[1]} receivers per shot, "
+                           f"BF16 checkpoints every "
+                           f"{g.ckpt_every}"}
+    return dict(step=step, updates=updates, bpu=bpu, cfg=cfg, extra=extra, graph_kernels=graph_kernels)
+
+
+WORKLOADS = {"temporal": _wl_temporal, "fmc_tfm": _wl_fmc_tfm, "batch8": _wl_batch8}
+
+
+def run_other(args):
+    """Every workload but fwi1024: the kernel-level JSON line (no e2e leg)."""
+    import torch
+
+    from neuralmech_gb300 import _lib
 
     dev = torch.device("cuda", 0)
     lib = _lib.load()
-    graph_kernels = 0
-    extra = {}
-    if args.workload == "temporal":
-        from neuralmech_gb300 import step2d_order2
-        from neuralmech_gb300.wavefd import step2d_exact, temporal_step
-        N, M = 8000, 16000  # 2D_wave_cuda_temporal.py:26
-        Mp = (M + 31) // 32 * 32
-        dx, dy = 1.0 / (N - 1), 2.0 / (M - 1)
-        dt = 0.95 * min(dx, dy) / math.sqrt(2)
-        x = torch.linspace(0, 1, N, device=dev)[:, None]
-        y = torch.linspace(0, 2, M, device=dev)[None, :]
-        u0 = torch.zeros((N, Mp), device=dev)
-        u0[:, :M] = torch.exp(-(x - 0.5) ** 2 / (2 * 0.02 ** 2)) * torch.exp(-(y - 0.5) ** 2 / (2 * 0.02 ** 2))
-        bufs = [u0, u0.clone(), torch.empty_like(u0), torch.empty_like(u0)]
-        state = {"k": 0}
-
-        def step():  # the driver's two pairs of arrays, swapped every launch
-            a, b = (0, 1) if state["k"] % 2 == 0 else (2, 3)
-            c, d = (2, 3) if state["k"] % 2 == 0 else (0, 1)
-            temporal_step(bufs[a], bufs[b], bufs[c], bufs[d], 1.0, dt, dx, dy, N, M)
-            state["k"] += 1
-
-        inner = (N - 2) * (M - 2)
-        for name, fn in (("padded_step_gcells", step2d_order2), ("exact_step_gcells", step2d_exact)):
-            def eight():
-                p, q = bufs[0], bufs[1]
-                for _ in range(8):
-                    p = fn(p, q, p, 1.0, dt, dx, dy, N, M)
-                    p, q = q, p
-            for _ in range(3):
-                eight()
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(5):
-                eight()
-            e1.record()
-            torch.cuda.synchronize()
-            extra[name] = 8 * inner * 5 / (e0.elapsed_time(e1) / 1e3) / 1e9
-        updates, bpu = 8.0 * inner, 16.0 / 8
-        cfg = {"workload": f"temporal: wfd_temporal_step, {N} x {M} (M_padded {Mp}), order 2, Dirichlet, "
-                           "8 updates per launch; bytes: both levels read and written once per launch",
-               "l2": "inputs larger than L2 (4 x 512 MB)"}
-    elif args.workload == "fmc_tfm":
-        from neuralmech_gb300 import Grid
-        from neuralmech_gb300.cuwave_compat import sineburst, stable_dt
-        from neuralmech_gb300.imaging import analytic_signal, full_matrix_capture, tfm
-        n, E, c = 512, 32, 1.0  # projects/18_fwi/plate.py:19-32
-        h = 1.0 / (n - 3)
-        dt0 = 0.9 * stable_dt((h, h), c, 8)
-        nt = math.ceil(2.5 / dt0) + 1
-        dt = 2.5 / (nt - 1)
-        grid = Grid((n, n), (h, h), dt, nt, order=8, sponge=0)
-        cols = np.round(np.linspace(0.1, 0.9, E) * (n - 1)).astype(np.int32)
-        el_cells = np.stack([np.full(E, 4, np.int32), cols], axis=1)       # (z, x): the top edge
-        el_xy = np.stack([cols * h, np.full(E, 4 * h)], axis=1)            # (x, y) in plate units
-        vel = torch.full((n, n), c, device=dev)
-        rng = np.random.default_rng(0)
-        for _ in range(4):  # circular slow voids (synthetic stand-ins for the plate's voids)
-            zc, xc, r = rng.uniform(0.3, 0.8) * n, rng.uniform(0.3, 0.7) * n, rng.uniform(0.02, 0.05) * n
-            zz, xx = torch.meshgrid(torch.arange(n, device=dev), torch.arange(n, device=dev), indexing="ij")
-            vel[(zz - zc) ** 2 + (xx - xc) ** 2 < r * r] = 0.5 * c
-        wav = torch.from_numpy(sineburst(np.arange(nt) * dt, 1.0, 20.0, 2)).to(dev)
-        px = torch.linspace(0, 1, 512, device=dev)
-        X, Y = torch.meshgrid(px, px, indexing="ij")
-        t0 = 2 / (2 * 20.0)
-        stage_ms = {"capture": [], "analytic": [], "tfm": []}
-        evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-
-        def step():
-            evs[0].record()
-            traces = full_matrix_capture(vel, wav, el_cells, grid)          # (E, nt, E)
-            evs[1].record()
-            hs = analytic_signal(traces.permute(0, 2, 1).contiguous())       # (E, E, nt)
-            evs[2].record()
-            tfm(hs, el_xy, t0, dt, c, X, Y)
-            evs[3].record()
-            torch.cuda.synchronize()
-            for k, name in enumerate(("capture", "analytic", "tfm")):
-                stage_ms[name].append(evs[k].elapsed_time(evs[k + 1]))
-        R = 4
-        updates, bpu = float(E) * (n - 2 * R) ** 2 * nt, 16.0
-        extra["stage_ms"] = stage_ms  # averaged over the timed calls below
-        cfg = {"workload": f"fmc_tfm: full matrix capture, {E} elements on a {n}^2 plate, {nt} steps, order 8, "
-                           "4 slow voids; analytic signal; TFM onto 512^2 pixels with reciprocity",
-               "pixels": 512 * 512, "traces": E * E, "samples": nt}
-    elif args.workload == "batch8":
-        from neuralmech_gb300.batch import BatchFWI
-        models = []
-        for w in wl("batch8"):
-            v = torch.from_numpy(w.vel).to(dev)
-            wav = torch.from_numpy(w.wavelet).to(dev)
-            src, rec = torch.from_numpy(w.src), torch.from_numpy(w.rec)
-            obs = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, w.grid)
-            models.append(dict(vel=v, wavelet=wav, src=src, rec=rec, observed=obs, grid=w.grid))
-        budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
-        batch = BatchFWI(models, autotune=True, level_budget=budget)
-        graph_kernels = batch.graph_kernels  # replays launch these without a host call each
-        step = batch.run
-        updates, bpu = batch.cell_updates, 18.0
-        cfg = {"workload": "batch8: 8 models 512^2..1536^2, 1000..3000 steps, 128 shots, Ricker 10..25 Hz, "
-                           "one graph-captured batch gradient (streams per model), autotuned kernels, "
-                           f"kept forward levels in {args.level_store_frac:.0%} of the GPU's memory",
-               "models": [[list(m.call.grid.shape), m.call.grid.nt, m.call.problem.nshot] for m in batch.models],
-               "configs": batch.configs,
-               "store_levels": [m.call.grid.store_levels for m in batch.models]}
-    else:
-        w = wl("fwi1024" if args.workload == "vd1024" else args.workload, scale=args.scale)
-        if args.shots:
-            w.src = w.src[:args.shots].copy()
-            if w.wavelet.ndim == 2:
-                w.wavelet = w.wavelet[:args.shots].copy()
-            if w.rec.ndim == 3:
-                w.rec = w.rec[:args.shots].copy()
-        g = w.grid
-        if args.nt:
-            g = dataclasses.replace(g, nt=args.nt, ckpt_every=min(g.ckpt_every or args.nt, args.nt))
-            w.wavelet = w.wavelet[..., :args.nt]
-        if args.ckpt_every:
-            g = dataclasses.replace(g, ckpt_every=args.ckpt_every)
-        v = torch.from_numpy(w.vel).to(dev)
-        wav = torch.from_numpy(w.wavelet).to(dev)
-        src, rec = torch.from_numpy(w.src), torch.from_numpy(w.rec)
-        R = g.order // 2
-        interior = float(np.prod([n - 2 * R for n in g.shape]))
-        if args.workload == "vd1024":
-            # the fwi1024 models with Gardner densities rho = 310 v^0.25 and kappa = rho v^2
-            from neuralmech_gb300.wavefd import vd_forward, vd_misfit_gradient
-            if args.level_store_frac > 0:
-                budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
-                g = dataclasses.replace(g, store_levels=levels_for_budget(g, w.nshot, budget))
-            rho_of = lambda v: 310.0 * np.power(v.astype(np.float64), 0.25)
-            r0, r1 = rho_of(w.vel), rho_of(w.vel_true)
-            kap = torch.from_numpy((r0 * w.vel.astype(np.float64) ** 2).astype(np.float32)).to(dev)
-            rho = torch.from_numpy(r0.astype(np.float32)).to(dev)
-            obs = vd_forward(torch.from_numpy((r1 * w.vel_true.astype(np.float64) ** 2).astype(np.float32)).to(dev),
-                             torch.from_numpy(r1.astype(np.float32)).to(dev), wav, src, rec, g)
-            step = lambda: vd_misfit_gradient(kap, rho, wav, src, rec, obs, g, check=False)
-            updates, bpu = 2.0 * w.nshot * interior * g.nt, 18.0
-            cfg = {"workload": f"vd1024: 2D variable-density FWI gradient (kappa, rho) {g.shape[0]}^2, {g.nt} steps, "
-                               f"{w.nshot} shots, {w.rec.shape[1]} receivers, order 8 staggered, 20-cell sponge, "
-                               f"Gardner densities, BF16 checkpoints every {g.ckpt_every}",
-                   "store_levels": g.store_levels}
-        elif args.workload == "fwd2048":
-            g = dataclasses.replace(g, field_format=args.field_format, tile_rows=args.tile_rows,
-                                    step_block=args.step_block if args.field_format == "fp32" else 1)
-            step = lambda: wave_forward(v, wav, src, rec, g, check=False)
-            updates, bpu = w.nshot * interior * g.nt, 16.0
-            cfg = {"workload": f"fwd2048: 2D forward {g.shape[0]}^2, {g.nt} steps, 1 shot, "
-                               f"{w.rec.shape[1]} receivers, order 8, 20-cell sponge",
-                   "field_format": g.field_format, "step_block": g.step_block, "tile_rows": g.tile_rows or 32}
-            if g.field_format != "fp32":  # the storage error against the FP32 forward
-                ref = wave_forward(v, wav, src, rec, dataclasses.replace(g, field_format="fp32"))
-                got = step()
-                cfg["traces_rel_l2_vs_fp32"] = float((got - ref).norm() / ref.norm())
-        else:
-            g = dataclasses.replace(g, group_shots=args.group_shots)
-            obs = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, g)
-            step = lambda: misfit_gradient(v, wav, src, rec, obs, g, check=False)
-            updates, bpu = 2.0 * w.nshot * interior * g.nt, 18.0
-            cfg = {"workload": f"fwi384_3d: 3D FWI gradient {g.shape[0]}^3, {g.nt} steps, {w.nshot} shots "
-                               f"in groups of {args.group_shots or w.nshot}, {w.rec.shape[1]} receivers per shot, "
-                               f"BF16 checkpoints every "
-                               f"{g.ckpt_every}"}
+    wk = WORKLOADS.get(args.workload, _wl_grid)(args, dev)
+    step, updates, bpu, cfg = wk["step"], wk["updates"], wk["bpu"], wk["cfg"]
+    extra, graph_kernels = wk["extra"], wk["graph_kernels"]
     if args.once:  # one step, no timing: the command profiled by ncu
         step()
         torch.cuda.synchronize()

@@ -101,7 +101,7 @@ def parse():
                     help="time steps per launch of the forward and the recompute")
     ap.add_argument("--group-shots", type=int, default=8,
                     help="fwi384_3d: shots per sequential group (0: all 16 at once)")
-    ap.add_argument("--level-store-frac", type=float, default=0.65,
+    ap.add_argument("--level-store-frac", type=float, default=0.8,
                     help="fraction of the GPU's memory for the forward levels the adjoint keeps "
                          "instead of recomputing them (0: recompute all but the last segment)")
     ap.add_argument("--workload", default="fwi1024",

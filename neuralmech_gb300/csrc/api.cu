@@ -1191,7 +1191,7 @@ const char* wfd_strerror(int status) {
 
 const char* wfd_last_error(void) { return g_last_error.c_str(); }
 
-int wfd_version(void) { return (2 << 16) | 0; }
+int wfd_version(void) { return (2 << 16) | 1; }  // minor 1: temporal, exact and overlap entries
 
 int wfd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes) {
     int rc = check_problem(p);

@@ -277,7 +277,9 @@ __global__ void __launch_bounds__(LANES_X * T3_TY / TR, 2)
             a.smp_out[((long long)s * a.smp_nt + a.smp_t) * a.smp_np + en.y] = v;
         }
         __syncthreads();  // plane zr + R and old group zr fully read; stores of plane z done
-        if (tid == 0) {
+        // the refill is issued by lane 0 of a warp that changes every plane, so
+        // that no warp carries the extra work into every next barrier
+        if (tid == 32 * (zr % (NTH / 32))) {
             fence_proxy_async_smem();
             if (zr + NB + R < total) issue(zr + NB + R);
         }

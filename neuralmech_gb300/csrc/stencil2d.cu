@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ?
             }
         }
         __syncthreads();  // stage b fully read; this shot's u_{n+1} stores done
-        if (tid == 0 && i + L::STAGES < ns) {
+        if (tid == 32 * (i % (T2_THREADS / 32)) && i + L::STAGES < ns) {  // (issuing warp rotates)
             fence_proxy_async_smem();
             issue(i + L::STAGES);
         }

@@ -212,6 +212,48 @@ def test_temporal_step_many_tiles_bitwise(cuda):
     assert torch.equal(w0[:, :M], a[:, :M]) and torch.equal(w1[:, :M], b[:, :M])
 
 
+@pytest.mark.parametrize("N,M,Mp", [(3, 3, 4), (5, 7, 8), (9, 150, 152), (40, 145, 148)])
+def test_temporal_step_equals_eight_exact_steps(cuda, N, M, Mp):
+    """Small and ragged grids (one interior cell, grids smaller than the
+    staged window, M not a multiple of the tile): one temporal_step launch
+    equals eight step2d_exact launches value for value, boundary included."""
+    from neuralmech_gb300.wavefd import step2d_exact, temporal_step
+    g = torch.Generator(device="cpu").manual_seed(N * 1000 + M)
+    u0 = torch.zeros((N, Mp))
+    u0[:, :M] = torch.rand((N, M), generator=g) - 0.5
+    u1 = u0.clone()
+    u1[:, :M] += 0.05 * (torch.rand((N, M), generator=g) - 0.5)
+    u0, u1 = u0.to(cuda), u1.to(cuda)
+    args = (1.0, 0.004, 0.01, 0.012, N, M)
+    a, b = u0.clone(), u1.clone()
+    for _ in range(8):
+        a = step2d_exact(a, b, a, *args)
+        a, b = b, a
+    v0, v1 = torch.full_like(u0, 3.0), torch.full_like(u0, 3.0)
+    temporal_step(u0, u1, v0, v1, *args)
+    assert torch.equal(v0[:, :M], a[:, :M]) and torch.equal(v1[:, :M], b[:, :M])
+    assert torch.all(v0[:, M:] == 3.0) and torch.all(v1[:, M:] == 3.0)
+
+
+def test_step2d_exact_single_interior_cell(cuda):
+    """N = M = 3: exactly one updated cell, equal to the expression in FP32."""
+    from neuralmech_gb300.wavefd import step2d_exact
+    f = np.float32
+    u0 = np.arange(12, dtype=f).reshape(3, 4) / f(7)
+    u1 = (np.arange(12, dtype=f).reshape(3, 4) ** 2) / f(50)
+    args = (1.0, 0.004, 0.01, 0.012, 3, 3)
+    got = step2d_exact(torch.from_numpy(u0).to(cuda), torch.from_numpy(u1).to(cuda),
+                       torch.from_numpy(u0.copy()).to(cuda), *args).cpu().numpy()
+    k = f(0.004) * f(0.004) * f(1.0) * f(1.0)
+    two = f(2) * u1[1, 1]
+    li = (u1[0, 1] - two) + u1[2, 1]
+    lj = (u1[1, 0] - two) + u1[1, 2]
+    want = (-u0[1, 1] + two) + k * (li / (f(0.01) * f(0.01)) + lj / (f(0.012) * f(0.012)))
+    expect = u0.copy()
+    expect[1, 1] = want
+    assert np.array_equal(got, expect)
+
+
 def test_temporal_step_rejects_overlapping_outputs(cuda):
     from neuralmech_gb300 import _lib
     from neuralmech_gb300.wavefd import temporal_step

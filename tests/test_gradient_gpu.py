@@ -243,6 +243,12 @@ def test_misfit_gradient_overlap_matches(cuda, orc):
     J2, g2 = misfit_gradient(*args, ob, grid, observed_ready=ready)
     assert abs(J2.item() - J1.item()) <= 1e-12 * J1.item()  # (FP64 atomic sums: order may differ)
     assert rel_l2(g2.cpu().numpy(), g1.cpu().numpy()) < 1e-6
+    # shot groups: the wait comes before the first group's residual
+    import dataclasses
+    grouped = dataclasses.replace(grid, group_shots=2)
+    J3, g3 = misfit_gradient(*args, ob, grouped, observed_ready=ready)
+    assert abs(J3.item() - J1.item()) <= 1e-12 * J1.item()
+    assert rel_l2(g3.cpu().numpy(), g1.cpu().numpy()) < 1e-6
 
 
 def test_shot_groups_match_one_batch(cuda, orc):

@@ -193,17 +193,21 @@ __global__ void __launch_bounds__(VD_THREADS, 2)
             dxr[r] = d;
             st4(FX + (warp * VD_RB + r) * VD_FXW + 4 + 4 * lane,
                 make_float4(bx.x * d.x, bx.y * d.y, bx.z * d.z, bx.w * d.w));
-            if (lane == 0 || lane == 31) {  // the tile's halo half points x0 - 4 .. x0 - 1, x0 + 128 .. x0 + 131
-                const int c0 = lane == 0 ? 0 : 4 * lane + 8;  // first staged column of the window
-                const float4 h0 = ld4(trow(fr) + c0), h1 = ld4(trow(fr) + c0 + 4), h2 = ld4(trow(fr) + c0 + 8);
-                const float hw[12] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w, h2.x, h2.y, h2.z, h2.w};
-                const float4 hd = dx4<R>(hw, a);
-                const float4 c4 = ld4(brow(br) + c0 + 4), c5 = ld4(brow(br) + c0 + 8);
-                const float4 hb = make_float4(0.5f * (c4.x + c4.y), 0.5f * (c4.y + c4.z), 0.5f * (c4.z + c4.w),
-                                              0.5f * (c4.w + c5.x));
-                st4(FX + (warp * VD_RB + r) * VD_FXW + (lane == 0 ? 0 : VD_TX + 4),
-                    make_float4(hb.x * hd.x, hb.y * hd.y, hb.z * hd.z, hb.w * hd.w));
-            }
+        }
+        // the tile's halo half points x0 - 4 .. x0 - 1 and x0 + 128 .. x0 + 131 of
+        // the warp's rows, one per lane of lanes 0 .. 8 RB - 1 (the same sums and
+        // rounding as dx4): half point h of row r sits after the cell in staged
+        // column sc
+        if (lane < 8 * VD_RB) {
+            const int r = lane >> 3, h = lane & 7;
+            const int fr = warp * VD_RB + r + 2 * R, br = warp * VD_RB + r + R;
+            const int sc = h < 4 ? 4 + h : 132 + h;
+            const float* tr = trow(fr);
+            float d = 0.f;
+#pragma unroll
+            for (int k = 1; k <= R; ++k) d = fmaf(a.cs[k - 1], tr[sc + k] - tr[sc - k + 1], d);
+            const float bx = 0.5f * (brow(br)[sc] + brow(br)[sc + 1]);
+            FX[(warp * VD_RB + r) * VD_FXW + (h < 4 ? h : VD_TX + h)] = bx * d;
         }
         // z: own half rows zb, zb + 1 from a window of field rows zb - R + 1 .. zb + R
         {

@@ -163,6 +163,31 @@ def test_dropin_arguments_rejected():
     assert "64" in lib.wfd_last_error().decode() or "aligned" in lib.wfd_last_error().decode()
 
 
+def test_exact_temporal_and_overlap_arguments_rejected():
+    """wfd_step2d_exact, wfd_temporal_step and wfd_misfit_gradient_overlap check
+    their arguments on the host (no launch, no device access here)."""
+    from neuralmech_gb300 import _lib
+    lib = _lib.load()
+    p = ctypes.c_void_p(4096)
+    q = ctypes.c_void_p(4096 + 64 * 64 * 4)       # a separate 64 x 64 field
+    r = ctypes.c_void_p(4096 + 2 * 64 * 64 * 4)
+    t = ctypes.c_void_p(4096 + 3 * 64 * 64 * 4)
+    assert lib.wfd_step2d_exact(None, p, p, 1.0, 1e-3, 1e-2, 1e-2, 64, 60, 64, None) == -1
+    assert lib.wfd_step2d_exact(p, p, p, 1.0, 1e-3, 1e-2, 1e-2, 64, 60, 59, None) == -1  # M_padded < M
+    assert lib.wfd_step2d_exact(p, p, p, 1.0, 1e-3, 1e-2, 1e-2, 2, 60, 64, None) == -1   # N < 3
+    assert lib.wfd_temporal_step(p, q, r, t, 1.0, 1e-3, 1e-2, 1e-2, 64, 60, 62, None) == -1  # M_padded % 4
+    assert lib.wfd_temporal_step(p, q, ctypes.c_void_p(4100), t, 1.0, 1e-3, 1e-2, 1e-2, 64, 60, 64,
+                                 None) == -1  # v0 not 16-byte aligned
+    assert lib.wfd_temporal_step(p, q, p, t, 1.0, 1e-3, 1e-2, 1e-2, 64, 60, 64, None) == -1  # v0 = u0
+    assert "overlap" in lib.wfd_last_error().decode()
+    assert lib.wfd_temporal_step(p, q, r, ctypes.c_void_p(4096 + 2 * 64 * 64 * 4 + 64), 1.0, 1e-3, 1e-2,
+                                 1e-2, 64, 60, 64, None) == -1  # v1 overlaps v0
+    pr = _problem()
+    assert lib.wfd_misfit_gradient_overlap(ctypes.byref(pr), p, None, None, None, p, p, p, p, None, None,
+                                           p, None, p, p, 1 << 20, None) == -1  # no event
+    assert "observed_ready" in lib.wfd_last_error().decode()
+
+
 def test_reduced_precision_fields_halve_the_forward_workspace():
     _, f32 = _ws(_problem(), 0)
     _, f16 = _ws(_problem(field_format=1), 0)

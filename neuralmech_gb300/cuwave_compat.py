@@ -4,7 +4,9 @@ projects/18_fwi (plate.py, helper.py, 2D_fwi.py) and projects/16_neuralopt
 drive the pip package cuwave through a small surface:
   ScalarWave(Nx, dx, N, dt, threads, precision, space_order, wavespeed, density),
   line, shots, point_source, Sensors, sineburst, stable_dt, simulate, measure,
-  misfit, misfit_gradient, resample, Adam.
+  misfit, misfit_gradient, resample, Adam, grid_coords; and, for the absorbing
+  layer of projects/0_conceptual_figures/4_analog_rnn.py:73,95-97,
+  pad_for_sponge and sponge.
 This module offers the same names and call shapes over PyTorch tensors, with
 every time step in the library's CUDA kernels. cuwave's own equations are
 not available (the package is absent), so the choices below are this
@@ -31,6 +33,16 @@ module's own. They are written here so callers can check parity:
   A sin(2 pi f t) sin^2(pi f t / cycles) on 0 <= t <= cycles / f.
 * Array axes follow the reference (x first); they map onto the library's
   (z, x) axes unchanged.
+* Absorbing layer. pad_for_sponge(resolution, dx, thickness) pads every
+  face by ceil(thickness / dx) cells; sponge(sim, field, width, beta) returns
+  the layer for ScalarWave.damping. The library damps with the product of
+  per-axis factors g (u_{n+1} = g (2 u_n + m L u_n) - g^2 u_{n-1}),
+  g = exp(-(a d)^2) at depth d of the layer's W cells and a = s / W. beta is
+  read as the reference states it, the peak damping d dt / 2m at the wall: a
+  centred damping term of that size shrinks the amplitude per step by
+  sqrt((1 - beta) / (1 + beta)), and s is chosen so the wall factor
+  exp(-s^2) equals it. A plain int is a width with the library's default
+  strength.
 * AcousticWave(..., rho1, rho2, kappa1, kappa2): the two-phase medium
   u_tt = kappa div(grad u / rho) + f of projects/8_physics_drivers/
   waveND.py:52-65. Like cuwave (1_benchmark_2D/README.md:141-144) it
@@ -51,6 +63,57 @@ from .wavefd import Grid, misfit_gradient as _misfit_gradient, stable_dt as _sta
 from .wavefd import vd_forward, vd_misfit_gradient, wave_forward_final
 
 
+@dataclass(frozen=True)
+class Sponge:
+    """An absorbing layer: (low, high) widths in cells per axis and the
+    strength s of the factor exp(-(s d / W)^2)."""
+    widths: tuple
+    strength: float
+
+
+def pad_for_sponge(resolution, dx, thickness: float, faces=None):
+    """(Nx, width, origin, region): the grid of `resolution` nodes padded by a
+    layer of `thickness` (length units) on every face, or on `faces` only,
+    given as (axis, side) pairs with side 0 (low) or 1 (high). width is the
+    layer's (low, high) cells per axis, origin the first node of the region of
+    interest, region its index slices."""
+    res = tuple(int(n) for n in resolution)
+    cells = tuple(int(math.ceil(thickness / h - 1e-9)) for h in dx)
+    on = set(faces) if faces is not None else {(a, sd) for a in range(len(res)) for sd in (0, 1)}
+    width = tuple((cells[a] if (a, 0) in on else 0, cells[a] if (a, 1) in on else 0) for a in range(len(res)))
+    Nx = tuple(n + lo + hi for n, (lo, hi) in zip(res, width))
+    origin = tuple(lo for lo, _ in width)
+    region = tuple(slice(o, o + n) for o, n in zip(origin, res))
+    return Nx, width, origin, region
+
+
+def sponge(sim, field, width, beta: float, faces=None) -> "Sponge":
+    """The absorbing layer for ``ScalarWave.damping`` (see the module notes):
+    `width` as pad_for_sponge returns it, or one int for every face; `beta`
+    the peak damping d dt / 2m at the wall; `field` (the reference passes an
+    array of ones of Nx_padded) only has to cover the grid."""
+    if field is not None and any(f < n for f, n in zip(tuple(field.shape), sim.Nx)):
+        raise ValueError("field does not cover the grid")
+    if not 0.0 < beta < 1.0:
+        raise ValueError("beta must lie in (0, 1)")
+    nd = len(sim.Nx)
+    w = [(int(width), int(width))] * nd if isinstance(width, (int, np.integer)) else [tuple(map(int, p)) for p in width]
+    if faces is not None:
+        on = set(faces)
+        w = [(lo if (a, 0) in on else 0, hi if (a, 1) in on else 0) for a, (lo, hi) in enumerate(w)]
+    wall = math.sqrt((1.0 - beta) / (1.0 + beta))
+    return Sponge(tuple(w), math.sqrt(-math.log(wall)))
+
+
+def grid_coords(Nx, dx, dtype=None, device="cuda"):
+    """Node coordinates of a ScalarWave grid, one array per axis
+    (x_i = -dx + i dx, the ghost node first), indexed like the fields."""
+    axes = [torch.arange(n, dtype=torch.float64) * h - h for n, h in zip(Nx, dx)]
+    mesh = torch.meshgrid(*axes, indexing="ij")
+    dt_ = dtype if isinstance(dtype, torch.dtype) else torch.float32
+    return tuple(m.to(device=device, dtype=dt_) for m in mesh)
+
+
 @dataclass
 class ScalarWave:
     """Simulation descriptor (cuwave.scalar.ScalarWave's arguments)."""
@@ -63,7 +126,7 @@ class ScalarWave:
     space_order: int = 2
     wavespeed: float = 1.0
     density: float = 1.0
-    damping: int = 0  # sponge width in cells on every face (0: reflecting plate)
+    damping: object = 0  # a sponge() layer, or its width in cells on every face (0: reflecting plate)
     device: str = "cuda"
 
     @property
@@ -83,8 +146,12 @@ class ScalarWave:
         return tuple((n + 7) // 8 * 8 for n in self.grid_shape)
 
     def grid(self) -> Grid:
+        if isinstance(self.damping, Sponge):
+            return Grid(self.grid_shape, tuple(self.dx), self.dt, self.N, order=self.space_order,
+                        sponge=[tuple(w) for w in self.damping.widths],
+                        sponge_strength=self.damping.strength, src_scale=1.0)
         return Grid(self.grid_shape, tuple(self.dx), self.dt, self.N, order=self.space_order,
-                    sponge=self.damping, src_scale=1.0)
+                    sponge=int(self.damping), src_scale=1.0)
 
     def node(self, coord) -> tuple:
         """Nearest node (padded grid index) of a physical coordinate."""

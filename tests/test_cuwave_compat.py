@@ -24,6 +24,33 @@ def test_geometry_and_helpers():
     assert np.allclose(src.signal, 1e-6 / (1 / 61 * 1 / 77))
 
 
+def test_sponge_helpers():
+    """pad_for_sponge / sponge / grid_coords (4_analog_rnn.py:73,95-97;
+    plate.py:56): widths from the thickness, the region inside, a wall factor
+    that matches the stated peak damping, and node coordinates."""
+    import dataclasses
+    import math
+    from neuralmech_gb300 import cuwave_compat as cw
+    Nx, width, origin, region = cw.pad_for_sponge((100, 80), (0.01, 0.02), 0.1)
+    assert width == ((10, 10), (5, 5)) and Nx == (120, 90) and origin == (10, 5)
+    assert region == (slice(10, 110), slice(5, 85))
+    Nx1, width1, origin1, _ = cw.pad_for_sponge((100, 80), (0.01, 0.02), 0.1, faces=[(0, 1), (1, 0)])
+    assert width1 == ((0, 10), (5, 0)) and Nx1 == (110, 85) and origin1 == (0, 5)
+    sim = cw.ScalarWave(Nx, (0.01, 0.02), 50, 1e-4, space_order=8)
+    layer = cw.sponge(sim, torch.ones(sim.Nx_padded), width, 0.1)
+    assert math.isclose(math.exp(-layer.strength ** 2), math.sqrt(0.9 / 1.1), rel_tol=1e-12)
+    g = dataclasses.replace(sim, damping=layer).grid()
+    assert g.sponge == [(10, 10), (5, 5)] and g.sponge_strength == layer.strength
+    assert dataclasses.replace(sim, damping=7).grid().sponge == 7
+    with pytest.raises(ValueError):
+        cw.sponge(sim, torch.ones(10, 10), width, 0.1)  # field does not cover the grid
+    with pytest.raises(ValueError):
+        cw.sponge(sim, None, width, 1.5)
+    x, y = cw.grid_coords((4, 3), (0.5, 1.0), device="cpu")
+    assert x.shape == (4, 3) and torch.allclose(x[:, 0], torch.tensor([-0.5, 0.0, 0.5, 1.0]))
+    assert torch.allclose(y[0], torch.tensor([-1.0, 0.0, 1.0]))
+
+
 def test_resample_and_adam():
     from neuralmech_gb300 import cuwave_compat as cw
     r = torch.arange(10, dtype=torch.float32)[:, None].repeat(1, 3)
@@ -106,6 +133,29 @@ def test_indicator_gradient_finite_difference(cuda, orc):
     fd = (J(gamma + d) - J(gamma - d)) / 2
     an = float((grad.double() * d.double()).sum())
     assert abs(fd - an) < 2e-3 * abs(fd), (fd, an)
+
+
+@pytest.mark.gpu
+def test_sponge_absorbs(cuda):
+    """A pulse in a padded plate: with the sponge layer the field left after
+    it has crossed the plate several times is far smaller than with
+    reflecting edges."""
+    import dataclasses
+    from neuralmech_gb300 import cuwave_compat as cw
+    Nx, width, origin, region = cw.pad_for_sponge((81, 81), (1 / 78, 1 / 78), 0.15)
+    dx = (1 / 78, 1 / 78)
+    dt = 0.5 * cw.stable_dt(dx, 1.0, 8)
+    N = int(3.0 / dt)
+    sim = cw.ScalarWave(Nx, dx, N, dt, space_order=8)
+    t = np.arange(N) * dt
+    src = cw.point_source(sim, ((origin[0] + 40) * dx[0] - dx[0], (origin[1] + 40) * dx[1] - dx[1]),
+                          cw.sineburst(t, 1.0, 8.0, 2))
+    gamma = torch.ones(sim.Nx_padded, device=cuda)
+    plain = cw.simulate(sim, src, gamma)
+    damped = cw.simulate(dataclasses.replace(sim, damping=cw.sponge(sim, gamma, width, 0.1)), src, gamma)
+    e_plain = float((plain[region] ** 2).sum())
+    e_damped = float((damped[region] ** 2).sum())
+    assert np.isfinite(e_damped) and e_damped < 0.05 * e_plain
 
 
 @pytest.mark.gpu

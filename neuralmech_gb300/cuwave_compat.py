@@ -53,6 +53,7 @@ module's own. They are written here so callers can check parity:
 """
 from __future__ import annotations
 
+import dataclasses
 import math
 from dataclasses import dataclass, field
 
@@ -224,6 +225,11 @@ class Sensors:
     def __post_init__(self):
         self.nodes = np.array([self.sim.node(c) for c in np.atleast_2d(self.coords)], dtype=np.int32)
 
+    def traces(self, um):
+        """The sensor traces (N, nsensors) of a simulate() record
+        (4_analog_rnn.py:128): the record already holds them."""
+        return um
+
 
 def _batch(sim, sources, sensors):
     srcs = list(sources) if isinstance(sources, (list, tuple)) else [sources]
@@ -244,18 +250,50 @@ def measure(sim: ScalarWave, sources, indicator, sensors: Sensors):
     return list(tr.unbind(0))
 
 
-def simulate(sim: ScalarWave, source: Source, indicator, sensors: Sensors | None = None):
-    """Final field u_N of one shot on the physical nodes (shape Nx); with
-    sensors also the record (N, nsensors)
-    (2D_scalar_wave_forward_B_hai.py:30, 4_analog_rnn.py:125-128)."""
-    s = sensors if sensors is not None else Sensors(sim, np.zeros((0, 2)))
+def simulate(sim: ScalarWave, source: Source, indicator, sensors=None, record_every: int | None = None):
+    """One shot. Returns the final field u_N on the physical nodes (shape Nx)
+    (2D_scalar_wave_forward_B_hai.py:30); with `sensors` (a Sensors, or
+    their node array as the reference passes it) also the record um
+    (N, nsensors); with `record_every` k also the frames u_0, u_k, u_2k, ...
+    on the physical nodes (animate_bhai_waves.py:29, 4_analog_rnn.py:125-128):
+    u, (u, um), (u, frames) or (u, um, frames). The library forward starts
+    from rest, so frame j is a forward of j k steps: frames cost
+    O(N^2 / k) steps, meant for the few snapshots a figure takes."""
+    if sensors is None:
+        s = Sensors(sim, np.zeros((0, 2)))
+    elif isinstance(sensors, Sensors):
+        s = sensors
+    else:  # a node array (padded-grid indices), as Sensors.nodes holds them
+        s = Sensors(sim, np.zeros((0, 2)))
+        s.nodes = np.atleast_2d(np.asarray(sensors, dtype=np.int32))
     src, wav, rec = _batch(sim, source, s)
     vel = sim.velocity(indicator)
     rec_t = torch.from_numpy(rec) if rec.shape[1] > 0 else torch.zeros((1, 0, 2), dtype=torch.int32)
-    traces, final = wave_forward_final(vel, torch.from_numpy(wav).to(vel.device), src, rec_t, sim.grid())
+    wav_t = torch.from_numpy(wav).to(vel.device)
+    grid = sim.grid()
+    traces, final = wave_forward_final(vel, wav_t, src, rec_t, grid)
     m = sim.margin
-    u = final[0, m:m + sim.Nx[0], m:m + sim.Nx[1]]
-    return (u, traces[0]) if sensors is not None else u
+
+    def physical(f):
+        return f[0, m:m + sim.Nx[0], m:m + sim.Nx[1]]
+
+    u = physical(final)
+    out = [u]
+    if sensors is not None:
+        out.append(traces[0])
+    if record_every:
+        k = int(record_every)
+        frames = [torch.zeros_like(u)]
+        none = torch.zeros((1, 0, 2), dtype=torch.int32)
+        for j in range(1, sim.N // k + 1):
+            n = j * k
+            if n == sim.N:
+                frames.append(u)
+                continue
+            g = dataclasses.replace(grid, nt=n, ckpt_every=0)
+            frames.append(physical(wave_forward_final(vel, wav_t[:, :n], src, none, g)[1]))
+        out.append(torch.stack(frames))
+    return out[0] if len(out) == 1 else tuple(out)
 
 
 def resample(record, dt_obs: float, dt: float, N: int):

@@ -159,6 +159,25 @@ def test_sponge_absorbs(cuda):
 
 
 @pytest.mark.gpu
+def test_simulate_frames_and_node_sensors(cuda):
+    """simulate(..., sensors=sensors.nodes, record_every=k) returns
+    (u, um, frames) as the analog-RNN drivers unpack it: um equals the record
+    with a Sensors object, frame j equals the final field of a j k-step run,
+    the last frame is u; Sensors.traces(um) is the record."""
+    import dataclasses
+    cw, sim, sources, sensors, gamma_true = _plate(cuda, N=120)
+    u, um = cw.simulate(sim, sources[3], gamma_true, sensors)
+    u2, um2, frames = cw.simulate(sim, sources[3], gamma_true, sensors=sensors.nodes, record_every=40)
+    assert torch.equal(u2, u) and torch.equal(um2, um) and torch.equal(sensors.traces(um2), um2)
+    assert frames.shape == (4,) + tuple(sim.Nx) and torch.all(frames[0] == 0) and torch.equal(frames[3], u)
+    short = dataclasses.replace(sim, N=80)
+    src80 = cw.Source(sources[3].nodes, sources[3].signal[:80])
+    assert rel_l2(frames[2].cpu().numpy(), cw.simulate(short, src80, gamma_true).cpu().numpy()) < 1e-6
+    u3, snaps = cw.simulate(sim, sources[3], gamma_true, record_every=60)
+    assert torch.equal(u3, u) and snaps.shape[0] == 3
+
+
+@pytest.mark.gpu
 def test_simulate_matches_measure(cuda):
     cw, sim, sources, sensors, gamma_true = _plate(cuda, N=120)
     u, record = cw.simulate(sim, sources[3], gamma_true, sensors)

@@ -24,7 +24,9 @@ module's own. They are written here so callers can check parity:
   drivers put them, in [:nx, :ny] of an array of shape Nx or larger
   (helper.py:76-77, 2D_fwi.py:176), and their edge values extend into the
   margin. Gradients come back in the indicator's shape and place. Nx_padded
-  rounds each axis up to a multiple of 8.
+  rounds each axis up to a multiple of 8. ScalarWave also takes 3D grids
+  (nx, ny, nz), as projects/8_physics_drivers/waveND.py does with DIM = 3;
+  AcousticWave is 2D.
 * Coordinates map to the nearest node, as cuwave's point sources and sensors
   do. point_source divides the signal by the cell volume dx dy
   (projects/9_structural_optimization/README.md:87) and scales it by dt^2
@@ -158,18 +160,29 @@ class ScalarWave:
         """Nearest node (padded grid index) of a physical coordinate."""
         return tuple(int(round(c / h)) + 1 + self.margin for c, h in zip(coord, self.dx))
 
-    def velocity(self, indicator) -> torch.Tensor:
-        """c = wavespeed sqrt(gamma) on the padded grid; gamma is read from
-        [:nx, :ny] of the indicator and extends into the margin."""
+    @property
+    def interior(self) -> tuple:
+        """Index slices of the Nx nodes on the library's grid."""
+        return tuple(slice(self.margin, self.margin + n) for n in self.Nx)
+
+    def extend(self, indicator) -> torch.Tensor:
+        """gamma on the library's grid: read from [:nx, :ny(, :nz)] of the
+        indicator, edge values extended into the margin."""
         g = torch.as_tensor(indicator, device=self.device, dtype=torch.float32)
-        nx, ny = self.Nx
-        if g.dim() != 2 or g.shape[0] < nx or g.shape[1] < ny:
+        nd = len(self.Nx)
+        if nd not in (2, 3):
+            raise ValueError(f"{nd}-dimensional grids are not supported (2 or 3)")
+        if g.dim() != nd or any(a < n for a, n in zip(g.shape, self.Nx)):
             raise ValueError(f"indicator of shape {tuple(g.shape)} does not cover {self.Nx}")
-        g = g[:nx, :ny]
+        g = g[tuple(slice(0, n) for n in self.Nx)]
         m = self.margin
         if m:
-            g = torch.nn.functional.pad(g[None, None], (m, m, m, m), mode="replicate")[0, 0]
-        return self.wavespeed * torch.sqrt(g.clamp_min(0.0))
+            g = torch.nn.functional.pad(g[None, None], (m, m) * nd, mode="replicate")[0, 0]
+        return g
+
+    def velocity(self, indicator) -> torch.Tensor:
+        """c = wavespeed sqrt(gamma) on the library's grid."""
+        return self.wavespeed * torch.sqrt(self.extend(indicator).clamp_min(0.0))
 
 
 def stable_dt(dx, c: float, order: int) -> float:
@@ -191,7 +204,7 @@ def line(a, b, n: int) -> np.ndarray:
 
 @dataclass
 class Source:
-    nodes: np.ndarray   # (nsrc, 2) padded-grid indices
+    nodes: np.ndarray   # (nsrc, D) padded-grid indices
     signal: np.ndarray  # (N, nsrc)
 
 
@@ -259,23 +272,23 @@ def simulate(sim: ScalarWave, source: Source, indicator, sensors=None, record_ev
     u, (u, um), (u, frames) or (u, um, frames). The library forward starts
     from rest, so frame j is a forward of j k steps: frames cost
     O(N^2 / k) steps, meant for the few snapshots a figure takes."""
+    nd = len(sim.Nx)
     if sensors is None:
-        s = Sensors(sim, np.zeros((0, 2)))
+        s = Sensors(sim, np.zeros((0, nd)))
     elif isinstance(sensors, Sensors):
         s = sensors
     else:  # a node array (padded-grid indices), as Sensors.nodes holds them
-        s = Sensors(sim, np.zeros((0, 2)))
-        s.nodes = np.atleast_2d(np.asarray(sensors, dtype=np.int32))
+        s = Sensors(sim, np.zeros((0, nd)))
+        s.nodes = np.asarray(sensors, dtype=np.int32).reshape(-1, nd)
     src, wav, rec = _batch(sim, source, s)
     vel = sim.velocity(indicator)
-    rec_t = torch.from_numpy(rec) if rec.shape[1] > 0 else torch.zeros((1, 0, 2), dtype=torch.int32)
+    rec_t = torch.from_numpy(rec) if rec.shape[1] > 0 else torch.zeros((1, 0, nd), dtype=torch.int32)
     wav_t = torch.from_numpy(wav).to(vel.device)
     grid = sim.grid()
     traces, final = wave_forward_final(vel, wav_t, src, rec_t, grid)
-    m = sim.margin
 
     def physical(f):
-        return f[0, m:m + sim.Nx[0], m:m + sim.Nx[1]]
+        return f[(0,) + sim.interior]
 
     u = physical(final)
     out = [u]
@@ -284,7 +297,7 @@ def simulate(sim: ScalarWave, source: Source, indicator, sensors=None, record_ev
     if record_every:
         k = int(record_every)
         frames = [torch.zeros_like(u)]
-        none = torch.zeros((1, 0, 2), dtype=torch.int32)
+        none = torch.zeros((1, 0, nd), dtype=torch.int32)
         for j in range(1, sim.N // k + 1):
             n = j * k
             if n == sim.N:
@@ -317,9 +330,8 @@ def misfit_gradient(sim: ScalarWave, sources, indicator, sensors: Sensors, obser
     J, gv = _misfit_gradient(vel, torch.from_numpy(wav).to(vel.device), src, rec, obs, sim.grid())
     # c = w sqrt(gamma): d cost / d gamma = d cost / d c * w^2 / (2 c)
     g_pad = gv * (sim.wavespeed ** 2) / (2.0 * vel.clamp_min(1e-6 * sim.wavespeed))
-    m = sim.margin
     out = torch.zeros_like(gamma)
-    out[:sim.Nx[0], :sim.Nx[1]] = g_pad[m:m + sim.Nx[0], m:m + sim.Nx[1]]
+    out[tuple(slice(0, n) for n in sim.Nx)] = g_pad[sim.interior]
     return J, out
 
 
@@ -358,16 +370,10 @@ class AcousticWave(ScalarWave):
     kappa2: float = 6.87e8
 
     def indicator(self, indicator) -> torch.Tensor:
-        """gamma on the padded grid: read from [:nx, :ny], edges extended."""
-        g = torch.as_tensor(indicator, device=self.device, dtype=torch.float32)
-        nx, ny = self.Nx
-        if g.dim() != 2 or g.shape[0] < nx or g.shape[1] < ny:
-            raise ValueError(f"indicator of shape {tuple(g.shape)} does not cover {self.Nx}")
-        g = g[:nx, :ny]
-        m = self.margin
-        if m:
-            g = torch.nn.functional.pad(g[None, None], (m, m, m, m), mode="replicate")[0, 0]
-        return g
+        """gamma on the library's grid (the variable-density kernels are 2D)."""
+        if len(self.Nx) != 2:
+            raise ValueError("AcousticWave runs on 2D grids")
+        return self.extend(indicator)
 
     def materials(self, indicator):
         """(kappa, rho) on the padded grid from 1/rho and 1/kappa linear in gamma."""
@@ -419,7 +425,6 @@ def acoustic_misfit_gradient(sim: AcousticWave, sources, indicator, sensors: Sen
         contrib = (gw[si].double() * sig).sum(0)
         for j, (a, b) in enumerate(s.nodes):
             g_pad[a, b] += contrib[j]
-    m = sim.margin
     out = torch.zeros_like(gamma)
-    out[:sim.Nx[0], :sim.Nx[1]] = g_pad[m:m + sim.Nx[0], m:m + sim.Nx[1]].float()
+    out[tuple(slice(0, n) for n in sim.Nx)] = g_pad[sim.interior].float()
     return J, out

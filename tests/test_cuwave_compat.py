@@ -178,6 +178,34 @@ def test_simulate_frames_and_node_sensors(cuda):
 
 
 @pytest.mark.gpu
+def test_simulate_3d_against_oracle(cuda, orc):
+    """waveND.py with DIM = 3: ScalarWave on a cube, a point source at the
+    origin, simulate() with sensors and frames. The final field and the
+    record match the FP64 oracle run on the adapter's grid and positions."""
+    from neuralmech_gb300 import cuwave_compat as cw
+    n, N, order = 28, 60, 4
+    dx = (1.0 / (n - 3),) * 3
+    dt = 0.9 * cw.stable_dt(dx, 0.5, order)
+    sim = cw.ScalarWave((n,) * 3, dx, N, dt, (4, 4, 64), space_order=order, wavespeed=0.5, density=1.0)
+    t = np.arange(N) * dt
+    source = cw.point_source(sim, (0.0, 0.0, 0.0), cw.sineburst(t, 1e3, 8.0, 2))
+    sensors = cw.Sensors(sim, cw.line((0.2, 0.5, 0.3), (0.8, 0.5, 0.3), 5))
+    indicator = torch.ones(sim.Nx_padded, device=cuda)
+    indicator[10:16, 10:16, 10:16] = 0.25
+    u, um, frames = cw.simulate(sim, source, indicator, sensors=sensors, record_every=20)
+    assert u.shape == (n,) * 3 and um.shape == (N, 5) and frames.shape == (4,) + (n,) * 3
+    assert torch.equal(frames[3], u)
+
+    src, wav, rec = cw._batch(sim, source, sensors)
+    geo = orc.Geometry(vel=sim.velocity(indicator).cpu().numpy().astype(np.float64),
+                       wavelet=wav.astype(np.float64), src=src, rec=rec, dt=float(np.float32(dt)),
+                       h=tuple(dx), order=order, sponge=None, src_scale=1.0)
+    tr, fin = orc.forward(geo, want_final=True)
+    assert rel_l2(u.cpu().numpy(), fin[(0,) + sim.interior]) < 1e-5
+    assert rel_l2(um.cpu().numpy(), tr[0]) < 1e-5
+
+
+@pytest.mark.gpu
 def test_simulate_matches_measure(cuda):
     cw, sim, sources, sensors, gamma_true = _plate(cuda, N=120)
     u, record = cw.simulate(sim, sources[3], gamma_true, sensors)

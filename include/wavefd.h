@@ -295,11 +295,24 @@ int wfd_step2d_exact(const float* u0, const float* u1, float* u2, float wavespee
  * store_levels keeps forward levels as in the constant-density path).
  * wfd_vd_misfit_gradient returns dJ/dkappa and dJ/drho, each [nz][nx] and
  * summed over the shots, and optionally dJ/dwavelet.
+ * The CFL check reads p->vmax as the operator's speed bound:
+ *     vmax^2 >= max_i kappa_i (B_i^z / dz^2 + B_i^x / dx^2) / (2 C (1/dz^2 + 1/dx^2)),
+ *     B_i = sum_k |c_k| (b_{i+k-1/2} + b_{i-k+1/2}) along that axis,  C = sum_k |c_k|,
+ * the absolute row sums of the operator (Gershgorin). For smooth media that
+ * is max kappa / rho; where 1/rho jumps between neighbours (air beside a
+ * solid) it is up to ~100x larger, and a vmax of max sqrt(kappa/rho) there
+ * lets an unstable dt through. neuralmech_gb300.wavefd.vd_vmax computes it.
  */
 int wfd_vd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes);
 int wfd_vd_forward(const wfd_problem* p, const float* kappa, const float* rho, const float* sponge_z,
                    const float* sponge_x, const float* wavelet, const int32_t* src, const int32_t* rec,
                    float* traces, void* workspace, size_t workspace_bytes, void* stream);
+/* wfd_vd_forward plus the last field u_nt of every shot, [nshot][nz][nx]
+ * (cuwave simulate on an AcousticWave, projects/8_physics_drivers/waveND.py:94
+ * with FORMULATION = "acoustic"). */
+int wfd_vd_forward_final(const wfd_problem* p, const float* kappa, const float* rho, const float* sponge_z,
+                         const float* sponge_x, const float* wavelet, const int32_t* src, const int32_t* rec,
+                         float* traces, float* u_final, void* workspace, size_t workspace_bytes, void* stream);
 int wfd_vd_misfit_gradient(const wfd_problem* p, const float* kappa, const float* rho, const float* sponge_z,
                            const float* sponge_x, const float* wavelet, const int32_t* src, const int32_t* rec,
                            const float* observed, float* traces, float* grad_kappa, float* grad_rho,

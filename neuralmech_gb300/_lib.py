@@ -29,7 +29,7 @@ EXPORTS = (
     "wfd_kernel_launches", "wfd_profile_begin", "wfd_profile_end", "wfd_forward_static",
     "wfd_analytic_signal", "wfd_tfm", "wfd_forward_final", "wfd_step2d_mixed", "wfd_step2d_scaled",
     "wfd_temporal_step", "wfd_step2d_exact", "wfd_misfit_gradient_overlap",
-    "wfd_step1d", "wfd_vd_workspace_bytes", "wfd_vd_forward", "wfd_vd_misfit_gradient",
+    "wfd_step1d", "wfd_vd_workspace_bytes", "wfd_vd_forward", "wfd_vd_forward_final", "wfd_vd_misfit_gradient",
 )
 
 
@@ -109,6 +109,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         lib.wfd_step1d.argtypes = [f, f, f, F, F, F, I, vp]
         lib.wfd_vd_workspace_bytes.argtypes = [P, ctypes.c_int, ctypes.POINTER(sz)]
         lib.wfd_vd_forward.argtypes = [P, f, f, f, f, f, i32, i32, f, vp, sz, vp]
+        lib.wfd_vd_forward_final.argtypes = [P, f, f, f, f, f, i32, i32, f, f, vp, sz, vp]
         lib.wfd_vd_misfit_gradient.argtypes = [P, f, f, f, f, f, i32, i32, f, f, f, f, f, d, vp, sz, vp]
         lib.wfd_kernel_launches.argtypes = []
         lib.wfd_kernel_launches.restype = ctypes.c_uint64

@@ -1414,6 +1414,29 @@ int wfd_vd_forward(const wfd_problem* p, const float* kappa, const float* rho, c
     return run_forward(p, g, L, w, st, wavelet, traces, false);
 }
 
+int wfd_vd_forward_final(const wfd_problem* p, const float* kappa, const float* rho, const float* sponge_z,
+                         const float* sponge_x, const float* wavelet, const int32_t* src, const int32_t* rec,
+                         float* traces, float* u_final, void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = vd_checks(p, kappa, rho, wavelet, src, rec);
+    if (rc) return rc;
+    if (!u_final) return fail(WFD_ERR_INVALID, "u_final is NULL");
+    const Geom g = make_geom(p, 0, 0, true);
+    const Layout L = make_layout(p, g, false);
+    if ((rc = check_workspace(workspace, workspace_bytes, L.total))) return rc;
+    Work w = carve(workspace, L, false);
+    w.rho = rho;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if ((rc = setup(p, g, w, kappa, src, rec, s))) return rc;
+    Stepper st{p, g, s, w.err, w.m, sponge_z, nullptr, sponge_x};
+    st.bfield = w.b;
+    if ((rc = st.init())) return rc;
+    int fb = 0;
+    if ((rc = run_forward(p, g, L, w, st, wavelet, traces, false, &fb))) return rc;
+    WFD_CUDA(cudaMemcpy2DAsync(u_final, (size_t)g.nx * 4, w.P[fb], (size_t)g.ld * 4, (size_t)g.nx * 4,
+                               (size_t)p->nshot * g.nz, cudaMemcpyDeviceToDevice, s));
+    return WFD_OK;
+}
+
 int wfd_vd_misfit_gradient(const wfd_problem* p, const float* kappa, const float* rho, const float* sponge_z,
                            const float* sponge_x, const float* wavelet, const int32_t* src, const int32_t* rec,
                            const float* observed, float* traces, float* grad_kappa, float* grad_rho,

@@ -63,7 +63,7 @@ import numpy as np
 import torch
 
 from .wavefd import Grid, misfit_gradient as _misfit_gradient, stable_dt as _stable_dt, wave_forward
-from .wavefd import vd_forward, vd_misfit_gradient, wave_forward_final
+from .wavefd import vd_forward, vd_forward_final, vd_misfit_gradient, vd_vmax, wave_forward_final
 
 
 @dataclass(frozen=True)
@@ -269,7 +269,8 @@ def simulate(sim: ScalarWave, source: Source, indicator, sensors=None, record_ev
     their node array as the reference passes it) also the record um
     (N, nsensors); with `record_every` k also the frames u_0, u_k, u_2k, ...
     on the physical nodes (animate_bhai_waves.py:29, 4_analog_rnn.py:125-128):
-    u, (u, um), (u, frames) or (u, um, frames). The library forward starts
+    u, (u, um), (u, frames) or (u, um, frames). An AcousticWave runs the
+    two-phase medium (waveND.py:52-65,94). The library forward starts
     from rest, so frame j is a forward of j k steps: frames cost
     O(N^2 / k) steps, meant for the few snapshots a figure takes."""
     nd = len(sim.Nx)
@@ -280,12 +281,21 @@ def simulate(sim: ScalarWave, source: Source, indicator, sensors=None, record_ev
     else:  # a node array (padded-grid indices), as Sensors.nodes holds them
         s = Sensors(sim, np.zeros((0, nd)))
         s.nodes = np.asarray(sensors, dtype=np.int32).reshape(-1, nd)
+    acoustic = isinstance(sim, AcousticWave)
+    if acoustic:  # the two-phase medium on the variable-density kernels
+        kap, rho = sim.materials(indicator)
+        source = _scaled_sources(sim, source, indicator)
+    else:
+        vel = sim.velocity(indicator)
     src, wav, rec = _batch(sim, source, s)
-    vel = sim.velocity(indicator)
     rec_t = torch.from_numpy(rec) if rec.shape[1] > 0 else torch.zeros((1, 0, nd), dtype=torch.int32)
-    wav_t = torch.from_numpy(wav).to(vel.device)
+    wav_t = torch.from_numpy(wav).to(sim.device)
     grid = sim.grid()
-    traces, final = wave_forward_final(vel, wav_t, src, rec_t, grid)
+
+    def run(g, w, r):
+        return vd_forward_final(kap, rho, w, src, r, g) if acoustic else wave_forward_final(vel, w, src, r, g)
+
+    traces, final = run(grid, wav_t, rec_t)
 
     def physical(f):
         return f[(0,) + sim.interior]
@@ -304,7 +314,7 @@ def simulate(sim: ScalarWave, source: Source, indicator, sensors=None, record_ev
                 frames.append(u)
                 continue
             g = dataclasses.replace(grid, nt=n, ckpt_every=0)
-            frames.append(physical(wave_forward_final(vel, wav_t[:, :n], src, none, g)[1]))
+            frames.append(physical(run(g, wav_t[:, :n], none)[1]))
         out.append(torch.stack(frames))
     return out[0] if len(out) == 1 else tuple(out)
 
@@ -385,6 +395,13 @@ class AcousticWave(ScalarWave):
     def velocity(self, indicator) -> torch.Tensor:
         kap, rho = self.materials(indicator)
         return torch.sqrt(kap / rho)
+
+    def max_speed(self, indicator) -> float:
+        """The speed to give stable_dt for this medium: sqrt(kappa / rho) in
+        a smooth medium, larger where 1/rho jumps between cells (air beside
+        a solid), as the staggered step's stability requires."""
+        kap, rho = self.materials(indicator)
+        return vd_vmax(kap, rho, self.space_order, tuple(self.dx))
 
 
 def _scaled_sources(sim: AcousticWave, sources, indicator):

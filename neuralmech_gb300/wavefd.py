@@ -525,8 +525,55 @@ def _vd_prepare(kappa, rho, wavelet, src, rec, grid: Grid, nshot=None):
         raise ValueError(f"rho has shape {tuple(rho.shape)}, grid {grid.shape}")
     rho = rho.detach().to(torch.float32).contiguous()
     call = _prepare(kappa, torch.as_tensor(wavelet, device=kappa.device), src, rec, grid, nshot)
-    call.problem.vmax = float(torch.sqrt((call.vel / rho).max()))
+    call.problem.vmax = vd_vmax(call.vel, rho, grid.order, grid.spacing)
     return call, rho
+
+
+def _stag_weights(R: int) -> list:
+    """Staggered first-derivative weights c_1..c_R (unit grid): the
+    Lagrange-product form, exact on polynomials up to degree 2R - 1."""
+    c = []
+    for k in range(1, R + 1):
+        v = 1.0 / (2 * k - 1)
+        for m in range(1, R + 1):
+            if m != k:
+                a, b = (2 * m - 1) ** 2, (2 * k - 1) ** 2
+                v *= a / (a - b)
+        c.append(v)
+    return c
+
+
+def vd_vmax(kappa: torch.Tensor, rho: torch.Tensor, order: int, spacing=(1.0, 1.0)) -> float:
+    """The speed that bounds the variable-density operator for the CFL check
+    (vmax dt sqrt(S (1/dz^2 + 1/dx^2)) <= 2, S = 4 (sum |c_k|)^2).
+
+    Row i of kappa Lb along one axis is kappa_i sum_k c_k (F_{i+k-1/2} -
+    F_{i-k+1/2}) with F = b_half D u, b_half the mean of two cells' b = 1/rho.
+    Its absolute sum is at most kappa_i 2 sum|c| B_i, B_i = sum_k |c_k|
+    (b_{i+k-1/2} + b_{i-k+1/2}), which bounds the spectral radius
+    (Gershgorin). vmax^2 = max_i kappa_i (B_i^z / dz^2 + B_i^x / dx^2) /
+    (2 sum|c| (1/dz^2 + 1/dx^2)): max kappa / rho in a smooth medium, larger
+    where 1/rho jumps (air beside a solid), where a cell's stiffness meets its
+    neighbour's large 1/rho and the step's stability follows that product."""
+    R = order // 2
+    c = _stag_weights(R)
+    csum = sum(abs(v) for v in c)
+    b = 1.0 / rho.detach().double()
+    kap = kappa.detach().double()
+    dz, dx = float(spacing[0]), float(spacing[-1])
+
+    def B(f):  # along the last axis of f
+        n = f.shape[-1]
+        fp = torch.nn.functional.pad(f, (R + 1, R + 1))   # b zero outside the grid
+        bh = 0.5 * (fp[..., :-1] + fp[..., 1:])           # bh[.., q] = b at q - R - 1/2
+        out = torch.zeros_like(f)
+        for k in range(1, R + 1):
+            # half points i + k - 1/2 and i - k + 1/2 are q = i + k + R and q = i - k + R + 1
+            out += abs(c[k - 1]) * (bh[..., k + R:k + R + n] + bh[..., R + 1 - k:R + 1 - k + n])
+        return out
+
+    row = kap * (B(b.t()).t() / dz ** 2 + B(b) / dx ** 2)
+    return float(torch.sqrt(row.max() / (2.0 * csum * (1.0 / dz ** 2 + 1.0 / dx ** 2))))
 
 
 def _vd_workspace(call: _Call, with_gradient: bool) -> torch.Tensor:
@@ -554,6 +601,25 @@ def vd_forward(kappa: torch.Tensor, rho: torch.Tensor, wavelet, src, rec, grid: 
     if check:
         _status(ws, "wfd_vd_forward")
     return traces
+
+
+def vd_forward_final(kappa: torch.Tensor, rho: torch.Tensor, wavelet, src, rec, grid: Grid, *,
+                     check: bool = True):
+    """(traces, u_final): vd_forward plus the last field u_nt of every shot,
+    shaped (nshot,) + grid.shape (no autograd)."""
+    call, rho = _vd_prepare(kappa, rho, wavelet, src, rec, grid)
+    p = call.problem
+    ws = _vd_workspace(call, False)
+    traces = torch.empty((p.nshot, p.nt, p.nrec), dtype=torch.float32, device=kappa.device)
+    final = torch.empty((p.nshot,) + tuple(grid.shape), dtype=torch.float32, device=kappa.device)
+    gz, _, gx = call.sponges
+    _lib.check(_lib.load().wfd_vd_forward_final(ctypes.byref(p), _ptr(call.vel), _ptr(rho), _ptr(gz), _ptr(gx),
+                                                _ptr(call.wavelet), _ptr(call.src), _ptr(call.rec), _ptr(traces),
+                                                _ptr(final), _ptr(ws), ws.numel(), _stream()),
+               "wfd_vd_forward_final")
+    if check:
+        _status(ws, "wfd_vd_forward_final")
+    return traces, final
 
 
 def vd_misfit_gradient(kappa: torch.Tensor, rho: torch.Tensor, wavelet, src, rec, observed: torch.Tensor,

@@ -206,6 +206,48 @@ def test_simulate_3d_against_oracle(cuda, orc):
 
 
 @pytest.mark.gpu
+def test_simulate_acoustic_against_oracle(cuda, orc):
+    """waveND.py with FORMULATION = "acoustic": simulate() on an AcousticWave
+    runs the two-phase medium. Final field, record and frames against the FP64
+    variable-density oracle on the adapter's grid, materials and signals."""
+    import dataclasses
+    from neuralmech_gb300 import cuwave_compat as cw
+    n, N = 48, 600
+    dx = (1.0 / (n - 3),) * 2
+    sim = cw.AcousticWave((n, n), dx, N, 1.0, space_order=4, rho1=1.204, rho2=2643.0, kappa1=1.419e5, kappa2=6.87e8)
+    gamma = torch.ones((n, n), device=cuda)
+    gamma[20:30, 15:35] = 0.3  # an air-like pocket in the solid: 1/rho jumps 1500x at its walls
+    # the walls set the step: a solid cell beside the pocket meets the air's 1/rho
+    vmax = sim.max_speed(gamma)
+    assert vmax > 10 * float(sim.velocity(gamma).max())
+    dt = 0.8 * cw.stable_dt(dx, vmax, 4)
+    sim = dataclasses.replace(sim, dt=dt)
+    t = np.arange(N) * dt
+    source = cw.point_source(sim, (0.43, 0.45), cw.sineburst(t, 1e3, 6.0 / (N * dt), 2))
+    sensors = cw.Sensors(sim, cw.line((0.35, 0.55), (0.55, 0.55), 4))
+    u, um, frames = cw.simulate(sim, source, gamma, sensors=sensors.nodes, record_every=200)
+    assert u.shape == (n, n) and um.shape == (N, 4) and frames.shape == (4, n, n)
+    assert torch.isfinite(u).all() and u.abs().max() > 0 and torch.equal(frames[3], u)
+
+    kap, rho = (a.cpu().numpy().astype(np.float64) for a in sim.materials(gamma))
+    src, wav, rec = cw._batch(sim, cw._scaled_sources(sim, source, gamma), sensors)
+    p3 = lambda p: np.stack([p[..., 0], 0 * p[..., 0], p[..., 1]], -1).astype(np.int32)
+
+    def oracle(nt):
+        geo = orc.VdGeometry(kap, rho, wav[:, :nt].astype(np.float64), p3(src), p3(rec), float(np.float32(dt)),
+                             tuple(dx), order=4)
+        return orc.vd_forward(geo, want_final=True)
+
+    # FP32 against FP64 over 600 steps across a 1500x jump of 1/rho: 1.8e-5
+    # measured on the final field; 5e-5 leaves room for the rounding's spread
+    tol = 5e-5
+    tr, fin = oracle(N)
+    assert rel_l2(u.cpu().numpy(), fin[(0,) + sim.interior]) < tol
+    assert rel_l2(um.cpu().numpy(), tr[0]) < tol
+    assert rel_l2(frames[2].cpu().numpy(), oracle(400)[1][(0,) + sim.interior]) < tol
+
+
+@pytest.mark.gpu
 def test_simulate_matches_measure(cuda):
     cw, sim, sources, sensors, gamma_true = _plate(cuda, N=120)
     u, record = cw.simulate(sim, sources[3], gamma_true, sensors)

@@ -209,3 +209,26 @@ def test_reconstruction_workspace_keeps_frames_not_checkpoints():
     # frame of one shot: 2 * 6 full rows of ld = 104 and 52 rows of 8 + (104 - 92) columns
     frame = 2 * (2 * 6 * 104 + (64 - 12) * (8 + 104 - 92)) * 4
     assert r6 - r0 == 101 * ((frame + 255) // 256 * 256)
+
+
+def test_variable_density_arguments_rejected():
+    """The variable-density entries refuse, before any launch: a NULL u_final,
+    a 3D problem, and a dt inside the collocated CFL bound but outside the
+    staggered operator's (S = 4 (sum|c_k|)^2 = 6.62 at order 8 against 6.50)."""
+    from neuralmech_gb300 import _lib, stable_dt
+    lib = _lib.load()
+    d = ctypes.c_void_p(256)  # never dereferenced: every call fails its host checks
+    ws = ctypes.c_size_t(0)
+
+    def final(p, u_final):
+        return lib.wfd_vd_forward_final(ctypes.byref(p), d, d, None, None, d, d, d, d, u_final, d, ws, None)
+
+    def forward(p):
+        return lib.wfd_vd_forward(ctypes.byref(p), d, d, None, None, d, d, d, d, d, ws, None)
+
+    assert final(_problem(), None) == -1
+    assert forward(_problem(ndim=3, ny=8)) == -1
+    dt = stable_dt((10.0, 10.0), 3000.0, 8)
+    assert _ws(_problem(dt=dt * 0.999))[0] == 0  # the collocated bound holds
+    assert forward(_problem(dt=dt * 0.999)) == -4
+    assert final(_problem(dt=dt * 0.999), d) == -4

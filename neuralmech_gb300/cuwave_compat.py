@@ -4,9 +4,9 @@ projects/18_fwi (plate.py, helper.py, 2D_fwi.py) and projects/16_neuralopt
 drive the pip package cuwave through a small surface:
   ScalarWave(Nx, dx, N, dt, threads, precision, space_order, wavespeed, density),
   line, shots, point_source, Sensors, sineburst, stable_dt, simulate, measure,
-  misfit, misfit_gradient, resample, Adam, grid_coords; and, for the absorbing
-  layer of projects/0_conceptual_figures/4_analog_rnn.py:73,95-97,
-  pad_for_sponge and sponge.
+  misfit, misfit_gradient, resample, Adam, grid_coords, interior_slice; and,
+  for the absorbing layer of projects/0_conceptual_figures/4_analog_rnn.py:
+  73,95-97, pad_for_sponge and sponge.
 This module offers the same names and call shapes over PyTorch tensors, with
 every time step in the library's CUDA kernels. cuwave's own equations are
 not available (the package is absent), so the choices below are this
@@ -106,6 +106,13 @@ def sponge(sim, field, width, beta: float, faces=None) -> "Sponge":
         w = [(lo if (a, 0) in on else 0, hi if (a, 1) in on else 0) for a, (lo, hi) in enumerate(w)]
     wall = math.sqrt((1.0 - beta) / (1.0 + beta))
     return Sponge(tuple(w), math.sqrt(-math.log(wall)))
+
+
+def interior_slice(sim) -> tuple:
+    """Index slices of the nodes on [0, L] along each axis (the ghost node
+    at each end left out), for an indicator or a simulate() field indexed
+    from node 0 (2D_fwi.py:47, 1_benchmark_2D/forward/wave.py:109)."""
+    return tuple(slice(1, n - 1) for n in sim.Nx)
 
 
 def grid_coords(Nx, dx, dtype=None, device="cuda"):

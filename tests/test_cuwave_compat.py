@@ -22,6 +22,12 @@ def test_geometry_and_helpers():
     assert np.all(s[t > 0.2] == 0) and np.abs(s).max() <= 2.0 and np.abs(s).max() > 1.5
     src = cw.point_source(sim, (0.5, 1.0), np.ones(100))
     assert np.allclose(src.signal, 1e-6 / (1 / 61 * 1 / 77))
+    # interior_slice: the nodes on [0, L], as the indicator and simulate() index them
+    inner = cw.interior_slice(sim)
+    assert inner == (slice(1, 63), slice(1, 79))
+    x, y = cw.grid_coords(sim.Nx, sim.dx, device="cpu")
+    assert abs(float(x[inner][0, 0])) < 1e-12 and abs(float(x[inner][-1, 0]) - 1.0) < 1e-6
+    assert abs(float(y[inner][0, -1]) - 1.0) < 1e-6 and x[inner].shape == (62, 78)
 
 
 def test_sponge_helpers():

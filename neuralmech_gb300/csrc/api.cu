@@ -48,10 +48,13 @@ class PhaseScope {
         if (g_profiling) {
             rec_.phase = phase;
             rec_.launches = launches;
-            if (cudaEventCreate(&rec_.start) == cudaSuccess &&
-                cudaEventCreate(&rec_.stop) == cudaSuccess) {
-                cudaEventRecord(rec_.start, s_);
-                active_ = true;
+            if (cudaEventCreate(&rec_.start) == cudaSuccess) {
+                if (cudaEventCreate(&rec_.stop) == cudaSuccess) {
+                    cudaEventRecord(rec_.start, s_);
+                    active_ = true;
+                } else {
+                    cudaEventDestroy(rec_.start);
+                }
             }
         }
     }

@@ -300,7 +300,7 @@ def _wl_temporal(args, dev):
     bufs = [u0, u0.clone(), torch.empty_like(u0), torch.empty_like(u0)]
     state = {"k": 0}
 
-    def step():  # the driver's two pairs of arrays, swapped every launch
+    def step():  # two pairs of arrays, swapped every launch, as 2D_wave_cuda_temporal.py does
         a, b = (0, 1) if state["k"] % 2 == 0 else (2, 3)
         c, d = (2, 3) if state["k"] % 2 == 0 else (0, 1)
         temporal_step(bufs[a], bufs[b], bufs[c], bufs[d], 1.0, dt, dx, dy, N, M)

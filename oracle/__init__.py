@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY. Only ``tests/``, ``__graft_entry__.smoke()`` and the
 CPU-baseline leg of ``bench.py`` may import this package, and only as the
-checker or the timed CPU baseline. The product (``neuralmech_gb300``) never
+reference results of the parity checks or the timed CPU baseline. The product (``neuralmech_gb300``) never
 imports it and has no CPU fallback.
 
 Contents:

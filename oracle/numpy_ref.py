@@ -1,6 +1,6 @@
 """The reference's CPU path for one wave step, in NumPy array slices.
 
-TEST INFRASTRUCTURE ONLY (checker and timed CPU baseline).
+TEST INFRASTRUCTURE ONLY (parity reference and timed CPU baseline).
 
 ``fd_step_order2`` restates ``fd_step`` of
 projects/18_simple_wave_fd/2D_wave_cupy.py:54-62 with ``cp`` replaced by

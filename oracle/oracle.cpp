@@ -1,7 +1,7 @@
 // FP64 CPU oracle for the finite-difference acoustic wave path.
 //
-// TEST INFRASTRUCTURE ONLY. This file is the checker: the parity tests, the
-// smoke check and the CPU baseline of bench.py call it; the product library
+// TEST INFRASTRUCTURE ONLY. The parity tests, the smoke check and the CPU
+// baseline of bench.py call it as their reference; the product library
 // never links, loads or falls back to it.
 //
 // What it restates:

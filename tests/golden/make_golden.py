@@ -1,7 +1,7 @@
 """Generates the golden vectors in this folder from the reference's own step
 kernels, compiled for the CPU from projects/18_simple_wave_fd/step2D_wave.cu and
 step1D_wave.cu by oracle/Makefile.ref (oracle.ref). Needs the reference
-sources, so it runs where they are mounted, never on the GPU machine:
+sources, so it runs where they are mounted, never at test time:
 
     python tests/golden/make_golden.py
 

@@ -280,6 +280,8 @@ def simulate(sim: ScalarWave, source: Source, indicator, sensors=None, record_ev
     two-phase medium (waveND.py:52-65,94). The library forward starts
     from rest, so frame j is a forward of j k steps: frames cost
     O(N^2 / k) steps, meant for the few snapshots a figure takes."""
+    if record_every is not None and int(record_every) < 1:
+        raise ValueError(f"record_every must be at least 1 (got {record_every})")
     nd = len(sim.Nx)
     if sensors is None:
         s = Sensors(sim, np.zeros((0, nd)))
@@ -311,7 +313,7 @@ def simulate(sim: ScalarWave, source: Source, indicator, sensors=None, record_ev
     out = [u]
     if sensors is not None:
         out.append(traces[0])
-    if record_every:
+    if record_every is not None:
         k = int(record_every)
         frames = [torch.zeros_like(u)]
         none = torch.zeros((1, 0, nd), dtype=torch.int32)

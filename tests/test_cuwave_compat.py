@@ -28,6 +28,9 @@ def test_geometry_and_helpers():
     x, y = cw.grid_coords(sim.Nx, sim.dx, device="cpu")
     assert abs(float(x[inner][0, 0])) < 1e-12 and abs(float(x[inner][-1, 0]) - 1.0) < 1e-6
     assert abs(float(y[inner][0, -1]) - 1.0) < 1e-6 and x[inner].shape == (62, 78)
+    for bad in (0, -3):  # refused before any device work
+        with pytest.raises(ValueError):
+            cw.simulate(sim, src, np.ones(sim.Nx), record_every=bad)
 
 
 def test_sponge_helpers():

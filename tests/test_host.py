@@ -167,3 +167,37 @@ def test_vd_speed_bound_covers_jumps(orc, order):
             assert radius > float((k / r).max()) * S * 2.0
     smooth = vd_vmax(torch.full((n, n), 4.0, dtype=torch.float64), torch.full((n, n), 2.0, dtype=torch.float64), order)
     assert abs(smooth - math.sqrt(2.0)) < 1e-12
+
+
+def test_bench_reference_arm_contract():
+    """`bench.py --impl reference` (the CPU arm, no GPU needed) prints one JSON
+    line with the contract's keys: the same metric, unit and config as the GPU
+    arm, a cpu_baseline describing the run, and an e2e block with no copies."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"],
+                         cwd=root, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    r = json.loads(lines[0])
+    assert r["impl"] == "reference" and r["n_gpus"] == 1 and r["steps"] == 1 and r["warmup"] == 0
+    assert r["value"] > 0 and r["ms_per_step"] > 0 and r["higher_is_better"] is True
+    metric = unit = None
+    for ln in open(os.path.join(root, "bench.py")):  # the GPU arm's constants
+        if ln.startswith("METRIC = "):
+            metric = json.loads(ln.split("=", 1)[1])
+        elif ln.startswith("UNIT = "):
+            unit = json.loads(ln.split("=", 1)[1])
+    assert r["metric"] == metric and r["unit"] == unit
+    assert r["scaling"] == "weak" and r["vs_baseline"] is None
+    assert r["data"].startswith("synthetic") and r["config"]["workload"].startswith("fwi1024")
+    cb = r["cpu_baseline"]
+    assert cb["value"] == r["value"] and cb["unit"] == r["unit"] and cb["cores"] >= 1
+    assert cb["kind"] in ("reference", "port") and cb["sample"]
+    e2e = r["e2e"]
+    assert e2e["value"] == r["value"] and e2e["unit"] == r["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0

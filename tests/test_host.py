@@ -1,6 +1,7 @@
 """CPU tests of the Python host layer: argument shaping, sponge profiles, the
-synthetic workload generators, and the refusal of CPU tensors (there is no
-CPU path)."""
+synthetic workload generators, the refusal of CPU tensors (there is no CPU
+path), the variable-density CFL speed bound, and the JSON line of the
+benchmark's CPU reference arm."""
 import math
 
 import numpy as np

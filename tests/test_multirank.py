@@ -2,7 +2,8 @@
 of the multi-GPU path, with the FP64 oracle standing in for each rank's GPU
 gradient. Also the failure path: a rank that raises before the collective
 makes the other rank's all-reduce end with an error after a short timeout
-(no GPU is involved, nothing hangs past the timeout)."""
+(no GPU is involved, nothing hangs past the timeout). And the benchmark's CPU
+reference arm launched under torchrun: one line from rank 0."""
 import datetime
 import os
 import socket
@@ -113,3 +114,22 @@ def test_failed_rank_surfaces_as_collective_error(tmp_path):
     status = _spawn("fail", tmp_path)
     assert status[1].startswith("RuntimeError: rank 1 fails")
     assert status[0] != "ok"  # rank 0's all-reduce ended with an error, not a hang
+
+
+def test_bench_reference_arm_under_torchrun():
+    """`bench.py --impl reference` launched as the multi-GPU bench is (torchrun,
+    two ranks on 127.0.0.1): rank 0 alone times the CPU reference and prints
+    one JSON line for the whole job; the other rank exits 0 without work."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()),
+           "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0"]
+    out = subprocess.run(cmd, cwd=root, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.lstrip().startswith("{")]
+    assert len(lines) == 1
+    r = json.loads(lines[0])
+    assert r["impl"] == "reference" and r["n_gpus"] == 2 and r["value"] > 0

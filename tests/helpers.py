@@ -45,3 +45,39 @@ def oracle_geometry(oracle, grid, v, wav, src, rec):
                            src=p3(src).astype(np.int32), rec=p3(rec).astype(np.int32),
                            dt=float(np.float32(grid.dt)), h=h, order=grid.order, sponge=sp,
                            src_scale=grid.src_scale, ckpt_every=grid.ckpt_every)
+
+
+def vd_operator(kappa, rho, c):
+    """kappa Lb of the variable-density step as a dense matrix on a unit grid,
+    assembled term by term from its definition (rows and columns of the cells
+    outside the fixed ring of R cells): F = b_half D u at the half points,
+    b_half the mean of the two cells' b = 1/rho, Lb u = D F on each axis,
+    (D f)_j = sum_k c_k (f_{j+k} - f_{j-k+1}), fields and b zero outside."""
+    nz, nx = kappa.shape
+    R = len(c)
+    b = 1.0 / rho
+    idx = {}
+    for z in range(R, nz - R):
+        for x in range(R, nx - R):
+            idx[(z, x)] = len(idx)
+    A = np.zeros((len(idx), len(idx)))
+
+    def bcell(z, x):
+        return b[z, x] if 0 <= z < nz and 0 <= x < nx else 0.0
+
+    for (z, x), row in idx.items():
+        for axis in (0, 1):
+            step = (1, 0) if axis == 0 else (0, 1)
+            pos = z if axis == 0 else x
+
+            def cell(q):
+                return (q, x) if axis == 0 else (z, q)
+            for k in range(1, R + 1):
+                for sgn, j in ((1.0, pos + k - 1), (-1.0, pos - k)):  # F at j + 1/2
+                    bh = 0.5 * (bcell(*cell(j)) + bcell(*cell(j + 1)))
+                    for m in range(1, R + 1):
+                        for s2, q in ((1.0, j + m), (-1.0, j - m + 1)):
+                            col = idx.get(cell(q))
+                            if col is not None:
+                                A[row, col] += kappa[z, x] * sgn * c[k - 1] * bh * s2 * c[m - 1]
+    return A

@@ -105,40 +105,6 @@ def test_autotune_selection_and_cache(tmp_path):
     assert best2["step_block"] == 2
 
 
-def _vd_operator(kappa, rho, c):
-    """kappa Lb as a matrix on a unit grid (rows and columns of the cells
-    outside the fixed ring of R cells): F = b_half D u at the half points,
-    Lb u = D F on each axis, fields and b zero outside the grid."""
-    nz, nx = kappa.shape
-    R = len(c)
-    b = 1.0 / rho
-    idx = {}
-    for z in range(R, nz - R):
-        for x in range(R, nx - R):
-            idx[(z, x)] = len(idx)
-    A = np.zeros((len(idx), len(idx)))
-
-    def bcell(z, x):
-        return b[z, x] if 0 <= z < nz and 0 <= x < nx else 0.0
-
-    for (z, x), row in idx.items():
-        for axis in (0, 1):
-            step = (1, 0) if axis == 0 else (0, 1)
-            pos = z if axis == 0 else x
-
-            def cell(q):
-                return (q, x) if axis == 0 else (z, q)
-            for k in range(1, R + 1):
-                for sgn, j in ((1.0, pos + k - 1), (-1.0, pos - k)):  # F at j + 1/2
-                    bh = 0.5 * (bcell(*cell(j)) + bcell(*cell(j + 1)))
-                    for m in range(1, R + 1):
-                        for s2, q in ((1.0, j + m), (-1.0, j - m + 1)):
-                            col = idx.get(cell(q))
-                            if col is not None:
-                                A[row, col] += kappa[z, x] * sgn * c[k - 1] * bh * s2 * c[m - 1]
-    return A
-
-
 @pytest.mark.parametrize("order", [2, 4, 8])
 def test_vd_speed_bound_covers_jumps(orc, order):
     """vd_vmax bounds the spectral radius of kappa Lb, in the form of the
@@ -148,6 +114,7 @@ def test_vd_speed_bound_covers_jumps(orc, order):
     along x and along z) and in a random medium, and within a factor 6 of it.
     max sqrt(kappa / rho) is not a bound at the jump; in a smooth medium the
     two agree."""
+    from helpers import vd_operator
     from neuralmech_gb300.wavefd import _stag_weights, vd_vmax
     c = orc.stag_coeffs(order)
     assert np.allclose(_stag_weights(order // 2), c, rtol=1e-15, atol=0)
@@ -161,7 +128,7 @@ def test_vd_speed_bound_covers_jumps(orc, order):
     cases = [(kappa, rho), (kappa.T.copy(), rho.T.copy()),
              (rng.uniform(1.0, 1e3, (n, n)), rng.uniform(0.01, 10.0, (n, n)))]
     for i, (k, r) in enumerate(cases):
-        radius = float(np.max(np.abs(np.linalg.eigvals(_vd_operator(k, r, c)))))
+        radius = float(np.max(np.abs(np.linalg.eigvals(vd_operator(k, r, c)))))
         bound = vd_vmax(torch.from_numpy(k), torch.from_numpy(r), order) ** 2 * S * 2.0
         assert radius <= bound * (1 + 1e-12) and radius > bound / 6, (i, radius / bound)
         if i < 2:

@@ -298,12 +298,13 @@ def test_vd_constant_density_order2_is_the_scalar_step(orc):
     assert rel_l2(t_vd, t_sc) < 1e-12
 
 
-@pytest.mark.parametrize("order", [2, 4, 8])
-def test_vd_operator_matches_assembled_matrix(orc, order):
+@pytest.mark.parametrize("order,sponge", [(2, False), (4, False), (8, False), (4, True)])
+def test_vd_operator_matches_assembled_matrix(orc, order, sponge):
     """The oracle's variable-density step applies the documented staggered
-    operator: from a random u_1 (a point source on every interior cell, w_1 =
-    0, no sponge), u_2 - 2 u_1 = dt^2 kappa Lb u_1 with kappa Lb assembled
-    term by term as a matrix, on random kappa, rho with a 100x jump of rho."""
+    operator and sponge: from u_1 = g w_0 (a point source on every interior
+    cell, w_1 = 0), u_2 / g - 2 u_1 = dt^2 kappa Lb u_1, g = gz[z] gx[x], with
+    kappa Lb assembled term by term as a matrix, on random kappa, rho with a
+    100x jump of rho (and random sponge profiles)."""
     from helpers import vd_operator
     R, n, dt = order // 2, 16, 0.01
     rng = np.random.default_rng(order)
@@ -313,18 +314,21 @@ def test_vd_operator_matches_assembled_matrix(orc, order):
     cells = [(z, x) for z in range(R, n - R) for x in range(R, n - R)]
     src = np.array([[z, 0, x] for z, x in cells], dtype=np.int32)[None]
     amp = rng.standard_normal(len(cells))
+    gz, gx = (rng.uniform(0.9, 1.0, n), rng.uniform(0.9, 1.0, n)) if sponge else (np.ones(n), np.ones(n))
 
     def final(nt):
         wav = np.zeros((1, nt, len(cells)))
         wav[0, 0, :] = amp
-        geo = orc.VdGeometry(kappa, rho, wav, src, np.zeros((1, 0, 3), np.int32), dt, (1.0, 1.0), order=order)
+        geo = orc.VdGeometry(kappa, rho, wav, src, np.zeros((1, 0, 3), np.int32), dt, (1.0, 1.0), order=order,
+                             sponge=(gz, gx) if sponge else None)
         return orc.vd_forward(geo, want_final=True)[1][0].ravel()
 
     idx = [z * n + x for z, x in cells]
+    g = np.outer(gz, gx).ravel()[idx]
     u1, u2 = final(1), final(2)
-    assert np.array_equal(u1[idx], amp)
+    assert np.allclose(u1[idx], g * amp, rtol=1e-15, atol=0)
     rhs = dt * dt * (vd_operator(kappa, rho, orc.stag_coeffs(order)) @ u1[idx])
-    assert np.abs((u2 - 2 * u1)[idx] - rhs).max() < 1e-11 * np.abs(rhs).max()
+    assert np.abs(u2[idx] / g - 2 * u1[idx] - rhs).max() < 1e-11 * np.abs(rhs).max()
 
 
 @pytest.mark.parametrize("order", [2, 8])

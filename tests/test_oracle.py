@@ -116,17 +116,25 @@ def test_mixed_step_golden_close_to_fp32(orc):
     assert rel_l2(g[last][:, :M].astype(np.float32), p[last][:, :M]) < 2e-2
 
 
-def test_numpy_generic_matches_oracle_3d(orc):
+@pytest.mark.parametrize("shape,order", [((20, 21, 22), 8), ((20, 21, 22), 4), ((20, 21, 22), 2),
+                                         ((30, 37), 8), ((30, 37), 4), ((30, 37), 2)])
+def test_numpy_generic_matches_oracle(orc, shape, order):
+    """The oracle's constant-density step against the NumPy slice-form
+    restatement: 2D and 3D, orders 2/4/8, unequal spacings, per-axis sponge."""
     from oracle import numpy_ref
-    rng = np.random.default_rng(0)
-    u = [rng.standard_normal((20, 21, 22)) for _ in range(2)]
-    w = rng.uniform(0.05, 0.2, (20, 21, 22))
-    gz, gy, gx = (rng.uniform(0.8, 1, n) for n in (20, 21, 22))
-    G = gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
+    rng = np.random.default_rng(order + len(shape))
+    u = [rng.standard_normal(shape) for _ in range(2)]
+    w = rng.uniform(0.05, 0.2, shape)
+    prof = [rng.uniform(0.8, 1, n) for n in shape]
+    G = np.ones(shape)
+    for axis, pr in enumerate(prof):
+        G = G * pr.reshape([-1 if i == axis else 1 for i in range(len(shape))])
+    h = (1.0, 1.1, 0.9) if len(shape) == 3 else (1.0, 0.9)
     a = u[0].copy()
-    numpy_ref.fd_step(u[0], u[1], a, w, (1.0, 1.1, 0.9), order=8, g=G)
+    numpy_ref.fd_step(u[0], u[1], a, w, h, order=order, g=G)
     b = u[0].copy()
-    orc.step(8, (1.0, 1.1, 0.9), u[0], u[1], b, w=w, sponge=(gz, gy, gx))
+    sponge = tuple(prof) if len(shape) == 3 else (prof[0], None, prof[1])
+    orc.step(order, h if len(shape) == 3 else (h[0], 1.0, h[1]), u[0], u[1], b, w=w, sponge=sponge)
     assert rel_l2(a, b) < 1e-14
 
 

@@ -28,9 +28,12 @@ module's own. They are written here so callers can check parity:
   (nx, ny, nz), as projects/8_physics_drivers/waveND.py does with DIM = 3;
   AcousticWave is 2D.
 * Coordinates map to the nearest node, as cuwave's point sources and sensors
-  do. point_source divides the signal by the cell volume dx dy
-  (projects/9_structural_optimization/README.md:87) and scales it by dt^2
-  (the source term of u_tt = c^2 Lap u + f).
+  do. Source and Sensors hold node numbers as cuwave does (check.py:54): an
+  array (D, n), node 0 the ghost node at -dx; the library's grid index is the
+  node number plus the margin. Source.signal is the source term f of
+  u_tt = c^2 Lap u + f: point_source divides the signal by the cell volume
+  dx dy (projects/9_structural_optimization/README.md:87), and dt^2 f is
+  added per step.
 * sineburst(t, A, f, cycles) is a Hann-windowed tone burst
   A sin(2 pi f t) sin^2(pi f t / cycles) on 0 <= t <= cycles / f.
 * Array axes follow the reference (x first); they map onto the library's
@@ -164,8 +167,9 @@ class ScalarWave:
                     sponge=int(self.damping), src_scale=1.0)
 
     def node(self, coord) -> tuple:
-        """Nearest node (padded grid index) of a physical coordinate."""
-        return tuple(int(round(c / h)) + 1 + self.margin for c, h in zip(coord, self.dx))
+        """Number of the nearest node of a physical coordinate (node i sits at
+        x = -dx + i dx, node 0 the ghost node), as Source and Sensors hold it."""
+        return tuple(int(round(c / h)) + 1 for c, h in zip(coord, self.dx))
 
     @property
     def interior(self) -> tuple:
@@ -209,20 +213,29 @@ def line(a, b, n: int) -> np.ndarray:
     return a[None, :] + np.linspace(0.0, 1.0, n)[:, None] * (b - a)[None, :]
 
 
+def _host(a) -> np.ndarray:
+    return a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+
+
 @dataclass
 class Source:
-    nodes: np.ndarray   # (nsrc, D) padded-grid indices
-    signal: np.ndarray  # (N, nsrc)
+    """A source as cuwave holds one (check.py:54): `nodes` (D, nsrc), the node
+    numbers it drives along each axis (node 0 the ghost node at -dx), and
+    `signal` (N, nsrc), the source term f of u_tt = c^2 Lap u + f at those
+    nodes. The step's dt^2 is applied when the library is called."""
+    nodes: np.ndarray
+    signal: np.ndarray
 
 
 def point_source(sim: ScalarWave, coords, signal) -> Source:
+    """Sources at the nodes nearest `coords`, the signal divided by the cell
+    volume (projects/9_structural_optimization/README.md:87)."""
     coords = np.atleast_2d(np.asarray(coords, dtype=np.float64))
-    nodes = np.array([sim.node(c) for c in coords], dtype=np.int32)
+    nodes = np.array([sim.node(c) for c in coords], dtype=np.int32).reshape(-1, len(sim.Nx)).T
     sig = np.asarray(signal, dtype=np.float64).reshape(sim.N, -1)
-    if sig.shape[1] == 1 and len(nodes) > 1:
-        sig = np.repeat(sig, len(nodes), axis=1)
-    vol = float(np.prod(sim.dx))
-    return Source(nodes, (sig * sim.dt * sim.dt / vol).astype(np.float32))
+    if sig.shape[1] == 1 and nodes.shape[1] > 1:
+        sig = np.repeat(sig, nodes.shape[1], axis=1)
+    return Source(nodes, sig / float(np.prod(sim.dx)))
 
 
 class _SourceList(list):
@@ -243,7 +256,10 @@ class Sensors:
     nodes: np.ndarray = field(init=False)
 
     def __post_init__(self):
-        self.nodes = np.array([self.sim.node(c) for c in np.atleast_2d(self.coords)], dtype=np.int32)
+        """nodes (D, nsensors): node numbers, laid out as Source.nodes."""
+        nd = len(self.sim.Nx)
+        pts = np.atleast_2d(np.asarray(self.coords, dtype=np.float64))
+        self.nodes = np.array([self.sim.node(c) for c in pts], dtype=np.int32).reshape(-1, nd).T
 
     def traces(self, um):
         """The sensor traces (N, nsensors) of a simulate() record
@@ -251,14 +267,27 @@ class Sensors:
         return um
 
 
+def _grid_points(sim, nodes) -> np.ndarray:
+    """(D, n) node numbers -> (n, D) int32 indices on the library's grid."""
+    a = _host(nodes).astype(np.int64).reshape(len(sim.Nx), -1)
+    return (a.T + sim.margin).astype(np.int32)
+
+
+def _grid_signal(sim, source) -> np.ndarray:
+    """(N, nsrc) source samples added per step: dt^2 f, FP32."""
+    return (np.asarray(_host(source.signal), dtype=np.float64).reshape(sim.N, -1) * (sim.dt * sim.dt)).astype(np.float32)
+
+
 def _batch(sim, sources, sensors):
+    """The library's arrays for a list of shots: positions (nshot, nsrc, D),
+    samples (nshot, N, nsrc) and receivers (nshot, nrec, D)."""
     srcs = list(sources) if isinstance(sources, (list, tuple)) else [sources]
-    nsrc = max(len(s.nodes) for s in srcs)
-    if any(len(s.nodes) != nsrc for s in srcs):
+    pts = [_grid_points(sim, s.nodes) for s in srcs]
+    if any(len(q) != len(pts[0]) for q in pts):
         raise ValueError("every shot needs the same number of source points")
-    src = np.stack([s.nodes for s in srcs])
-    wav = np.stack([s.signal for s in srcs])  # (nshot, N, nsrc)
-    rec = np.repeat(sensors.nodes[None], len(srcs), axis=0)
+    src = np.stack(pts)
+    wav = np.stack([_grid_signal(sim, s) for s in srcs])
+    rec = np.repeat(_grid_points(sim, sensors.nodes)[None], len(srcs), axis=0)
     return src, wav, rec
 
 
@@ -287,9 +316,9 @@ def simulate(sim: ScalarWave, source: Source, indicator, sensors=None, record_ev
         s = Sensors(sim, np.zeros((0, nd)))
     elif isinstance(sensors, Sensors):
         s = sensors
-    else:  # a node array (padded-grid indices), as Sensors.nodes holds them
+    else:  # a node array (D, nsensors), as Sensors.nodes holds it
         s = Sensors(sim, np.zeros((0, nd)))
-        s.nodes = np.asarray(sensors, dtype=np.int32).reshape(-1, nd)
+        s.nodes = _host(sensors).astype(np.int32).reshape(nd, -1)
     acoustic = isinstance(sim, AcousticWave)
     if acoustic:  # the two-phase medium on the variable-density kernels
         kap, rho = sim.materials(indicator)
@@ -419,8 +448,8 @@ def _scaled_sources(sim: AcousticWave, sources, indicator):
     srcs = list(sources) if isinstance(sources, (list, tuple)) else [sources]
     out = []
     for s in srcs:
-        w = torch.as_tensor(np.asarray(g.detach().cpu())[s.nodes[:, 0], s.nodes[:, 1]], dtype=torch.float32)
-        out.append(Source(s.nodes, (s.signal * w.numpy()[None, :]).astype(np.float32)))
+        w = g.detach().cpu().numpy().astype(np.float64)[tuple(_grid_points(sim, s.nodes).T)]
+        out.append(Source(s.nodes, np.asarray(_host(s.signal), dtype=np.float64) * w[None, :]))
     return _SourceList(out)
 
 
@@ -447,9 +476,9 @@ def acoustic_misfit_gradient(sim: AcousticWave, sources, indicator, sensors: Sen
     # the source samples scale with gamma at their nodes: + sum_n dJ/dw_n * signal_n
     srcs = list(sources) if isinstance(sources, (list, tuple)) else [sources]
     for si, s in enumerate(srcs):
-        sig = torch.from_numpy(s.signal).to(kap.device).double()  # (N, nsrc)
+        sig = torch.from_numpy(_grid_signal(sim, s)).to(kap.device).double()  # (N, nsrc), dt^2 f
         contrib = (gw[si].double() * sig).sum(0)
-        for j, (a, b) in enumerate(s.nodes):
+        for j, (a, b) in enumerate(_grid_points(sim, s.nodes)):
             g_pad[a, b] += contrib[j]
     out = torch.zeros_like(gamma)
     out[tuple(slice(0, n) for n in sim.Nx)] = g_pad[sim.interior].float()

@@ -10,18 +10,19 @@ def test_geometry_and_helpers():
     from neuralmech_gb300 import cuwave_compat as cw
     sim = cw.ScalarWave((64, 80), (1 / 61, 1 / 77), 100, 1e-3, space_order=8)
     assert sim.margin == 3 and sim.grid_shape == (70, 86) and sim.Nx_padded == (72, 88)
-    # node i of the physical grid sits at x = -dx + i dx; the margin shifts it
-    assert sim.node((0.0, 0.0)) == (4, 4)
-    assert sim.node((1.0, 1.0)) == (61 + 4, 77 + 4)  # the last physical interior node
+    # node i sits at x = -dx + i dx (node 0 the ghost node); on the library's
+    # grid it is index i + margin
+    assert sim.node((0.0, 0.0)) == (1, 1)
+    assert sim.node((1.0, 1.0)) == (62, 78)  # the last node on [0, L]
     R = 4
-    assert sim.node((1.0, 1.0))[1] < sim.grid_shape[1] - R  # updated by the order-8 stencil
+    assert sim.node((1.0, 1.0))[1] + sim.margin < sim.grid_shape[1] - R  # updated by the order-8 stencil
     pts = cw.line((0.1, 1.0), (0.9, 1.0), 5)
     assert pts.shape == (5, 2) and np.allclose(pts[:, 1], 1.0) and np.isclose(pts[2, 0], 0.5)
     t = np.linspace(0, 0.5, 1001)
     s = cw.sineburst(t, 2.0, 10.0, 2)
     assert np.all(s[t > 0.2] == 0) and np.abs(s).max() <= 2.0 and np.abs(s).max() > 1.5
     src = cw.point_source(sim, (0.5, 1.0), np.ones(100))
-    assert np.allclose(src.signal, 1e-6 / (1 / 61 * 1 / 77))
+    assert src.nodes.shape == (2, 1) and np.allclose(src.signal, 1.0 / (1 / 61 * 1 / 77))
     # interior_slice: the nodes on [0, L], as the indicator and simulate() index them
     inner = cw.interior_slice(sim)
     assert inner == (slice(1, 63), slice(1, 79))
@@ -31,6 +32,32 @@ def test_geometry_and_helpers():
     for bad in (0, -3):  # refused before any device work
         with pytest.raises(ValueError):
             cw.simulate(sim, src, np.ones(sim.Nx), record_every=bad)
+
+
+def test_source_and_sensor_conventions():
+    """Source(indices (D, nsrc), signal (N, nsrc)) built by hand, as check.py:54
+    does, drives node n // 2 of each axis (the library's index n // 2 + margin)
+    with dt^2 signal per step; point_source at a node's coordinate gives the
+    same shot with the signal divided by the cell volume; Sensors and node
+    arrays are (D, n), in 2D and 3D."""
+    from neuralmech_gb300 import cuwave_compat as cw
+    for Nx in ((40, 52), (20, 22, 24)):
+        nd = len(Nx)
+        dx = tuple(1.0 / (n - 3) for n in Nx)
+        sim = cw.ScalarWave(Nx, dx, 30, 2e-3, space_order=8, device="cpu")
+        sig = np.sin(np.arange(30.0))[:, None]
+        hand = cw.Source(np.array([[n // 2] for n in Nx], dtype=np.int32), sig)
+        sensors = cw.Sensors(sim, [tuple(0.25 for _ in Nx), tuple(0.5 for _ in Nx)])
+        assert sensors.nodes.shape == (nd, 2)
+        src, wav, rec = cw._batch(sim, hand, sensors)
+        assert src.shape == (1, 1, nd) and tuple(src[0, 0]) == tuple(n // 2 + sim.margin for n in Nx)
+        assert wav.dtype == np.float32 and np.allclose(wav[0, :, 0], sig[:, 0] * 2e-3 ** 2, rtol=1e-6, atol=0)
+        assert tuple(rec[0, 1]) == tuple(k + sim.margin for k in sim.node((0.5,) * nd))
+        coord = tuple((n // 2 - 1) * h for n, h in zip(Nx, dx))
+        ps = cw.point_source(sim, coord, sig[:, 0])
+        s2, w2, _ = cw._batch(sim, ps, sensors)
+        assert np.array_equal(s2, src)
+        assert np.allclose(w2 * np.prod(dx), wav, rtol=1e-6, atol=0)
 
 
 def test_sponge_helpers():
@@ -264,9 +291,8 @@ def test_simulate_matches_measure(cuda):
     ref = cw.measure(sim, sources[3:4], gamma_true, sensors)[0]
     assert rel_l2(record.cpu().numpy(), ref.cpu().numpy()) < 1e-6
     # the last recorded sample is the final field at the sensor nodes
-    m = sim.margin
-    nodes = sensors.nodes - m
-    assert rel_l2(u[nodes[:, 0], nodes[:, 1]].cpu().numpy(), record[-1].cpu().numpy()) < 1e-6
+    nodes = sensors.nodes  # (2, nsensors) node numbers index simulate()'s field directly
+    assert rel_l2(u[nodes[0], nodes[1]].cpu().numpy(), record[-1].cpu().numpy()) < 1e-6
 
 
 @pytest.mark.gpu

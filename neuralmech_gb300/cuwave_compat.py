@@ -4,7 +4,8 @@ projects/18_fwi (plate.py, helper.py, 2D_fwi.py) and projects/16_neuralopt
 drive the pip package cuwave through a small surface:
   ScalarWave(Nx, dx, N, dt, threads, precision, space_order, wavespeed, density),
   line, shots, point_source, Sensors, sineburst, stable_dt, simulate, measure,
-  misfit, misfit_gradient, resample, Adam, grid_coords, interior_slice; and,
+  misfit, misfit_gradient, resample, Adam, grid_coords, interior_slice, circle,
+  box, nodes, threshold; and,
   for the absorbing layer of projects/0_conceptual_figures/4_analog_rnn.py:
   73,95-97, pad_for_sponge and sponge.
 This module offers the same names and call shapes over PyTorch tensors, with
@@ -109,6 +110,36 @@ def sponge(sim, field, width, beta: float, faces=None) -> "Sponge":
         w = [(lo if (a, 0) in on else 0, hi if (a, 1) in on else 0) for a, (lo, hi) in enumerate(w)]
     wall = math.sqrt((1.0 - beta) / (1.0 + beta))
     return Sponge(tuple(w), math.sqrt(-math.log(wall)))
+
+
+def circle(coords, center, radius: float) -> torch.Tensor:
+    """Mask of the nodes within `radius` of `center` (grid_coords arrays;
+    fwi_penalization.py:92, cylinder_snapshots.py:37)."""
+    d2 = sum((torch.as_tensor(x).double() - float(c)) ** 2 for x, c in zip(coords, center))
+    return d2 <= float(radius) ** 2
+
+
+def box(coords, center, size) -> torch.Tensor:
+    """Mask of the nodes with |x_d - center_d| <= size_d / 2 on every axis
+    (topopt_acoustic2D.py:144-147)."""
+    m = None
+    for x, c, w in zip(coords, center, size):
+        inside = (torch.as_tensor(x).double() - float(c)).abs() <= 0.5 * float(w)
+        m = inside if m is None else m & inside
+    return m
+
+
+def nodes(mask) -> np.ndarray:
+    """(D, n) numbers of the masked nodes, the layout of Source and Sensors
+    node arrays (topopt_acoustic2D.py:144 passes it as the sensors)."""
+    idx = torch.nonzero(torch.as_tensor(mask).bool().cpu(), as_tuple=False)
+    return idx.T.numpy().astype(np.int32)
+
+
+def threshold(field, level: float):
+    """1 where field > level, else 0, in the field's type (analog_rnn_train.py:179)."""
+    f = torch.as_tensor(field)
+    return (f > level).to(f.dtype)
 
 
 def interior_slice(sim) -> tuple:

@@ -1,4 +1,6 @@
 """The cuwave-shaped adapter (projects/18_fwi call sequence on this library)."""
+import math
+
 import numpy as np
 import pytest
 import torch
@@ -58,6 +60,27 @@ def test_source_and_sensor_conventions():
         s2, w2, _ = cw._batch(sim, ps, sensors)
         assert np.array_equal(s2, src)
         assert np.allclose(w2 * np.prod(dx), wav, rtol=1e-6, atol=0)
+
+
+def test_geometry_masks_and_nodes():
+    """circle, box, nodes and threshold on grid_coords: the masks select the
+    nodes inside the shape; nodes gives their (D, n) numbers, usable as
+    sensors (node i at x = -dx + i dx)."""
+    from neuralmech_gb300 import cuwave_compat as cw
+    sim = cw.ScalarWave((43, 53), (1 / 40, 1 / 50), 10, 1e-3, space_order=4, device="cpu")
+    x, y = cw.grid_coords(sim.Nx, sim.dx, device="cpu")
+    disc = cw.circle((x, y), (0.5, 0.5), 0.1)
+    assert disc.shape == sim.Nx and bool(disc[21, 26]) and not bool(disc[21, 40])
+    assert abs(int(disc.sum()) - math.pi * 0.1 ** 2 / (sim.dx[0] * sim.dx[1])) < 0.1 * int(disc.sum())
+    rect = cw.box((x, y), (0.5, 0.5), (0.21, 0.11))  # edges between nodes
+    assert int(rect.sum()) == 9 * 5  # x = 0.4 .. 0.6 (9 nodes), y = 0.46 .. 0.54 (5 nodes)
+    n = cw.nodes(rect)
+    assert n.shape == (2, 45) and n.dtype == np.int32
+    assert np.allclose(x[n[0], n[1]].numpy(), x[rect].numpy()) and (np.abs(x[n[0], n[1]].numpy() - 0.5) <= 0.105).all()
+    src, wav, rec = cw._batch(sim, cw.point_source(sim, (0.5, 0.5), np.ones(10)), type("S", (), {"nodes": n})())
+    assert rec.shape == (1, 45, 2) and (rec[0] == n.T + sim.margin).all()
+    t = cw.threshold(torch.tensor([0.2, 0.5, 0.7]), 0.5)
+    assert t.tolist() == [0.0, 0.0, 1.0] and t.dtype == torch.float32
 
 
 def test_sponge_helpers():

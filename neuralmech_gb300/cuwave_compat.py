@@ -5,7 +5,7 @@ drive the pip package cuwave through a small surface:
   ScalarWave(Nx, dx, N, dt, threads, precision, space_order, wavespeed, density),
   line, shots, point_source, Sensors, sineburst, stable_dt, simulate, measure,
   misfit, misfit_gradient, resample, Adam, grid_coords, interior_slice, circle,
-  box, nodes, threshold; and,
+  box, nodes, threshold, energy, response, response_gradient; and,
   for the absorbing layer of projects/0_conceptual_figures/4_analog_rnn.py:
   73,95-97, pad_for_sponge and sponge.
 This module offers the same names and call shapes over PyTorch tensors, with
@@ -386,6 +386,60 @@ def simulate(sim: ScalarWave, source: Source, indicator, sensors=None, record_ev
             frames.append(physical(run(g, wav_t[:, :n], none)[1]))
         out.append(torch.stack(frames))
     return out[0] if len(out) == 1 else tuple(out)
+
+
+def energy(sim):
+    """The objective of topopt_acoustic2D.py:171 as a callable on a record
+    (N, nsensors): dt times the sum of its squares, the time-integrated
+    squared field at the sensor nodes."""
+    dt = float(sim.dt)
+    return lambda um: dt * (um.double() ** 2).sum()
+
+
+def response(sim, source, indicator, sensors, objective):
+    """(objective(record), record) of one shot (topopt_acoustic2D.py:179,260);
+    `sensors` a Sensors or a node array."""
+    _, um = simulate(sim, source, indicator, sensors)
+    return float(objective(um)), um
+
+
+def response_gradient(sim, source, indicator, sensors, objective, adjoint=None):
+    """(objective, d objective / d indicator) of one shot
+    (topopt_acoustic2D.py:194-195). `objective` maps the record (N, nsensors)
+    to a scalar tensor; the gradient has the indicator's shape, nonzero in
+    [:nx, :ny] only. `adjoint` is taken for the call's shape: the library's
+    checkpointed adjoint runs.
+
+    ScalarWave: autograd through wave_forward (the library's adjoint behind
+    torch.autograd) and c = wavespeed sqrt(gamma). AcousticWave: the
+    variable-density misfit gradient with observed = record - s dJ/d(record),
+    whose residual is s dJ/d(record), so its gradient is s times the
+    objective's; s = max|record| / max|dJ/d(record)| keeps that residual at
+    the record's scale in FP32."""
+    sens = sensors
+    if not isinstance(sens, Sensors):
+        sens = Sensors(sim, np.zeros((0, len(sim.Nx))))
+        sens.nodes = _host(sensors).astype(np.int32).reshape(len(sim.Nx), -1)
+    gamma = torch.as_tensor(indicator, device=sim.device, dtype=torch.float32)
+    if isinstance(sim, AcousticWave):
+        record = acoustic_measure(sim, [source], gamma, sens)[0]
+        um = record.detach().double().requires_grad_(True)
+        J = objective(um)
+        (cot,) = torch.autograd.grad(J, um)
+        J = J.detach()
+        peak = float(cot.abs().max())
+        if peak == 0.0:
+            return float(J), torch.zeros_like(gamma)
+        scale = max(float(record.abs().max()), 1e-30) / peak
+        observed = (record.double() - scale * cot).float()
+        _, grad = acoustic_misfit_gradient(sim, [source], gamma, sens, [observed])
+        return float(J), grad / scale
+    src, wav, rec = _batch(sim, source, sens)
+    g = gamma.detach().clone().requires_grad_(True)
+    record = wave_forward(sim.velocity(g), torch.from_numpy(wav).to(g.device), src, rec, sim.grid())[0]
+    J = objective(record)
+    J.backward()
+    return float(J.detach()), g.grad
 
 
 def resample(record, dt_obs: float, dt: float, N: int):

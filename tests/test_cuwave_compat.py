@@ -83,6 +83,69 @@ def test_geometry_masks_and_nodes():
     assert t.tolist() == [0.0, 0.0, 1.0] and t.dtype == torch.float32
 
 
+def test_response_gradient_chain(monkeypatch):
+    """response_gradient's host logic with differentiable stand-ins for the
+    library calls. ScalarWave: the gradient through c = wavespeed sqrt(gamma)
+    and the indicator's margin extension matches central differences of the
+    objective. AcousticWave: with a linear record M gamma, the scaled misfit
+    residual returns M^T dJ/d(record)."""
+    from neuralmech_gb300 import cuwave_compat as cw
+    n, N = 20, 12
+    dx = (1 / (n - 3),) * 2
+    sim = cw.ScalarWave((n, n), dx, N, 1e-3, space_order=4, wavespeed=1.5, device="cpu")
+    src = cw.point_source(sim, (0.5, 0.5), np.linspace(0.0, 1.0, N))
+    sensors = cw.Sensors(sim, cw.line((0.2, 0.3), (0.8, 0.3), 3))
+    rng = np.random.default_rng(0)
+
+    def fake_forward(vel, wav, src_, rec_, grid):  # smooth, nonlinear in vel
+        assert tuple(vel.shape) == grid.shape
+        r = torch.as_tensor(rec_)[0].long()
+        v = vel[r[:, 0], r[:, 1]]
+        t = torch.arange(grid.nt, dtype=vel.dtype)[:, None]
+        return (torch.sin(v[None, :] * (1 + t)) * vel.mean() + wav[0, :, :1] * v[None, :] ** 2)[None]
+
+    monkeypatch.setattr(cw, "wave_forward", fake_forward)
+    gamma = torch.from_numpy(rng.uniform(0.5, 1.0, sim.Nx_padded).astype(np.float32))
+    obj = cw.energy(sim)
+    J, grad = cw.response_gradient(sim, src, gamma, sensors, obj)
+    assert grad.shape == gamma.shape and float(grad[n:, :].abs().max()) == 0.0
+    d = torch.zeros_like(gamma)
+    d[:n, :n] = torch.from_numpy(rng.standard_normal((n, n)).astype(np.float32))
+    eps = 1e-2
+
+    def Jof(gm):
+        s_, w_, r_ = cw._batch(sim, src, sensors)
+        return float(obj(fake_forward(sim.velocity(gm).double(), torch.from_numpy(w_).double(), s_, r_, sim.grid())[0]))
+
+    fd = (Jof(gamma + eps * d) - Jof(gamma - eps * d)) / (2 * eps)
+    an = float((grad.double() * d.double()).sum())
+    assert abs(fd - an) < 1e-2 * abs(fd), (fd, an)
+
+    ac = cw.AcousticWave((n, n), dx, N, 1e-3, space_order=4, device="cpu")
+    M = torch.from_numpy(rng.standard_normal((N * 3, n * n)))
+
+    def rec_of(gm):
+        return (M @ torch.as_tensor(gm)[:n, :n].double().reshape(-1)).reshape(N, 3).float()
+
+    def fake_measure(sim_, sources, gm, sens):
+        return [rec_of(gm)]
+
+    def fake_misfit_gradient(sim_, sources, gm, sens, observed):
+        res = (rec_of(gm) - observed[0]).double().reshape(-1)
+        g = torch.zeros(tuple(torch.as_tensor(gm).shape), dtype=torch.float64)
+        g[:n, :n] = (M.T @ res).reshape(n, n)
+        return 0.5 * float((res ** 2).sum()), g.float()
+
+    monkeypatch.setattr(cw, "acoustic_measure", fake_measure)
+    monkeypatch.setattr(cw, "acoustic_misfit_gradient", fake_misfit_gradient)
+    gm = torch.from_numpy(rng.uniform(0.0, 1.0, (n, n)).astype(np.float32))
+    Ja, ga = cw.response_gradient(ac, src, gm, sensors.nodes, obj)
+    um = rec_of(gm).double()
+    want = (M.T @ (2 * ac.dt * um).reshape(-1)).reshape(n, n)
+    assert abs(Ja - float(ac.dt * (um ** 2).sum())) < 1e-9 * abs(Ja)
+    assert rel_l2(ga.double().numpy(), want.numpy()) < 1e-5
+
+
 def test_sponge_helpers():
     """pad_for_sponge / sponge / grid_coords (4_analog_rnn.py:73,95-97;
     plate.py:56): widths from the thickness, the region inside, a wall factor

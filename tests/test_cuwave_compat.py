@@ -1,4 +1,10 @@
-"""The cuwave-shaped adapter (projects/18_fwi call sequence on this library)."""
+"""The cuwave-shaped adapter: the call sequences of projects/18_fwi,
+8_physics_drivers (waveND, topopt_acoustic2D) and the analog-RNN drivers on
+this library. CPU: node numbering and layout, sources, sensors, sponge and
+geometry helpers, and response_gradient's chain rule with stand-ins for the
+library calls. GPU: the FWI flow, indicator gradients against FP64 finite
+differences, simulate's call forms against measure and the FP64 oracle (2D,
+3D, two-phase), and the sponge's absorption."""
 import math
 
 import numpy as np

@@ -297,6 +297,11 @@ class Sensors:
         (4_analog_rnn.py:128): the record already holds them."""
         return um
 
+    def objective(self, objective):
+        """`objective` applied to the sensor traces of a record, for
+        response_gradient (analog_rnn_train.py:143)."""
+        return lambda um: objective(self.traces(um))
+
 
 def _grid_points(sim, nodes) -> np.ndarray:
     """(D, n) node numbers -> (n, D) int32 indices on the library's grid."""
@@ -389,26 +394,45 @@ def simulate(sim: ScalarWave, source: Source, indicator, sensors=None, record_ev
 
 
 def energy(sim):
-    """The objective of topopt_acoustic2D.py:171 as a callable on a record
-    (N, nsensors): dt times the sum of its squares, the time-integrated
-    squared field at the sensor nodes."""
+    """The objective of topopt_acoustic2D.py:171: dt times the sum of the
+    record's squares (the time-integrated squared field at the sensor nodes),
+    returned with its derivative, (cost, dJ/d(record)), as the reference's
+    objectives do (analog_rnn_fixture.py:106-121)."""
     dt = float(sim.dt)
-    return lambda um: dt * (um.double() ** 2).sum()
+    def objective(um):
+        u = torch.as_tensor(um).detach().double()
+        return dt * float((u ** 2).sum()), 2.0 * dt * u
+
+    return objective
+
+
+def _cost_and_cotangent(objective, um):
+    """(cost, dJ/d(record)) of an objective that returns that pair, or of one
+    that returns a differentiable scalar tensor (its derivative by autograd)."""
+    x = um.detach().double().requires_grad_(True)
+    out = objective(x)
+    if isinstance(out, tuple):
+        cost, cot = out
+        return float(cost), torch.as_tensor(cot, dtype=torch.float64, device=um.device).detach()
+    (cot,) = torch.autograd.grad(out, x)
+    return float(out.detach()), cot
 
 
 def response(sim, source, indicator, sensors, objective):
-    """(objective(record), record) of one shot (topopt_acoustic2D.py:179,260);
-    `sensors` a Sensors or a node array."""
+    """(cost, record) of one shot (topopt_acoustic2D.py:179,260); `sensors`
+    a Sensors or a node array, `objective` as for response_gradient."""
     _, um = simulate(sim, source, indicator, sensors)
-    return float(objective(um)), um
+    out = objective(um)
+    return float(out[0] if isinstance(out, tuple) else out), um
 
 
 def response_gradient(sim, source, indicator, sensors, objective, adjoint=None):
-    """(objective, d objective / d indicator) of one shot
-    (topopt_acoustic2D.py:194-195). `objective` maps the record (N, nsensors)
-    to a scalar tensor; the gradient has the indicator's shape, nonzero in
-    [:nx, :ny] only. `adjoint` is taken for the call's shape: the library's
-    checkpointed adjoint runs.
+    """(cost, d cost / d indicator) of one shot (topopt_acoustic2D.py:194-195).
+    `objective` maps the record (N, nsensors) to (cost, dJ/d(record)), as the
+    reference's objectives do, or to a differentiable scalar tensor. The
+    gradient has the indicator's shape, nonzero in [:nx, :ny] only.
+    `adjoint` is taken for the call's shape: the library's checkpointed
+    adjoint runs.
 
     ScalarWave: autograd through wave_forward (the library's adjoint behind
     torch.autograd) and c = wavespeed sqrt(gamma). AcousticWave: the
@@ -423,23 +447,20 @@ def response_gradient(sim, source, indicator, sensors, objective, adjoint=None):
     gamma = torch.as_tensor(indicator, device=sim.device, dtype=torch.float32)
     if isinstance(sim, AcousticWave):
         record = acoustic_measure(sim, [source], gamma, sens)[0]
-        um = record.detach().double().requires_grad_(True)
-        J = objective(um)
-        (cot,) = torch.autograd.grad(J, um)
-        J = J.detach()
+        J, cot = _cost_and_cotangent(objective, record)
         peak = float(cot.abs().max())
         if peak == 0.0:
-            return float(J), torch.zeros_like(gamma)
+            return J, torch.zeros_like(gamma)
         scale = max(float(record.abs().max()), 1e-30) / peak
         observed = (record.double() - scale * cot).float()
         _, grad = acoustic_misfit_gradient(sim, [source], gamma, sens, [observed])
-        return float(J), grad / scale
+        return J, grad / scale
     src, wav, rec = _batch(sim, source, sens)
     g = gamma.detach().clone().requires_grad_(True)
     record = wave_forward(sim.velocity(g), torch.from_numpy(wav).to(g.device), src, rec, sim.grid())[0]
-    J = objective(record)
-    J.backward()
-    return float(J.detach()), g.grad
+    J, cot = _cost_and_cotangent(objective, record)
+    record.backward(cot.to(record.dtype))
+    return J, g.grad
 
 
 def resample(record, dt_obs: float, dt: float, N: int):

@@ -113,15 +113,18 @@ def test_response_gradient_chain(monkeypatch):
     monkeypatch.setattr(cw, "wave_forward", fake_forward)
     gamma = torch.from_numpy(rng.uniform(0.5, 1.0, sim.Nx_padded).astype(np.float32))
     obj = cw.energy(sim)
-    J, grad = cw.response_gradient(sim, src, gamma, sensors, obj)
+    J, grad = cw.response_gradient(sim, src, gamma, sensors, sensors.objective(obj))
     assert grad.shape == gamma.shape and float(grad[n:, :].abs().max()) == 0.0
+    # the same objective as a differentiable scalar (autograd for dJ/d(record))
+    J2, grad2 = cw.response_gradient(sim, src, gamma, sensors.nodes, lambda um: sim.dt * (um ** 2).sum())
+    assert abs(J2 - J) < 1e-12 * abs(J) and torch.allclose(grad2, grad, rtol=1e-6, atol=0)
     d = torch.zeros_like(gamma)
     d[:n, :n] = torch.from_numpy(rng.standard_normal((n, n)).astype(np.float32))
     eps = 1e-2
 
     def Jof(gm):
         s_, w_, r_ = cw._batch(sim, src, sensors)
-        return float(obj(fake_forward(sim.velocity(gm).double(), torch.from_numpy(w_).double(), s_, r_, sim.grid())[0]))
+        return obj(fake_forward(sim.velocity(gm).double(), torch.from_numpy(w_).double(), s_, r_, sim.grid())[0])[0]
 
     fd = (Jof(gamma + eps * d) - Jof(gamma - eps * d)) / (2 * eps)
     an = float((grad.double() * d.double()).sum())

@@ -241,6 +241,48 @@ def cpu_gradient_sample(w, steps: int, nshot: int = 1):
     return 2.0 * nshot * interior * steps, dt, desc
 
 
+def numpy_fd_step_legs(steps: int = 1000):
+    """The reference's NumPy CPU path, fd_step (projects/18_simple_wave_fd/
+    2D_wave_cupy.py:54-62), timed on the fwd256 workload (256^2, dx 10 m,
+    layered + anomaly model, 1000 steps) on one core (NumPy elementwise work is
+    single-threaded): as written (order 2, constant wave speed = the model's
+    maximum, Dirichlet ring) and in its slice form at order 8 with the velocity
+    field and the 20-cell sponge. Forward cell-updates per second."""
+    from oracle import numpy_ref
+    from neuralmech_gb300 import sponge_profiles
+    from neuralmech_gb300.synth import workload as wl
+    w = wl("fwd256")
+    g = w.grid
+    n = g.shape[0]
+    steps = min(steps, g.nt)
+    src = tuple(int(c) for c in w.src[0, 0])
+    out = {}
+    vmax = float(w.vel.max())
+    gz, _, gx = sponge_profiles(g)
+    gfield = (gz[:, None] * gx[None, :]).astype(np.float32)
+    wfield = (w.vel.astype(np.float32) * np.float32(g.dt)) ** 2
+    for name, R in (("order2_as_written", 1), ("order8_sponge_slices", 4)):
+        u0 = np.zeros((n, n), np.float32)
+        u1 = np.zeros((n, n), np.float32)
+        t0 = time.perf_counter()
+        for k in range(steps):
+            if R == 1:
+                numpy_ref.fd_step_order2(u0, u1, u0, np.float32(g.dt), np.float32(g.spacing[1]),
+                                         np.float32(g.spacing[0]), np.float32(vmax))
+            else:
+                numpy_ref.fd_step(u0, u1, u0, wfield, g.spacing, order=8, g=gfield)
+            u0[src] += w.wavelet[k]
+            u0, u1 = u1, u0
+        dt = time.perf_counter() - t0
+        inner = (n - 2 * R) ** 2
+        out[name] = {"value": inner * steps / dt / 1e9, "unit": "Gcell-updates/s (forward)", "cores": 1,
+                     "kind": "port",
+                     "sample": f"fwd256: {n}^2, {steps} steps, one shot, NumPy FP32 on one core"
+                               + (" (fd_step as written, cp -> np: order 2, wave speed = model max)" if R == 1
+                                  else " (the same slice form at order 8, velocity field, 20-cell sponge)")}
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -262,7 +304,7 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": config_of(w, args),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": desc + " per step"},
+                         "sample": desc + " per step", "numpy_fd_step": numpy_fd_step_legs()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -704,7 +746,7 @@ def main():
             steps = args.cpu_sample_steps if args.scale >= 1 else max(10, int(args.cpu_sample_steps * args.scale))
             u, tcpu, desc = cpu_gradient_sample(w, steps)
             line["cpu_baseline"] = {"value": u / tcpu / 1e9, "unit": UNIT, "cores": os.cpu_count(),
-                                    "kind": "port", "sample": desc}
+                                    "kind": "port", "sample": desc, "numpy_fd_step": numpy_fd_step_legs()}
 
     if rank == 0:
         print(json.dumps(line), flush=True)

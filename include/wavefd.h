@@ -65,6 +65,25 @@ extern "C" {
 #define WFD_LAP_BF16 1 /* L u_k in BF16 */
 #define WFD_LAP_FP32 2 /* L u_k in FP32 */
 
+/* How the forward evaluates the update (wfd_problem.update_form). Both forms are
+ * the same recursion; they differ in FP32 rounding and memory traffic. */
+#define WFD_UPDATE_AUTO 0     /* WFD_UPDATE_SUMMED for a forward that saves the state of a
+                                 gradient where that form is available (2D, one step per
+                                 launch, FP32 fields, lap_store auto, checkpoint adjoint, not
+                                 variable density), WFD_UPDATE_LEAPFROG otherwise */
+#define WFD_UPDATE_LEAPFROG 1 /* u_{n+1} over u_{n-1}: 16 bytes per update */
+#define WFD_UPDATE_SUMMED 2   /* the summed (increment) form: the state is (u_n, d_n =
+                                 u_n - u_{n-1}), d_{n+1} = g^2 d_n - (1 - g)^2 u_n + g m L u_n,
+                                 u_{n+1} = u_n + d_{n+1} (Henrici's summed form of the
+                                 two-step recursion). The increment keeps its own FP32
+                                 rounding, which cuts the accumulated rounding error of
+                                 the traces about 4x and of a gradient from residuals
+                                 far smaller than the traces about 9x; 20 bytes per update
+                                 (d is read and written, u_{n+1} written). Checkpoints then
+                                 hold (d_n, u_n). Forward only: the recompute and the
+                                 adjoint stay leapfrog. Only where WFD_UPDATE_AUTO would
+                                 choose it; elsewhere WFD_ERR_INVALID */
+
 typedef struct wfd_problem {
     int32_t ndim;          /* 2 or 3 */
     int32_t order;         /* space order: 2, 4 or 8 */
@@ -97,6 +116,7 @@ typedef struct wfd_problem {
     float dz, dy, dx;      /* grid spacing (dy ignored in 2D) */
     float src_scale;       /* factor on every injected wavelet sample */
     float vmax;            /* max velocity for the CFL check; <= 0 skips the check */
+    int32_t update_form;   /* WFD_UPDATE_AUTO, _LEAPFROG or _SUMMED */
 } wfd_problem;
 
 /* Human-readable text of a status code. */

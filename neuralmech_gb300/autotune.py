@@ -7,6 +7,11 @@ forward (`steps` time steps) for every candidate:
   * two steps per launch (step_block 2, 120 x 32 tiles) x shots_per_cta
     (automatic, 1, 2, 4, ...).
 
+For the forward of a gradient (``for_gradient``) whose grid asks for the
+summed update form ("auto" or "summed"), only one-step candidates compete,
+timed in that form: the two-step kernel has the leapfrog form only, whose
+accumulated rounding a gradient from small residuals cannot afford.
+
 It keeps the fastest, and caches the choice in a JSON file (default
 ``~/.cache/neuralmech_gb300/autotune.json``, or ``$WAVEFD_AUTOTUNE_CACHE``).
 The candidate timings use CUDA events on the current stream after one warm-up
@@ -44,17 +49,25 @@ def _store(path, data):
     os.replace(tmp, path)
 
 
-def problem_key(arch: str, shape, order: int, nshot: int) -> str:
-    return f"{arch}|{'x'.join(map(str, shape))}|o{order}|s{nshot}"
+def problem_key(arch: str, shape, order: int, nshot: int, summed: bool = False) -> str:
+    return f"{arch}|{'x'.join(map(str, shape))}|o{order}|s{nshot}" + ("|summed" if summed else "")
 
 
-def candidates(nshot: int):
+def candidates(nshot: int, summed: bool = False):
     spcs = [s for s in (1, 2, 4, 8, 16, 32) if s <= max(1, nshot)]
     if nshot <= 32 and nshot not in spcs:
         spcs.append(nshot)
     one = [{"tile_rows": tr, "shots_per_cta": s, "step_block": 1} for tr in (32, 16) for s in spcs]
     two = [{"tile_rows": 0, "shots_per_cta": s, "step_block": 2} for s in [0] + spcs]
-    return one + two
+    return one if summed else one + two
+
+
+def summed_for(grid, for_gradient: bool) -> bool:
+    """Whether the forward that the tuned configuration serves runs in the
+    summed form (2D FP32 fields, lap_store auto, checkpoint adjoint)."""
+    avail = grid.ndim == 2 and grid.field_format == "fp32" and grid.lap_store == "auto" and \
+        grid.adjoint == "checkpoint"
+    return avail and (grid.update == "summed" or (grid.update == "auto" and for_gradient))
 
 
 def select(timings: dict) -> dict:
@@ -64,7 +77,7 @@ def select(timings: dict) -> dict:
 
 
 def tune(grid, nshot: int, vel=None, steps: int = 16, device=None, path: str | None = None,
-         timer=None, refresh: bool = False) -> dict:
+         timer=None, refresh: bool = False, for_gradient: bool = False) -> dict:
     """Best {tile_rows, shots_per_cta, step_block} for `grid` with `nshot` shots (2D).
 
     `timer(config) -> seconds` replaces the GPU timing (used by tests)."""
@@ -73,14 +86,16 @@ def tune(grid, nshot: int, vel=None, steps: int = 16, device=None, path: str | N
     import torch
     path = path or cache_path()
     arch = "cpu-timer" if timer else torch.cuda.get_device_name(device)
-    key = problem_key(arch, grid.shape, grid.order, nshot)
+    summed = summed_for(grid, for_gradient)
+    key = problem_key(arch, grid.shape, grid.order, nshot, summed)
     with _lock:
         cache = _load(path)
         if key in cache and not refresh:
             return cache[key]["best"]
     if timer is None:
-        timer = _gpu_timer(grid, nshot, vel, steps, device)
-    timings = {json.dumps(c, sort_keys=True): float(timer(c)) for c in candidates(nshot)}
+        timer = _gpu_timer(dataclasses.replace(grid, update="summed" if summed else "leapfrog"), nshot, vel,
+                           steps, device)
+    timings = {json.dumps(c, sort_keys=True): float(timer(c)) for c in candidates(nshot, summed)}
     best = select(timings)
     with _lock:
         cache = _load(path)

@@ -6,7 +6,9 @@ This is the fwi workload family of many surveys at once (e.g. 8 models
 512^2..1536^2, 1000..3000 steps, 128 shots in total).
 
 ``BatchFWI`` works in four steps:
-  * it chooses each model's kernel configuration with the autotuner;
+  * it chooses each model's kernel configuration with the autotuner (for
+    the forward of a gradient: the summed update form where the grid asks
+    for it);
   * it allocates every workspace and output once;
   * it captures one CUDA graph in which each model's checkpointed
     forward + adjoint (``wfd_misfit_gradient``) runs on its own stream branch,
@@ -82,7 +84,7 @@ class BatchFWI:
             obs = m["observed"].to(torch.float32).contiguous()
             nshot = obs.shape[0]
             if autotune:
-                grid = _autotune.tuned(grid, nshot, vel=m["vel"], **(tune_kw or {}))
+                grid = _autotune.tuned(grid, nshot, vel=m["vel"], for_gradient=True, **(tune_kw or {}))
             if share > 0:
                 grid = dataclasses.replace(grid, store_levels=levels_for_budget(grid, nshot, share))
             call = _prepare(m["vel"], torch.as_tensor(m["wavelet"], device=self.device), m["src"], m["rec"],

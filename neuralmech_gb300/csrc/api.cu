@@ -243,6 +243,13 @@ int check_problem(const wfd_problem* p) {
     if (p->adjoint_mode == WFD_ADJOINT_RECONSTRUCT &&
         (p->ndim != 2 || p->step_block == 2 || p->lap_store != WFD_LAP_AUTO || p->field_format != WFD_FIELD_FP32))
         return fail(WFD_ERR_INVALID, "the reconstruction adjoint: 2D, one step per launch, lap_store auto, FP32");
+    if (p->update_form < WFD_UPDATE_AUTO || p->update_form > WFD_UPDATE_SUMMED)
+        return fail(WFD_ERR_INVALID, "unknown update_form %d", p->update_form);
+    if (p->update_form == WFD_UPDATE_SUMMED &&
+        (p->ndim != 2 || p->step_block == 2 || p->field_format != WFD_FIELD_FP32 ||
+         p->lap_store != WFD_LAP_AUTO || p->adjoint_mode != WFD_ADJOINT_CHECKPOINT))
+        return fail(WFD_ERR_INVALID, "the summed update form: 2D, one step per launch, FP32 fields, "
+                                     "lap_store auto, checkpoint adjoint");
     if (p->recon_band < 0 || 2 * p->recon_band > std::min(p->nz, p->nx))
         return fail(WFD_ERR_INVALID, "recon_band must lie in [0, min(nz, nx) / 2]");
     if (p->tile_rows != 0 && p->tile_rows != 16 && p->tile_rows != 32)
@@ -374,11 +381,21 @@ struct Layout {
     size_t S[2], scale_bytes;  // reduced-precision fields: the int16 block scales
     size_t b, Gbx, Gbz;        // variable density: b = 1/rho, half-point gradient sums
     size_t frames, frame_bytes;  // reconstruction adjoint: the damped frame of u_1 .. u_nt
+    size_t D;                  // summed form: the increment field d_n (0: leapfrog)
     int nlap;  // slots of the lap region: K stored L u_k, or levels u_k (u store): from
                // u_{k0_store - 1} to u_nt, and at least K + 2 for a recomputed segment
 };
 
 size_t up256(size_t v) { return (v + 255) / 256 * 256; }
+
+// Whether the forward runs in the summed form (state u_n, d_n): forced by
+// WFD_UPDATE_SUMMED, or chosen by WFD_UPDATE_AUTO for a forward that saves the
+// state of a gradient, where the 2D one-step u-store path runs.
+bool summed_forward(const wfd_problem* p, const Geom& g, bool save) {
+    const bool avail = g.ndim == 2 && !g.vd && g.sb == 1 && p->field_format == WFD_FIELD_FP32 && g.ustore &&
+                       !g.recon;
+    return avail && (p->update_form == WFD_UPDATE_SUMMED || (p->update_form == WFD_UPDATE_AUTO && save));
+}
 
 Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     Layout L{};
@@ -393,6 +410,7 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     L.m = take((size_t)g.cells * 4);
     if (g.vd) L.b = take((size_t)g.cells * 4);
     for (int b = 0; b < L.nbuf; ++b) L.P[b] = take(L.field_bytes);
+    if (summed_forward(p, g, grad)) L.D = take(L.field_bytes);  // the increment d_n
     if (p->field_format == WFD_FIELD_I16) {
         L.scale_bytes = (size_t)p->nshot * g.nz * scale_blocks(g.ld) * 4;
         for (int b = 0; b < 2; ++b) L.S[b] = take(L.scale_bytes);
@@ -442,6 +460,7 @@ struct Work {
     float *m, *P[4], *Q[4], *G, *res;
     float* S[2];  // int16 block scales of P[0], P[1] (reduced-precision fields)
     float *b, *Gbx, *Gbz;  // variable density (workspace)
+    float* D;              // summed form: the increment d_n, [nshot][cells] (null: leapfrog)
     const float* rho;      // variable density: the caller's rho, for setup and the gradient
     float* grad_rho;       // variable density: dJ/drho output
     unsigned char* frames; // reconstruction adjoint: frame n at frames + n frame_bytes
@@ -466,6 +485,7 @@ Work carve(void* ws, const Layout& L, bool grad) {
         w.Gbz = reinterpret_cast<float*>(b + L.Gbz);
     }
     for (int k = 0; k < L.nbuf; ++k) w.P[k] = reinterpret_cast<float*>(b + L.P[k]);
+    if (L.D) w.D = reinterpret_cast<float*>(b + L.D);
     if (L.S[0])
         for (int k = 0; k < 2; ++k) w.S[k] = reinterpret_cast<float*>(b + L.S[k]);
     w.counts = reinterpret_cast<int*>(b + L.counts);
@@ -730,18 +750,26 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
         if (us) return fail(WFD_ERR_INVALID, "internal: final level requested from a u-store forward");
         *final_buf = loc(p->nt);
     }
+    // summed form: the state is (u_n, d_n); u_{n+1} still goes over u_{n-1}
+    // (or to a slot), d_{n+1} over d_n
+    const bool summed = summed_forward(p, g, save);
+    if (summed && !w.D) return fail(WFD_ERR_INVALID, "internal: summed forward without its increment field");
     WFD_CUDA(cudaMemsetAsync(buf[loc(-1)], 0, L.field_bytes, s));
     WFD_CUDA(cudaMemsetAsync(buf[loc(0)], 0, L.field_bytes, s));
+    if (summed) WFD_CUDA(cudaMemsetAsync(w.D, 0, L.field_bytes, s));
     std::vector<CUtensorMap> mc(buf.size()), mo(buf.size());
     int rc;
     for (size_t b = 0; b < buf.size(); ++b)
         if ((rc = g.sb == 2 ? st.map_k2(buf[b], &mc[b], &mo[b]) : st.map_pair(buf[b], buf[b], &mc[b], &mo[b])))
             return rc;
+    CUtensorMap mdc{}, mdo{};  // d_n as the staged "old" tile
+    if (summed && (rc = st.map_pair(w.D, w.D, &mdc, &mdo))) return rc;
     const long long n_all = (long long)p->nshot * g.cells;
-    auto checkpoint = [&](int n) -> int {  // (u_{n-1}, u_n) at the start of segment n / K
+    // (u_{n-1}, u_n) at the start of segment n / K; (d_n, u_n) in the summed form
+    auto checkpoint = [&](int n) -> int {
         if (!save || rc_mode || n % g.K != 0 || (us && n >= g.k0_store)) return WFD_OK;  // (kept segments need none)
         unsigned char* slot = w.ckpt + (size_t)(n / g.K) * 2 * L.ckpt_field_bytes;
-        WFD_CUDA(launch_pack(buf[loc(n - 1)], slot, n_all, p->ckpt_format, s));
+        WFD_CUDA(launch_pack(summed ? w.D : buf[loc(n - 1)], slot, n_all, p->ckpt_format, s));
         WFD_CUDA(launch_pack(buf[loc(n)], slot + L.ckpt_field_bytes, n_all, p->ckpt_format, s));
         return WFD_OK;
     };
@@ -799,7 +827,12 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
             a.lap = w.lap + (size_t)(n - g.k0_last) * L.lap_field_bytes;
             a.lap_bf16 = g.lap_bf16;
         }
-        if ((rc = st.launch(lap ? MODE_SAVE_LAP : MODE_PLAIN, mc[bc], mo[bo], mc[bc], a))) return rc;
+        if (summed) {
+            a.d_new = w.D;
+            if ((rc = st.launch(MODE_SUMMED, mc[bc], mdo, mc[bc], a))) return rc;
+        } else if ((rc = st.launch(lap ? MODE_SAVE_LAP : MODE_PLAIN, mc[bc], mo[bo], mc[bc], a))) {
+            return rc;
+        }
         if (rc_mode)  // the damped frame of u_{n+1} (sources included: after the launch)
             WFD_CUDA(launch_band(buf[bn], reinterpret_cast<float*>(w.frames + (size_t)(n + 1) * L.frame_bytes),
                                  g.cells, p->nshot, g.nz, g.ld, g.band_w, g.band_cl, g.band_cr, true, s));
@@ -889,6 +922,7 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
     const Geom ga = adjoint_geom(p, g);
     Stepper sa = st;
     sa.g = ga;
+    const bool summed = summed_forward(p, g, true);  // the checkpoints hold (d_k0, u_k0)
     WFD_CUDA(cudaMemsetAsync(w.Q[0], 0, L.field_bytes, s));
     WFD_CUDA(cudaMemsetAsync(w.Q[1], 0, L.field_bytes, s));
     if (zero_G) {
@@ -947,8 +981,11 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
         if (j < g.jstore) {
             PhaseScope scope(PH_RECOMPUTE, s, g.sb == 2 ? (k1 - k0) / 2 : k1 - k0 - 1);
             const unsigned char* ck = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
-            WFD_CUDA(launch_unpack(ck, w.slot(L, 0), n_all, p->ckpt_format, s));
             WFD_CUDA(launch_unpack(ck + L.ckpt_field_bytes, w.slot(L, 1), n_all, p->ckpt_format, s));
+            if (summed)  // (d_k0, u_k0): u_{k0-1} = u_k0 - d_k0 for the leapfrog recompute
+                WFD_CUDA(launch_unpack_diff(ck, w.slot(L, 1), w.slot(L, 0), n_all, p->ckpt_format, s));
+            else
+                WFD_CUDA(launch_unpack(ck, w.slot(L, 0), n_all, p->ckpt_format, s));
             for (int k = k0; k + 1 < k1;) {  // u_{k+1} (and u_{k+2}) up to u_{k1-1}
                 const int i = k - k0 + 1;     // slot of u_k
                 const bool two = g.sb == 2 && k + 2 < k1;
@@ -1194,7 +1231,7 @@ const char* wfd_strerror(int status) {
 
 const char* wfd_last_error(void) { return g_last_error.c_str(); }
 
-int wfd_version(void) { return (2 << 16) | 1; }  // minor 1: temporal, exact and overlap entries
+int wfd_version(void) { return (3 << 16) | 0; }  // major 3: wfd_problem.update_form
 
 int wfd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes) {
     int rc = check_problem(p);
@@ -1374,6 +1411,8 @@ int vd_checks(const wfd_problem* p, const float* kappa, const float* rho, const 
         p->field_format != WFD_FIELD_FP32 || p->group_shots != 0)
         return fail(WFD_ERR_INVALID,
                     "variable density: 2D, one step per launch, lap_store auto, FP32 fields, no shot groups");
+    if (p->update_form == WFD_UPDATE_SUMMED)
+        return fail(WFD_ERR_INVALID, "variable density: the leapfrog update only");
     if (p->vmax > 0) {  // the staggered operator's bound: vmax dt sqrt((2 sum|c_k|)^2 sum 1/h^2) <= 2
         double c[5] = {0, 0, 0, 0, 0};
         stag_weights(p->order / 2, c);

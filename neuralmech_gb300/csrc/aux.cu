@@ -131,11 +131,20 @@ __global__ void pack_kernel(const float4* __restrict__ src, void* dst, long long
     }
 }
 
-__global__ void unpack_kernel(const void* src, float4* __restrict__ dst, long long n4, int fmt) {
+// from[i] - v instead of v where `from` is given (from may not alias dst)
+__device__ __forceinline__ float4 minus_from(const float4* __restrict__ from, long long i, float4 v) {
+    if (!from) return v;
+    const float4 f = from[i];
+    return make_float4(f.x - v.x, f.y - v.y, f.z - v.z, f.w - v.w);
+}
+
+__global__ void unpack_kernel(const void* src, float4* __restrict__ dst, long long n4, int fmt,
+                              const float4* __restrict__ from) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
          i += (long long)gridDim.x * blockDim.x) {
-        dst[i] = fmt == 1 ? unpack_bf16x4(static_cast<const uint2*>(src)[i])
-                          : static_cast<const float4*>(src)[i];
+        const float4 v = fmt == 1 ? unpack_bf16x4(static_cast<const uint2*>(src)[i])
+                                  : static_cast<const float4*>(src)[i];
+        dst[i] = minus_from(from, i, v);
     }
 }
 
@@ -165,12 +174,12 @@ __global__ void pack_i16_kernel(const float4* __restrict__ src, short4* __restri
 }
 
 __global__ void unpack_i16_kernel(const short4* __restrict__ q, const float* __restrict__ scales,
-                                  float4* __restrict__ dst, long long n4) {
+                                  float4* __restrict__ dst, long long n4, const float4* __restrict__ from) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4;
          i += (long long)gridDim.x * blockDim.x) {
         const short4 v = q[i];
         const float sc = scales[i / 8];
-        dst[i] = make_float4(v.x * sc, v.y * sc, v.z * sc, v.w * sc);
+        dst[i] = minus_from(from, i, make_float4(v.x * sc, v.y * sc, v.z * sc, v.w * sc));
     }
 }
 
@@ -345,19 +354,34 @@ cudaError_t launch_pack(const float* src, void* dst, long long n, int format, cu
     return cudaGetLastError();
 }
 
-cudaError_t launch_unpack(const void* src, float* dst, long long n, int format, cudaStream_t s) {
+namespace {
+
+cudaError_t unpack_impl(const void* src, const float* from, float* dst, long long n, int format,
+                        cudaStream_t s) {
+    const float4* f = reinterpret_cast<const float4*>(from);
     if (format == 2) {
         const short4* q = static_cast<const short4*>(src);
         const float* sc = reinterpret_cast<const float*>(static_cast<const unsigned char*>(src) +
                                                          (n * 2 + 15) / 16 * 16);
-        unpack_i16_kernel<<<grid_for(n / 4), 256, 0, s>>>(q, sc, reinterpret_cast<float4*>(dst), n / 4);
+        unpack_i16_kernel<<<grid_for(n / 4), 256, 0, s>>>(q, sc, reinterpret_cast<float4*>(dst), n / 4, f);
         count_launch();
     } else {
         unpack_kernel<<<grid_for(n / 4), 256, 0, s>>>(src, reinterpret_cast<float4*>(dst), n / 4,
-                                                      format);
+                                                      format, f);
         count_launch();
     }
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_unpack(const void* src, float* dst, long long n, int format, cudaStream_t s) {
+    return unpack_impl(src, nullptr, dst, n, format, s);
+}
+
+cudaError_t launch_unpack_diff(const void* src, const float* from, float* dst, long long n, int format,
+                               cudaStream_t s) {
+    return unpack_impl(src, from, dst, n, format, s);
 }
 
 cudaError_t launch_residual_misfit(const float* d, const float* obs, float* res, long long n,

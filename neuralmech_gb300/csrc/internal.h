@@ -33,6 +33,9 @@ enum StepMode : int {
     MODE_GRAD = 2,      // update + accumulate q_{k+1} * L u_k into the gradient (adjoint)
     MODE_GRAD_U = 3,    // as MODE_GRAD, with L u_k computed in the kernel from a staged u_k
                         // tile (2D one-step kernel; the map_lap box is then the u_n box)
+    MODE_SUMMED = 4,    // update only, in the summed (increment) form (2D one-step kernel):
+                        // the state is (u_n, d_n = u_n - u_{n-1}); map_old stages d_n,
+                        // d_{n+1} goes to d_new in place and u_{n+1} = u_n + d_{n+1} to u_new
 };
 
 // A set of points (sources or receivers) bucketed by the tile that owns them.
@@ -83,6 +86,8 @@ struct StepArgs {
     float *grad_bx, *grad_bz;  // MODE_GRAD_U accumulators at the half points (z, x+1/2), (z+1/2, x)
     int zero_ring;             // 2D one-step kernel: also write the fixed ring (and the row
                                // padding) of u_new, as 0; else leave those cells untouched
+    float* d_new;              // MODE_SUMMED: the increment field d, [nshot][cells], updated
+                               // in place (injections are added to it as well as to u_new)
     unsigned* err;
 };
 
@@ -214,6 +219,9 @@ cudaError_t launch_gather(const float* u, long long shot_stride, PointLists list
 size_t ckpt_bytes(int format, long long n);
 cudaError_t launch_pack(const float* src, void* dst, long long n, int format, cudaStream_t s);
 cudaError_t launch_unpack(const void* src, float* dst, long long n, int format, cudaStream_t s);
+// dst = from - (the unpacked src): u_{k0-1} = u_k0 - d_k0 from a summed-form checkpoint
+cudaError_t launch_unpack_diff(const void* src, const float* from, float* dst, long long n, int format,
+                               cudaStream_t s);
 cudaError_t launch_residual_misfit(const float* d, const float* obs, float* res, long long n,
                                    double* misfit, cudaStream_t s);
 cudaError_t launch_grad_finalize(const float* G, const float* vel, float* grad_vel, int nz,

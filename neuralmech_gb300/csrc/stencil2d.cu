@@ -31,6 +31,19 @@
 //     and L u_k formed in the kernel: the recompute then stores nothing but
 //     the levels it writes anyway. This mode runs on 16-row tiles: with the
 //     third tile, two stages of 32-row tiles would leave one CTA per SM.
+//
+// MODE_SUMMED advances the same recursion in its summed (increment) form
+// (P. Henrici, Discrete Variable Methods in Ordinary Differential Equations,
+// 1962): the state is u_n and the increment d_n = u_n - u_{n-1}, and
+//   d_{n+1} = g^2 d_n - (1 - g)^2 u_n + g m L u_n,   u_{n+1} = u_n + d_{n+1},
+// which is u_{n+1} = g (2 u_n + m L u_n) - g^2 u_{n-1} rearranged. In FP32 the
+// increment, about (omega dt) |u| in size, keeps its own low bits. The
+// leapfrog form instead feeds the rounding of two stored levels of size |u|
+// into the velocity u_n - u_{n-1} at every step, where the recursion
+// amplifies it by about 1 / (omega dt). The staged "old" tile is d_n;
+// d_{n+1} is written over it in place (each cell is read and written by its
+// own thread) and u_{n+1} goes to u_new. 4 more bytes per update than the
+// leapfrog step (the d write).
 #include "common.cuh"
 #include "internal.h"
 
@@ -57,7 +70,7 @@ struct Layout2D {
 };
 
 template <int R, int MODE, int RB>
-__global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ? 3 : 2)
+__global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U && MODE != MODE_SUMMED) ? 3 : 2)
     step2d_kernel(const __grid_constant__ CUtensorMap map_cur,
                   const __grid_constant__ CUtensorMap map_old,
                   const __grid_constant__ CUtensorMap map_lap, const StepArgs a) {
@@ -200,29 +213,46 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ?
             const float4 ov =
                 *reinterpret_cast<const float4*>(old + (warp * RB + r) * T2_TX + 4 * lane);
             const float4 l = lap_row<R>(lv, cv, rv, V, r + R, a);
-            float lap[4], nv[4];
+            float lap[4], nv[4], dv[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 const float acc = comp(l, e);
                 lap[e] = acc;
                 const float g = gzr[r] * gxe[e];
                 const float c = comp(cv, e);
-                nv[e] = g * fmaf(comp(mrow[r], e), acc, 2.f * c) - (g * g) * comp(ov, e);
+                if (MODE == MODE_SUMMED) {  // ov is d_n; g = 1 gives d_n + m L u_n
+                    const float omg = 1.f - g;
+                    dv[e] = fmaf(g * comp(mrow[r], e), acc, fmaf(g * g, comp(ov, e), -(omg * omg) * c));
+                    nv[e] = c + dv[e];
+                } else {
+                    nv[e] = g * fmaf(comp(mrow[r], e), acc, 2.f * c) - (g * g) * comp(ov, e);
+                }
             }
             const long long off = (long long)z * a.ld + x;
+            float* dn = MODE == MODE_SUMMED ? a.d_new + (long long)s * a.shot_stride : nullptr;
             if (zin[r] && all_x) {
                 *reinterpret_cast<float4*>(un + off) = make_float4(nv[0], nv[1], nv[2], nv[3]);
+                if (MODE == MODE_SUMMED)
+                    *reinterpret_cast<float4*>(dn + off) = make_float4(dv[0], dv[1], dv[2], dv[3]);
             } else if (a.zero_ring) {
                 // the fixed ring (and the row padding) as 0, so that a level
                 // written to a fresh buffer needs no separate clearing
-                if (z < a.nz && x < a.ld)  // (ld is a multiple of 8: x + 3 < ld)
+                if (z < a.nz && x < a.ld) {  // (ld is a multiple of 8: x + 3 < ld)
                     *reinterpret_cast<float4*>(un + off) =
                         make_float4(zin[r] && xin[0] ? nv[0] : 0.f, zin[r] && xin[1] ? nv[1] : 0.f,
                                     zin[r] && xin[2] ? nv[2] : 0.f, zin[r] && xin[3] ? nv[3] : 0.f);
+                    if (MODE == MODE_SUMMED)
+                        *reinterpret_cast<float4*>(dn + off) =
+                            make_float4(zin[r] && xin[0] ? dv[0] : 0.f, zin[r] && xin[1] ? dv[1] : 0.f,
+                                        zin[r] && xin[2] ? dv[2] : 0.f, zin[r] && xin[3] ? dv[3] : 0.f);
+                }
             } else if (zin[r]) {
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
-                    if (xin[e]) un[off + e] = nv[e];
+                    if (xin[e]) {
+                        un[off + e] = nv[e];
+                        if (MODE == MODE_SUMMED) dn[off + e] = dv[e];
+                    }
             }
             if (MODE == MODE_SAVE_LAP && zin[r]) {
                 const long long lo = (long long)s * a.shot_stride + off;
@@ -288,6 +318,7 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U) ?
                 if (a.inj_times_m) v *= (a.m != nullptr ? a.m[en.x] : a.m_const);
                 const float g = (a.gz ? a.gz[z] : 1.f) * (a.gx ? a.gx[xx] : 1.f);
                 atomicAdd(un + en.x, g * v);
+                if (MODE == MODE_SUMMED) atomicAdd(a.d_new + (long long)s * a.shot_stride + en.x, g * v);
             }
         }
     }
@@ -336,6 +367,7 @@ cudaError_t dispatch_mode(int mode, const CUtensorMap& mc, const CUtensorMap& mo
         case MODE_SAVE_LAP: return launch_impl<R, MODE_SAVE_LAP, RB>(mc, mo, ml, a, s);
         case MODE_GRAD: return launch_impl<R, MODE_GRAD, RB>(mc, mo, ml, a, s);
         case MODE_GRAD_U: return launch_impl<R, MODE_GRAD_U, RB>(mc, mo, ml, a, s);
+        case MODE_SUMMED: return launch_impl<R, MODE_SUMMED, RB>(mc, mo, ml, a, s);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -328,7 +328,7 @@ def _batch(sim, sources, sensors):
 
 
 def measure(sim: ScalarWave, sources, indicator, sensors: Sensors):
-    """Records of every shot: a list of (N, nsensors) tensors (plate.py:140-142)."""
+    """Records of every shot: a list of (N, nsensors) tensors (plate.py:62-64)."""
     src, wav, rec = _batch(sim, sources, sensors)
     vel = sim.velocity(indicator)
     tr = wave_forward(vel, torch.from_numpy(wav).to(vel.device), src, rec, sim.grid())

@@ -3,7 +3,7 @@
 The consumer side of the wave path in projects/18_fwi:
   * ``full_matrix_capture``: every element of an array fires once while all
     elements listen. These are the shots of one batched ``wave_forward``, and
-    the traces come out (emitter, step, receiver) (plate.py:140-142);
+    the traces come out (emitter, step, receiver) (plate.py:62-64);
   * ``analytic_signal``: x + i H[x] along time, the periodic discrete Hilbert
     transform of scipy.signal.hilbert (2D_tfm.py:37), by the library's own
     circular-convolution kernel;

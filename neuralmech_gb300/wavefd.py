@@ -8,7 +8,7 @@ Mapping to the reference (cmpmech/neuralmech):
   * ``step2d_order2``  <- padded_step, projects/18_simple_wave_fd/step2D_wave.cu:59-81
     as driven by 2D_wave_cuda_padding.py:66-76 (same arguments, u2 may alias u0);
   * ``wave_forward``   <- cuwave ``measure(sim, sources, indicator, sensors)``
-    (projects/18_fwi/plate.py:140-142): one forward per shot, traces stacked
+    (projects/18_fwi/plate.py:62-64): one forward per shot, traces stacked
     (shot, step, receiver); differentiable through ``torch.autograd``;
   * ``misfit_gradient`` <- cuwave ``misfit_gradient(sim, sources, gamma, sensors,
     observed) -> (cost, gradient)`` (projects/18_fwi/2D_fwi.py:40), here with
@@ -38,6 +38,7 @@ CKPT_FORMATS = {"fp32": 0, "bf16": 1, "i16": 2}
 LAP_STORES = {"auto": 0, "bf16": 1, "fp32": 2}
 FIELD_FORMATS = {"fp32": 0, "fp16": 1, "i16": 2}
 ADJOINT_MODES = {"checkpoint": 0, "reconstruct": 1}
+UPDATE_FORMS = {"auto": 0, "leapfrog": 1, "summed": 2}
 
 
 @dataclass(frozen=True)
@@ -76,6 +77,15 @@ class Grid:
              (checkpoints, kept levels, recomputed segments) or "reconstruct"
              (time reversal from the last two levels; the sponge frame of every
              level is saved by the forward instead of checkpoints)
+    update       how the forward evaluates the update: "leapfrog" (u_{n+1} over
+             u_{n-1}, 16 B per update), "summed" (state u_n and the increment
+             d_n = u_n - u_{n-1}, d_{n+1} = g^2 d_n - (1 - g)^2 u_n + g m L u_n,
+             u_{n+1} = u_n + d_{n+1}: the FP32 rounding of the increment is no
+             longer that of |u|, so a misfit gradient whose residuals are much
+             smaller than the traces keeps its accuracy; 20 B per update; 2D
+             one-step FP32 fields, lap_store "auto", checkpoint adjoint) or
+             "auto" (summed for the forward of a gradient where available,
+             leapfrog otherwise)
     """
     shape: tuple
     spacing: tuple
@@ -95,6 +105,7 @@ class Grid:
     store_levels: int = 0
     field_format: str = "fp32"
     adjoint: str = "checkpoint"
+    update: str = "auto"
 
     @property
     def ndim(self) -> int:
@@ -175,7 +186,7 @@ def _problem(grid: Grid, nshot: int, nsrc: int, nrec: int, vmax: float) -> _lib.
                         grid.shots_per_cta, grid.group_shots, grid.tile_rows, grid.step_block, grid.store_levels,
                         FIELD_FORMATS[grid.field_format], ADJOINT_MODES[grid.adjoint],
                         max(max(w) for w in grid.sponge_widths()) if grid.adjoint == "reconstruct" else 0,
-                        grid.dt, dz, dy, dx, grid.src_scale, vmax)
+                        grid.dt, dz, dy, dx, grid.src_scale, vmax, UPDATE_FORMS[grid.update])
 
 
 # ---------------------------------------------------------------- argument prep

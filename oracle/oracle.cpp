@@ -17,7 +17,7 @@
 //  * point sources added at their cells (scaled by s and by g) and receivers
 //    sampling u_{n+1} at their cells, traces laid out (shot, step, receiver)
 //    as the reference's full matrix capture stacks them
-//    (projects/18_fwi/plate.py:140-142);
+//    (projects/18_fwi/plate.py:62-64);
 //  * the L2 misfit J = 1/2 sum (d - d_obs)^2 and its exact discrete adjoint
 //    gradient with respect to the velocity and to the wavelets, computed with
 //    exact FP64 checkpoints and segment recomputation.

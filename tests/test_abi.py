@@ -30,7 +30,7 @@ def test_header_declarations_exported():
 def test_version_and_strerror():
     from neuralmech_gb300 import _lib
     lib = _lib.load()
-    assert lib.wfd_version() >> 16 == 2
+    assert lib.wfd_version() >> 16 == 3
     for code in range(0, -8, -1):
         assert lib.wfd_strerror(code).decode()
     assert lib.wfd_strerror(-99).decode() == "unknown status"
@@ -50,6 +50,27 @@ def _ws(p, grad=1):
     n = ctypes.c_size_t(0)
     rc = _lib.load().wfd_workspace_bytes(ctypes.byref(p), grad, ctypes.byref(n))
     return rc, n.value
+
+
+def test_update_form_checks_and_workspace():
+    """The summed form adds one field (the increment d_n) to the workspace of
+    a gradient (auto and summed) or of a forced-summed forward; it is refused
+    where only the leapfrog kernels exist."""
+    from neuralmech_gb300 import _lib
+    field = 2 * 64 * 104 * 4
+    _, lf = _ws(_problem(update_form=1), 1)
+    _, au = _ws(_problem(update_form=0), 1)
+    _, su = _ws(_problem(update_form=2), 1)
+    assert au == su and au - lf >= field
+    _, f0 = _ws(_problem(update_form=0), 0)
+    _, f2 = _ws(_problem(update_form=2), 0)
+    assert f2 - f0 >= field
+    for bad in (dict(update_form=3), dict(update_form=-1),
+                dict(update_form=2, ndim=3, ny=64), dict(update_form=2, step_block=2),
+                dict(update_form=2, lap_store=2), dict(update_form=2, field_format=1),
+                dict(update_form=2, adjoint_mode=1)):
+        rc, _ = _ws(_problem(**bad), 0)
+        assert rc == _lib.WFD_ERR_INVALID, bad
 
 
 def test_workspace_bytes_grows_with_gradient():

@@ -78,13 +78,15 @@ def test_gradient_checkpoint_formats(cuda, orc, fmt, lap_store, tol):
 ])
 def test_u_store_matches_lap_store(cuda, orc, order, shape, nt, ckpt, rows, group):
     """The u-store adjoint (levels u_k kept, L u_k formed in the adjoint
-    kernel) against the stored-FP32-L u adjoint: the same arithmetic per cell,
-    so the gradients agree to FP32 summation-order noise (1e-6)."""
+    kernel) against the stored-FP32-L u adjoint: with the leapfrog forward of
+    both, the same arithmetic per cell, so the gradients agree to FP32
+    summation-order noise (1e-6). The summed-form forward (the default of the
+    u-store path) changes only the forward's rounding: within 1e-4 of both."""
     import dataclasses
     from neuralmech_gb300 import misfit_gradient
     grid, v, wav, src, rec = small_problem(shape=shape, nshot=5, nt=nt, order=order, ckpt_every=ckpt,
                                            seed=21, tile_rows=rows)
-    grid = dataclasses.replace(grid, group_shots=group)
+    grid = dataclasses.replace(grid, group_shots=group, update="leapfrog")
     obs = _observed(orc, grid, v, wav, src, rec)
     args = (torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
             torch.from_numpy(rec), torch.from_numpy(obs).to(cuda))
@@ -96,18 +98,27 @@ def test_u_store_matches_lap_store(cuda, orc, order, shape, nt, ckpt, rows, grou
     assert abs(Ja.item() - Jf.item()) <= 1e-6 * abs(Jf.item())
     assert rel_l2(ga.cpu().numpy(), gf.cpu().numpy()) < 1e-6
     assert rel_l2(gwa.cpu().numpy(), gwf.cpu().numpy()) < 1e-6
+    Js, gs, gws = misfit_gradient(*args, dataclasses.replace(grid, update="auto"), want_wavelet=True)
+    assert abs(Js.item() - Jf.item()) <= 1e-5 * abs(Jf.item())
+    assert rel_l2(gs.cpu().numpy(), gf.cpu().numpy()) < 1e-4
+    assert rel_l2(gws.cpu().numpy(), gwf.cpu().numpy()) < 1e-4
 
 
+@pytest.mark.parametrize("update,tol", [("leapfrog", 1e-6), ("auto", 2e-6)])
 @pytest.mark.parametrize("nt,ckpt,levels", [(100, 13, 30), (100, 13, 10 ** 6), (61, 20, 45)])
-def test_kept_levels_match_recompute(cuda, orc, nt, ckpt, levels):
+def test_kept_levels_match_recompute(cuda, orc, nt, ckpt, levels, update, tol):
     """store_levels: the forward keeps the levels of its last segments and the
-    adjoint recomputes only the others. With FP32 checkpoints the recompute
-    reproduces the kept levels exactly, so the gradients agree to summation
-    order (1e-6); with BF16 checkpoints the kept levels are the exact forward
-    ones, and the gradient is no further from the FP64 oracle than before."""
+    adjoint recomputes only the others. With FP32 checkpoints and the leapfrog
+    forward the recompute reproduces the kept levels exactly, so the gradients
+    agree to summation order (1e-6). With the summed forward (the default) the
+    recompute restarts the leapfrog recursion from u_{k0-1} = u_k0 - d_k0, one
+    rounding away from the forward's levels (2e-6). With BF16 checkpoints the
+    kept levels are the exact forward ones, and the gradient is no further
+    from the FP64 oracle than before."""
     import dataclasses
     from neuralmech_gb300 import misfit_gradient
     grid, v, wav, src, rec = small_problem(shape=(72, 210), nshot=4, nt=nt, ckpt_every=ckpt, seed=8)
+    grid = dataclasses.replace(grid, update=update)
     obs = _observed(orc, grid, v, wav, src, rec)
     args = (torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
             torch.from_numpy(rec), torch.from_numpy(obs).to(cuda))
@@ -118,7 +129,7 @@ def test_kept_levels_match_recompute(cuda, orc, nt, ckpt, levels):
             g = dataclasses.replace(grid, ckpt_format=fmt, store_levels=lv)
             res[fmt, lv] = misfit_gradient(*args, g, want_wavelet=True)
     for k in (1, 2):
-        assert rel_l2(res["fp32", levels][k].cpu().numpy(), res["fp32", 0][k].cpu().numpy()) < 1e-6
+        assert rel_l2(res["fp32", levels][k].cpu().numpy(), res["fp32", 0][k].cpu().numpy()) < tol
     e_rec = rel_l2(res["bf16", 0][1].cpu().numpy(), gr)
     e_kept = rel_l2(res["bf16", levels][1].cpu().numpy(), gr)
     print(f"bf16 checkpoints: gradient rel L2 {e_rec:.2e} recomputed, {e_kept:.2e} with kept levels")
@@ -298,8 +309,8 @@ def test_two_step_matches_one_step_autograd(cuda, orc):
     grid, v, wav, src, rec = small_problem(shape=(64, 200), nshot=2, nt=71, ckpt_every=10, seed=23)
     obs = torch.from_numpy(_observed(orc, grid, v, wav, src, rec)).to(cuda)
     grads = []
-    for sb in (1, 2):
-        g = dataclasses.replace(grid, step_block=sb)
+    for sb in (1, 2):  # (the two-step kernel has the leapfrog form only)
+        g = dataclasses.replace(grid, step_block=sb, update="leapfrog")
         vel = torch.from_numpy(v).to(cuda).requires_grad_(True)
         t = wave_forward(vel, torch.from_numpy(wav).to(cuda), torch.from_numpy(src), torch.from_numpy(rec), g)
         (0.5 * ((t - obs) ** 2).sum()).backward()

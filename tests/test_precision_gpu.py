@@ -3,13 +3,18 @@
 two of its 64 shots, against the FP64 oracle.
 
 * Forward traces: 1e-5 relative L2 (the trace tolerance of this path against
-  the reference solver; measured 5.7e-7).
-* Gradient: on this workload the residuals are ~3.5e-4 of the traces (the
-  2000-step record ends before the deep reflections return), so FP32
-  trace rounding (~6e-7), magnified by that ratio, sets the gradient error
-  (~4e-3) for every checkpoint format. The test states this: BF16 and int16
-  checkpoint storage stay within 5% of the FP32-checkpoint error, and that
-  error stays below 1e-2.
+  the reference solver).
+* Gradient: 1e-3 relative L2, the bound on the FWI gradient against an FP64
+  oracle. On this workload the residuals are about 1.1e-4 of the traces (the
+  2000-step record ends before the deep reflections return), so the gradient
+  sees the FP32 trace error magnified about 10^4 times. The leapfrog update
+  u_{n+1} = g (2 u_n + m L u_n) - g^2 u_{n-1} puts the rounding of two stored
+  levels of size |u| into the velocity u_n - u_{n-1} at every step; its
+  gradient misses the bound (about 4.4e-3, asserted here as a documented
+  miss). The summed form of the same recursion (state u_n and the increment
+  d_n, the default for the forward of a gradient) keeps the increment's own
+  rounding and meets it, with FP32, BF16 and int16 checkpoints alike: every
+  segment but the last is recomputed from a checkpoint here (store_levels 0).
 """
 import dataclasses
 
@@ -30,19 +35,27 @@ def test_fwi1024_two_shots_against_fp64(cuda, orc):
     src, rec = w.src[sel], w.rec[sel]
     wav = np.repeat(w.wavelet[None], 2, 0).astype(np.float32)
     g = w.grid
+    assert g.store_levels == 0 and g.update == "auto"
     obs = orc.forward(oracle_geometry(orc, g, w.vel_true, wav[:, :, None], src, rec)).astype(np.float32)
     geo = oracle_geometry(orc, g, w.vel, wav[:, :, None], src, rec)
-    Jr, gr, _, _ = orc.gradient(geo, obs)
+    Jr, gr, _, tr_ref = orc.gradient(geo, obs)
     args = (torch.from_numpy(w.vel).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
             torch.from_numpy(rec))
-    tr = wave_forward(*args, g).cpu().numpy()
-    e_tr = rel_l2(tr, orc.forward(geo))
-    errs = {}
+    e_tr = {}
+    for form in ("leapfrog", "summed"):
+        tr = wave_forward(*args, dataclasses.replace(g, update=form)).cpu().numpy()
+        e_tr[form] = rel_l2(tr, tr_ref)
+    errs, e_J = {}, {}
+    for form, fmt in (("auto", "fp32"), ("auto", "i16"), ("auto", "bf16"), ("leapfrog", "bf16")):
+        J, gv = misfit_gradient(*args, torch.from_numpy(obs).to(cuda),
+                                dataclasses.replace(g, ckpt_format=fmt, update=form))
+        errs[(form, fmt)] = rel_l2(gv.cpu().numpy(), gr)
+        e_J[(form, fmt)] = abs(float(J) - Jr) / Jr
+    print(f"fwi1024 (2 shots): traces rel L2 {e_tr}; gradient rel L2 {errs}; misfit rel {e_J}")
+    assert e_tr["leapfrog"] < 1e-5 and e_tr["summed"] < 1e-5
+    assert e_tr["summed"] < 0.5 * e_tr["leapfrog"]
     for fmt in ("fp32", "i16", "bf16"):
-        J, gv = misfit_gradient(*args, torch.from_numpy(obs).to(cuda), dataclasses.replace(g, ckpt_format=fmt))
-        errs[fmt] = rel_l2(gv.cpu().numpy(), gr)
-    print(f"fwi1024 (2 shots): traces rel L2 {e_tr:.2e}; gradient rel L2 {errs}")
-    assert e_tr < 1e-5
-    assert errs["fp32"] < 1e-2
-    for fmt in ("i16", "bf16"):
-        assert abs(errs[fmt] - errs["fp32"]) < 0.05 * errs["fp32"]
+        assert errs[("auto", fmt)] <= 1e-3, fmt
+        assert e_J[("auto", fmt)] <= 5e-3, fmt
+    # the leapfrog form's floor: the documented miss of the 1e-3 bound
+    assert 1e-3 < errs[("leapfrog", "bf16")] < 1e-2

@@ -33,9 +33,10 @@ The other workloads (not the headline) print the same JSON line for:
              total focusing onto 512^2 pixels; value = capture cell-updates/s,
              the per-stage times beside it.
 
-Multi-GPU (torchrun, one process per GPU): every rank runs the full 64-shot
-gradient of its own shot set (weak scaling) and the gradients and misfits are
-summed with one all-reduce per step.
+Multi-GPU (torchrun, one process per GPU): the survey holds 64 shots per rank
+(weak scaling); neuralmech_gb300.shard.distributed_misfit_gradient gives each
+rank its contiguous block of 64 and sums the gradients and misfits with one
+all-reduce per step.
 
 --impl reference times the reference's CPU path for this workload on the host
 cores: the FP64 C++/OpenMP restatement in oracle/ (the reference's own solver
@@ -200,6 +201,30 @@ def workload(scale: float, nt: int = 0, shots: int = 0):
     return w
 
 
+def weak_survey(wavelet, src, rec, observed_block, world: int, rank: int):
+    """The survey of a weak-scaling run on `world` ranks: the single-GPU
+    survey's shots once per rank (the same geometry, block r belongs to rank
+    r, as shard_range splits them). Returns full-survey (wavelet, src, rec,
+    observed) tensors; of `observed` only this rank's block is filled, the
+    only block this rank reads."""
+    import torch
+    from neuralmech_gb300.shard import shard_range
+    n = observed_block.shape[0]
+    total = n * world
+    if wavelet.dim() == 1:
+        wavelet = wavelet.reshape(1, -1)
+    wav_all = wavelet.expand(total, *wavelet.shape[1:]).contiguous() if wavelet.shape[0] == 1 else \
+        wavelet.repeat(world, *([1] * (wavelet.dim() - 1)))
+    src_all = src.repeat(world, *([1] * (src.dim() - 1)))
+    rec_all = rec.repeat(world, *([1] * (rec.dim() - 1))) if rec.dim() == 3 else rec
+    obs_all = torch.zeros((total,) + tuple(observed_block.shape[1:]), dtype=observed_block.dtype,
+                          device=observed_block.device)
+    sl = shard_range(total, rank, world)
+    assert sl.stop - sl.start == n
+    obs_all[sl] = observed_block
+    return wav_all, src_all, rec_all, obs_all
+
+
 def kept_segments(g) -> int:
     """Segments whose forward levels the adjoint keeps (the last one at least)."""
     K = g.ckpt_every or int(np.ceil(np.sqrt(g.nt)))
@@ -324,13 +349,127 @@ def config_of(w, args):
             "parallelism": f"{args.gpus} GPU(s), shots batched per GPU, gradient all-reduce"}
 
 
-def _wl_temporal(args, dev):
-    """The order-2 drop-ins on the reference temporal driver's grid."""
+def order2_pairs(dev, grids=((256, 256), (2048, 2048), (8000, 16000)), reps=None):
+    """The reference's own order-2 step kernels (projects/18_simple_wave_fd/
+    step2D_wave.cu, built for sm_103a with --use_fast_math as its drivers build
+    them; oracle/ref_gpu.cpp) beside this library's drop-ins on the same grids
+    and inputs: G updates/s of each and ours / reference.
+      padded_step x 8   vs wfd_step2d_order2 x 8 (and wfd_step2d_exact x 8)
+      temporal_step     vs wfd_temporal_step_fast (and wfd_temporal_step)
+      mixed_step x 8    vs wfd_step2d_mixed x 8 (FP16 storage)
+    Grids: fwd256's and fwd2048's sizes and the temporal driver's 8000 x 16000
+    (2D_wave_cuda_temporal.py:26), the drivers' Gaussian pulse, unit wave
+    speed, dt at 0.95 of the order-2 bound; launches as the drivers launch
+    them (ours on the same stream, one call per launch)."""
     import torch
 
-    extra, graph_kernels = {}, 0
     from neuralmech_gb300 import step2d_order2
-    from neuralmech_gb300.wavefd import step2d_exact, temporal_step
+    from neuralmech_gb300.wavefd import step2d_exact, step2d_mixed, temporal_step, temporal_step_fast
+    from oracle import ref
+    if not ref.gpu_available():
+        return {"unavailable": "the reference's GPU module files were not built (they need its sources)"}
+    out = {}
+    for N, M in grids:
+        Mp = (M + 32) // 32 * 32  # (the FP16 drop-in needs M_padded > M)
+        dx, dy = 1.0 / (N - 1), 2.0 / (M - 1)
+        dt = 0.95 * min(dx, dy) / math.sqrt(2)
+        x = torch.linspace(0, 1, N, device=dev)[:, None]
+        y = torch.linspace(0, 2, M, device=dev)[None, :]
+        u = torch.zeros((N, Mp), device=dev)
+        u[:, :M] = torch.exp(-(x - 0.5) ** 2 / (2 * 0.02 ** 2)) * torch.exp(-(y - 0.5) ** 2 / (2 * 0.02 ** 2))
+        args = (1.0, dt, dx, dy, N, M)
+        inner = (N - 2) * (M - 2)
+        n = reps or max(5, min(200, int(4e8 // (N * M))))
+        bufs = [u.clone(), u.clone(), torch.zeros_like(u), torch.zeros_like(u)]
+        hb = [u.half(), u.half()]
+
+        def eight(fn, a, b):
+            def go():
+                p, q = a, b
+                for _ in range(8):
+                    p = fn(p, q, p, *args)
+                    p, q = q, p
+            return go
+
+        def pair_launch(fn):
+            k = {"k": 0}
+
+            def go():
+                i0, i1, o0, o1 = (0, 1, 2, 3) if k["k"] % 2 == 0 else (2, 3, 0, 1)
+                fn(bufs[i0], bufs[i1], bufs[o0], bufs[o1], *args)
+                k["k"] += 1
+            return go
+
+        def rate(go):
+            for _ in range(2):
+                go()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(n):
+                go()
+            e1.record()
+            torch.cuda.synchronize()
+            return 8 * inner * n / (e0.elapsed_time(e1) / 1e3) / 1e9
+
+        ref.MODE["build"] = "fast"
+        r = {
+            "padded_step x8 (reference, fast math)": rate(eight(ref.padded_step_gpu, bufs[0], bufs[1])),
+            "wfd_step2d_order2 x8": rate(eight(step2d_order2, bufs[0], bufs[1])),
+            "wfd_step2d_exact x8": rate(eight(step2d_exact, bufs[0], bufs[1])),
+            "temporal_step (reference, fast math)": rate(pair_launch(ref.temporal_step_gpu)),
+            "wfd_temporal_step_fast": rate(pair_launch(temporal_step_fast)),
+            "wfd_temporal_step": rate(pair_launch(temporal_step)),
+            "mixed_step x8 (reference, fast math)": rate(eight(ref.mixed_step_gpu, hb[0], hb[1])),
+            "wfd_step2d_mixed x8": rate(eight(step2d_mixed, hb[0], hb[1])),
+        }
+        r["ratio padded"] = r["wfd_step2d_order2 x8"] / r["padded_step x8 (reference, fast math)"]
+        r["ratio temporal"] = r["wfd_temporal_step_fast"] / r["temporal_step (reference, fast math)"]
+        r["ratio mixed"] = r["wfd_step2d_mixed x8"] / r["mixed_step x8 (reference, fast math)"]
+        out[f"{N}x{M}"] = {k: round(v, 2) for k, v in r.items()}
+        del bufs, hb, u
+        torch.cuda.empty_cache()
+    out["unit"] = "G cell-updates/s (8 order-2 updates per timed call)"
+    return out
+
+
+def secondary_legs(dev):
+    """Short legs of the other configurations, in the default run: the fwd2048
+    forward (2048^2, 4000 steps, one shot, order 8, sponge) and the order-2
+    drop-ins beside the reference's own kernels on the temporal driver's
+    8000 x 16000 grid."""
+    import torch
+
+    from neuralmech_gb300 import wave_forward
+    from neuralmech_gb300.synth import workload as wl
+    out = {}
+    w = wl("fwd2048")
+    args = (torch.from_numpy(w.vel).to(dev), torch.from_numpy(w.wavelet).to(dev), torch.from_numpy(w.src),
+            torch.from_numpy(w.rec))
+    for _ in range(3):
+        wave_forward(*args, w.grid, check=False)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        wave_forward(*args, w.grid, check=False)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 5
+    R = w.grid.order // 2
+    out["fwd2048_forward"] = {"value": (2048 - 2 * R) ** 2 * w.grid.nt / (ms / 1e3) / 1e9,
+                              "unit": "Gcell-updates/s", "ms_per_run": ms,
+                              "config": "2048^2, 4000 steps, 1 shot, 2048 receivers, order 8, 20-cell sponge"}
+    out["order2_pairs"] = order2_pairs(dev, grids=((8000, 16000),))
+    return out
+
+
+def _wl_temporal(args, dev):
+    """The order-2 drop-ins on the reference temporal driver's grid, with the
+    reference's own kernels beside them."""
+    import torch
+
+    from neuralmech_gb300.wavefd import temporal_step_fast
     N, M = 8000, 16000  # 2D_wave_cuda_temporal.py:26
     Mp = (M + 31) // 32 * 32
     dx, dy = 1.0 / (N - 1), 2.0 / (M - 1)
@@ -345,31 +484,16 @@ def _wl_temporal(args, dev):
     def step():  # two pairs of arrays, swapped every launch, as 2D_wave_cuda_temporal.py does
         a, b = (0, 1) if state["k"] % 2 == 0 else (2, 3)
         c, d = (2, 3) if state["k"] % 2 == 0 else (0, 1)
-        temporal_step(bufs[a], bufs[b], bufs[c], bufs[d], 1.0, dt, dx, dy, N, M)
+        temporal_step_fast(bufs[a], bufs[b], bufs[c], bufs[d], 1.0, dt, dx, dy, N, M)
         state["k"] += 1
 
     inner = (N - 2) * (M - 2)
-    for name, fn in (("padded_step_gcells", step2d_order2), ("exact_step_gcells", step2d_exact)):
-        def eight():
-            p, q = bufs[0], bufs[1]
-            for _ in range(8):
-                p = fn(p, q, p, 1.0, dt, dx, dy, N, M)
-                p, q = q, p
-        for _ in range(3):
-            eight()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(5):
-            eight()
-        e1.record()
-        torch.cuda.synchronize()
-        extra[name] = 8 * inner * 5 / (e0.elapsed_time(e1) / 1e3) / 1e9
+    extra = {"pairs": order2_pairs(dev)}
     updates, bpu = 8.0 * inner, 16.0 / 8
-    cfg = {"workload": f"temporal: wfd_temporal_step, {N} x {M} (M_padded {Mp}), order 2, Dirichlet, "
+    cfg = {"workload": f"temporal: wfd_temporal_step_fast, {N} x {M} (M_padded {Mp}), order 2, Dirichlet, "
                        "8 updates per launch; bytes: both levels read and written once per launch",
            "l2": "inputs larger than L2 (4 x 512 MB)"}
-    return dict(step=step, updates=updates, bpu=bpu, cfg=cfg, extra=extra, graph_kernels=graph_kernels)
+    return dict(step=step, updates=updates, bpu=bpu, cfg=cfg, extra=extra, graph_kernels=0)
 
 
 def _wl_fmc_tfm(args, dev):
@@ -604,13 +728,15 @@ def main():
     src = torch.from_numpy(w.src)
     rec = torch.from_numpy(w.rec)
     observed = wave_forward(torch.from_numpy(w.vel_true).to(dev), wav, src, rec, g)
+    if world > 1:  # the survey of all ranks, sharded by shot block
+        from neuralmech_gb300.shard import distributed_misfit_gradient
+        survey = weak_survey(wav, src, rec, observed, world, rank)
 
     def step():
-        J, grad = misfit_gradient(vel, wav, src, rec, observed, g, check=False)
         if world > 1:
-            dist.all_reduce(grad)
-            dist.all_reduce(J)
-        return J, grad
+            return distributed_misfit_gradient(vel, *survey, g,
+                                               compute=lambda *a: misfit_gradient(*a, check=False))
+        return misfit_gradient(vel, wav, src, rec, observed, g, check=False)
 
     def barrier():
         if world > 1:
@@ -729,8 +855,11 @@ def main():
 
         # plain: one shot per call (per-shot forward/adjoint, one launch per step)
         P = min(args.plain_shots, w.nshot)
+        # the batched call's level budget too (one shot's levels all fit: nothing is recomputed)
         gp = Grid(g.shape, g.spacing, g.dt, g.nt, order=g.order, sponge=g.sponge, ckpt_every=g.ckpt_every,
                   ckpt_format=g.ckpt_format, shots_per_cta=1)
+        if args.level_store_frac > 0:
+            gp = dataclasses.replace(gp, store_levels=levels_for_budget(gp, 1, budget))
         misfit_gradient(vel, wav, src[:1], rec[:1], observed[:1].contiguous(), gp, check=False)
         barrier()
         e0.record(stream)
@@ -747,6 +876,7 @@ def main():
             u, tcpu, desc = cpu_gradient_sample(w, steps)
             line["cpu_baseline"] = {"value": u / tcpu / 1e9, "unit": UNIT, "cores": os.cpu_count(),
                                     "kind": "port", "sample": desc, "numpy_fd_step": numpy_fd_step_legs()}
+            line["secondary"] = secondary_legs(dev)
 
     if rank == 0:
         print(json.dumps(line), flush=True)

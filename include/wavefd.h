@@ -219,12 +219,25 @@ int wfd_misfit_gradient_overlap(const wfd_problem* p, const float* vel, const fl
  * a device looks up the array's device address with cudaGetSymbolAddress; make
  * it before any stream capture. All calls share the array: calls that overlap
  * on the GPU race, so serialise them; each call clears what must start at zero.
- * Device-side errors of the last call are not reported by wfd_status (the
- * status word lives in the static array); check positions on the host.
+ * Device-side errors go to the static array's status word:
+ * read them with wfd_forward_static_status.
  */
 int wfd_forward_static(const wfd_problem* p, const float* vel, const float* sponge_z,
                        const float* sponge_y, const float* sponge_x, const float* wavelet,
                        const int32_t* src, const int32_t* rec, float* traces, void* stream);
+
+/*
+ * Status of wfd_forward_static on the current device: synchronises `stream`,
+ * returns the first device-side error that calls of wfd_forward_static have
+ * recorded in the static array since the last call of this function
+ * (WFD_ERR_TIMEOUT for a TMA wait that gave up, WFD_ERR_POSITION for a source
+ * or receiver outside the interior, whose samples are then not written) or 0,
+ * and clears it: wfd_status for the static array. The array's device address
+ * is cached per device at the first call of either entry point and belongs to
+ * that device's context: after cudaDeviceReset, do not call either again in
+ * the process. No counterpart in the reference.
+ */
+int wfd_forward_static_status(void* stream);
 
 /*
  * Analytic signal h = x + i H[x] of `ntraces` traces of `nt` samples each
@@ -377,6 +390,20 @@ int wfd_step2d_scaled(const int16_t* q0, const float* s0, const int16_t* q1, con
  */
 int wfd_temporal_step(const float* u0, const float* u1, float* v0, float* v1, float wavespeed, float dt,
                       float dx, float dy, int N, int M, int M_padded, void* stream);
+
+/*
+ * temporal_step's eight updates (the arguments, cells and level roles of
+ * wfd_temporal_step) evaluated as u_{n+1} = (2 u - u_{n-1}) + cx (u_{i-1} -
+ * 2u + u_{i+1}) + cy (u_{j-1} - 2u + u_{j+1}) with the weights cx = k / dx^2,
+ * cy = k / dy^2 divided once (k = dt^2 c^2) and fused multiply-adds: no
+ * division per cell. Within FP32 rounding of the reference expression (1e-5
+ * relative L2 over many launches), as the reference's own build with
+ * --use_fast_math (2D_wave_cuda_temporal.py, COMPILER_OPTIONS) is, not value
+ * for value. The window of each CTA lives in registers. Any M_padded >= M; no
+ * alignment requirement. No counterpart beyond temporal_step itself.
+ */
+int wfd_temporal_step_fast(const float* u0, const float* u1, float* v0, float* v1, float wavespeed, float dt,
+                           float dx, float dy, int N, int M, int M_padded, void* stream);
 
 /*
  * The 1D 3-point step: step1D, projects/18_simple_wave_fd/step1D_wave.cu:4-17.

@@ -27,8 +27,9 @@ EXPORTS = (
     "wfd_strerror", "wfd_last_error", "wfd_version", "wfd_workspace_bytes", "wfd_forward",
     "wfd_backward", "wfd_misfit_gradient", "wfd_status", "wfd_sum_sq", "wfd_step2d_order2",
     "wfd_kernel_launches", "wfd_profile_begin", "wfd_profile_end", "wfd_forward_static",
+    "wfd_forward_static_status",
     "wfd_analytic_signal", "wfd_tfm", "wfd_forward_final", "wfd_step2d_mixed", "wfd_step2d_scaled",
-    "wfd_temporal_step", "wfd_step2d_exact", "wfd_misfit_gradient_overlap",
+    "wfd_temporal_step", "wfd_temporal_step_fast", "wfd_step2d_exact", "wfd_misfit_gradient_overlap",
     "wfd_step1d", "wfd_vd_workspace_bytes", "wfd_vd_forward", "wfd_vd_forward_final", "wfd_vd_misfit_gradient",
 )
 
@@ -99,12 +100,14 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         lib.wfd_step2d_order2.argtypes = [f, f, f, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                           ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
         lib.wfd_forward_static.argtypes = [P, f, f, f, f, f, i32, i32, f, vp]
+        lib.wfd_forward_static_status.argtypes = [vp]
         lib.wfd_forward_final.argtypes = [P, f, f, f, f, f, i32, i32, f, f, vp, sz, vp]
         lib.wfd_analytic_signal.argtypes = [f, ctypes.c_int64, ctypes.c_int, f, f, vp]
         F, I = ctypes.c_float, ctypes.c_int
         lib.wfd_tfm.argtypes = [f, I, f, f, I, F, F, F, f, f, I, I, f, vp]
         lib.wfd_step2d_mixed.argtypes = [vp, vp, vp, F, F, F, F, I, I, I, vp]
         lib.wfd_temporal_step.argtypes = [vp, vp, vp, vp, F, F, F, F, I, I, I, vp]
+        lib.wfd_temporal_step_fast.argtypes = [vp, vp, vp, vp, F, F, F, F, I, I, I, vp]
         lib.wfd_step2d_exact.argtypes = [vp, vp, vp, F, F, F, F, I, I, I, vp]
         lib.wfd_step2d_scaled.argtypes = [vp, f, vp, f, vp, f, F, F, F, F, I, I, I, vp]
         lib.wfd_step1d.argtypes = [f, f, f, F, F, F, I, vp]

@@ -1611,6 +1611,25 @@ int wfd_temporal_step(const float* u0, const float* u1, float* v0, float* v1, fl
     return WFD_OK;
 }
 
+int wfd_temporal_step_fast(const float* u0, const float* u1, float* v0, float* v1, float wavespeed, float dt,
+                           float dx, float dy, int N, int M, int M_padded, void* stream) {
+    if (!u0 || !u1 || !v0 || !v1) return fail(WFD_ERR_INVALID, "NULL field");
+    if (N < 3 || M < 3 || M_padded < M) return fail(WFD_ERR_INVALID, "need N, M >= 3 and M_padded >= M");
+    if ((long long)N * M_padded >= (1ll << 31)) return fail(WFD_ERR_INVALID, "grid too large");
+    if ((N + 31) / 32 > 65535) return fail(WFD_ERR_INVALID, "N too large");
+    const uintptr_t n = (uintptr_t)N * M_padded * sizeof(float);
+    auto overlap = [n](const void* a, const void* b) {
+        const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+        return x < y + n && y < x + n;
+    };
+    if (overlap(v0, u0) || overlap(v0, u1) || overlap(v1, u0) || overlap(v1, u1) || overlap(v0, v1))
+        return fail(WFD_ERR_INVALID, "v0 and v1 must not overlap each other, u0 or u1");
+    const cudaError_t e = launch_temporal_reg(u0, u1, v0, v1, wavespeed, dt, dx, dy, N, M, M_padded, false,
+                                              static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "temporal step launch failed: %s", cudaGetErrorString(e));
+    return WFD_OK;
+}
+
 int wfd_step2d_order2(const float* u0, const float* u1, float* u2, float wavespeed, float dt,
                       float dx, float dy, int N, int M, int M_padded, void* stream) {
     if (!u0 || !u1 || !u2) return fail(WFD_ERR_INVALID, "NULL field");

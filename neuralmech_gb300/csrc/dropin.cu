@@ -228,12 +228,146 @@ __global__ void __launch_bounds__(TT_THREADS)
     }
 }
 
+// Eight steps per launch with the window in registers (temporal_step's
+// arguments and results). A CTA of 8 warps holds a 256-column x 40-row window:
+// thread t owns column t, both levels of its 40 rows in registers. The
+// vertical neighbours are registers of the same thread, the horizontal ones
+// come from the neighbouring lanes by warp shuffles; at a warp's edge, lane 0
+// and lane 31 read the neighbouring warp's edge column, which every warp
+// publishes in shared memory at each step (double-buffered by step parity:
+// one CTA barrier per step). The halo is 8 cells on every side, so the
+// 240 x 24 inner tile is exact after the eight steps; the global boundary is
+// never updated, as in temporal_step. Each cell is
+// loaded and stored once per launch with coalesced row accesses (a warp reads
+// 128 contiguous bytes of a row).
+//   EXACT: the reference expression in IEEE operations (update2d), value for
+//          value the reference's padded_step applied eight times;
+//   else:  u_{n+1} = (2 u - u_{n-1}) + cx (u_{i-1} - 2u + u_{i+1}) + cy (...),
+//          cx = k / dx^2, cy = k / dy^2 (fused multiply-adds, no division):
+//          within FP32 rounding of the reference, as its own --use_fast_math
+//          build (approximate division) is.
+constexpr int TR_NW = 8;                    // warps per CTA
+constexpr int TR_W = 32 * TR_NW;            // window columns, one per thread
+constexpr int TR_H = 40;                    // window rows held by each thread
+constexpr int TR_MINB = 2;                  // resident CTAs per SM the register budget allows
+constexpr int TR_HALO = 8;                  // = steps per launch
+constexpr int TR_OX = TR_W - 2 * TR_HALO;   // 240 output columns per CTA
+
+// One step on the window: old <- the new level from (old, cur). GUARD: test
+// every cell against the shrinking window and the global boundary (CTAs whose
+// window reaches the boundary). Without it (windows inside the interior),
+// every cell but the window's first and last rows is updated: the window's
+// edge cells then take values from missing neighbours, but after s steps
+// those spread s cells inwards at most, and the stored tile lies 8 cells in.
+template <bool EXACT, bool GUARD, int H>
+__device__ __forceinline__ void reg_step(float (&old)[H], const float (&cur)[H], float (*edge)[2][H], int warp,
+                                         int lane, bool cupd, int rmin, int rmax, float k, float dx2, float dy2,
+                                         float cx, float cy) {
+    if (lane == 0 || lane == 31) {  // this warp's edge column, for the neighbouring warps
+        float* dst = edge[warp][lane == 31 ? 1 : 0];
+#pragma unroll
+        for (int r = 0; r < H; ++r) dst[r] = cur[r];
+    }
+    __syncthreads();
+    // lane 0: the previous warp's lane-31 column; lane 31: the next warp's
+    // lane-0 column (the window's outer columns are never updated)
+    const float* nb = lane == 31 ? edge[min(warp + 1, TR_NW - 1)][0] : edge[max(warp - 1, 0)][1];
+#pragma unroll
+    for (int r = 1; r < H - 1; ++r) {
+        const float c = cur[r];
+        float l = __shfl_up_sync(0xffffffffu, c, 1);
+        float rr = __shfl_down_sync(0xffffffffu, c, 1);
+        const float e = nb[r];
+        if (lane == 0) l = e;
+        if (lane == 31) rr = e;
+        if (!GUARD || (cupd && r > rmin && r < rmax)) {
+            if (EXACT) {
+                old[r] = update2d(old[r], c, cur[r - 1], cur[r + 1], l, rr, k, dx2, dy2);
+            } else {
+                const float two_c = 2.f * c;
+                old[r] = fmaf(cx, (cur[r - 1] - two_c) + cur[r + 1], fmaf(cy, (l - two_c) + rr, two_c - old[r]));
+            }
+        }
+    }
+}
+
+// H window rows per thread (H - 16 output rows per CTA), MINB resident CTAs
+// per SM for the register allocation.
+template <bool EXACT, int H, int MINB>
+__global__ void __launch_bounds__(TR_W, MINB)
+    temporal_reg_kernel(const float* __restrict__ u0, const float* __restrict__ u1, float* __restrict__ v0,
+                        float* __restrict__ v1, float k, float dx2, float dy2, float cx, float cy, int N, int M,
+                        int Mp) {
+    __shared__ float edge[2][TR_NW][2][H];  // [step parity][warp][lane 0 / lane 31][row]
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int j = blockIdx.x * TR_OX - TR_HALO + t;
+    const int i0 = blockIdx.y * (H - 2 * TR_HALO) - TR_HALO;
+    const bool jin = j >= 0 && j < M;
+    float A[H], B[H];  // u_{n-1}, u_n; they trade roles every step
+    grid_dependency_wait();
+#pragma unroll
+    for (int r = 0; r < H; ++r) {
+        const int i = i0 + r;
+        const bool in = jin && i >= 0 && i < N;  // cells outside the grid hold 0
+        const long long c = (long long)i * Mp + j;
+        A[r] = in ? __ldg(u0 + c) : 0.f;
+        B[r] = in ? __ldg(u1 + c) : 0.f;
+    }
+    if (t == 0) launch_dependents();
+    const bool jupd = j > 0 && j < M - 1;  // the boundary columns (and beyond) stay untouched
+    const int j0 = blockIdx.x * TR_OX - TR_HALO;
+    const bool inner = i0 >= 1 && i0 + H - 1 <= N - 2 && j0 >= 1 && j0 + TR_W - 1 <= M - 2;  // (CTA-uniform)
+    for (int st = 0; st < TR_HALO; st += 2) {
+        if (inner) {
+            reg_step<EXACT, false, H>(A, B, edge[0], warp, lane, true, 0, 0, k, dx2, dy2, cx, cy);
+            reg_step<EXACT, false, H>(B, A, edge[1], warp, lane, true, 0, 0, k, dx2, dy2, cx, cy);
+            continue;
+        }
+        // updated rows: inside the shrinking window and inside (0, N - 1)
+        for (int h = 0; h < 2; ++h) {
+            const int s2 = st + h;
+            const int rmin = max(s2, -i0), rmax = min(H - 1 - s2, N - 1 - i0);
+            const bool cupd = jupd && t > s2 && t < TR_W - 1 - s2;
+            if (h == 0)
+                reg_step<EXACT, true, H>(A, B, edge[0], warp, lane, cupd, rmin, rmax, k, dx2, dy2, cx, cy);
+            else
+                reg_step<EXACT, true, H>(B, A, edge[1], warp, lane, cupd, rmin, rmax, k, dx2, dy2, cx, cy);
+        }
+    }
+    // A holds u_{n+7}, B u_{n+8}
+    if (t >= TR_HALO && t < TR_W - TR_HALO && j < M) {
+#pragma unroll
+        for (int r = TR_HALO; r < H - TR_HALO; ++r) {
+            const int i = i0 + r;
+            if (i < N) {
+                const long long c = (long long)i * Mp + j;
+                v0[c] = A[r];
+                v1[c] = B[r];
+            }
+        }
+    }
+}
+
 }  // namespace
 
 // the staged window of temporal_kernel: TMA box (columns, rows)
 void temporal_box(unsigned* cols, unsigned* rows) {
     *cols = TT_W;
     *rows = TT_WZ;
+}
+
+cudaError_t launch_temporal_reg(const float* u0, const float* u1, float* v0, float* v1, float wavespeed, float dt,
+                                float dx, float dy, int N, int M, int Mp, bool exact, cudaStream_t s) {
+    constexpr int OZ = TR_H - 2 * TR_HALO;
+    const dim3 grid((M + TR_OX - 1) / TR_OX, (N + OZ - 1) / OZ);
+    const float k = kcoef(wavespeed, dt), dx2 = dx * dx, dy2 = dy * dy;
+    const cudaError_t e =
+        exact ? launch_pdl(temporal_reg_kernel<true, TR_H, TR_MINB>, grid, dim3(TR_W), 0, s, u0, u1, v0, v1, k, dx2,
+                           dy2, k / dx2, k / dy2, N, M, Mp)
+              : launch_pdl(temporal_reg_kernel<false, TR_H, TR_MINB>, grid, dim3(TR_W), 0, s, u0, u1, v0, v1, k,
+                           dx2, dy2, k / dx2, k / dy2, N, M, Mp);
+    count_launch();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_temporal(const CUtensorMap& m0, const CUtensorMap& m1, float* v0, float* v1, float wavespeed,

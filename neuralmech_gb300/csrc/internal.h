@@ -116,6 +116,11 @@ struct LpArgs {
 void temporal_box(unsigned* cols, unsigned* rows);
 cudaError_t launch_temporal(const CUtensorMap& m0, const CUtensorMap& m1, float* v0, float* v1, float wavespeed,
                             float dt, float dx, float dy, int N, int M, int Mp, cudaStream_t s);
+// The eight-step drop-in with the window in registers (no TMA): exact = the
+// reference expression in IEEE operations, else pre-divided weights and FMAs.
+// Grid (ceil(M / 240), ceil(N / 32)) CTAs of 256 threads.
+cudaError_t launch_temporal_reg(const float* u0, const float* u1, float* v0, float* v1, float wavespeed, float dt,
+                                float dx, float dy, int N, int M, int Mp, bool exact, cudaStream_t s);
 cudaError_t launch_step2d_lp(int R, int fmt, const CUtensorMap& map_cur, const CUtensorMap& map_old,
                              const CUtensorMap& map_cs, const CUtensorMap& map_os, const LpArgs& p,
                              cudaStream_t s);

@@ -25,6 +25,16 @@
 // forward clears what must start at zero: both wavefield levels, the point
 // counters and the status word. Calls that overlap on the GPU (for example on
 // two streams at once) race on the array; serialise them.
+//
+// Device-side errors (a bounded TMA wait that gave up, a source or receiver
+// outside the interior) go to the status word at the start of the array, the
+// place wfd_status reads in a caller workspace; wfd_forward_static_status
+// reads and clears it.
+//
+// The cached device address belongs to the device's primary context as it was
+// at the first call. After cudaDeviceReset (or anything else that destroys
+// that context) it no longer names the array: do not call these entry points
+// on that device again in the same process.
 #include <mutex>
 
 #include "../../include/wavefd.h"
@@ -42,6 +52,29 @@ void* g_scratch_address[kMaxDevices] = {};
 
 }  // namespace
 
+// The array's device address on the current device, looked up (and cached)
+// on the first use; nullptr with the error recorded when that fails.
+static void* scratch_address(int* status) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        *status = wfd::set_error(WFD_ERR_CUDA, "wfd_forward_static: no usable current device");
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_address[dev]) {
+        void* addr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&addr, g_static_scratch);
+        if (e != cudaSuccess || addr == nullptr) {
+            *status = wfd::set_error(WFD_ERR_CUDA, "wfd_forward_static: cudaGetSymbolAddress of the static "
+                                                   "scratch failed");
+            return nullptr;
+        }
+        g_scratch_address[dev] = addr;
+    }
+    *status = WFD_OK;
+    return g_scratch_address[dev];
+}
+
 extern "C" int wfd_forward_static(const wfd_problem* p, const float* vel, const float* sponge_z,
                                   const float* sponge_y, const float* sponge_x,
                                   const float* wavelet, const int32_t* src, const int32_t* rec,
@@ -53,23 +86,15 @@ extern "C" int wfd_forward_static(const wfd_problem* p, const float* vel, const 
         return wfd::set_error(WFD_ERR_WORKSPACE,
                               "wfd_forward_static: the forward scratch of this problem exceeds the "
                               "64 MiB static array; use wfd_forward with a caller workspace");
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-        return wfd::set_error(WFD_ERR_CUDA, "wfd_forward_static: no usable current device");
-    void* scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_scratch_mutex);
-        if (!g_scratch_address[dev]) {
-            void* addr = nullptr;
-            const cudaError_t e = cudaGetSymbolAddress(&addr, g_static_scratch);
-            if (e != cudaSuccess || addr == nullptr)
-                return wfd::set_error(WFD_ERR_CUDA,
-                                      "wfd_forward_static: cudaGetSymbolAddress of the static "
-                                      "scratch failed");
-            g_scratch_address[dev] = addr;
-        }
-        scratch = g_scratch_address[dev];
-    }
+    void* scratch = scratch_address(&rc);
+    if (!scratch) return rc;
     return wfd_forward(p, vel, sponge_z, sponge_y, sponge_x, wavelet, src, rec, traces, 0,
                        scratch, kStaticScratchBytes, stream);
+}
+
+extern "C" int wfd_forward_static_status(void* stream) {
+    int rc = WFD_OK;
+    void* scratch = scratch_address(&rc);
+    if (!scratch) return rc;
+    return wfd_status(scratch, stream);  // the status word is the array's first bytes
 }

@@ -492,6 +492,16 @@ def temporal_step(u0, u1, v0, v1, wavespeed: float, dt: float, dx: float, dy: fl
     return v0, v1
 
 
+def temporal_step_fast(u0, u1, v0, v1, wavespeed: float, dt: float, dx: float, dy: float, N: int, M: int):
+    """temporal_step's eight updates with pre-divided weights and fused
+    multiply-adds (no division per cell): within FP32 rounding of the
+    reference expression, as the reference's --use_fast_math build is."""
+    _check_fields(torch.float32, (("u0", u0), ("u1", u1), ("v0", v0), ("v1", v1)), 2)
+    _lib.check(_lib.load().wfd_temporal_step_fast(_ptr(u0), _ptr(u1), _ptr(v0), _ptr(v1), wavespeed, dt, dx, dy,
+                                                  N, M, u1.shape[1], _stream()), "wfd_temporal_step_fast")
+    return v0, v1
+
+
 def step2d_scaled(q0, s0, q1, s1, q2, s2, wavespeed: float, dt: float, dx: float, dy: float, N: int,
                   M: int):
     """scaled_step (step2D_wave.cu:128-183): the padded_step update on int16

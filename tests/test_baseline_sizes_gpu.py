@@ -1,0 +1,104 @@
+"""Parity at the benchmark configurations' own sizes, against the FP64 oracle.
+
+  * fwd256 (256^2, 1000 steps, one shot, 256 receivers) and fwd2048 (2048^2,
+    4000 steps, one shot, 2048 receivers): forward traces within 1e-5
+    relative L2, for the leapfrog update (the default of a forward) and the
+    summed form;
+  * batch8: the largest of its eight models (grid and step count of the
+    seeded draw), two of its shots, misfit gradient with BF16 and FP32
+    checkpoints (every shot's segments but the last recomputed): the errors
+    are stated (printed) and bounded by 1e-3, the bound of the 2D gradient;
+  * fwi384_3d: the full 384^3 grid, one shot with its 64 x 64 receivers, the
+    first 200 steps, checkpoints every 39 in BF16 and in FP32 (3D has the
+    leapfrog update only): traces within 1e-5, the gradient errors stated and
+    bounded by 1e-2.
+
+The observed data of the gradients are the oracle's FP64 traces of the true
+model, rounded to FP32.
+"""
+import dataclasses
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+from helpers import oracle_geometry
+
+pytestmark = pytest.mark.gpu
+
+
+def _args(w, sel, cuda):
+    src, rec = w.src[sel], (w.rec[sel] if w.rec.ndim == 3 else w.rec)
+    wav = np.repeat(np.asarray(w.wavelet)[None], len(sel), 0).astype(np.float32)
+    t = (torch.from_numpy(w.vel).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+         torch.from_numpy(rec))
+    return t, wav, src, rec
+
+
+@pytest.mark.parametrize("name", ["fwd256", "fwd2048"])
+def test_forward_traces_at_full_size(cuda, orc, name):
+    from neuralmech_gb300 import synth, wave_forward
+    w = synth.workload(name)
+    args, wav, src, rec = _args(w, [0], cuda)
+    ref = orc.forward(oracle_geometry(orc, w.grid, w.vel, wav[:, :, None], src, rec))
+    errs = {}
+    for form in ("leapfrog", "summed"):
+        tr = wave_forward(*args, dataclasses.replace(w.grid, update=form)).cpu().numpy()
+        errs[form] = rel_l2(tr, ref)
+    print(f"{name}: {w.grid.shape} x {w.grid.nt} steps, traces rel L2 vs FP64 {errs}")
+    assert errs["leapfrog"] < 1e-5 and errs["summed"] < 1e-5
+
+
+def test_batch8_largest_model_gradient(cuda, orc):
+    from neuralmech_gb300 import misfit_gradient, synth
+    models = synth.workload("batch8")
+    w = max(models, key=lambda m: (m.grid.shape[0], m.grid.nt))
+    sel = [0, w.nshot - 1]
+    args, wav, src, rec = _args(w, sel, cuda)
+    g = w.grid
+    obs = orc.forward(oracle_geometry(orc, g, w.vel_true, wav[:, :, None], src, rec)).astype(np.float32)
+    Jr, gr, _, _ = orc.gradient(oracle_geometry(orc, g, w.vel, wav[:, :, None], src, rec), obs)
+    errs = {}
+    for fmt in ("bf16", "fp32"):
+        J, gv = misfit_gradient(*args, torch.from_numpy(obs).to(cuda), dataclasses.replace(g, ckpt_format=fmt))
+        errs[fmt] = rel_l2(gv.cpu().numpy(), gr)
+    print(f"batch8 largest model {g.shape} x {g.nt} steps (ckpt every {g.ckpt_every or 'sqrt'}), "
+          f"2 shots: gradient rel L2 vs FP64 {errs}")
+    for fmt, e in errs.items():
+        assert e <= 1e-3, fmt
+
+
+def _host_memory_gb() -> float:
+    try:
+        return os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES") / 2**30
+    except (ValueError, OSError):
+        return 0.0
+
+
+def test_fwi384_3d_full_grid(cuda, orc):
+    """The oracle keeps FP64 checkpoints and L u of a segment on the host:
+    about 20 GB at 384^3 (skipped on hosts with less than 64 GB)."""
+    if _host_memory_gb() < 64:
+        pytest.skip("the FP64 oracle at 384^3 needs about 20 GB of host memory")
+    from neuralmech_gb300 import misfit_gradient, synth, wave_forward
+    w = synth.workload("fwi384_3d")
+    nt = 200
+    g = dataclasses.replace(w.grid, nt=nt)
+    w.wavelet = w.wavelet[:nt]
+    args, wav, src, rec = _args(w, [0], cuda)
+    geo_true = oracle_geometry(orc, g, w.vel_true, wav[:, :, None], src, rec)
+    obs = orc.forward(geo_true).astype(np.float32)
+    geo = dataclasses.replace(oracle_geometry(orc, g, w.vel, wav[:, :, None], src, rec), ckpt_every=20)
+    Jr, gr, _, tr_ref = orc.gradient(geo, obs)
+    e_tr = rel_l2(wave_forward(*args, g).cpu().numpy(), tr_ref)
+    errs = {}
+    for fmt in ("bf16", "fp32"):
+        J, gv = misfit_gradient(*args, torch.from_numpy(obs).to(cuda), dataclasses.replace(g, ckpt_format=fmt))
+        errs[fmt] = rel_l2(gv.cpu().numpy(), gr)
+    print(f"fwi384_3d: 384^3, {nt} steps, 1 shot, ckpt every {g.ckpt_every}: traces rel L2 {e_tr:.2e}, "
+          f"gradient rel L2 vs FP64 {errs}")
+    assert e_tr < 1e-5
+    for fmt, e in errs.items():
+        assert e <= 1e-2, fmt

@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import GOLDEN, ROOT
+from conftest import GOLDEN, ROOT, rel_l2
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(ROOT, "tests", "golden")
@@ -261,3 +261,39 @@ def test_temporal_step_rejects_overlapping_outputs(cuda):
     with pytest.raises(_lib.WaveFDError):
         temporal_step(u, u.clone(), u, torch.zeros_like(u), 1.0, 1e-3, 0.1, 0.1, 20, 60)
 
+
+
+@pytest.mark.parametrize("N,M,Mp", [(3, 3, 4), (5, 7, 8), (9, 150, 152), (40, 145, 148), (77, 301, 301),
+                                    (700, 1500, 1504)])
+def test_temporal_step_fast_tracks_exact(cuda, N, M, Mp):
+    """wfd_temporal_step_fast (pre-divided weights, the window in registers):
+    within 1e-6 relative L2 of the exact drop-in after three launches, on
+    grids smaller than one window (boundary path only), ragged edges, an
+    unaligned row stride and several waves of interior windows; the padding
+    columns stay untouched."""
+    from neuralmech_gb300.wavefd import temporal_step, temporal_step_fast
+    g = torch.Generator(device="cpu").manual_seed(N * 7 + M)
+    x = torch.linspace(0, 1, N)[:, None]
+    y = torch.linspace(0, 2, M)[None, :]
+    u = torch.zeros((N, Mp))
+    u[:, :M] = torch.exp(-((x - 0.45) ** 2 + (y - 0.8) ** 2) / (2 * 0.1 ** 2)) + \
+        0.01 * (torch.rand((N, M), generator=g) - 0.5)
+    u = u.to(cuda)
+    dx, dy = 1.0 / max(N - 1, 1), 2.0 / max(M - 1, 1)
+    args = (1.0, 0.9 * min(dx, dy) / math.sqrt(2), dx, dy, N, M)
+    out = {}
+    for name, fn in (("exact", temporal_step), ("fast", temporal_step_fast)):
+        a0, a1 = u.clone(), (u * 0.999).clone()
+        b0, b1 = torch.full_like(u, 3.0), torch.full_like(u, 3.0)
+        for _ in range(3):
+            fn(a0, a1, b0, b1, *args)
+            a0, a1, b0, b1 = b0, b1, a0, a1
+        out[name] = (a0, a1)
+    for lev in (0, 1):
+        e, f = out["exact"][lev], out["fast"][lev]
+        assert torch.isfinite(f).all()
+        assert rel_l2(f[:, :M].cpu().numpy(), e[:, :M].cpu().numpy()) < 1e-6
+        assert torch.equal(f[:, M:], e[:, M:])
+        # the fixed boundary keeps its values exactly
+        assert torch.equal(f[0, :M], e[0, :M]) and torch.equal(f[-1, :M], e[-1, :M])
+        assert torch.equal(f[:, 0], e[:, 0]) and torch.equal(f[:, M - 1], e[:, M - 1])

@@ -68,8 +68,13 @@ def _worker(rank, world, port, mode, result_dir):
     try:
         if mode == "fail" and rank == 1:
             raise RuntimeError("rank 1 fails before its collective")
-        J, g = distributed_misfit_gradient(t(v.astype(np.float64)), t(wav), t(src), t(rec), t(obs), grid,
-                                           compute=_oracle_compute)
+        if mode == "bench":  # the benchmark's weak-scaling survey: the shots once per rank
+            import bench
+            survey = bench.weak_survey(t(wav), t(src), t(rec), t(obs), world, rank)
+            J, g = distributed_misfit_gradient(t(v.astype(np.float64)), *survey, grid, compute=_oracle_compute)
+        else:
+            J, g = distributed_misfit_gradient(t(v.astype(np.float64)), t(wav), t(src), t(rec), t(obs), grid,
+                                               compute=_oracle_compute)
         np.save(os.path.join(result_dir, f"g{rank}.npy"), g.numpy())
         np.save(os.path.join(result_dir, f"J{rank}.npy"), J.numpy())
         status = "ok"
@@ -108,6 +113,22 @@ def test_two_ranks_match_one_process(tmp_path):
         Jr = float(np.load(tmp_path / f"J{r}.npy"))
         assert np.linalg.norm(gr - g.numpy()) <= 1e-12 * np.linalg.norm(g.numpy())
         assert abs(Jr - float(J)) <= 1e-12 * float(J)
+
+
+def test_bench_weak_survey_two_ranks(tmp_path):
+    """The multi-GPU benchmark's path (bench.weak_survey + the shard module)
+    on two gloo ranks: each rank computes its own block of the doubled survey,
+    and the all-reduced misfit and gradient are twice those of one block."""
+    status = _spawn("bench", tmp_path)
+    assert status == ["ok", "ok"], status
+    grid, v, wav, src, rec, obs = _problem()
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a))
+    J, g = _oracle_compute(t(v.astype(np.float64)), t(wav), t(src), t(rec), t(obs), grid)
+    for r in range(2):
+        gr = np.load(tmp_path / f"g{r}.npy")
+        Jr = float(np.load(tmp_path / f"J{r}.npy"))
+        assert np.linalg.norm(gr - 2 * g.numpy()) <= 1e-12 * np.linalg.norm(g.numpy())
+        assert abs(Jr - 2 * float(J)) <= 1e-12 * float(J)
 
 
 def test_failed_rank_surfaces_as_collective_error(tmp_path):

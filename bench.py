@@ -87,6 +87,8 @@ def parse():
     ap.add_argument("--plain-shots", type=int, default=4)
     ap.add_argument("--cpu-sample-steps", type=int, default=200)
     ap.add_argument("--no-extras", action="store_true", help="skip e2e, plain and CPU legs")
+    ap.add_argument("--timeline", action="store_true",
+                    help="batch8: device occupancy of one replay from the CUDA activity trace")
     ap.add_argument("--once", action="store_true",
                     help="run one gradient and exit (the command profiled by ncu)")
     ap.add_argument("--nt", type=int, default=0, help="override the number of time steps (profiling)")
@@ -356,7 +358,7 @@ def order2_pairs(dev, grids=((256, 256), (2048, 2048), (8000, 16000)), reps=None
     and inputs: G updates/s of each and ours / reference.
       padded_step x 8   vs wfd_step2d_order2 x 8 (and wfd_step2d_exact x 8)
       temporal_step     vs wfd_temporal_step_fast (and wfd_temporal_step)
-      mixed_step x 8    vs wfd_step2d_mixed x 8 (FP16 storage)
+      mixed_step x 8    vs wfd_step2d_mixed_fast x 8 (and wfd_step2d_mixed x 8; FP16 storage)
     Grids: fwd256's and fwd2048's sizes and the temporal driver's 8000 x 16000
     (2D_wave_cuda_temporal.py:26), the drivers' Gaussian pulse, unit wave
     speed, dt at 0.95 of the order-2 bound; launches as the drivers launch
@@ -364,7 +366,8 @@ def order2_pairs(dev, grids=((256, 256), (2048, 2048), (8000, 16000)), reps=None
     import torch
 
     from neuralmech_gb300 import step2d_order2
-    from neuralmech_gb300.wavefd import step2d_exact, step2d_mixed, temporal_step, temporal_step_fast
+    from neuralmech_gb300.wavefd import (step2d_exact, step2d_mixed, step2d_mixed_fast, temporal_step,
+                                         temporal_step_fast)
     from oracle import ref
     if not ref.gpu_available():
         return {"unavailable": "the reference's GPU module files were not built (they need its sources)"}
@@ -421,11 +424,12 @@ def order2_pairs(dev, grids=((256, 256), (2048, 2048), (8000, 16000)), reps=None
             "wfd_temporal_step_fast": rate(pair_launch(temporal_step_fast)),
             "wfd_temporal_step": rate(pair_launch(temporal_step)),
             "mixed_step x8 (reference, fast math)": rate(eight(ref.mixed_step_gpu, hb[0], hb[1])),
+            "wfd_step2d_mixed_fast x8": rate(eight(step2d_mixed_fast, hb[0], hb[1])),
             "wfd_step2d_mixed x8": rate(eight(step2d_mixed, hb[0], hb[1])),
         }
         r["ratio padded"] = r["wfd_step2d_order2 x8"] / r["padded_step x8 (reference, fast math)"]
         r["ratio temporal"] = r["wfd_temporal_step_fast"] / r["temporal_step (reference, fast math)"]
-        r["ratio mixed"] = r["wfd_step2d_mixed x8"] / r["mixed_step x8 (reference, fast math)"]
+        r["ratio mixed"] = r["wfd_step2d_mixed_fast x8"] / r["mixed_step x8 (reference, fast math)"]
         out[f"{N}x{M}"] = {k: round(v, 2) for k, v in r.items()}
         del bufs, hb, u
         torch.cuda.empty_cache()
@@ -566,6 +570,8 @@ def _wl_batch8(args, dev):
     batch = BatchFWI(models, autotune=True, level_budget=budget)
     graph_kernels = batch.graph_kernels  # replays launch these without a host call each
     step = batch.run
+    if args.timeline:
+        extra["timeline"] = kernel_timeline(step)
     updates, bpu = batch.cell_updates, 18.0
     cfg = {"workload": "batch8: 8 models 512^2..1536^2, 1000..3000 steps, 128 shots, Ricker 10..25 Hz, "
                        "one graph-captured batch gradient (streams per model), autotuned kernels, "
@@ -574,6 +580,49 @@ def _wl_batch8(args, dev):
            "configs": batch.configs,
            "store_levels": [m.call.grid.store_levels for m in batch.models]}
     return dict(step=step, updates=updates, bpu=bpu, cfg=cfg, extra=extra, graph_kernels=graph_kernels)
+
+
+def kernel_timeline(step):
+    """Device-side occupancy of one call of `step` from the CUDA activity
+    trace (torch.profiler / CUPTI): the kernels' [start, end) intervals, their
+    union (time with at least one kernel running), and the gaps between
+    consecutive kernel activity (launch gaps, graph-edge latency). Returns the
+    busy fraction of the span and the gap statistics."""
+    import torch
+    from torch.profiler import ProfilerActivity, profile
+    step()
+    torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as prof:
+        step()
+        torch.cuda.synchronize()
+    iv = []
+    for e in prof.profiler.kineto_results.events():  # raw activity records (graph kernels included)
+        if e.device_type() != torch.autograd.DeviceType.CUDA:
+            continue
+        name = e.name().lower()
+        if "memcpy" in name or "memset" in name:
+            continue
+        t0 = e.start_ns() if hasattr(e, "start_ns") else 1000 * e.start_us()
+        dur = e.duration_ns() if hasattr(e, "duration_ns") else 1000 * e.duration_us()
+        if dur > 0:
+            iv.append((t0 / 1e3, (t0 + dur) / 1e3))
+    if not iv:
+        return {"unavailable": "no CUDA kernel activity recorded"}
+    iv.sort()
+    busy, gaps, cur_s, cur_e = 0.0, [], iv[0][0], iv[0][1]
+    for s0, e0 in iv[1:]:
+        if s0 > cur_e:
+            busy += cur_e - cur_s
+            gaps.append(s0 - cur_e)
+            cur_s, cur_e = s0, e0
+        else:
+            cur_e = max(cur_e, e0)
+    busy += cur_e - cur_s
+    span = iv[-1][1] - iv[0][0]
+    gaps.sort()
+    return {"kernels": len(iv), "span_ms": span / 1e3, "busy_ms": busy / 1e3, "busy_frac": busy / span,
+            "gaps": len(gaps), "gap_total_ms": sum(gaps) / 1e3,
+            "gap_median_us": gaps[len(gaps) // 2] if gaps else 0.0, "gap_max_us": gaps[-1] if gaps else 0.0}
 
 
 def _wl_grid(args, dev):

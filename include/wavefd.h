@@ -363,6 +363,17 @@ int wfd_step2d_mixed(const void* u0, const void* u1, void* u2, float wavespeed, 
                      float dy, int N, int M, int M_padded, void* stream);
 
 /*
+ * mixed_step's update on FP16 fields with pre-divided weights, cx = k / dx^2
+ * and cy = k / dy^2 (k = dt^2 c^2), and fused multiply-adds in FP32, rounded
+ * to FP16 once per cell: within an FP16 rounding of the reference kernel as
+ * its drivers build it (--use_fast_math, 2D_wave_cuda_mixed.py), not value for
+ * value. A thread owns 8 consecutive values (16-byte loads and stores).
+ * M_padded a multiple of 8, fields 16-byte aligned; u2 may alias u0.
+ */
+int wfd_step2d_mixed_fast(const void* u0, const void* u1, void* u2, float wavespeed, float dt, float dx,
+                          float dy, int N, int M, int M_padded, void* stream);
+
+/*
  * The same step with the field stored as int16 plus one FP32 scale per block
  * of 32 values along a row, u = s q: scaled_step, step2D_wave.cu:128-183, as
  * driven by 2D_wave_cuda_scaled.py. q* are [N][M_padded] int16 (8-byte

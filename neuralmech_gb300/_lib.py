@@ -28,7 +28,7 @@ EXPORTS = (
     "wfd_backward", "wfd_misfit_gradient", "wfd_status", "wfd_sum_sq", "wfd_step2d_order2",
     "wfd_kernel_launches", "wfd_profile_begin", "wfd_profile_end", "wfd_forward_static",
     "wfd_forward_static_status",
-    "wfd_analytic_signal", "wfd_tfm", "wfd_forward_final", "wfd_step2d_mixed", "wfd_step2d_scaled",
+    "wfd_analytic_signal", "wfd_tfm", "wfd_forward_final", "wfd_step2d_mixed", "wfd_step2d_mixed_fast", "wfd_step2d_scaled",
     "wfd_temporal_step", "wfd_temporal_step_fast", "wfd_step2d_exact", "wfd_misfit_gradient_overlap",
     "wfd_step1d", "wfd_vd_workspace_bytes", "wfd_vd_forward", "wfd_vd_forward_final", "wfd_vd_misfit_gradient",
 )
@@ -106,6 +106,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         F, I = ctypes.c_float, ctypes.c_int
         lib.wfd_tfm.argtypes = [f, I, f, f, I, F, F, F, f, f, I, I, f, vp]
         lib.wfd_step2d_mixed.argtypes = [vp, vp, vp, F, F, F, F, I, I, I, vp]
+        lib.wfd_step2d_mixed_fast.argtypes = [vp, vp, vp, F, F, F, F, I, I, I, vp]
         lib.wfd_temporal_step.argtypes = [vp, vp, vp, vp, F, F, F, F, I, I, I, vp]
         lib.wfd_temporal_step_fast.argtypes = [vp, vp, vp, vp, F, F, F, F, I, I, I, vp]
         lib.wfd_step2d_exact.argtypes = [vp, vp, vp, F, F, F, F, I, I, I, vp]

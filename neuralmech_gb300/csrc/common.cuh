@@ -195,6 +195,39 @@ __device__ __forceinline__ float4 lap_row(const float4& lv, const float4& cv, co
     return make_float4(lo.x, lo.y, hi.x, hi.y);
 }
 
+// L u at the four cells of a row as sums of neighbour differences,
+// sum_k cx_k ((u_{x-k} - u) + (u_{x+k} - u)) + cz_k ((u_{z-k} - u) + (u_{z+k} - u)),
+// accumulated k = 1 .. R with x before z (the centre weight is -2 sum_k (cx_k +
+// cz_k), so this is L u). Each difference of neighbouring values of a smooth
+// field is exact or nearly so in FP32, and the sum's rounding is relative to
+// the differences instead of to |u| times the centre weight. Packed FP32x2
+// pairs as lap_row.
+template <int R, int N>
+__device__ __forceinline__ float4 lap_row_diff(const float4& lv, const float4& cv, const float4& rv,
+                                               const float4 (&V)[N], int C, const StepArgs& a) {
+    const float w[12] = {lv.x, lv.y, lv.z, lv.w, cv.x, cv.y, cv.z, cv.w, rv.x, rv.y, rv.z, rv.w};
+    // minus the centre values: x - u as one packed add of -u (the negation is exact)
+    const float2 nl = make_float2(-cv.x, -cv.y), nh = make_float2(-cv.z, -cv.w);
+    float2 lo = make_float2(0.f, 0.f), hi = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 1; k <= R; ++k) {
+        const float2 cx = a.cxp[k - 1];
+        const float2 cz = a.czp[k - 1];
+        const float2 xl = __fadd2_rn(__fadd2_rn(make_float2(w[4 - k], w[5 - k]), nl),
+                                     __fadd2_rn(make_float2(w[4 + k], w[5 + k]), nl));
+        const float2 xh = __fadd2_rn(__fadd2_rn(make_float2(w[6 - k], w[7 - k]), nh),
+                                     __fadd2_rn(make_float2(w[6 + k], w[7 + k]), nh));
+        lo = __ffma2_rn(cx, xl, lo);
+        hi = __ffma2_rn(cx, xh, hi);
+        const float4 up = V[C - k], dn = V[C + k];
+        lo = __ffma2_rn(cz, __fadd2_rn(__fadd2_rn(make_float2(up.x, up.y), nl), __fadd2_rn(make_float2(dn.x, dn.y), nl)),
+                        lo);
+        hi = __ffma2_rn(cz, __fadd2_rn(__fadd2_rn(make_float2(up.z, up.w), nh), __fadd2_rn(make_float2(dn.z, dn.w), nh)),
+                        hi);
+    }
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
 // u_{n+1} = m L u_n + 2 u_n - u_{n-1} at 4 interior cells outside the sponge
 // (g = 1), in packed pairs: the general update g (m L u + 2 u) - g^2 u_{n-1}
 // with g = 1, value for value.

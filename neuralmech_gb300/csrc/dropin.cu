@@ -87,6 +87,62 @@ __global__ void mixed_kernel(const __half* __restrict__ u0, const __half* __rest
     }
 }
 
+// FP16 storage with pre-divided weights (the mixed_step update within FP32
+// rounding, as the reference's --use_fast_math build computes it): a thread
+// owns 8 consecutive values j .. j + 7 (j a multiple of 8) of row i, loaded
+// and stored as 16 bytes; the left and right neighbours of the octet are two
+// scalar loads. u2 = (2u - u0) + cx (u_{i-1} - 2u + u_{i+1}) + cy (u_{j-1} -
+// 2u + u_{j+1}), cx = k / dx^2, cy = k / dy^2, rounded to FP16 once.
+__global__ void mixed_fast_kernel(const __half* __restrict__ u0, const __half* __restrict__ u1,
+                                  __half* __restrict__ u2, float cx, float cy, int N, int M, int Mp) {
+    const int j = 8 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i <= 0 || i >= N - 1 || j >= M - 1) return;
+    const size_t c = (size_t)i * Mp + j;
+    const uint4 ra = *reinterpret_cast<const uint4*>(u0 + c);
+    const uint4 rb = *reinterpret_cast<const uint4*>(u1 + c);
+    const uint4 ru = *reinterpret_cast<const uint4*>(u1 + c - Mp);
+    const uint4 rd = *reinterpret_cast<const uint4*>(u1 + c + Mp);
+    float w[10];  // u1 at j - 1 .. j + 8 of row i
+    w[0] = j > 0 ? __half2float(u1[c - 1]) : 0.f;
+    w[9] = j + 8 < Mp ? __half2float(u1[c + 8]) : 0.f;  // (row i + 1 starts after the padding)
+    const __half2* hb = reinterpret_cast<const __half2*>(&rb);
+    const __half2* ha = reinterpret_cast<const __half2*>(&ra);
+    const __half2* hu = reinterpret_cast<const __half2*>(&ru);
+    const __half2* hd = reinterpret_cast<const __half2*>(&rd);
+    float a[8], up[8], dn[8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float2 vb = __half22float2(hb[q]), va = __half22float2(ha[q]);
+        const float2 vu = __half22float2(hu[q]), vd = __half22float2(hd[q]);
+        w[1 + 2 * q] = vb.x;
+        w[2 + 2 * q] = vb.y;
+        a[2 * q] = va.x;
+        a[2 * q + 1] = va.y;
+        up[2 * q] = vu.x;
+        up[2 * q + 1] = vu.y;
+        dn[2 * q] = vd.x;
+        dn[2 * q + 1] = vd.y;
+    }
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const float two_c = 2.f * w[e + 1];
+        v[e] = fmaf(cx, (up[e] - two_c) + dn[e], fmaf(cy, (w[e] - two_c) + w[e + 2], two_c - a[e]));
+    }
+    if (j > 0 && j + 7 < M - 1) {
+        uint4 o;
+        __half2* ho = reinterpret_cast<__half2*>(&o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) ho[q] = __floats2half2_rn(v[2 * q], v[2 * q + 1]);
+        *reinterpret_cast<uint4*>(u2 + c) = o;
+    } else {
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+            if (j + e > 0 && j + e < M - 1) u2[c + e] = __float2half_rn(v[e]);
+    }
+}
+
 // Block-scaled int16: a thread owns 4 values (j .. j + 3, j a multiple of 4) of
 // row i; the 8 lanes of an aligned lane octet hold one 32-value block and
 // share its scale. Rows of the warp: a warp covers 128 columns of one row.
@@ -434,6 +490,25 @@ int wfd_step2d_mixed(const void* u0, const void* u1, void* u2, float wavespeed, 
     mixed_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const __half*>(u0), static_cast<const __half*>(u1), static_cast<__half*>(u2),
         kcoef(wavespeed, dt), dx * dx, dy * dy, N, M, M_padded);
+    count_launch();
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? WFD_OK : set_error(WFD_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int wfd_step2d_mixed_fast(const void* u0, const void* u1, void* u2, float wavespeed, float dt, float dx,
+                          float dy, int N, int M, int M_padded, void* stream) {
+    if (!u0 || !u1 || !u2) return set_error(WFD_ERR_INVALID, "NULL field");
+    if (N < 3 || M < 3 || M_padded < M || M_padded % 8)
+        return set_error(WFD_ERR_INVALID, "need N, M >= 3 and M_padded >= M, a multiple of 8");
+    for (const void* p : {u0, u1, (const void*)u2})
+        if (reinterpret_cast<uintptr_t>(p) % 16) return set_error(WFD_ERR_INVALID, "fields must be 16-byte aligned");
+    if ((long long)N * M_padded >= (1ll << 31)) return set_error(WFD_ERR_INVALID, "grid too large");
+    if ((N + 3) / 4 > 65535) return set_error(WFD_ERR_INVALID, "N too large (more than 262140 rows)");
+    const float k = kcoef(wavespeed, dt);
+    const dim3 block(64, 4), grid((M_padded / 8 + 63) / 64, (N + 3) / 4);
+    mixed_fast_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const __half*>(u0), static_cast<const __half*>(u1), static_cast<__half*>(u2), k / (dx * dx),
+        k / (dy * dy), N, M, M_padded);
     count_launch();
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? WFD_OK : set_error(WFD_ERR_CUDA, cudaGetErrorString(e));

@@ -40,7 +40,10 @@
 // increment, about (omega dt) |u| in size, keeps its own low bits. The
 // leapfrog form instead feeds the rounding of two stored levels of size |u|
 // into the velocity u_n - u_{n-1} at every step, where the recursion
-// amplifies it by about 1 / (omega dt). The staged "old" tile is d_n;
+// amplifies it by about 1 / (omega dt). The Laplacian of this mode is formed
+// from neighbour differences (lap_row_diff), whose rounding is relative to
+// the differences rather than to |u|: with the increment rounded on its own
+// scale, the Laplacian's rounding is the next largest term. The staged "old" tile is d_n;
 // d_{n+1} is written over it in place (each cell is read and written by its
 // own thread) and u_{n+1} goes to u_new. 4 more bytes per update than the
 // leapfrog step (the d write).
@@ -212,7 +215,8 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U &&
             const float4 rv = *reinterpret_cast<const float4*>(row + 2 * T2_XH);
             const float4 ov =
                 *reinterpret_cast<const float4*>(old + (warp * RB + r) * T2_TX + 4 * lane);
-            const float4 l = lap_row<R>(lv, cv, rv, V, r + R, a);
+            const float4 l = MODE == MODE_SUMMED ? lap_row_diff<R>(lv, cv, rv, V, r + R, a)
+                                                 : lap_row<R>(lv, cv, rv, V, r + R, a);
             float lap[4], nv[4], dv[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {

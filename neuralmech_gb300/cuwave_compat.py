@@ -5,7 +5,9 @@ drive the pip package cuwave through a small surface:
   ScalarWave(Nx, dx, N, dt, threads, precision, space_order, wavespeed, density),
   line, shots, point_source, Sensors, sineburst, stable_dt, simulate, measure,
   misfit, misfit_gradient, resample, Adam, grid_coords, interior_slice, circle,
-  box, nodes, threshold, energy, response, response_gradient; and,
+  box, nodes, threshold, energy, response, response_gradient,
+  reconstruction_sensitivity, reconstruction_nodes,
+  ScalarWave.parametrization_jacobian; and,
   for the absorbing layer of projects/0_conceptual_figures/4_analog_rnn.py:
   73,95-97, pad_for_sponge and sponge.
 This module offers the same names and call shapes over PyTorch tensors, with
@@ -226,6 +228,13 @@ class ScalarWave:
         """c = wavespeed sqrt(gamma) on the library's grid."""
         return self.wavespeed * torch.sqrt(self.extend(indicator).clamp_min(0.0))
 
+    def parametrization_jacobian(self, indicator):
+        """(d mass / d gamma, d stiff / d gamma) in the indicator's shape
+        (analog_rnn_train.py:136). This adapter's scalar medium has mass 1
+        and stiffness gamma (c^2 = wavespeed^2 stiff / mass): (0, 1)."""
+        g = torch.as_tensor(indicator, device=self.device, dtype=torch.float32)
+        return torch.zeros_like(g), torch.ones_like(g)
+
 
 def stable_dt(dx, c: float, order: int) -> float:
     return _stable_dt(tuple(dx), c, order)
@@ -431,7 +440,9 @@ def response_gradient(sim, source, indicator, sensors, objective, adjoint=None):
     `objective` maps the record (N, nsensors) to (cost, dJ/d(record)), as the
     reference's objectives do, or to a differentiable scalar tensor. The
     gradient has the indicator's shape, nonzero in [:nx, :ny] only.
-    `adjoint` is taken for the call's shape: the library's checkpointed
+    `adjoint`: reconstruction_sensitivity runs the library's reconstruction
+    adjoint (topopt_acoustic2D.py:195) and combines its mass and stiffness
+    gradients with parametrization_jacobian; otherwise the checkpointed
     adjoint runs.
 
     ScalarWave: autograd through wave_forward (the library's adjoint behind
@@ -440,6 +451,10 @@ def response_gradient(sim, source, indicator, sensors, objective, adjoint=None):
     whose residual is s dJ/d(record), so its gradient is s times the
     objective's; s = max|record| / max|dJ/d(record)| keeps that residual at
     the record's scale in FP32."""
+    if adjoint is reconstruction_sensitivity:
+        J, grads, _, _ = reconstruction_sensitivity(sim, source, indicator, sensors, objective)
+        d_mass, d_stiff = sim.parametrization_jacobian(indicator)
+        return J, d_mass * grads["mass"] + d_stiff * grads["stiff"]
     sens = sensors
     if not isinstance(sens, Sensors):
         sens = Sensors(sim, np.zeros((0, len(sim.Nx))))
@@ -540,6 +555,15 @@ class AcousticWave(ScalarWave):
         kap, rho = self.materials(indicator)
         return torch.sqrt(kap / rho)
 
+    def parametrization_jacobian(self, indicator):
+        """(d mass / d gamma, d stiff / d gamma) in the indicator's shape: the
+        mass is 1/kappa and the stiffness 1/rho, both linear in gamma
+        (1_benchmark_2D/README.md:141-144), so the derivatives are the
+        constants 1/kappa2 - 1/kappa1 and 1/rho2 - 1/rho1."""
+        g = torch.as_tensor(indicator, device=self.device, dtype=torch.float32)
+        return (torch.full_like(g, 1.0 / self.kappa2 - 1.0 / self.kappa1),
+                torch.full_like(g, 1.0 / self.rho2 - 1.0 / self.rho1))
+
     def max_speed(self, indicator) -> float:
         """The speed to give stable_dt for this medium: sqrt(kappa / rho) in
         a smooth medium, larger where 1/rho jumps between cells (air beside
@@ -566,26 +590,112 @@ def acoustic_measure(sim: AcousticWave, sources, indicator, sensors: Sensors):
     return list(tr.unbind(0))
 
 
-def acoustic_misfit_gradient(sim: AcousticWave, sources, indicator, sensors: Sensors, observed):
-    """(cost, d cost / d indicator) for the two-phase medium."""
-    gamma = torch.as_tensor(indicator, device=sim.device, dtype=torch.float32)
+def _acoustic_parts(sim: AcousticWave, sources, gamma, sensors: Sensors, observed, grid):
+    """The variable-density misfit gradient's parts on the library's grid (FP64):
+    (J, dJ/dkappa, dJ/drho, the source term dJ/dgamma at the source nodes,
+    kappa, rho)."""
     kap, rho = sim.materials(gamma)
     scaled = _scaled_sources(sim, sources, gamma)
     src, wav, rec = _batch(sim, scaled, sensors)
     obs = torch.stack([torch.as_tensor(o, device=kap.device, dtype=torch.float32) for o in observed])
-    J, gk, gr, gw = vd_misfit_gradient(kap, rho, torch.from_numpy(wav).to(kap.device), src, rec, obs, sim.grid(),
+    J, gk, gr, gw = vd_misfit_gradient(kap, rho, torch.from_numpy(wav).to(kap.device), src, rec, obs, grid,
                                        want_wavelet=True)
-    # kappa = 1 / ((1-g)/k1 + g/k2): d kappa / d g = -kappa^2 (1/k2 - 1/k1); rho likewise
-    dk = -kap.double() ** 2 * (1 / sim.kappa2 - 1 / sim.kappa1)
-    dr = -rho.double() ** 2 * (1 / sim.rho2 - 1 / sim.rho1)
-    g_pad = (gk.double() * dk + gr.double() * dr)
-    # the source samples scale with gamma at their nodes: + sum_n dJ/dw_n * signal_n
+    # the source samples scale with gamma at their nodes: sum_n dJ/dw_n * signal_n
+    g_src = torch.zeros_like(gk, dtype=torch.float64)
     srcs = list(sources) if isinstance(sources, (list, tuple)) else [sources]
     for si, s in enumerate(srcs):
         sig = torch.from_numpy(_grid_signal(sim, s)).to(kap.device).double()  # (N, nsrc), dt^2 f
         contrib = (gw[si].double() * sig).sum(0)
         for j, (a, b) in enumerate(_grid_points(sim, s.nodes)):
-            g_pad[a, b] += contrib[j]
+            g_src[a, b] += contrib[j]
+    return J, gk.double(), gr.double(), g_src, kap, rho
+
+
+def _to_indicator(sim, g_pad, gamma):
+    """A field on the library's grid -> the indicator's shape (the Nx nodes)."""
     out = torch.zeros_like(gamma)
-    out[tuple(slice(0, n) for n in sim.Nx)] = g_pad[sim.interior].float()
-    return J, out
+    out[tuple(slice(0, n) for n in sim.Nx)] = g_pad[sim.interior].to(out.dtype)
+    return out
+
+
+def acoustic_misfit_gradient(sim: AcousticWave, sources, indicator, sensors: Sensors, observed):
+    """(cost, d cost / d indicator) for the two-phase medium."""
+    gamma = torch.as_tensor(indicator, device=sim.device, dtype=torch.float32)
+    J, gk, gr, g_src, kap, rho = _acoustic_parts(sim, sources, gamma, sensors, observed, sim.grid())
+    # kappa = 1 / ((1-g)/k1 + g/k2): d kappa / d g = -kappa^2 (1/k2 - 1/k1); rho likewise
+    dk = -kap.double() ** 2 * (1 / sim.kappa2 - 1 / sim.kappa1)
+    dr = -rho.double() ** 2 * (1 / sim.rho2 - 1 / sim.rho1)
+    return J, _to_indicator(sim, gk * dk + gr * dr + g_src, gamma)
+
+
+def reconstruction_nodes(sim):
+    """(nodes, count): the nodes whose values the reconstruction adjoint saves
+    at every step (the frame of the grid where the sponge damps, as the
+    library's reconstruction adjoint restores it), as a (D, n) array of node
+    numbers (Source / Sensors numbering, margin nodes negative or beyond Nx),
+    and n; analog_rnn_fixture.py:84 sizes its memory from it. A reflecting
+    plate (no sponge) saves none."""
+    grid = sim.grid()
+    if len(sim.Nx) != 2:
+        raise ValueError("the reconstruction adjoint runs on 2D grids")
+    W = max(max(w) for w in grid.sponge_widths())
+    nz, nx = grid.shape
+    if W == 0:
+        return np.zeros((2, 0), dtype=np.int32), 0
+    z, x = np.meshgrid(np.arange(nz), np.arange(nx), indexing="ij")
+    band = (z < W) | (z >= nz - W) | (x < W) | (x >= nx - W)
+    pts = np.stack([z[band], x[band]]) - sim.margin
+    return pts.astype(np.int32), int(pts.shape[1])
+
+
+def reconstruction_sensitivity(sim, source, indicator, sensors, objective):
+    """(loss, grads, record, None) of one shot with the reconstruction adjoint
+    (analog_rnn_train.py:142; cuwave.sensitivity): the adjoint rebuilds the
+    forward levels by running the step backwards from the last two, with the
+    damped frame restored from per-step copies, instead of checkpoints.
+    `sensors` is a node array (D, n) or a Sensors; `objective` maps the record
+    (N, nsensors) to (cost, dJ/d(record)) or to a differentiable scalar.
+    grads = {"mass": dJ/d mass, "stiff": dJ/d stiff} in the indicator's shape,
+    for the parametrisation of parametrization_jacobian, so that
+    d_mass * grads["mass"] + d_stiff * grads["stiff"] is dJ/d gamma:
+      ScalarWave   mass 1, stiff gamma: dJ/d stiff = dJ/d gamma,
+                   dJ/d mass = -gamma dJ/d gamma;
+      AcousticWave mass 1/kappa, stiff 1/rho: dJ/d mass = -kappa^2 dJ/d kappa,
+                   dJ/d stiff = -rho^2 dJ/d rho; the source samples scale with
+                   gamma at their nodes (this adapter's choice), and that term
+                   is added to dJ/d mass there, divided by d mass / d gamma.
+    2D grids."""
+    if len(sim.Nx) != 2:
+        raise ValueError("the reconstruction adjoint runs on 2D grids")
+    sens = sensors
+    if not isinstance(sens, Sensors):
+        sens = Sensors(sim, np.zeros((0, len(sim.Nx))))
+        sens.nodes = _host(sensors).astype(np.int32).reshape(len(sim.Nx), -1)
+    gamma = torch.as_tensor(indicator, device=sim.device, dtype=torch.float32)
+    grid = dataclasses.replace(sim.grid(), adjoint="reconstruct")
+    if isinstance(sim, AcousticWave):
+        kap, rho = sim.materials(gamma)
+        scaled = _scaled_sources(sim, [source], gamma)
+        src, wav, rec = _batch(sim, scaled, sens)
+        record = vd_forward(kap, rho, torch.from_numpy(wav).to(kap.device), src, rec, grid)[0]
+        J, cot = _cost_and_cotangent(objective, record)
+        peak = float(cot.abs().max())
+        if peak == 0.0:
+            z = torch.zeros_like(gamma)
+            return J, {"mass": z, "stiff": z.clone()}, record, None
+        # residual s dJ/d(record): observed = record - s cot (as response_gradient)
+        scale = max(float(record.abs().max()), 1e-30) / peak
+        observed = (record.double() - scale * cot).float()
+        _, gk, gr, g_src, kap, rho = _acoustic_parts(sim, [source], gamma, sens, [observed], grid)
+        d_mass = 1.0 / sim.kappa2 - 1.0 / sim.kappa1
+        g_mass = (-kap.double() ** 2 * gk + g_src / d_mass) / scale
+        g_stiff = (-rho.double() ** 2 * gr) / scale
+        return J, {"mass": _to_indicator(sim, g_mass, gamma), "stiff": _to_indicator(sim, g_stiff, gamma)}, \
+            record, None
+    src, wav, rec = _batch(sim, source, sens)
+    g = gamma.detach().clone().requires_grad_(True)
+    record = wave_forward(sim.velocity(g), torch.from_numpy(wav).to(g.device), src, rec, grid)[0]
+    J, cot = _cost_and_cotangent(objective, record)
+    record.backward(cot.to(record.dtype))
+    dg = g.grad
+    return J, {"mass": -gamma * dg, "stiff": dg}, record.detach(), None

@@ -472,6 +472,16 @@ def step2d_mixed(u0, u1, u2, wavespeed: float, dt: float, dx: float, dy: float, 
     return u2
 
 
+def step2d_mixed_fast(u0, u1, u2, wavespeed: float, dt: float, dx: float, dy: float, N: int, M: int):
+    """mixed_step's update on (N, M_padded) float16 tensors with pre-divided
+    weights and FMAs (within an FP16 rounding of the reference's fast-math
+    build); M_padded a multiple of 8; u2 may be u0."""
+    _check_fields(torch.float16, (("u0", u0), ("u1", u1), ("u2", u2)), 2)
+    _lib.check(_lib.load().wfd_step2d_mixed_fast(_ptr(u0), _ptr(u1), _ptr(u2), wavespeed, dt, dx, dy,
+                                                 N, M, u1.shape[1], _stream()), "wfd_step2d_mixed_fast")
+    return u2
+
+
 def step2d_exact(u0, u1, u2, wavespeed: float, dt: float, dx: float, dy: float, N: int, M: int):
     """padded_step / shared_step (M_padded = u1.shape[1]) or basic_step /
     coalesced_step (M_padded = M) evaluated as the reference kernels evaluate

@@ -12,9 +12,11 @@ Outputs (small .npz files, committed):
                    a multiple of 32 as in the driver)
   mixed_step.npz   the same for mixed_step (FP16 storage)
   step1d.npz       the same for step1D
-  scaled_step.npz  the same for scaled_step (int16 + FP32 scale per 32 values),
-                   from the NumPy restatement oracle.numpy_ref.scaled_step (the
-                   kernel's warp shuffles do not run in the CPU build)
+  scaled_step.npz  written by make_golden_gpu.py from the reference's own
+                   scaled_step built for the GPU (its warp shuffles do not run
+                   in the CPU build); scaled_golden() below gives the same
+                   arrays from the NumPy restatement oracle.numpy_ref.scaled_step
+                   (a CPU test checks that they are equal)
   temporal_step.npz  two distinct levels (u0, u1) and the level pairs after 8
                    and 16 padded_step updates: what one and two temporal_step
                    launches return (step2D_wave.cu:244-304; the reference states
@@ -105,7 +107,6 @@ def main():
         if t in (0, 1, 24):
             out[f"step{t}"] = b.copy()
     np.savez_compressed(os.path.join(HERE, "step1d.npz"), **out)
-    scaled_golden()
     temporal_golden()
     basic_golden()
     print("golden vectors written to", HERE)
@@ -157,9 +158,10 @@ def temporal_golden():
     np.savez_compressed(os.path.join(HERE, "temporal_step.npz"), **out)
 
 
-def scaled_golden():
-    """scaled_step golden vectors from the NumPy restatement (oracle.numpy_ref):
-    the reference kernel's warp shuffles do not run in the CPU build."""
+def scaled_golden(write: bool = True):
+    """scaled_step vectors from the NumPy restatement (oracle.numpy_ref), in
+    the layout of scaled_step.npz (which make_golden_gpu.py writes from the
+    reference's own kernel). Returns them; writes them only when asked."""
     from oracle import numpy_ref as nr
     out = {}
     for ci, (N, M, L, steps, seed) in enumerate(CASES):
@@ -179,7 +181,9 @@ def scaled_golden():
             a, b = b, a
             if t in (0, 1, steps - 1):
                 out[f"c{ci}_step{t}_q"], out[f"c{ci}_step{t}_s"] = b[0].copy(), b[1].copy()
-    np.savez_compressed(os.path.join(HERE, "scaled_step.npz"), **out)
+    if write:
+        np.savez_compressed(os.path.join(HERE, "scaled_step.npz"), **out)
+    return out
 
 
 if __name__ == "__main__":

@@ -13,12 +13,17 @@ Outputs (default: this folder):
                      and in the layout of make_golden.py: the levels after
                      the first, second and last step, in-place rotation as in
                      2D_wave_cuda_scaled.py
-  temporal_step.npz  temporal_step (step2D_wave.cu:244-304, block barriers)
-                     itself: one and two launches from the two levels of
-                     make_golden.py's temporal case
+  ref_gpu_digests.json  SHA-256 digests of what temporal_step
+                     (step2D_wave.cu:244-304, block barriers) itself returns
+                     after one and two launches from the two levels of each
+                     case of temporal_step.npz (the levels make_golden.py made
+                     by 8 and 16 padded_step updates): the CPU tests check the
+                     committed levels against them without a second copy
 """
 from __future__ import annotations
 
+import hashlib
+import json
 import math
 import os
 import sys
@@ -80,10 +85,22 @@ def temporal(out_dir):
         ref.temporal_step_gpu(u0, u1, v0, v1, *args, N, M)
         ref.temporal_step_gpu(v0, v1, w0, w1, *args, N, M)
         torch.cuda.synchronize()
-        out[f"c{ci}_launch1_v0"], out[f"c{ci}_launch1_v1"] = v0.cpu().numpy(), v1.cpu().numpy()
-        out[f"c{ci}_launch2_v0"], out[f"c{ci}_launch2_v1"] = w0.cpu().numpy(), w1.cpu().numpy()
+        out[f"c{ci}_after8_v0"], out[f"c{ci}_after8_v1"] = v0.cpu().numpy(), v1.cpu().numpy()
+        out[f"c{ci}_after16_v0"], out[f"c{ci}_after16_v1"] = w0.cpu().numpy(), w1.cpu().numpy()
         ci += 1
-    np.savez_compressed(os.path.join(out_dir, "temporal_step_ref_gpu.npz"), **out)
+    digests = {k: digest(v) for k, v in sorted(out.items())}
+    with open(os.path.join(out_dir, "ref_gpu_digests.json"), "w") as f:
+        json.dump({"temporal_step": digests}, f, indent=1, sort_keys=True)
+
+
+def digest(a: np.ndarray) -> str:
+    """SHA-256 of a C-contiguous array's dtype, shape and bytes."""
+    h = hashlib.sha256()
+    a = np.ascontiguousarray(a)
+    h.update(str(a.dtype).encode())
+    h.update(str(a.shape).encode())
+    h.update(a.tobytes())
+    return h.hexdigest()
 
 
 if __name__ == "__main__":

@@ -426,3 +426,80 @@ def test_acoustic_indicator_gradient(cuda, orc):
     an = float((grad.double() * d.double()).sum())
     print("acoustic adapter: fd", fd, "analytic", an)
     assert abs(fd - an) < 5e-3 * abs(fd), (fd, an)
+
+
+def test_parametrization_jacobian():
+    """parametrization_jacobian against central differences of the adapter's
+    own parametrisation: AcousticWave mass 1/kappa and stiffness 1/rho from
+    materials(); ScalarWave (0, 1) with stiffness gamma."""
+    from neuralmech_gb300 import cuwave_compat as cw
+    ac = cw.AcousticWave((12, 10), (0.1, 0.1), 5, 1e-3, space_order=4, device="cpu")
+    g = torch.full((12, 10), 0.4, dtype=torch.float64)
+    dm, ds = ac.parametrization_jacobian(g)
+    h = 0.2  # (1/kappa and 1/rho are linear in gamma; materials() returns FP32)
+
+    def inv(gm):
+        k, r = ac.materials(gm)
+        return 1 / k.double(), 1 / r.double()
+
+    (mp, sp), (mm, sm) = inv(g + h), inv(g - h)
+    fd_m = float(((mp - mm) / (2 * h)).mean())
+    fd_s = float(((sp - sm) / (2 * h)).mean())
+    assert abs(float(dm[0, 0]) - fd_m) < 1e-3 * abs(fd_m)
+    assert abs(float(ds[0, 0]) - fd_s) < 1e-3 * abs(fd_s)
+    sc = cw.ScalarWave((12, 10), (0.1, 0.1), 5, 1e-3, space_order=4, device="cpu")
+    z, o = sc.parametrization_jacobian(torch.ones((12, 10)))
+    assert float(z.abs().max()) == 0.0 and float((o - 1).abs().max()) == 0.0
+
+
+def test_reconstruction_nodes_frame():
+    """reconstruction_nodes: the frame of sponge-width cells along every edge
+    of the library's grid, in node numbers; none for a reflecting plate."""
+    from neuralmech_gb300 import cuwave_compat as cw
+    sim = cw.ScalarWave((40, 30), (0.1, 0.1), 5, 1e-3, space_order=8, damping=6, device="cpu")
+    nodes, n = cw.reconstruction_nodes(sim)
+    nz, nx = sim.grid_shape
+    assert n == nz * nx - (nz - 12) * (nx - 12) and nodes.shape == (2, n)
+    assert nodes.min() == -sim.margin and nodes[0].max() == nz - 1 - sim.margin
+    plate = cw.ScalarWave((40, 30), (0.1, 0.1), 5, 1e-3, space_order=8, device="cpu")
+    assert cw.reconstruction_nodes(plate)[1] == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["scalar", "acoustic"])
+def test_reconstruction_sensitivity_matches_checkpoint_adjoint(cuda, kind):
+    """reconstruction_sensitivity (the library's reconstruction adjoint,
+    analog_rnn_train.py:142) combined with parametrization_jacobian as the
+    driver combines it equals response_gradient with the checkpointed
+    adjoint (1e-4 relative L2: both are the exact discrete gradient, in FP32),
+    on a padded plate with a sponge; the record and loss agree too."""
+    import dataclasses
+    from neuralmech_gb300 import cuwave_compat as cw
+    n, N = 56, 240
+    Nx, width, origin, region = cw.pad_for_sponge((n, n), (1 / (n - 3), 1 / (n - 3)), 0.1)
+    dx = (1 / (n - 3), 1 / (n - 3))
+    if kind == "scalar":
+        dt = 0.5 * cw.stable_dt(dx, 1.0, 8)
+        sim = cw.ScalarWave(Nx, dx, N, dt, space_order=8)
+    else:
+        dt = 0.5 * cw.stable_dt(dx, float(np.sqrt(6.87e8 / 2643.0)), 8)
+        sim = cw.AcousticWave(Nx, dx, N, dt, space_order=8, rho1=1.204, rho2=2643.0, kappa1=1.419e5,
+                              kappa2=6.87e8)
+    gamma = torch.full(sim.Nx_padded, 0.85, device=cuda)
+    gamma[origin[0] + 20:origin[0] + 30, origin[1] + 15:origin[1] + 35] = 0.6
+    sim = dataclasses.replace(sim, damping=cw.sponge(sim, gamma, width, 0.1))
+    t = np.arange(N) * dt
+    c0 = ((origin[0] + 8) * dx[0], (origin[1] + n // 2) * dx[1])
+    src = cw.point_source(sim, c0, cw.sineburst(t, 1.0, 6.0 / (N * dt), 2))
+    sensors = cw.Sensors(sim, [((origin[0] + 8) * dx[0], (origin[1] + k) * dx[1]) for k in range(5, n - 5, 6)])
+    obj = sensors.objective(cw.energy(sim))
+    J1, g1 = cw.response_gradient(sim, src, gamma, sensors.nodes, obj)
+    J2, grads, um, _ = cw.reconstruction_sensitivity(sim, src, gamma, sensors.nodes, obj)
+    d_mass, d_stiff = sim.parametrization_jacobian(gamma)
+    g2 = d_mass * grads["mass"] + d_stiff * grads["stiff"]
+    J3, g3 = cw.response_gradient(sim, src, gamma, sensors.nodes, obj, adjoint=cw.reconstruction_sensitivity)
+    assert um.shape == (N, sensors.nodes.shape[1])
+    assert abs(J1 - J2) <= 1e-5 * abs(J1) and abs(J3 - J2) <= 1e-12 * abs(J2)
+    assert torch.isfinite(g2).all() and float(g1.abs().max()) > 0
+    assert rel_l2(g2.cpu().numpy(), g1.cpu().numpy()) < 1e-4
+    assert rel_l2(g3.cpu().numpy(), g2.cpu().numpy()) < 1e-12

@@ -263,14 +263,15 @@ def test_temporal_step_rejects_overlapping_outputs(cuda):
 
 
 
-@pytest.mark.parametrize("N,M,Mp", [(3, 3, 4), (5, 7, 8), (9, 150, 152), (40, 145, 148), (77, 301, 301),
+@pytest.mark.parametrize("N,M,Mp", [(3, 3, 4), (5, 7, 8), (9, 150, 152), (40, 145, 148), (77, 301, 304),
                                     (700, 1500, 1504)])
 def test_temporal_step_fast_tracks_exact(cuda, N, M, Mp):
     """wfd_temporal_step_fast (pre-divided weights, the window in registers):
     within 1e-6 relative L2 of the exact drop-in after three launches, on
-    grids smaller than one window (boundary path only), ragged edges, an
-    unaligned row stride and several waves of interior windows; the padding
-    columns stay untouched."""
+    grids smaller than one window (boundary path only), ragged edges and
+    several waves of interior windows; the padding columns stay untouched.
+    On unpadded rows (M_padded = M, which the exact drop-in does not take) it
+    gives the same values as on the padded ones."""
     from neuralmech_gb300.wavefd import temporal_step, temporal_step_fast
     g = torch.Generator(device="cpu").manual_seed(N * 7 + M)
     x = torch.linspace(0, 1, N)[:, None]
@@ -297,3 +298,40 @@ def test_temporal_step_fast_tracks_exact(cuda, N, M, Mp):
         # the fixed boundary keeps its values exactly
         assert torch.equal(f[0, :M], e[0, :M]) and torch.equal(f[-1, :M], e[-1, :M])
         assert torch.equal(f[:, 0], e[:, 0]) and torch.equal(f[:, M - 1], e[:, M - 1])
+    a0, a1 = u[:, :M].contiguous(), (u * 0.999)[:, :M].contiguous()
+    b0, b1 = torch.zeros_like(a0), torch.zeros_like(a0)
+    for _ in range(3):  # the fast form on unpadded rows: the same values
+        temporal_step_fast(a0, a1, b0, b1, *args)
+        a0, a1, b0, b1 = b0, b1, a0, a1
+    assert torch.equal(a1, out["fast"][1][:, :M]) and torch.equal(a0, out["fast"][0][:, :M])
+
+
+@pytest.mark.parametrize("N,M,Mp", [(3, 3, 8), (9, 150, 152), (300, 701, 704), (257, 1024, 1032)])
+def test_mixed_fast_tracks_exact(cuda, N, M, Mp):
+    """wfd_step2d_mixed_fast (pre-divided weights, 8 values per thread) against
+    the value-for-value FP16 drop-in over 30 in-place steps: within 2e-3
+    relative L2 (an FP16 rounding here and there), the boundary and the
+    padding untouched."""
+    from neuralmech_gb300.wavefd import step2d_mixed, step2d_mixed_fast
+    x = torch.linspace(0, 1, N)[:, None]
+    y = torch.linspace(0, 2, M)[None, :]
+    u = torch.zeros((N, Mp))
+    u[:, :M] = torch.exp(-((x - 0.45) ** 2 + (y - 0.8) ** 2) / (2 * 0.1 ** 2))
+    u = u.half().to(cuda)
+    dx, dy = 1.0 / max(N - 1, 1), 2.0 / max(M - 1, 1)
+    args = (1.0, 0.9 * min(dx, dy) / math.sqrt(2), dx, dy, N, M)
+    out = {}
+    for name, fn in (("exact", step2d_mixed), ("fast", step2d_mixed_fast)):
+        a, b = u.clone(), (u * 0.999).clone()
+        b[:, M:] = 7.0
+        a[:, M:] = 7.0
+        for _ in range(30):
+            a = fn(a, b, a, *args)
+            a, b = b, a
+        out[name] = b
+    e, f = out["exact"].float(), out["fast"].float()
+    assert torch.isfinite(f).all()
+    assert rel_l2(f[:, :M].cpu().numpy(), e[:, :M].cpu().numpy()) < 2e-3
+    assert torch.equal(f[:, M:], e[:, M:]) and bool((f[:, M:] == 7.0).all())
+    assert torch.equal(f[0], e[0]) and torch.equal(f[-1], e[-1])
+    assert torch.equal(f[:, 0], e[:, 0]) and torch.equal(f[:, M - 1], e[:, M - 1])

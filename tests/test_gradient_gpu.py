@@ -152,10 +152,16 @@ def test_autograd_matches_fused_call(cuda, orc):
     assert rel_l2(vel.grad.cpu().numpy(), g.cpu().numpy()) < 1e-6
 
 
-def test_adjoint_dot_product(cuda):
-    """<S w, y> = <w, S^T y> for the linear map S: wavelets -> traces."""
+@pytest.mark.parametrize("update,tol", [("leapfrog", 1e-5), ("auto", 5e-5)])
+def test_adjoint_dot_product(cuda, update, tol):
+    """<S w, y> = <w, S^T y> for the linear map S: wavelets -> traces. With the
+    leapfrog forward, forward and adjoint are transposes in the same FP32
+    arithmetic (1e-5); the summed forward (the default of a gradient) rounds
+    differently from the leapfrog adjoint (5e-5 on white-noise wavelets)."""
+    import dataclasses
     from neuralmech_gb300 import wave_forward
     grid, v, wav, src, rec = small_problem(shape=(64, 180), nshot=3, nsrc=2, nrec=23, nt=110, seed=2)
+    grid = dataclasses.replace(grid, update=update)
     rng = np.random.default_rng(0)
     w = torch.from_numpy(rng.standard_normal(wav.shape).astype(np.float32)).to(cuda).requires_grad_(True)
     y = torch.from_numpy(rng.standard_normal((3, 110, 23)).astype(np.float32)).to(cuda)
@@ -164,7 +170,7 @@ def test_adjoint_dot_product(cuda):
     traces.backward(y)
     lhs = float((traces.detach().double() * y.double()).sum())
     rhs = float((w.detach().double() * w.grad.double()).sum())
-    assert abs(lhs - rhs) / max(abs(lhs), abs(rhs)) < 1e-5
+    assert abs(lhs - rhs) / max(abs(lhs), abs(rhs)) < tol
 
 
 def test_gradient_finite_differences(cuda, orc):

@@ -369,3 +369,38 @@ def test_vd_gradient_finite_differences(orc, order):
     Jp = 0.5 * ((orc.vd_forward(orc.VdGeometry(**{**g.__dict__, "wavelet": wp})) - obs) ** 2).sum()
     Jm = 0.5 * ((orc.vd_forward(orc.VdGeometry(**{**g.__dict__, "wavelet": wm})) - obs) ** 2).sum()
     assert abs((Jp - Jm) / (2 * eps) - gw[1, 5, 0]) < 1e-6 * abs(gw[1, 5, 0])
+
+
+def test_scaled_golden_is_the_reference_kernel_and_restatement():
+    """scaled_step.npz comes from the reference's own scaled_step run on the
+    GPU (make_golden_gpu.py: its source built for sm_103a with IEEE division
+    and no fused multiply-adds); the NumPy restatement that the GPU drop-in
+    was written against gives the same int16 levels and scales, bit for bit."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from make_golden import scaled_golden
+    want = np.load(os.path.join(GOLDEN, "scaled_step.npz"))
+    got = scaled_golden(write=False)
+    assert sorted(got) == sorted(want.keys())
+    for k in want.keys():
+        assert np.array_equal(got[k], want[k]), k
+
+
+def test_temporal_golden_is_the_reference_kernel():
+    """The committed temporal_step levels (8 and 16 padded_step updates of the
+    reference's CPU build) are what the reference's own temporal_step returns
+    after one and two launches on the GPU: equal SHA-256 digests (recorded by
+    make_golden_gpu.py from that GPU run)."""
+    import json
+    import sys
+    sys.path.insert(0, GOLDEN)
+    from make_golden_gpu import digest
+    with open(os.path.join(GOLDEN, "ref_gpu_digests.json")) as f:
+        ref = json.load(f)["temporal_step"]
+    g = np.load(os.path.join(GOLDEN, "temporal_step.npz"))
+    checked = 0
+    for k in g.keys():
+        if "_after" in k:
+            assert digest(g[k]) == ref[k], k
+            checked += 1
+    assert checked >= 10

@@ -11,8 +11,8 @@ against this library's drop-ins on the same inputs:
     padded_step and temporal_step agree with wfd_step2d_order2 and
     wfd_temporal_step_fast to 1e-5 relative L2 (approximate division and
     contracted products against the IEEE or pre-divided forms), mixed_step
-    with wfd_step2d_mixed to 2e-3 (FP16 storage: a different rounding of one
-    value moves it by an FP16 ulp).
+    with wfd_step2d_mixed and wfd_step2d_mixed_fast to 2e-3 (FP16 storage: a
+    different rounding of one value moves it by an FP16 ulp).
 
 Skipped where the module files were not built (they need the reference
 sources at build time)."""
@@ -87,6 +87,9 @@ def test_mixed_step_bitwise_and_fast(cuda, ref):
     ref.MODE["build"] = "fast"
     fast = _run(ref.mixed_step_gpu, h, args, N, M, 20)
     assert rel_l2(mine.float().cpu().numpy(), fast.float().cpu().numpy()) < 2e-3
+    from neuralmech_gb300.wavefd import step2d_mixed_fast
+    mine_fast = _run(step2d_mixed_fast, h, args, N, M, 20)
+    assert rel_l2(mine_fast.float().cpu().numpy(), fast.float().cpu().numpy()) < 2e-3
 
 
 def test_scaled_step_bitwise(cuda, ref):

@@ -471,11 +471,10 @@ def test_reconstruction_sensitivity_matches_checkpoint_adjoint(cuda, kind, monke
     """reconstruction_sensitivity (the library's reconstruction adjoint,
     analog_rnn_train.py:142) combined with parametrization_jacobian as the
     driver combines it equals response_gradient with the checkpointed
-    adjoint (FP32 checkpoints here), on a padded plate with a sponge; the
-    record and loss agree too. Both are the exact discrete gradient; the
-    bound, 3e-4 relative L2, is the FP32 rounding of running the recursion
-    backwards over 240 steps of a low-frequency burst (the reversal's
-    rounding grows about as the forward's does, by ~1 / (omega dt))."""
+    adjoint, here with FP32 checkpoints (BF16 checkpoints alone move the
+    checkpointed gradient by ~1e-3 on this plate), on a padded plate with a
+    sponge; the record and loss agree too. Both are the exact discrete
+    gradient in FP32: 1e-5 relative L2 (measured 3.5e-7 and 4.2e-7)."""
     import dataclasses
     from neuralmech_gb300 import cuwave_compat as cw
     grid_of = cw.ScalarWave.grid
@@ -508,5 +507,5 @@ def test_reconstruction_sensitivity_matches_checkpoint_adjoint(cuda, kind, monke
     assert torch.isfinite(g2).all() and float(g1.abs().max()) > 0
     err = rel_l2(g2.cpu().numpy(), g1.cpu().numpy())
     print(f"reconstruction_sensitivity ({kind}) vs checkpointed adjoint: gradient rel L2 {err:.2e}")
-    assert err < 3e-4
+    assert err < 1e-5
     assert rel_l2(g3.cpu().numpy(), g2.cpu().numpy()) < 1e-12

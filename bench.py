@@ -607,7 +607,10 @@ def _wl_batch8(args, dev):
         sb = BatchFWI(short, autotune=True)
         extra["timeline"] = kernel_timeline(sb.run)
         extra["timeline"]["batch"] = "batch8 models with a tenth of their steps, one graph replay"
-        del sb
+        se = BatchFWI(short, autotune=True, graph=False)
+        extra["timeline_eager"] = kernel_timeline(se.run)
+        extra["timeline_eager"]["batch"] = "the same batch launched eagerly on its streams"
+        del sb, se
     updates, bpu = batch.cell_updates, 18.0
     cfg = {"workload": "batch8: 8 models 512^2..1536^2, 1000..3000 steps, 128 shots, Ricker 10..25 Hz, "
                        "one graph-captured batch gradient (streams per model), autotuned kernels, "
@@ -631,19 +634,24 @@ def kernel_timeline(step):
     with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as prof:
         step()
         torch.cuda.synchronize()
-    iv = []
+    iv, kinds = [], {}
     for e in prof.profiler.kineto_results.events():  # raw activity records (graph kernels included)
-        if e.device_type() != torch.autograd.DeviceType.CUDA:
+        kind = str(e.device_type())
+        kinds[kind] = kinds.get(kind, 0) + 1
+        if "CUDA" not in kind:
             continue
         name = e.name().lower()
         if "memcpy" in name or "memset" in name:
             continue
-        t0 = e.start_ns() if hasattr(e, "start_ns") else 1000 * e.start_us()
-        dur = e.duration_ns() if hasattr(e, "duration_ns") else 1000 * e.duration_us()
+        t0, dur = e.start_ns(), e.duration_ns()
         if dur > 0:
             iv.append((t0 / 1e3, (t0 + dur) / 1e3))
+    if not iv:  # the aggregated events, where the raw records hold no device activity
+        for e in prof.events():
+            if "CUDA" in str(e.device_type) and e.time_range.elapsed_us() > 0:
+                iv.append((float(e.time_range.start), float(e.time_range.end)))
     if not iv:
-        return {"unavailable": "no CUDA kernel activity recorded"}
+        return {"unavailable": "no CUDA kernel activity recorded", "records": kinds}
     iv.sort()
     busy, gaps, cur_s, cur_e = 0.0, [], iv[0][0], iv[0][1]
     for s0, e0 in iv[1:]:

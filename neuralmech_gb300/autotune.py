@@ -8,9 +8,9 @@ forward (`steps` time steps) for every candidate:
     (automatic, 1, 2, 4, ...).
 
 For the forward of a gradient (``for_gradient``) whose grid asks for the
-summed update form ("auto" or "summed"), only one-step candidates compete,
-timed in that form: the two-step kernel has the leapfrog form only, whose
-accumulated rounding a gradient from small residuals cannot afford.
+summed update form ("auto" or "summed"), the candidates are timed in that
+form (both kernels have it): the leapfrog form's accumulated rounding is
+what a gradient from small residuals cannot afford.
 
 It keeps the fastest, and caches the choice in a JSON file (default
 ``~/.cache/neuralmech_gb300/autotune.json``, or ``$WAVEFD_AUTOTUNE_CACHE``).
@@ -59,7 +59,7 @@ def candidates(nshot: int, summed: bool = False):
         spcs.append(nshot)
     one = [{"tile_rows": tr, "shots_per_cta": s, "step_block": 1} for tr in (32, 16) for s in spcs]
     two = [{"tile_rows": 0, "shots_per_cta": s, "step_block": 2} for s in [0] + spcs]
-    return one if summed else one + two
+    return one + two
 
 
 def summed_for(grid, for_gradient: bool) -> bool:

@@ -246,10 +246,9 @@ int check_problem(const wfd_problem* p) {
     if (p->update_form < WFD_UPDATE_AUTO || p->update_form > WFD_UPDATE_SUMMED)
         return fail(WFD_ERR_INVALID, "unknown update_form %d", p->update_form);
     if (p->update_form == WFD_UPDATE_SUMMED &&
-        (p->ndim != 2 || p->step_block == 2 || p->field_format != WFD_FIELD_FP32 ||
-         p->lap_store != WFD_LAP_AUTO || p->adjoint_mode != WFD_ADJOINT_CHECKPOINT))
-        return fail(WFD_ERR_INVALID, "the summed update form: 2D, one step per launch, FP32 fields, "
-                                     "lap_store auto, checkpoint adjoint");
+        (p->ndim != 2 || p->field_format != WFD_FIELD_FP32 || p->lap_store != WFD_LAP_AUTO ||
+         p->adjoint_mode != WFD_ADJOINT_CHECKPOINT))
+        return fail(WFD_ERR_INVALID, "the summed update form: 2D, FP32 fields, lap_store auto, checkpoint adjoint");
     if (p->recon_band < 0 || 2 * p->recon_band > std::min(p->nz, p->nx))
         return fail(WFD_ERR_INVALID, "recon_band must lie in [0, min(nz, nx) / 2]");
     if (p->tile_rows != 0 && p->tile_rows != 16 && p->tile_rows != 32)
@@ -392,8 +391,7 @@ size_t up256(size_t v) { return (v + 255) / 256 * 256; }
 // WFD_UPDATE_SUMMED, or chosen by WFD_UPDATE_AUTO for a forward that saves the
 // state of a gradient, where the 2D one-step u-store path runs.
 bool summed_forward(const wfd_problem* p, const Geom& g, bool save) {
-    const bool avail = g.ndim == 2 && !g.vd && g.sb == 1 && p->field_format == WFD_FIELD_FP32 && g.ustore &&
-                       !g.recon;
+    const bool avail = g.ndim == 2 && !g.vd && p->field_format == WFD_FIELD_FP32 && g.ustore && !g.recon;
     return avail && (p->update_form == WFD_UPDATE_SUMMED || (p->update_form == WFD_UPDATE_AUTO && save));
 }
 
@@ -410,7 +408,8 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     L.m = take((size_t)g.cells * 4);
     if (g.vd) L.b = take((size_t)g.cells * 4);
     for (int b = 0; b < L.nbuf; ++b) L.P[b] = take(L.field_bytes);
-    if (summed_forward(p, g, grad)) L.D = take(L.field_bytes);  // the increment d_n
+    // the increment d_n; with two steps per launch d_n, d_{n+2} and d_{n+1}
+    if (summed_forward(p, g, grad)) L.D = take((g.sb == 2 ? 3 : 1) * L.field_bytes);
     if (p->field_format == WFD_FIELD_I16) {
         L.scale_bytes = (size_t)p->nshot * g.nz * scale_blocks(g.ld) * 4;
         for (int b = 0; b < 2; ++b) L.S[b] = take(L.scale_bytes);
@@ -756,20 +755,32 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
     if (summed && !w.D) return fail(WFD_ERR_INVALID, "internal: summed forward without its increment field");
     WFD_CUDA(cudaMemsetAsync(buf[loc(-1)], 0, L.field_bytes, s));
     WFD_CUDA(cudaMemsetAsync(buf[loc(0)], 0, L.field_bytes, s));
-    if (summed) WFD_CUDA(cudaMemsetAsync(w.D, 0, L.field_bytes, s));
+    // increment buffers: one step per launch D[0] (in place); two steps per
+    // launch d_n in D[(n / 2) % 2], d_{n+2} in the other, d_{n+1} in D[2]
+    float* D[3] = {w.D, nullptr, nullptr};
+    if (summed && g.sb == 2)
+        for (int k = 1; k < 3; ++k) D[k] = w.D + (size_t)k * (L.field_bytes / sizeof(float));
+    if (summed) WFD_CUDA(cudaMemsetAsync(w.D, 0, L.field_bytes, s));  // d_0 = 0
     std::vector<CUtensorMap> mc(buf.size()), mo(buf.size());
     int rc;
     for (size_t b = 0; b < buf.size(); ++b)
         if ((rc = g.sb == 2 ? st.map_k2(buf[b], &mc[b], &mo[b]) : st.map_pair(buf[b], buf[b], &mc[b], &mo[b])))
             return rc;
     CUtensorMap mdc{}, mdo{};  // d_n as the staged "old" tile
-    if (summed && (rc = st.map_pair(w.D, w.D, &mdc, &mdo))) return rc;
+    CUtensorMap mdu[2]{}, mde[2]{};  // two steps per launch: d_n on the extended region, per buffer
+    if (summed && g.sb == 1 && (rc = st.map_pair(w.D, w.D, &mdc, &mdo))) return rc;
+    if (summed && g.sb == 2)
+        for (int k = 0; k < 2; ++k)
+            if ((rc = st.map_k2(D[k], &mdu[k], &mde[k]))) return rc;
     const long long n_all = (long long)p->nshot * g.cells;
+    // whether level k gets a checkpoint (the start of a segment the adjoint recomputes)
+    auto ckpt_at = [&](int k) { return save && !rc_mode && k % g.K == 0 && !(us && k >= g.k0_store); };
     // (u_{n-1}, u_n) at the start of segment n / K; (d_n, u_n) in the summed form
-    auto checkpoint = [&](int n) -> int {
-        if (!save || rc_mode || n % g.K != 0 || (us && n >= g.k0_store)) return WFD_OK;  // (kept segments need none)
+    // (two steps per launch: d_n in dsrc)
+    auto checkpoint = [&](int n, const float* dsrc) -> int {
+        if (!ckpt_at(n)) return WFD_OK;  // (kept segments need none)
         unsigned char* slot = w.ckpt + (size_t)(n / g.K) * 2 * L.ckpt_field_bytes;
-        WFD_CUDA(launch_pack(summed ? w.D : buf[loc(n - 1)], slot, n_all, p->ckpt_format, s));
+        WFD_CUDA(launch_pack(summed ? dsrc : buf[loc(n - 1)], slot, n_all, p->ckpt_format, s));
         WFD_CUDA(launch_pack(buf[loc(n)], slot + L.ckpt_field_bytes, n_all, p->ckpt_format, s));
         return WFD_OK;
     };
@@ -802,13 +813,27 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
                 q.smp_t1 = n - 1;
                 q.a.smp_t = two ? n : -1;
             }
+            if (summed) {
+                // (u_n, d_n) -> (u_{n+2}, d_{n+2}); the intermediate level leaves the
+                // CTAs only where a checkpoint or a kept level needs it
+                const int din = (n / 2) & 1;
+                q.summed = 1;
+                q.d_out = D[din ^ 1];
+                q.d_mid = two ? D[2] : D[din ^ 1];
+                q.write_mid = !two || ckpt_at(n + 1) || (us && n + 1 >= g.k0_store - 1);
+                if ((rc = st.launch_k2(mc[loc(n)], mde[din], q))) return rc;
+                if ((rc = checkpoint(n, D[din]))) return rc;
+                if (two && (rc = checkpoint(n + 1, D[2]))) return rc;
+                n += two ? 2 : 1;
+                continue;
+            }
             if ((rc = st.launch_k2(mc[loc(n)], mo[loc(n - 1)], q))) return rc;
             for (int k = n; k < n + (two ? 2 : 1); ++k)  // (every level read there is still held)
-                if ((rc = checkpoint(k))) return rc;
+                if ((rc = checkpoint(k, nullptr))) return rc;
             n += two ? 2 : 1;
             continue;
         }
-        if ((rc = checkpoint(n))) return rc;
+        if ((rc = checkpoint(n, w.D))) return rc;
         const int bo = loc(n - 1), bc = loc(n), bn = loc(n + 1);
         const bool lap = save && !g.ustore && n >= g.k0_last;
         StepArgs a = st.base(buf[bn]);

@@ -165,10 +165,18 @@ struct Step2Args {
     int inj_t1;         // step-1 injection time index (-1: none)
     int smp_t1;         // step-1 sampling time index of u_n (-1: none)
     int two_steps;      // 0: step 1 only (u_{n+1} to u_mid)
+    // summed form (the state is u_n and d_n = u_n - u_{n-1}): map_o stages d_n
+    // on E; d_{n+2} goes to d_out, u_{n+2} to a.u_new; the intermediate level
+    // (u_{n+1} to u_mid, d_{n+1} to d_mid) is written only with write_mid (a
+    // checkpoint or a kept level needs it), or when two_steps is 0
+    int summed;
+    float* d_out;       // d_{n+2}, [nshot][cells]; may not alias the staged d_n
+    float* d_mid;       // d_{n+1}, [nshot][cells] (write_mid or !two_steps)
+    int write_mid;
 };
 
-// map_u: u_n (box K2_UW x (K2_TZ + 4R) x 1); map_o: u_{n-1} (box K2_EW x (K2_TZ + 2R) x 1);
-// map_m: m ([nz][ld], box K2_EW x (K2_TZ + 2R)).
+// map_u: u_n (box K2_UW x (K2_TZ + 4R) x 1); map_o: u_{n-1}, or d_n in the summed form
+// (box K2_EW x (K2_TZ + 2R) x 1); map_m: m ([nz][ld], box K2_EW x (K2_TZ + 2R)).
 // Plain steps only (no L u store, no gradient term); a.shots_per_cta shots per CTA.
 cudaError_t launch_step2d_k2(int R, const CUtensorMap& map_u, const CUtensorMap& map_o,
                              const CUtensorMap& map_m, const Step2Args& p, cudaStream_t s);

@@ -23,6 +23,16 @@
 // fall in E (also those owned by neighbouring tiles) are added in shared
 // memory. Step 2 runs over T with lanes 1..30, the same column ownership.
 // Both steps form L u with the packed FP32x2 row stencil of the one-step kernel.
+//
+// SUMMED: the same two steps in the summed (increment) form of the one-step
+// kernel's MODE_SUMMED, state (u_n, d_n = u_n - u_{n-1}):
+//   d_{n+1} = g^2 d_n - (1 - g)^2 u_n + g m L u_n,  u_{n+1} = u_n + d_{n+1},
+// L from neighbour differences. O stages d_n on E; step 1 writes u_{n+1} over
+// it and d_{n+1} into a fourth E buffer D1; step 2 reads both on the tile.
+// Only u_{n+2} and d_{n+2} leave the CTA, to buffers the launch does not read
+// (d_n is read with a halo by the neighbouring tiles, so d is double-
+// buffered): 16 field bytes per two updates instead of 40 for two summed
+// one-step launches. The intermediate level is written only on request.
 #include "common.cuh"
 #include "internal.h"
 
@@ -31,7 +41,7 @@ namespace {
 
 __host__ __device__ constexpr int al128(int v) { return (v + 127) / 128 * 128; }
 
-template <int R>
+template <int R, bool SUMMED = false>
 struct LayoutK2 {
     static constexpr int EH = K2_TZ + 2 * R;  // E rows
     static constexpr int UH = K2_TZ + 4 * R;  // U rows
@@ -41,7 +51,8 @@ struct LayoutK2 {
     static constexpr int STAGE = O_OFF + al128(E_BYTES);
     static constexpr int STAGES = 2;
     static constexpr int M_OFF = STAGES * STAGE;  // m on E, once per CTA
-    static constexpr int BAR_OFF = M_OFF + al128(E_BYTES);
+    static constexpr int D1_OFF = M_OFF + al128(E_BYTES);  // summed: d_{n+1} on E
+    static constexpr int BAR_OFF = D1_OFF + (SUMMED ? al128(E_BYTES) : 0);
     static constexpr int BYTES = BAR_OFF + 64 + 128;  // + barriers + alignment slack
     static constexpr int RB1 = (EH + 7) / 8;  // E rows per warp in step 1
     static constexpr int RB2 = K2_TZ / 8;     // T rows per warp in step 2
@@ -66,17 +77,33 @@ __device__ __forceinline__ void store_level(float* p, const float4& v, bool zin,
     }
 }
 
-template <int R>
+// The summed update of 4 cells: (d_new, u_new) from (u, d, m, L u, g), the
+// one-step kernel's expression; g = 1 gives d + m L u.
+__device__ __forceinline__ void summed4(const float4& u, const float4& d, const float4& m, const float4& l,
+                                        const float* g, float4& dn, float4& un) {
+    float dd[4], uu[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const float omg = 1.f - g[e];
+        dd[e] = fmaf(g[e] * comp(m, e), comp(l, e), fmaf(g[e] * g[e], comp(d, e), -(omg * omg) * comp(u, e)));
+        uu[e] = comp(u, e) + dd[e];
+    }
+    dn = make_float4(dd[0], dd[1], dd[2], dd[3]);
+    un = make_float4(uu[0], uu[1], uu[2], uu[3]);
+}
+
+template <int R, bool SUMMED>
 __global__ void __launch_bounds__(K2_THREADS, 2)
     step2d_k2_kernel(const __grid_constant__ CUtensorMap map_u, const __grid_constant__ CUtensorMap map_o,
                      const __grid_constant__ CUtensorMap map_m, const Step2Args p) {
-    using L = LayoutK2<R>;
+    using L = LayoutK2<R, SUMMED>;
     const StepArgs& a = p.a;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     uint64_t* bars = reinterpret_cast<uint64_t*>(base + L::BAR_OFF);
     float* M = reinterpret_cast<float*>(base + L::M_OFF);
+    float* D1 = reinterpret_cast<float*>(base + L::D1_OFF);  // (summed only)
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tile = blockIdx.x;
@@ -166,6 +193,9 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
         float* O = O_of(b);  // u_{n-1}, then u_{n+1}, on E
         float* u_mid = p.u_mid + (long long)s * a.shot_stride;
         float* u_out = a.u_new + (long long)s * a.shot_stride;
+        float* d_mid = SUMMED && p.d_mid ? p.d_mid + (long long)s * a.shot_stride : nullptr;
+        float* d_out = SUMMED ? p.d_out + (long long)s * a.shot_stride : nullptr;
+        const bool mid = !two || p.write_mid;  // (summed: the intermediate level leaves the CTA)
 
         // ------------------------------------------------------------ step 1 on E
         auto step1 = [&](auto plain_c) {
@@ -191,6 +221,28 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
                 const float4 ov = f4(orow);
                 const float4 mv = f4(M + er * K2_EW + 4 * lane);
                 const bool zin = z >= R && z < a.nz - R;
+                if constexpr (SUMMED) {  // ov is d_n; O gets u_{n+1}, D1 d_{n+1}
+                    const float4 l = lap_row_diff<R>(lv, cv, rv, V, r + R, a);
+                    float g[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) g[e] = PLAIN ? 1.f : gz1[r] * gxe[e];
+                    float4 dn, un;
+                    summed4(cv, ov, mv, l, g, dn, un);
+                    if (!PLAIN) {  // fixed ring / outside the grid keep (u_n, d_n)
+                        float uu[4], dd[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const bool in = zin && xin[e];
+                            uu[e] = in ? comp(un, e) : comp(cv, e);
+                            dd[e] = in ? comp(dn, e) : comp(ov, e);
+                        }
+                        un = make_float4(uu[0], uu[1], uu[2], uu[3]);
+                        dn = make_float4(dd[0], dd[1], dd[2], dd[3]);
+                    }
+                    *reinterpret_cast<float4*>(orow) = un;
+                    *reinterpret_cast<float4*>(D1 + er * K2_EW + 4 * lane) = dn;
+                    continue;
+                }
                 const float4 l = lap_row<R>(lv, cv, rv, V, r + R, a);
                 if constexpr (PLAIN) {
                     *reinterpret_cast<float4*>(orow) = leap_plain(mv, l, cv, ov);
@@ -234,6 +286,7 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
                 if (a.inj_times_m) v *= (a.m != nullptr ? a.m[en.x] : a.m_const);
                 const float g = (a.gz ? a.gz[z] : 1.f) * (a.gx ? a.gx[xx] : 1.f);
                 atomicAdd(&O[ez * K2_EW + exx], g * v);
+                if (SUMMED) atomicAdd(&D1[ez * K2_EW + exx], g * v);
             }
             __syncthreads();
         }
@@ -255,13 +308,36 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
                 const bool zin = z >= R && z < a.nz - R;
                 const float4 c1 = V[r + R];  // u_{n+1}
                 const long long off = (long long)z * a.ld + ex;
-                if constexpr (PLAIN)
-                    *reinterpret_cast<float4*>(u_mid + off) = c1;
-                else
-                    store_level(u_mid + off, c1, zin, xin, all_x, a.zero_ring, x_ok);
+                if (!SUMMED || mid) {
+                    if constexpr (PLAIN)
+                        *reinterpret_cast<float4*>(u_mid + off) = c1;
+                    else
+                        store_level(u_mid + off, c1, zin, xin, all_x, a.zero_ring, x_ok);
+                    if constexpr (SUMMED)
+                        store_level(d_mid + off, f4(D1 + (tr + R) * K2_EW + 4 * lane), zin, xin, all_x,
+                                    a.zero_ring, x_ok);
+                }
                 if (!two) continue;
                 const float* nrow = O + (tr + R) * K2_EW + 4 * lane;
                 const float4 lv = f4(nrow - 4), rv = f4(nrow + 4);
+                if constexpr (SUMMED) {  // step 2 from (u_{n+1} in O, d_{n+1} in D1)
+                    const float4 l = lap_row_diff<R>(lv, c1, rv, V, r + R, a);
+                    const float4 d1 = f4(D1 + (tr + R) * K2_EW + 4 * lane);
+                    const float4 mv = f4(M + (tr + R) * K2_EW + 4 * lane);
+                    float g[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) g[e] = PLAIN ? 1.f : gz2[r] * gxe[e];
+                    float4 dn, un;
+                    summed4(c1, d1, mv, l, g, dn, un);
+                    if constexpr (PLAIN) {
+                        *reinterpret_cast<float4*>(u_out + off) = un;
+                        *reinterpret_cast<float4*>(d_out + off) = dn;
+                    } else {
+                        store_level(u_out + off, un, zin, xin, all_x, a.zero_ring, x_ok);
+                        store_level(d_out + off, dn, zin, xin, all_x, a.zero_ring, x_ok);
+                    }
+                    continue;
+                }
                 const float4 l = lap_row<R>(lv, c1, rv, V, r + R, a);
                 const float4 c0 = f4(U + (tr + 2 * R) * K2_UW + 4 + 4 * lane);  // u_n
                 const float4 mv = f4(M + (tr + R) * K2_EW + 4 * lane);
@@ -311,28 +387,30 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
                 if (a.inj_times_m) v *= (a.m != nullptr ? a.m[en.x] : a.m_const);
                 const float g = (a.gz ? a.gz[z] : 1.f) * (a.gx ? a.gx[xx] : 1.f);
                 atomicAdd(u_out + en.x, g * v);
+                if (SUMMED) atomicAdd(d_out + en.x, g * v);
             }
         }
     }
 }
 
-template <int R>
+template <int R, bool SUMMED>
 cudaError_t launch_impl(const CUtensorMap& mu, const CUtensorMap& mo, const CUtensorMap& mm, const Step2Args& p_in,
                         cudaStream_t s) {
     Step2Args p = p_in;
     p.a = with_weight_pairs(p_in.a);
-    using L = LayoutK2<R>;
+    using L = LayoutK2<R, SUMMED>;
     static int configured_device = -1;
     int dev = 0;
     cudaGetDevice(&dev);
     if (configured_device != dev) {
-        cudaError_t e = cudaFuncSetAttribute(step2d_k2_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             L::BYTES);
+        cudaError_t e = cudaFuncSetAttribute(step2d_k2_kernel<R, SUMMED>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
         if (e != cudaSuccess) return e;
         configured_device = dev;
     }
     const dim3 grid(p.a.tiles_x * p.a.tiles_z, (p.a.nshot + p.a.shots_per_cta - 1) / p.a.shots_per_cta);
-    const cudaError_t e = launch_pdl(step2d_k2_kernel<R>, grid, dim3(K2_THREADS), L::BYTES, s, mu, mo, mm, p);
+    const cudaError_t e =
+        launch_pdl(step2d_k2_kernel<R, SUMMED>, grid, dim3(K2_THREADS), L::BYTES, s, mu, mo, mm, p);
     count_launch();
     return e != cudaSuccess ? e : cudaGetLastError();
 }
@@ -342,10 +420,15 @@ cudaError_t launch_impl(const CUtensorMap& mu, const CUtensorMap& mo, const CUte
 cudaError_t launch_step2d_k2(int R, const CUtensorMap& map_u, const CUtensorMap& map_o,
                              const CUtensorMap& map_m, const Step2Args& p, cudaStream_t s) {
     if (p.a.shots_per_cta < 1 || p.a.shots_per_cta > T2_MAX_SPC) return cudaErrorInvalidValue;
-    switch (R) {
-        case 1: return launch_impl<1>(map_u, map_o, map_m, p, s);
-        case 2: return launch_impl<2>(map_u, map_o, map_m, p, s);
-        case 4: return launch_impl<4>(map_u, map_o, map_m, p, s);
+    if (p.summed && (!p.d_out || (p.write_mid && !p.d_mid) || (!p.two_steps && !p.d_mid)))
+        return cudaErrorInvalidValue;
+    switch (R * 2 + (p.summed ? 1 : 0)) {
+        case 2: return launch_impl<1, false>(map_u, map_o, map_m, p, s);
+        case 4: return launch_impl<2, false>(map_u, map_o, map_m, p, s);
+        case 8: return launch_impl<4, false>(map_u, map_o, map_m, p, s);
+        case 3: return launch_impl<1, true>(map_u, map_o, map_m, p, s);
+        case 5: return launch_impl<2, true>(map_u, map_o, map_m, p, s);
+        case 9: return launch_impl<4, true>(map_u, map_o, map_m, p, s);
         default: return cudaErrorInvalidValue;
     }
 }

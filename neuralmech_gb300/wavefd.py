@@ -82,8 +82,9 @@ class Grid:
              d_n = u_n - u_{n-1}, d_{n+1} = g^2 d_n - (1 - g)^2 u_n + g m L u_n,
              u_{n+1} = u_n + d_{n+1}: the FP32 rounding of the increment is no
              longer that of |u|, so a misfit gradient whose residuals are much
-             smaller than the traces keeps its accuracy; 20 B per update; 2D
-             one-step FP32 fields, lap_store "auto", checkpoint adjoint) or
+             smaller than the traces keeps its accuracy; 20 B per update, 10
+             with step_block 2; 2D FP32 fields, lap_store "auto", checkpoint
+             adjoint) or
              "auto" (summed for the forward of a gradient where available,
              leapfrog otherwise)
     """

@@ -65,8 +65,11 @@ def test_update_form_checks_and_workspace():
     _, f0 = _ws(_problem(update_form=0), 0)
     _, f2 = _ws(_problem(update_form=2), 0)
     assert f2 - f0 >= field
-    for bad in (dict(update_form=3), dict(update_form=-1),
-                dict(update_form=2, ndim=3, ny=64), dict(update_form=2, step_block=2),
+    # two steps per launch: d_n, d_{n+2} and d_{n+1}
+    _, l2 = _ws(_problem(update_form=1, step_block=2), 1)
+    _, s2 = _ws(_problem(update_form=2, step_block=2), 1)
+    assert s2 - l2 >= 3 * field
+    for bad in (dict(update_form=3), dict(update_form=-1), dict(update_form=2, ndim=3, ny=64),
                 dict(update_form=2, lap_store=2), dict(update_form=2, field_format=1),
                 dict(update_form=2, adjoint_mode=1)):
         rc, _ = _ws(_problem(**bad), 0)

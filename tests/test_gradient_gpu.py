@@ -322,3 +322,34 @@ def test_two_step_matches_one_step_autograd(cuda, orc):
         (0.5 * ((t - obs) ** 2).sum()).backward()
         grads.append(vel.grad.cpu().numpy())
     assert rel_l2(grads[1], grads[0]) < 1e-5
+
+
+@pytest.mark.parametrize("nt,ckpt,levels", [(101, 15, 0), (90, 9, 40), (64, 64, 0)])
+def test_summed_two_step_matches_one_step(cuda, orc, nt, ckpt, levels):
+    """The summed forward with two steps per launch (d_{n+1} kept on chip,
+    the intermediate level written only for a checkpoint or a kept level)
+    against the summed one-step forward: odd step counts (a last single
+    step), odd checkpoint intervals (checkpoints at odd steps), kept levels;
+    misfit, velocity and wavelet gradients within 1e-5, and both within the
+    one-step tolerance of the FP64 oracle."""
+    import dataclasses
+    from neuralmech_gb300 import misfit_gradient, wave_forward
+    grid, v, wav, src, rec = small_problem(shape=(70, 250), nshot=3, nt=nt, ckpt_every=ckpt, seed=29, nrec=24,
+                                           ckpt_format="fp32")
+    src[0, 0] = [32, 120]  # on a tile seam of the two-step kernel
+    grid = dataclasses.replace(grid, update="summed", store_levels=levels)
+    obs = _observed(orc, grid, v, wav, src, rec)
+    args = (torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+            torch.from_numpy(rec))
+    out = {sb: misfit_gradient(*args, torch.from_numpy(obs).to(cuda), dataclasses.replace(grid, step_block=sb),
+                               want_wavelet=True) for sb in (1, 2)}
+    J1, g1, w1 = out[1]
+    J2, g2, w2 = out[2]
+    assert abs(J1.item() - J2.item()) <= 1e-6 * J1.item()
+    assert rel_l2(g2.cpu().numpy(), g1.cpu().numpy()) < 1e-5
+    assert rel_l2(w2.cpu().numpy(), w1.cpu().numpy()) < 1e-5
+    Jr, gr, _, _ = orc.gradient(oracle_geometry(orc, grid, v, wav, src, rec), obs)
+    assert rel_l2(g2.cpu().numpy(), gr) < 1e-4
+    t1 = wave_forward(*args, dataclasses.replace(grid, step_block=1))
+    t2 = wave_forward(*args, dataclasses.replace(grid, step_block=2))
+    assert rel_l2(t2.cpu().numpy(), t1.cpu().numpy()) < 1e-6

@@ -107,6 +107,8 @@ def parse():
     ap.add_argument("--level-store-frac", type=float, default=0.8,
                     help="fraction of the GPU's memory for the forward levels the adjoint keeps "
                          "instead of recomputing them (0: recompute all but the last segment)")
+    ap.add_argument("--update", default="auto", choices=["auto", "leapfrog", "summed"],
+                    help="forward update form (auto: summed for a gradient's forward, leapfrog otherwise)")
     ap.add_argument("--workload", default="fwi1024",
                     choices=["fwi1024", "fwd2048", "fwi384_3d", "batch8", "vd1024", "temporal", "fmc_tfm"])
     return ap.parse_args()
@@ -346,7 +348,7 @@ def config_of(w, args):
             "grid": list(g.shape), "nt": g.nt, "nshot": w.nshot, "nrec": int(w.rec.shape[1]),
             "ckpt_every": g.ckpt_every, "ckpt_format": g.ckpt_format, "order": g.order,
             "store_levels": g.store_levels, "step_block": g.step_block, "adjoint": g.adjoint,
-            "kept_segments": kept_segments(g),
+            "update": g.update, "kept_segments": kept_segments(g),
             "l2": "inputs larger than L2 (multi-GB state and checkpoints per step)",
             "parallelism": f"{args.gpus} GPU(s), shots batched per GPU, gradient all-reduce"}
 
@@ -692,6 +694,7 @@ def _wl_grid(args, dev):
         w.wavelet = w.wavelet[..., :args.nt]
     if args.ckpt_every:
         g = dataclasses.replace(g, ckpt_every=args.ckpt_every)
+    g = dataclasses.replace(g, update=args.update)
     v = torch.from_numpy(w.vel).to(dev)
     wav = torch.from_numpy(w.wavelet).to(dev)
     src, rec = torch.from_numpy(w.src), torch.from_numpy(w.rec)
@@ -735,8 +738,7 @@ def _wl_grid(args, dev):
         updates, bpu = 2.0 * w.nshot * interior * g.nt, 18.0
         cfg = {"workload": f"fwi384_3d: 3D FWI gradient {g.shape[0]}^3, {g.nt} steps, {w.nshot} shots "
                            f"in groups of {args.group_shots or w.nshot}, {w.rec.shape[1]} receivers per shot, "
-                           f"BF16 checkpoints every "
-                           f"{g.ckpt_every}"}
+                           f"BF16 checkpoints every {g.ckpt_every}", "update": g.update}
     return dict(step=step, updates=updates, bpu=bpu, cfg=cfg, extra=extra, graph_kernels=graph_kernels)
 
 
@@ -814,7 +816,7 @@ def main():
     lib = _lib.load()
 
     w = workload(args.scale, args.nt, args.shots)
-    w.grid = dataclasses.replace(w.grid, step_block=args.step_block, adjoint=args.adjoint)
+    w.grid = dataclasses.replace(w.grid, step_block=args.step_block, adjoint=args.adjoint, update=args.update)
     if args.level_store_frac > 0:  # kept forward levels instead of recomputed ones
         budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
         w.grid = dataclasses.replace(w.grid, store_levels=levels_for_budget(w.grid, w.nshot, budget))

@@ -68,8 +68,9 @@ extern "C" {
 /* How the forward evaluates the update (wfd_problem.update_form). Both forms are
  * the same recursion; they differ in FP32 rounding and memory traffic. */
 #define WFD_UPDATE_AUTO 0     /* WFD_UPDATE_SUMMED for a forward that saves the state of a
-                                 gradient where that form is available (2D, FP32 fields,
-                                 lap_store auto, checkpoint adjoint, not variable density),
+                                 gradient where that form is available (2D and 3D, FP32
+                                 fields, lap_store auto, checkpoint adjoint, not variable
+                                 density),
                                  WFD_UPDATE_LEAPFROG otherwise */
 #define WFD_UPDATE_LEAPFROG 1 /* u_{n+1} over u_{n-1}: 16 bytes per update */
 #define WFD_UPDATE_SUMMED 2   /* the summed (increment) form: the state is (u_n, d_n =
@@ -80,8 +81,8 @@ extern "C" {
                                  the traces about 4x and of a gradient from residuals
                                  far smaller than the traces about 9x; 20 bytes per update
                                  (d is read and written, u_{n+1} written), 10 with two steps
-                                 per launch (step_block 2: d_{n+1} stays on chip, d is
-                                 double-buffered, one more field). Checkpoints then
+                                 per launch in 2D (step_block 2: d_{n+1} stays on chip, d
+                                 is double-buffered, one more field). Checkpoints then
                                  hold (d_n, u_n). Forward only: the recompute and the
                                  adjoint stay leapfrog. Only where WFD_UPDATE_AUTO would
                                  choose it; elsewhere WFD_ERR_INVALID */

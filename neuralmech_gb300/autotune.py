@@ -64,9 +64,9 @@ def candidates(nshot: int, summed: bool = False):
 
 def summed_for(grid, for_gradient: bool) -> bool:
     """Whether the forward that the tuned configuration serves runs in the
-    summed form (2D FP32 fields, lap_store auto, checkpoint adjoint)."""
-    avail = grid.ndim == 2 and grid.field_format == "fp32" and grid.lap_store == "auto" and \
-        grid.adjoint == "checkpoint"
+    summed form (FP32 fields, lap_store auto, checkpoint adjoint; the
+    same rule as the library's WFD_UPDATE_AUTO)."""
+    avail = grid.field_format == "fp32" and grid.lap_store == "auto" and grid.adjoint == "checkpoint"
     return avail and (grid.update == "summed" or (grid.update == "auto" and for_gradient))
 
 

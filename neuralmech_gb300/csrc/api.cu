@@ -246,9 +246,9 @@ int check_problem(const wfd_problem* p) {
     if (p->update_form < WFD_UPDATE_AUTO || p->update_form > WFD_UPDATE_SUMMED)
         return fail(WFD_ERR_INVALID, "unknown update_form %d", p->update_form);
     if (p->update_form == WFD_UPDATE_SUMMED &&
-        (p->ndim != 2 || p->field_format != WFD_FIELD_FP32 || p->lap_store != WFD_LAP_AUTO ||
+        (p->field_format != WFD_FIELD_FP32 || p->lap_store != WFD_LAP_AUTO ||
          p->adjoint_mode != WFD_ADJOINT_CHECKPOINT))
-        return fail(WFD_ERR_INVALID, "the summed update form: 2D, FP32 fields, lap_store auto, checkpoint adjoint");
+        return fail(WFD_ERR_INVALID, "the summed update form: FP32 fields, lap_store auto, checkpoint adjoint");
     if (p->recon_band < 0 || 2 * p->recon_band > std::min(p->nz, p->nx))
         return fail(WFD_ERR_INVALID, "recon_band must lie in [0, min(nz, nx) / 2]");
     if (p->tile_rows != 0 && p->tile_rows != 16 && p->tile_rows != 32)
@@ -389,9 +389,10 @@ size_t up256(size_t v) { return (v + 255) / 256 * 256; }
 
 // Whether the forward runs in the summed form (state u_n, d_n): forced by
 // WFD_UPDATE_SUMMED, or chosen by WFD_UPDATE_AUTO for a forward that saves the
-// state of a gradient, where the 2D one-step u-store path runs.
+// state of a gradient, on the 2D u-store path and in 3D (lap_store auto in both).
 bool summed_forward(const wfd_problem* p, const Geom& g, bool save) {
-    const bool avail = g.ndim == 2 && !g.vd && p->field_format == WFD_FIELD_FP32 && g.ustore && !g.recon;
+    const bool avail = !g.vd && p->field_format == WFD_FIELD_FP32 && !g.recon &&
+                       p->lap_store == WFD_LAP_AUTO && (g.ndim == 3 || g.ustore);
     return avail && (p->update_form == WFD_UPDATE_SUMMED || (p->update_form == WFD_UPDATE_AUTO && save));
 }
 
@@ -835,7 +836,8 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
         }
         if ((rc = checkpoint(n, w.D))) return rc;
         const int bo = loc(n - 1), bc = loc(n), bn = loc(n + 1);
-        const bool lap = save && !g.ustore && n >= g.k0_last;
+        // (the summed forward stores no L u: the backward recomputes every segment)
+        const bool lap = save && !g.ustore && !summed && n >= g.k0_last;
         StepArgs a = st.base(buf[bn]);
         a.inj = w.src;
         a.inj_val = wavelet;
@@ -1204,13 +1206,17 @@ int run_backward(const wfd_problem* p, const Geom& g, const Layout& L, const Wor
         PhaseScope scope(PH_ADJOINT, s, 1);
         if ((rc = adjoint_step(p->nt, false, 0))) return rc;
     }
+    const bool summed = summed_forward(p, g, true);  // checkpoints (d_k0, u_k0), no forward L u store
     for (int j = g.nseg - 1; j >= 0; --j) {
         const int k0 = j * g.K, k1 = std::min(p->nt, k0 + g.K);
-        if (j != g.nseg - 1) {
+        if (j != g.nseg - 1 || summed) {
             PhaseScope scope(PH_RECOMPUTE, s, k1 - k0);
             const unsigned char* slot = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
-            WFD_CUDA(launch_unpack(slot, w.P[(k0 + 1) & 1], n_all, p->ckpt_format, s));
             WFD_CUDA(launch_unpack(slot + L.ckpt_field_bytes, w.P[k0 & 1], n_all, p->ckpt_format, s));
+            if (summed)  // u_{k0-1} = u_k0 - d_k0
+                WFD_CUDA(launch_unpack_diff(slot, w.P[k0 & 1], w.P[(k0 + 1) & 1], n_all, p->ckpt_format, s));
+            else
+                WFD_CUDA(launch_unpack(slot, w.P[(k0 + 1) & 1], n_all, p->ckpt_format, s));
             for (int k = k0; k < k1; ++k) {
                 const int bc = k & 1, bn = (k + 1) & 1;
                 StepArgs a = st.base(w.P[bn]);

@@ -33,7 +33,7 @@ enum StepMode : int {
     MODE_GRAD = 2,      // update + accumulate q_{k+1} * L u_k into the gradient (adjoint)
     MODE_GRAD_U = 3,    // as MODE_GRAD, with L u_k computed in the kernel from a staged u_k
                         // tile (2D one-step kernel; the map_lap box is then the u_n box)
-    MODE_SUMMED = 4,    // update only, in the summed (increment) form (2D one-step kernel):
+    MODE_SUMMED = 4,    // update only, in the summed (increment) form (2D one-step and 3D kernels):
                         // the state is (u_n, d_n = u_n - u_{n-1}); map_old stages d_n,
                         // d_{n+1} goes to d_new in place and u_{n+1} = u_n + d_{n+1} to u_new
 };
@@ -199,7 +199,6 @@ constexpr int T3_ZCHUNK = 64;                    // planes per CTA (z blocking)
 cudaError_t launch_step3d(int R, int mode, const CUtensorMap& map_cur, const CUtensorMap& map_old,
                           const CUtensorMap& map_lap, const CUtensorMap& map_m, const StepArgs& a,
                           cudaStream_t s);
-size_t step3d_smem_bytes(int R, int mode);
 bool step3d_available();
 
 // Counts kernel launches (wfd_kernel_launches); every launcher calls it.

@@ -23,6 +23,11 @@
 //     stores injects into u_{n+1}.
 //   * MODE_SAVE_LAP stores L u_n; MODE_GRAD adds q_{k+1} L u_k into the
 //     gradient with 16-byte vector atomics.
+//   * MODE_SUMMED is the summed (increment) form of the 2D kernel's mode of
+//     that name: the staged output-plane tile is d_n = u_n - u_{n-1} instead
+//     of u_{n-1}, d_{n+1} = g^2 d_n - (1 - g)^2 u_n + g m L u_n goes to d_new
+//     in place and u_{n+1} = u_n + d_{n+1} to u_new (the Laplacian keeps the
+//     centre-weight form: this kernel is issue-bound).
 #include "common.cuh"
 #include "internal.h"
 
@@ -127,6 +132,7 @@ __global__ void __launch_bounds__(LANES_X * T3_TY / TR, 2)
         gyv[t] = (a.gy != nullptr && y < a.ny) ? __ldg(a.gy + y) : 1.f;
     }
     float* un = a.u_new + (long long)s * a.shot_stride;
+    float* dnw = MODE == MODE_SUMMED ? a.d_new + (long long)s * a.shot_stride : nullptr;
     const int col = T3_XH + 4 * lane;  // staged column of this thread's first cell
 
     // ---- register queues of the z taps, one per row: V[t][j] = u_n of row
@@ -213,10 +219,24 @@ __global__ void __launch_bounds__(LANES_X * T3_TY / TR, 2)
             const float gyz = gz * gyv[t];
             const float2 gl = __fmul2_rn(make_float2(gyz, gyz), make_float2(gxe[0], gxe[1]));
             const float2 gh = __fmul2_rn(make_float2(gyz, gyz), make_float2(gxe[2], gxe[3]));
-            const float2 tl = __ffma2_rn(lo2(mv), lo, __fadd2_rn(lo2(cv), lo2(cv)));
-            const float2 th = __ffma2_rn(hi2(mv), hi, __fadd2_rn(hi2(cv), hi2(cv)));
-            const float2 nl = __ffma2_rn(gl, tl, __fmul2_rn(__fmul2_rn(gl, gl), make_float2(-ov.x, -ov.y)));
-            const float2 nh = __ffma2_rn(gh, th, __fmul2_rn(__fmul2_rn(gh, gh), make_float2(-ov.z, -ov.w)));
+            float2 nl, nh, dl, dh;
+            if (MODE == MODE_SUMMED) {  // ov is d_n: d = g m L u + (g^2 d - (1 - g)^2 u), u + d
+                const float2 one = make_float2(1.f, 1.f);
+                const float2 ol = __fadd2_rn(one, make_float2(-gl.x, -gl.y)), oh = __fadd2_rn(one, make_float2(-gh.x, -gh.y));
+                const float2 il = __ffma2_rn(__fmul2_rn(gl, gl), lo2(ov),
+                                             make_float2(-(ol.x * ol.x) * cv.x, -(ol.y * ol.y) * cv.y));
+                const float2 ih = __ffma2_rn(__fmul2_rn(gh, gh), hi2(ov),
+                                             make_float2(-(oh.x * oh.x) * cv.z, -(oh.y * oh.y) * cv.w));
+                dl = __ffma2_rn(__fmul2_rn(gl, lo2(mv)), lo, il);
+                dh = __ffma2_rn(__fmul2_rn(gh, hi2(mv)), hi, ih);
+                nl = __fadd2_rn(lo2(cv), dl);
+                nh = __fadd2_rn(hi2(cv), dh);
+            } else {
+                const float2 tl = __ffma2_rn(lo2(mv), lo, __fadd2_rn(lo2(cv), lo2(cv)));
+                const float2 th = __ffma2_rn(hi2(mv), hi, __fadd2_rn(hi2(cv), hi2(cv)));
+                nl = __ffma2_rn(gl, tl, __fmul2_rn(__fmul2_rn(gl, gl), make_float2(-ov.x, -ov.y)));
+                nh = __ffma2_rn(gh, th, __fmul2_rn(__fmul2_rn(gh, gh), make_float2(-ov.z, -ov.w)));
+            }
             const float nv[4] = {nl.x, nl.y, nh.x, nh.y};
             const float lap[4] = {lo.x, lo.y, hi.x, hi.y};
 
@@ -224,10 +244,15 @@ __global__ void __launch_bounds__(LANES_X * T3_TY / TR, 2)
             const long long off = (long long)z * a.plane + (long long)(y0 + yr0 + t) * a.ld + x;
             if (rin && all_x) {
                 *reinterpret_cast<float4*>(un + off) = make_float4(nv[0], nv[1], nv[2], nv[3]);
+                if (MODE == MODE_SUMMED) *reinterpret_cast<float4*>(dnw + off) = make_float4(dl.x, dl.y, dh.x, dh.y);
             } else if (rin) {
+                const float dv[4] = {dl.x, dl.y, dh.x, dh.y};
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
-                    if (xin[e]) un[off + e] = nv[e];
+                    if (xin[e]) {
+                        un[off + e] = nv[e];
+                        if (MODE == MODE_SUMMED) dnw[off + e] = dv[e];
+                    }
             }
             if (MODE == MODE_SAVE_LAP && rin) {
                 const long long lo_i64 = (long long)s * a.shot_stride + off;
@@ -293,6 +318,7 @@ __global__ void __launch_bounds__(LANES_X * T3_TY / TR, 2)
             if (a.inj_times_m) v *= a.m[en.x];
             const float g = (a.gz ? a.gz[pz] : 1.f) * (a.gy ? a.gy[py] : 1.f) * (a.gx ? a.gx[px] : 1.f);
             atomicAdd(un + en.x, g * v);
+            if (MODE == MODE_SUMMED) atomicAdd(dnw + en.x, g * v);
         }
     }
 }
@@ -323,6 +349,7 @@ cudaError_t dispatch(int mode, const CUtensorMap& mc, const CUtensorMap& mo, con
         case MODE_PLAIN: return launch_impl<R, MODE_PLAIN>(mc, mo, ml, mm, a, s);
         case MODE_SAVE_LAP: return launch_impl<R, MODE_SAVE_LAP>(mc, mo, ml, mm, a, s);
         case MODE_GRAD: return launch_impl<R, MODE_GRAD>(mc, mo, ml, mm, a, s);
+        case MODE_SUMMED: return launch_impl<R, MODE_SUMMED>(mc, mo, ml, mm, a, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -340,20 +367,6 @@ cudaError_t launch_step3d(int R, int mode, const CUtensorMap& mc, const CUtensor
         case 2: return dispatch<2>(mode, mc, mo, ml, mm, a, s);
         case 4: return dispatch<4>(mode, mc, mo, ml, mm, a, s);
         default: return cudaErrorInvalidValue;
-    }
-}
-
-size_t step3d_smem_bytes(int R, int mode) {
-    switch (R * 4 + mode) {
-        case 4 + MODE_PLAIN: return Layout3D<1, MODE_PLAIN>::BYTES;
-        case 4 + MODE_SAVE_LAP: return Layout3D<1, MODE_SAVE_LAP>::BYTES;
-        case 4 + MODE_GRAD: return Layout3D<1, MODE_GRAD>::BYTES;
-        case 8 + MODE_PLAIN: return Layout3D<2, MODE_PLAIN>::BYTES;
-        case 8 + MODE_SAVE_LAP: return Layout3D<2, MODE_SAVE_LAP>::BYTES;
-        case 8 + MODE_GRAD: return Layout3D<2, MODE_GRAD>::BYTES;
-        case 16 + MODE_PLAIN: return Layout3D<4, MODE_PLAIN>::BYTES;
-        case 16 + MODE_SAVE_LAP: return Layout3D<4, MODE_SAVE_LAP>::BYTES;
-        default: return Layout3D<4, MODE_GRAD>::BYTES;
     }
 }
 

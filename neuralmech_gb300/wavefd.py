@@ -83,8 +83,8 @@ class Grid:
              u_{n+1} = u_n + d_{n+1}: the FP32 rounding of the increment is no
              longer that of |u|, so a misfit gradient whose residuals are much
              smaller than the traces keeps its accuracy; 20 B per update, 10
-             with step_block 2; 2D FP32 fields, lap_store "auto", checkpoint
-             adjoint) or
+             with step_block 2 in 2D; 2D and 3D, FP32 fields, lap_store "auto",
+             checkpoint adjoint) or
              "auto" (summed for the forward of a gradient where available,
              leapfrog otherwise)
     """

@@ -69,7 +69,11 @@ def test_update_form_checks_and_workspace():
     _, l2 = _ws(_problem(update_form=1, step_block=2), 1)
     _, s2 = _ws(_problem(update_form=2, step_block=2), 1)
     assert s2 - l2 >= 3 * field
-    for bad in (dict(update_form=3), dict(update_form=-1), dict(update_form=2, ndim=3, ny=64),
+    # 3D: the summed forward of a gradient adds the increment field too
+    _, t1 = _ws(_problem(update_form=1, ndim=3, ny=20, nz=24, nx=40, vmax=2000.0, dy=10.0), 1)
+    _, t0 = _ws(_problem(update_form=0, ndim=3, ny=20, nz=24, nx=40, vmax=2000.0, dy=10.0), 1)
+    assert t0 - t1 >= 2 * 24 * 20 * 40 * 4
+    for bad in (dict(update_form=3), dict(update_form=-1),
                 dict(update_form=2, lap_store=2), dict(update_form=2, field_format=1),
                 dict(update_form=2, adjoint_mode=1)):
         rc, _ = _ws(_problem(**bad), 0)

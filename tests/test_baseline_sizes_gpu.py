@@ -9,9 +9,11 @@
     checkpoints (every shot's segments but the last recomputed): the errors
     are stated (printed) and bounded by 1e-3, the bound of the 2D gradient;
   * fwi384_3d: the full 384^3 grid and 1500 steps, one shot with its 64 x 64
-    receivers, checkpoints every 39 in BF16 and in FP32 (3D has the leapfrog
-    update only): traces within 1e-5, the gradient errors stated, and bounded
-    by 1e-2 beyond 6 cells of the source. At the source cell the imaging sum
+    receivers, checkpoints every 39 in BF16 and in FP32, the gradient's
+    forward in the summed form (the default): traces within 1e-5, the
+    gradient errors stated, and bounded beyond 6 cells of the source by 5e-3
+    (BF16) and 1e-3 (FP32; measured 2.1e-3 and 6.0e-4, against 7.1e-3 and
+    1.3e-3 with the leapfrog forward). At the source cell the imaging sum
     q L u meets the point source's singular L u: there the FP32 sum over the
     steps keeps an absolute error (about 2e-8 on 192^3 whatever the residual)
     that dominates when the residual, and with it the gradient, is small, as
@@ -114,5 +116,4 @@ def test_fwi384_3d_full_grid(cuda, orc):
           f"residual / traces {res:.2e}, gradient rel L2 vs FP64 {errs}; beyond 6 cells of the source "
           f"{errs_far} (the source's neighbourhood holds {share:.2e} of the gradient's norm)")
     assert e_tr < 1e-5
-    for fmt, e in errs_far.items():
-        assert e <= 1e-2, fmt
+    assert errs_far["bf16"] <= 5e-3 and errs_far["fp32"] <= 1e-3, errs_far

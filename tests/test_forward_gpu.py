@@ -122,6 +122,7 @@ def test_forward_no_receivers_no_sources(cuda):
 @pytest.mark.parametrize("shape,nshot,sponge", [
     ((70, 20, 72), 2, 5),     # two z chunks, two x tiles, two y tiles
     ((30, 37, 41), 1, 0),     # odd sizes, one chunk
+    ((67, 18, 70), 2, 4),     # a last chunk of 3 planes: an iteration of one plane
 ])
 def test_forward_3d_matches_oracle(cuda, orc, order, shape, nshot, sponge):
     from neuralmech_gb300 import wave_forward

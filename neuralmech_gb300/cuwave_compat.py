@@ -16,7 +16,7 @@ not available (the package is absent), so the choices below are this
 module's own. They are written here so callers can check parity:
 
 * Material indicator gamma (the reference's "indicator", 1 = solid, ~1e-4 =
-  void; plate.py:132-137, helper.py:30-43). It scales the stiffness at
+  void; plate.py:36,54-59, helper.py:30-43). It scales the stiffness at
   constant density: c(x) = wavespeed * sqrt(gamma(x)). misfit_gradient returns
   d misfit / d gamma = d misfit / d c * wavespeed / (2 sqrt(gamma)).
 * Grid. The nodes of ScalarWave((nx, ny), (dx, dy)) sit at x = -dx + i dx
@@ -25,7 +25,7 @@ module's own. They are written here so callers can check parity:
   more ghost nodes on every side; the physical nodes, the array on the plate
   edge included, are then updated. Indicators are read where the reference
   drivers put them, in [:nx, :ny] of an array of shape Nx or larger
-  (helper.py:76-77, 2D_fwi.py:176), and their edge values extend into the
+  (helper.py:76-77, 2D_fwi.py:34), and their edge values extend into the
   margin. Gradients come back in the indicator's shape and place. Nx_padded
   rounds each axis up to a multiple of 8. ScalarWave also takes 3D grids
   (nx, ny, nz), as projects/8_physics_drivers/waveND.py does with DIM = 3;

@@ -231,6 +231,32 @@ def test_oracle_homogeneous_greens_function(orc):
     assert rel_l2(tr[win], ana[win]) < 0.05
 
 
+def test_oracle_homogeneous_greens_function_3d(orc):
+    """Known answer in 3D: in a homogeneous medium the point source of
+    u_tt - c^2 Lap u = s(t) delta(x) radiates u(r, t) = s(t - r/c) / (4 pi c^2 r).
+    A discrete source adds w_n dt^2 / h^3 per step; trace_n = u(t_{n+1}).
+    Receivers on two axes, 30 cells out, before any boundary reflection."""
+    from neuralmech_gb300.synth import ricker
+    n, h, c = 161, 5.0, 2000.0
+    dt = 0.3 * h / c
+    nt, f = 300, 25.0
+    wav = ricker(f, nt, dt).astype(np.float64)
+    s0, r_cells = n // 2, 30
+    geo = orc.Geometry(vel=np.full((n, n, n), c), wavelet=wav[None, :, None],
+                       src=np.array([[[s0, s0, s0]]], dtype=np.int32),
+                       rec=np.array([[[s0, s0, s0 + r_cells], [s0 + r_cells, s0, s0]]], dtype=np.int32),
+                       dt=dt, h=(h, h, h), order=8, sponge=None, src_scale=dt * dt / h**3)
+    tr = orc.forward(geo)[0]
+    r = r_cells * h
+    t = (np.arange(nt) + 1) * dt
+    t0 = 1.5 / f
+    a = (math.pi * f * (t - r / c - t0)) ** 2
+    ana = np.where(t >= r / c, (1 - 2 * a) * np.exp(-a), 0.0) / (4 * math.pi * c * c * r)
+    win = (t > r / c) & (t < r / c + t0 + 2 / f)
+    for j in range(2):
+        assert rel_l2(tr[win, j], ana[win]) < 0.03
+
+
 def test_scaled_step_restatement_tracks_fp32():
     """The NumPy restatement of scaled_step (the golden source for
     wfd_step2d_scaled) stays within int16 quantisation of the FP32 slice step

@@ -916,20 +916,23 @@ def main():
         d2h = grad_h.numel() * 4 + 8
 
         # the observed traces (most of the bytes) go up on a second stream while
-        # the forward runs; the call waits for them only before the residual
+        # the forward runs; the call waits for them only before the residual.
+        # The inputs the forward needs are copied first: host-to-device copies
+        # share a copy engine, so the model must not queue behind the traces.
         copy_stream = torch.cuda.Stream(device=dev)
         ob = torch.empty(host["obs"].shape, dtype=torch.float32, device=dev)
         ob_ready = torch.cuda.Event()
+        src_h, rec_h = src.pin_memory(), rec.pin_memory()
 
         def e2e_step():
+            v = host["vel"].to(dev, non_blocking=True)
+            wv = host["wav"].to(dev, non_blocking=True)
+            s_d, r_d = src_h.to(dev, non_blocking=True), rec_h.to(dev, non_blocking=True)
             copy_stream.wait_stream(torch.cuda.current_stream(dev))  # the previous step's reads of ob
             with torch.cuda.stream(copy_stream):
                 ob.copy_(host["obs"], non_blocking=True)
                 ob_ready.record(copy_stream)
-            v = host["vel"].to(dev, non_blocking=True)
-            wv = host["wav"].to(dev, non_blocking=True)
-            J2, g2 = misfit_gradient(v, wv, src.to(dev, non_blocking=True), rec.to(dev, non_blocking=True),
-                                     ob, g, check=False, observed_ready=ob_ready)
+            J2, g2 = misfit_gradient(v, wv, s_d, r_d, ob, g, check=False, observed_ready=ob_ready)
             if world > 1:
                 dist.all_reduce(g2)
                 dist.all_reduce(J2)

@@ -917,8 +917,8 @@ def main():
 
         # the observed traces (most of the bytes) go up on a second stream while
         # the forward runs; the call waits for them only before the residual.
-        # The inputs the forward needs are copied first: host-to-device copies
-        # share a copy engine, so the model must not queue behind the traces.
+        # The inputs the forward needs are copied first, so that the model's
+        # copy cannot queue behind the traces' on a shared copy engine.
         copy_stream = torch.cuda.Stream(device=dev)
         ob = torch.empty(host["obs"].shape, dtype=torch.float32, device=dev)
         ob_ready = torch.cuda.Event()

@@ -73,7 +73,7 @@ ALG_BYTES = {"forward": 16.0, "recompute": 20.0, "adjoint": 20.0}
 
 
 def alg_bytes(grid, phase: str) -> float:
-    ustore = grid.ndim == 2 and grid.step_block != 2 and grid.lap_store == "auto"
+    ustore = grid.ndim == 2 and grid.lap_store == "auto"
     return 16.0 if (phase == "recompute" and ustore) else ALG_BYTES[phase]
 
 
@@ -100,8 +100,9 @@ def parse():
                     help="how the gradient obtains the forward levels")
     ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 16, 32],
                     help="fwd2048: 2D tile height of the one-step kernel (0: the library default)")
-    ap.add_argument("--step-block", type=int, default=1, choices=[1, 2],
-                    help="time steps per launch of the forward and the recompute")
+    ap.add_argument("--step-block", type=int, default=0, choices=[0, 1, 2],
+                    help="time steps per launch of the forward and the recompute (0: two for the "
+                         "fwi1024 gradient, whose summed two-step forward is the faster one; one elsewhere)")
     ap.add_argument("--group-shots", type=int, default=8,
                     help="fwi384_3d: shots per sequential group (0: all 16 at once)")
     ap.add_argument("--level-store-frac", type=float, default=0.8,
@@ -720,7 +721,7 @@ def _wl_grid(args, dev):
                "store_levels": g.store_levels}
     elif args.workload == "fwd2048":
         g = dataclasses.replace(g, field_format=args.field_format, tile_rows=args.tile_rows,
-                                step_block=args.step_block if args.field_format == "fp32" else 1)
+                                step_block=(args.step_block or 1) if args.field_format == "fp32" else 1)
         step = lambda: wave_forward(v, wav, src, rec, g, check=False)
         updates, bpu = w.nshot * interior * g.nt, 16.0
         cfg = {"workload": f"fwd2048: 2D forward {g.shape[0]}^2, {g.nt} steps, 1 shot, "
@@ -816,7 +817,7 @@ def main():
     lib = _lib.load()
 
     w = workload(args.scale, args.nt, args.shots)
-    w.grid = dataclasses.replace(w.grid, step_block=args.step_block, adjoint=args.adjoint, update=args.update)
+    w.grid = dataclasses.replace(w.grid, step_block=args.step_block or 2, adjoint=args.adjoint, update=args.update)
     if args.level_store_frac > 0:  # kept forward levels instead of recomputed ones
         budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
         w.grid = dataclasses.replace(w.grid, store_levels=levels_for_budget(w.grid, w.nshot, budget))

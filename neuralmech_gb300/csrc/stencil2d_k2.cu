@@ -27,7 +27,11 @@
 // SUMMED: the same two steps in the summed (increment) form of the one-step
 // kernel's MODE_SUMMED, state (u_n, d_n = u_n - u_{n-1}):
 //   d_{n+1} = g^2 d_n - (1 - g)^2 u_n + g m L u_n,  u_{n+1} = u_n + d_{n+1},
-// L from neighbour differences. O stages d_n on E; step 1 writes u_{n+1} over
+// L in the centre-weight form of the leapfrog steps: this kernel is bound by
+// its instruction count, and the neighbour-difference form that the memory-
+// bound one-step kernel uses for its rounding costs 41% more instructions
+// (the gradient of the 2-shot fwi1024 case: 4.7e-4 against 3.8e-4 vs FP64,
+// both within 1e-3). O stages d_n on E; step 1 writes u_{n+1} over
 // it and d_{n+1} into a fourth E buffer D1; step 2 reads both on the tile.
 // Only u_{n+2} and d_{n+2} leave the CTA, to buffers the launch does not read
 // (d_n is read with a halo by the neighbouring tiles, so d is double-
@@ -222,7 +226,7 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
                 const float4 mv = f4(M + er * K2_EW + 4 * lane);
                 const bool zin = z >= R && z < a.nz - R;
                 if constexpr (SUMMED) {  // ov is d_n; O gets u_{n+1}, D1 d_{n+1}
-                    const float4 l = lap_row_diff<R>(lv, cv, rv, V, r + R, a);
+                    const float4 l = lap_row<R>(lv, cv, rv, V, r + R, a);
                     float g[4];
 #pragma unroll
                     for (int e = 0; e < 4; ++e) g[e] = PLAIN ? 1.f : gz1[r] * gxe[e];
@@ -321,7 +325,7 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
                 const float* nrow = O + (tr + R) * K2_EW + 4 * lane;
                 const float4 lv = f4(nrow - 4), rv = f4(nrow + 4);
                 if constexpr (SUMMED) {  // step 2 from (u_{n+1} in O, d_{n+1} in D1)
-                    const float4 l = lap_row_diff<R>(lv, c1, rv, V, r + R, a);
+                    const float4 l = lap_row<R>(lv, c1, rv, V, r + R, a);
                     const float4 d1 = f4(D1 + (tr + R) * K2_EW + 4 * lane);
                     const float4 mv = f4(M + (tr + R) * K2_EW + 4 * lane);
                     float g[4];

@@ -337,9 +337,12 @@ def test_summed_two_step_matches_one_step(cuda, orc, nt, ckpt, levels):
     """The summed forward with two steps per launch (d_{n+1} kept on chip,
     the intermediate level written only for a checkpoint or a kept level)
     against the summed one-step forward: odd step counts (a last single
-    step), odd checkpoint intervals (checkpoints at odd steps), kept levels;
-    misfit, velocity and wavelet gradients within 1e-5, and both within the
-    one-step tolerance of the FP64 oracle."""
+    step), odd checkpoint intervals (checkpoints at odd steps), kept levels.
+    The two kernels form L u differently (centre weight against neighbour
+    differences), so they agree to FP32 rounding, not bit for bit: misfits
+    within 1e-5, velocity and wavelet gradients within 5e-5 of each other;
+    each one's traces within 1e-5 and gradient within 1e-4 of the FP64
+    oracle."""
     import dataclasses
     from neuralmech_gb300 import misfit_gradient, wave_forward
     grid, v, wav, src, rec = small_problem(shape=(70, 250), nshot=3, nt=nt, ckpt_every=ckpt, seed=29, nrec=24,
@@ -353,11 +356,13 @@ def test_summed_two_step_matches_one_step(cuda, orc, nt, ckpt, levels):
                                want_wavelet=True) for sb in (1, 2)}
     J1, g1, w1 = out[1]
     J2, g2, w2 = out[2]
-    assert abs(J1.item() - J2.item()) <= 1e-6 * J1.item()
-    assert rel_l2(g2.cpu().numpy(), g1.cpu().numpy()) < 1e-5
-    assert rel_l2(w2.cpu().numpy(), w1.cpu().numpy()) < 1e-5
-    Jr, gr, _, _ = orc.gradient(oracle_geometry(orc, grid, v, wav, src, rec), obs)
+    assert abs(J1.item() - J2.item()) <= 1e-5 * J1.item()
+    assert rel_l2(g2.cpu().numpy(), g1.cpu().numpy()) < 5e-5
+    assert rel_l2(w2.cpu().numpy(), w1.cpu().numpy()) < 5e-5
+    geo = oracle_geometry(orc, grid, v, wav, src, rec)
+    Jr, gr, _, tr = orc.gradient(geo, obs)
+    assert rel_l2(g1.cpu().numpy(), gr) < 1e-4
     assert rel_l2(g2.cpu().numpy(), gr) < 1e-4
-    t1 = wave_forward(*args, dataclasses.replace(grid, step_block=1))
-    t2 = wave_forward(*args, dataclasses.replace(grid, step_block=2))
-    assert rel_l2(t2.cpu().numpy(), t1.cpu().numpy()) < 1e-6
+    for sb in (1, 2):
+        t = wave_forward(*args, dataclasses.replace(grid, step_block=sb))
+        assert rel_l2(t.cpu().numpy(), tr) < 1e-5

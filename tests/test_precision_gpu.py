@@ -15,6 +15,8 @@ two of its 64 shots, against the FP64 oracle.
   d_n, the default for the forward of a gradient) keeps the increment's own
   rounding and meets it, with FP32, BF16 and int16 checkpoints alike: every
   segment but the last is recomputed from a checkpoint here (store_levels 0).
+  The benchmark's configuration, two steps per launch (whose summed kernel
+  forms L u in the centre-weight form), meets it too (4.7e-4).
 """
 import dataclasses
 
@@ -46,16 +48,18 @@ def test_fwi1024_two_shots_against_fp64(cuda, orc):
         tr = wave_forward(*args, dataclasses.replace(g, update=form)).cpu().numpy()
         e_tr[form] = rel_l2(tr, tr_ref)
     errs, e_J = {}, {}
-    for form, fmt in (("auto", "fp32"), ("auto", "i16"), ("auto", "bf16"), ("leapfrog", "bf16")):
+    for form, fmt, sb in (("auto", "fp32", 1), ("auto", "i16", 1), ("auto", "bf16", 1), ("auto", "bf16", 2),
+                          ("leapfrog", "bf16", 1)):
         J, gv = misfit_gradient(*args, torch.from_numpy(obs).to(cuda),
-                                dataclasses.replace(g, ckpt_format=fmt, update=form))
-        errs[(form, fmt)] = rel_l2(gv.cpu().numpy(), gr)
-        e_J[(form, fmt)] = abs(float(J) - Jr) / Jr
+                                dataclasses.replace(g, ckpt_format=fmt, update=form, step_block=sb))
+        key = (form, fmt) if sb == 1 else (form, fmt, "two steps per launch")
+        errs[key] = rel_l2(gv.cpu().numpy(), gr)
+        e_J[key] = abs(float(J) - Jr) / Jr
     print(f"fwi1024 (2 shots): traces rel L2 {e_tr}; gradient rel L2 {errs}; misfit rel {e_J}")
     assert e_tr["leapfrog"] < 1e-5 and e_tr["summed"] < 1e-5
     assert e_tr["summed"] < 0.5 * e_tr["leapfrog"]
-    for fmt in ("fp32", "i16", "bf16"):
-        assert errs[("auto", fmt)] <= 1e-3, fmt
-        assert e_J[("auto", fmt)] <= 5e-3, fmt
+    for key in (("auto", "fp32"), ("auto", "i16"), ("auto", "bf16"), ("auto", "bf16", "two steps per launch")):
+        assert errs[key] <= 1e-3, key
+        assert e_J[key] <= 5e-3, key
     # the leapfrog form's floor: the documented miss of the 1e-3 bound
     assert 1e-3 < errs[("leapfrog", "bf16")] < 1e-2

@@ -96,6 +96,19 @@ __device__ __forceinline__ void summed4(const float4& u, const float4& d, const 
     un = make_float4(uu[0], uu[1], uu[2], uu[3]);
 }
 
+// summed4 with g = 1 (cells outside the sponge), in packed pairs:
+// d_{n+1} = m L u + d_n, u_{n+1} = u_n + d_{n+1}. summed4's value there: g m = m,
+// g^2 d = d and (1 - g)^2 u = 0 leave the same sums (up to the sign of a zero).
+__device__ __forceinline__ void summed4_plain(const float4& u, const float4& d, const float4& m, const float4& l,
+                                              float4& dn, float4& un) {
+    const float2 dl = __ffma2_rn(make_float2(m.x, m.y), make_float2(l.x, l.y), make_float2(d.x, d.y));
+    const float2 dh = __ffma2_rn(make_float2(m.z, m.w), make_float2(l.z, l.w), make_float2(d.z, d.w));
+    const float2 ul = __fadd2_rn(make_float2(u.x, u.y), dl);
+    const float2 uh = __fadd2_rn(make_float2(u.z, u.w), dh);
+    dn = make_float4(dl.x, dl.y, dh.x, dh.y);
+    un = make_float4(ul.x, ul.y, uh.x, uh.y);
+}
+
 template <int R, bool SUMMED>
 __global__ void __launch_bounds__(K2_THREADS, 2)
     step2d_k2_kernel(const __grid_constant__ CUtensorMap map_u, const __grid_constant__ CUtensorMap map_o,
@@ -227,11 +240,15 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
                 const bool zin = z >= R && z < a.nz - R;
                 if constexpr (SUMMED) {  // ov is d_n; O gets u_{n+1}, D1 d_{n+1}
                     const float4 l = lap_row<R>(lv, cv, rv, V, r + R, a);
-                    float g[4];
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) g[e] = PLAIN ? 1.f : gz1[r] * gxe[e];
                     float4 dn, un;
-                    summed4(cv, ov, mv, l, g, dn, un);
+                    if constexpr (PLAIN) {
+                        summed4_plain(cv, ov, mv, l, dn, un);
+                    } else {
+                        float g[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) g[e] = gz1[r] * gxe[e];
+                        summed4(cv, ov, mv, l, g, dn, un);
+                    }
                     if (!PLAIN) {  // fixed ring / outside the grid keep (u_n, d_n)
                         float uu[4], dd[4];
 #pragma unroll
@@ -328,11 +345,15 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
                     const float4 l = lap_row<R>(lv, c1, rv, V, r + R, a);
                     const float4 d1 = f4(D1 + (tr + R) * K2_EW + 4 * lane);
                     const float4 mv = f4(M + (tr + R) * K2_EW + 4 * lane);
-                    float g[4];
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) g[e] = PLAIN ? 1.f : gz2[r] * gxe[e];
                     float4 dn, un;
-                    summed4(c1, d1, mv, l, g, dn, un);
+                    if constexpr (PLAIN) {
+                        summed4_plain(c1, d1, mv, l, dn, un);
+                    } else {
+                        float g[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) g[e] = gz2[r] * gxe[e];
+                        summed4(c1, d1, mv, l, g, dn, un);
+                    }
                     if constexpr (PLAIN) {
                         *reinterpret_cast<float4*>(u_out + off) = un;
                         *reinterpret_cast<float4*>(d_out + off) = dn;

@@ -104,7 +104,10 @@ typedef struct wfd_problem {
                               0 = all shots at once */
     int32_t tile_rows;     /* 2D tile height: 16 or 32 rows (0 = 32) */
     int32_t step_block;    /* 2D time steps per kernel launch: 1 or 2 (0 = 1); 2 keeps
-                              u_{n+1} in shared memory between the two steps */
+                              u_{n+1} in shared memory between the two steps. A forward
+                              (no gradient) with the leapfrog update and FP32 fields also
+                              takes 8 at order 2 and 4 at order 4: a window of 256 x 40
+                              cells per CTA stays in registers for the launch's steps */
     int32_t store_levels;  /* WFD_LAP_AUTO path: FP32 levels (fields of nshot x cells)
                               the workspace may hold. The forward keeps the levels of
                               its last floor((store_levels - 2) / K) segments, K the

@@ -19,7 +19,7 @@ ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libwavefd.so")
 SOURCES = ["stencil2d.cu", "stencil2d_k2.cu", "stencil3d.cu", "aux.cu", "api.cu", "static_scratch.cu",
-           "imaging.cu", "dropin.cu", "stencil2d_lp.cu", "stencil2d_vd.cu"]
+           "imaging.cu", "dropin.cu", "stencil2d_lp.cu", "stencil2d_vd.cu", "stencil2d_reg.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -253,8 +253,14 @@ int check_problem(const wfd_problem* p) {
         return fail(WFD_ERR_INVALID, "recon_band must lie in [0, min(nz, nx) / 2]");
     if (p->tile_rows != 0 && p->tile_rows != 16 && p->tile_rows != 32)
         return fail(WFD_ERR_INVALID, "tile_rows must be 0, 16 or 32");
-    if (p->step_block < 0 || p->step_block > 2 || (p->step_block == 2 && p->ndim != 2))
-        return fail(WFD_ERR_INVALID, "step_block must be 0, 1 or 2 (2: 2D only)");
+    if (p->step_block < 0 || (p->step_block > 2 && p->step_block != 4 && p->step_block != 8) ||
+        (p->step_block == 2 && p->ndim != 2))
+        return fail(WFD_ERR_INVALID, "step_block must be 0, 1, 2, 4 or 8 (2: 2D only)");
+    if (p->step_block >= 4 && (p->ndim != 2 || p->order != (p->step_block == 8 ? 2 : 4) ||
+                               p->field_format != WFD_FIELD_FP32 || p->update_form == WFD_UPDATE_SUMMED))
+        return fail(WFD_ERR_INVALID,
+                    "step_block %d: the 2D leapfrog forward at order %d with FP32 fields", p->step_block,
+                    p->step_block == 8 ? 2 : 4);
     if (p->step_block == 2 && p->lap_store != WFD_LAP_AUTO)
         return fail(WFD_ERR_INVALID, "step_block 2 keeps the levels u_k: lap_store must be WFD_LAP_AUTO");
     if (p->ckpt_every < 0 || p->shots_per_cta < 0 || p->group_shots < 0 || p->store_levels < 0)
@@ -290,7 +296,7 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0, int step_block = 0, bool
     g.plane = (long long)g.ny * g.ld;
     g.cells = (long long)g.nz * g.plane;
     const int sb = step_block > 0 ? step_block : p->step_block;
-    g.sb = (p->ndim == 2 && sb == 2) ? 2 : 1;
+    g.sb = (p->ndim == 2 && (sb == 2 || (sb >= 4 && g.R * sb == WR_HALO))) ? sb : 1;
     if (vd) {
         g.sb = 1;
         g.tile_z = 16;  // the variable-density kernel's 128 x 16 tile
@@ -300,6 +306,10 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0, int step_block = 0, bool
         g.tile_z = K2_TZ;
         g.tile_y = 1;
         g.tile_x = K2_TX;
+    } else if (g.ndim == 2 && g.sb >= 4) {  // the register window's output tile
+        g.tile_z = WR_OZ;
+        g.tile_y = 1;
+        g.tile_x = WR_OX;
     } else if (g.ndim == 2 && p->field_format != WFD_FIELD_FP32) {
         g.tile_z = 32;  // the reduced-precision kernel's 128 x 32 tile
         g.tile_y = 1;
@@ -404,7 +414,7 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     const bool alists = grad && (ga.tile_z != g.tile_z || ga.tile_x != g.tile_x);
     const size_t keys = (size_t)p->nshot * std::max(g.ntiles, alists ? ga.ntiles : 0);
     L.field_bytes = (size_t)p->nshot * g.cells * (p->field_format == WFD_FIELD_FP32 ? 4 : 2);
-    L.nbuf = g.sb == 2 ? 4 : 2;
+    L.nbuf = g.sb >= 2 ? 4 : 2;  // (K steps per launch: two pairs of levels, read one, write the other)
     L.err = take(256);
     L.m = take((size_t)g.cells * 4);
     if (g.vd) L.b = take((size_t)g.cells * 4);
@@ -420,7 +430,7 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
     L.src_ent = take((size_t)p->nshot * p->nsrc * 8 + 8);
     L.rec_off = take((keys + 1) * 4);
     L.rec_ent = take((size_t)p->nshot * p->nrec * 8 + 8);
-    if (g.sb == 2) {  // a point joins up to 4 extended tile regions
+    if (g.sb >= 2) {  // a point joins up to 4 extended tile regions (windows)
         L.srce_off = take((keys + 1) * 4);
         L.srce_ent = take((size_t)p->nshot * p->nsrc * 32 + 8);
     }
@@ -694,11 +704,12 @@ int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
     WFD_CUDA(launch_build_lists(rec, p->nshot, p->nrec, g.nz, g.ny, g.nx, g.ld, g.R, g.tile_z,
                                 g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
                                 const_cast<int*>(w.rec.off), const_cast<int2*>(w.rec.ent), w.err, s));
-    if (g.sb == 2) {  // points inside each tile's extended region (R rows, 4 columns)
+    if (g.sb >= 2) {  // points inside each tile's extended region (R rows, 4 columns) or window
+        const int hz = g.sb == 2 ? g.R : WR_HALO, hx = g.sb == 2 ? 4 : WR_HALO;
         WFD_CUDA(launch_build_lists(src, p->nshot, p->nsrc, g.nz, g.ny, g.nx, g.ld, g.R, g.tile_z,
                                     g.tile_y, g.tile_x, g.tiles_z, g.tiles_y, g.tiles_x, w.counts,
                                     const_cast<int*>(w.src_e.off), const_cast<int2*>(w.src_e.ent),
-                                    w.err, s, g.R, 4));
+                                    w.err, s, hz, hx));
     }
     if (w.own_alists) {  // the u-store adjoint's 16-row tiles
         const Geom a = adjoint_geom(p, g);
@@ -728,9 +739,51 @@ int setup(const wfd_problem* p, const Geom& g, const Work& w, const float* vel,
 int run_forward_lp(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                    const Stepper& st, const float* wavelet, float* traces, int* final_buf);
 
+// Forward of K = WR_HALO / R steps per launch (step_block 8 at order 2, 4 at
+// order 4; leapfrog, no checkpoints): the levels (u_{n-1}, u_n) in one pair of
+// buffers, P[2i] and P[2i + 1]; a launch of k steps writes (u_{n+k-1}, u_{n+k})
+// to the other pair. The kernel samples the receivers after every step.
+int run_forward_reg(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w, const Stepper& st,
+                    const float* wavelet, float* traces, int* final_buf) {
+    cudaStream_t s = st.s;
+    for (int b = 0; b < 4; ++b) WFD_CUDA(cudaMemsetAsync(w.P[b], 0, L.field_bytes, s));
+    const int K = WR_HALO / g.R;
+    int pair = 0;
+    PhaseScope scope(PH_FORWARD, s, (p->nt + K - 1) / K);
+    for (int n = 0; n < p->nt; n += K) {
+        StepArgs a = st.base(nullptr);
+        a.inj_val = wavelet;
+        a.inj_np = p->nsrc; a.inj_nt = p->nt;
+        a.inj_scale = p->src_scale;
+        if (traces && p->nrec > 0) {
+            a.smp = w.rec;
+            a.smp_out = traces;
+            a.smp_np = p->nrec; a.smp_nt = p->nt;
+            a.smp_scale = 1.f;
+        }
+        RegArgs q{};
+        q.u0 = w.P[2 * pair];
+        q.u1 = w.P[2 * pair + 1];
+        q.v0 = w.P[2 * (pair ^ 1)];
+        q.v1 = w.P[2 * (pair ^ 1) + 1];
+        if (p->nsrc > 0) q.src = w.src_e;
+        q.n0 = n;
+        q.ksteps = std::min(K, p->nt - n);
+        const cudaError_t e = launch_wave_reg(g.R, a, q, s);
+        if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "multi-step launch failed: %s", cudaGetErrorString(e));
+        pair ^= 1;
+    }
+    if (final_buf) *final_buf = 2 * pair + 1;
+    return WFD_OK;
+}
+
 int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                 const Stepper& st, const float* wavelet, float* traces, bool save,
                 int* final_buf = nullptr) {
+    if (g.sb >= 4) {
+        if (save) return fail(WFD_ERR_INVALID, "step_block %d is a forward-only mode", g.sb);
+        return run_forward_reg(p, g, L, w, st, wavelet, traces, final_buf);
+    }
     if (p->field_format != WFD_FIELD_FP32) {
         if (save) return fail(WFD_ERR_INVALID, "reduced-precision fields are a forward-only mode");
         return run_forward_lp(p, g, L, w, st, wavelet, traces, final_buf);
@@ -1270,6 +1323,8 @@ int wfd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes) 
     if (!bytes) return fail(WFD_ERR_INVALID, "bytes is NULL");
     if (with_gradient && p->field_format != WFD_FIELD_FP32)
         return fail(WFD_ERR_INVALID, "reduced-precision fields are a forward-only mode");
+    if (with_gradient && p->step_block >= 4)
+        return fail(WFD_ERR_INVALID, "step_block %d is a forward-only mode", p->step_block);
     const wfd_problem q = group_problem(p, 0);  // the workspace serves one group at a time
     const Geom g = make_geom(&q);
     *bytes = make_layout(&q, g, with_gradient != 0).total;
@@ -1347,6 +1402,7 @@ int wfd_backward(const wfd_problem* p, const float* vel, const float* sponge_z,
         return fail(WFD_ERR_INVALID, "grad_vel/dtraces is NULL");
     if (p->field_format != WFD_FIELD_FP32)
         return fail(WFD_ERR_INVALID, "reduced-precision fields are a forward-only mode");
+    if (p->step_block >= 4) return fail(WFD_ERR_INVALID, "step_block %d is a forward-only mode", p->step_block);
     if (group_size(p) < p->nshot)
         return fail(WFD_ERR_INVALID, "wfd_backward cannot be split into shot groups");
     const Geom g = make_geom(p);
@@ -1374,6 +1430,7 @@ int misfit_gradient_impl(const wfd_problem* p, const float* vel, const float* sp
         return fail(WFD_ERR_INVALID, "grad_vel/misfit/observed is NULL");
     if (p->field_format != WFD_FIELD_FP32)
         return fail(WFD_ERR_INVALID, "reduced-precision fields are a forward-only mode");
+    if (p->step_block >= 4) return fail(WFD_ERR_INVALID, "step_block %d is a forward-only mode", p->step_block);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     WFD_CUDA(cudaMemsetAsync(misfit, 0, sizeof(double), s));
     const int G = group_size(p);

@@ -360,7 +360,6 @@ __global__ void __launch_bounds__(TR_W, MINB)
     const int i0 = blockIdx.y * (H - 2 * TR_HALO) - TR_HALO;
     const bool jin = j >= 0 && j < M;
     float A[H], B[H];  // u_{n-1}, u_n; they trade roles every step
-    grid_dependency_wait();
 #pragma unroll
     for (int r = 0; r < H; ++r) {
         const int i = i0 + r;
@@ -369,7 +368,6 @@ __global__ void __launch_bounds__(TR_W, MINB)
         A[r] = in ? __ldg(u0 + c) : 0.f;
         B[r] = in ? __ldg(u1 + c) : 0.f;
     }
-    if (t == 0) launch_dependents();
     const bool jupd = j > 0 && j < M - 1;  // the boundary columns (and beyond) stay untouched
     const int j0 = blockIdx.x * TR_OX - TR_HALO;
     const bool inner = i0 >= 1 && i0 + H - 1 <= N - 2 && j0 >= 1 && j0 + TR_W - 1 <= M - 2;  // (CTA-uniform)
@@ -417,13 +415,16 @@ cudaError_t launch_temporal_reg(const float* u0, const float* u1, float* v0, flo
     constexpr int OZ = TR_H - 2 * TR_HALO;
     const dim3 grid((M + TR_OX - 1) / TR_OX, (N + OZ - 1) / OZ);
     const float k = kcoef(wavespeed, dt), dx2 = dx * dx, dy2 = dy * dy;
-    const cudaError_t e =
-        exact ? launch_pdl(temporal_reg_kernel<true, TR_H, TR_MINB>, grid, dim3(TR_W), 0, s, u0, u1, v0, v1, k, dx2,
-                           dy2, k / dx2, k / dy2, N, M, Mp)
-              : launch_pdl(temporal_reg_kernel<false, TR_H, TR_MINB>, grid, dim3(TR_W), 0, s, u0, u1, v0, v1, k,
-                           dx2, dy2, k / dx2, k / dy2, N, M, Mp);
+    // a plain launch: the window's read-only loads of u0 and u1, the previous
+    // launch's output, are ordered after it by the kernel boundary
+    if (exact)
+        temporal_reg_kernel<true, TR_H, TR_MINB><<<grid, TR_W, 0, s>>>(u0, u1, v0, v1, k, dx2, dy2, k / dx2, k / dy2,
+                                                                     N, M, Mp);
+    else
+        temporal_reg_kernel<false, TR_H, TR_MINB><<<grid, TR_W, 0, s>>>(u0, u1, v0, v1, k, dx2, dy2, k / dx2, k / dy2,
+                                                                      N, M, Mp);
     count_launch();
-    return e != cudaSuccess ? e : cudaGetLastError();
+    return cudaGetLastError();
 }
 
 cudaError_t launch_temporal(const CUtensorMap& m0, const CUtensorMap& m1, float* v0, float* v1, float wavespeed,

@@ -181,6 +181,33 @@ struct Step2Args {
 cudaError_t launch_step2d_k2(int R, const CUtensorMap& map_u, const CUtensorMap& map_o,
                              const CUtensorMap& map_m, const Step2Args& p, cudaStream_t s);
 
+// ---------------------------------------------------------------- 2D, K steps per launch (orders 2, 4)
+// A window of WR_W columns x WR_H rows per CTA, held in registers (a column
+// per thread); K = WR_HALO / R steps per launch (8 at order 2, 4 at order 4),
+// after which the inner WR_OX x WR_OZ tile is exact.
+constexpr int WR_W = 256;
+constexpr int WR_H = 40;
+constexpr int WR_HALO = 8;
+constexpr int WR_OX = WR_W - 2 * WR_HALO;  // 240 output columns per CTA
+constexpr int WR_OZ = WR_H - 2 * WR_HALO;  // 24 output rows per CTA
+
+struct RegArgs {
+    const float* u0;  // u_{n-1}, [nshot][cells]
+    const float* u1;  // u_n
+    float* v0;        // u_{n+k-1} on the output tiles (neither input aliases an output)
+    float* v1;        // u_{n+k}
+    PointLists src;   // sources inside each tile's window (the tile plus WR_HALO on every side)
+    int n0;           // absolute index of the launch's first step (u_{n0} -> u_{n0+1})
+    int ksteps;       // steps of this launch, 1 .. WR_HALO / R
+};
+
+// Forward steps n0 .. n0 + ksteps - 1 of every shot (leapfrog, FP32, 2D, R = 1
+// or 2): a.m, a.gz, a.gx, the weights and the tile geometry (a.tiles_x,
+// a.tiles_z of WR_OX x WR_OZ tiles); sources from q.src, wavelet a.inj_val
+// (a.inj_nt, a.inj_np, a.inj_scale); receivers a.smp (tile lists), sampled
+// after every step into a.smp_out[shot][step][rec] (the level u_{step+1}).
+cudaError_t launch_wave_reg(int R, const StepArgs& a, const RegArgs& q, cudaStream_t s);
+
 // ---------------------------------------------------------------- 3D tiles
 // One CTA (one shot) marches along z through a (TY x TX) column of the grid
 // for T3_ZCHUNK output planes; a thread owns 4 x cells and keeps the 2R + 1

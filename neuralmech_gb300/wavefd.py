@@ -65,7 +65,9 @@ class Grid:
              autograd) in sequential groups of this many, sharing one workspace
              sized for a group (0 = all at once)
     tile_rows    2D tile height, 16 or 32 rows (0 = 32)
-    step_block   2D time steps per kernel launch, 1 or 2 (0 = 1)
+    step_block   2D time steps per kernel launch, 1 or 2 (0 = 1); for a
+             forward (no gradient) with the leapfrog update and FP32 fields
+             also 8 at order 2 or 4 at order 4 (a register window per CTA)
     store_levels FP32 levels the adjoint's workspace may hold (lap_store "auto"):
              the forward keeps the levels of its last (store_levels - 2) // K
              segments and only the earlier ones are recomputed (0: the last

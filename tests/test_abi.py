@@ -260,3 +260,22 @@ def test_variable_density_arguments_rejected():
     assert _ws(_problem(dt=dt * 0.999))[0] == 0  # the collocated bound holds
     assert forward(_problem(dt=dt * 0.999)) == -4
     assert final(_problem(dt=dt * 0.999), d) == -4
+
+
+def test_register_window_step_blocks():
+    """step_block 8 (order 2) and 4 (order 4): 2D leapfrog FP32 forwards only;
+    refused with another order, in 3D, with a gradient, with the summed
+    update or reduced-precision fields, and any other value."""
+    from neuralmech_gb300 import _lib
+    ok = [dict(step_block=8, order=2), dict(step_block=4, order=4)]
+    for kw in ok:
+        rc, n = _ws(_problem(**kw), 0)
+        assert rc == 0 and n > 0, kw
+        assert _ws(_problem(**kw), 1)[0] == _lib.WFD_ERR_INVALID, kw  # forward only
+        assert _ws(_problem(update_form=2, **kw), 0)[0] == _lib.WFD_ERR_INVALID, kw
+        assert _ws(_problem(field_format=1, **kw), 0)[0] == _lib.WFD_ERR_INVALID, kw
+    bad = [dict(step_block=8, order=8), dict(step_block=8, order=4), dict(step_block=4, order=2),
+           dict(step_block=3, order=2), dict(step_block=16, order=2),
+           dict(step_block=8, order=2, ndim=3, ny=20, nz=24, nx=40, vmax=2000.0, dy=10.0)]
+    for kw in bad:
+        assert _ws(_problem(**kw), 0)[0] == _lib.WFD_ERR_INVALID, kw

@@ -213,3 +213,48 @@ def test_homogeneous_greens_function(cuda, ndim):
         err = rel_l2(tr[win, j], ana[win])
         print(f"{ndim}D Green's function, receiver {j}: rel L2 {err:.3e}")
         assert err < (0.05 if ndim == 2 else 0.03)
+
+
+@pytest.mark.parametrize("order,shape,nshot,nt,sponge", [
+    (2, (100, 600), 3, 77, 10),            # 3 x 5 windows, a last launch of 5 steps
+    (4, (53, 487), 2, 61, [(6, 11), (4, 9)]),  # odd sizes, per-face sponge, a last launch of 1 step
+    (2, (30, 250), 1, 40, 0),              # one window row, no sponge
+    (4, (240, 260), 2, 33, 8),
+])
+def test_forward_register_window(cuda, orc, order, shape, nshot, nt, sponge):
+    """step_block 8 (order 2) and 4 (order 4): K steps per launch in a register
+    window, against the FP64 oracle (1e-5) and the one-step forward (traces
+    and final level, 1e-6). Sources and receivers sit on and around the window
+    seams (columns 240 k and 240 k +- 8, rows 24 k and 24 k +- 8), where a
+    source joins up to four windows' halos."""
+    import dataclasses
+    from neuralmech_gb300 import wave_forward
+    from neuralmech_gb300.wavefd import wave_forward_final
+    grid, v, wav, src, rec = small_problem(shape=shape, nshot=nshot, nt=nt, order=order, sponge=sponge,
+                                           nsrc=3, nrec=40, seed=order * 5 + nshot)
+    R = order // 2
+    nz, nx = shape
+    clampz = lambda z: int(min(max(z, R), nz - R - 1))
+    clampx = lambda x: int(min(max(x, R), nx - R - 1))
+    seams = [(24, 240), (16, 232), (32, 248), (23, 239), (47, 241), (8, 120)]
+    for s in range(nshot):
+        for i in range(3):
+            z, x = seams[(s + i) % len(seams)]
+            src[s, i] = [clampz(z), clampx(x)]
+        for i in range(12):
+            z, x = seams[i % len(seams)]
+            rec[s, i] = [clampz(z + i // len(seams)), clampx(x + 2 * (i // len(seams)))]
+    args = (torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+            torch.from_numpy(rec))
+    gk = dataclasses.replace(grid, step_block=8 if order == 2 else 4)
+    g1 = dataclasses.replace(grid, step_block=1)
+    tk = wave_forward(*args, gk).cpu().numpy()
+    t1 = wave_forward(*args, g1).cpu().numpy()
+    ref = orc.forward(oracle_geometry(orc, grid, v, wav, src, rec))
+    assert np.abs(ref).max() > 0
+    assert rel_l2(tk, ref) < 1e-5
+    assert rel_l2(tk, t1) < 1e-6
+    fk = wave_forward_final(*args, gk)[1].cpu().numpy()
+    f1 = wave_forward_final(*args, g1)[1].cpu().numpy()
+    assert np.abs(f1).max() > 0
+    assert rel_l2(fk, f1) < 1e-6

@@ -460,11 +460,56 @@ def l2_copy_gbs(dev, mb: int = 32) -> float:
     return 2.0 * n * 4 * 1000 / (e0.elapsed_time(e1) / 1e3) / 1e9
 
 
+def multistep_pairs(dev, cases=((2048, 2048, 4000), (8000, 16000, 64)), reps=3):
+    """The wave path's forward at orders 2 and 4, one step per launch against
+    K steps per launch in a register window (step_block 8 at order 2, 4 at
+    order 4): one shot, a 20-cell sponge, the velocity of fwd2048's model
+    class (1500..3500 m/s layers), a source near the top and a receiver on
+    every column of row 5. G cell-updates/s of each and the ratio."""
+    import dataclasses
+
+    import torch
+
+    from neuralmech_gb300 import Grid, wave_forward
+    from neuralmech_gb300.synth import layered, ricker
+    out = {}
+    for nz, nx, nt in cases:
+        v = layered((nz, nx), [0, nz // 3, 2 * nz // 3], [1500.0, 2500.0, 3500.0]).astype(np.float32)
+        dx = 10.0
+        vel = torch.from_numpy(v).to(dev)
+        src = torch.tensor([[[5, nx // 2]]], dtype=torch.int32)
+        rec = torch.from_numpy(np.stack([np.full(nx - 8, 5), np.arange(4, nx - 4)], -1)[None].astype(np.int32))
+        for order, K in ((2, 8), (4, 4)):
+            dt = 0.4 * dx / 3500.0
+            wav = torch.from_numpy(ricker(15.0, nt, dt).astype(np.float32)).reshape(1, nt, 1).to(dev)
+            g = Grid((nz, nx), (dx, dx), dt, nt, order=order, sponge=20)
+            R = order // 2
+            upd = (nz - 2 * R) * (nx - 2 * R) * nt
+            r = {}
+            for sb in (1, K):
+                gg = dataclasses.replace(g, step_block=sb)
+                wave_forward(vel, wav, src, rec, gg, check=False)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    wave_forward(vel, wav, src, rec, gg, check=False)
+                e1.record()
+                torch.cuda.synchronize()
+                r[f"{sb} step{'s' if sb > 1 else ''} per launch"] = round(upd * reps / (e0.elapsed_time(e1) / 1e3) / 1e9, 1)
+            vals = list(r.values())
+            r["ratio"] = round(vals[1] / vals[0], 2)
+            out[f"order {order}, {nz}x{nx}, {nt} steps"] = r
+    out["unit"] = "G cell-updates/s (one shot, receivers on a row)"
+    return out
+
+
 def secondary_legs(dev):
     """Short legs of the other configurations, in the default run: the fwd2048
-    forward (2048^2, 4000 steps, one shot, order 8, sponge) and the order-2
+    forward (2048^2, 4000 steps, one shot, order 8, sponge), the order-2
     drop-ins beside the reference's own kernels on the temporal driver's
-    8000 x 16000 grid."""
+    8000 x 16000 grid, and the wave path's multi-step forward at orders 2
+    and 4 beside one step per launch."""
     import torch
 
     from neuralmech_gb300 import wave_forward
@@ -491,6 +536,7 @@ def secondary_legs(dev):
                               "fields": "u_n, u_{n-1}, m: 3 x 16.8 MB, resident in L2 across steps",
                               "alg_gbs": rate * 16.0, "l2_copy_gbs": l2, "alg_frac_of_l2_copy": rate * 16.0 / l2}
     out["order2_pairs"] = order2_pairs(dev, grids=((8000, 16000),))
+    out["multistep"] = multistep_pairs(dev)
     return out
 
 
@@ -518,7 +564,7 @@ def _wl_temporal(args, dev):
         state["k"] += 1
 
     inner = (N - 2) * (M - 2)
-    extra = {"pairs": order2_pairs(dev)}
+    extra = {"pairs": order2_pairs(dev), "multistep": multistep_pairs(dev)}
     updates, bpu = 8.0 * inner, 16.0 / 8
     cfg = {"workload": f"temporal: wfd_temporal_step_fast, {N} x {M} (M_padded {Mp}), order 2, Dirichlet, "
                        "8 updates per launch; bytes: both levels read and written once per launch",

@@ -65,8 +65,10 @@ __device__ __forceinline__ void add_at(float (&v)[WR_H], int rr, float x) {
 // One step over the window: nxt (the level before cur) <- the level after cur.
 // GUARD: update only cells of the grid's interior (windows that reach the
 // grid's fixed ring or beyond); otherwise every row with its 2R vertical
-// neighbours inside the window is updated.
-template <int R, bool GUARD>
+// neighbours inside the window is updated. PLAIN: g = 1 on the whole window
+// (no sponge there), where the update g (m L u + 2 u) - g^2 u_{n-1} is
+// (m L u + 2 u) - u_{n-1}, value for value.
+template <int R, bool GUARD, bool PLAIN>
 __device__ __forceinline__ void wr_step(float (&nxt)[WR_H], const float (&cur)[WR_H], float* edge, const float* msh,
                                         const float* gzs, int t, int lane, int warp, float gxj, bool col_ok, int i0,
                                         const StepArgs& a) {
@@ -81,9 +83,17 @@ __device__ __forceinline__ void wr_step(float (&nxt)[WR_H], const float (&cur)[W
         for (int r = 0; r < WR_H; ++r) d[r] = cur[r];
     }
     __syncthreads();
-    // (the window's outermost columns read their own warp's edge in place of a
-    // missing neighbour: finite values that never reach the output tile)
+    // the neighbouring warps' edge column that lanes < k (left) and lanes
+    // >= 32 - k (right) read for the tap at distance k: one shared-memory load
+    // per row and tap through a per-lane pointer (the window's outermost
+    // columns read their own warp's edge in place of a missing neighbour:
+    // finite values that never reach the output tile)
     const int wl = max(warp - 1, 0), wr = min(warp + 1, WR_NW - 1);
+    int nb[R];  // offsets into edge; lanes that use no edge value read an in-range slot
+#pragma unroll
+    for (int k = 1; k <= R; ++k)
+        nb[k - 1] = lane < 16 ? ((wl * 2 + 1) * R + min(R - k + lane, R - 1)) * WR_H
+                              : ((wr * 2 + 0) * R + min(max(lane + k - 32, 0), R - 1)) * WR_H;
 #pragma unroll
     for (int r = R; r < WR_H - R; ++r) {
         const float c = cur[r];
@@ -92,13 +102,19 @@ __device__ __forceinline__ void wr_step(float (&nxt)[WR_H], const float (&cur)[W
         for (int k = 1; k <= R; ++k) {
             float l = __shfl_up_sync(0xffffffffu, c, k);
             float rr = __shfl_down_sync(0xffffffffu, c, k);
-            if (lane < k) l = edge[((wl * 2 + 1) * R + (R - k + lane)) * WR_H + r];
-            if (lane >= 32 - k) rr = edge[((wr * 2 + 0) * R + (lane + k - 32)) * WR_H + r];
+            const float e = edge[nb[k - 1] + r];
+            if (lane < k) l = e;
+            if (lane >= 32 - k) rr = e;
             acc = fmaf(a.cx[k - 1], l + rr, acc);
             acc = fmaf(a.cz[k - 1], cur[r - k] + cur[r + k], acc);
         }
-        const float g = gzs[r] * gxj;
-        const float nv = g * fmaf(msh[r * WR_W + t], acc, 2.f * c) - (g * g) * nxt[r];
+        float nv;
+        if (PLAIN) {
+            nv = fmaf(msh[r * WR_W + t], acc, 2.f * c) - nxt[r];
+        } else {
+            const float g = gzs[r] * gxj;
+            nv = g * fmaf(msh[r * WR_W + t], acc, 2.f * c) - (g * g) * nxt[r];
+        }
         if (!GUARD || (col_ok && i0 + r >= R && i0 + r < a.nz - R)) nxt[r] = nv;
     }
 }
@@ -143,7 +159,9 @@ __global__ void __launch_bounds__(WR_W, 2) wave_reg_kernel(const StepArgs a, con
         gzs[t] = (a.gz != nullptr && i >= 0 && i < a.nz) ? __ldg(a.gz + i) : 1.f;
     }
     const float gxj = (a.gx != nullptr && jin) ? __ldg(a.gx + jcol) : 1.f;
-    __syncthreads();  // list heads initialised
+    // g = 1 on the whole window: every column's gx and every row's gz is 1
+    const bool g1 = gxj == 1.f && (t >= WR_H || gzs[t] == 1.f);
+    const bool plain = __syncthreads_and(g1 ? 1 : 0) != 0;  // (also: list heads initialised)
 
     // link the window's sources and the tile's receivers into per-column lists
     const long long key = (long long)shot * ntiles + tile;
@@ -203,20 +221,23 @@ __global__ void __launch_bounds__(WR_W, 2) wave_reg_kernel(const StepArgs a, con
         }
     };
 
+    const int kind = inner ? (plain ? 0 : 1) : 2;  // (CTA-uniform)
+    auto step = [&](float (&nxt)[WR_H], const float (&cur)[WR_H], float* edge) {
+        if (kind == 0)
+            wr_step<R, false, true>(nxt, cur, edge, msh, gzs, t, lane, warp, gxj, col_ok, i0, a);
+        else if (kind == 1)
+            wr_step<R, false, false>(nxt, cur, edge, msh, gzs, t, lane, warp, gxj, col_ok, i0, a);
+        else
+            wr_step<R, true, false>(nxt, cur, edge, msh, gzs, t, lane, warp, gxj, col_ok, i0, a);
+    };
     for (int st = 0; st < q.ksteps; ++st) {
         float* edge = edge_base + (st & 1) * (WR_NW * 2 * R * WR_H);
         const int n = q.n0 + st;
         if ((st & 1) == 0) {
-            if (inner)
-                wr_step<R, false>(A, B, edge, msh, gzs, t, lane, warp, gxj, col_ok, i0, a);
-            else
-                wr_step<R, true>(A, B, edge, msh, gzs, t, lane, warp, gxj, col_ok, i0, a);
+            step(A, B, edge);
             points(A, n);
         } else {
-            if (inner)
-                wr_step<R, false>(B, A, edge, msh, gzs, t, lane, warp, gxj, col_ok, i0, a);
-            else
-                wr_step<R, true>(B, A, edge, msh, gzs, t, lane, warp, gxj, col_ok, i0, a);
+            step(B, A, edge);
             points(B, n);
         }
     }

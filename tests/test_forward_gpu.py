@@ -258,3 +258,27 @@ def test_forward_register_window(cuda, orc, order, shape, nshot, nt, sponge):
     f1 = wave_forward_final(*args, g1)[1].cpu().numpy()
     assert np.abs(f1).max() > 0
     assert rel_l2(fk, f1) < 1e-6
+
+
+def test_forward_register_window_many_points(cuda, orc):
+    """More than the 1024 sources and receivers a CTA links into its
+    per-column lists (1100 sources in one window, 1500 receivers in one
+    tile): the overflow entries take the scanning path, with the same results
+    as one step per launch (1e-6) and the FP64 oracle (1e-5)."""
+    import dataclasses
+    from neuralmech_gb300 import wave_forward
+    grid, v, wav, src, rec = small_problem(shape=(40, 250), nshot=1, nt=20, order=2, sponge=4, nsrc=1, nrec=1,
+                                           seed=31)
+    rng = np.random.default_rng(31)
+    cells = rng.permutation(16 * 200)[:1500]  # distinct cells of tile (0, 0): rows 8..23, columns 20..219
+    rec = np.stack([8 + cells // 200, 20 + cells % 200], -1)[None].astype(np.int32)
+    src = np.stack([rng.integers(2, 38, 1100), rng.integers(2, 248, 1100)], -1)[None].astype(np.int32)
+    wav = (np.repeat(wav[:, :, :1], 1100, axis=2) * rng.uniform(0.5, 1.5, (1, 1, 1100))).astype(np.float32)
+    args = (torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+            torch.from_numpy(rec))
+    tk = wave_forward(*args, dataclasses.replace(grid, step_block=8)).cpu().numpy()
+    t1 = wave_forward(*args, dataclasses.replace(grid, step_block=1)).cpu().numpy()
+    ref = orc.forward(oracle_geometry(orc, grid, v, wav, src, rec))
+    assert np.abs(ref).max() > 0
+    assert rel_l2(tk, t1) < 1e-6
+    assert rel_l2(tk, ref) < 1e-5

@@ -108,6 +108,10 @@ def parse():
     ap.add_argument("--level-store-frac", type=float, default=0.8,
                     help="fraction of the GPU's memory for the forward levels the adjoint keeps "
                          "instead of recomputing them (0: recompute all but the last segment)")
+    ap.add_argument("--level-format", default="fp32", choices=["fp32", "bfp16"],
+                    help="kept forward levels of the fwi1024 gradient: FP32, or block floating point "
+                         "(2.25 B per cell: more levels kept in the same budget, each encoded by the "
+                         "forward and decoded by the adjoint; the same time on this workload)")
     ap.add_argument("--update", default="auto", choices=["auto", "leapfrog", "summed"],
                     help="forward update form (auto: summed for a gradient's forward, leapfrog otherwise)")
     ap.add_argument("--workload", default="fwi1024",
@@ -348,7 +352,8 @@ def config_of(w, args):
                          f"20-cell sponge, checkpoints every {g.ckpt_every} ({g.ckpt_format})"),
             "grid": list(g.shape), "nt": g.nt, "nshot": w.nshot, "nrec": int(w.rec.shape[1]),
             "ckpt_every": g.ckpt_every, "ckpt_format": g.ckpt_format, "order": g.order,
-            "store_levels": g.store_levels, "step_block": g.step_block, "adjoint": g.adjoint,
+            "store_levels": g.store_levels, "level_format": g.level_format, "step_block": g.step_block,
+            "adjoint": g.adjoint,
             "update": g.update, "kept_segments": kept_segments(g),
             "l2": "inputs larger than L2 (multi-GB state and checkpoints per step)",
             "parallelism": f"{args.gpus} GPU(s), shots batched per GPU, gradient all-reduce"}
@@ -864,6 +869,7 @@ def main():
 
     w = workload(args.scale, args.nt, args.shots)
     w.grid = dataclasses.replace(w.grid, step_block=args.step_block or 2, adjoint=args.adjoint, update=args.update)
+    w.grid = dataclasses.replace(w.grid, level_format=args.level_format)
     if args.level_store_frac > 0:  # kept forward levels instead of recomputed ones
         budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
         w.grid = dataclasses.replace(w.grid, store_levels=levels_for_budget(w.grid, w.nshot, budget))

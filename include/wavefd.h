@@ -87,6 +87,20 @@ extern "C" {
                                  adjoint stay leapfrog. Only where WFD_UPDATE_AUTO would
                                  choose it; elsewhere WFD_ERR_INVALID */
 
+/* How the forward keeps the levels u_k of the segments the adjoint does not
+ * recompute (wfd_problem.level_format; store_levels counts levels in either). */
+#define WFD_LEVEL_FP32 0  /* FP32: 4 bytes per cell */
+#define WFD_LEVEL_BFP16 1 /* block floating point: 16-bit mantissas and one exponent byte per
+                             4 cells along x, u = q 2^(t - 141) with q in [-32767, 32767] (stored
+                             as q + 32768) and t the FP32 exponent field of the block's largest
+                             magnitude (blocks below 2^-112 kept as 0):
+                             2.25 bytes per cell, each value within 2^-15 of its block's
+                             largest. About 1.8x the kept levels in the same memory, so fewer
+                             segments are recomputed; the forward encodes and the adjoint
+                             decodes every kept level in exchange. 2D, two steps per launch,
+                             the summed forward (FP32 fields, lap_store auto, checkpoint
+                             adjoint) */
+
 typedef struct wfd_problem {
     int32_t ndim;          /* 2 or 3 */
     int32_t order;         /* space order: 2, 4 or 8 */
@@ -108,8 +122,8 @@ typedef struct wfd_problem {
                               (no gradient) with the leapfrog update and FP32 fields also
                               takes 8 at order 2 and 4 at order 4: a window of 256 x 40
                               cells per CTA stays in registers for the launch's steps */
-    int32_t store_levels;  /* WFD_LAP_AUTO path: FP32 levels (fields of nshot x cells)
-                              the workspace may hold. The forward keeps the levels of
+    int32_t store_levels;  /* WFD_LAP_AUTO path: levels (fields of nshot x cells, in
+                              level_format) the workspace may hold. The forward keeps the levels of
                               its last floor((store_levels - 2) / K) segments, K the
                               checkpoint interval, and the adjoint recomputes only
                               the others; 0 (or <= K + 2) = the last segment only */
@@ -123,6 +137,7 @@ typedef struct wfd_problem {
     float src_scale;       /* factor on every injected wavelet sample */
     float vmax;            /* max velocity for the CFL check; <= 0 skips the check */
     int32_t update_form;   /* WFD_UPDATE_AUTO, _LEAPFROG or _SUMMED */
+    int32_t level_format;  /* kept levels: WFD_LEVEL_FP32 or _BFP16 (ABI 3.1) */
 } wfd_problem;
 
 /* Human-readable text of a status code. */

@@ -53,7 +53,7 @@ class Problem(ctypes.Structure):
         ("field_format", ctypes.c_int32), ("adjoint_mode", ctypes.c_int32), ("recon_band", ctypes.c_int32),
         ("dt", ctypes.c_float), ("dz", ctypes.c_float), ("dy", ctypes.c_float),
         ("dx", ctypes.c_float), ("src_scale", ctypes.c_float), ("vmax", ctypes.c_float),
-        ("update_form", ctypes.c_int32),
+        ("update_form", ctypes.c_int32), ("level_format", ctypes.c_int32),
     ]
 
 

@@ -170,6 +170,7 @@ struct Geom {
     int K, nseg, k0_last;    // checkpoint interval, segments, first step of the last segment
     bool ustore;             // the adjoint forms L u_k from stored levels u_k (2D, one step)
     int jstore, k0_store;    // u store: the forward keeps the levels of segments >= jstore
+    bool lvl16;              // ... in block floating point (WFD_LEVEL_BFP16), not as FP32 slots
     bool lap_bf16;           // stored L u_k in BF16 (when !ustore)
     float c0, cz[4], cy[4], cx[4];
     bool vd;                 // variable density (2D): 128 x 16 tiles, staggered operator
@@ -249,6 +250,15 @@ int check_problem(const wfd_problem* p) {
         (p->field_format != WFD_FIELD_FP32 || p->lap_store != WFD_LAP_AUTO ||
          p->adjoint_mode != WFD_ADJOINT_CHECKPOINT))
         return fail(WFD_ERR_INVALID, "the summed update form: FP32 fields, lap_store auto, checkpoint adjoint");
+    if (p->level_format < WFD_LEVEL_FP32 || p->level_format > WFD_LEVEL_BFP16)
+        return fail(WFD_ERR_INVALID, "unknown level_format %d", p->level_format);
+    if (p->level_format == WFD_LEVEL_BFP16 &&
+        (p->ndim != 2 || p->step_block != 2 || p->update_form == WFD_UPDATE_LEAPFROG ||
+         p->field_format != WFD_FIELD_FP32 || p->lap_store != WFD_LAP_AUTO ||
+         p->adjoint_mode != WFD_ADJOINT_CHECKPOINT))
+        return fail(WFD_ERR_INVALID,
+                    "block-floating-point levels: 2D, step_block 2, the summed forward (FP32 fields, "
+                    "lap_store auto, checkpoint adjoint)");
     if (p->recon_band < 0 || 2 * p->recon_band > std::min(p->nz, p->nx))
         return fail(WFD_ERR_INVALID, "recon_band must lie in [0, min(nz, nx) / 2]");
     if (p->tile_rows != 0 && p->tile_rows != 16 && p->tile_rows != 32)
@@ -348,6 +358,7 @@ Geom make_geom(const wfd_problem* p, int tile_rows = 0, int step_block = 0, bool
     if (g.ustore && p->store_levels > g.K + 2)
         g.jstore = std::max(0, g.nseg - (p->store_levels - 2) / g.K);
     g.k0_store = g.jstore * g.K;
+    g.lvl16 = g.ustore && !vd && p->level_format == WFD_LEVEL_BFP16;
     g.lap_bf16 = p->lap_store == WFD_LAP_BF16;
     g.recon = p->adjoint_mode == WFD_ADJOINT_RECONSTRUCT;
     if (g.recon) {
@@ -393,6 +404,10 @@ struct Layout {
     size_t D;                  // summed form: the increment field d_n (0: leapfrog)
     int nlap;  // slots of the lap region: K stored L u_k, or levels u_k (u store): from
                // u_{k0_store - 1} to u_nt, and at least K + 2 for a recomputed segment
+    // block-floating-point kept levels u_{k0_store} .. u_{nt-1} (level i = u_{k0_store + i}),
+    // in the same region: the adjoint is done with them before a segment is recomputed
+    int nlvl;
+    size_t lvl_q_bytes, lvl_bytes;  // mantissas of a level; mantissas + exponents
 };
 
 size_t up256(size_t v) { return (v + 255) / 256 * 256; }
@@ -445,7 +460,12 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
         // per-field slots start on 256-byte boundaries (TMA bases, short4/float4 access)
         L.ckpt_field_bytes = up256(ckpt_bytes(p->ckpt_format, (long long)p->nshot * g.cells));
         L.lap_field_bytes = up256((size_t)p->nshot * g.cells * (g.lap_bf16 ? 2 : 4));
-        L.nlap = g.recon ? 0 : g.ustore ? std::max(g.K + 2, p->nt - g.k0_store + 2) : g.K;
+        L.nlap = g.recon ? 0 : g.lvl16 ? g.K + 2 : g.ustore ? std::max(g.K + 2, p->nt - g.k0_store + 2) : g.K;
+        if (g.lvl16) {
+            L.nlvl = p->nt - g.k0_store;
+            L.lvl_q_bytes = up256((size_t)p->nshot * g.cells * 2);
+            L.lvl_bytes = L.lvl_q_bytes + up256((size_t)p->nshot * g.nz * bfp_eld(g.ld));
+        }
         for (int b = 0; b < 2; ++b) L.Q[b] = take(L.field_bytes);  // (the adjoint is one-step)
         L.G = take((size_t)g.cells * 4);
         if (g.vd) {
@@ -458,7 +478,7 @@ Layout make_layout(const wfd_problem* p, const Geom& g, bool grad) {
             L.frame_bytes = up256((size_t)band_cells(g.nz, g.ld, g.band_w, g.band_cl, g.band_cr) * p->nshot * 4);
             L.frames = take((size_t)(p->nt + 1) * L.frame_bytes);
         }
-        L.lap = take((size_t)L.nlap * L.lap_field_bytes);
+        L.lap = take(std::max((size_t)L.nlap * L.lap_field_bytes, (size_t)L.nlvl * L.lvl_bytes));
         L.res = take((size_t)p->nshot * p->nt * p->nrec * 4 + 4);
     }
     L.total = o;
@@ -481,6 +501,12 @@ struct Work {
     bool own_alists;          // src_a / rec_a are separate lists that setup() builds
     float* slot(const Layout& L, int i) const {  // u-store level slot i
         return reinterpret_cast<float*>(lap + (size_t)i * L.lap_field_bytes);
+    }
+    short* lvl_q(const Layout& L, int i) const {  // block-floating-point level i: mantissas
+        return reinterpret_cast<short*>(lap + (size_t)i * L.lvl_bytes);
+    }
+    unsigned char* lvl_e(const Layout& L, int i) const {  // ... and exponents
+        return lap + (size_t)i * L.lvl_bytes + L.lvl_q_bytes;
     }
 };
 
@@ -658,9 +684,9 @@ struct Stepper {
     }
 
     int launch(int mode, const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
-               const StepArgs& a) const {
+               const StepArgs& a, const CUtensorMap* mx = nullptr) const {
         cudaError_t e = g.vd           ? launch_step2d_vd(g.R, mode, mc, mo, ml, map_m, a, s)
-                        : g.ndim == 2 ? launch_step2d(g.R, mode, g.tile_z, mc, mo, ml, a, s)
+                        : g.ndim == 2 ? launch_step2d(g.R, mode, g.tile_z, mc, mo, ml, a, s, mx)
                                       : launch_step3d(g.R, mode, mc, mo, ml, map_m, a, s);
         if (e != cudaSuccess) return fail(WFD_ERR_CUDA, "step launch failed: %s", cudaGetErrorString(e));
         return WFD_OK;
@@ -791,11 +817,16 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
     cudaStream_t s = st.s;
     const bool rc_mode = save && g.recon;  // reconstruction adjoint: frames, no checkpoints or slots
     const bool us = save && g.ustore && !rc_mode;
+    // kept levels as block-floating-point copies beside the FP32 state (which then
+    // stays in P), or as FP32 slots that the state itself runs through
+    const bool keep16 = us && g.lvl16;
+    const bool uslots = us && !g.lvl16;
     const int np = L.nbuf;
-    const int nslot = us ? L.nlap : 0;
+    const int nslot = uslots ? L.nlap : 0;
     auto loc = [&](int k) -> int {
-        return us && k >= g.k0_store - 1 ? np + (k - g.k0_store + 1) : ((k % np) + np) % np;
+        return uslots && k >= g.k0_store - 1 ? np + (k - g.k0_store + 1) : ((k % np) + np) % np;
     };
+    auto kept16 = [&](int k) { return keep16 && k >= g.k0_store && k < p->nt; };
     std::vector<float*> buf(np + nslot);
     for (int b = 0; b < np; ++b) buf[b] = w.P[b];
     for (int i = 0; i < nslot; ++i) buf[np + i] = w.slot(L, i);
@@ -815,6 +846,7 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
     if (summed && g.sb == 2)
         for (int k = 1; k < 3; ++k) D[k] = w.D + (size_t)k * (L.field_bytes / sizeof(float));
     if (summed) WFD_CUDA(cudaMemsetAsync(w.D, 0, L.field_bytes, s));  // d_0 = 0
+    if (kept16(0)) WFD_CUDA(cudaMemsetAsync(w.lvl_q(L, 0), 0, L.lvl_bytes, s));  // u_0 = 0
     std::vector<CUtensorMap> mc(buf.size()), mo(buf.size());
     int rc;
     for (size_t b = 0; b < buf.size(); ++b)
@@ -874,7 +906,16 @@ int run_forward(const wfd_problem* p, const Geom& g, const Layout& L, const Work
                 q.summed = 1;
                 q.d_out = D[din ^ 1];
                 q.d_mid = two ? D[2] : D[din ^ 1];
-                q.write_mid = !two || ckpt_at(n + 1) || (us && n + 1 >= g.k0_store - 1);
+                q.write_mid = !two || ckpt_at(n + 1) || (uslots && n + 1 >= g.k0_store - 1);
+                q.eld = bfp_eld(g.ld);
+                if (kept16(n + 1)) {
+                    q.lq_mid = w.lvl_q(L, n + 1 - g.k0_store);
+                    q.le_mid = w.lvl_e(L, n + 1 - g.k0_store);
+                }
+                if (two && kept16(n + 2)) {
+                    q.lq_out = w.lvl_q(L, n + 2 - g.k0_store);
+                    q.le_out = w.lvl_e(L, n + 2 - g.k0_store);
+                }
                 if ((rc = st.launch_k2(mc[loc(n)], mde[din], q))) return rc;
                 if ((rc = checkpoint(n, D[din]))) return rc;
                 if (two && (rc = checkpoint(n + 1, D[2]))) return rc;
@@ -1024,10 +1065,27 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
             return rc;
         if ((rc = sa.map_pair(w.slot(L, i), w.slot(L, i), &ua[i], &unused[i]))) return rc;
     }
+    // block-floating-point kept levels: mantissa and exponent tiles of the adjoint's
+    // 16-row tiles (boxes at x0 - 8 and, in exponent bytes, x0/4 - 16)
+    std::vector<CUtensorMap> lq(L.nlvl), le(L.nlvl);
+    if (g.lvl16) {
+        const int eld = bfp_eld(g.ld);
+        const cuuint64_t qd[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.nz, (cuuint64_t)p->nshot};
+        const cuuint64_t qs[2] = {(cuuint64_t)g.ld * 2, (cuuint64_t)g.nz * g.ld * 2};
+        const cuuint64_t ed[3] = {(cuuint64_t)(g.ld / 4), (cuuint64_t)g.nz, (cuuint64_t)p->nshot};
+        const cuuint64_t es[2] = {(cuuint64_t)eld, (cuuint64_t)g.nz * eld};
+        const cuuint32_t qb[3] = {T2_TX + 16, cuuint32_t(ga.tile_z + 2 * g.R), 1};
+        const cuuint32_t eb[3] = {64, cuuint32_t(ga.tile_z + 2 * g.R), 1};
+        for (int i = 0; i < L.nlvl; ++i) {
+            if ((rc = make_map3(&lq[i], w.lvl_q(L, i), CU_TENSOR_MAP_DATA_TYPE_UINT16, qd, qs, qb))) return rc;
+            if ((rc = make_map3(&le[i], w.lvl_e(L, i), CU_TENSOR_MAP_DATA_TYPE_UINT8, ed, es, eb))) return rc;
+        }
+    }
     const long long n_all = (long long)p->nshot * g.cells;
 
-    // q_k from (q_{k+1}, q_{k+2}); with the gradient term q_{k+1} L u_k, u_k in slot `slot`
-    auto adjoint_step = [&](int k, int slot) -> int {
+    // q_k from (q_{k+1}, q_{k+2}); with the gradient term q_{k+1} L u_k, u_k in slot
+    // `slot` (FP32), or in block-floating-point level `slot` when lvl is set
+    auto adjoint_step = [&](int k, int slot, bool lvl = false) -> int {
         const int bc = (k + 1) & 1, bn = k & 1;
         StepArgs a = sa.base(w.Q[bn]);
         if (p->nrec > 0) {
@@ -1048,6 +1106,7 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
         a.grad = w.G;
         a.grad_bx = w.Gbx;
         a.grad_bz = w.Gbz;
+        if (lvl) return sa.launch(MODE_GRAD_U16, qc[bc], qo[bn], lq[slot], a, &le[slot]);
         return sa.launch(MODE_GRAD_U, qc[bc], qo[bn], ua[slot], a);
     };
 
@@ -1101,8 +1160,9 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
             }
         }
         PhaseScope scope(PH_ADJOINT, s, k1 - std::max(k0, 1));
+        const bool lvl = g.lvl16 && j >= g.jstore;  // (block-floating-point level k - k0_store)
         for (int k = k1 - 1; k >= std::max(k0, 1); --k)
-            if ((rc = adjoint_step(k, k - base + 1))) return rc;
+            if ((rc = lvl ? adjoint_step(k, k - g.k0_store, true) : adjoint_step(k, k - base + 1))) return rc;
     }
     if (grad_wavelet && p->nsrc > 0)  // q_1 at the sources -> d J / d w_0
         WFD_CUDA(launch_gather(w.Q[1], ga.cells, w.src_a, ga.ntiles, p->nshot, p->nsrc, w.m,
@@ -1315,7 +1375,7 @@ const char* wfd_strerror(int status) {
 
 const char* wfd_last_error(void) { return g_last_error.c_str(); }
 
-int wfd_version(void) { return (3 << 16) | 0; }  // major 3: wfd_problem.update_form
+int wfd_version(void) { return (3 << 16) | 1; }  // 3.0: update_form; 3.1: level_format
 
 int wfd_workspace_bytes(const wfd_problem* p, int with_gradient, size_t* bytes) {
     int rc = check_problem(p);

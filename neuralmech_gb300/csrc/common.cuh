@@ -163,6 +163,42 @@ __device__ __forceinline__ float comp(const float4& v, int e) {
     return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
 }
 
+// Block floating point of 4 cells (WFD_LEVEL_BFP16): mantissas q and one
+// exponent byte t with v = q 2^(t - 141), t the FP32 exponent field of the
+// block's largest magnitude M. M < 2^(t - 126) makes |v 2^(141 - t)| < 2^15, so
+// q = rint(v 2^(141 - t)) clamped to +-32767 keeps every value within 2^-15 of
+// 2^(t - 126). Both scalings are exact powers of two; blocks with t < 15
+// (M < 2^-112) are stored as 0, which keeps 2^(t - 141) a normal FP32 number.
+// A mantissa is stored as the 16 bits u = q + 32768. Both directions go
+// through FP32 values of exponent 23, whose low mantissa bits hold an integer
+// (B = 2^23 + 32768): rint(x) + B is fma(x, 1, B) rounded to the nearest
+// integer, ties to even, and the float with the bits 0x4B00 0000 | u is
+// 2^23 + u, so q 2^k = fma(2^23 + u, 2^k, -B 2^k) exactly. No integer/float
+// conversion instruction is involved.
+__device__ __forceinline__ void bfp4_encode(const float4& v, uint2& q, unsigned& t) {
+    const float M = fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
+    const int e = (__float_as_int(M) >> 23) & 0xff;
+    if (e < 15) {
+        q = make_uint2(0x80008000u, 0x80008000u);  // q = 0
+        t = 0u;
+        return;
+    }
+    const float inv = __int_as_float((268 - e) << 23);  // 2^(141 - e)
+    constexpr float B = 8421376.f;                        // 2^23 + 32768
+    auto m16 = [&](float x) { return __float_as_uint(fminf(fmaxf(fmaf(x, inv, B), B - 32767.f), B + 32767.f)); };
+    q = make_uint2(__byte_perm(m16(v.x), m16(v.y), 0x5410), __byte_perm(m16(v.z), m16(v.w), 0x5410));
+    t = unsigned(e);
+}
+
+__device__ __forceinline__ float4 bfp4_decode(uint2 q, unsigned t) {
+    const float sc = t ? __int_as_float(int(t - 14u) << 23) : 0.f;  // 2^(t - 141)
+    const float2 s2 = make_float2(sc, sc), c2 = make_float2(-8421376.f * sc, -8421376.f * sc);
+    auto f = [](unsigned w, unsigned sel) { return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)); };
+    const float2 lo = __ffma2_rn(make_float2(f(q.x, 0x7610), f(q.x, 0x7632)), s2, c2);
+    const float2 hi = __ffma2_rn(make_float2(f(q.y, 0x7610), f(q.y, 0x7632)), s2, c2);
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
 // L u at the four cells of a row: horizontal taps from (lv, cv, rv), vertical
 // taps from the register window V (centre row C). The cells go in pairs
 // through the packed FP32x2 arithmetic of sm_100+, with the operations and

@@ -36,7 +36,15 @@ enum StepMode : int {
     MODE_SUMMED = 4,    // update only, in the summed (increment) form (2D one-step and 3D kernels):
                         // the state is (u_n, d_n = u_n - u_{n-1}); map_old stages d_n,
                         // d_{n+1} goes to d_new in place and u_{n+1} = u_n + d_{n+1} to u_new
+    MODE_GRAD_U16 = 5,  // as MODE_GRAD_U with u_k kept in block floating point: map_lap stages
+                        // its int16 mantissas (box 144 x (tile_rows + 2R) x 1 at x0 - 8),
+                        // map_lx its exponent bytes (box 64 x (tile_rows + 2R) x 1 at x0/4 - 16)
 };
+
+// Kept levels in block floating point (WFD_LEVEL_BFP16): a level is
+// [nshot][nz][ld] int16 mantissas plus [nshot][nz][eld] exponent bytes, one per
+// 4 cells along x (eld = ld / 4 rounded up to 16 bytes, the TMA row pitch).
+inline int bfp_eld(int ld) { return (ld / 4 + 15) / 16 * 16; }
 
 // A set of points (sources or receivers) bucketed by the tile that owns them.
 // off[s * ntiles + t] .. off[s * ntiles + t + 1] index ent[], ent = {cell, p}
@@ -142,11 +150,13 @@ cudaError_t launch_vd_finalize(const float* G, const float* Gbx, const float* Gb
 // Launches one time step of the 2D kernel of half-width R (1, 2, 4), mode and
 // tile height tile_rows (16 or 32).
 // map_cur: u_n (box T2_W x (tile_rows + 2R) x 1); map_old: u_{n-1} (box
-// T2_TX x tile_rows x 1); map_lap: Laplacian store (box T2_TX x tile_rows x 1),
-// used by MODE_GRAD only.
+// T2_TX x tile_rows x 1); map_lap: Laplacian store (box T2_TX x tile_rows x 1,
+// MODE_GRAD), the level u_k (MODE_GRAD_U: the box of map_cur) or its mantissas
+// (MODE_GRAD_U16).
+// map_lx: MODE_GRAD_U16's exponent tiles (null otherwise).
 cudaError_t launch_step2d(int R, int mode, int tile_rows, const CUtensorMap& map_cur,
                           const CUtensorMap& map_old, const CUtensorMap& map_lap, const StepArgs& a,
-                          cudaStream_t s);
+                          cudaStream_t s, const CUtensorMap* map_lx = nullptr);
 
 // ---------------------------------------------------------------- 2D, two steps per launch
 // Tile T = K2_TX x K2_TZ cells; u_n is staged on T plus 2R rows / 8 columns
@@ -173,6 +183,14 @@ struct Step2Args {
     float* d_out;       // d_{n+2}, [nshot][cells]; may not alias the staged d_n
     float* d_mid;       // d_{n+1}, [nshot][cells] (write_mid or !two_steps)
     int write_mid;
+    // summed form: block-floating-point copies of the kept levels u_{n+1}
+    // (lq_mid, le_mid) and u_{n+2} (lq_out, le_out), null where not kept;
+    // mantissas [nshot][cells], exponents [nshot][nz][eld]
+    short* lq_mid;
+    unsigned char* le_mid;
+    short* lq_out;
+    unsigned char* le_out;
+    int eld;
 };
 
 // map_u: u_n (box K2_UW x (K2_TZ + 4R) x 1); map_o: u_{n-1}, or d_n in the summed form

@@ -31,6 +31,9 @@
 //     and L u_k formed in the kernel: the recompute then stores nothing but
 //     the levels it writes anyway. This mode runs on 16-row tiles: with the
 //     third tile, two stages of 32-row tiles would leave one CTA per SM.
+//   * MODE_GRAD_U16: MODE_GRAD_U for a level kept in block floating point
+//     (int16 mantissas, one exponent byte per 4 cells: 2.25 bytes per cell),
+//     each thread decoding the blocks it reads.
 //
 // MODE_SUMMED advances the same recursion in its summed (increment) form
 // (P. Henrici, Discrete Variable Methods in Ordinary Differential Equations,
@@ -61,22 +64,31 @@ struct Layout2D {
     static constexpr int H = TZ + 2 * R;
     static constexpr int CUR = H * T2_W * 4;  // TMA box bytes of u_n
     static constexpr int OLD = TZ * T2_TX * 4;
-    static constexpr int LAP = MODE == MODE_GRAD ? TZ * T2_TX * 4 : MODE == MODE_GRAD_U ? H * T2_W * 4 : 0;
+    // MODE_GRAD_U16: u_k's int16 mantissas (144 columns from x0 - 8) and
+    // exponent bytes (64, one per 4 cells from x0 - 64)
+    static constexpr int Q16 = H * (T2_TX + 16) * 2;
+    static constexpr int E8 = H * 64;
+    static constexpr int LAP = MODE == MODE_GRAD     ? TZ * T2_TX * 4
+                               : MODE == MODE_GRAD_U ? H * T2_W * 4
+                               : MODE == MODE_GRAD_U16 ? align_up(Q16, 128) + E8
+                                                       : 0;
     // every TMA destination starts on a 128-byte boundary
     static constexpr int CUR_AL = align_up(CUR, 128);
     static constexpr int OLD_AL = align_up(OLD, 128);
     static constexpr int STAGE = align_up(CUR_AL + OLD_AL + LAP, 128);
     // TMA stages in flight per CTA: three for the u-store adjoint, whose three
     // tiles per shot make a stage the longest to arrive
-    static constexpr int STAGES = MODE == MODE_GRAD_U ? 3 : T2_STAGES;
+    static constexpr bool GU = MODE == MODE_GRAD_U || MODE == MODE_GRAD_U16;
+    static constexpr int STAGES = GU ? 3 : T2_STAGES;
     static constexpr int BYTES = STAGES * STAGE + 64 + 128;  // + barriers + alignment slack
 };
 
 template <int R, int MODE, int RB>
-__global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U && MODE != MODE_SUMMED) ? 3 : 2)
+__global__ void __launch_bounds__(T2_THREADS, (RB == 2 && !Layout2D<R, MODE, RB>::GU && MODE != MODE_SUMMED) ? 3 : 2)
     step2d_kernel(const __grid_constant__ CUtensorMap map_cur,
                   const __grid_constant__ CUtensorMap map_old,
-                  const __grid_constant__ CUtensorMap map_lap, const StepArgs a) {
+                  const __grid_constant__ CUtensorMap map_lap,
+                  const __grid_constant__ CUtensorMap map_lx, const StepArgs a) {
     using L = Layout2D<R, MODE, RB>;
     constexpr int TZ = L::TZ;
     extern __shared__ unsigned char smem_raw[];
@@ -94,9 +106,10 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U &&
     if (ns <= 0) return;
 
     const uint32_t lap_bytes =
-        MODE == MODE_GRAD     ? uint32_t(TZ * T2_TX * (a.lap_bf16 ? 2 : 4))
-        : MODE == MODE_GRAD_U ? uint32_t(L::CUR)
-                              : 0u;
+        MODE == MODE_GRAD       ? uint32_t(TZ * T2_TX * (a.lap_bf16 ? 2 : 4))
+        : MODE == MODE_GRAD_U   ? uint32_t(L::CUR)
+        : MODE == MODE_GRAD_U16 ? uint32_t(L::Q16 + L::E8)
+                                : 0u;
     const uint32_t stage_tx = uint32_t(L::CUR + L::OLD) + lap_bytes;
     auto cur_buf = [&](int b) { return reinterpret_cast<float*>(base + b * L::STAGE); };
     auto old_buf = [&](int b) { return reinterpret_cast<float*>(base + b * L::STAGE + L::CUR_AL); };
@@ -110,6 +123,10 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U &&
         if (MODE == MODE_GRAD) tma_load_3d(lap_buf(b), &map_lap, x0, z0, s0 + i, &bars[b]);
         if (MODE == MODE_GRAD_U)  // u_k with the halo of u_n
             tma_load_3d(lap_buf(b), &map_lap, x0 - T2_XH, z0 - R, s0 + i, &bars[b]);
+        if (MODE == MODE_GRAD_U16) {  // its mantissas and exponents (16-byte aligned x: x0 - 8, x0/4 - 16)
+            tma_load_3d(lap_buf(b), &map_lap, x0 - 8, z0 - R, s0 + i, &bars[b]);
+            tma_load_3d(lap_buf(b) + align_up(L::Q16, 128), &map_lx, x0 / 4 - 16, z0 - R, s0 + i, &bars[b]);
+        }
     };
 
     // point-list ranges of this tile for every shot of the CTA, staged once
@@ -174,20 +191,30 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U &&
 
         // MODE_GRAD_U: L u_k of this thread's cells from the staged u_k tile,
         // times q_{k+1} at the cells into the gradient sum (before the q
-        // window is loaded, so that the two register windows never coexist)
-        if (MODE == MODE_GRAD_U) {
-            const float* ut = reinterpret_cast<const float*>(lap_buf(b));
+        // window is loaded, so that the two register windows never coexist).
+        // MODE_GRAD_U16 decodes each 4-cell block it reads from the staged
+        // mantissas (144 columns from x0 - 8) and exponents (from x0 - 64).
+        if (L::GU) {
+            // staged row j, 4-cell block c (cells x0 - 4 + 4 c, the u_n box's column 4 c)
+            auto u4 = [&](int j, int c) -> float4 {
+                if constexpr (MODE == MODE_GRAD_U16) {
+                    const unsigned char* st = lap_buf(b);
+                    const uint2 q = *reinterpret_cast<const uint2*>(st + (j * (T2_TX + 16) + 4 + 4 * c) * 2);
+                    return bfp4_decode(q, st[align_up(L::Q16, 128) + j * 64 + 15 + c]);
+                } else {
+                    return *reinterpret_cast<const float4*>(reinterpret_cast<const float*>(lap_buf(b)) + j * T2_W +
+                                                            4 * c);
+                }
+            };
             float4 W[RB + 2 * R];
 #pragma unroll
-            for (int j = 0; j < RB + 2 * R; ++j)
-                W[j] = *reinterpret_cast<const float4*>(ut + (warp * RB + j) * T2_W + T2_XH + 4 * lane);
+            for (int j = 0; j < RB + 2 * R; ++j) W[j] = u4(warp * RB + j, lane + 1);
 #pragma unroll
             for (int r = 0; r < RB; ++r) {
                 if (!zin[r]) continue;
-                const float* row = ut + (warp * RB + r + R) * T2_W + 4 * lane;
-                const float4 lv = *reinterpret_cast<const float4*>(row);
+                const float4 lv = u4(warp * RB + r + R, lane);
                 const float4 cv = W[r + R];
-                const float4 rv = *reinterpret_cast<const float4*>(row + 2 * T2_XH);
+                const float4 rv = u4(warp * RB + r + R, lane + 2);
                 const float4 qv =
                     *reinterpret_cast<const float4*>(cur + (warp * RB + r + R) * T2_W + T2_XH + 4 * lane);
                 const float4 lu = lap_row<R>(lv, cv, rv, W, r + R, a);
@@ -327,7 +354,7 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U &&
         }
     }
 
-    if (MODE == MODE_GRAD || MODE == MODE_GRAD_U) {
+    if (MODE == MODE_GRAD || L::GU) {
 #pragma unroll
         for (int r = 0; r < RB; ++r) {
             if (!zin[r]) continue;
@@ -345,7 +372,7 @@ __global__ void __launch_bounds__(T2_THREADS, (RB == 2 && MODE != MODE_GRAD_U &&
 
 template <int R, int MODE, int RB>
 cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
-                        const StepArgs& a_in, cudaStream_t s) {
+                        const CUtensorMap& mx, const StepArgs& a_in, cudaStream_t s) {
     const StepArgs a = with_weight_pairs(a_in);
     using L = Layout2D<R, MODE, RB>;
     static int configured_device = -1;
@@ -358,31 +385,35 @@ cudaError_t launch_impl(const CUtensorMap& mc, const CUtensorMap& mo, const CUte
         configured_device = dev;
     }
     const dim3 grid(a.tiles_x * a.tiles_z, (a.nshot + a.shots_per_cta - 1) / a.shots_per_cta);
-    const cudaError_t e = launch_pdl(step2d_kernel<R, MODE, RB>, grid, dim3(T2_THREADS), L::BYTES, s, mc, mo, ml, a);
+    const cudaError_t e =
+        launch_pdl(step2d_kernel<R, MODE, RB>, grid, dim3(T2_THREADS), L::BYTES, s, mc, mo, ml, mx, a);
     count_launch();
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <int R, int RB>
-cudaError_t dispatch_mode(int mode, const CUtensorMap& mc, const CUtensorMap& mo,
-                          const CUtensorMap& ml, const StepArgs& a, cudaStream_t s) {
+cudaError_t dispatch_mode(int mode, const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
+                          const CUtensorMap& mx, const StepArgs& a, cudaStream_t s) {
     switch (mode) {
-        case MODE_PLAIN: return launch_impl<R, MODE_PLAIN, RB>(mc, mo, ml, a, s);
-        case MODE_SAVE_LAP: return launch_impl<R, MODE_SAVE_LAP, RB>(mc, mo, ml, a, s);
-        case MODE_GRAD: return launch_impl<R, MODE_GRAD, RB>(mc, mo, ml, a, s);
-        case MODE_GRAD_U: return launch_impl<R, MODE_GRAD_U, RB>(mc, mo, ml, a, s);
-        case MODE_SUMMED: return launch_impl<R, MODE_SUMMED, RB>(mc, mo, ml, a, s);
+        case MODE_PLAIN: return launch_impl<R, MODE_PLAIN, RB>(mc, mo, ml, mx, a, s);
+        case MODE_SAVE_LAP: return launch_impl<R, MODE_SAVE_LAP, RB>(mc, mo, ml, mx, a, s);
+        case MODE_GRAD: return launch_impl<R, MODE_GRAD, RB>(mc, mo, ml, mx, a, s);
+        case MODE_GRAD_U: return launch_impl<R, MODE_GRAD_U, RB>(mc, mo, ml, mx, a, s);
+        case MODE_SUMMED: return launch_impl<R, MODE_SUMMED, RB>(mc, mo, ml, mx, a, s);
+        // (the u-store adjoint runs on 16-row tiles)
+        case MODE_GRAD_U16: return RB == 2 ? launch_impl<R, MODE_GRAD_U16, 2>(mc, mo, ml, mx, a, s)
+                                           : cudaErrorInvalidValue;
         default: return cudaErrorInvalidValue;
     }
 }
 
 template <int RB>
-cudaError_t dispatch_r(int R, int mode, const CUtensorMap& mc, const CUtensorMap& mo,
-                       const CUtensorMap& ml, const StepArgs& a, cudaStream_t s) {
+cudaError_t dispatch_r(int R, int mode, const CUtensorMap& mc, const CUtensorMap& mo, const CUtensorMap& ml,
+                       const CUtensorMap& mx, const StepArgs& a, cudaStream_t s) {
     switch (R) {
-        case 1: return dispatch_mode<1, RB>(mode, mc, mo, ml, a, s);
-        case 2: return dispatch_mode<2, RB>(mode, mc, mo, ml, a, s);
-        case 4: return dispatch_mode<4, RB>(mode, mc, mo, ml, a, s);
+        case 1: return dispatch_mode<1, RB>(mode, mc, mo, ml, mx, a, s);
+        case 2: return dispatch_mode<2, RB>(mode, mc, mo, ml, mx, a, s);
+        case 4: return dispatch_mode<4, RB>(mode, mc, mo, ml, mx, a, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -391,10 +422,12 @@ cudaError_t dispatch_r(int R, int mode, const CUtensorMap& mc, const CUtensorMap
 
 cudaError_t launch_step2d(int R, int mode, int tile_rows, const CUtensorMap& mc,
                           const CUtensorMap& mo, const CUtensorMap& ml, const StepArgs& a,
-                          cudaStream_t s) {
+                          cudaStream_t s, const CUtensorMap* mx) {
+    if (mode == MODE_GRAD_U16 && !mx) return cudaErrorInvalidValue;
+    const CUtensorMap& x = mx ? *mx : ml;
     switch (tile_rows) {
-        case 16: return dispatch_r<2>(R, mode, mc, mo, ml, a, s);
-        case 32: return dispatch_r<4>(R, mode, mc, mo, ml, a, s);
+        case 16: return dispatch_r<2>(R, mode, mc, mo, ml, x, a, s);
+        case 32: return dispatch_r<4>(R, mode, mc, mo, ml, x, a, s);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -81,6 +81,21 @@ __device__ __forceinline__ void store_level(float* p, const float4& v, bool zin,
     }
 }
 
+// A kept level's 4 cells at (shot base q, e; in-shot offset off = z ld + x, x a
+// multiple of 4) in block floating point; with ring, the fixed ring and row
+// padding (cells outside xin / zin) as 0, as store_level writes them.
+__device__ __forceinline__ void store_bfp(short* q, unsigned char* e, long long off, int z, int x, int eld,
+                                          float4 v, bool ring, bool zin, const bool* xin) {
+    if (ring)
+        v = make_float4(zin && xin[0] ? v.x : 0.f, zin && xin[1] ? v.y : 0.f, zin && xin[2] ? v.z : 0.f,
+                        zin && xin[3] ? v.w : 0.f);
+    uint2 qv;
+    unsigned t;
+    bfp4_encode(v, qv, t);
+    *reinterpret_cast<uint2*>(q + off) = qv;
+    e[(long long)z * eld + (x >> 2)] = (unsigned char)t;
+}
+
 // The summed update of 4 cells: (d_new, u_new) from (u, d, m, L u, g), the
 // one-step kernel's expression; g = 1 gives d + m L u.
 __device__ __forceinline__ void summed4(const float4& u, const float4& d, const float4& m, const float4& l,
@@ -109,7 +124,7 @@ __device__ __forceinline__ void summed4_plain(const float4& u, const float4& d, 
     un = make_float4(ul.x, ul.y, uh.x, uh.y);
 }
 
-template <int R, bool SUMMED>
+template <int R, bool SUMMED, bool LVL16 = false>
 __global__ void __launch_bounds__(K2_THREADS, 2)
     step2d_k2_kernel(const __grid_constant__ CUtensorMap map_u, const __grid_constant__ CUtensorMap map_o,
                      const __grid_constant__ CUtensorMap map_m, const Step2Args p) {
@@ -213,6 +228,12 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
         float* d_mid = SUMMED && p.d_mid ? p.d_mid + (long long)s * a.shot_stride : nullptr;
         float* d_out = SUMMED ? p.d_out + (long long)s * a.shot_stride : nullptr;
         const bool mid = !two || p.write_mid;  // (summed: the intermediate level leaves the CTA)
+        // block-floating-point copies of kept levels (summed form)
+        // (LVL16: the launch writes at least one of them)
+        short* lq_mid = LVL16 && p.lq_mid ? p.lq_mid + (long long)s * a.shot_stride : nullptr;
+        short* lq_out = LVL16 && p.lq_out ? p.lq_out + (long long)s * a.shot_stride : nullptr;
+        unsigned char* le_mid = lq_mid ? p.le_mid + (long long)s * a.nz * p.eld : nullptr;
+        unsigned char* le_out = lq_out ? p.le_out + (long long)s * a.nz * p.eld : nullptr;
 
         // ------------------------------------------------------------ step 1 on E
         auto step1 = [&](auto plain_c) {
@@ -338,6 +359,7 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
                         store_level(d_mid + off, f4(D1 + (tr + R) * K2_EW + 4 * lane), zin, xin, all_x,
                                     a.zero_ring, x_ok);
                 }
+                if (LVL16 && lq_mid && x_ok) store_bfp(lq_mid, le_mid, off, z, ex, p.eld, c1, !PLAIN, zin, xin);
                 if (!two) continue;
                 const float* nrow = O + (tr + R) * K2_EW + 4 * lane;
                 const float4 lv = f4(nrow - 4), rv = f4(nrow + 4);
@@ -361,6 +383,8 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
                         store_level(u_out + off, un, zin, xin, all_x, a.zero_ring, x_ok);
                         store_level(d_out + off, dn, zin, xin, all_x, a.zero_ring, x_ok);
                     }
+                    // (blocks holding a source of step n + 1 are encoded again after the injection)
+                    if (LVL16 && lq_out && x_ok) store_bfp(lq_out, le_out, off, z, ex, p.eld, un, !PLAIN, zin, xin);
                     continue;
                 }
                 const float4 l = lap_row<R>(lv, c1, rv, V, r + R, a);
@@ -414,11 +438,27 @@ __global__ void __launch_bounds__(K2_THREADS, 2)
                 atomicAdd(u_out + en.x, g * v);
                 if (SUMMED) atomicAdd(d_out + en.x, g * v);
             }
+            // the kept copy of u_{n+2}: the blocks of the injected cells again, from
+            // u_{n+2} in global memory once every injection of the tile is in (the
+            // condition is uniform over the CTA; a block's 4 cells lie in this tile)
+            if (LVL16 && lq_out && inj_rng[i].y > inj_rng[i].x) {
+                __syncthreads();
+                for (int j = lo + tid; j < hi; j += K2_THREADS) {
+                    const int2 en = a.inj.ent[j];
+                    const int z = en.x / a.ld, xx = (en.x - z * a.ld) & ~3;
+                    const long long off = (long long)z * a.ld + xx;
+                    const float4 v = __ldcg(reinterpret_cast<const float4*>(u_out + off));
+                    bool xi[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) xi[e] = xx + e >= R && xx + e < a.nx - R;
+                    store_bfp(lq_out, le_out, off, z, xx, p.eld, v, true, z >= R && z < a.nz - R, xi);
+                }
+            }
         }
     }
 }
 
-template <int R, bool SUMMED>
+template <int R, bool SUMMED, bool LVL16 = false>
 cudaError_t launch_impl(const CUtensorMap& mu, const CUtensorMap& mo, const CUtensorMap& mm, const Step2Args& p_in,
                         cudaStream_t s) {
     Step2Args p = p_in;
@@ -428,14 +468,14 @@ cudaError_t launch_impl(const CUtensorMap& mu, const CUtensorMap& mo, const CUte
     int dev = 0;
     cudaGetDevice(&dev);
     if (configured_device != dev) {
-        cudaError_t e = cudaFuncSetAttribute(step2d_k2_kernel<R, SUMMED>,
+        cudaError_t e = cudaFuncSetAttribute(step2d_k2_kernel<R, SUMMED, LVL16>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, L::BYTES);
         if (e != cudaSuccess) return e;
         configured_device = dev;
     }
     const dim3 grid(p.a.tiles_x * p.a.tiles_z, (p.a.nshot + p.a.shots_per_cta - 1) / p.a.shots_per_cta);
     const cudaError_t e =
-        launch_pdl(step2d_k2_kernel<R, SUMMED>, grid, dim3(K2_THREADS), L::BYTES, s, mu, mo, mm, p);
+        launch_pdl(step2d_k2_kernel<R, SUMMED, LVL16>, grid, dim3(K2_THREADS), L::BYTES, s, mu, mo, mm, p);
     count_launch();
     return e != cudaSuccess ? e : cudaGetLastError();
 }
@@ -447,6 +487,15 @@ cudaError_t launch_step2d_k2(int R, const CUtensorMap& map_u, const CUtensorMap&
     if (p.a.shots_per_cta < 1 || p.a.shots_per_cta > T2_MAX_SPC) return cudaErrorInvalidValue;
     if (p.summed && (!p.d_out || (p.write_mid && !p.d_mid) || (!p.two_steps && !p.d_mid)))
         return cudaErrorInvalidValue;
+    if (p.lq_mid || p.lq_out) {  // kept levels in block floating point (summed form only)
+        if (!p.summed) return cudaErrorInvalidValue;
+        switch (R) {
+            case 1: return launch_impl<1, true, true>(map_u, map_o, map_m, p, s);
+            case 2: return launch_impl<2, true, true>(map_u, map_o, map_m, p, s);
+            case 4: return launch_impl<4, true, true>(map_u, map_o, map_m, p, s);
+            default: return cudaErrorInvalidValue;
+        }
+    }
     switch (R * 2 + (p.summed ? 1 : 0)) {
         case 2: return launch_impl<1, false>(map_u, map_o, map_m, p, s);
         case 4: return launch_impl<2, false>(map_u, map_o, map_m, p, s);

@@ -39,6 +39,7 @@ LAP_STORES = {"auto": 0, "bf16": 1, "fp32": 2}
 FIELD_FORMATS = {"fp32": 0, "fp16": 1, "i16": 2}
 ADJOINT_MODES = {"checkpoint": 0, "reconstruct": 1}
 UPDATE_FORMS = {"auto": 0, "leapfrog": 1, "summed": 2}
+LEVEL_FORMATS = {"fp32": 0, "bfp16": 1}
 
 
 @dataclass(frozen=True)
@@ -68,10 +69,15 @@ class Grid:
     step_block   2D time steps per kernel launch, 1 or 2 (0 = 1); for a
              forward (no gradient) with the leapfrog update and FP32 fields
              also 8 at order 2 or 4 at order 4 (a register window per CTA)
-    store_levels FP32 levels the adjoint's workspace may hold (lap_store "auto"):
+    store_levels levels the adjoint's workspace may hold (lap_store "auto"):
              the forward keeps the levels of its last (store_levels - 2) // K
              segments and only the earlier ones are recomputed (0: the last
              segment only); see levels_for_budget()
+    level_format how those kept levels are stored: "fp32" (4 B per cell) or
+             "bfp16" (block floating point: int16 mantissas and one exponent
+             byte per 4 cells along x, 2.25 B per cell, each value within 2^-15
+             of its block's largest; about 1.8x the kept levels in the same
+             memory; 2D, step_block 2, the summed forward)
     field_format storage of the wavefields in a forward without gradient (2D):
              "fp32", "fp16" or "i16" (int16 with one FP32 scale per 32 cells
              along x); arithmetic is FP32 in every format
@@ -109,6 +115,7 @@ class Grid:
     field_format: str = "fp32"
     adjoint: str = "checkpoint"
     update: str = "auto"
+    level_format: str = "fp32"
 
     @property
     def ndim(self) -> int:
@@ -135,11 +142,18 @@ def fd_weights(order: int) -> np.ndarray:
 
 
 def levels_for_budget(grid: Grid, nshot: int, budget_bytes: float) -> int:
-    """store_levels that fit `budget_bytes` of FP32 levels (nshot fields of the
-    grid, rows padded to 8 cells)."""
+    """store_levels that fit `budget_bytes` of kept levels in the grid's
+    level_format (nshot fields of the grid, rows padded to 8 cells; "bfp16":
+    2-byte mantissas plus one exponent byte per 4 cells, exponent rows padded
+    to 16 bytes)."""
     nx = grid.shape[-1]
-    cells = int(np.prod(grid.shape[:-1])) * ((nx + 7) // 8 * 8)
-    return max(0, int(budget_bytes // (4 * cells * nshot)))
+    ld = (nx + 7) // 8 * 8
+    rows = int(np.prod(grid.shape[:-1]))
+    if grid.level_format == "bfp16":
+        per = nshot * rows * (2 * ld + (ld // 4 + 15) // 16 * 16)
+    else:
+        per = 4 * nshot * rows * ld
+    return max(0, int(budget_bytes // per))
 
 
 def stable_dt(spacing, vmax: float, order: int = 8) -> float:
@@ -189,7 +203,8 @@ def _problem(grid: Grid, nshot: int, nsrc: int, nrec: int, vmax: float) -> _lib.
                         grid.shots_per_cta, grid.group_shots, grid.tile_rows, grid.step_block, grid.store_levels,
                         FIELD_FORMATS[grid.field_format], ADJOINT_MODES[grid.adjoint],
                         max(max(w) for w in grid.sponge_widths()) if grid.adjoint == "reconstruct" else 0,
-                        grid.dt, dz, dy, dx, grid.src_scale, vmax, UPDATE_FORMS[grid.update])
+                        grid.dt, dz, dy, dx, grid.src_scale, vmax, UPDATE_FORMS[grid.update],
+                        LEVEL_FORMATS[grid.level_format])
 
 
 # ---------------------------------------------------------------- argument prep

@@ -54,6 +54,7 @@ static int layout(void) {
     FIELD(shots_per_cta); FIELD(group_shots); FIELD(tile_rows); FIELD(step_block);
     FIELD(store_levels); FIELD(field_format); FIELD(adjoint_mode); FIELD(recon_band);
     FIELD(dt); FIELD(dz); FIELD(dy); FIELD(dx); FIELD(src_scale); FIELD(vmax); FIELD(update_form);
+    FIELD(level_format);
     return 0;
 }
 

@@ -80,6 +80,38 @@ def test_update_form_checks_and_workspace():
         assert rc == _lib.WFD_ERR_INVALID, bad
 
 
+def test_block_float_levels_workspace_and_checks():
+    """WFD_LEVEL_BFP16 keeps the same levels in 2.25 instead of 4 bytes per
+    cell; the region also holds the K + 2 FP32 slots of a recomputed segment.
+    It needs the two-step summed forward."""
+    from neuralmech_gb300 import _lib
+    field = 2 * 64 * 104 * 4
+    slot = (field + 255) // 256 * 256
+    q16 = (2 * 64 * 104 * 2 + 255) // 256 * 256
+    e8 = (2 * 64 * 32 + 255) // 256 * 256  # exponent rows of 104 / 4 bytes padded to 32
+    kw = dict(nt=100, ckpt_every=10, step_block=2, store_levels=45)  # 4 kept segments: u_60 .. u_99
+    rc32, n32 = _ws(_problem(**kw))
+    rc16, n16 = _ws(_problem(level_format=1, **kw))
+    assert rc32 == 0 and rc16 == 0
+    assert n32 - n16 == 42 * slot - 40 * (q16 + e8)
+    # the same budget in bytes holds more levels
+    from neuralmech_gb300 import Grid, levels_for_budget
+    g = Grid((64, 100), (10.0, 10.0), 1e-3, 100)
+    b = 10 ** 9
+    l32 = levels_for_budget(g, 2, b)
+    l16 = levels_for_budget(Grid((64, 100), (10.0, 10.0), 1e-3, 100, level_format="bfp16"), 2, b)
+    assert l32 == b // field and l16 == b // (2 * 64 * (2 * 104 + 32))
+    assert 1.7 < l16 / l32 < 1.9
+    for bad in (dict(level_format=2), dict(level_format=-1), dict(level_format=1),  # step_block 1
+                dict(level_format=1, step_block=2, update_form=1),
+                dict(level_format=1, step_block=2, lap_store=2),
+                dict(level_format=1, step_block=2, field_format=1)):
+        rc, _ = _ws(_problem(**bad))
+        assert rc == _lib.WFD_ERR_INVALID, bad
+    _ws(_problem(level_format=1))
+    assert "block-floating-point levels" in _lib.load().wfd_last_error().decode()
+
+
 def test_workspace_bytes_grows_with_gradient():
     rc0, n0 = _ws(_problem(), 0)
     rc1, n1 = _ws(_problem(), 1)

@@ -332,6 +332,40 @@ def test_two_step_matches_one_step_autograd(cuda, orc):
     assert rel_l2(grads[1], grads[0]) < 1e-5
 
 
+@pytest.mark.parametrize("nt,ckpt,levels", [(101, 15, 40), (90, 9, 200), (64, 64, 0), (77, 10, 10 ** 6)])
+def test_block_float_levels(cuda, orc, nt, ckpt, levels):
+    """Kept levels in block floating point (level_format "bfp16": int16
+    mantissas, one exponent byte per 4 cells) against FP32 kept levels, with
+    some segments kept and the rest recomputed, only the last kept (levels 0,
+    here the only one, from u_0), and every one kept (10^6); odd step counts and
+    checkpoint intervals; a source on a tile seam (its block encoded again after
+    the injection). Only the adjoint's u_k differ, by the 2^-15 block rounding:
+    the misfits agree to 1e-12 and the wavelet gradients (which do not see u_k)
+    to 1e-6; the velocity gradients within 3e-4 of each other and of the FP64
+    oracle."""
+    import dataclasses
+    from neuralmech_gb300 import misfit_gradient
+    grid, v, wav, src, rec = small_problem(shape=(70, 250), nshot=3, nt=nt, ckpt_every=ckpt, seed=31, nrec=24,
+                                           ckpt_format="fp32")
+    src[0, 0] = [32, 120]  # on a tile seam of the two-step kernel
+    src[1, 0] = [33, 119]
+    grid = dataclasses.replace(grid, step_block=2, store_levels=levels)
+    obs = _observed(orc, grid, v, wav, src, rec)
+    args = (torch.from_numpy(v).to(cuda), torch.from_numpy(wav).to(cuda), torch.from_numpy(src),
+            torch.from_numpy(rec), torch.from_numpy(obs).to(cuda))
+    J32, g32, w32 = misfit_gradient(*args, grid, want_wavelet=True)
+    J16, g16, w16 = misfit_gradient(*args, dataclasses.replace(grid, level_format="bfp16"), want_wavelet=True)
+    assert abs(J16.item() - J32.item()) <= 1e-12 * J32.item()
+    assert rel_l2(w16.cpu().numpy(), w32.cpu().numpy()) < 1e-6
+    e16 = rel_l2(g16.cpu().numpy(), g32.cpu().numpy())
+    Jr, gr, _, _ = orc.gradient(oracle_geometry(orc, grid, v, wav, src, rec), obs)
+    e_or = rel_l2(g16.cpu().numpy(), gr)
+    print(f"bfp16 levels: vs FP32 levels {e16:.2e}, vs FP64 oracle {e_or:.2e} "
+          f"(FP32 levels {rel_l2(g32.cpu().numpy(), gr):.2e})")
+    assert 0 < e16 < 3e-4
+    assert e_or < 3e-4
+
+
 @pytest.mark.parametrize("nt,ckpt,levels", [(101, 15, 0), (90, 9, 40), (64, 64, 0)])
 def test_summed_two_step_matches_one_step(cuda, orc, nt, ckpt, levels):
     """The summed forward with two steps per launch (d_{n+1} kept on chip,

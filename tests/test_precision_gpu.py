@@ -16,7 +16,8 @@ two of its 64 shots, against the FP64 oracle.
   rounding and meets it, with FP32, BF16 and int16 checkpoints alike: every
   segment but the last is recomputed from a checkpoint here (store_levels 0).
   The benchmark's configuration, two steps per launch (whose summed kernel
-  forms L u in the centre-weight form), meets it too (4.7e-4).
+  forms L u in the centre-weight form), meets it too (4.7e-4), and so it does
+  with every level kept in block floating point (level_format "bfp16").
 """
 import dataclasses
 
@@ -55,10 +56,19 @@ def test_fwi1024_two_shots_against_fp64(cuda, orc):
         key = (form, fmt) if sb == 1 else (form, fmt, "two steps per launch")
         errs[key] = rel_l2(gv.cpu().numpy(), gr)
         e_J[key] = abs(float(J) - Jr) / Jr
+    # every level kept in block floating point (level_format "bfp16"): no
+    # segment recomputed, the adjoint's u_k rounded to 2^-15 of their 4-cell block
+    key = ("auto", "bf16", "two steps per launch", "bfp16 levels")
+    J, gv = misfit_gradient(*args, torch.from_numpy(obs).to(cuda),
+                            dataclasses.replace(g, ckpt_format="bf16", step_block=2, store_levels=10 ** 6,
+                                                level_format="bfp16"))
+    errs[key] = rel_l2(gv.cpu().numpy(), gr)
+    e_J[key] = abs(float(J) - Jr) / Jr
     print(f"fwi1024 (2 shots): traces rel L2 {e_tr}; gradient rel L2 {errs}; misfit rel {e_J}")
     assert e_tr["leapfrog"] < 1e-5 and e_tr["summed"] < 1e-5
     assert e_tr["summed"] < 0.5 * e_tr["leapfrog"]
-    for key in (("auto", "fp32"), ("auto", "i16"), ("auto", "bf16"), ("auto", "bf16", "two steps per launch")):
+    for key in (("auto", "fp32"), ("auto", "i16"), ("auto", "bf16"), ("auto", "bf16", "two steps per launch"),
+                ("auto", "bf16", "two steps per launch", "bfp16 levels")):
         assert errs[key] <= 1e-3, key
         assert e_J[key] <= 5e-3, key
     # the leapfrog form's floor: the documented miss of the 1e-3 bound

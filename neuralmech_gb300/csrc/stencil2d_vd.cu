@@ -290,9 +290,32 @@ __global__ void __launch_bounds__(VD_THREADS, 2)
             __syncthreads();
             divergence(lbu);
             __syncthreads();  // the flux buffers are free again
+            // G += q_{k+1} Lb u_k now, so that Lb u_k is no longer live
+#pragma unroll
+            for (int r = 0; r < VD_RB; ++r) {
+                if (!zin[r]) continue;
+                const float4 cv = ld4(F + (warp * VD_RB + r + 2 * R) * VD_W + 8 + 4 * lane);
+                gk[r].x += xin[0] ? cv.x * lbu[r].x : 0.f;
+                gk[r].y += xin[1] ? cv.y * lbu[r].y : 0.f;
+                gk[r].z += xin[2] ? cv.z * lbu[r].z : 0.f;
+                gk[r].w += xin[3] ? cv.w * lbu[r].w : 0.f;
+            }
         }
         float4 dxq[VD_RB], dzq[VD_RB], lb[VD_RB];
         fluxes(F, dxq, dzq);
+        if (MODE == MODE_GRAD_U) {  // the half-point terms now: the four differences die here
+#pragma unroll
+            for (int r = 0; r < VD_RB; ++r) {
+                gbx[r].x -= dxq[r].x * dxu[r].x;
+                gbx[r].y -= dxq[r].y * dxu[r].y;
+                gbx[r].z -= dxq[r].z * dxu[r].z;
+                gbx[r].w -= dxq[r].w * dxu[r].w;
+                gbz[r].x -= a.vd_sz * dzq[r].x * dzu[r].x;
+                gbz[r].y -= a.vd_sz * dzq[r].y * dzu[r].y;
+                gbz[r].z -= a.vd_sz * dzq[r].z * dzu[r].z;
+                gbz[r].w -= a.vd_sz * dzq[r].w * dzu[r].w;
+            }
+        }
         __syncthreads();
         // MODE_GRAD_U: u_{n-1} comes from global memory (plain loads: u_new is
         // this level's buffer, each cell read here and written below); issued
@@ -329,22 +352,6 @@ __global__ void __launch_bounds__(VD_THREADS, 2)
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
                     if (xin[e]) un[off + e] = nv[e];
-            }
-            if (MODE == MODE_GRAD_U) {
-                if (zin[r]) {
-                    gk[r].x += xin[0] ? cv.x * lbu[r].x : 0.f;
-                    gk[r].y += xin[1] ? cv.y * lbu[r].y : 0.f;
-                    gk[r].z += xin[2] ? cv.z * lbu[r].z : 0.f;
-                    gk[r].w += xin[3] ? cv.w * lbu[r].w : 0.f;
-                }
-                gbx[r].x -= dxq[r].x * dxu[r].x;
-                gbx[r].y -= dxq[r].y * dxu[r].y;
-                gbx[r].z -= dxq[r].z * dxu[r].z;
-                gbx[r].w -= dxq[r].w * dxu[r].w;
-                gbz[r].x -= a.vd_sz * dzq[r].x * dzu[r].x;
-                gbz[r].y -= a.vd_sz * dzq[r].y * dzu[r].y;
-                gbz[r].z -= a.vd_sz * dzq[r].z * dzu[r].z;
-                gbz[r].w -= a.vd_sz * dzq[r].w * dzu[r].w;
             }
         }
 

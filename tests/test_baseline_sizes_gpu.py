@@ -9,11 +9,12 @@
     checkpoints (every shot's segments but the last recomputed): the errors
     are stated (printed) and bounded by 1e-3, the bound of the 2D gradient;
   * fwi384_3d: the full 384^3 grid and 1500 steps, one shot with its 64 x 64
-    receivers, checkpoints every 39 in BF16 and in FP32, the gradient's
-    forward in the summed form (the default): traces within 1e-5, the
-    gradient errors stated, and bounded beyond 6 cells of the source by 5e-3
-    (BF16) and 1e-3 (FP32; measured 2.1e-3 and 6.0e-4, against 7.1e-3 and
-    1.3e-3 with the leapfrog forward). At the source cell the imaging sum
+    receivers, checkpoints every 39 in BF16, int16 (one scale per 32 cells)
+    and FP32, the gradient's forward in the summed form (the default):
+    traces within 1e-5, the gradient errors stated, and bounded beyond 6
+    cells of the source by 5e-3 (BF16) and 1e-3 (int16, FP32; measured 2.1e-3
+    and 6.0e-4 for BF16 and FP32, against 7.1e-3 and 1.3e-3 with the leapfrog
+    forward). At the source cell the imaging sum
     q L u meets the point source's singular L u: there the FP32 sum over the
     steps keeps an absolute error (about 2e-8 on 192^3 whatever the residual)
     that dominates when the residual, and with it the gradient, is small, as
@@ -105,7 +106,7 @@ def test_fwi384_3d_full_grid(cuda, orc):
     s0 = src[0, 0]
     far = (zz - s0[0]) ** 2 + (yy - s0[1]) ** 2 + (xx - s0[2]) ** 2 > 36
     errs, errs_far = {}, {}
-    for fmt in ("bf16", "fp32"):
+    for fmt in ("bf16", "i16", "fp32"):
         J, gv = misfit_gradient(*args, torch.from_numpy(obs).to(cuda), dataclasses.replace(g, ckpt_format=fmt))
         gv = gv.cpu().numpy()
         errs[fmt] = rel_l2(gv, gr)
@@ -117,3 +118,5 @@ def test_fwi384_3d_full_grid(cuda, orc):
           f"{errs_far} (the source's neighbourhood holds {share:.2e} of the gradient's norm)")
     assert e_tr < 1e-5
     assert errs_far["bf16"] <= 5e-3 and errs_far["fp32"] <= 1e-3, errs_far
+    # 16-bit checkpoints with a scale per 32 cells (2.125 B per cell, 6% over BF16)
+    assert errs_far["i16"] <= 1e-3, errs_far

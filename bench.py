@@ -647,7 +647,9 @@ def _wl_batch8(args, dev):
         models.append(dict(vel=v, wavelet=wav, src=src, rec=rec, observed=obs, grid=w.grid))
     budget = args.level_store_frac * torch.cuda.get_device_properties(dev).total_memory
     batch = BatchFWI(models, autotune=True, level_budget=budget)
-    graph_kernels = batch.graph_kernels  # replays launch these without a host call each
+    # wfd_batch_run adds the kernels of each replay to wfd_kernel_launches itself
+    graph_kernels = 0
+    extra["graph_kernels_per_replay"] = batch.graph_kernels
     step = batch.run
     if args.timeline:
         # the same batch with a tenth of the steps (the same grids, kernels and

@@ -286,6 +286,41 @@ int wfd_tfm(const float* h, int E, const float* xe, const float* ye, int nt, flo
             float c, const float* xp, const float* yp, int npix, int reciprocity, float* image,
             void* stream);
 
+/*
+ * Batches of independent misfit gradients (several models of different sizes,
+ * each with its own shots and workspace) replayed as one CUDA graph: the
+ * graph-captured batch of the reference's graph driver
+ * (projects/18_simple_wave_fd/2D_wave_cuda_graph.py:73-95) for whole gradients.
+ * An item holds the arguments of one wfd_misfit_gradient call (device
+ * pointers; the workspace sized with with_gradient = 1).
+ *
+ * wfd_batch_plan runs every item once on a stream of its own, forked from and
+ * joined to `stream` (this checks the arguments and configures the kernels;
+ * the outputs hold that run's results), then records the same calls as one
+ * CUDA graph with the items on parallel branches. The items and their
+ * problem structs are copied; the device buffers they point to must stay
+ * valid for the plan's life. wfd_batch_run launches the graph on `stream`:
+ * the gradients of the buffers' current contents (write new velocities or
+ * observed data into the same buffers between runs). Device-side errors go to
+ * each item's workspace (wfd_status). wfd_batch_launches: kernels one run
+ * launches. No counterpart in the reference's API beyond the graph driver.
+ */
+typedef struct wfd_batch_item {
+    const wfd_problem* problem;
+    const float *vel, *sponge_z, *sponge_y, *sponge_x, *wavelet;
+    const int32_t *src, *rec;
+    const float* observed;
+    float *traces, *grad_vel, *grad_wavelet; /* traces, grad_wavelet may be NULL */
+    double* misfit;
+    void* workspace;
+    size_t workspace_bytes;
+} wfd_batch_item;
+typedef struct wfd_batch wfd_batch; /* opaque */
+int wfd_batch_plan(const wfd_batch_item* items, int count, void* stream, wfd_batch** out);
+int wfd_batch_run(wfd_batch* batch, void* stream);
+uint64_t wfd_batch_launches(const wfd_batch* batch);
+int wfd_batch_free(wfd_batch* batch);
+
 /* Synchronises `stream`, returns the first device-side error recorded in the
  * workspace since the last call (WFD_ERR_TIMEOUT, WFD_ERR_POSITION) or 0, and
  * clears it. */

@@ -31,6 +31,7 @@ EXPORTS = (
     "wfd_analytic_signal", "wfd_tfm", "wfd_forward_final", "wfd_step2d_mixed", "wfd_step2d_mixed_fast", "wfd_step2d_scaled",
     "wfd_temporal_step", "wfd_temporal_step_fast", "wfd_step2d_exact", "wfd_misfit_gradient_overlap",
     "wfd_step1d", "wfd_vd_workspace_bytes", "wfd_vd_forward", "wfd_vd_forward_final", "wfd_vd_misfit_gradient",
+    "wfd_batch_plan", "wfd_batch_run", "wfd_batch_launches", "wfd_batch_free",
 )
 
 
@@ -55,6 +56,14 @@ class Problem(ctypes.Structure):
         ("dx", ctypes.c_float), ("src_scale", ctypes.c_float), ("vmax", ctypes.c_float),
         ("update_form", ctypes.c_int32), ("level_format", ctypes.c_int32),
     ]
+
+
+class BatchItem(ctypes.Structure):
+    """Mirror of ``wfd_batch_item`` (include/wavefd.h): one wfd_misfit_gradient call."""
+    _fields_ = [("problem", ctypes.POINTER(Problem))] + [
+        (n, ctypes.c_void_p) for n in ("vel", "sponge_z", "sponge_y", "sponge_x", "wavelet", "src", "rec",
+                                       "observed", "traces", "grad_vel", "grad_wavelet", "misfit", "workspace")
+    ] + [("workspace_bytes", ctypes.c_size_t)]
 
 
 class WaveFDError(RuntimeError):
@@ -118,10 +127,15 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         lib.wfd_vd_misfit_gradient.argtypes = [P, f, f, f, f, f, i32, i32, f, f, f, f, f, d, vp, sz, vp]
         lib.wfd_kernel_launches.argtypes = []
         lib.wfd_kernel_launches.restype = ctypes.c_uint64
+        lib.wfd_batch_plan.argtypes = [ctypes.POINTER(BatchItem), ctypes.c_int, vp, ctypes.POINTER(vp)]
+        lib.wfd_batch_run.argtypes = [vp, vp]
+        lib.wfd_batch_launches.argtypes = [vp]
+        lib.wfd_batch_launches.restype = ctypes.c_uint64
+        lib.wfd_batch_free.argtypes = [vp]
         lib.wfd_profile_begin.argtypes = []
         lib.wfd_profile_end.argtypes = [ctypes.POINTER(PhaseTimes)]
         for name in EXPORTS:
-            if name not in ("wfd_strerror", "wfd_last_error", "wfd_kernel_launches"):
+            if name not in ("wfd_strerror", "wfd_last_error", "wfd_kernel_launches", "wfd_batch_launches"):
                 getattr(lib, name).restype = ctypes.c_int
         _lib = lib
         return lib

@@ -10,24 +10,26 @@ This is the fwi workload family of many surveys at once (e.g. 8 models
     the forward of a gradient: the summed update form where the grid asks
     for it);
   * it allocates every workspace and output once;
-  * it captures one CUDA graph in which each model's checkpointed
-    forward + adjoint (``wfd_misfit_gradient``) runs on its own stream branch,
-    forked from and joined to the capturing stream, so the GPU overlaps the
-    models' step kernels;
-  * ``run()`` replays that graph: one host call per batch gradient.
+  * the library plans the batch (``wfd_batch_plan``): it runs each model's
+    checkpointed forward + adjoint (``wfd_misfit_gradient``) once on a stream
+    of its own and records the same calls as one CUDA graph with the models
+    on parallel branches, so the GPU overlaps the models' step kernels;
+  * ``run()`` replays that graph (``wfd_batch_run``): one host call per batch
+    gradient.
 
 Inputs live in tensors owned by the batch. ``set_velocity`` / ``set_observed``
 update them in place, so the next replay sees the new values.
 """
 from __future__ import annotations
 
+import ctypes
 import dataclasses
 
 import torch
 
 from . import _lib
 from . import autotune as _autotune
-from .wavefd import Grid, _misfit_gradient_into, _prepare, _workspace, levels_for_budget
+from .wavefd import Grid, _misfit_gradient_into, _prepare, _ptr, _stream, _workspace, levels_for_budget
 
 
 def _level_shares(models, budget: float) -> list:
@@ -95,18 +97,34 @@ class BatchFWI:
                                       torch.cuda.Stream(device=self.device)))
         self.configs = [(x.call.grid.tile_rows, x.call.grid.shots_per_cta, x.call.grid.step_block)
                         for x in self.models]
-        self.graph = None
-        self._launch()  # eager run: sets kernel attributes, validates arguments
+        self.graph = None  # the library's batch plan (its graph), when graph=True
+        self.graph_kernels = 0  # kernels of one replay
+        if not graph:
+            self._launch()  # eager run: validates arguments
+            torch.cuda.synchronize(self.device)
+            return
+        self._items = (_lib.BatchItem * len(self.models))()
+        for it, m in zip(self._items, self.models):
+            gz, gy, gx = m.call.sponges
+            it.problem = ctypes.pointer(m.call.problem)
+            for name, t in (("vel", m.call.vel), ("sponge_z", gz), ("sponge_y", gy), ("sponge_x", gx),
+                            ("wavelet", m.call.wavelet), ("src", m.call.src), ("rec", m.call.rec),
+                            ("observed", m.observed), ("grad_vel", m.grad), ("misfit", m.misfit),
+                            ("workspace", m.ws)):
+                setattr(it, name, _ptr(t))
+            it.workspace_bytes = m.ws.numel()
+        lib = _lib.load()
+        plan = ctypes.c_void_p()
+        _lib.check(lib.wfd_batch_plan(self._items, len(self.models), _stream(), ctypes.byref(plan)),
+                   "wfd_batch_plan")
+        self.graph = plan
+        self.graph_kernels = int(lib.wfd_batch_launches(plan))
         torch.cuda.synchronize(self.device)
-        # kernels of one replay: what the library launched while the graph was captured
-        self.graph_kernels = 0
-        if graph:
-            lib = _lib.load()
-            n0 = lib.wfd_kernel_launches()
-            self.graph = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(self.graph):
-                self._launch()
-            self.graph_kernels = int(lib.wfd_kernel_launches() - n0)
+
+    def __del__(self):
+        if getattr(self, "graph", None) is not None and _lib is not None:
+            _lib.load().wfd_batch_free(self.graph)
+            self.graph = None
 
     def _launch(self):
         main = torch.cuda.current_stream(self.device)
@@ -126,7 +144,7 @@ class BatchFWI:
     def run(self):
         """(misfits float64 [n_models], [grad_vel per model]) of the current inputs."""
         if self.graph is not None:
-            self.graph.replay()
+            _lib.check(_lib.load().wfd_batch_run(self.graph, _stream()), "wfd_batch_run")
         else:
             self._launch()
         return torch.stack([m.misfit for m in self.models]), [m.grad for m in self.models]

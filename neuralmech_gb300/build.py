@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libwavefd.so")
-SOURCES = ["stencil2d.cu", "stencil2d_k2.cu", "stencil3d.cu", "aux.cu", "api.cu", "static_scratch.cu",
+SOURCES = ["stencil2d.cu", "stencil2d_k2.cu", "stencil3d.cu", "aux.cu", "api.cu", "static_scratch.cu", "batch.cu",
            "imaging.cu", "dropin.cu", "stencil2d_lp.cu", "stencil2d_vd.cu", "stencil2d_reg.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

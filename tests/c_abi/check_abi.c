@@ -18,6 +18,8 @@
  *                     - wfd_misfit_gradient against zero observed data (J equals
  *                       half the sum of squares of its own traces; the gradient
  *                       is finite, nonzero, and zero on the fixed ring);
+ *                     - the same gradient twice in one planned batch (one CUDA
+ *                       graph), replayed twice: each item as the single call;
  *                     - a source on the fixed ring reported by wfd_status as
  *                       WFD_ERR_POSITION (the kernel skips that point).
  * Exit status 0 when every check holds; each failed check prints one line.
@@ -117,6 +119,11 @@ static int host(void) {
     CHECK(wfd_step2d_order2(NULL, NULL, NULL, 1.0f, 1.0f, 1.0f, 1.0f, 10, 10, 12, NULL) == WFD_ERR_INVALID,
           "wfd_step2d_order2 with NULL fields");
     CHECK(wfd_status(NULL, NULL) == WFD_ERR_WORKSPACE, "wfd_status without a workspace");
+    wfd_batch* none = NULL;
+    wfd_batch_item empty[2];
+    memset(empty, 0, sizeof empty);
+    CHECK(wfd_batch_plan(empty, 2, NULL, &none) == WFD_ERR_INVALID && none == NULL, "batch item without a problem");
+    CHECK(wfd_batch_plan(empty, 0, NULL, &none) == WFD_ERR_INVALID, "empty batch");
     CHECK(wfd_kernel_launches() == 0, "a host-only call launched a kernel");
     return failures;
 }
@@ -289,6 +296,45 @@ static int gpu(void) {
     CHECK(finite && ring == 0.0 && inner > 0.0, "gradient: finite %d, ring %.3e, interior %.3e", finite, ring,
           inner);
     free(g);
+
+    /* the same gradient as a two-item batch (one graph): each item against the single call */
+    {
+        float* d_g2[2];
+        double* d_J2[2];
+        void* ws2[2];
+        wfd_batch_item it[2];
+        memset(it, 0, sizeof it);
+        for (int i = 0; i < 2; ++i) {
+            d_g2[i] = dalloc(cells * sizeof(float));
+            d_J2[i] = dalloc(sizeof(double));
+            ws2[i] = dalloc(wsb);
+            it[i].problem = &p;
+            it[i].vel = d_vel; it[i].wavelet = d_wav; it[i].src = d_src; it[i].rec = d_rec;
+            it[i].observed = d_obs; it[i].grad_vel = d_g2[i]; it[i].misfit = d_J2[i];
+            it[i].workspace = ws2[i]; it[i].workspace_bytes = wsb;
+        }
+        wfd_batch* bt = NULL;
+        CHECK(wfd_batch_plan(it, 2, NULL, &bt) == WFD_OK && bt != NULL, "wfd_batch_plan");
+        CHECK(wfd_batch_launches(bt) > 0, "batch graph without kernels");
+        float* g1 = malloc(cells * sizeof(float));
+        float* g2 = malloc(cells * sizeof(float));
+        cudaMemcpy(g1, d_g, cells * sizeof(float), D2H);
+        for (int rep = 0; rep < 2; ++rep) {
+            for (int i = 0; i < 2; ++i) cudaMemset(d_g2[i], 0, cells * sizeof(float));
+            CHECK(wfd_batch_run(bt, NULL) == WFD_OK, "wfd_batch_run");
+            for (int i = 0; i < 2; ++i) {
+                double Jb = 0.0;
+                cudaMemcpy(&Jb, d_J2[i], sizeof Jb, D2H);
+                cudaMemcpy(g2, d_g2[i], cells * sizeof(float), D2H);
+                CHECK(fabs(Jb - J) <= 1e-9 * J, "batch misfit %.9e against %.9e", Jb, J);
+                CHECK(rel_diff(g2, g1, cells) <= 1e-6, "batch gradient %.3e", rel_diff(g2, g1, cells));
+                CHECK(wfd_status(ws2[i], NULL) == WFD_OK, "wfd_status of a batch item");
+            }
+        }
+        CHECK(wfd_batch_free(bt) == WFD_OK, "wfd_batch_free");
+        for (int i = 0; i < 2; ++i) { cudaFree(d_g2[i]); cudaFree(d_J2[i]); cudaFree(ws2[i]); }
+        free(g1); free(g2);
+    }
 
     /* a source on the fixed ring: reported on the device, the point skipped */
     int32_t bad[2][1][3] = {{{1, 0, 30}}, {{6, 0, 70}}};

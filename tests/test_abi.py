@@ -311,3 +311,21 @@ def test_register_window_step_blocks():
            dict(step_block=8, order=2, ndim=3, ny=20, nz=24, nx=40, vmax=2000.0, dy=10.0)]
     for kw in bad:
         assert _ws(_problem(**kw), 0)[0] == _lib.WFD_ERR_INVALID, kw
+
+
+def test_batch_plan_arguments_rejected():
+    """wfd_batch_plan checks its arguments before any CUDA call."""
+    from neuralmech_gb300 import _lib
+    lib = _lib.load()
+    out = ctypes.c_void_p(123)
+    items = (_lib.BatchItem * 2)()
+    assert lib.wfd_batch_plan(items, 2, None, None) == _lib.WFD_ERR_INVALID
+    assert lib.wfd_batch_plan(None, 2, None, ctypes.byref(out)) == _lib.WFD_ERR_INVALID
+    assert out.value is None  # cleared on failure
+    assert lib.wfd_batch_plan(items, 0, None, ctypes.byref(out)) == _lib.WFD_ERR_INVALID
+    assert lib.wfd_batch_plan(items, 2, None, ctypes.byref(out)) == _lib.WFD_ERR_INVALID  # no problem
+    assert "problem" in lib.wfd_last_error().decode()
+    assert lib.wfd_batch_run(None, None) == _lib.WFD_ERR_INVALID
+    assert lib.wfd_batch_launches(None) == 0
+    assert lib.wfd_batch_free(None) == 0
+

@@ -949,6 +949,11 @@ def main():
                 "traffic": None if tr is None else tr * w.nshot * interior,
                 "kernel": f"step2d_kernel ({dom} phase)", "peak_source": peak_src,
                 "alg_bytes_per_launch": bytes_per_launch, "ms_per_launch": per_launch_ms}
+    if phases.ms[1] > 0 and kept_segments(g) >= 2:
+        # the library recomputes each segment on a second stream beside the adjoint
+        # of the segment after it: both phases' launch times include the other's
+        # share of DRAM, and the phase times overlap in wall time
+        roofline["concurrent_with"] = "recompute" if dom == "adjoint" else "adjoint"
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -6,6 +6,9 @@
 
 #include <atomic>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -1028,6 +1031,37 @@ int run_forward_lp(const wfd_problem* p, const Geom& g, const Layout& L, const W
     return WFD_OK;
 }
 
+// A second stream and a pool of events per (device, primary stream), for the
+// recompute that overlaps the adjoint (run_backward_ustore). They are created
+// only outside a stream capture (a capture uses the ones an earlier eager call
+// made); without them the backward runs on the primary stream alone.
+struct AuxStream {
+    cudaStream_t r = nullptr;
+    std::vector<cudaEvent_t> ev;
+};
+std::mutex g_aux_mu;
+std::map<std::pair<int, cudaStream_t>, AuxStream> g_aux;
+
+const AuxStream* aux_stream(cudaStream_t s, size_t nev) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lock(g_aux_mu);
+    AuxStream& a = g_aux[{dev, s}];
+    if (a.r && a.ev.size() >= nev) return &a;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return nullptr;
+    if (!a.r && cudaStreamCreateWithFlags(&a.r, cudaStreamNonBlocking) != cudaSuccess) {
+        a.r = nullptr;
+        return nullptr;
+    }
+    while (a.ev.size() < nev) {
+        cudaEvent_t e;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        a.ev.push_back(e);
+    }
+    return &a;
+}
+
 // Adjoint with the u store (2D, one step per launch). The forward left the
 // levels of segments >= jstore in the slots (u_k in slot k - k0_store + 1).
 // Every earlier segment j restores (u_{k0-1}, u_k0) into slots 0 and 1 and
@@ -1035,6 +1069,15 @@ int run_forward_lp(const wfd_problem* p, const Geom& g, const Layout& L, const W
 // new slot: nothing else is stored). The adjoint step k stages u_k from its
 // slot next to q_{k+1} and forms L u_k itself (MODE_GRAD_U) on 16-row tiles;
 // the recompute runs on the forward's tiles.
+//
+// With two or more recomputed segments and room for two sets of K + 2 slots
+// in the region the kept levels leave free, the recompute of segment j - 1
+// runs on a second stream while the adjoint of segment j runs: recomputed
+// segments alternate between slot sets [K + 2, 2K + 4) and [0, K + 2), the
+// recompute of segment j waits for the adjoint of segment j + 2 (the last
+// reader of its set: a kept segment or the recomputed one before), and the
+// adjoint of segment j for its recompute. The recompute is latency-bound and
+// the adjoint DRAM-bound, so together they fill the memory system better.
 int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, const Work& w,
                         const Stepper& st, const float* wavelet, const float* dtraces,
                         float* grad_vel, float* grad_wavelet, const float* vel, bool zero_G,
@@ -1114,55 +1157,87 @@ int run_backward_ustore(const wfd_problem* p, const Geom& g, const Layout& L, co
         PhaseScope scope(PH_ADJOINT, s, 1);
         if ((rc = adjoint_step(p->nt, -1))) return rc;  // q_nt: its gradient term is 0
     }
+    // the recompute on a second stream (see above), or on s
+    const AuxStream* aux = (g.jstore >= 2 && L.nlap >= 2 * (g.K + 2)) ? aux_stream(s, 2 * (size_t)g.nseg + 1)
+                                                                       : nullptr;
+    const cudaStream_t r = aux ? aux->r : s;
+    Stepper sr = st;
+    sr.s = r;
+    auto ev_adj = [&](int j) { return aux->ev[1 + j]; };
+    auto ev_rec = [&](int j) { return aux->ev[1 + g.nseg + j]; };
+    auto set_base = [&](int j) { return aux && ((g.jstore - 1 - j) % 2 == 0) ? g.K + 2 : 0; };
+    if (aux) {  // (the second stream joins here: everything it reads is ready)
+        WFD_CUDA(cudaEventRecord(aux->ev[0], s));
+        WFD_CUDA(cudaStreamWaitEvent(r, aux->ev[0], 0));
+    }
+    // u_k0 .. u_{k1-1} of recomputed segment j into slots sb .. sb + k1 - k0 on stream r
+    auto recompute = [&](int j) -> int {
+        const int k0 = j * g.K, k1 = std::min(p->nt, k0 + g.K), sb = set_base(j);
+        if (aux && j + 2 < g.nseg) WFD_CUDA(cudaStreamWaitEvent(r, ev_adj(j + 2), 0));
+        PhaseScope scope(PH_RECOMPUTE, r, g.sb == 2 ? (k1 - k0) / 2 : k1 - k0 - 1);
+        const unsigned char* ck = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
+        WFD_CUDA(launch_unpack(ck + L.ckpt_field_bytes, w.slot(L, sb + 1), n_all, p->ckpt_format, r));
+        if (summed)  // (d_k0, u_k0): u_{k0-1} = u_k0 - d_k0 for the leapfrog recompute
+            WFD_CUDA(launch_unpack_diff(ck, w.slot(L, sb + 1), w.slot(L, sb), n_all, p->ckpt_format, r));
+        else
+            WFD_CUDA(launch_unpack(ck, w.slot(L, sb), n_all, p->ckpt_format, r));
+        for (int k = k0; k + 1 < k1;) {  // u_{k+1} (and u_{k+2}) up to u_{k1-1}
+            const int i = sb + k - k0 + 1;  // slot of u_k
+            const bool two = g.sb == 2 && k + 2 < k1;
+            if (g.sb == 2) {
+                Step2Args q{};
+                q.a = sr.base(w.slot(L, i + (two ? 2 : 1)));
+                q.u_mid = w.slot(L, i + 1);
+                q.two_steps = two;
+                q.inj_t1 = -1;
+                q.a.inj_t = -1;
+                q.smp_t1 = -1;
+                q.a.smp_t = -1;
+                if (p->nsrc > 0) {
+                    q.inj_e = w.src_e;
+                    q.inj_t1 = k;
+                    q.a.inj = w.src;
+                    q.a.inj_val = wavelet;
+                    q.a.inj_np = p->nsrc; q.a.inj_nt = p->nt; q.a.inj_t = two ? k + 1 : -1;
+                    q.a.inj_scale = p->src_scale;
+                }
+                if ((rc = sr.launch_k2(uc[i], uo[i - 1], q))) return rc;
+            } else {
+                StepArgs a = sr.base(w.slot(L, i + 1));
+                if (p->nsrc > 0) {
+                    a.inj = w.src;
+                    a.inj_val = wavelet;
+                    a.inj_np = p->nsrc; a.inj_nt = p->nt; a.inj_t = k;
+                    a.inj_scale = p->src_scale;
+                }
+                if ((rc = sr.launch(MODE_PLAIN, uc[i], uo[i - 1], uc[i], a))) return rc;
+            }
+            k += two ? 2 : 1;
+        }
+        if (aux) WFD_CUDA(cudaEventRecord(ev_rec(j), r));
+        return WFD_OK;
+    };
     for (int j = g.nseg - 1; j >= 0; --j) {
         const int k0 = j * g.K, k1 = std::min(p->nt, k0 + g.K);
-        const int base = j >= g.jstore ? g.k0_store : k0;  // u_k is in slot k - base + 1
         if (j < g.jstore) {
-            PhaseScope scope(PH_RECOMPUTE, s, g.sb == 2 ? (k1 - k0) / 2 : k1 - k0 - 1);
-            const unsigned char* ck = w.ckpt + (size_t)j * 2 * L.ckpt_field_bytes;
-            WFD_CUDA(launch_unpack(ck + L.ckpt_field_bytes, w.slot(L, 1), n_all, p->ckpt_format, s));
-            if (summed)  // (d_k0, u_k0): u_{k0-1} = u_k0 - d_k0 for the leapfrog recompute
-                WFD_CUDA(launch_unpack_diff(ck, w.slot(L, 1), w.slot(L, 0), n_all, p->ckpt_format, s));
-            else
-                WFD_CUDA(launch_unpack(ck, w.slot(L, 0), n_all, p->ckpt_format, s));
-            for (int k = k0; k + 1 < k1;) {  // u_{k+1} (and u_{k+2}) up to u_{k1-1}
-                const int i = k - k0 + 1;     // slot of u_k
-                const bool two = g.sb == 2 && k + 2 < k1;
-                if (g.sb == 2) {
-                    Step2Args q{};
-                    q.a = st.base(w.slot(L, i + (two ? 2 : 1)));
-                    q.u_mid = w.slot(L, i + 1);
-                    q.two_steps = two;
-                    q.inj_t1 = -1;
-                    q.a.inj_t = -1;
-                    q.smp_t1 = -1;
-                    q.a.smp_t = -1;
-                    if (p->nsrc > 0) {
-                        q.inj_e = w.src_e;
-                        q.inj_t1 = k;
-                        q.a.inj = w.src;
-                        q.a.inj_val = wavelet;
-                        q.a.inj_np = p->nsrc; q.a.inj_nt = p->nt; q.a.inj_t = two ? k + 1 : -1;
-                        q.a.inj_scale = p->src_scale;
-                    }
-                    if ((rc = st.launch_k2(uc[i], uo[i - 1], q))) return rc;
-                } else {
-                    StepArgs a = st.base(w.slot(L, i + 1));
-                    if (p->nsrc > 0) {
-                        a.inj = w.src;
-                        a.inj_val = wavelet;
-                        a.inj_np = p->nsrc; a.inj_nt = p->nt; a.inj_t = k;
-                        a.inj_scale = p->src_scale;
-                    }
-                    if ((rc = st.launch(MODE_PLAIN, uc[i], uo[i - 1], uc[i], a))) return rc;
-                }
-                k += two ? 2 : 1;
+            if (!aux) {
+                if ((rc = recompute(j))) return rc;
+            } else {  // (issued with the segment after it, on r)
+                WFD_CUDA(cudaStreamWaitEvent(s, ev_rec(j), 0));
             }
         }
-        PhaseScope scope(PH_ADJOINT, s, k1 - std::max(k0, 1));
-        const bool lvl = g.lvl16 && j >= g.jstore;  // (block-floating-point level k - k0_store)
-        for (int k = k1 - 1; k >= std::max(k0, 1); --k)
-            if ((rc = lvl ? adjoint_step(k, k - g.k0_store, true) : adjoint_step(k, k - base + 1))) return rc;
+        // the next segment's recompute, on r beside this adjoint
+        if (aux && j - 1 >= 0 && j - 1 < g.jstore && (rc = recompute(j - 1))) return rc;
+        {
+            PhaseScope scope(PH_ADJOINT, s, k1 - std::max(k0, 1));
+            // u_k: kept levels from slot k - k0_store + 1 (or block-floating-point
+            // level k - k0_store), recomputed ones from slot set_base(j) + k - k0 + 1
+            const bool lvl = g.lvl16 && j >= g.jstore;
+            const int first = j >= g.jstore ? 1 - g.k0_store : set_base(j) + 1 - k0;
+            for (int k = k1 - 1; k >= std::max(k0, 1); --k)
+                if ((rc = lvl ? adjoint_step(k, k - g.k0_store, true) : adjoint_step(k, k + first))) return rc;
+        }
+        if (aux) WFD_CUDA(cudaEventRecord(ev_adj(j), s));
     }
     if (grad_wavelet && p->nsrc > 0)  // q_1 at the sources -> d J / d w_0
         WFD_CUDA(launch_gather(w.Q[1], ga.cells, w.src_a, ga.ntiles, p->nshot, p->nsrc, w.m,

@@ -105,10 +105,14 @@ def test_u_store_matches_lap_store(cuda, orc, order, shape, nt, ckpt, rows, grou
 
 
 @pytest.mark.parametrize("update,tol", [("leapfrog", 1e-6), ("auto", 2e-6)])
-@pytest.mark.parametrize("nt,ckpt,levels", [(100, 13, 30), (100, 13, 10 ** 6), (61, 20, 45)])
+@pytest.mark.parametrize("nt,ckpt,levels", [(100, 13, 30), (100, 13, 10 ** 6), (61, 20, 45), (100, 10, 60),
+                                             (101, 9, 50)])
 def test_kept_levels_match_recompute(cuda, orc, nt, ckpt, levels, update, tol):
     """store_levels: the forward keeps the levels of its last segments and the
-    adjoint recomputes only the others. With FP32 checkpoints and the leapfrog
+    adjoint recomputes only the others. With (100, 10, 60) and (101, 9, 50)
+    the kept levels leave room for two sets of recompute slots, so the
+    recompute of each segment runs on a second stream beside the adjoint of
+    the segment after it, alternating between the sets. With FP32 checkpoints and the leapfrog
     forward the recompute reproduces the kept levels exactly, so the gradients
     agree to summation order (1e-6). With the summed forward (the default) the
     recompute restarts the leapfrog recursion from u_{k0-1} = u_k0 - d_k0, one

@@ -1034,11 +1034,13 @@ int run_forward_lp(const wfd_problem* p, const Geom& g, const Layout& L, const W
 // A second stream and a pool of events per (device, primary stream), for the
 // recompute that overlaps the adjoint (run_backward_ustore). They are created
 // only outside a stream capture (a capture uses the ones an earlier eager call
-// made); without them the backward runs on the primary stream alone.
+// made), for at most AUX_MAX primary streams per process (they live as long as
+// it does); without them the backward runs on the primary stream alone.
 struct AuxStream {
     cudaStream_t r = nullptr;
     std::vector<cudaEvent_t> ev;
 };
+constexpr size_t AUX_MAX = 64;
 std::mutex g_aux_mu;
 std::map<std::pair<int, cudaStream_t>, AuxStream> g_aux;
 
@@ -1046,7 +1048,9 @@ const AuxStream* aux_stream(cudaStream_t s, size_t nev) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
     std::lock_guard<std::mutex> lock(g_aux_mu);
-    AuxStream& a = g_aux[{dev, s}];
+    const std::pair<int, cudaStream_t> key{dev, s};
+    if (g_aux.find(key) == g_aux.end() && g_aux.size() >= AUX_MAX) return nullptr;
+    AuxStream& a = g_aux[key];
     if (a.r && a.ev.size() >= nev) return &a;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return nullptr;

@@ -4,8 +4,8 @@
  * no C++ and no PyTorch on the caller's side.
  *
  *   check_abi layout  prints sizeof(wfd_problem) and every field's offset, one
- *                     "name offset" line each, for comparison with the ctypes
- *                     mirror of the struct;
+ *                     "name offset" line each (wfd_batch_item's as "item.name"),
+ *                     for comparison with the ctypes mirrors of the structs;
  *   check_abi host    host-only calls: version, status texts, workspace sizes
  *                     and the argument checks (no CUDA call; runs without a GPU);
  *   check_abi gpu     compute calls on device 0 through the CUDA runtime:
@@ -57,6 +57,12 @@ static int layout(void) {
     FIELD(store_levels); FIELD(field_format); FIELD(adjoint_mode); FIELD(recon_band);
     FIELD(dt); FIELD(dz); FIELD(dy); FIELD(dx); FIELD(src_scale); FIELD(vmax); FIELD(update_form);
     FIELD(level_format);
+    printf("item.sizeof %zu\n", sizeof(wfd_batch_item));
+#define ITEM(name) printf("item." #name " %zu\n", offsetof(wfd_batch_item, name))
+    ITEM(problem); ITEM(vel); ITEM(sponge_z); ITEM(sponge_y); ITEM(sponge_x); ITEM(wavelet); ITEM(src);
+    ITEM(rec); ITEM(observed); ITEM(traces); ITEM(grad_vel); ITEM(grad_wavelet); ITEM(misfit);
+    ITEM(workspace); ITEM(workspace_bytes);
+#undef ITEM
     return 0;
 }
 

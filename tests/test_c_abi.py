@@ -1,13 +1,14 @@
 """The C boundary from a plain C caller: tests/c_abi/check_abi.c is compiled
 by gcc against include/wavefd.h and linked to the in-tree libwavefd.so, as a
 cgo / JNI / N-API binding of the reference would link it.
-  * layout: the C compiler's sizeof and field offsets of wfd_problem equal
-    those of the ctypes mirror the Python side passes;
+  * layout: the C compiler's sizeof and field offsets of wfd_problem and
+    wfd_batch_item equal those of the ctypes mirrors the Python side passes;
   * host: version, status texts, workspace sizes and argument checks, with no
     CUDA call (runs here);
   * gpu: the compute entry points on device 0 (the order-2 drop-ins against
     the update evaluated in double, the three forwards against each other,
-    the misfit gradient's invariants, a device-side position error).
+    the misfit gradient's invariants, a two-item batch plan against the
+    single call, a device-side position error).
 """
 import ctypes
 import glob
@@ -59,8 +60,11 @@ def test_struct_layout_matches_ctypes(check_abi):
     r = _run(check_abi, "layout")
     assert r.returncode == 0, r.stderr
     got = dict((k, int(v)) for k, v in (line.split() for line in r.stdout.splitlines()))
+    item = {k[5:]: got.pop(k) for k in list(got) if k.startswith("item.")}
     assert got.pop("sizeof") == ctypes.sizeof(_lib.Problem)
     assert got == {name: getattr(_lib.Problem, name).offset for name, _ in _lib.Problem._fields_}
+    assert item.pop("sizeof") == ctypes.sizeof(_lib.BatchItem)
+    assert item == {name: getattr(_lib.BatchItem, name).offset for name, _ in _lib.BatchItem._fields_}
 
 
 def test_host_calls_from_c(check_abi):

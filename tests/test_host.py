@@ -169,3 +169,48 @@ def test_bench_reference_arm_contract():
     e2e = r["e2e"]
     assert e2e["value"] == r["value"] and e2e["unit"] == r["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def _bfp16_decode(q16, t):
+    """The kept-level format of WFD_LEVEL_BFP16 as include/wavefd.h states it:
+    per 4 cells along x one exponent byte t and four stored 16-bit values
+    u = q + 32768, v = q 2^(t - 141) (t = 0: the block is 0)."""
+    q = q16.astype(np.int64) - 32768
+    return np.where(t[..., None] > 0, np.ldexp(q.astype(np.float64), t[..., None].astype(np.int64) - 141), 0.0)
+
+
+def _bfp16_encode(v):
+    """An encoder of that format, from the statement alone: t the FP32 exponent
+    field of the block's largest magnitude M (0 when it is below 15),
+    q = rint(v 2^(141 - t)) (ties to even) clamped to +-32767."""
+    v = v.astype(np.float32).reshape(-1, 4)
+    M = np.abs(v).max(axis=1)
+    t = ((M.view(np.uint32) >> 23) & 0xFF).astype(np.int64)
+    t = np.where(t >= 15, t, 0)
+    q = np.rint(np.ldexp(v.astype(np.float64), (141 - t)[:, None])).clip(-32767, 32767)
+    q = np.where(t[:, None] > 0, q, 0)
+    return (q + 32768).astype(np.uint16), t.astype(np.uint8)
+
+
+def test_block_float_level_format():
+    """The documented kept-level format: 2.25 bytes per cell, decoding exact in
+    FP32 (every decoded value is an FP32 number), each value within one step
+    2^(t - 141) of the original (half a step unless clamped at the block's
+    top), and blocks below 2^-112 stored as 0."""
+    rng = np.random.default_rng(5)
+    v = (rng.standard_normal((4096, 4)) * np.exp(rng.uniform(-40, 40, (4096, 1)))).astype(np.float32)
+    v[::9] *= np.float32(1e-35)  # blocks below the format's range
+    q16, t = _bfp16_encode(v)
+    assert q16.dtype.itemsize * 4 + t.dtype.itemsize == 9  # 2.25 bytes per cell
+    d = _bfp16_decode(q16.reshape(-1, 4), t)
+    assert np.array_equal(d, d.astype(np.float32).astype(np.float64))
+    live = t > 0
+    step = np.ldexp(1.0, t[live].astype(np.int64) - 141)[:, None]
+    err = np.abs(d[live] - v[live].astype(np.float64))
+    assert np.all(err <= step)
+    top = np.abs(v[live]).astype(np.float64) >= 32767.5 * step  # the clamped values
+    assert np.all((err <= 0.5 * step) | top)
+    M = np.abs(v).max(axis=1)
+    assert np.all((M[~live] < 2.0 ** -112)) and np.all(d[~live] == 0)
+    # relative to the block's largest value M: within 2^-15 M (M >= 2^(t - 127))
+    assert np.all(err <= 2.0 ** -15 * np.abs(v[live]).astype(np.float64).max(axis=1, keepdims=True))
